@@ -1,0 +1,45 @@
+#!/bin/sh
+# Builds the reference's own quasi-static shear step from its sources, read in
+# place under the reference tree, into oracle/_ref/libstzref.so (test-only).
+#
+#   oracle/build_ref.sh [REFERENCE_ROOT]     (default: /root/reference)
+#
+# Recipe (the reference's own make files are not used):
+#   1. esim/tgmg/tgmg_compile.pl expands tgmg.in.cc into tgmg.cc.  The script
+#      reads ./tgmg.in.cc and writes ./tgmg.cc, so it runs in a scratch
+#      directory under oracle/_ref/ holding a symlink to tgmg.in.cc; the
+#      scratch directory is deleted after compiling.
+#   2. g++ compiles esim/sb/main/{shear_sim,qs_multi,common}.cc and
+#      esim/shared/mat.cc with the reference's flags (esim/config/
+#      config.mk.linux:4: -Wall -ansi -pedantic -fopenmp -O3) plus -fPIC,
+#      together with oracle/ref_driver.cc, into one shared library.
+# Only x86/Arm-neutral flags are used; nothing here runs on the GPU.
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+ESIM="$REF/esim"
+if [ ! -f "$ESIM/tgmg/tgmg.in.cc" ]; then
+    echo "build_ref: reference sources not found under $REF" >&2
+    exit 2
+fi
+mkdir -p "$OUT"
+GEN="$OUT/gen"
+rm -rf "$GEN"
+mkdir -p "$GEN"
+ln -s "$ESIM/tgmg/tgmg.in.cc" "$GEN/tgmg.in.cc"
+(cd "$GEN" && perl "$ESIM/tgmg/tgmg_compile.pl")
+CXX=${CXX:-g++}
+FLAGS="-Wall -ansi -pedantic -fopenmp -O3 -fPIC -Wno-unused-variable -Wno-unused-but-set-variable"
+INC="-I$GEN -I$ESIM/tgmg -I$ESIM/shared -I$ESIM/sb/main"
+OBJ="$OUT/obj"
+mkdir -p "$OBJ"
+$CXX $FLAGS $INC -c "$ESIM/sb/main/shear_sim.cc" -o "$OBJ/shear_sim.o" &
+$CXX $FLAGS $INC -c "$ESIM/sb/main/qs_multi.cc" -o "$OBJ/qs_multi.o" &
+$CXX $FLAGS $INC -c "$ESIM/sb/main/common.cc" -o "$OBJ/common.o" &
+$CXX $FLAGS $INC -c "$ESIM/shared/mat.cc" -o "$OBJ/mat.o" &
+$CXX $FLAGS $INC -c "$HERE/ref_driver.cc" -o "$OBJ/ref_driver.o" &
+wait
+$CXX -shared -fopenmp -o "$OUT/libstzref.so" "$OBJ"/*.o
+rm -rf "$GEN" "$OBJ"
+echo "build_ref: wrote $OUT/libstzref.so"

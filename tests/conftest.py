@@ -1,0 +1,40 @@
+import glob
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+TESTS = os.path.dirname(os.path.abspath(__file__))
+if TESTS not in sys.path:
+    sys.path.insert(0, TESTS)
+
+GOLDEN = os.path.join(TESTS, "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a GB300 (runs the CUDA path)")
+
+
+def golden_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load_golden(name):
+    from stz_gb300.params import StzParams
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(d["meta"]))
+    P = StzParams()
+    for k, v in meta["params"].items():
+        setattr(P, k, v)
+    fields = {k: d[k] for k in d.files if k not in ("meta",)}
+    return P, meta, fields
+
+
+@pytest.fixture(params=golden_names())
+def golden(request):
+    return (request.param,) + load_golden(request.param)

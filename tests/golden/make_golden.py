@@ -1,0 +1,74 @@
+"""Regenerates the golden fixtures from the reference itself.
+
+Run in a checkout that has the SURGroup/STZ tree available (default
+/root/reference, override with STZ_REFERENCE_ROOT):
+
+    python tests/golden/make_golden.py
+
+It builds oracle/_ref/libstzref.so from the reference sources
+(oracle/build_ref.sh), runs the reference's own
+shear_sim::step_forward_quasistatic (esim/sb/main/shear_sim.cc:280) on seeded
+inputs, and stores inputs and outputs as compressed .npz files next to this
+script.  The chi inputs come from the oracle's seeded random-field generator;
+they are stored in the fixture, so the fixtures do not depend on it.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.bind import ReferenceSim, random_chi  # noqa: E402
+from stz_gb300.params import (STZ_LINEAR, STZ_NONLINEAR, STZ_NONLINEAR_ATHERMAL,  # noqa: E402
+                              plastic_shear, simple_shear)
+
+# name -> (params, chi (l, std, seed), dt, steps, tolerance multiplier)
+# The tight cases use multiplier 10 in place of the default 1e4
+# (qs_multi.cc:14): ~1e-12 solver error, inside a 1e-10 parity gate.
+# The thermal laws are stiff at t_scale=1 (the adaptive sub-stepping of
+# shear_sim.cc:523-542 then never ends), so their cases use small t_scale.
+CASES = {
+    "elastic16_default": (simple_shear(16), (4, 30, 1), 0.01, 50, 1e4),
+    "elastic32_tight": (simple_shear(32), (4, 30, 2), 0.01, 40, 10.0),
+    "plastic32": (plastic_shear(32), (4, 30, 3), 0.01, 100, 10.0),
+    "plastic24_oddlevels": (plastic_shear(24), (4, 30, 4), 0.01, 100, 10.0),
+    "plastic_rect40x24": (plastic_shear(40, 24, u_bdry=3.0), (3, 30, 5), 0.01, 100, 10.0),
+    "thermal_linear32": (plastic_shear(32, stz_model=STZ_LINEAR, u_bdry=3.0, t_scale=1e-18),
+                         (4, 30, 6), 0.01, 100, 10.0),
+    "thermal_nonlinear16": (plastic_shear(16, stz_model=STZ_NONLINEAR, u_bdry=3.0), (2, 30, 7), 0.01, 100, 10.0),
+    "athermal_nonlinear16": (plastic_shear(16, stz_model=STZ_NONLINEAR_ATHERMAL), (2, 30, 8), 0.01, 100, 10.0),
+    "truncation1_16": (plastic_shear(16, t_model=1), (2, 30, 9), 0.01, 100, 10.0),
+    "chi_diffusion32": (plastic_shear(32, chi_diff=2e-3, chi_len=0.05), (4, 30, 10), 0.01, 100, 10.0),
+    "viscous20": (plastic_shear(20, viscosity=0.02), (2, 30, 11), 0.01, 80, 10.0),
+}
+
+
+def make(name, spec):
+    P, (l, std, seed), dt, steps, mult = spec
+    chi = random_chi(P.m, P.n, l, 600.0, std, P.TZ, seed)
+    sim = ReferenceSim(P, chi)
+    sim.set_acc_mult(mult)
+    cycles = sim.steps(dt, steps)
+    f = sim.fields()
+    out = {k: v for k, v in f.items()}
+    out["chi0"] = chi
+    out["vel"] = sim.vel()
+    meta = {"params": P.as_dict(), "dt": dt, "steps": steps, "acc_mult": mult,
+            "cycles": int(cycles), "time": sim.time,
+            "source": "reference shear_sim::step_forward_quasistatic, built from source"}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **out)
+    return cycles
+
+
+def main():
+    for name, spec in CASES.items():
+        c = make(name, spec)
+        print(f"{name}: {c} V-cycles")
+
+
+if __name__ == "__main__":
+    main()
