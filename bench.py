@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""Throughput of the quasi-static STZ time step on one or more GB300s.
+
+Workload (the headline configuration): simple shear on a 2048x2048 grid,
+periodic in x, walls at +-1e-4, mu=1, K=2.5, athermal linear STZ law,
+seeded Gaussian chi (mean 600 K, std 40 K, correlation length 16 cells),
+dt=1e-2, multigrid to a relative residual of 1e-10, mixed precision (FP32
+V-cycles inside FP64 iterative refinement).  A step is one quasi-static time
+step (advection + STZ plasticity + projection).  The ~0.6 GB FP64 state is
+larger than the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  With N>1 (launched under torch.distributed.run) every
+rank runs an independent replica (the step does not shard; weak scaling) and
+value is the sum over ranks, timed by the slowest rank.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s"
+GRID = 2048
+DT = 1e-2
+RTOL = 1e-10
+CHI = dict(l=16.0, tem_avg=600.0, tem_std=40.0)
+
+# Algorithmic bytes (FP64 state, FP32 multigrid vectors), per cell or node:
+ADVECT_BYTES_PER_CELL = 128      # read u,v,p,q,s,tau,chi,X,Y; write p,q,s,tau,chi,X,Y (8 B each)
+VCYCLE32_BYTES_PER_NODE = 69.3   # 17.3 words of 4 B: 13 W on the top level x (1 + 1/4 + 1/16 + ...)
+VCYCLE64_BYTES_PER_NODE = 138.7
+SWEEP32_BYTES_PER_NODE = 24      # one Gauss-Seidel sweep: read z, b; write z (float2)
+RESID64_BYTES_PER_NODE = 40      # read z, b (double2); write r (float2)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=GRID)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-extrapolate", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=0, help="FP64 comparison steps (0: = steps+warmup, capped)")
+    ap.add_argument("--skip-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, ws, rank, local, backend="nccl"):
+        self.ws, self.rank, self.local = ws, rank, local
+        self.pg = None
+        if ws > 1:
+            import torch
+            import torch.distributed as td
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            td.init_process_group(backend=backend)
+            self.td, self.torch = td, torch
+            self.pg = True
+
+    def barrier(self):
+        if self.pg:
+            if self.td.get_backend() == "nccl":
+                self.td.barrier(device_ids=[self.local])
+            else:
+                self.td.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        dev = f"cuda:{self.local}" if self.td.get_backend() == "nccl" else "cpu"
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.gpu)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_params(N):
+    from stz_gb300.params import simple_shear
+    return simple_shear(N)
+
+
+def cpu_baseline(P, chi, steps, warm=1):
+    """The oracle restatement of the reference step on the host cores,
+    relative residual 1e-10 like the GPU path."""
+    from oracle.bind import OracleSim, oracle_threads
+    t0 = time.time()
+    o = OracleSim(P, chi)
+    o.set_tolerance(1, RTOL)
+    o.steps(DT, warm)
+    o.seconds = 0.0
+    o.steps(DT, steps)
+    sec = o.seconds
+    n = P.m * P.n
+    return {"value": n * steps / sec, "unit": METRIC, "cores": oracle_threads(), "kind": "port",
+            "sample": f"{P.m}x{P.n}, {steps} timed steps after {warm} warm-up step(s), oracle restatement "
+                      f"(C, OpenMP) at relative residual {RTOL:g}; set-up {time.time() - t0 - sec:.1f} s untimed",
+            "ms_per_step": 1e3 * sec / steps}
+
+
+def run_reference(args, dist):
+    """Reference arm: the reference's CPU implementation of the step on the
+    host cores.  The reference's own build is x86-only here, so the C
+    restatement of it (oracle/stz_oracle.c) is timed."""
+    if dist.rank != 0:
+        return None
+    from stz_gb300.shear_sim import random_chi
+    from oracle.bind import OracleSim, oracle_threads
+    N = args.size
+    P = make_params(N)
+    chi = random_chi(N, N, CHI["l"], CHI["tem_avg"], CHI["tem_std"], P.TZ, 2)
+    o = OracleSim(P, chi)
+    o.set_tolerance(1, RTOL)
+    o.steps(DT, args.warmup)
+    o.seconds = 0.0
+    t0 = time.time()
+    o.steps(DT, args.steps)
+    wall = time.time() - t0
+    sec = o.seconds
+    value = N * N * args.steps / sec
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian chi)",
+            "impl": "reference",
+            "config": {"workload": f"quasi-static STZ simple shear {N}x{N}, FP64, relative residual {RTOL:g}",
+                       "grid": N, "dt": DT, "chi": CHI},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": oracle_threads(), "kind": "port",
+                             "sample": f"{args.steps} steps of {N}x{N} after {args.warmup} warm-up steps; "
+                                       f"wall {wall:.1f} s"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+def run_ours(args, dist):
+    from stz_gb300 import _lib
+    from stz_gb300.shear_sim import ShearSim, random_chi
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    N = args.size
+    P = make_params(N)
+    chi = random_chi(N, N, CHI["l"], CHI["tem_avg"], CHI["tem_std"], P.TZ, 2 + dist.rank)
+    prec = _lib.MIXED if args.precision == "mixed" else _lib.FP64
+    extrap = not args.no_extrapolate
+    sim = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, device=dist.local,
+                   extrapolate=extrap)
+    sim.steps(DT, args.warmup)
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    dist.barrier()
+    t0 = time.time()
+    sim.steps(DT, args.steps)
+    wall = time.time() - t0
+    st = sim.stats
+    dev_s = dist.max(st.seconds)
+    dist.barrier()
+    clk = clocks.stop()
+    per_rank = N * N * args.steps / dev_s
+    value = per_rank * dist.ws
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32" if prec == _lib.MIXED else "f64",
+            "data": "synthetic (seeded Gaussian chi, mean 600 K, std 40 K, l=16 cells)",
+            "config": {"workload": f"quasi-static STZ simple shear {N}x{N}, "
+                                   f"{'FP32 V-cycles in FP64 iterative refinement' if prec else 'FP64'} multigrid, "
+                                   f"relative residual {RTOL:g}",
+                       "grid": N, "dt": DT, "precision": args.precision, "extrapolated_guess": extrap,
+                       "l2": "state (~0.6 GB FP64) larger than L2; no flush", "replicas": dist.ws},
+            "clocks": clk, "gpu_launches": int(st.kernel_launches),
+            "vcycles_per_step": st.vcycles / args.steps, "refinements_per_step": st.refinements / args.steps,
+            "wall_ms_per_step": 1e3 * wall / args.steps}
+    if dist.rank != 0:
+        return None
+
+    # FP64 GPU path and the mixed-vs-FP64 error from the same initial state
+    if prec == _lib.MIXED:
+        nsteps = args.fp64_steps or min(args.warmup + args.steps, 60)
+        a = ShearSim(P, chi, precision=_lib.FP64, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, extrapolate=extrap)
+        b = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, extrapolate=extrap)
+        a.steps(DT, nsteps)
+        b.steps(DT, nsteps)
+        from parity import group_errors
+        err = group_errors(a.fields(), b.fields(), N)
+        a2 = ShearSim(P, chi, precision=_lib.FP64, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, extrapolate=extrap)
+        a2.steps(DT, args.warmup)
+        a2.steps(DT, max(5, min(args.steps, 20)))
+        k64 = max(5, min(args.steps, 20))
+        fp64_value = N * N * k64 / a2.stats.seconds
+        line["fp64"] = {"value": fp64_value, "ms_per_step": 1e3 * a2.stats.seconds / k64,
+                        "vcycles_per_step": a2.stats.vcycles / k64, "steps": k64}
+        line["speedup_mixed_vs_fp64"] = value / dist.ws / fp64_value
+        line["rel_err_mixed_vs_fp64"] = {"steps": nsteps, **{k: float(v) for k, v in err.items()}}
+        for h in (a, b, a2):
+            h.close()
+
+    # roofline of the dominant kernels, timed in isolation on the library's stream
+    peak, peak_kind = measured_peaks()
+    nn = N * (N + 1)
+    t_adv = sim.time_kernel(DT, 0, 10)
+    rows = {"advect": (t_adv, ADVECT_BYTES_PER_CELL * N * N, 1.0)}
+    if prec == _lib.MIXED:
+        t_v32 = sim.time_kernel(DT, 4, 10)
+        t_r64 = sim.time_kernel(DT, 5, 10)
+        vc = st.vcycles / args.steps
+        rows["vcycle_fp32"] = (t_v32, VCYCLE32_BYTES_PER_NODE * nn, vc)
+        rows["residual_fp64"] = (t_r64, RESID64_BYTES_PER_NODE * nn, st.refinements / args.steps + 1)
+    else:
+        t_v64 = sim.time_kernel(DT, 3, 10)
+        rows["vcycle_fp64"] = (t_v64, VCYCLE64_BYTES_PER_NODE * nn, st.vcycles / args.steps)
+    shares = {k: t * c for k, (t, b, c) in rows.items()}
+    dom = max(shares, key=shares.get)
+    t, b, c = rows[dom]
+    achieved = b / (t * 1e-3) / 1e9
+    line["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                        "ms_per_launch": t, "algorithmic_bytes": b,
+                        "share_of_step": shares[dom] / (1e3 * dev_s / args.steps)}
+    line["kernels"] = {k: {"ms": t, "per_step": c, "GBs": b / (t * 1e-3) / 1e9} for k, (t, b, c) in rows.items()}
+    line["mg_hbm_gbs"] = line["kernels"].get("vcycle_fp32", line["kernels"].get("vcycle_fp64"))["GBs"]
+
+    # end to end through the C ABI with host buffers: upload the state,
+    # step, download the state, every step
+    import torch
+    cells, nodes = N * (N + 2), N * (N + 1)
+    up = [torch.empty(cells, dtype=torch.float64, pin_memory=True) for _ in range(5)]
+    up += [torch.empty(nodes, dtype=torch.float64, pin_memory=True) for _ in range(2)]
+    up += [torch.empty(2 * nodes, dtype=torch.float64, pin_memory=True)]
+    down = up + [torch.empty(N * N, dtype=torch.float64, pin_memory=True)]
+    sim.download([t.data_ptr() for t in down])
+    k_e2e = max(3, min(args.steps, 20))
+    t0 = time.time()
+    for _ in range(k_e2e):
+        sim.upload([t.data_ptr() for t in up])
+        sim.steps(DT, 1)
+        sim.download([t.data_ptr() for t in down])
+    e2e_s = time.time() - t0
+    h2d = sum(t.numel() * 8 for t in up)
+    d2h = sum(t.numel() * 8 for t in down)
+    line["e2e"] = {"value": N * N * k_e2e / e2e_s * dist.ws, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h, "steps": k_e2e,
+                   "api": "stzg_upload + stzg_step_qs + stzg_download (pinned host buffers)"}
+    sim.close()
+
+    if not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(P, chi, args.cpu_steps)
+    return line
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        line = run_reference(args, Dist(1, 0, 0))
+        print(json.dumps(line), flush=True)
+        return 0
+    dist = Dist(ws, rank, local)
+    line = run_ours(args, dist)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,171 @@
+/* stzg.h - C ABI of the GB300-native quasi-static STZ time step.
+ *
+ * One handle (stzg_sim) owns one simulation on one GPU: its fields in HBM,
+ * its multigrid hierarchy, its CUDA stream and captured graphs.  Host arrays
+ * passed in are copied; the caller keeps ownership.  Every entry point returns
+ * an int status (STZG_OK on success) and never exits the process.
+ *
+ * Each entry point names the reference interface it stands in for
+ * (paths inside the SURGroup/STZ tree).
+ */
+#ifndef STZG_H
+#define STZG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------
+ * The reference exits the process on a failed solve (qs_multi.hh:51-53,
+ * tgmg.in.cc:285-287) and on file errors (common.cc:12-29). */
+enum {
+    STZG_OK = 0,
+    STZG_EINVAL = 1,        /* bad argument or unsupported configuration */
+    STZG_ENOMEM = 2,        /* device allocation failed */
+    STZG_ECUDA = 3,         /* CUDA runtime error */
+    STZG_ENOTCONV = 4,      /* multigrid did not reach the tolerance (tgmg.in.cc:285) */
+    STZG_ENAN = 5,          /* NaN residual (tgmg.in.cc:300) */
+    STZG_ESUBSTEP = 6,      /* plastic sub-stepping hit its iteration cap */
+    STZG_ENODEV = 7         /* no usable sm_103 device */
+};
+
+/* ---- parameters ---------------------------------------------------------
+ * shear_sim constructor arguments (shear_sim.hh:95-99) and the STZ law
+ * (stz_model.hh:9-207).  s_y is the yield stress, hard-wired to 1 in the
+ * reference (stz_model.hh:26, :111). */
+typedef struct {
+    int m, n;          /* cells in x (periodic) and y (walls at ay, by) */
+    int stz_model;     /* 0 linear, 1 nonlinear, 2 linear athermal, 3 nonlinear athermal */
+    int t_model;       /* truncation model of the linear athermal law (-1..4) */
+    double ax, bx, ay, by;
+    double mu, K, viscosity, chi_diff, chi_len, t_scale, adapt_fac, u_bdry;
+    double TZ, c0, tau0, kappa, Delta, Omegaeps0, chi_inf, theta, rho, s_y;
+} stz_params;
+
+enum { STZG_FP64 = 0, STZG_MIXED = 1 };
+enum { STZG_TOL_REFERENCE = 0, STZG_TOL_RELATIVE = 1 };
+
+typedef struct {
+    int precision;     /* STZG_FP64: FP64 V-cycles; STZG_MIXED: FP32 V-cycles inside
+                          FP64 iterative refinement */
+    int tol_mode;      /* STZG_TOL_REFERENCE: mean squared residual below
+                          (DBL_EPSILON*tol*2(tmufac1+tmufac2))^2, qs_multi.cc:14 with
+                          tol the multiplier (1e4 there);  STZG_TOL_RELATIVE:
+                          ||b-Az||_2 <= tol*||b||_2 */
+    double tol;
+    int track_plastic; /* accumulate eps_pl = sum ddev/(2 mu) per cell */
+    int device;        /* CUDA device ordinal */
+    int inner_cycles;  /* mixed precision: FP32 V-cycles per refinement pass (0: auto) */
+    int use_graphs;    /* capture the V-cycle in a CUDA graph (1 default) */
+    int extrapolate;   /* initial guess of each solve: 2 v(n) - v(n-1) instead of the
+                          previous solution v(n) (tgmg keeps z between solves) */
+    int substep_cap;   /* iteration cap of the plastic sub-stepping per cell and step
+                          (0: 4194304); reaching it returns STZG_ESUBSTEP */
+    int reserved[6];
+} stzg_options;
+
+typedef struct {
+    long vcycles;      /* V-cycles counted like tgmg_predict::add_iters (tgmg_predict.hh:24) */
+    long extra_vcycles;/* the extra cycle run after convergence (tgmg_config.hh:45) */
+    long solves;
+    long refinements;  /* FP64 outer passes (mixed precision) */
+    long checks;       /* residual evaluations */
+    double last_error; /* last convergence measure */
+    double seconds;    /* device time of the stepped region (CUDA events) */
+    long substeps_max; /* largest plastic sub-step count seen (reported when tracked) */
+    long kernel_launches; /* kernels this library launched (graph nodes included) */
+} stzg_stats;
+
+/* Field ids, shared with the oracle: node fields (m x (n+1), rows 0..n):
+ * 0 u, 1 v, 7 X, 8 Y.  Cell fields (m x (n+2), rows -1..n with the ghost
+ * rows): 2 p, 3 q, 4 s, 5 tau, 6 chi, 9 ddev.  10 eps_pl (m x n). */
+enum { STZG_U = 0, STZG_V = 1, STZG_P = 2, STZG_Q = 3, STZG_S = 4, STZG_TAU = 5,
+       STZG_CHI = 6, STZG_X = 7, STZG_Y = 8, STZG_DDEV = 9, STZG_EPS_PL = 10 };
+
+typedef struct stzg_sim stzg_sim;
+
+void stzg_default_options(stzg_options *opt);
+const char *stzg_strerror(int status);
+/* Last CUDA or validation message of this thread. */
+const char *stzg_last_message(void);
+
+/* Replaces: shear_sim::shear_sim (shear_sim.cc:26-44) together with
+ * qs_multi::qs_multi (qs_multi.cc:9-15) and tgmg::tgmg (tgmg.in.cc:11-30). */
+int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out);
+/* Replaces: shear_sim::~shear_sim (shear_sim.cc:47-52). */
+int stzg_destroy(stzg_sim *s);
+
+/* Initial state used by the reference drivers after initialize_random
+ * (shear_sim.cc:932-984): zero velocity and stress, identity reference map,
+ * chi per cell (m*n, row 0 at y=ay), ghost rows extrapolated as
+ * set_boundaries (shear_sim.cc:552-581); time reset to 0. */
+int stzg_set_state(stzg_sim *s, const double *chi);
+/* Field access: write/read the public c_field members (fields.hh:7-114)
+ * and shear_sim::time (shear_sim.hh:87).  Layouts as the field ids above. */
+int stzg_set_field(stzg_sim *s, int field, const double *host);
+int stzg_get_field(stzg_sim *s, int field, double *host);
+int stzg_set_time(stzg_sim *s, double time);
+int stzg_get_time(stzg_sim *s, double *time);
+
+/* Bulk state transfer for callers that keep the fields in host memory, as
+ * the reference does (shear_sim::fm, vel, shear_sim.hh:79-82).  up[8]:
+ * p, q, s, tau, chi (m*(n+2) with ghost rows), X, Y (m*(n+1)), vel
+ * (m*(n+1) x,y pairs, the solver array).  down[9]: the same plus eps_pl
+ * (m*n).  Entries may be NULL to skip a field.  Time and wall speed are
+ * kept.  Pinned host memory gives full copy bandwidth. */
+int stzg_upload(stzg_sim *s, const double *const *up);
+int stzg_download(stzg_sim *s, double *const *down);
+
+/* Replaces: shear_sim::step_forward_quasistatic (shear_sim.cc:280-291),
+ * called nsteps times; stats may be NULL. */
+int stzg_step_qs(stzg_sim *s, double dt, int nsteps, stzg_stats *stats);
+/* Replaces: shear_sim::advection_step + chi_diffusion (shear_sim.cc:296-386),
+ * one call, time not advanced. */
+int stzg_advection_step(stzg_sim *s, double dt);
+/* Replaces: shear_sim::projection_step (shear_sim.cc:391-438). */
+int stzg_projection_step(stzg_sim *s, double dt, stzg_stats *stats);
+/* Replaces: shear_sim::avg_iters (shear_sim.hh:116) / tgmg_predict::avg_iters
+ * (tgmg_predict.hh:28-32): mean V-cycles per solve since the last call. */
+int stzg_avg_iters(stzg_sim *s, double *avg);
+
+/* tgmg drop-in.  Replaces: tgmg<qs_multi,vec,mat>::solve_v_cycle(tgmg_predict&)
+ * (tgmg.hh:439-441, tgmg.in.cc:266-301) on this handle's operator for time
+ * step dt (qs_multi::init(visc/dt), qs_multi.cc:31-55).  src and vel are
+ * m*(n+1) (x,y) pairs; vel holds the initial guess and receives the solution. */
+int stzg_mg_solve(stzg_sim *s, double dt, const double *src, double *vel, int *ncycles);
+/* Replaces: tgmg::v_cycle (tgmg.in.cc:313-328), one cycle. */
+int stzg_mg_vcycle(stzg_sim *s, double dt, const double *src, double *vel);
+/* Replaces: tgmg_base::l2_error (tgmg.hh:146) = mds()/mn for src/vel. */
+int stzg_mg_l2_error(stzg_sim *s, double dt, const double *src, const double *vel, double *err);
+/* Replaces: the hierarchy of tgmg::tgmg (tgmg.in.cc:17-29): number of
+ * coarse levels; dims receives (m,n) per coarse level (up to 16). */
+int stzg_mg_levels(stzg_sim *s, double dt, int *nlevels, int *dims);
+/* Replaces: the stored coarse stencils tgmg_level::s (tgmg.hh:235, 256-265):
+ * 10 2x2 blocks (dl,dc,dr,cl,cc,cr,ul,uc,ur,inverse of cc) per point,
+ * (a,b,c,d) each, of coarse level l, expanded to m*n*40 doubles. */
+int stzg_mg_stencil(stzg_sim *s, double dt, int level, double *out);
+
+/* Instrumentation (no counterpart in the reference, whose timing is
+ * omp_get_wtime per frame, shear_sim.cc:165-179): average device time in ms
+ * of `reps` back-to-back launches of one kernel group on the handle's stream,
+ * measured with CUDA events.  kernel: 0 advection (writes the spare buffer,
+ * state unchanged), 1 FP64 top-level sweep (changes the velocity iterate),
+ * 2 FP32 top-level sweep (scratch), 3 FP64 V-cycle, 4 FP32 V-cycle
+ * (scratch), 5 FP64 residual + FP32 copy + norms. */
+int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
+
+/* Replaces: shear_sim::l2_comparison (shear_sim.cc:460-502) between two
+ * handles of the same grid: l2[4] = velocity, stress, chi, reference map. */
+int stzg_l2_comparison(stzg_sim *a, stzg_sim *b, double *l2);
+
+/* Replaces: shear_sim::initialize_random (shear_sim.cc:932-984) with a
+ * counter-based seed in place of libc rand(): writes chi (m*n) on the host. */
+int stzg_random_chi(int m, int n, double l, double tem_avg, double tem_std, double TZ,
+                    unsigned long long seed, double *chi);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,798 @@
+// C ABI (include/stzg.h): handle management, the time-step driver and the
+// multigrid solve policy.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mg.cuh"
+#include "step.cuh"
+
+#include <atomic>
+
+namespace stzg {
+
+static thread_local std::string g_msg;
+static std::atomic<long> g_launches(0);
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+int fail(int status, const std::string &msg) {
+    g_msg = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    g_msg = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return STZG_ENOMEM;
+    return STZG_ECUDA;
+}
+
+}  // namespace stzg
+
+using namespace stzg;
+
+struct stzg_sim {
+    stz_params P;
+    stzg_options O;
+    int m, n;
+    double time = 0;
+    double bv_state = 0;  // wall speed of the stored state (u=-bv on row 0, +bv on row n)
+    cudaStream_t st = nullptr;
+    step_consts sc;
+    fields_dev F;
+    int cur = 0;
+    std::vector<void *> owned;
+    // multigrid
+    qs_constants q;
+    double viscdt = -1;
+    std::vector<level_ops> ops;
+    hierarchy<double> h64;
+    hierarchy<float> h32;
+    double *partials = nullptr;  // device, 2 per block
+    double *dnorm = nullptr;     // device: [r2, b2]
+    double *hnorm = nullptr;     // pinned host copy
+    int npart = 0;
+    // tgmg_predict state (tgmg_predict.hh:6-33, tgmg_config.hh:26-45)
+    int lim = 16 * 8, mult = 16, decay = 32, max_thresh = 16 * 2048, extra_iters = 1;
+    long avg_vcount = 0, avg_solves = 0;
+    stzg_stats acc{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // captured graphs: one FP64 V-cycle; mixed: initial residual, one pass
+    cudaGraphExec_t g_vc64 = nullptr, g_res32 = nullptr, g_pass32 = nullptr;
+    long n_vc64 = 0, n_res32 = 0, n_pass32 = 0;  // kernel nodes per graph
+    int g_inner = 0;
+    double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)
+    bool have_prev = false;
+};
+
+namespace {
+
+int dev_alloc(stzg_sim *s, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    s->owned.push_back(*p);
+    STZG_CUDA(cudaMemsetAsync(*p, 0, bytes, s->st));
+    return STZG_OK;
+}
+
+double bdry_vel(const stzg_sim *s, double t) { return t < 1 ? t * s->P.u_bdry : s->P.u_bdry; }
+double bdry_pos(const stzg_sim *s, double t) {
+    return t < 1 ? s->P.u_bdry * t * t * 0.5 : s->P.u_bdry * (t - 0.5);
+}
+
+int validate(const stz_params *p) {
+    if (!p) return fail(STZG_EINVAL, "null parameters");
+    if (p->m < 4 || p->n < 4) return fail(STZG_EINVAL, "grid needs m,n >= 4");
+    if (p->m & 1) return fail(STZG_EINVAL, "m must be even (two-colour top-level smoother on a periodic line)");
+    if (!(p->bx > p->ax) || !(p->by > p->ay)) return fail(STZG_EINVAL, "empty domain");
+    if (p->stz_model < 0 || p->stz_model > 3) return fail(STZG_EINVAL, "unknown STZ law");
+    if (!(p->mu > 0)) return fail(STZG_EINVAL, "shear modulus must be positive");
+    long pts = (long)p->m * (p->n + 2);
+    if (pts > (1L << 31) / 2) return fail(STZG_EINVAL, "grid too large for 32-bit row indexing");
+    return STZG_OK;
+}
+
+void drop_graphs(stzg_sim *s) {
+    cudaGraphExec_t *g[3] = {&s->g_vc64, &s->g_res32, &s->g_pass32};
+    for (int k = 0; k < 3; k++)
+        if (*g[k]) {
+            cudaGraphExecDestroy(*g[k]);
+            *g[k] = nullptr;
+        }
+}
+
+// Captures the work `body` enqueues on the handle's stream into *out;
+// *nodes receives the number of kernels it holds.
+template <class F> int capture(stzg_sim *s, cudaGraphExec_t *out, long *nodes, F &&body) {
+    if (*out) return STZG_OK;
+    STZG_CUDA(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    const long c0 = launch_count();
+    body();
+    *nodes = launch_count() - c0;
+    g_launches.fetch_sub(*nodes);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->st, &g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    return STZG_OK;
+}
+
+// Sets up the operator hierarchy for viscosity/dt (qs_multi::init,
+// qs_multi.cc:31-55 -> tgmg::setup, tgmg.hh:331-351).
+int ensure_ops(stzg_sim *s, double dt) {
+    double viscdt = s->P.viscosity / dt;
+    if (viscdt == s->viscdt && !s->ops.empty()) return STZG_OK;
+    drop_graphs(s);
+    s->q.init(s->P, viscdt);
+    s->ops = build_coarse_ops(s->q, s->m, s->n + 1);
+    top_op<double> o = s->q.op<double>();
+    STZG_CHECK(s->h64.upload_ops(s->ops, o));
+    if (s->O.precision == STZG_MIXED) STZG_CHECK(s->h32.upload_ops(s->ops, o));
+    s->viscdt = viscdt;
+    return STZG_OK;
+}
+
+// Residual norms of the current vel/src (FP64) into dnorm = [r.r, b.b];
+// the mixed variant also leaves r in FP32 as the right-hand side of the
+// next FP32 V-cycles.
+void launch_norms(stzg_sim *s, bool mixed) {
+    const int M = s->m, N = s->n + 1;
+    if (mixed)
+        mixed_residual(s->q.op<double>(), s->F.vel, s->F.src, M, N, s->h32.lv[0].b, s->partials, s->npart,
+                       s->dnorm, s->dnorm + 1, s->st);
+    else
+        top_residual_sqnorm(s->h64, s->partials, s->npart, s->dnorm, s->dnorm + 1, s->st);
+}
+
+// Reads dnorm and evaluates the stopping rule.
+int read_check(stzg_sim *s, double *err, bool *ok) {
+    const int M = s->m, N = s->n + 1;
+    STZG_CUDA(cudaMemcpyAsync(s->hnorm, s->dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    s->acc.checks++;
+    double r2 = s->hnorm[0], b2 = s->hnorm[1];
+    if (std::isnan(r2)) return fail(STZG_ENAN, "NaN residual");
+    if (s->O.tol_mode == STZG_TOL_REFERENCE) {
+        *err = r2 / ((double)M * N);  // l2_error() = mds()/mn, tgmg.hh:146
+        *ok = *err < s->q.reference_acc(s->O.tol);
+    } else {
+        *err = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+        *ok = b2 > 0 ? r2 <= s->O.tol * s->O.tol * b2 : r2 == 0;
+    }
+    s->acc.last_error = *err;
+    return STZG_OK;
+}
+
+int check(stzg_sim *s, bool mixed, double *err, bool *ok) {
+    launch_norms(s, mixed);
+    return read_check(s, err, ok);
+}
+
+int run_vcycles(stzg_sim *s, int k) {
+    if (k <= 0) return STZG_OK;
+    if (s->O.use_graphs) {
+        STZG_CHECK(capture(s, &s->g_vc64, &s->n_vc64, [&] { vcycle<double>(s->h64, s->st, 10, 1); }));
+        for (int c = 0; c < k; c++) {
+            STZG_CUDA(cudaGraphLaunch(s->g_vc64, s->st));
+            g_launches.fetch_add(s->n_vc64);
+        }
+    } else {
+        for (int c = 0; c < k; c++) vcycle<double>(s->h64, s->st, 10, 1);
+    }
+    return STZG_OK;
+}
+
+// tgmg::solve(4, tgmg_predict&) (tgmg.in.cc:266-301) in FP64.
+int solve_fp64(stzg_sim *s, int *ncyc) {
+    int nc = s->lim / s->mult;
+    STZG_CHECK(run_vcycles(s, nc));
+    double err;
+    bool ok;
+    STZG_CHECK(check(s, false, &err, &ok));
+    if (ok) {
+        if (s->lim > 0) s->lim -= 1 + s->lim / s->decay;
+    } else {
+        int k = 0;
+        do {
+            s->lim += ++k * s->mult;
+            if (s->lim > s->max_thresh) return fail(STZG_ENOTCONV, "multigrid did not converge");
+            nc += k;
+            STZG_CHECK(run_vcycles(s, k));
+            STZG_CHECK(check(s, false, &err, &ok));
+        } while (!ok);
+    }
+    STZG_CHECK(run_vcycles(s, s->extra_iters));
+    s->acc.vcycles += nc;
+    s->acc.extra_vcycles += s->extra_iters;
+    s->acc.solves++;
+    s->avg_vcount += nc;
+    s->avg_solves++;
+    if (ncyc) *ncyc = nc;
+    return STZG_OK;
+}
+
+// FP32 V-cycles inside FP64 iterative refinement.  One pass: e = 0,
+// `inner` FP32 V-cycles on A e = r (coarsest level solved in FP64), z += e in
+// FP64, then the FP64 residual r = b - A z (kept in FP32 for the next pass)
+// and its norm.  The number of passes between host checks follows the
+// tgmg_predict policy (tgmg.in.cc:266-301) applied to passes.
+int run_passes(stzg_sim *s, int k) {
+    const long count = (long)s->m * (s->n + 1);
+    const int inner = s->g_inner;
+    auto pass = [&] {
+        cudaMemsetAsync(s->h32.lv[0].z, 0, sizeof(float2) * count, s->st);
+        for (int c = 0; c < inner; c++) vcycle<float>(s->h32, s->st, 10, 1);
+        mixed_correct(s->F.vel, s->h32.lv[0].z, count, s->st);
+        launch_norms(s, true);
+    };
+    if (k <= 0) return STZG_OK;
+    if (s->O.use_graphs) {
+        STZG_CHECK(capture(s, &s->g_pass32, &s->n_pass32, pass));
+        for (int c = 0; c < k; c++) {
+            STZG_CUDA(cudaGraphLaunch(s->g_pass32, s->st));
+            g_launches.fetch_add(s->n_pass32);
+        }
+    } else {
+        for (int c = 0; c < k; c++) pass();
+    }
+    s->acc.refinements += k;
+    return STZG_OK;
+}
+
+int solve_mixed(stzg_sim *s, int *ncyc) {
+    const int inner = s->O.inner_cycles > 0 ? s->O.inner_cycles : 2;
+    if (inner != s->g_inner && s->g_pass32) {
+        cudaGraphExecDestroy(s->g_pass32);
+        s->g_pass32 = nullptr;
+    }
+    s->g_inner = inner;
+    launch_norms(s, true);  // initial residual of the warm start
+    int np = s->lim / s->mult;
+    STZG_CHECK(run_passes(s, np));
+    double err;
+    bool ok;
+    STZG_CHECK(read_check(s, &err, &ok));
+    if (ok) {
+        if (s->lim > 0) s->lim -= 1 + s->lim / s->decay;
+    } else {
+        int k = 0;
+        do {
+            s->lim += ++k * s->mult;
+            if (s->lim > s->max_thresh) return fail(STZG_ENOTCONV, "iterative refinement did not converge");
+            np += k;
+            STZG_CHECK(run_passes(s, k));
+            STZG_CHECK(read_check(s, &err, &ok));
+        } while (!ok);
+    }
+    const int cycles = np * inner;
+    s->acc.vcycles += cycles;
+    s->acc.solves++;
+    s->avg_vcount += cycles;
+    s->avg_solves++;
+    if (ncyc) *ncyc = cycles;
+    return STZG_OK;
+}
+
+int solve(stzg_sim *s, int *ncyc) {
+    return s->O.precision == STZG_MIXED ? solve_mixed(s, ncyc) : solve_fp64(s, ncyc);
+}
+
+int do_projection(stzg_sim *s, double dt) {
+    STZG_CHECK(ensure_ops(s, dt));
+    const double bv = bdry_vel(s, s->time), bp = bdry_pos(s, s->time);
+    projection_source(s->sc, s->F, s->cur, dt, s->q.bcs * s->q.cxx * bv, s->st);
+    if (s->O.extrapolate) {
+        const long cnt = (long)s->m * (s->n + 1);
+        if (s->have_prev) {
+            extrapolate_guess(s->F.vel, s->vel_prev, cnt, s->st);
+        } else {
+            STZG_CUDA(cudaMemcpyAsync(s->vel_prev, s->F.vel, cnt * sizeof(double2), cudaMemcpyDeviceToDevice, s->st));
+            s->have_prev = true;
+        }
+    }
+    STZG_CHECK(solve(s, nullptr));
+    projection_apply(s->sc, s->F, s->cur, dt, bv, bp, s->st);
+    s->bv_state = bv;
+    return STZG_OK;
+}
+
+int do_advection(stzg_sim *s, double dt) {
+    advection(s->sc, s->F, s->cur, dt, s->bv_state, s->st);
+    s->cur ^= 1;
+    return STZG_OK;
+}
+
+int check_flags(stzg_sim *s) {
+    int h[2];
+    STZG_CUDA(cudaMemcpyAsync(h, s->F.flags, sizeof(h), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    if (h[1] > s->acc.substeps_max) s->acc.substeps_max = h[1];
+    if (h[0]) return fail(STZG_ESUBSTEP, "plastic sub-stepping reached its iteration cap");
+    return STZG_OK;
+}
+
+size_t cell_count(const stzg_sim *s) { return (size_t)s->m * (s->n + 2); }
+
+}  // namespace
+
+extern "C" {
+
+void stzg_default_options(stzg_options *o) {
+    std::memset(o, 0, sizeof(*o));
+    o->precision = STZG_FP64;
+    o->tol_mode = STZG_TOL_REFERENCE;
+    o->tol = 1e4;
+    o->track_plastic = 1;
+    o->device = 0;
+    o->inner_cycles = 0;
+    o->use_graphs = 1;
+    o->extrapolate = 0;
+}
+
+const char *stzg_strerror(int st) {
+    switch (st) {
+        case STZG_OK: return "ok";
+        case STZG_EINVAL: return "invalid argument";
+        case STZG_ENOMEM: return "out of device memory";
+        case STZG_ECUDA: return "CUDA error";
+        case STZG_ENOTCONV: return "multigrid did not converge";
+        case STZG_ENAN: return "NaN residual";
+        case STZG_ESUBSTEP: return "plastic sub-step cap reached";
+        case STZG_ENODEV: return "no usable GPU";
+    }
+    return "unknown status";
+}
+
+const char *stzg_last_message(void) { return g_msg.c_str(); }
+
+int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
+    if (!out) return fail(STZG_EINVAL, "null output handle");
+    *out = nullptr;
+    STZG_CHECK(validate(p));
+    stzg_options o;
+    if (opt) o = *opt;
+    else stzg_default_options(&o);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(STZG_ENODEV, "no CUDA device");
+    if (o.device < 0 || o.device >= ndev) return fail(STZG_EINVAL, "device ordinal out of range");
+    STZG_CUDA(cudaSetDevice(o.device));
+    stzg_sim *s = new stzg_sim;
+    s->P = *p;
+    s->O = o;
+    s->m = p->m;
+    s->n = p->n;
+    s->sc = make_step_consts(*p);
+    s->sc.track_plastic = o.track_plastic;
+    if (o.substep_cap > 0) s->sc.substep_cap = o.substep_cap;
+    int st = STZG_OK;
+    auto bail = [&](int code) {
+        stzg_destroy(s);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(STZG_ECUDA, "stream creation failed"));
+    const size_t nc = cell_count(s), nn = (size_t)s->m * (s->n + 1);
+    std::memset(&s->F, 0, sizeof(s->F));
+    for (int b = 0; b < 2; b++)
+        for (int k = 0; k < F_COUNT; k++)
+            if ((st = dev_alloc(s, (void **)&s->F.f[b][k], nc * sizeof(double))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->F.ddev, nc * sizeof(double))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->F.eps_pl, (size_t)s->m * s->n * sizeof(double))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->F.vel, nn * sizeof(double2))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->F.src, nn * sizeof(double2))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->F.flags, 4 * sizeof(int))) != STZG_OK) return bail(st);
+    if (o.extrapolate)
+        if ((st = dev_alloc(s, (void **)&s->vel_prev, nn * sizeof(double2))) != STZG_OK) return bail(st);
+    s->npart = reduction_blocks();
+    if ((st = dev_alloc(s, (void **)&s->partials, 2 * s->npart * sizeof(double))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->dnorm, 2 * sizeof(double))) != STZG_OK) return bail(st);
+    if (cudaMallocHost(&s->hnorm, 2 * sizeof(double)) != cudaSuccess) return bail(fail(STZG_ENOMEM, "pinned alloc"));
+    // FP64 hierarchy over vel/src; FP32 hierarchy with its own top arrays
+    if ((st = s->h64.allocate(s->m, s->n + 1, s->F.vel, s->F.src)) != STZG_OK) return bail(st);
+    if (o.precision == STZG_MIXED)
+        if ((st = s->h32.allocate(s->m, s->n + 1, nullptr, nullptr)) != STZG_OK) return bail(st);
+    cudaEventCreate(&s->ev0);
+    cudaEventCreate(&s->ev1);
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return bail(fail(STZG_ECUDA, "set-up failed"));
+    *out = s;
+    return STZG_OK;
+}
+
+int stzg_destroy(stzg_sim *s) {
+    if (!s) return STZG_OK;
+    if (s->st) cudaStreamSynchronize(s->st);
+    drop_graphs(s);
+    for (void *p : s->owned) cudaFree(p);
+    s->h64.release();
+    s->h32.release();
+    if (s->hnorm) cudaFreeHost(s->hnorm);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return STZG_OK;
+}
+
+int stzg_set_state(stzg_sim *s, const double *chi) {
+    if (!s || !chi) return fail(STZG_EINVAL, "null argument");
+    const int m = s->m, n = s->n;
+    const size_t nc = cell_count(s);
+    std::vector<double> zero(nc, 0.0), X(nc, 0.0), Y(nc, 0.0), C(nc, 0.0);
+    const double dx = (s->P.bx - s->P.ax) / m, dy = (s->P.by - s->P.ay) / n;
+    for (int j = -1; j <= n; j++)
+        for (int i = 0; i < m; i++) {
+            size_t k = (size_t)(j + 1) * m + i;
+            X[k] = s->P.ax + i * dx;
+            Y[k] = s->P.ay + j * dy;
+            if (j >= 0 && j < n) C[k] = chi[(size_t)j * m + i];
+        }
+    for (int i = 0; i < m; i++) {
+        C[i] = 2 * C[(size_t)m + i] - C[(size_t)2 * m + i];
+        C[(size_t)(n + 1) * m + i] = 2 * C[(size_t)n * m + i] - C[(size_t)(n - 1) * m + i];
+    }
+    for (int b = 0; b < 2; b++) {
+        for (int k = 0; k < F_CHI; k++)
+            STZG_CUDA(cudaMemcpyAsync(s->F.f[b][k], zero.data(), nc * 8, cudaMemcpyHostToDevice, s->st));
+        STZG_CUDA(cudaMemcpyAsync(s->F.f[b][F_CHI], C.data(), nc * 8, cudaMemcpyHostToDevice, s->st));
+        STZG_CUDA(cudaMemcpyAsync(s->F.f[b][F_X], X.data(), nc * 8, cudaMemcpyHostToDevice, s->st));
+        STZG_CUDA(cudaMemcpyAsync(s->F.f[b][F_Y], Y.data(), nc * 8, cudaMemcpyHostToDevice, s->st));
+    }
+    STZG_CUDA(cudaMemsetAsync(s->F.ddev, 0, nc * 8, s->st));
+    STZG_CUDA(cudaMemsetAsync(s->F.eps_pl, 0, (size_t)m * n * 8, s->st));
+    STZG_CUDA(cudaMemsetAsync(s->F.vel, 0, (size_t)m * (n + 1) * sizeof(double2), s->st));
+    STZG_CUDA(cudaMemsetAsync(s->F.flags, 0, 4 * sizeof(int), s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    s->time = 0;
+    s->bv_state = 0;
+    s->cur = 0;
+    s->have_prev = false;
+    return STZG_OK;
+}
+
+static int field_slot(int field) {
+    switch (field) {
+        case STZG_P: return F_P;
+        case STZG_Q: return F_Q;
+        case STZG_S: return F_S;
+        case STZG_TAU: return F_TAU;
+        case STZG_CHI: return F_CHI;
+        case STZG_X: return F_X;
+        case STZG_Y: return F_Y;
+    }
+    return -1;
+}
+
+int stzg_get_field(stzg_sim *s, int field, double *host) {
+    if (!s || !host) return fail(STZG_EINVAL, "null argument");
+    const int m = s->m, n = s->n;
+    const size_t nn = (size_t)m * (n + 1), nc = cell_count(s);
+    if (field == STZG_U || field == STZG_V) {
+        std::vector<double2> v(nn);
+        STZG_CUDA(cudaMemcpyAsync(v.data(), s->F.vel, nn * sizeof(double2), cudaMemcpyDeviceToHost, s->st));
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+        const double bv = s->bv_state;
+        for (int j = 0; j <= n; j++)
+            for (int i = 0; i < m; i++) {
+                size_t k = (size_t)j * m + i;
+                double val = field == STZG_U ? v[k].x : v[k].y;
+                if (j == 0) val = field == STZG_U ? -bv : 0.0;
+                if (j == n) val = field == STZG_U ? bv : 0.0;
+                host[k] = val;
+            }
+        return STZG_OK;
+    }
+    if (field == STZG_EPS_PL) {
+        STZG_CUDA(cudaMemcpyAsync(host, s->F.eps_pl, (size_t)m * n * 8, cudaMemcpyDeviceToHost, s->st));
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+        return STZG_OK;
+    }
+    if (field == STZG_DDEV) {
+        STZG_CUDA(cudaMemcpyAsync(host, s->F.ddev, nc * 8, cudaMemcpyDeviceToHost, s->st));
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+        return STZG_OK;
+    }
+    int slot = field_slot(field);
+    if (slot < 0) return fail(STZG_EINVAL, "unknown field id");
+    const double *src = s->F.f[s->cur][slot];
+    if (slot == F_X || slot == F_Y) src += m;  // node rows 0..n
+    size_t cnt = (slot == F_X || slot == F_Y) ? nn : nc;
+    STZG_CUDA(cudaMemcpyAsync(host, src, cnt * 8, cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+int stzg_set_field(stzg_sim *s, int field, const double *host) {
+    if (!s || !host) return fail(STZG_EINVAL, "null argument");
+    const int m = s->m, n = s->n;
+    const size_t nn = (size_t)m * (n + 1), nc = cell_count(s);
+    if (field == STZG_U || field == STZG_V) {
+        std::vector<double2> v(nn);
+        STZG_CUDA(cudaMemcpy(v.data(), s->F.vel, nn * sizeof(double2), cudaMemcpyDeviceToHost));
+        for (size_t k = 0; k < nn; k++) (field == STZG_U ? v[k].x : v[k].y) = host[k];
+        STZG_CUDA(cudaMemcpy(s->F.vel, v.data(), nn * sizeof(double2), cudaMemcpyHostToDevice));
+        s->have_prev = false;
+        // walls carry +-bv on u and 0 on v (set_boundaries, shear_sim.cc:557-572)
+        if (field == STZG_U) s->bv_state = host[(size_t)n * m];
+        return STZG_OK;
+    }
+    if (field == STZG_EPS_PL) {
+        STZG_CUDA(cudaMemcpy(s->F.eps_pl, host, (size_t)m * n * 8, cudaMemcpyHostToDevice));
+        return STZG_OK;
+    }
+    if (field == STZG_DDEV) {
+        STZG_CUDA(cudaMemcpy(s->F.ddev, host, nc * 8, cudaMemcpyHostToDevice));
+        return STZG_OK;
+    }
+    int slot = field_slot(field);
+    if (slot < 0) return fail(STZG_EINVAL, "unknown field id");
+    for (int b = 0; b < 2; b++) {
+        double *dst = s->F.f[b][slot];
+        if (slot == F_X || slot == F_Y) dst += m;
+        size_t cnt = (slot == F_X || slot == F_Y) ? nn : nc;
+        STZG_CUDA(cudaMemcpy(dst, host, cnt * 8, cudaMemcpyHostToDevice));
+    }
+    return STZG_OK;
+}
+
+int stzg_set_time(stzg_sim *s, double t) {
+    if (!s) return fail(STZG_EINVAL, "null handle");
+    s->time = t;
+    return STZG_OK;
+}
+
+int stzg_get_time(stzg_sim *s, double *t) {
+    if (!s || !t) return fail(STZG_EINVAL, "null argument");
+    *t = s->time;
+    return STZG_OK;
+}
+
+int stzg_step_qs(stzg_sim *s, double dt, int nsteps, stzg_stats *stats) {
+    if (!s || nsteps < 0 || !(dt > 0)) return fail(STZG_EINVAL, "bad step arguments");
+    stzg_stats before = s->acc;
+    const long l0 = launch_count();
+    STZG_CHECK(ensure_ops(s, dt));
+    STZG_CUDA(cudaEventRecord(s->ev0, s->st));
+    for (int k = 0; k < nsteps; k++) {
+        s->time += dt;  // shear_sim.cc:283
+        STZG_CHECK(do_advection(s, dt));
+        STZG_CHECK(do_projection(s, dt));
+        STZG_CHECK(check_flags(s));
+    }
+    STZG_CUDA(cudaEventRecord(s->ev1, s->st));
+    STZG_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->acc.seconds += ms * 1e-3;
+    STZG_CHECK(check_flags(s));
+    if (stats) {
+        *stats = s->acc;
+        stats->vcycles -= before.vcycles;
+        stats->extra_vcycles -= before.extra_vcycles;
+        stats->solves -= before.solves;
+        stats->refinements -= before.refinements;
+        stats->checks -= before.checks;
+        stats->seconds -= before.seconds;
+        stats->kernel_launches = launch_count() - l0;
+    }
+    return STZG_OK;
+}
+
+int stzg_upload(stzg_sim *s, const double *const *up) {
+    if (!s || !up) return fail(STZG_EINVAL, "null argument");
+    const int m = s->m;
+    const size_t nn = (size_t)m * (s->n + 1), nc = cell_count(s);
+    for (int k = 0; k < 7; k++) {
+        if (!up[k]) continue;
+        double *dst = s->F.f[s->cur][k];
+        size_t cnt = nc;
+        if (k == F_X || k == F_Y) {
+            dst += m;
+            cnt = nn;
+        }
+        STZG_CUDA(cudaMemcpyAsync(dst, up[k], cnt * 8, cudaMemcpyHostToDevice, s->st));
+    }
+    if (up[7]) {
+        STZG_CUDA(cudaMemcpyAsync(s->F.vel, up[7], nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
+        s->have_prev = false;
+    }
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+int stzg_download(stzg_sim *s, double *const *down) {
+    if (!s || !down) return fail(STZG_EINVAL, "null argument");
+    const int m = s->m;
+    const size_t nn = (size_t)m * (s->n + 1), nc = cell_count(s);
+    for (int k = 0; k < 7; k++) {
+        if (!down[k]) continue;
+        const double *src = s->F.f[s->cur][k];
+        size_t cnt = nc;
+        if (k == F_X || k == F_Y) {
+            src += m;
+            cnt = nn;
+        }
+        STZG_CUDA(cudaMemcpyAsync(down[k], src, cnt * 8, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (down[7]) STZG_CUDA(cudaMemcpyAsync(down[7], s->F.vel, nn * sizeof(double2), cudaMemcpyDeviceToHost, s->st));
+    if (down[8])
+        STZG_CUDA(cudaMemcpyAsync(down[8], s->F.eps_pl, (size_t)m * s->n * 8, cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {
+    if (!s || !ms || reps < 1 || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(ensure_ops(s, dt));
+    if ((kernel == 2 || kernel == 4 || kernel == 5) && s->O.precision != STZG_MIXED)
+        return fail(STZG_EINVAL, "FP32 kernels need a mixed-precision handle");
+    auto one = [&]() -> int {
+        switch (kernel) {
+            case 0: advection(s->sc, s->F, s->cur, dt, s->bv_state, s->st); break;
+            case 1: top_sweep<double>(s->h64, s->st); break;
+            case 2: top_sweep<float>(s->h32, s->st); break;
+            case 3: vcycle<double>(s->h64, s->st, 10, 1); break;
+            case 4: vcycle<float>(s->h32, s->st, 10, 1); break;
+            case 5: launch_norms(s, true); break;
+            default: return fail(STZG_EINVAL, "unknown kernel id");
+        }
+        return STZG_OK;
+    };
+    STZG_CHECK(one());  // warm-up
+    STZG_CUDA(cudaEventRecord(s->ev0, s->st));
+    for (int r = 0; r < reps; r++) STZG_CHECK(one());
+    STZG_CUDA(cudaEventRecord(s->ev1, s->st));
+    STZG_CUDA(cudaEventSynchronize(s->ev1));
+    float t = 0;
+    cudaEventElapsedTime(&t, s->ev0, s->ev1);
+    *ms = t / reps;
+    return STZG_OK;
+}
+
+int stzg_advection_step(stzg_sim *s, double dt) {
+    if (!s || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(do_advection(s, dt));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return check_flags(s);
+}
+
+int stzg_projection_step(stzg_sim *s, double dt, stzg_stats *stats) {
+    if (!s || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(do_projection(s, dt));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    if (stats) *stats = s->acc;
+    return STZG_OK;
+}
+
+int stzg_avg_iters(stzg_sim *s, double *avg) {
+    if (!s || !avg) return fail(STZG_EINVAL, "null argument");
+    *avg = s->avg_solves ? (double)s->avg_vcount / s->avg_solves : 0.0;
+    s->avg_vcount = s->avg_solves = 0;
+    return STZG_OK;
+}
+
+int stzg_mg_solve(stzg_sim *s, double dt, const double *src, double *vel, int *ncycles) {
+    if (!s || !src || !vel || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(ensure_ops(s, dt));
+    const size_t nn = (size_t)s->m * (s->n + 1);
+    STZG_CUDA(cudaMemcpyAsync(s->F.src, src, nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
+    STZG_CUDA(cudaMemcpyAsync(s->F.vel, vel, nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
+    int st = solve(s, ncycles);
+    STZG_CUDA(cudaMemcpyAsync(vel, s->F.vel, nn * sizeof(double2), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return st;
+}
+
+int stzg_mg_vcycle(stzg_sim *s, double dt, const double *src, double *vel) {
+    if (!s || !src || !vel || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(ensure_ops(s, dt));
+    const size_t nn = (size_t)s->m * (s->n + 1);
+    STZG_CUDA(cudaMemcpyAsync(s->F.src, src, nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
+    STZG_CUDA(cudaMemcpyAsync(s->F.vel, vel, nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
+    STZG_CHECK(run_vcycles(s, 1));
+    STZG_CUDA(cudaMemcpyAsync(vel, s->F.vel, nn * sizeof(double2), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+int stzg_mg_l2_error(stzg_sim *s, double dt, const double *src, const double *vel, double *err) {
+    if (!s || !src || !vel || !err || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(ensure_ops(s, dt));
+    const size_t nn = (size_t)s->m * (s->n + 1);
+    STZG_CUDA(cudaMemcpyAsync(s->F.src, src, nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
+    STZG_CUDA(cudaMemcpyAsync(s->F.vel, vel, nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
+    top_residual_sqnorm(s->h64, s->partials, s->npart, s->dnorm, s->dnorm + 1, s->st);
+    STZG_CUDA(cudaMemcpyAsync(s->hnorm, s->dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    *err = s->hnorm[0] / (double)nn;
+    return STZG_OK;
+}
+
+int stzg_mg_levels(stzg_sim *s, double dt, int *nlevels, int *dims) {
+    if (!s || !nlevels || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(ensure_ops(s, dt));
+    *nlevels = (int)s->ops.size();
+    if (dims)
+        for (size_t l = 0; l < s->ops.size(); l++) {
+            dims[2 * l] = s->ops[l].m;
+            dims[2 * l + 1] = s->ops[l].n;
+        }
+    return STZG_OK;
+}
+
+int stzg_mg_stencil(stzg_sim *s, double dt, int level, double *out) {
+    if (!s || !out || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CHECK(ensure_ops(s, dt));
+    if (level < 0 || level >= (int)s->ops.size()) return fail(STZG_EINVAL, "level out of range");
+    const level_ops &L = s->ops[level];
+    for (int j = 0; j < L.n; j++)
+        for (int i = 0; i < L.m; i++) {
+            int c = L.homog ? L.cls[j] : L.cls[(size_t)j * L.m + i];
+            const stencil9<double> &t = L.table[c];
+            double *o = out + 40 * ((size_t)j * L.m + i);
+            for (int e = 0; e < 10; e++) {
+                o[4 * e] = t.e[e].a;
+                o[4 * e + 1] = t.e[e].b;
+                o[4 * e + 2] = t.e[e].c;
+                o[4 * e + 3] = t.e[e].d;
+            }
+        }
+    return STZG_OK;
+}
+
+int stzg_l2_comparison(stzg_sim *a, stzg_sim *b, double *l2) {
+    if (!a || !b || !l2) return fail(STZG_EINVAL, "null argument");
+    if (a->m != b->m || a->n != b->n) return fail(STZG_EINVAL, "grids differ");
+    const int m = a->m, n = a->n;
+    const size_t nn = (size_t)m * (n + 1), nc = cell_count(a);
+    std::vector<double> fa(nc), fb(nc);
+    // shear_sim::l2_comparison, shear_sim.cc:460-502
+    double c[4] = {0, 0, 0, 0};
+    std::vector<double> ua(nn), ub(nn), va(nn), vb(nn), Xa(nn), Xb(nn), Ya(nn), Yb(nn);
+    STZG_CHECK(stzg_get_field(a, STZG_U, ua.data()));
+    STZG_CHECK(stzg_get_field(b, STZG_U, ub.data()));
+    STZG_CHECK(stzg_get_field(a, STZG_V, va.data()));
+    STZG_CHECK(stzg_get_field(b, STZG_V, vb.data()));
+    STZG_CHECK(stzg_get_field(a, STZG_X, Xa.data()));
+    STZG_CHECK(stzg_get_field(b, STZG_X, Xb.data()));
+    STZG_CHECK(stzg_get_field(a, STZG_Y, Ya.data()));
+    STZG_CHECK(stzg_get_field(b, STZG_Y, Yb.data()));
+    std::vector<std::vector<double>> SA(5, std::vector<double>(nc)), SB(5, std::vector<double>(nc));
+    const int ids[5] = {STZG_P, STZG_Q, STZG_S, STZG_TAU, STZG_CHI};
+    for (int k = 0; k < 5; k++) {
+        STZG_CHECK(stzg_get_field(a, ids[k], SA[k].data()));
+        STZG_CHECK(stzg_get_field(b, ids[k], SB[k].data()));
+    }
+    for (int j = 0; j <= n; j++) {
+        double c0 = 0, c3 = 0;
+        for (int i = 0; i < m; i++) {
+            size_t k = (size_t)j * m + i;
+            double du = ua[k] - ub[k], dv = va[k] - vb[k], dX = Xa[k] - Xb[k], dY = Ya[k] - Yb[k];
+            c0 += du * du + dv * dv;
+            c3 += dX * dX + dY * dY;
+        }
+        double w = (j == 0 || j == n) ? 0.5 : 1.0;
+        c[0] += w * c0;
+        c[3] += w * c3;
+    }
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            size_t k = (size_t)(j + 1) * m + i;
+            double dp = SA[0][k] - SB[0][k], dq = SA[1][k] - SB[1][k], ds = SA[2][k] - SB[2][k],
+                   dt = SA[3][k] - SB[3][k], dc = SA[4][k] - SB[4][k];
+            c[1] += 2 * (dt * dt + ds * ds) + 3 * dp * dp + 6 * dq * dq;
+            c[2] += dc * dc;
+        }
+    const double fac = ((a->P.bx - a->P.ax) / m) * ((a->P.by - a->P.ay) / n);
+    for (int k = 0; k < 4; k++) l2[k] = c[k] * fac;
+    return STZG_OK;
+}
+
+}  // extern "C"

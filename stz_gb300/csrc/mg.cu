@@ -1,0 +1,843 @@
+// Multigrid kernels and hierarchy set-up (see mg.cuh for the design).
+#include "mg.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <map>
+
+namespace stzg {
+
+// ---------------------------------------------------------------------------
+// qs_multi constants (qs_multi.cc:9-15 and qs_multi::init, qs_multi.cc:31-55)
+
+void qs_constants::init(const stz_params &p, double viscdt) {
+    const double dx = (p.bx - p.ax) / p.m, dy = (p.by - p.ay) / p.n;
+    const double xsp = 1. / dx, ysp = 1. / dy;
+    mu = p.mu;
+    Kq = p.K + p.mu / 3.0;
+    qK = .25 * Kq * xsp * ysp;
+    Kmu = Kq + p.mu;
+    xsp2 = xsp * xsp;
+    ysp2 = ysp * ysp;
+    xyfac = xsp2 + ysp2;
+    tmufac1 = Kmu * xsp2 + p.mu * ysp2;
+    tmufac2 = p.mu * xsp2 + Kmu * ysp2;
+    bcs = 4;
+    Kmx = (Kmu + viscdt) * xsp2;
+    Kmy = (Kmu + viscdt) * ysp2;
+    mx = (p.mu + viscdt) * xsp2;
+    my = (p.mu + viscdt) * ysp2;
+    cxx = -2 * (tmufac1 + viscdt * xyfac);
+    cyy = -2 * (tmufac2 + viscdt * xyfac);
+}
+
+double qs_constants::reference_acc(double mult) const {
+    double a = DBL_EPSILON * mult * (2 * (tmufac1 + tmufac2));
+    return a * a;
+}
+
+template <typename T> top_op<T> qs_constants::op() const {
+    top_op<T> o;
+    o.Kmx = (T)Kmx; o.Kmy = (T)Kmy; o.mx = (T)mx; o.my = (T)my; o.qK = (T)qK;
+    o.cxx = (T)cxx; o.cyy = (T)cyy;
+    o.icxx = (T)(1 / cxx); o.icyy = (T)(1 / cyy);
+    o.bcxx = (T)(bcs * cxx); o.bcyy = (T)(bcs * cyy);
+    o.ibcxx = (T)(1 / (bcs * cxx)); o.ibcyy = (T)(1 / (bcs * cyy));
+    return o;
+}
+template top_op<double> qs_constants::op<double>() const;
+template top_op<float> qs_constants::op<float>() const;
+
+// ---------------------------------------------------------------------------
+// Hierarchy sizes: child of (m,n) is ((m+1)>>1, (n+2)>>1) for x periodic and
+// y bounded (tgmg.hh:108-110); stop once m*n <= 10 (tgmg_config.hh:23).  A
+// periodic line shorter than 3 would alias its own neighbours, so
+// coarsening also stops there (the reference collapses such levels,
+// tgmg.in.cc:738-746).
+
+std::vector<std::pair<int, int>> coarse_sizes(int m, int n) {
+    std::vector<std::pair<int, int>> out;
+    int am = (m + 1) >> 1, an = (n + 2) >> 1;
+    while (am * an > 10 && am >= 3 && (int)out.size() < 16) {
+        out.push_back(std::make_pair(am, an));
+        int nm = (am + 1) >> 1, nn = (an + 2) >> 1;
+        am = nm;
+        an = nn;
+    }
+    return out;
+}
+
+// 1D prolongation: coarse points (and weights) that feed fine index f of a
+// line of um points (apply_t / t_line, tgmg.in.cc:552-621).
+__host__ __device__ inline int p1d(int f, int um, int prd, int *c, double *w) {
+    int sm = (um + (prd ? 1 : 2)) >> 1;
+    if (!(f & 1)) { c[0] = f >> 1; w[0] = 1; return 1; }
+    if (!prd && !(um & 1) && f == um - 1) { c[0] = sm - 1; w[0] = 1; return 1; }
+    c[0] = f >> 1; w[0] = 0.5;
+    c[1] = (prd && f == um - 1) ? 0 : (f >> 1) + 1; w[1] = 0.5;
+    return 2;
+}
+// Weight of coarse index c at fine index f (0 when c does not feed f).
+__host__ __device__ inline double pw(int f, int um, int prd, int c) {
+    int cc[2]; double ww[2];
+    int k = p1d(f, um, prd, cc, ww);
+    double w = 0;
+    for (int a = 0; a < k; a++) if (cc[a] == c) w += ww[a];
+    return w;
+}
+
+// ---------------------------------------------------------------------------
+// Galerkin coarse operators (tgmg_base::rat and the generated compute_rat,
+// tgmg.in.cc:667-736, tgmg_compile.pl:151-338), formed as sum_k sum_l
+// P(k,I) A(k,l) P(l,J) per coarse point I and neighbour J.
+
+namespace {
+
+typedef mat2<double> M2;
+
+inline M2 mz() { M2 r = {0, 0, 0, 0}; return r; }
+inline M2 mk(double a, double b, double c, double d) { M2 r = {a, b, c, d}; return r; }
+inline bool is_zero(const M2 &A) { return A.a == 0 && A.b == 0 && A.c == 0 && A.d == 0; }
+inline M2 inverse(const M2 &f) {  // 1/M as the reference's operator/(double,mat)
+    double idet = 1. / (f.a * f.d - f.b * f.c);
+    return mk(f.d * idet, -f.b * idet, -f.c * idet, f.a * idet);
+}
+
+// Fine operator of a level, entry k (dl dc dr cl cc cr ul uc ur) at (i,j).
+struct fine_access {
+    const qs_constants *q = nullptr;  // top level when set
+    const level_ops *L = nullptr;
+    int m, n;
+    M2 entry(int i, int j, int k) const {
+        if (q) {
+            bool wall = j == 0 || j == n - 1;
+            if (wall) return k == 4 ? mk(q->bcs * q->cxx, 0, 0, q->bcs * q->cyy) : mz();
+            switch (k) {
+                case 0: case 8: return mk(0, q->qK, q->qK, 0);
+                case 2: case 6: return mk(0, -q->qK, -q->qK, 0);
+                // The operator applied by qs_multi::mul_a (qs_multi.hh:41-50):
+                // horizontal neighbours (Kmx, mx), vertical (my, Kmy).  The
+                // reference's a_cl/a_dc (qs_multi.hh:26-29) swap mx and my in
+                // the second component, which only agrees for dx == dy.
+                case 3: case 5: return mk(q->Kmx, 0, 0, q->mx);
+                case 1: case 7: return mk(q->my, 0, 0, q->Kmy);
+                default: return mk(q->cxx, 0, 0, q->cyy);
+            }
+        }
+        int c = L->homog ? L->cls[j] : L->cls[(size_t)j * m + i];
+        return L->table[c].e[k];
+    }
+};
+
+void rap_point(const fine_access &A, int cm, int cn, int I, int J, stencil9<double> &out) {
+    const int fm = A.m, fn = A.n;
+    M2 acc[9];
+    for (int k = 0; k < 9; k++) acc[k] = mz();
+    for (int fy = 2 * J - 1; fy <= 2 * J + 1; fy++) {
+        if (fy < 0 || fy >= fn) continue;
+        double wyk = pw(fy, fn, 0, J);
+        if (wyk == 0) continue;
+        for (int d = -1; d <= 1; d++) {
+            int fx = ((2 * I + d) % fm + fm) % fm;
+            double wxk = pw(fx, fm, 1, I);
+            if (wxk == 0) continue;
+            double rk = wxk * wyk;
+            for (int sy = -1; sy <= 1; sy++) {
+                int ly = fy + sy;
+                if (ly < 0 || ly >= fn) continue;
+                for (int sx = -1; sx <= 1; sx++) {
+                    int lx = ((fx + sx) % fm + fm) % fm;
+                    M2 a = A.entry(fx, fy, (sy + 1) * 3 + sx + 1);
+                    if (is_zero(a)) continue;
+                    int cy[2], cx[2], ny, nx;
+                    double wy[2], wx[2];
+                    ny = p1d(ly, fn, 0, cy, wy);
+                    nx = p1d(lx, fm, 1, cx, wx);
+                    for (int b = 0; b < ny; b++)
+                        for (int c = 0; c < nx; c++) {
+                            int oy = cy[b] - J, ox = cx[c] - I;
+                            if (ox > cm / 2) ox -= cm;
+                            if (ox < -(cm / 2)) ox += cm;
+                            int k = (oy + 1) * 3 + ox + 1;
+                            double w = rk * wx[c] * wy[b];
+                            acc[k].a += w * a.a; acc[k].b += w * a.b;
+                            acc[k].c += w * a.c; acc[k].d += w * a.d;
+                        }
+                }
+            }
+        }
+    }
+    for (int k = 0; k < 9; k++) out.e[k] = acc[k];
+    out.e[9] = inverse(acc[4]);
+}
+
+bool same(const stencil9<double> &a, const stencil9<double> &b) {
+    return std::memcmp(&a, &b, sizeof(a)) == 0;
+}
+
+int class_of(std::vector<stencil9<double>> &table, const stencil9<double> &s) {
+    for (size_t k = 0; k < table.size(); k++)
+        if (same(table[k], s)) return (int)k;
+    table.push_back(s);
+    return (int)table.size() - 1;
+}
+
+}  // namespace
+
+std::vector<level_ops> build_coarse_ops(const qs_constants &q, int m, int n) {
+    std::vector<level_ops> out;
+    std::vector<std::pair<int, int>> sizes = coarse_sizes(m, n);
+    fine_access A;
+    A.q = &q;
+    A.m = m;
+    A.n = n;
+    bool fine_homog = true;
+    for (size_t l = 0; l < sizes.size(); l++) {
+        level_ops L;
+        L.m = sizes[l].first;
+        L.n = sizes[l].second;
+        // Uniform coarsening of a homogeneous periodic line keeps the
+        // operator x-homogeneous: one column per row suffices.
+        L.homog = fine_homog && (A.m % 2 == 0);
+        if (L.homog) {
+            L.cls.resize(L.n);
+            for (int J = 0; J < L.n; J++) {
+                stencil9<double> s;
+                rap_point(A, L.m, L.n, 0, J, s);
+                L.cls[J] = class_of(L.table, s);
+            }
+        } else {
+            L.cls.resize((size_t)L.m * L.n);
+            for (int J = 0; J < L.n; J++)
+                for (int I = 0; I < L.m; I++) {
+                    stencil9<double> s;
+                    rap_point(A, L.m, L.n, I, J, s);
+                    L.cls[(size_t)J * L.m + I] = class_of(L.table, s);
+                }
+        }
+        out.push_back(L);
+        fine_homog = L.homog;
+        A.q = nullptr;
+        A.L = &out.back();
+        A.m = L.m;
+        A.n = L.n;
+        // out may reallocate on the next push_back: re-point after it.
+        A.L = nullptr;
+        A.L = &out[l];
+    }
+    return out;
+}
+
+// Dense inverse of the coarsest operator by Gauss-Jordan elimination with
+// partial pivoting.  The reference smooths the coarsest level with 10+10
+// Gauss-Seidel sweeps (tgmg.in.cc:350-352); an exact solve is at least as
+// accurate and replaces ~80 dependent colour phases by one product.
+std::vector<double> coarsest_inverse(const level_ops &L) {
+    const int m = L.m, n = L.n, N = 2 * m * n;
+    std::vector<double> inv;
+    if (N > 1024) return inv;
+    std::vector<double> A((size_t)N * N, 0.0);
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            const int c = L.homog ? L.cls[j] : L.cls[(size_t)j * m + i];
+            const stencil9<double> &s = L.table[c];
+            const int row = 2 * (j * m + i);
+            for (int dy = -1; dy <= 1; dy++) {
+                int y = j + dy;
+                if (y < 0 || y >= n) continue;
+                for (int dx = -1; dx <= 1; dx++) {
+                    int x = ((i + dx) % m + m) % m;
+                    const mat2<double> &b = s.e[(dy + 1) * 3 + dx + 1];
+                    const int col = 2 * (y * m + x);
+                    A[(size_t)row * N + col] += b.a;
+                    A[(size_t)row * N + col + 1] += b.b;
+                    A[(size_t)(row + 1) * N + col] += b.c;
+                    A[(size_t)(row + 1) * N + col + 1] += b.d;
+                }
+            }
+        }
+    inv.assign((size_t)N * N, 0.0);
+    for (int k = 0; k < N; k++) inv[(size_t)k * N + k] = 1;
+    for (int c = 0; c < N; c++) {
+        int piv = c;
+        for (int r = c + 1; r < N; r++)
+            if (std::fabs(A[(size_t)r * N + c]) > std::fabs(A[(size_t)piv * N + c])) piv = r;
+        if (A[(size_t)piv * N + c] == 0) return std::vector<double>();
+        if (piv != c)
+            for (int k = 0; k < N; k++) {
+                std::swap(A[(size_t)piv * N + k], A[(size_t)c * N + k]);
+                std::swap(inv[(size_t)piv * N + k], inv[(size_t)c * N + k]);
+            }
+        const double d = 1.0 / A[(size_t)c * N + c];
+        for (int k = 0; k < N; k++) {
+            A[(size_t)c * N + k] *= d;
+            inv[(size_t)c * N + k] *= d;
+        }
+        for (int r = 0; r < N; r++) {
+            if (r == c) continue;
+            const double f = A[(size_t)r * N + c];
+            if (f == 0) continue;
+            for (int k = 0; k < N; k++) {
+                A[(size_t)r * N + k] -= f * A[(size_t)c * N + k];
+                inv[(size_t)r * N + k] -= f * inv[(size_t)c * N + k];
+            }
+        }
+    }
+    return inv;
+}
+
+// ---------------------------------------------------------------------------
+// Device hierarchy
+
+template <typename T> int hierarchy<T>::allocate(int m, int n, V *top_z, V *top_b) {
+    release();
+    std::vector<std::pair<int, int>> sz = coarse_sizes(m, n);
+    nl = 1 + (int)sz.size();
+    for (int l = 0; l < nl; l++) {
+        level_view<T> &L = lv[l];
+        std::memset(&L, 0, sizeof(L));
+        L.m = l == 0 ? m : sz[l - 1].first;
+        L.n = l == 0 ? n : sz[l - 1].second;
+        L.colors_x = (L.m & 1) ? 3 : 2;
+        size_t cnt = (size_t)L.m * L.n;
+        V *p[3] = {nullptr, nullptr, nullptr};
+        for (int k = 0; k < 3; k++) {
+            if (l == 0 && k == 0 && top_z) { p[k] = top_z; continue; }
+            if (l == 0 && k == 1 && top_b) { p[k] = top_b; continue; }
+            cudaError_t e = cudaMalloc((void **)&p[k], cnt * sizeof(V));
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(level)");
+            cudaMemset(p[k], 0, cnt * sizeof(V));
+            owned_.push_back(p[k]);
+            bytes_ += cnt * sizeof(V);
+        }
+        L.z = p[0];
+        L.b = p[1];
+        L.r = p[2];
+    }
+    return STZG_OK;
+}
+
+template <typename T> int hierarchy<T>::upload_ops(const std::vector<level_ops> &ops, const top_op<double> &o) {
+    op.Kmx = (T)o.Kmx; op.Kmy = (T)o.Kmy; op.mx = (T)o.mx; op.my = (T)o.my; op.qK = (T)o.qK;
+    op.cxx = (T)o.cxx; op.cyy = (T)o.cyy; op.icxx = (T)o.icxx; op.icyy = (T)o.icyy;
+    op.bcxx = (T)o.bcxx; op.bcyy = (T)o.bcyy; op.ibcxx = (T)o.ibcxx; op.ibcyy = (T)o.ibcyy;
+    if ((int)ops.size() != nl - 1) return fail(STZG_EINVAL, "hierarchy/operator level mismatch");
+    for (int l = 1; l < nl; l++) {
+        const level_ops &L = ops[l - 1];
+        level_view<T> &D = lv[l];
+        D.homog = L.homog ? 1 : 0;
+        std::vector<stencil9<T>> tab(L.table.size());
+        for (size_t k = 0; k < L.table.size(); k++)
+            for (int e = 0; e < 10; e++) {
+                tab[k].e[e].a = (T)L.table[k].e[e].a; tab[k].e[e].b = (T)L.table[k].e[e].b;
+                tab[k].e[e].c = (T)L.table[k].e[e].c; tab[k].e[e].d = (T)L.table[k].e[e].d;
+            }
+        STZG_CHECK(grow(l, tab.size(), L.cls.size()));
+        STZG_CUDA(cudaMemcpy((void *)D.st, tab.data(), sizeof(stencil9<T>) * tab.size(), cudaMemcpyHostToDevice));
+        STZG_CUDA(cudaMemcpy((void *)D.cls, L.cls.data(), sizeof(int) * L.cls.size(), cudaMemcpyHostToDevice));
+    }
+    bottom_inv = nullptr;
+    bottom_unknowns = 0;
+    if (nl > 1) {
+        std::vector<double> inv = coarsest_inverse(ops.back());
+        if (!inv.empty()) {
+            if (inv.size() > inv_cap_) {
+                void *p;
+                cudaError_t e = cudaMalloc(&p, sizeof(double) * inv.size());
+                if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(coarsest inverse)");
+                owned_.push_back(p);
+                bytes_ += sizeof(double) * inv.size();
+                inv_dev_ = (double *)p;
+                inv_cap_ = inv.size();
+            }
+            STZG_CUDA(cudaMemcpy(inv_dev_, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice));
+            bottom_inv = inv_dev_;
+            bottom_unknowns = 2 * ops.back().m * ops.back().n;
+        }
+    }
+    return STZG_OK;
+}
+
+template <typename T> int hierarchy<T>::grow(int l, size_t st_need, size_t cls_need) {
+    level_view<T> &D = lv[l];
+    if (st_need > st_cap_[l]) {
+        void *p;
+        cudaError_t e = cudaMalloc(&p, sizeof(stencil9<T>) * st_need);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(stencils)");
+        owned_.push_back(p);
+        bytes_ += sizeof(stencil9<T>) * st_need;
+        D.st = (const stencil9<T> *)p;
+        st_cap_[l] = st_need;
+    }
+    if (cls_need > cls_cap_[l]) {
+        void *p;
+        cudaError_t e = cudaMalloc(&p, sizeof(int) * cls_need);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(classes)");
+        owned_.push_back(p);
+        bytes_ += sizeof(int) * cls_need;
+        D.cls = (const int *)p;
+        cls_cap_[l] = cls_need;
+    }
+    return STZG_OK;
+}
+
+template <typename T> void hierarchy<T>::release() {
+    for (int l = 0; l < 17; l++) st_cap_[l] = cls_cap_[l] = 0;
+    inv_cap_ = 0;
+    inv_dev_ = nullptr;
+    bottom_inv = nullptr;
+    for (void *p : owned_) cudaFree(p);
+    owned_.clear();
+    bytes_ = 0;
+    nl = 0;
+}
+
+template class hierarchy<double>;
+template class hierarchy<float>;
+
+// ---------------------------------------------------------------------------
+// Kernels
+
+namespace {
+
+template <typename V, typename T> __device__ inline void madd(V &acc, const mat2<T> &A, const V &z) {
+    acc.x += A.a * z.x + A.b * z.y;
+    acc.y += A.c * z.x + A.d * z.y;
+}
+
+// One colour of the top-level Gauss-Seidel sweep.  Colour c updates the x
+// component where (i+j)&1 == c and the y component elsewhere.
+template <typename T>
+__global__ void k_top_color(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
+                            const typename vec2_t<T>::type *__restrict__ b, int m, int n, int color) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const size_t ij = (size_t)j * m + i;
+    const bool xc = ((i + j) & 1) == color;
+    if (j == 0 || j == n - 1) {  // Dirichlet wall rows: z = regcbi*b
+        if (xc) z[ij].x = op.ibcxx * b[ij].x;
+        else z[ij].y = op.ibcyy * b[ij].y;
+        return;
+    }
+    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+    const typename vec2_t<T>::type *zd = z + (size_t)(j - 1) * m, *zc = z + (size_t)j * m,
+                                   *zu = z + (size_t)(j + 1) * m;
+    if (xc) {
+        T a = op.Kmx * (zc[il].x + zc[ir].x) + op.my * (zd[i].x + zu[i].x) +
+              op.qK * (zd[il].y + zu[ir].y - zd[ir].y - zu[il].y);
+        z[ij].x = op.icxx * (b[ij].x - a);
+    } else {
+        T a = op.mx * (zc[il].y + zc[ir].y) + op.Kmy * (zd[i].y + zu[i].y) +
+              op.qK * (zd[il].x + zu[ir].x - zd[ir].x - zu[il].x);
+        z[ij].y = op.icyy * (b[ij].y - a);
+    }
+}
+
+// Residual of the top level: r = b - A z (qs_multi::mul_a + a_cc).
+template <typename T, typename V>
+__device__ inline V top_res(const top_op<T> &op, const V *__restrict__ z, const V *__restrict__ b, int m, int n,
+                            int i, int j) {
+    const size_t ij = (size_t)j * m + i;
+    V r;
+    if (j == 0 || j == n - 1) {
+        r.x = b[ij].x - op.bcxx * z[ij].x;
+        r.y = b[ij].y - op.bcyy * z[ij].y;
+        return r;
+    }
+    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+    const V *zd = z + (size_t)(j - 1) * m, *zc = z + (size_t)j * m, *zu = z + (size_t)(j + 1) * m;
+    T ax = op.Kmx * (zc[il].x + zc[ir].x) + op.my * (zd[i].x + zu[i].x) +
+           op.qK * (zd[il].y + zu[ir].y - zd[ir].y - zu[il].y);
+    T ay = op.mx * (zc[il].y + zc[ir].y) + op.Kmy * (zd[i].y + zu[i].y) +
+           op.qK * (zd[il].x + zu[ir].x - zd[ir].x - zu[il].x);
+    r.x = b[ij].x - ax - op.cxx * zc[i].x;
+    r.y = b[ij].y - ay - op.cyy * zc[i].y;
+    return r;
+}
+
+template <typename T>
+__global__ void k_top_residual(top_op<T> op, const typename vec2_t<T>::type *__restrict__ z,
+                               const typename vec2_t<T>::type *__restrict__ b,
+                               typename vec2_t<T>::type *__restrict__ r, int m, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    r[(size_t)j * m + i] = top_res<T>(op, z, b, m, n, i, j);
+}
+
+template <typename T>
+__device__ inline const stencil9<T> &stencil_at(const level_view<T> &L, int i, int j) {
+    int c = L.homog ? L.cls[j] : L.cls[(size_t)j * L.m + i];
+    return L.st[c];
+}
+
+// Off-diagonal product of a coarse level (tgmg_level::mul_a, tgmg.in.cc:536-547)
+template <typename T, typename V>
+__device__ inline V lev_offdiag(const level_view<T> &L, const stencil9<T> &s, const V *__restrict__ z, int i, int j) {
+    const int m = L.m, n = L.n;
+    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+    V acc;
+    acc.x = 0;
+    acc.y = 0;
+    if (j > 0) {
+        const V *zd = z + (size_t)(j - 1) * m;
+        madd(acc, s.e[0], zd[il]); madd(acc, s.e[1], zd[i]); madd(acc, s.e[2], zd[ir]);
+    }
+    const V *zc = z + (size_t)j * m;
+    madd(acc, s.e[3], zc[il]); madd(acc, s.e[5], zc[ir]);
+    if (j < n - 1) {
+        const V *zu = z + (size_t)(j + 1) * m;
+        madd(acc, s.e[6], zu[il]); madd(acc, s.e[7], zu[i]); madd(acc, s.e[8], zu[ir]);
+    }
+    return acc;
+}
+
+template <typename T>
+__device__ inline int color_of(const level_view<T> &L, int i, int j) {
+    int cx = (L.colors_x == 3 && i == L.m - 1) ? 2 : (i & 1);
+    return (j & 1) * L.colors_x + cx;
+}
+
+// One colour (cx, cy) of a coarse-level sweep; thread (ti, tj) owns point
+// (2 ti + cx, 2 tj + cy), or the last column for the third colour of an odd
+// periodic line.
+template <typename T> __global__ void k_lev_color(level_view<T> L, int cx, int cy) {
+    typedef typename vec2_t<T>::type V;
+    const int ti = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 2 * (blockIdx.y * blockDim.y + threadIdx.y) + cy;
+    if (j >= L.n) return;
+    int i;
+    if (cx == 2) {
+        if (ti > 0) return;
+        i = L.m - 1;
+    } else {
+        i = 2 * ti + cx;
+        if (i >= L.m || (L.colors_x == 3 && i == L.m - 1)) return;
+    }
+    const stencil9<T> &s = stencil_at(L, i, j);
+    const size_t ij = (size_t)j * L.m + i;
+    V a = lev_offdiag<T, V>(L, s, L.z, i, j);
+    V r, out;
+    r.x = L.b[ij].x - a.x;
+    r.y = L.b[ij].y - a.y;
+    out.x = s.e[9].a * r.x + s.e[9].b * r.y;
+    out.y = s.e[9].c * r.x + s.e[9].d * r.y;
+    L.z[ij] = out;
+}
+
+template <typename T> __global__ void k_lev_residual(level_view<T> L) {
+    typedef typename vec2_t<T>::type V;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= L.m || j >= L.n) return;
+    const stencil9<T> &s = stencil_at(L, i, j);
+    const size_t ij = (size_t)j * L.m + i;
+    V a = lev_offdiag<T, V>(L, s, L.z, i, j);
+    madd(a, s.e[4], L.z[ij]);
+    V r;
+    r.x = L.b[ij].x - a.x;
+    r.y = L.b[ij].y - a.y;
+    L.r[ij] = r;
+}
+
+// Full-weighting restriction b_c = P^T r_f (apply_r, tgmg.in.cc:626-647):
+// every coarse point gathers its fine support (within +-1 of 2I, 2J).
+template <typename T>
+__global__ void k_restrict(const typename vec2_t<T>::type *__restrict__ r, int fm, int fn,
+                           typename vec2_t<T>::type *__restrict__ bc, int cm, int cn) {
+    typedef typename vec2_t<T>::type V;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    if (I >= cm || J >= cn) return;
+    T ax = 0, ay = 0;
+    for (int dy = -1; dy <= 1; dy++) {
+        int fy = 2 * J + dy;
+        if (fy < 0 || fy >= fn) continue;
+        T wy = (T)pw(fy, fn, 0, J);
+        if (wy == 0) continue;
+        for (int dx = -1; dx <= 1; dx++) {
+            int fx = 2 * I + dx;
+            fx = fx < 0 ? fx + fm : (fx >= fm ? fx - fm : fx);
+            T wx = (T)pw(fx, fm, 1, I);
+            if (wx == 0) continue;
+            V v = r[(size_t)fy * fm + fx];
+            ax += wx * wy * v.x;
+            ay += wx * wy * v.y;
+        }
+    }
+    V o;
+    o.x = ax;
+    o.y = ay;
+    bc[(size_t)J * cm + I] = o;
+}
+
+// Bilinear prolongation added to the fine z (apply_t, tgmg.in.cc:552-621).
+template <typename T>
+__global__ void k_prolong_add(const typename vec2_t<T>::type *__restrict__ zc, int cm, int cn,
+                              typename vec2_t<T>::type *__restrict__ zf, int fm, int fn) {
+    typedef typename vec2_t<T>::type V;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= fm || j >= fn) return;
+    int cy[2], cx[2];
+    double wy[2], wx[2];
+    int ny = p1d(j, fn, 0, cy, wy), nx = p1d(i, fm, 1, cx, wx);
+    T ax = 0, ay = 0;
+    for (int b = 0; b < ny; b++)
+        for (int a = 0; a < nx; a++) {
+            T w = (T)(wx[a] * wy[b]);
+            V v = zc[(size_t)cy[b] * cm + cx[a]];
+            ax += w * v.x;
+            ay += w * v.y;
+        }
+    V &f = zf[(size_t)j * fm + i];
+    f.x += ax;
+    f.y += ay;
+}
+
+// Bottom level: `down` sweeps from zero then `up` sweeps (v_cycle_internal,
+// tgmg.in.cc:350-352), one block, arithmetic in TC.
+template <typename T, typename TC> __global__ void k_bottom(level_view<T> L, int down, int up) {
+    typedef typename vec2_t<T>::type V;
+    const int mn = L.m * L.n;
+    const int ncol = 2 * L.colors_x;
+    for (int k = threadIdx.x; k < mn; k += blockDim.x) {
+        L.z[k].x = 0;
+        L.z[k].y = 0;
+    }
+    __syncthreads();
+    for (int sweep = 0; sweep < down + up; sweep++) {
+        for (int c = 0; c < ncol; c++) {
+            for (int k = threadIdx.x; k < mn; k += blockDim.x) {
+                int i = k % L.m, j = k / L.m;
+                if (color_of(L, i, j) != c) continue;
+                const stencil9<T> &s = stencil_at(L, i, j);
+                const int il = i == 0 ? L.m - 1 : i - 1, ir = i == L.m - 1 ? 0 : i + 1;
+                TC ax = 0, ay = 0;
+                const int nb[9][2] = {{il, j - 1}, {i, j - 1}, {ir, j - 1}, {il, j}, {i, j}, {ir, j},
+                                      {il, j + 1}, {i, j + 1}, {ir, j + 1}};
+                for (int e = 0; e < 9; e++) {
+                    if (e == 4) continue;
+                    int y = nb[e][1];
+                    if (y < 0 || y >= L.n) continue;
+                    V zz = L.z[(size_t)y * L.m + nb[e][0]];
+                    ax += (TC)s.e[e].a * (TC)zz.x + (TC)s.e[e].b * (TC)zz.y;
+                    ay += (TC)s.e[e].c * (TC)zz.x + (TC)s.e[e].d * (TC)zz.y;
+                }
+                TC rx = (TC)L.b[k].x - ax, ry = (TC)L.b[k].y - ay;
+                V o;
+                o.x = (T)((TC)s.e[9].a * rx + (TC)s.e[9].b * ry);
+                o.y = (T)((TC)s.e[9].c * rx + (TC)s.e[9].d * ry);
+                L.z[k] = o;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Exact coarsest solve z = A^-1 b (FP64 arithmetic, any storage precision).
+template <typename T> __global__ void k_bottom_direct(level_view<T> L, const double *__restrict__ inv, int N) {
+    typedef typename vec2_t<T>::type V;
+    extern __shared__ double bsh[];
+    for (int k = threadIdx.x; k < N / 2; k += blockDim.x) {
+        V b = L.b[k];
+        bsh[2 * k] = (double)b.x;
+        bsh[2 * k + 1] = (double)b.y;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < N; r += blockDim.x) {
+        const double *row = inv + (size_t)r * N;
+        double a = 0;
+        for (int k = 0; k < N; k++) a += row[k] * bsh[k];
+        T *zz = (T *)L.z;
+        zz[r] = (T)a;
+    }
+}
+
+// Deterministic block reduction of a double (warp shuffles, fixed order).
+__device__ inline double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    __syncthreads();
+    return t;
+}
+
+constexpr int kRedThreads = 256;
+
+template <typename T>
+__global__ void k_top_sqnorm(top_op<T> op, const typename vec2_t<T>::type *__restrict__ z,
+                             const typename vec2_t<T>::type *__restrict__ b, int m, int n, double *partials) {
+    typedef typename vec2_t<T>::type V;
+    __shared__ double sh[32];
+    const long total = (long)m * n;
+    double sr = 0, sb = 0;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (long)gridDim.x * blockDim.x) {
+        int i = (int)(k % m), j = (int)(k / m);
+        V r = top_res<T>(op, z, b, m, n, i, j);
+        sr += (double)r.x * r.x + (double)r.y * r.y;
+        V bb = b[k];
+        sb += (double)bb.x * bb.x + (double)bb.y * bb.y;
+    }
+    double a = block_sum(sr, sh);
+    double c = block_sum(sb, sh);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = a;
+        partials[2 * blockIdx.x + 1] = c;
+    }
+}
+
+// Sums the per-block partials with one block in a fixed order.
+__global__ void k_final_sum(const double *partials, int npart, double *out, double *out_b) {
+    __shared__ double sh[32];
+    double a = 0, c = 0;
+    for (int k = threadIdx.x; k < npart; k += blockDim.x) {
+        a += partials[2 * k];
+        c += partials[2 * k + 1];
+    }
+    a = block_sum(a, sh);
+    c = block_sum(c, sh);
+    if (threadIdx.x == 0) {
+        *out = a;
+        if (out_b) *out_b = c;
+    }
+}
+
+__global__ void k_mixed_residual(top_op<double> op, const double2 *__restrict__ z, const double2 *__restrict__ b,
+                                 int m, int n, float2 *__restrict__ r32, double *partials) {
+    __shared__ double sh[32];
+    const long total = (long)m * n;
+    double sr = 0, sb = 0;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (long)gridDim.x * blockDim.x) {
+        int i = (int)(k % m), j = (int)(k / m);
+        double2 r = top_res<double>(op, z, b, m, n, i, j);
+        r32[k] = make_float2((float)r.x, (float)r.y);
+        sr += r.x * r.x + r.y * r.y;
+        double2 bb = b[k];
+        sb += bb.x * bb.x + bb.y * bb.y;
+    }
+    double a = block_sum(sr, sh);
+    double c = block_sum(sb, sh);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = a;
+        partials[2 * blockIdx.x + 1] = c;
+    }
+}
+
+__global__ void k_mixed_correct(double2 *__restrict__ z, const float2 *__restrict__ e, long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        float2 d = e[k];
+        double2 v = z[k];
+        v.x += (double)d.x;
+        v.y += (double)d.y;
+        z[k] = v;
+    }
+}
+
+__global__ void k_extrapolate(double2 *__restrict__ z, double2 *__restrict__ prev, long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        double2 a = z[k], p = prev[k];
+        prev[k] = a;
+        z[k] = make_double2(2 * a.x - p.x, 2 * a.y - p.y);
+    }
+}
+
+inline dim3 grid2(int m, int n, dim3 blk) { return dim3(ceil_div(m, blk.x), ceil_div(n, blk.y)); }
+
+}  // namespace
+
+int reduction_blocks() { return 4 * 152; }
+
+template <typename T> void top_sweep(hierarchy<T> &h, cudaStream_t st) {
+    level_view<T> &L = h.lv[0];
+    dim3 blk(32, 8);
+    for (int c = 0; c < 2; c++) {
+        k_top_color<T><<<grid2(L.m, L.n, blk), blk, 0, st>>>(h.op, L.z, L.b, L.m, L.n, c);
+        note_launch();
+    }
+}
+
+template <typename T> static void lev_sweep(level_view<T> &L, cudaStream_t st) {
+    dim3 blk(32, 8);
+    dim3 g(ceil_div((L.m + 1) / 2, blk.x), ceil_div((L.n + 1) / 2, blk.y));
+    for (int cy = 0; cy < 2; cy++)
+        for (int cx = 0; cx < L.colors_x; cx++) {
+            k_lev_color<T><<<g, blk, 0, st>>>(L, cx, cy);
+            note_launch();
+        }
+}
+
+template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64) {
+    dim3 blk(32, 8);
+    const int ml = h.nl - 1;
+    top_sweep(h, st);
+    if (ml > 0) {
+        level_view<T> &T0 = h.lv[0];
+        k_top_residual<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.op, T0.z, T0.b, T0.r, T0.m, T0.n); note_launch();
+        k_restrict<T><<<grid2(h.lv[1].m, h.lv[1].n, blk), blk, 0, st>>>(T0.r, T0.m, T0.n, h.lv[1].b, h.lv[1].m,
+                                                                       h.lv[1].n); note_launch();
+        for (int i = 1; i < ml; i++) {
+            level_view<T> &L = h.lv[i];
+            cudaMemsetAsync(L.z, 0, sizeof(typename vec2_t<T>::type) * (size_t)L.m * L.n, st);
+            lev_sweep(L, st);
+            k_lev_residual<T><<<grid2(L.m, L.n, blk), blk, 0, st>>>(L); note_launch();
+            level_view<T> &C = h.lv[i + 1];
+            k_restrict<T><<<grid2(C.m, C.n, blk), blk, 0, st>>>(L.r, L.m, L.n, C.b, C.m, C.n); note_launch();
+        }
+        level_view<T> &B = h.lv[ml];
+        if (h.bottom_inv)
+            k_bottom_direct<T><<<1, 256, sizeof(double) * h.bottom_unknowns, st>>>(B, h.bottom_inv,
+                                                                                  h.bottom_unknowns);
+        else if (bottom_fp64)
+            k_bottom<T, double><<<1, 256, 0, st>>>(B, bottom_sweeps, bottom_sweeps);
+        else
+            k_bottom<T, T><<<1, 256, 0, st>>>(B, bottom_sweeps, bottom_sweeps);
+        note_launch();
+        for (int i = ml; i >= 1; i--) {
+            level_view<T> &C = h.lv[i], &F = h.lv[i - 1];
+            k_prolong_add<T><<<grid2(F.m, F.n, blk), blk, 0, st>>>(C.z, C.m, C.n, F.z, F.m, F.n); note_launch();
+            if (i > 1) lev_sweep(F, st);
+        }
+    }
+    top_sweep(h, st);
+}
+
+template <typename T>
+void top_residual_sqnorm(hierarchy<T> &h, double *partials, int npart, double *out, double *out_b,
+                         cudaStream_t st) {
+    level_view<T> &L = h.lv[0];
+    k_top_sqnorm<T><<<npart, kRedThreads, 0, st>>>(h.op, L.z, L.b, L.m, L.n, partials); note_launch();
+    k_final_sum<<<1, 256, 0, st>>>(partials, npart, out, out_b); note_launch();
+}
+
+void mixed_residual(const top_op<double> &op64, const double2 *z64, const double2 *b64, int m, int n, float2 *r32,
+                    double *partials, int npart, double *out, double *out_b, cudaStream_t st) {
+    k_mixed_residual<<<npart, kRedThreads, 0, st>>>(op64, z64, b64, m, n, r32, partials); note_launch();
+    k_final_sum<<<1, 256, 0, st>>>(partials, npart, out, out_b); note_launch();
+}
+
+void mixed_correct(double2 *z64, const float2 *e32, long count, cudaStream_t st) {
+    k_mixed_correct<<<4 * 152, 256, 0, st>>>(z64, e32, count); note_launch();
+}
+
+void extrapolate_guess(double2 *z, double2 *prev, long count, cudaStream_t st) {
+    k_extrapolate<<<4 * 152, 256, 0, st>>>(z, prev, count); note_launch();
+}
+
+template void vcycle<double>(hierarchy<double> &, cudaStream_t, int, int);
+template void vcycle<float>(hierarchy<float> &, cudaStream_t, int, int);
+template void top_sweep<double>(hierarchy<double> &, cudaStream_t);
+template void top_sweep<float>(hierarchy<float> &, cudaStream_t);
+template void top_residual_sqnorm<double>(hierarchy<double> &, double *, int, double *, double *, cudaStream_t);
+template void top_residual_sqnorm<float>(hierarchy<float> &, double *, int, double *, double *, cudaStream_t);
+
+}  // namespace stzg

@@ -1,0 +1,375 @@
+// Time-step kernels: fused ENO advection + STZ plasticity, chi diffusion,
+// projection source, stress correction and boundaries.
+#include "step.cuh"
+
+namespace stzg {
+
+step_consts make_step_consts(const stz_params &p) {
+    step_consts c;
+    c.m = p.m;
+    c.n = p.n;
+    c.ax = p.ax;
+    c.ay = p.ay;
+    c.by = p.by;
+    c.lx = p.bx - p.ax;
+    c.dx = c.lx / p.m;
+    c.dy = (p.by - p.ay) / p.n;
+    c.xsp = 1. / c.dx;
+    c.ysp = 1. / c.dy;
+    c.mu = p.mu;
+    c.K = p.K;
+    c.stz_model = p.stz_model;
+    c.t_model = p.t_model;
+    c.t_scale = p.t_scale;
+    c.adapt_fac = p.adapt_fac;
+    c.chi_inf = p.chi_inf;
+    c.s_y = p.s_y;
+    c.theta = p.theta;
+    c.Delta = p.Delta;
+    c.Omegaeps0 = p.Omegaeps0;
+    c.tau0 = p.tau0;
+    c.c0 = p.c0;
+    c.kappa = p.kappa;
+    c.rho = p.rho;
+    c.chi_diff = p.chi_diff;
+    c.chi_len = p.chi_len;
+    c.track_plastic = 0;
+    c.substep_cap = 1 << 22;
+    return c;
+}
+
+namespace {
+
+__device__ __forceinline__ double eno2(double p0, double p1, double p2, double p3) {
+    // shear_sim::eno2, shear_sim.cc:653-655
+    return fabs(p0 - 2 * p1 + p2) > fabs(p1 - 2 * p2 + p3) ? 3 * p1 - 4 * p2 + p3 : p0 - p2;
+}
+
+// STZ plastic rate (stz_model.hh:9-207) with the yield stress s_y in place
+// of the reference's unit s0 and `sbar<1`.
+__device__ double dplastic(const step_consts &c, double sbar, double chi, double &dchi1, double &dchi2) {
+    const double s0 = c.s_y, thetainv = 1 / c.theta;
+    const double Om = c.Omegaeps0, De = c.Delta, tau0 = c.tau0;
+    if (c.stz_model == 0 || c.stz_model == 1) {
+        double sC1, sC2, sC, sT;
+        if (c.stz_model == 0) {  // stz_model.hh:58-67
+            sC1 = exp(-De * thetainv);
+            sC2 = cosh(Om * sbar * thetainv);
+            sC = sC1 * sC2;
+            sT = tanh(Om * sbar * thetainv);
+        } else {  // stz_model.hh:76-87
+            double x = Om * sbar / De;
+            sC1 = exp(-De * thetainv);
+            sC = exp(-De * cosh(x) * thetainv) * cosh(De * sinh(x) * thetainv);
+            sC2 = sC / sC1;
+            sT = tanh(De * sinh(x) * thetainv);
+        }
+        // Dplastic_common, stz_model.hh:30-48
+        double sbart = sbar > 1e-12 ? sbar : 1e-12, bfac = exp(-1 / chi);
+        double pM = 1 + sbart * sT / s0 + c.rho / (2 * sC2);
+        double M = s0 / (2 * sbart) * (pM - sqrt(pM * pM - 4 * sbart * sT / s0));
+        double Dpl = bfac * sC * (sT - M) / tau0;
+        double Gamma = 2 * tau0 * Dpl * sbar / (s0 * bfac);
+        bfac /= tau0 * c.c0;
+        dchi1 = bfac * Gamma;
+        dchi2 = bfac * c.kappa * sC1 * c.rho;
+        return Dpl;
+    }
+    dchi2 = 0;
+    if (sbar < s0) {
+        dchi1 = 0;
+        return 0;
+    }
+    double sC, sT;
+    if (c.stz_model == 3) {  // stz_model.hh:179-206
+        double x = Om * sbar / De;
+        sC = 0.5 * (exp(-De * thetainv * exp(x)) + exp(-De * thetainv * exp(-x)));
+        sT = tanh(De * sinh(x) * thetainv);
+    } else {  // stz_model.hh:103-151
+        const int tm = c.t_model;
+        if (tm == -1 || De >= Om * sbar) {
+            sC = 0.5 * (exp((Om * sbar - De) * thetainv) + exp((-Om * sbar - De) * thetainv));
+        } else {
+            double tmp;
+            switch (tm) {
+                case 0: sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + 1); break;
+                case 1: tmp = Om * sbar / De;
+                        sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + sqrt(0.5 * (1 + tmp * tmp))); break;
+                case 2: tmp = Om * sbar / De;
+                        sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + (0.5 * (1 + tmp * tmp))); break;
+                case 3: sC = sbar * (0.5 * Om / De); break;  // t_icpt=0, t_grad=Omegaeps0/(2 Delta)
+                case 4: sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + (Om * sbar - De) * thetainv + 1); break;
+                default: sC = 0;
+            }
+        }
+        sT = tm != 3 ? tanh(Om * sbar * thetainv) : 1;
+    }
+    double bfac = exp(-1 / chi);
+    double Dpl = bfac * sC * (sT - s0 / sbar) / tau0;
+    double Gamma = 2 * tau0 * Dpl * sbar / (s0 * bfac);
+    dchi1 = bfac * Gamma / (tau0 * c.c0);
+    return Dpl;
+}
+
+// shear_sim::adaptive_plastic_term, shear_sim.cc:513-548, with an iteration
+// cap (the reference loop has none and never ends in stiff regimes).
+__device__ double adaptive_plastic(const step_consts &c, double sbar, double &chiv, double &ddev, double dt,
+                                   int &iters) {
+    const double theta_loc = 0;
+    iters = 0;
+    if (sbar < 1e-12) {
+        ddev = 0;
+        return 0;
+    }
+    double dtl = dt, osbar = sbar, dplas, dchi1, dchi2, adt;
+    bool adapt = true;
+    do {
+        dplas = 2 * c.t_scale * c.mu * dplastic(c, sbar, chiv, dchi1, dchi2);
+        if (fabs(dtl * dplas) > c.adapt_fac) {
+            adt = c.adapt_fac / fabs(dplas);
+            dtl -= adt;
+        } else {
+            adapt = false;
+            adt = dtl;
+        }
+        sbar -= adt * dplas;
+        chiv += (dchi1 * (c.chi_inf - chiv) + dchi2 * (theta_loc - chiv)) * c.t_scale * adt;
+        if (++iters >= c.substep_cap) break;
+    } while (adapt);
+    ddev = osbar - sbar;
+    return ddev == 0 ? 0.0 : ddev / osbar;
+}
+
+struct velo {
+    const double2 *vel;
+    int m, n;
+    double bv;
+    __device__ __forceinline__ double u(int i, int j) const {
+        return j == 0 ? -bv : (j == n ? bv : vel[(size_t)j * m + i].x);
+    }
+    __device__ __forceinline__ double v(int i, int j) const {
+        return (j == 0 || j == n) ? 0.0 : vel[(size_t)j * m + i].y;
+    }
+};
+
+#define IDX(i, j) ((size_t)((j) + 1) * m + (i))
+
+// Fused advection + STZ step per cell (i,j) and its lower-left node.
+__global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int cur, double dt, double bv,
+                                                int chi_only_pre) {
+    const int m = c.m, n = c.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const double *__restrict__ const *A = F.f[cur];
+    double *const *B = F.f[cur ^ 1];
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt, lx = c.lx;
+    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+    const int il2 = i <= 1 ? i + m - 2 : i - 2, ir2 = i >= m - 2 ? i + 2 - m : i + 2;
+    const size_t ci = IDX(i, j);
+    velo V{F.vel, m, n, bv};
+    double uc, vc;
+    // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
+    if (j > 0) {
+        const double *X = A[F_X], *Y = A[F_Y];
+        double Xx, Xy, Yx, Yy;
+        uc = V.u(i, j);
+        vc = V.v(i, j);
+        if (uc > 0) {
+            Xx = hx * eno2(X[IDX(ir, j)] + (i == m - 1 ? lx : 0), X[ci], X[IDX(il, j)] + (i == 0 ? -lx : 0),
+                           X[IDX(il2, j)] + (i <= 1 ? -lx : 0));
+            Yx = hx * eno2(Y[IDX(ir, j)], Y[ci], Y[IDX(il, j)], Y[IDX(il2, j)]);
+        } else {
+            Xx = -hx * eno2(X[IDX(il, j)] + (i == 0 ? -lx : 0), X[ci], X[IDX(ir, j)] + (i == m - 1 ? lx : 0),
+                            X[IDX(ir2, j)] + (i >= m - 2 ? lx : 0));
+            Yx = -hx * eno2(Y[IDX(il, j)], Y[ci], Y[IDX(ir, j)], Y[IDX(ir2, j)]);
+        }
+        if (vc > 0) {
+            if (j > 1) {
+                Xy = hy * eno2(X[IDX(i, j + 1)], X[ci], X[IDX(i, j - 1)], X[IDX(i, j - 2)]);
+                Yy = hy * eno2(Y[IDX(i, j + 1)], Y[ci], Y[IDX(i, j - 1)], Y[IDX(i, j - 2)]);
+            } else {
+                Xy = 2 * hy * (X[ci] - X[IDX(i, j - 1)]);
+                Yy = 2 * hy * (Y[ci] - Y[IDX(i, j - 1)]);
+            }
+        } else {
+            if (j < n - 1) {
+                Xy = -hy * eno2(X[IDX(i, j - 1)], X[ci], X[IDX(i, j + 1)], X[IDX(i, j + 2)]);
+                Yy = -hy * eno2(Y[IDX(i, j - 1)], Y[ci], Y[IDX(i, j + 1)], Y[IDX(i, j + 2)]);
+            } else {
+                Xy = 2 * -hy * (X[ci] - X[IDX(i, j + 1)]);
+                Yy = 2 * -hy * (Y[ci] - Y[IDX(i, j + 1)]);
+            }
+        }
+        B[F_X][ci] = X[ci] + (-uc * Xx - vc * Xy);
+        B[F_Y][ci] = Y[ci] + (-uc * Yx - vc * Yy);
+    }
+    // staggered velocity and spin (shear_sim.cc:330-333)
+    const double u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
+    const double v00 = V.v(i, j), v10 = V.v(ir, j), v01 = V.v(i, j + 1), v11 = V.v(ir, j + 1);
+    uc = 0.25 * (u00 + u10 + u01 + u11);
+    vc = 0.25 * (v00 + v10 + v01 + v11);
+    const double two_omega = hx * (-v00 + v10 - v01 + v11) - hy * (-u00 - u10 + u01 + u11);
+    // ENO derivatives of p, q, s, tau, chi (shear_sim.cc:336-338)
+    double f1[5], f2[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const double *G = A[k];
+        if (uc > 0) f1[k] = hx * eno2(G[IDX(ir, j)], G[ci], G[IDX(il, j)], G[IDX(il2, j)]);
+        else f1[k] = -hx * eno2(G[IDX(il, j)], G[ci], G[IDX(ir, j)], G[IDX(ir2, j)]);
+        if (vc > 0) {
+            if (j > 0) f2[k] = hy * eno2(G[IDX(i, j + 1)], G[ci], G[IDX(i, j - 1)], G[IDX(i, j - 2)]);
+            else f2[k] = 2 * hy * (G[ci] - G[IDX(i, j - 1)]);
+        } else {
+            if (j < n - 1) f2[k] = -hy * eno2(G[IDX(i, j - 1)], G[ci], G[IDX(i, j + 1)], G[IDX(i, j + 2)]);
+            else f2[k] = 2 * -hy * (G[ci] - G[IDX(i, j + 1)]);
+        }
+    }
+    const double p = A[F_P][ci], q = A[F_Q][ci], s = A[F_S][ci], t = A[F_TAU][ci];
+    double cchi = A[F_CHI][ci] - uc * f1[4] - vc * f2[4], ddev, dtmp;
+    const double devsq = 3 * q * q + s * s + t * t;
+    // Cells far enough below the cut-offs return exactly ddev = 0 and leave
+    // chi unchanged in the reference loop (sbar < 1e-12, or an athermal law
+    // below yield); they skip the FP64 square root and the loop.  The margin
+    // keeps the test exact under the rounding of sqrt.
+    const bool athermal = c.stz_model >= 2;
+    if (devsq < 0.999e-24 || (athermal && devsq < c.s_y * c.s_y * (1 - 1e-12))) {
+        ddev = 0;
+        dtmp = 0;
+    } else {
+        int iters;
+        dtmp = adaptive_plastic(c, sqrt(devsq), cchi, ddev, dt, iters);
+        if (iters >= c.substep_cap) atomicExch(&F.flags[0], 1);
+        if (iters > 1) atomicMax(&F.flags[1], iters);
+    }
+    B[F_CHI][ci] = cchi;
+    F.ddev[ci] = ddev;
+    if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
+    B[F_P][ci] = p + (-uc * f1[0] - vc * f2[0]);
+    B[F_Q][ci] = q + (-uc * f1[1] - vc * f2[1] - dtmp * q);
+    B[F_S][ci] = s + (-uc * f1[2] - vc * f2[2] + two_omega * t - dtmp * s);
+    B[F_TAU][ci] = t + (-uc * f1[3] - vc * f2[3] - two_omega * s - dtmp * t);
+    (void)chi_only_pre;
+}
+
+// chi_diffusion (shear_sim.cc:364-386): B.chi holds cchi; old chi in A.
+__global__ void k_chi_diffusion(step_consts c, fields_dev F, int cur, double dt) {
+    const int m = c.m, n = c.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
+    const double hxxcd = 2 * c.xsp * hx * c.chi_diff, hyycd = 2 * c.ysp * hy * c.chi_diff,
+                 hccd = 2 * (hxxcd + hyycd);
+    const double dfac = 0.25 * c.chi_len * c.chi_len * (1 / c.mu), dfacx = dfac * c.xsp * c.xsp,
+                 dfacy = dfac * c.ysp * c.ysp;
+    const double *ch = F.f[cur][F_CHI], *dd = F.ddev;
+    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+    const size_t k = IDX(i, j), kl = IDX(il, j), kr = IDX(ir, j), kd = IDX(i, j - 1), ku = IDX(i, j + 1);
+    const double Dd = dd[k] + dd[kd], Dl = dd[k] + dd[kl], Dr = dd[k] + dd[kr], Du = dd[k] + dd[ku];
+    F.f[cur ^ 1][F_CHI][k] += hxxcd * (ch[kr] + ch[kl]) + hyycd * (ch[ku] + ch[kd]) - hccd * ch[k] +
+                              dfacx * (Dr * ch[kr] - (Dr + Dl) * ch[k] + Dl * ch[kl]) +
+                              dfacy * (Du * ch[ku] - (Du + Dd) * ch[k] + Dd * ch[kd]);
+}
+
+// Source of the projection (shear_sim.cc:399-409): net force of the stress
+// on interior nodes, Dirichlet data on the walls.
+__global__ void k_source(step_consts c, fields_dev F, int cur, double xfac, double yfac, double xbc_bv) {
+    const int m = c.m, n = c.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j > n) return;
+    double2 f;
+    if (j == 0) {
+        f.x = -xbc_bv;
+        f.y = 0;
+    } else if (j == n) {
+        f.x = xbc_bv;
+        f.y = 0;
+    } else {
+        const double *p = F.f[cur][F_P], *q = F.f[cur][F_Q], *s = F.f[cur][F_S], *t = F.f[cur][F_TAU];
+        const int il = i == 0 ? m - 1 : i - 1;
+        const size_t k0 = IDX(il, j - 1), k1 = IDX(i, j - 1), k2 = IDX(il, j), k3 = IDX(i, j);
+        f.x = (-p[k0] + p[k1] - p[k2] + p[k3] - q[k0] + q[k1] - q[k2] + q[k3] + s[k0] - s[k1] + s[k2] - s[k3]) * xfac +
+              (t[k0] + t[k1] - t[k2] - t[k3]) * yfac;
+        f.y = (t[k0] - t[k1] + t[k2] - t[k3]) * xfac +
+              (-p[k0] - p[k1] + p[k2] + p[k3] - q[k0] - q[k1] + q[k2] + q[k3] - s[k0] - s[k1] + s[k2] + s[k3]) * yfac;
+    }
+    F.src[(size_t)j * m + i] = f;
+}
+
+// Stress correction from the solved velocity (shear_sim.cc:418-434).
+__global__ void k_project(step_consts c, fields_dev F, int cur, double hx, double hy) {
+    const int m = c.m, n = c.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const int ir = i == m - 1 ? 0 : i + 1;
+    const double2 a = F.vel[(size_t)j * m + i], b = F.vel[(size_t)j * m + ir], cu = F.vel[(size_t)(j + 1) * m + i],
+                  d = F.vel[(size_t)(j + 1) * m + ir];
+    const double ux = hx * (-a.x + b.x - cu.x + d.x), uy = hy * (-a.x - b.x + cu.x + d.x),
+                 vx = hx * (-a.y + b.y - cu.y + d.y), vy = hy * (-a.y - b.y + cu.y + d.y);
+    const size_t k = IDX(i, j);
+    double *const *S = F.f[cur];
+    const double third = 1 / 3.0;
+    S[F_P][k] += -c.K * (ux + vy);
+    S[F_Q][k] += -c.mu * third * (ux + vy);
+    S[F_S][k] += c.mu * (ux - vy);
+    S[F_TAU][k] += c.mu * (uy + vx);
+}
+
+// set_boundaries (shear_sim.cc:552-581): ghost rows by linear extrapolation,
+// wall nodes of the reference map.  Wall velocities are not stored: the
+// advection kernel takes them as arguments.
+__global__ void k_boundaries(step_consts c, fields_dev F, int cur, double bp) {
+    const int m = c.m, n = c.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    double *const *S = F.f[cur];
+    S[F_X][IDX(i, 0)] = c.ax + i * c.dx + bp;
+    S[F_Y][IDX(i, 0)] = c.ay;
+    S[F_X][IDX(i, n)] = c.ax + i * c.dx - bp;
+    S[F_Y][IDX(i, n)] = c.by;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        double *G = S[k];
+        G[IDX(i, -1)] = 2 * G[IDX(i, 0)] - G[IDX(i, 1)];
+        G[IDX(i, n)] = 2 * G[IDX(i, n - 1)] - G[IDX(i, n - 2)];
+    }
+}
+
+#undef IDX
+
+inline dim3 g2(int m, int n, dim3 b) { return dim3(ceil_div(m, b.x), ceil_div(n, b.y)); }
+
+}  // namespace
+
+void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st) {
+    dim3 blk(32, 8);
+    k_advect<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt, bv, 0); note_launch();
+    if (c.chi_diff != 0 || c.chi_len != 0) {
+        k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);
+        note_launch();
+    }
+}
+
+void projection_source(const step_consts &c, fields_dev &F, int cur, double dt, double xbc_bv, cudaStream_t st) {
+    dim3 blk(32, 8);
+    const double xfac = 0.5 / dt * c.xsp, yfac = 0.5 / dt * c.ysp;
+    k_source<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, cur, xfac, yfac, xbc_bv); note_launch();
+}
+
+void projection_apply(const step_consts &c, fields_dev &F, int cur, double dt, double bv, double bp,
+                      cudaStream_t st) {
+    dim3 blk(32, 8);
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
+    k_project<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, hx, hy); note_launch();
+    k_boundaries<<<ceil_div(c.m, 128), 128, 0, st>>>(c, F, cur, bp); note_launch();
+    (void)bv;
+}
+
+void set_boundaries(const step_consts &c, fields_dev &F, int cur, double bp, cudaStream_t st) {
+    k_boundaries<<<ceil_div(c.m, 128), 128, 0, st>>>(c, F, cur, bp); note_launch();
+}
+
+}  // namespace stzg

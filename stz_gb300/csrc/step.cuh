@@ -1,0 +1,50 @@
+// Time-step kernels of the quasi-static STZ simulation.
+#pragma once
+
+#include "common.cuh"
+
+namespace stzg {
+
+// Field storage: every per-point array holds rows -1..n of m entries
+// (ghost rows of the cell fields; node fields use rows 0..n), index
+// (j+1)*m + i.  The state is double-buffered: the advection kernel reads
+// buffer `cur` and writes buffer `cur^1`.
+enum { F_P = 0, F_Q, F_S, F_TAU, F_CHI, F_X, F_Y, F_COUNT };
+
+struct fields_dev {
+    double *f[2][F_COUNT];
+    double *ddev;    // per-step stress drop osbar-sbar (fields.hh:27)
+    double *eps_pl;  // accumulated plastic strain (cells, m*n)
+    double2 *vel;    // node velocity, rows 0..n, index j*m+i (solver array)
+    double2 *src;    // projection right-hand side, same layout
+    int *flags;      // [0]: plastic sub-step cap reached, [1]: max sub-steps
+};
+
+struct step_consts {
+    int m, n;
+    double ax, ay, by, dx, dy, lx, xsp, ysp;
+    double mu, K;
+    // STZ law
+    int stz_model, t_model;
+    double t_scale, adapt_fac, chi_inf, s_y, theta, Delta, Omegaeps0, tau0, c0, kappa, rho;
+    double chi_diff, chi_len;
+    int track_plastic;
+    int substep_cap;
+};
+
+step_consts make_step_consts(const stz_params &p);
+
+// shear_sim::advection_step + chi_diffusion + the field update
+// (shear_sim.cc:296-386, fields.hh:61-80).  bv is the wall speed of the
+// current state (u = -bv on row 0 and +bv on row n, set_boundaries).
+void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st);
+// projection_step source term (shear_sim.cc:399-409, net_force :447-453).
+void projection_source(const step_consts &c, fields_dev &F, int cur, double dt, double xbc_bv, cudaStream_t st);
+// stress correction and velocity copy (shear_sim.cc:418-434) followed by
+// set_boundaries (shear_sim.cc:552-581) at the wall speed/position bv, bp.
+void projection_apply(const step_consts &c, fields_dev &F, int cur, double dt, double bv, double bp,
+                      cudaStream_t st);
+// set_boundaries alone (ghost rows and wall nodes of buffer cur).
+void set_boundaries(const step_consts &c, fields_dev &F, int cur, double bp, cudaStream_t st);
+
+}  // namespace stzg
