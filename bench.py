@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--fp64-steps", type=int, default=0, help="FP64 comparison steps (0: = steps+warmup, capped)")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--inner", type=int, default=0, help="FP32 V-cycles per refinement pass (0: library default)")
+    ap.add_argument("--skip-extras", action="store_true", help="only the timed line (no FP64 leg, e2e, CPU)")
     return ap.parse_args()
 
 
@@ -225,7 +227,7 @@ def run_ours(args, dist):
     prec = _lib.MIXED if args.precision == "mixed" else _lib.FP64
     extrap = not args.no_extrapolate
     sim = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, device=dist.local,
-                   extrapolate=extrap)
+                   extrapolate=extrap, inner_cycles=args.inner)
     sim.steps(DT, args.warmup)
     clocks = ClockSampler(dist.local)
     clocks.start()
@@ -254,6 +256,9 @@ def run_ours(args, dist):
             "wall_ms_per_step": 1e3 * wall / args.steps}
     if dist.rank != 0:
         return None
+    if args.skip_extras:
+        line["inner_cycles"] = args.inner
+        return line
 
     # FP64 GPU path and the mixed-vs-FP64 error from the same initial state
     if prec == _lib.MIXED:

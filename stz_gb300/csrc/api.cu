@@ -248,7 +248,7 @@ int run_passes(stzg_sim *s, int k) {
 }
 
 int solve_mixed(stzg_sim *s, int *ncyc) {
-    const int inner = s->O.inner_cycles > 0 ? s->O.inner_cycles : 2;
+    const int inner = s->O.inner_cycles > 0 ? s->O.inner_cycles : 3;
     if (inner != s->g_inner && s->g_pass32) {
         cudaGraphExecDestroy(s->g_pass32);
         s->g_pass32 = nullptr;
@@ -285,8 +285,9 @@ int solve(stzg_sim *s, int *ncyc) {
     return s->O.precision == STZG_MIXED ? solve_mixed(s, ncyc) : solve_fp64(s, ncyc);
 }
 
-int do_projection(stzg_sim *s, double dt) {
+int do_projection(stzg_sim *s, double dt, bool fresh_combinations) {
     STZG_CHECK(ensure_ops(s, dt));
+    if (!fresh_combinations) precombine(s->sc, s->F, s->cur, dt, s->st);
     const double bv = bdry_vel(s, s->time), bp = bdry_pos(s, s->time);
     projection_source(s->sc, s->F, s->cur, dt, s->q.bcs * s->q.cxx * bv, s->st);
     if (s->O.extrapolate) {
@@ -389,6 +390,8 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if ((st = dev_alloc(s, (void **)&s->F.vel, nn * sizeof(double2))) != STZG_OK) return bail(st);
     if ((st = dev_alloc(s, (void **)&s->F.src, nn * sizeof(double2))) != STZG_OK) return bail(st);
     if ((st = dev_alloc(s, (void **)&s->F.flags, 4 * sizeof(int))) != STZG_OK) return bail(st);
+    for (int k = 0; k < 4; k++)
+        if ((st = dev_alloc(s, (void **)&s->F.pre[k], nc * sizeof(double))) != STZG_OK) return bail(st);
     if (o.extrapolate)
         if ((st = dev_alloc(s, (void **)&s->vel_prev, nn * sizeof(double2))) != STZG_OK) return bail(st);
     s->npart = reduction_blocks();
@@ -563,7 +566,7 @@ int stzg_step_qs(stzg_sim *s, double dt, int nsteps, stzg_stats *stats) {
     for (int k = 0; k < nsteps; k++) {
         s->time += dt;  // shear_sim.cc:283
         STZG_CHECK(do_advection(s, dt));
-        STZG_CHECK(do_projection(s, dt));
+        STZG_CHECK(do_projection(s, dt, true));
         STZG_CHECK(check_flags(s));
     }
     STZG_CUDA(cudaEventRecord(s->ev1, s->st));
@@ -665,7 +668,7 @@ int stzg_advection_step(stzg_sim *s, double dt) {
 
 int stzg_projection_step(stzg_sim *s, double dt, stzg_stats *stats) {
     if (!s || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
-    STZG_CHECK(do_projection(s, dt));
+    STZG_CHECK(do_projection(s, dt, false));
     STZG_CUDA(cudaStreamSynchronize(s->st));
     if (stats) *stats = s->acc;
     return STZG_OK;

@@ -88,6 +88,23 @@ __host__ __device__ inline double pw(int f, int um, int prd, int c) {
     return w;
 }
 
+// Integer form used by the kernels: halves (1 or 2) instead of weights, so
+// that single-precision transfer kernels do no double-precision arithmetic.
+__host__ __device__ inline int p1d_halves(int f, int um, int prd, int *c, int *h) {
+    int sm = (um + (prd ? 1 : 2)) >> 1;
+    if (!(f & 1)) { c[0] = f >> 1; h[0] = 2; return 1; }
+    if (!prd && !(um & 1) && f == um - 1) { c[0] = sm - 1; h[0] = 2; return 1; }
+    c[0] = f >> 1; h[0] = 1;
+    c[1] = (prd && f == um - 1) ? 0 : (f >> 1) + 1; h[1] = 1;
+    return 2;
+}
+__host__ __device__ inline int halves_of(int f, int um, int prd, int c) {
+    int cc[2], hh[2];
+    int k = p1d_halves(f, um, prd, cc, hh), w = 0;
+    for (int a = 0; a < k; a++) if (cc[a] == c) w += hh[a];
+    return w;
+}
+
 // ---------------------------------------------------------------------------
 // Galerkin coarse operators (tgmg_base::rat and the generated compute_rat,
 // tgmg.in.cc:667-736, tgmg_compile.pl:151-338), formed as sum_k sum_l
@@ -319,6 +336,8 @@ template <typename T> int hierarchy<T>::allocate(int m, int n, V *top_z, V *top_
     return STZG_OK;
 }
 
+template <typename T> cudaError_t prepare_tail_kernel();
+
 template <typename T> int hierarchy<T>::upload_ops(const std::vector<level_ops> &ops, const top_op<double> &o) {
     op.Kmx = (T)o.Kmx; op.Kmy = (T)o.Kmy; op.mx = (T)o.mx; op.my = (T)o.my; op.qK = (T)o.qK;
     op.cxx = (T)o.cxx; op.cyy = (T)o.cyy; op.icxx = (T)o.icxx; op.icyy = (T)o.icyy;
@@ -338,6 +357,7 @@ template <typename T> int hierarchy<T>::upload_ops(const std::vector<level_ops> 
         STZG_CUDA(cudaMemcpy((void *)D.st, tab.data(), sizeof(stencil9<T>) * tab.size(), cudaMemcpyHostToDevice));
         STZG_CUDA(cudaMemcpy((void *)D.cls, L.cls.data(), sizeof(int) * L.cls.size(), cudaMemcpyHostToDevice));
     }
+    STZG_CUDA(prepare_tail_kernel<T>());
     bottom_inv = nullptr;
     bottom_unknowns = 0;
     if (nl > 1) {
@@ -556,16 +576,17 @@ __global__ void k_restrict(const typename vec2_t<T>::type *__restrict__ r, int f
     for (int dy = -1; dy <= 1; dy++) {
         int fy = 2 * J + dy;
         if (fy < 0 || fy >= fn) continue;
-        T wy = (T)pw(fy, fn, 0, J);
-        if (wy == 0) continue;
+        int hy = halves_of(fy, fn, 0, J);
+        if (hy == 0) continue;
         for (int dx = -1; dx <= 1; dx++) {
             int fx = 2 * I + dx;
             fx = fx < 0 ? fx + fm : (fx >= fm ? fx - fm : fx);
-            T wx = (T)pw(fx, fm, 1, I);
-            if (wx == 0) continue;
+            int hx = halves_of(fx, fm, 1, I);
+            if (hx == 0) continue;
+            const T w = (T)(hx * hy) * (T)0.25;
             V v = r[(size_t)fy * fm + fx];
-            ax += wx * wy * v.x;
-            ay += wx * wy * v.y;
+            ax += w * v.x;
+            ay += w * v.y;
         }
     }
     V o;
@@ -582,13 +603,12 @@ __global__ void k_prolong_add(const typename vec2_t<T>::type *__restrict__ zc, i
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= fm || j >= fn) return;
-    int cy[2], cx[2];
-    double wy[2], wx[2];
-    int ny = p1d(j, fn, 0, cy, wy), nx = p1d(i, fm, 1, cx, wx);
+    int cy[2], cx[2], hy[2], hx[2];
+    int ny = p1d_halves(j, fn, 0, cy, hy), nx = p1d_halves(i, fm, 1, cx, hx);
     T ax = 0, ay = 0;
     for (int b = 0; b < ny; b++)
         for (int a = 0; a < nx; a++) {
-            T w = (T)(wx[a] * wy[b]);
+            const T w = (T)(hx[a] * hy[b]) * (T)0.25;
             V v = zc[(size_t)cy[b] * cm + cx[a]];
             ax += w * v.x;
             ay += w * v.y;
@@ -751,6 +771,596 @@ __global__ void k_extrapolate(double2 *__restrict__ z, double2 *__restrict__ pre
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fused top-level kernels (single precision).  A block owns a tile of TCX x
+// TCY coarse points and the 2TCX x 2TCY fine points below them.  It stages z
+// and b of the tile plus a halo in shared memory, runs both colours of the
+// Gauss-Seidel sweep there (recomputing the halo points that neighbouring
+// blocks own, with the same arithmetic, so every copy agrees), and then either
+// restricts the residual (down) or, after adding the prolongation, writes the
+// swept tile (up).  One launch replaces the five or three launches of the
+// colour-by-colour path; HBM sees z and b once per sweep.
+
+constexpr int TCX = 32, TCY = 8;
+constexpr int DW = 2 * TCX + 7, DH = 2 * TCY + 7;   // down: fine x in [2I0-4, 2I1+2]
+constexpr int UW = 2 * TCX + 4, UH = 2 * TCY + 4;   // up:   fine x in [2I0-2, 2I1+1]
+constexpr int kFusedThreads = 256;
+constexpr int kFusedMinWidth = 2 * TCX + 16;       // no self-aliasing of the periodic halo
+
+__device__ __forceinline__ int wrapx(int x, int m) { return x < 0 ? x + m : (x >= m ? x - m : x); }
+
+// One colour of the top-level sweep on tile points [lo, W-1-lo] x [lo, H-1-lo].
+template <typename T, int W, int H>
+__device__ inline void tile_top_color(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
+                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int m, int n, int color,
+                                      int lo) {
+    typedef typename vec2_t<T>::type V;
+    const int w = W - 2 * lo, h = H - 2 * lo;
+    for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
+        const int ty = lo + k / w, tx = lo + k % w;
+        const int gy = y0 + ty;
+        if (gy < 0 || gy >= n) continue;
+        const int gx = wrapx(x0 + tx, m);
+        const bool xc = ((gx + gy) & 1) == color;
+        V &zc = zs[ty][tx];
+        const V bb = bs[ty][tx];
+        if (gy == 0 || gy == n - 1) {
+            if (xc) zc.x = op.ibcxx * bb.x;
+            else zc.y = op.ibcyy * bb.y;
+            continue;
+        }
+        const V l = zs[ty][tx - 1], r = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
+        const V dl = zs[ty - 1][tx - 1], ur = zs[ty + 1][tx + 1], dr = zs[ty - 1][tx + 1], ul = zs[ty + 1][tx - 1];
+        if (xc) {
+            T a = op.Kmx * (l.x + r.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
+            zc.x = op.icxx * (bb.x - a);
+        } else {
+            T a = op.mx * (l.y + r.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
+            zc.y = op.icyy * (bb.y - a);
+        }
+    }
+}
+
+// Pre-smooth + residual + restriction of the top level (apply_r after one
+// gauss_seidel, tgmg.in.cc:313-320).
+template <typename T>
+__global__ void __launch_bounds__(kFusedThreads) k_top_down(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
+                                                         const typename vec2_t<T>::type *__restrict__ b, int m,
+                                                         int n, typename vec2_t<T>::type *__restrict__ bc, int cm,
+                                                         int cn) {
+    typedef typename vec2_t<T>::type V;
+    __shared__ V zs[DH][DW];
+    __shared__ V bs[DH][DW];
+    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
+    for (int k = threadIdx.x; k < DH * DW; k += blockDim.x) {
+        const int ty = k / DW, tx = k % DW, gy = y0 + ty;
+        V zz, bb;
+        zz.x = zz.y = bb.x = bb.y = 0;
+        if (gy >= 0 && gy < n) {
+            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
+            zz = z[g];
+            bb = b[g];
+        }
+        zs[ty][tx] = zz;
+        bs[ty][tx] = bb;
+    }
+    __syncthreads();
+    tile_top_color<T, DW, DH>(op, zs, bs, x0, y0, m, n, 0, 1);
+    __syncthreads();
+    tile_top_color<T, DW, DH>(op, zs, bs, x0, y0, m, n, 1, 2);
+    __syncthreads();
+    // residual on [3, W-4] x [3, H-4], written over b
+    {
+        const int lo = 3, w = DW - 2 * lo, h = DH - 2 * lo;
+        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
+            const int ty = lo + k / w, tx = lo + k % w, gy = y0 + ty;
+            if (gy < 0 || gy >= n) continue;
+            const V c = zs[ty][tx], bb = bs[ty][tx];
+            V r;
+            if (gy == 0 || gy == n - 1) {
+                r.x = bb.x - op.bcxx * c.x;
+                r.y = bb.y - op.bcyy * c.y;
+            } else {
+                const V l = zs[ty][tx - 1], rr = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
+                const V dl = zs[ty - 1][tx - 1], ur = zs[ty + 1][tx + 1], dr = zs[ty - 1][tx + 1],
+                        ul = zs[ty + 1][tx - 1];
+                T ax = op.Kmx * (l.x + rr.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
+                T ay = op.mx * (l.y + rr.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
+                r.x = bb.x - ax - op.cxx * c.x;
+                r.y = bb.y - ay - op.cyy * c.y;
+            }
+            bs[ty][tx] = r;
+        }
+    }
+    __syncthreads();
+    // restriction to the coarse tile, and the swept fine tile back to HBM
+    for (int k = threadIdx.x; k < TCX * TCY; k += blockDim.x) {
+        const int cI = k % TCX, cJ = k / TCX, I = I0 + cI, J = J0 + cJ;
+        if (I >= cm || J >= cn) continue;
+        T ax = 0, ay = 0;
+        for (int dy = -1; dy <= 1; dy++) {
+            const int fy = 2 * J + dy;
+            if (fy < 0 || fy >= n) continue;
+            const int hy = halves_of(fy, n, 0, J);
+            if (!hy) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int hx = halves_of(wrapx(2 * I + dx, m), m, 1, I);
+                if (!hx) continue;
+                const V r = bs[2 * cJ + 4 + dy][2 * cI + 4 + dx];
+                const T wgt = (T)(hx * hy) * (T)0.25;
+                ax += wgt * r.x;
+                ay += wgt * r.y;
+            }
+        }
+        V o;
+        o.x = ax;
+        o.y = ay;
+        bc[(size_t)J * cm + I] = o;
+    }
+    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
+        const int tx = 4 + k % (2 * TCX), ty = 4 + k / (2 * TCX);
+        const int gx = x0 + tx, gy = y0 + ty;
+        if (gx >= m || gy >= n) continue;
+        z[(size_t)gy * m + gx] = zs[ty][tx];
+    }
+}
+
+// Prolongation + post-smooth of the top level (apply_t of level 0, then
+// up_gs_iterations, tgmg.in.cc:323-327).
+template <typename T>
+__global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
+                                                       const typename vec2_t<T>::type *__restrict__ b, int m, int n,
+                                                       const typename vec2_t<T>::type *__restrict__ zc, int cm,
+                                                       int cn) {
+    typedef typename vec2_t<T>::type V;
+    __shared__ V zs[UH][UW];
+    __shared__ V bs[UH][UW];
+    __shared__ V cs[TCY + 3][TCX + 3];
+    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int x0 = 2 * I0 - 2, y0 = 2 * J0 - 2;
+    for (int k = threadIdx.x; k < UH * UW; k += blockDim.x) {
+        const int ty = k / UW, tx = k % UW, gy = y0 + ty;
+        V zz, bb;
+        zz.x = zz.y = bb.x = bb.y = 0;
+        if (gy >= 0 && gy < n) {
+            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
+            zz = z[g];
+            bb = b[g];
+        }
+        zs[ty][tx] = zz;
+        bs[ty][tx] = bb;
+    }
+    for (int k = threadIdx.x; k < (TCY + 3) * (TCX + 3); k += blockDim.x) {
+        const int ly = k / (TCX + 3), lx = k % (TCX + 3), J = J0 - 1 + ly;
+        V v;
+        v.x = v.y = 0;
+        if (J >= 0 && J < cn) v = zc[(size_t)J * cm + wrapx(I0 - 1 + lx, cm)];
+        cs[ly][lx] = v;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < UH * UW; k += blockDim.x) {
+        const int ty = k / UW, tx = k % UW, gy = y0 + ty;
+        if (gy < 0 || gy >= n) continue;
+        const int gx = wrapx(x0 + tx, m);
+        int cy[2], cx[2], hy[2], hx[2];
+        const int ny = p1d_halves(gy, n, 0, cy, hy), nx = p1d_halves(gx, m, 1, cx, hx);
+        T ax = 0, ay = 0;
+        bool inside = true;
+        for (int bq = 0; bq < ny; bq++)
+            for (int a = 0; a < nx; a++) {
+                int lx = cx[a] - (I0 - 1);
+                if (lx < 0) lx += cm;
+                if (lx >= cm) lx -= cm;
+                const int ly = cy[bq] - (J0 - 1);
+                // Points of a partial last tile far beyond its owned columns
+                // (wrapped copies that no owned output depends on) may map
+                // outside the staged coarse patch.
+                if (lx < 0 || lx >= TCX + 3 || ly < 0 || ly >= TCY + 3) {
+                    inside = false;
+                    continue;
+                }
+                const V v = cs[ly][lx];
+                const T wgt = (T)(hx[a] * hy[bq]) * (T)0.25;
+                ax += wgt * v.x;
+                ay += wgt * v.y;
+            }
+        if (!inside) ax = ay = 0;
+        zs[ty][tx].x += ax;
+        zs[ty][tx].y += ay;
+    }
+    __syncthreads();
+    tile_top_color<T, UW, UH>(op, zs, bs, x0, y0, m, n, 0, 1);
+    __syncthreads();
+    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
+        const int tx = 2 + k % (2 * TCX), ty = 2 + k / (2 * TCX);
+        const int gx = x0 + tx, gy = y0 + ty;
+        if (gx >= m || gy >= n) continue;
+        V &zcur = zs[ty][tx];
+        const V bb = bs[ty][tx];
+        const bool xc = ((gx + gy) & 1) == 1;
+        if (gy == 0 || gy == n - 1) {
+            if (xc) zcur.x = op.ibcxx * bb.x;
+            else zcur.y = op.ibcyy * bb.y;
+        } else {
+            const V l = zs[ty][tx - 1], r = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
+            const V dl = zs[ty - 1][tx - 1], ur = zs[ty + 1][tx + 1], dr = zs[ty - 1][tx + 1], ul = zs[ty + 1][tx - 1];
+            if (xc) {
+                T a = op.Kmx * (l.x + r.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
+                zcur.x = op.icxx * (bb.x - a);
+            } else {
+                T a = op.mx * (l.y + r.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
+                zcur.y = op.icyy * (bb.y - a);
+            }
+        }
+        z[(size_t)gy * m + gx] = zcur;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused coarse-level kernels (single precision, even periodic lines): the
+// same tiling as the top level, with the four-colour block Gauss-Seidel of
+// the stored Galerkin stencils.  Down: the sweep starts from z = 0
+// (down_gs_iterations, tgmg.hh:273-279), so only b is read; the residual is
+// restricted to the child.  Up: prolongation of the child plus one sweep.
+
+constexpr int LDW = 2 * TCX + 11, LDH = 2 * TCY + 11;  // down: fine x in [2I0-6, 2I1+4]
+constexpr int LUW = 2 * TCX + 8, LUH = 2 * TCY + 8;    // up:   fine x in [2I0-4, 2I1+3]
+
+template <typename T, int W, int H>
+__device__ inline void tile_lev_color(const level_view<T> &L, typename vec2_t<T>::type (*zs)[W],
+                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int cx, int cy, int lo) {
+    typedef typename vec2_t<T>::type V;
+    // points of colour (cx, cy) inside [lo, W-1-lo] x [lo, H-1-lo]
+    const int txs = lo + (((cx - (x0 + lo)) % 2) + 2) % 2, tys = lo + (((cy - (y0 + lo)) % 2) + 2) % 2;
+    const int nx = (W - 1 - lo - txs) / 2 + 1, ny = (H - 1 - lo - tys) / 2 + 1;
+    if (nx <= 0 || ny <= 0) return;
+    for (int k = threadIdx.x; k < nx * ny; k += blockDim.x) {
+        const int tx = txs + 2 * (k % nx), ty = tys + 2 * (k / nx);
+        const int gy = y0 + ty;
+        if (gy < 0 || gy >= L.n) continue;
+        const int gx = wrapx(x0 + tx, L.m);
+        const stencil9<T> &s = stencil_at(L, gx, gy);
+        V a;
+        a.x = a.y = 0;
+        if (gy > 0) {
+            madd(a, s.e[0], zs[ty - 1][tx - 1]); madd(a, s.e[1], zs[ty - 1][tx]); madd(a, s.e[2], zs[ty - 1][tx + 1]);
+        }
+        madd(a, s.e[3], zs[ty][tx - 1]); madd(a, s.e[5], zs[ty][tx + 1]);
+        if (gy < L.n - 1) {
+            madd(a, s.e[6], zs[ty + 1][tx - 1]); madd(a, s.e[7], zs[ty + 1][tx]); madd(a, s.e[8], zs[ty + 1][tx + 1]);
+        }
+        const V bb = bs[ty][tx];
+        const T rx = bb.x - a.x, ry = bb.y - a.y;
+        V o;
+        o.x = s.e[9].a * rx + s.e[9].b * ry;
+        o.y = s.e[9].c * rx + s.e[9].d * ry;
+        zs[ty][tx] = o;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, level_view<T> C) {
+    typedef typename vec2_t<T>::type V;
+    __shared__ V zs[LDH][LDW];
+    __shared__ V bs[LDH][LDW];
+    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int x0 = 2 * I0 - 6, y0 = 2 * J0 - 6;
+    for (int k = threadIdx.x; k < LDH * LDW; k += blockDim.x) {
+        const int ty = k / LDW, tx = k % LDW, gy = y0 + ty;
+        V bb, zz;
+        bb.x = bb.y = zz.x = zz.y = 0;
+        if (gy >= 0 && gy < L.n) bb = L.b[(size_t)gy * L.m + wrapx(x0 + tx, L.m)];
+        zs[ty][tx] = zz;
+        bs[ty][tx] = bb;
+    }
+    __syncthreads();
+    for (int p = 0; p < 4; p++) {
+        tile_lev_color<T, LDW, LDH>(L, zs, bs, x0, y0, p & 1, p >> 1, 1 + p);
+        __syncthreads();
+    }
+    // residual on [5, W-6], over b
+    {
+        const int lo = 5, w = LDW - 2 * lo, h = LDH - 2 * lo;
+        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
+            const int ty = lo + k / w, tx = lo + k % w, gy = y0 + ty;
+            if (gy < 0 || gy >= L.n) continue;
+            const int gx = wrapx(x0 + tx, L.m);
+            const stencil9<T> &s = stencil_at(L, gx, gy);
+            V a;
+            a.x = a.y = 0;
+            if (gy > 0) {
+                madd(a, s.e[0], zs[ty - 1][tx - 1]); madd(a, s.e[1], zs[ty - 1][tx]); madd(a, s.e[2], zs[ty - 1][tx + 1]);
+            }
+            madd(a, s.e[3], zs[ty][tx - 1]); madd(a, s.e[4], zs[ty][tx]); madd(a, s.e[5], zs[ty][tx + 1]);
+            if (gy < L.n - 1) {
+                madd(a, s.e[6], zs[ty + 1][tx - 1]); madd(a, s.e[7], zs[ty + 1][tx]); madd(a, s.e[8], zs[ty + 1][tx + 1]);
+            }
+            V r;
+            r.x = bs[ty][tx].x - a.x;
+            r.y = bs[ty][tx].y - a.y;
+            bs[ty][tx] = r;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < TCX * TCY; k += blockDim.x) {
+        const int cI = k % TCX, cJ = k / TCX, I = I0 + cI, J = J0 + cJ;
+        if (I >= C.m || J >= C.n) continue;
+        T ax = 0, ay = 0;
+        for (int dy = -1; dy <= 1; dy++) {
+            const int fy = 2 * J + dy;
+            if (fy < 0 || fy >= L.n) continue;
+            const int hy = halves_of(fy, L.n, 0, J);
+            if (!hy) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int hx = halves_of(wrapx(2 * I + dx, L.m), L.m, 1, I);
+                if (!hx) continue;
+                const V r = bs[2 * cJ + 6 + dy][2 * cI + 6 + dx];
+                const T wgt = (T)(hx * hy) * (T)0.25;
+                ax += wgt * r.x;
+                ay += wgt * r.y;
+            }
+        }
+        V o;
+        o.x = ax;
+        o.y = ay;
+        C.b[(size_t)J * C.m + I] = o;
+    }
+    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
+        const int tx = 6 + k % (2 * TCX), ty = 6 + k / (2 * TCX);
+        const int gx = x0 + tx, gy = y0 + ty;
+        if (gx >= L.m || gy >= L.n) continue;
+        L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level_view<T> C) {
+    typedef typename vec2_t<T>::type V;
+    __shared__ V zs[LUH][LUW];
+    __shared__ V bs[LUH][LUW];
+    __shared__ V cs[TCY + 5][TCX + 5];
+    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
+    for (int k = threadIdx.x; k < LUH * LUW; k += blockDim.x) {
+        const int ty = k / LUW, tx = k % LUW, gy = y0 + ty;
+        V zz, bb;
+        zz.x = zz.y = bb.x = bb.y = 0;
+        if (gy >= 0 && gy < L.n) {
+            const size_t g = (size_t)gy * L.m + wrapx(x0 + tx, L.m);
+            zz = L.z[g];
+            bb = L.b[g];
+        }
+        zs[ty][tx] = zz;
+        bs[ty][tx] = bb;
+    }
+    for (int k = threadIdx.x; k < (TCY + 5) * (TCX + 5); k += blockDim.x) {
+        const int ly = k / (TCX + 5), lx = k % (TCX + 5), J = J0 - 2 + ly;
+        V v;
+        v.x = v.y = 0;
+        if (J >= 0 && J < C.n) v = C.z[(size_t)J * C.m + wrapx(I0 - 2 + lx, C.m)];
+        cs[ly][lx] = v;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < LUH * LUW; k += blockDim.x) {
+        const int ty = k / LUW, tx = k % LUW, gy = y0 + ty;
+        if (gy < 0 || gy >= L.n) continue;
+        const int gx = wrapx(x0 + tx, L.m);
+        int cy[2], cx[2], hy[2], hx[2];
+        const int ny = p1d_halves(gy, L.n, 0, cy, hy), nx = p1d_halves(gx, L.m, 1, cx, hx);
+        T ax = 0, ay = 0;
+        bool inside = true;
+        for (int bq = 0; bq < ny; bq++)
+            for (int a = 0; a < nx; a++) {
+                int lx = cx[a] - (I0 - 2);
+                if (lx < 0) lx += C.m;
+                if (lx >= C.m) lx -= C.m;
+                const int ly = cy[bq] - (J0 - 2);
+                if (lx < 0 || lx >= TCX + 5 || ly < 0 || ly >= TCY + 5) {
+                    inside = false;
+                    continue;
+                }
+                const V v = cs[ly][lx];
+                const T wgt = (T)(hx[a] * hy[bq]) * (T)0.25;
+                ax += wgt * v.x;
+                ay += wgt * v.y;
+            }
+        if (!inside) ax = ay = 0;
+        zs[ty][tx].x += ax;
+        zs[ty][tx].y += ay;
+    }
+    __syncthreads();
+    for (int p = 0; p < 4; p++) {
+        tile_lev_color<T, LUW, LUH>(L, zs, bs, x0, y0, p & 1, p >> 1, 1 + p);
+        __syncthreads();
+    }
+    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
+        const int tx = 4 + k % (2 * TCX), ty = 4 + k / (2 * TCX);
+        const int gx = x0 + tx, gy = y0 + ty;
+        if (gx >= L.m || gy >= L.n) continue;
+        L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tail of the V-cycle on small levels, one block: levels t..ml-1 go down
+// (clear, sweep, residual, restriction), the coarsest level is solved, and
+// the levels come back up to t (prolongation, sweep).  Phases are separated by
+// __syncthreads; the data stays in L1/L2.
+
+struct tail_levels {
+    int t, ml;
+    const double *inv;
+    int inv_n;
+};
+
+template <typename T>
+__device__ void tail_sweep(const level_view<T> &L) {
+    typedef typename vec2_t<T>::type V;
+    const int hm = (L.m + 1) >> 1, hn = (L.n + 1) >> 1;
+    for (int cy = 0; cy < 2; cy++)
+        for (int cx = 0; cx < L.colors_x; cx++) {
+            const int cnt = cx == 2 ? hn : hm * hn;
+            for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+                int i, j;
+                if (cx == 2) {
+                    i = L.m - 1;
+                    j = 2 * k + cy;
+                } else {
+                    i = 2 * (k % hm) + cx;
+                    j = 2 * (k / hm) + cy;
+                    if (L.colors_x == 3 && i == L.m - 1) continue;
+                }
+                if (i >= L.m || j >= L.n) continue;
+                const stencil9<T> &s = stencil_at(L, i, j);
+                const size_t ij = (size_t)j * L.m + i;
+                V a = lev_offdiag<T, V>(L, s, L.z, i, j);
+                V r, o;
+                r.x = L.b[ij].x - a.x;
+                r.y = L.b[ij].y - a.y;
+                o.x = s.e[9].a * r.x + s.e[9].b * r.y;
+                o.y = s.e[9].c * r.x + s.e[9].d * r.y;
+                L.z[ij] = o;
+            }
+            __syncthreads();
+        }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T> H) {
+    typedef typename vec2_t<T>::type V;
+    extern __shared__ __align__(16) unsigned char tail_raw[];
+    double *tsh = (double *)tail_raw;
+    V *p = (V *)(tail_raw + ((sizeof(double) * tl.inv_n + 15) & ~(size_t)15));
+    // every level of the tail lives in shared memory; level t exchanges b
+    // and z with its global arrays
+    level_view<T> S[17];
+    for (int l = tl.t; l <= tl.ml; l++) {
+        S[l] = H.lv[l];
+        const int mn = S[l].m * S[l].n;
+        S[l].z = p;
+        p += mn;
+        S[l].b = p;
+        p += mn;
+        S[l].r = p;
+        p += mn;
+    }
+    {
+        const int mn = S[tl.t].m * S[tl.t].n;
+        for (int k = threadIdx.x; k < mn; k += blockDim.x) S[tl.t].b[k] = H.lv[tl.t].b[k];
+    }
+    __syncthreads();
+    for (int i = tl.t; i < tl.ml; i++) {
+        const level_view<T> &L = S[i];
+        const int mn = L.m * L.n;
+        for (int k = threadIdx.x; k < mn; k += blockDim.x) {
+            L.z[k].x = 0;
+            L.z[k].y = 0;
+        }
+        __syncthreads();
+        tail_sweep(L);
+        for (int k = threadIdx.x; k < mn; k += blockDim.x) {
+            const int ii = k % L.m, jj = k / L.m;
+            const stencil9<T> &s = stencil_at(L, ii, jj);
+            V a = lev_offdiag<T, V>(L, s, L.z, ii, jj);
+            madd(a, s.e[4], L.z[k]);
+            V r;
+            r.x = L.b[k].x - a.x;
+            r.y = L.b[k].y - a.y;
+            L.r[k] = r;
+        }
+        __syncthreads();
+        const level_view<T> &C = S[i + 1];
+        for (int k = threadIdx.x; k < C.m * C.n; k += blockDim.x) {
+            const int I = k % C.m, J = k / C.m;
+            T ax = 0, ay = 0;
+            for (int dy = -1; dy <= 1; dy++) {
+                const int fy = 2 * J + dy;
+                if (fy < 0 || fy >= L.n) continue;
+                const int hy = halves_of(fy, L.n, 0, J);
+                if (!hy) continue;
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int fx = wrapx(2 * I + dx, L.m);
+                    const int hx = halves_of(fx, L.m, 1, I);
+                    if (!hx) continue;
+                    const V v = L.r[(size_t)fy * L.m + fx];
+                    const T wgt = (T)(hx * hy) * (T)0.25;
+                    ax += wgt * v.x;
+                    ay += wgt * v.y;
+                }
+            }
+            C.b[k].x = ax;
+            C.b[k].y = ay;
+        }
+        __syncthreads();
+    }
+    // coarsest level: z = A^-1 b in FP64
+    {
+        const level_view<T> &B = S[tl.ml];
+        const int N = tl.inv_n;
+        for (int k = threadIdx.x; k < N / 2; k += blockDim.x) {
+            tsh[2 * k] = (double)B.b[k].x;
+            tsh[2 * k + 1] = (double)B.b[k].y;
+        }
+        __syncthreads();
+        T *zz = (T *)B.z;
+        for (int r = threadIdx.x; r < N; r += blockDim.x) {
+            const double *row = tl.inv + (size_t)r * N;
+            double a = 0;
+            for (int k = 0; k < N; k++) a += row[k] * tsh[k];
+            zz[r] = (T)a;
+        }
+        __syncthreads();
+    }
+    for (int i = tl.ml; i > tl.t; i--) {
+        const level_view<T> &C = S[i], &F = S[i - 1];
+        for (int k = threadIdx.x; k < F.m * F.n; k += blockDim.x) {
+            const int ii = k % F.m, jj = k / F.m;
+            int cy[2], cx[2], hy[2], hx[2];
+            const int ny = p1d_halves(jj, F.n, 0, cy, hy), nx = p1d_halves(ii, F.m, 1, cx, hx);
+            T ax = 0, ay = 0;
+            for (int bq = 0; bq < ny; bq++)
+                for (int a = 0; a < nx; a++) {
+                    const V v = C.z[(size_t)cy[bq] * C.m + cx[a]];
+                    const T wgt = (T)(hx[a] * hy[bq]) * (T)0.25;
+                    ax += wgt * v.x;
+                    ay += wgt * v.y;
+                }
+            F.z[k].x += ax;
+            F.z[k].y += ay;
+        }
+        __syncthreads();
+        tail_sweep(F);
+    }
+    {
+        const int mn = S[tl.t].m * S[tl.t].n;
+        for (int k = threadIdx.x; k < mn; k += blockDim.x) H.lv[tl.t].z[k] = S[tl.t].z[k];
+    }
+}
+
+constexpr size_t kTailSmem = 200 * 1024;
+
+template <typename T> size_t tail_smem_bytes(const hierarchy<T> &h, int t) {
+    size_t b = ((sizeof(double) * h.bottom_unknowns + 15) & ~(size_t)15);
+    for (int l = t; l < h.nl; l++) b += 3 * sizeof(typename vec2_t<T>::type) * (size_t)h.lv[l].m * h.lv[l].n;
+    return b;
+}
+
+}  // namespace
+
+// Opt the tail kernel into the shared memory it needs (set once per
+// process, outside any stream capture).
+template <typename T> cudaError_t prepare_tail_kernel() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    done = true;
+    return cudaFuncSetAttribute(k_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem + 1024);
+}
+template cudaError_t prepare_tail_kernel<float>();
+template cudaError_t prepare_tail_kernel<double>();
+
+namespace {
+
 inline dim3 grid2(int m, int n, dim3 blk) { return dim3(ceil_div(m, blk.x), ceil_div(n, blk.y)); }
 
 }  // namespace
@@ -776,23 +1386,75 @@ template <typename T> static void lev_sweep(level_view<T> &L, cudaStream_t st) {
         }
 }
 
+// First level handled by the single-block tail (levels of at most
+// tail_points points, plus a direct coarsest solve); ml+1 when there is none.
+template <typename T> static int tail_start(const hierarchy<T> &h) {
+    const int ml = h.nl - 1;
+    if (ml < 1 || !h.bottom_inv) return ml + 1;
+    const long limit = sizeof(T) == 4 ? 4400 : 300;
+    int t = ml;
+    while (t > 1 && (long)h.lv[t - 1].m * h.lv[t - 1].n <= limit && tail_smem_bytes(h, t - 1) <= kTailSmem) t--;
+    if (tail_smem_bytes(h, t) > kTailSmem) return ml + 1;
+    return t;
+}
+
+// Levels wide enough for the single-precision tile kernels (an even periodic
+// line that the halo cannot wrap onto itself).
+template <typename T> static bool tile_level(const level_view<T> &L) {
+    return sizeof(T) == 4 && L.colors_x == 2 && L.m >= kFusedMinWidth;
+}
+
 template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64) {
+    typedef typename vec2_t<T>::type V;
     dim3 blk(32, 8);
     const int ml = h.nl - 1;
-    top_sweep(h, st);
-    if (ml > 0) {
-        level_view<T> &T0 = h.lv[0];
-        k_top_residual<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.op, T0.z, T0.b, T0.r, T0.m, T0.n); note_launch();
+    level_view<T> &T0 = h.lv[0];
+    const bool fused = sizeof(T) == 4 && ml > 0 && T0.m >= kFusedMinWidth;
+    if (ml == 0) {
+        top_sweep(h, st);
+        top_sweep(h, st);
+        return;
+    }
+    const int t = tail_start(h);
+    if (fused) {
+        dim3 g(ceil_div(h.lv[1].m, TCX), ceil_div(h.lv[1].n, TCY));
+        k_top_down<T><<<g, kFusedThreads, 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].b, h.lv[1].m, h.lv[1].n);
+        note_launch();
+    } else {
+        top_sweep(h, st);
+        k_top_residual<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.op, T0.z, T0.b, T0.r, T0.m, T0.n);
+        note_launch();
         k_restrict<T><<<grid2(h.lv[1].m, h.lv[1].n, blk), blk, 0, st>>>(T0.r, T0.m, T0.n, h.lv[1].b, h.lv[1].m,
-                                                                       h.lv[1].n); note_launch();
-        for (int i = 1; i < ml; i++) {
-            level_view<T> &L = h.lv[i];
-            cudaMemsetAsync(L.z, 0, sizeof(typename vec2_t<T>::type) * (size_t)L.m * L.n, st);
-            lev_sweep(L, st);
-            k_lev_residual<T><<<grid2(L.m, L.n, blk), blk, 0, st>>>(L); note_launch();
-            level_view<T> &C = h.lv[i + 1];
-            k_restrict<T><<<grid2(C.m, C.n, blk), blk, 0, st>>>(L.r, L.m, L.n, C.b, C.m, C.n); note_launch();
+                                                                       h.lv[1].n);
+        note_launch();
+    }
+    const int down_end = t <= ml ? t : ml;  // levels [1, down_end) go down outside the tail
+    for (int i = 1; i < down_end; i++) {
+        level_view<T> &L = h.lv[i];
+        level_view<T> &C = h.lv[i + 1];
+        if (tile_level(L)) {
+            dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
+            k_lev_down<T><<<g, kFusedThreads, 0, st>>>(L, C);
+            note_launch();
+            continue;
         }
+        cudaMemsetAsync(L.z, 0, sizeof(V) * (size_t)L.m * L.n, st);
+        lev_sweep(L, st);
+        k_lev_residual<T><<<grid2(L.m, L.n, blk), blk, 0, st>>>(L);
+        note_launch();
+        k_restrict<T><<<grid2(C.m, C.n, blk), blk, 0, st>>>(L.r, L.m, L.n, C.b, C.m, C.n);
+        note_launch();
+    }
+    int up_from;
+    if (t <= ml) {
+        hierarchy_view<T> hv;
+        for (int l = 0; l < h.nl; l++) hv.lv[l] = h.lv[l];
+        tail_levels tl{t, ml, h.bottom_inv, h.bottom_unknowns};
+        const size_t smem = tail_smem_bytes(h, t);
+        k_tail<T><<<1, 1024, smem, st>>>(tl, hv);
+        note_launch();
+        up_from = t;
+    } else {
         level_view<T> &B = h.lv[ml];
         if (h.bottom_inv)
             k_bottom_direct<T><<<1, 256, sizeof(double) * h.bottom_unknowns, st>>>(B, h.bottom_inv,
@@ -802,13 +1464,30 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         else
             k_bottom<T, T><<<1, 256, 0, st>>>(B, bottom_sweeps, bottom_sweeps);
         note_launch();
-        for (int i = ml; i >= 1; i--) {
-            level_view<T> &C = h.lv[i], &F = h.lv[i - 1];
-            k_prolong_add<T><<<grid2(F.m, F.n, blk), blk, 0, st>>>(C.z, C.m, C.n, F.z, F.m, F.n); note_launch();
-            if (i > 1) lev_sweep(F, st);
-        }
+        up_from = ml;
     }
-    top_sweep(h, st);
+    for (int i = up_from; i >= 2; i--) {
+        level_view<T> &C = h.lv[i], &F = h.lv[i - 1];
+        if (tile_level(F)) {
+            dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
+            k_lev_up<T><<<g, kFusedThreads, 0, st>>>(F, C);
+            note_launch();
+            continue;
+        }
+        k_prolong_add<T><<<grid2(F.m, F.n, blk), blk, 0, st>>>(C.z, C.m, C.n, F.z, F.m, F.n);
+        note_launch();
+        lev_sweep(F, st);
+    }
+    if (fused) {
+        dim3 g(ceil_div(h.lv[1].m, TCX), ceil_div(h.lv[1].n, TCY));
+        k_top_up<T><<<g, kFusedThreads, 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].z, h.lv[1].m, h.lv[1].n);
+        note_launch();
+    } else {
+        k_prolong_add<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.lv[1].z, h.lv[1].m, h.lv[1].n, T0.z, T0.m,
+                                                                 T0.n);
+        note_launch();
+        top_sweep(h, st);
+    }
 }
 
 template <typename T>

@@ -44,6 +44,11 @@ template <typename T> struct level_view {
     V *z, *b, *r;
 };
 
+// All levels by value, for kernels that walk several levels.
+template <typename T> struct hierarchy_view {
+    level_view<T> lv[17];
+};
+
 // Host copy of a coarse level's operator.
 struct level_ops {
     int m, n;

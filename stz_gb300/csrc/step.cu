@@ -156,7 +156,7 @@ struct velo {
 
 // Fused advection + STZ step per cell (i,j) and its lower-left node.
 __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int cur, double dt, double bv,
-                                                int chi_only_pre) {
+                                                int emit_source) {
     const int m = c.m, n = c.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -245,11 +245,36 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     B[F_CHI][ci] = cchi;
     F.ddev[ci] = ddev;
     if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
-    B[F_P][ci] = p + (-uc * f1[0] - vc * f2[0]);
-    B[F_Q][ci] = q + (-uc * f1[1] - vc * f2[1] - dtmp * q);
-    B[F_S][ci] = s + (-uc * f1[2] - vc * f2[2] + two_omega * t - dtmp * s);
-    B[F_TAU][ci] = t + (-uc * f1[3] - vc * f2[3] - two_omega * s - dtmp * t);
-    (void)chi_only_pre;
+    const double pn = p + (-uc * f1[0] - vc * f2[0]);
+    const double qn = q + (-uc * f1[1] - vc * f2[1] - dtmp * q);
+    const double sn = s + (-uc * f1[2] - vc * f2[2] + two_omega * t - dtmp * s);
+    const double tn = t + (-uc * f1[3] - vc * f2[3] - two_omega * s - dtmp * t);
+    B[F_P][ci] = pn;
+    B[F_Q][ci] = qn;
+    B[F_S][ci] = sn;
+    B[F_TAU][ci] = tn;
+    if (emit_source) {
+        const double xf = 0.5 / dt * c.xsp, yf = 0.5 / dt * c.ysp;
+        const double pq = pn + qn, Aa = pq - sn, Bb = pq + sn;
+        F.pre[0][ci] = xf * Aa + yf * tn;
+        F.pre[1][ci] = xf * Aa - yf * tn;
+        F.pre[2][ci] = xf * tn - yf * Bb;
+        F.pre[3][ci] = xf * tn + yf * Bb;
+    }
+}
+
+__global__ void k_precombine(step_consts c, fields_dev F, int cur, double xf, double yf) {
+    const int m = c.m, n = c.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const size_t k = IDX(i, j);
+    const double pn = F.f[cur][F_P][k], qn = F.f[cur][F_Q][k], sn = F.f[cur][F_S][k], tn = F.f[cur][F_TAU][k];
+    const double pq = pn + qn, Aa = pq - sn, Bb = pq + sn;
+    F.pre[0][k] = xf * Aa + yf * tn;
+    F.pre[1][k] = xf * Aa - yf * tn;
+    F.pre[2][k] = xf * tn - yf * Bb;
+    F.pre[3][k] = xf * tn + yf * Bb;
 }
 
 // chi_diffusion (shear_sim.cc:364-386): B.chi holds cchi; old chi in A.
@@ -273,8 +298,11 @@ __global__ void k_chi_diffusion(step_consts c, fields_dev F, int cur, double dt)
 }
 
 // Source of the projection (shear_sim.cc:399-409): net force of the stress
-// on interior nodes, Dirichlet data on the walls.
-__global__ void k_source(step_consts c, fields_dev F, int cur, double xfac, double yfac, double xbc_bv) {
+// on interior nodes from the four surrounding cells (net_force,
+// shear_sim.cc:447-453) as fx = U(i,j-1) - W(i-1,j-1) + W(i,j) - U(i-1,j),
+// fy = Y1(i-1,j-1) - Y2(i,j-1) + Y2(i-1,j) - Y1(i,j); Dirichlet data on the
+// walls.
+__global__ void k_source(step_consts c, fields_dev F, double xbc_bv) {
     const int m = c.m, n = c.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -287,13 +315,11 @@ __global__ void k_source(step_consts c, fields_dev F, int cur, double xfac, doub
         f.x = xbc_bv;
         f.y = 0;
     } else {
-        const double *p = F.f[cur][F_P], *q = F.f[cur][F_Q], *s = F.f[cur][F_S], *t = F.f[cur][F_TAU];
         const int il = i == 0 ? m - 1 : i - 1;
         const size_t k0 = IDX(il, j - 1), k1 = IDX(i, j - 1), k2 = IDX(il, j), k3 = IDX(i, j);
-        f.x = (-p[k0] + p[k1] - p[k2] + p[k3] - q[k0] + q[k1] - q[k2] + q[k3] + s[k0] - s[k1] + s[k2] - s[k3]) * xfac +
-              (t[k0] + t[k1] - t[k2] - t[k3]) * yfac;
-        f.y = (t[k0] - t[k1] + t[k2] - t[k3]) * xfac +
-              (-p[k0] - p[k1] + p[k2] + p[k3] - q[k0] - q[k1] + q[k2] + q[k3] - s[k0] - s[k1] + s[k2] + s[k3]) * yfac;
+        const double *U = F.pre[0], *W = F.pre[1], *Y1 = F.pre[2], *Y2 = F.pre[3];
+        f.x = (U[k1] - W[k0]) + (W[k3] - U[k2]);
+        f.y = (Y1[k0] - Y2[k1]) + (Y2[k2] - Y1[k3]);
     }
     F.src[(size_t)j * m + i] = f;
 }
@@ -346,7 +372,7 @@ inline dim3 g2(int m, int n, dim3 b) { return dim3(ceil_div(m, b.x), ceil_div(n,
 
 void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st) {
     dim3 blk(32, 8);
-    k_advect<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt, bv, 0); note_launch();
+    k_advect<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt, bv, 1); note_launch();
     if (c.chi_diff != 0 || c.chi_len != 0) {
         k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);
         note_launch();
@@ -355,8 +381,16 @@ void advection(const step_consts &c, fields_dev &F, int cur, double dt, double b
 
 void projection_source(const step_consts &c, fields_dev &F, int cur, double dt, double xbc_bv, cudaStream_t st) {
     dim3 blk(32, 8);
-    const double xfac = 0.5 / dt * c.xsp, yfac = 0.5 / dt * c.ysp;
-    k_source<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, cur, xfac, yfac, xbc_bv); note_launch();
+    k_source<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, xbc_bv);
+    note_launch();
+    (void)cur;
+    (void)dt;
+}
+
+void precombine(const step_consts &c, fields_dev &F, int cur, double dt, cudaStream_t st) {
+    dim3 blk(32, 8);
+    k_precombine<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, 0.5 / dt * c.xsp, 0.5 / dt * c.ysp);
+    note_launch();
 }
 
 void projection_apply(const step_consts &c, fields_dev &F, int cur, double dt, double bv, double bp,

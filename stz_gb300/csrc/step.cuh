@@ -18,6 +18,11 @@ struct fields_dev {
     double2 *vel;    // node velocity, rows 0..n, index j*m+i (solver array)
     double2 *src;    // projection right-hand side, same layout
     int *flags;      // [0]: plastic sub-step cap reached, [1]: max sub-steps
+    // Per-cell combinations of the advected stress that the nodal net force
+    // (shear_sim::net_force, shear_sim.cc:447-453) sums with +-1 weights:
+    // U = xf A + yf tau, W = xf A - yf tau, Y1 = xf tau - yf B,
+    // Y2 = xf tau + yf B, A = p+q-s, B = p+q+s (xf, yf of projection_step).
+    double *pre[4];
 };
 
 struct step_consts {
@@ -38,6 +43,9 @@ step_consts make_step_consts(const stz_params &p);
 // (shear_sim.cc:296-386, fields.hh:61-80).  bv is the wall speed of the
 // current state (u = -bv on row 0 and +bv on row n, set_boundaries).
 void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st);
+// The per-cell combinations above from the current stress (used when the
+// projection runs without the advection kernel in front of it).
+void precombine(const step_consts &c, fields_dev &F, int cur, double dt, cudaStream_t st);
 // projection_step source term (shear_sim.cc:399-409, net_force :447-453).
 void projection_source(const step_consts &c, fields_dev &F, int cur, double dt, double xbc_bv, cudaStream_t st);
 // stress correction and velocity copy (shear_sim.cc:418-434) followed by

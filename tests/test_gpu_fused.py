@@ -1,0 +1,53 @@
+"""The fused single-precision tile kernels (top level, N >= 80) and the
+single-block tail of small levels, against the FP64 colour-by-colour path
+and the oracle."""
+import numpy as np
+import pytest
+
+from oracle.bind import OracleSim
+from parity import group_errors
+from stz_gb300 import _lib
+from stz_gb300.params import plastic_shear, simple_shear
+from stz_gb300.shear_sim import ShearSim, random_chi
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("N", [80, 96, 160, 256])
+def test_mixed_vs_fp64_fused_sizes(N):
+    P = plastic_shear(N, u_bdry=1.0)
+    chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, N)
+    a = ShearSim(P, chi, precision=_lib.FP64, tol_mode=_lib.TOL_RELATIVE, tol=1e-11)
+    b = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-11)
+    a.steps(0.01, 25)
+    b.steps(0.01, 25)
+    err = group_errors(a.fields(), b.fields(), N)
+    assert max(err.values()) < 1e-8, err
+    # the FP32 V-cycles contract like the FP64 ones: comparable cycle counts
+    assert b.cycles <= 1.5 * a.cycles + 25, (b.cycles, a.cycles)
+
+
+@pytest.mark.parametrize("N", [128, 192])
+def test_mixed_against_oracle(N):
+    P = simple_shear(N)
+    chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, 3)
+    g = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-12)
+    g.steps(0.01, 12)
+    o = OracleSim(P, chi)
+    o.set_tolerance(1, 1e-13)
+    o.steps(0.01, 12)
+    err = group_errors(o.fields(), g.fields(), N)
+    assert max(err.values()) < 1e-9, err
+
+
+@pytest.mark.parametrize("inner", [1, 3, 5])
+def test_inner_cycle_counts_converge(inner):
+    N = 128
+    P = simple_shear(N)
+    chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, 9)
+    a = ShearSim(P, chi, precision=_lib.FP64, tol_mode=_lib.TOL_RELATIVE, tol=1e-11)
+    b = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-11, inner_cycles=inner)
+    a.steps(0.01, 10)
+    b.steps(0.01, 10)
+    err = group_errors(a.fields(), b.fields(), N)
+    assert max(err.values()) < 1e-8, err
