@@ -1,0 +1,45 @@
+"""The C++ drop-in header (include/stzg_shear_sim.hh), compiled into a small
+driver that uses the reference's constructor arguments, against the oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle.bind import OracleSim
+from parity import group_errors
+from stz_gb300.params import plastic_shear
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_cpp_dropin_matches_oracle(tmp_path):
+    exe = tmp_path / "dropin"
+    lib = os.path.join(ROOT, "stz_gb300", "_build")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "cpp", "dropin_main.cc"), "-o", str(exe),
+                           "-L", lib, "-lstzg", f"-Wl,-rpath,{lib}"])
+    out = tmp_path / "fields.bin"
+    r = subprocess.run([str(exe), str(out), "10"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    N = 32
+    raw = np.fromfile(out)
+    cells, nodes = N * (N + 2), N * (N + 1)
+    sizes = [N * N] + [cells] * 5 + [nodes] * 4 + [N * N]
+    parts = np.split(raw, np.cumsum(sizes)[:-1])
+    chi0 = parts[0].reshape(N, N)
+    names = ["p", "q", "s", "tau", "chi", "X", "Y", "u", "v", "eps_pl"]
+    got = {k: v for k, v in zip(names, parts[1:])}
+    for k in ("p", "q", "s", "tau", "chi"):
+        got[k] = got[k].reshape(N + 2, N)
+    for k in ("X", "Y", "u", "v"):
+        got[k] = got[k].reshape(N + 1, N)
+    got["eps_pl"] = got["eps_pl"].reshape(N, N)
+    P = plastic_shear(N)
+    o = OracleSim(P, chi0)
+    o.set_tolerance(0, 10.0)
+    o.steps(0.01, 80)
+    err = group_errors(o.fields(), got, N)
+    assert max(err.values()) < 1e-9, err
+    assert "avg_iters" in r.stdout
