@@ -156,6 +156,25 @@ int stzg_mg_stencil(stzg_sim *s, double dt, int level, double *out);
  * (scratch), 5 FP64 residual + FP32 copy + norms. */
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
 
+/* No counterpart in the reference.  Squared residual norms of the
+ * quasi-static system for time step dt on caller-owned device arrays,
+ * without allocating any device memory: out_dev[0] = sum |b - A z|^2,
+ * out_dev[1] = sum |b|^2 (z_dev, b_dev: m*(n+1) (x,y) pairs in the solver
+ * layout of stzg_mg_solve; out_dev: 2 doubles; all on the current device).
+ * For callers that cannot let a library call cudaMalloc: applications whose
+ * caching allocator owns the device memory, services with a fixed memory
+ * budget, and threads that must not stall the GPU (cudaMalloc/cudaFree can
+ * synchronize the device).  The reduction's scratch is a fixed 128 KiB array
+ * in the library's static device memory, held on every GPU that loads the
+ * library until exit; grids above 8,388,608 nodes are rejected with
+ * STZG_EINVAL.  The first call on a device looks up that array's device
+ * address (make it before capturing work on that device into a graph).
+ * Calls share the array: calls that overlap on the GPU race.  Work is
+ * enqueued on `stream` (a cudaStream_t, NULL for the default stream) and
+ * the call returns without synchronizing. */
+int stzg_residual_norms_noalloc(const stz_params *p, double dt, const double *z_dev, const double *b_dev,
+                                double *out_dev, void *stream);
+
 /* Replaces: shear_sim::l2_comparison (shear_sim.cc:460-502) between two
  * handles of the same grid: l2[4] = velocity, stress, chi, reference map. */
 int stzg_l2_comparison(stzg_sim *a, stzg_sim *b, double *l2);

@@ -29,6 +29,7 @@ EXPORTS = [
     "stzg_step_qs", "stzg_advection_step", "stzg_projection_step", "stzg_avg_iters",
     "stzg_mg_solve", "stzg_mg_vcycle", "stzg_mg_l2_error", "stzg_mg_levels", "stzg_mg_stencil",
     "stzg_l2_comparison", "stzg_random_chi", "stzg_upload", "stzg_download", "stzg_time_kernel",
+    "stzg_residual_norms_noalloc",
 ]
 
 
@@ -96,6 +97,8 @@ def load(path=None):
         "stzg_upload": (I, [V, ctypes.POINTER(ctypes.c_void_p)]),
         "stzg_download": (I, [V, ctypes.POINTER(ctypes.c_void_p)]),
         "stzg_time_kernel": (I, [V, D, I, I, _P]),
+        "stzg_residual_norms_noalloc": (I, [ctypes.POINTER(StzParams), D, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p]),
     }
     for name, (res, args) in decl.items():
         f = getattr(lib, name)
