@@ -1,0 +1,44 @@
+"""Run a few quasi-static steps of the simple-shear configuration on the GPU.
+
+    python -m stz_gb300.run_steps --size 2048 --precision mixed --warmup 1 --steps 2
+
+Prints ms/step and multigrid statistics.  This is the command the profiles
+under profiles/ were captured with (ncu wraps it).
+"""
+import argparse
+import time
+
+from . import _lib
+from .params import simple_shear
+from .shear_sim import ShearSim, random_chi
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--std", type=float, default=40.0)
+    ap.add_argument("--corr", type=float, default=16.0)
+    ap.add_argument("--no-extrapolate", action="store_true")
+    a = ap.parse_args(argv)
+    N = a.size
+    P = simple_shear(N)
+    chi = random_chi(N, N, a.corr, 600.0, a.std, P.TZ, 2)
+    prec = _lib.MIXED if a.precision == "mixed" else _lib.FP64
+    sim = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=a.tol,
+                   extrapolate=not a.no_extrapolate)
+    sim.steps(1e-2, a.warmup)
+    t0 = time.time()
+    sim.steps(1e-2, a.steps)
+    t = time.time() - t0
+    st = sim.stats
+    print(f"N={N} {a.precision}: {1e3 * t / max(a.steps, 1):.2f} ms/step, {st.vcycles / max(a.steps, 1):.1f} "
+          f"V-cycles/step, {st.refinements / max(a.steps, 1):.1f} passes/step, {st.kernel_launches} kernels")
+    sim.close()
+
+
+if __name__ == "__main__":
+    main()
