@@ -429,31 +429,37 @@ template <typename V, typename T> __device__ inline void madd(V &acc, const mat2
 }
 
 // One colour of the top-level Gauss-Seidel sweep.  Colour c updates the x
-// component where (i+j)&1 == c and the y component elsewhere.
+// component where (i+j)&1 == c and the y component elsewhere.  A thread takes
+// the node pair (2p, 2p+1) of a row and performs the x update on one and the y
+// update on the other, so lanes never diverge on the component.
 template <typename T>
 __global__ void k_top_color(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
                             const typename vec2_t<T>::type *__restrict__ b, int m, int n, int color) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    typedef typename vec2_t<T>::type V;
+    const int pr = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= m || j >= n) return;
-    const size_t ij = (size_t)j * m + i;
-    const bool xc = ((i + j) & 1) == color;
+    if (2 * pr >= m || j >= n) return;
+    const int ia = 2 * pr;
+    const bool a_is_x = ((ia + j) & 1) == color;
+    const int ix = a_is_x ? ia : ia + 1, iy = a_is_x ? ia + 1 : ia;
+    const size_t row = (size_t)j * m;
     if (j == 0 || j == n - 1) {  // Dirichlet wall rows: z = regcbi*b
-        if (xc) z[ij].x = op.ibcxx * b[ij].x;
-        else z[ij].y = op.ibcyy * b[ij].y;
+        z[row + ix].x = op.ibcxx * b[row + ix].x;
+        z[row + iy].y = op.ibcyy * b[row + iy].y;
         return;
     }
-    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
-    const typename vec2_t<T>::type *zd = z + (size_t)(j - 1) * m, *zc = z + (size_t)j * m,
-                                   *zu = z + (size_t)(j + 1) * m;
-    if (xc) {
-        T a = op.Kmx * (zc[il].x + zc[ir].x) + op.my * (zd[i].x + zu[i].x) +
+    const V *zd = z + row - m, *zc = z + row, *zu = z + row + m;
+    {
+        const int il = ix == 0 ? m - 1 : ix - 1, ir = ix == m - 1 ? 0 : ix + 1;
+        T a = op.Kmx * (zc[il].x + zc[ir].x) + op.my * (zd[ix].x + zu[ix].x) +
               op.qK * (zd[il].y + zu[ir].y - zd[ir].y - zu[il].y);
-        z[ij].x = op.icxx * (b[ij].x - a);
-    } else {
-        T a = op.mx * (zc[il].y + zc[ir].y) + op.Kmy * (zd[i].y + zu[i].y) +
+        z[row + ix].x = op.icxx * (b[row + ix].x - a);
+    }
+    {
+        const int il = iy == 0 ? m - 1 : iy - 1, ir = iy == m - 1 ? 0 : iy + 1;
+        T a = op.mx * (zc[il].y + zc[ir].y) + op.Kmy * (zd[iy].y + zu[iy].y) +
               op.qK * (zd[il].x + zu[ir].x - zd[ir].x - zu[il].x);
-        z[ij].y = op.icyy * (b[ij].y - a);
+        z[row + iy].y = op.icyy * (b[row + iy].y - a);
     }
 }
 
@@ -736,53 +742,129 @@ __global__ void k_extrapolate(double2 *__restrict__ z, double2 *__restrict__ pre
 }
 
 // ---------------------------------------------------------------------------
-// Fused top-level kernels (single precision).  A block owns a tile of TCX x
-// TCY coarse points and the 2TCX x 2TCY fine points below them.  It stages z
-// and b of the tile plus a halo in shared memory, runs both colours of the
-// Gauss-Seidel sweep there (recomputing the halo points that neighbouring
-// blocks own, with the same arithmetic, so every copy agrees), and then either
-// restricts the residual (down) or, after adding the prolongation, writes the
-// swept tile (up).  One launch replaces the five or three launches of the
-// colour-by-colour path; HBM sees z and b once per sweep.
+// Fused top-level kernels (single precision).  A block (32 x 8 threads) owns a
+// tile of TCX x TCY coarse points and the 2TCX x 2TCY fine points below them.
+// It stages z and b of the tile plus a halo in shared memory, runs both
+// colours of the Gauss-Seidel sweep there (recomputing the halo points that
+// neighbouring blocks own, with the same arithmetic, so every copy agrees),
+// and then either restricts the residual (down) or, after adding the
+// prolongation, writes the swept tile (up).  One launch replaces the five or
+// three launches of the colour-by-colour path; HBM sees z and b once per
+// sweep.  Loops are two-dimensional (no division), and in each colour a
+// thread updates a horizontal pair of nodes: the x component of the one whose
+// parity matches the colour and the y component of the other, so the warps
+// do not diverge.
 
 constexpr int TCX = 32, TCY = 8;
 constexpr int DW = 2 * TCX + 7, DH = 2 * TCY + 7;   // down: fine x in [2I0-4, 2I1+2]
 constexpr int UW = 2 * TCX + 4, UH = 2 * TCY + 4;   // up:   fine x in [2I0-2, 2I1+1]
-constexpr int kFusedThreads = 256;
+constexpr int kFusedThreads = 256;                 // blockDim (32, 8)
 constexpr int kFusedMinWidth = 2 * TCX + 16;       // no self-aliasing of the periodic halo
 
 __device__ __forceinline__ int wrapx(int x, int m) { return x < 0 ? x + m : (x >= m ? x - m : x); }
 
-// One colour of the top-level sweep on tile points [lo, W-1-lo] x [lo, H-1-lo].
-template <typename T, int W, int H>
+// Flattened loop over a RH x RW rectangle of a tile starting at (R0, C0).
+#define TILE_FOR(RH, RW, R0, C0, ty, tx)                                                   \
+    for (int k_ = threadIdx.y * blockDim.x + threadIdx.x; k_ < (RH) * (RW); k_ += blockDim.x * blockDim.y) \
+        if (const int ty = (R0) + k_ / (RW), tx = (C0) + k_ % (RW); true)
+
+template <typename T, int W>
+__device__ __forceinline__ void top_x_update(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
+                                             typename vec2_t<T>::type (*bs)[W], int ty, int tx, bool wall) {
+    if (wall) {
+        zs[ty][tx].x = op.ibcxx * bs[ty][tx].x;
+        return;
+    }
+    const T l = zs[ty][tx - 1].x, r = zs[ty][tx + 1].x, d = zs[ty - 1][tx].x, u = zs[ty + 1][tx].x;
+    const T dl = zs[ty - 1][tx - 1].y, ur = zs[ty + 1][tx + 1].y, dr = zs[ty - 1][tx + 1].y,
+            ul = zs[ty + 1][tx - 1].y;
+    const T a = op.Kmx * (l + r) + op.my * (d + u) + op.qK * (dl + ur - dr - ul);
+    zs[ty][tx].x = op.icxx * (bs[ty][tx].x - a);
+}
+
+template <typename T, int W>
+__device__ __forceinline__ void top_y_update(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
+                                             typename vec2_t<T>::type (*bs)[W], int ty, int tx, bool wall) {
+    if (wall) {
+        zs[ty][tx].y = op.ibcyy * bs[ty][tx].y;
+        return;
+    }
+    const T l = zs[ty][tx - 1].y, r = zs[ty][tx + 1].y, d = zs[ty - 1][tx].y, u = zs[ty + 1][tx].y;
+    const T dl = zs[ty - 1][tx - 1].x, ur = zs[ty + 1][tx + 1].x, dr = zs[ty - 1][tx + 1].x,
+            ul = zs[ty + 1][tx - 1].x;
+    const T a = op.mx * (l + r) + op.Kmy * (d + u) + op.qK * (dl + ur - dr - ul);
+    zs[ty][tx].y = op.icyy * (bs[ty][tx].y - a);
+}
+
+// One colour of the top-level sweep on tile rows/columns [LO, H-1-LO] x
+// [LO, W-1-LO]: colour c updates x where (i+j)&1 == c and y elsewhere.  The
+// (row, pair) index is flattened with compile-time divisors so that every
+// lane has work.
+template <typename T, int W, int H, int LO>
 __device__ inline void tile_top_color(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
-                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int m, int n, int color,
-                                      int lo) {
-    typedef typename vec2_t<T>::type V;
-    const int w = W - 2 * lo, h = H - 2 * lo;
-    for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-        const int ty = lo + k / w, tx = lo + k % w;
+                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int n, int color) {
+    constexpr int HI = W - 1 - LO, NPR = (HI - LO + 2) >> 1, NR = H - 2 * LO;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int k = tid; k < NR * NPR; k += nth) {
+        const int ty = LO + k / NPR, ta = LO + 2 * (k % NPR);
         const int gy = y0 + ty;
         if (gy < 0 || gy >= n) continue;
-        const int gx = wrapx(x0 + tx, m);
-        const bool xc = ((gx + gy) & 1) == color;
-        V &zc = zs[ty][tx];
-        const V bb = bs[ty][tx];
-        if (gy == 0 || gy == n - 1) {
-            if (xc) zc.x = op.ibcxx * bb.x;
-            else zc.y = op.ibcyy * bb.y;
-            continue;
-        }
-        const V l = zs[ty][tx - 1], r = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
+        const bool wall = gy == 0 || gy == n - 1;
+        const bool a_is_x = ((x0 + ta + gy) & 1) == color;
+        const int tx_x = a_is_x ? ta : ta + 1, tx_y = a_is_x ? ta + 1 : ta;
+        if (tx_x <= HI) top_x_update<T, W>(op, zs, bs, ty, tx_x, wall);
+        if (tx_y <= HI) top_y_update<T, W>(op, zs, bs, ty, tx_y, wall);
+    }
+}
+
+// Residual b - A z of the top level at a tile point (written over b).
+template <typename T, int W>
+__device__ __forceinline__ void top_residual_at(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
+                                                typename vec2_t<T>::type (*bs)[W], int ty, int tx, bool wall) {
+    typedef typename vec2_t<T>::type V;
+    const V c = zs[ty][tx], bb = bs[ty][tx];
+    V r;
+    if (wall) {
+        r.x = bb.x - op.bcxx * c.x;
+        r.y = bb.y - op.bcyy * c.y;
+    } else {
+        const V l = zs[ty][tx - 1], rr = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
         const V dl = zs[ty - 1][tx - 1], ur = zs[ty + 1][tx + 1], dr = zs[ty - 1][tx + 1], ul = zs[ty + 1][tx - 1];
-        if (xc) {
-            T a = op.Kmx * (l.x + r.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
-            zc.x = op.icxx * (bb.x - a);
-        } else {
-            T a = op.mx * (l.y + r.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
-            zc.y = op.icyy * (bb.y - a);
+        const T ax = op.Kmx * (l.x + rr.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
+        const T ay = op.mx * (l.y + rr.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
+        r.x = bb.x - ax - op.cxx * c.x;
+        r.y = bb.y - ay - op.cyy * c.y;
+    }
+    bs[ty][tx] = r;
+}
+
+// Full weighting of the residual held in rs at coarse point (I, J); the fine
+// point 2I+dx sits at tile column cx0 + dx.  Periodic x with an even line
+// always has the weights (1, 2, 1)/2.
+template <typename T, int W>
+__device__ __forceinline__ typename vec2_t<T>::type restrict_at(typename vec2_t<T>::type (*rs)[W], int I, int J,
+                                                                int n, int cx0, int cy0) {
+    typedef typename vec2_t<T>::type V;
+    T ax = 0, ay = 0;
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++) {
+        const int fy = 2 * J + dy;
+        if (fy < 0 || fy >= n) continue;
+        const int hy = halves_of(fy, n, 0, J);
+        if (!hy) continue;
+#pragma unroll
+        for (int dx = -1; dx <= 1; dx++) {
+            const T wgt = (T)((dx == 0 ? 2 : 1) * hy) * (T)0.25;
+            const V r = rs[cy0 + dy][cx0 + dx];
+            ax += wgt * r.x;
+            ay += wgt * r.y;
         }
     }
+    V o;
+    o.x = ax;
+    o.y = ay;
+    (void)I;
+    return o;
 }
 
 // Pre-smooth + residual + restriction of the top level (apply_r after one
@@ -797,8 +879,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_top_down(top_op<T> op, typena
     __shared__ V bs[DH][DW];
     const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
     const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
-    for (int k = threadIdx.x; k < DH * DW; k += blockDim.x) {
-        const int ty = k / DW, tx = k % DW, gy = y0 + ty;
+    TILE_FOR(DH, DW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
         V zz, bb;
         zz.x = zz.y = bb.x = bb.y = 0;
         if (gy >= 0 && gy < n) {
@@ -810,63 +892,22 @@ __global__ void __launch_bounds__(kFusedThreads) k_top_down(top_op<T> op, typena
         bs[ty][tx] = bb;
     }
     __syncthreads();
-    tile_top_color<T, DW, DH>(op, zs, bs, x0, y0, m, n, 0, 1);
+    tile_top_color<T, DW, DH, 1>(op, zs, bs, x0, y0, n, 0);
     __syncthreads();
-    tile_top_color<T, DW, DH>(op, zs, bs, x0, y0, m, n, 1, 2);
+    tile_top_color<T, DW, DH, 2>(op, zs, bs, x0, y0, n, 1);
     __syncthreads();
-    // residual on [3, W-4] x [3, H-4], written over b
+    TILE_FOR(DH - 6, DW - 6, 3, 3, ty, tx) {
+        const int gy = y0 + ty;
+        if (gy >= 0 && gy < n) top_residual_at<T, DW>(op, zs, bs, ty, tx, gy == 0 || gy == n - 1);
+    }
+    __syncthreads();
     {
-        const int lo = 3, w = DW - 2 * lo, h = DH - 2 * lo;
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-            const int ty = lo + k / w, tx = lo + k % w, gy = y0 + ty;
-            if (gy < 0 || gy >= n) continue;
-            const V c = zs[ty][tx], bb = bs[ty][tx];
-            V r;
-            if (gy == 0 || gy == n - 1) {
-                r.x = bb.x - op.bcxx * c.x;
-                r.y = bb.y - op.bcyy * c.y;
-            } else {
-                const V l = zs[ty][tx - 1], rr = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
-                const V dl = zs[ty - 1][tx - 1], ur = zs[ty + 1][tx + 1], dr = zs[ty - 1][tx + 1],
-                        ul = zs[ty + 1][tx - 1];
-                T ax = op.Kmx * (l.x + rr.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
-                T ay = op.mx * (l.y + rr.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
-                r.x = bb.x - ax - op.cxx * c.x;
-                r.y = bb.y - ay - op.cyy * c.y;
-            }
-            bs[ty][tx] = r;
-        }
+        const int cI = threadIdx.x, cJ = threadIdx.y, I = I0 + cI, J = J0 + cJ;
+        if (I < cm && J < cn) bc[(size_t)J * cm + I] = restrict_at<T, DW>(bs, I, J, n, 2 * cI + 4, 2 * cJ + 4);
     }
-    __syncthreads();
-    // restriction to the coarse tile, and the swept fine tile back to HBM
-    for (int k = threadIdx.x; k < TCX * TCY; k += blockDim.x) {
-        const int cI = k % TCX, cJ = k / TCX, I = I0 + cI, J = J0 + cJ;
-        if (I >= cm || J >= cn) continue;
-        T ax = 0, ay = 0;
-        for (int dy = -1; dy <= 1; dy++) {
-            const int fy = 2 * J + dy;
-            if (fy < 0 || fy >= n) continue;
-            const int hy = halves_of(fy, n, 0, J);
-            if (!hy) continue;
-            for (int dx = -1; dx <= 1; dx++) {
-                const int hx = halves_of(wrapx(2 * I + dx, m), m, 1, I);
-                if (!hx) continue;
-                const V r = bs[2 * cJ + 4 + dy][2 * cI + 4 + dx];
-                const T wgt = (T)(hx * hy) * (T)0.25;
-                ax += wgt * r.x;
-                ay += wgt * r.y;
-            }
-        }
-        V o;
-        o.x = ax;
-        o.y = ay;
-        bc[(size_t)J * cm + I] = o;
-    }
-    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
-        const int tx = 4 + k % (2 * TCX), ty = 4 + k / (2 * TCX);
-        const int gx = x0 + tx, gy = y0 + ty;
-        if (gx >= m || gy >= n) continue;
-        z[(size_t)gy * m + gx] = zs[ty][tx];
+    TILE_FOR(2 * TCY, 2 * TCX, 4, 4, ty, tx) {
+        const int gy = y0 + ty, gx = x0 + tx;
+        if (gy < n && gx < m) z[(size_t)gy * m + gx] = zs[ty][tx];
     }
 }
 
@@ -883,8 +924,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename
     __shared__ V cs[TCY + 3][TCX + 3];
     const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
     const int x0 = 2 * I0 - 2, y0 = 2 * J0 - 2;
-    for (int k = threadIdx.x; k < UH * UW; k += blockDim.x) {
-        const int ty = k / UW, tx = k % UW, gy = y0 + ty;
+    TILE_FOR(UH, UW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
         V zz, bb;
         zz.x = zz.y = bb.x = bb.y = 0;
         if (gy >= 0 && gy < n) {
@@ -895,69 +936,61 @@ __global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename
         zs[ty][tx] = zz;
         bs[ty][tx] = bb;
     }
-    for (int k = threadIdx.x; k < (TCY + 3) * (TCX + 3); k += blockDim.x) {
-        const int ly = k / (TCX + 3), lx = k % (TCX + 3), J = J0 - 1 + ly;
+    TILE_FOR(TCY + 3, TCX + 3, 0, 0, ly, lx) {
+        const int J = J0 - 1 + ly;
         V v;
         v.x = v.y = 0;
         if (J >= 0 && J < cn) v = zc[(size_t)J * cm + wrapx(I0 - 1 + lx, cm)];
         cs[ly][lx] = v;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < UH * UW; k += blockDim.x) {
-        const int ty = k / UW, tx = k % UW, gy = y0 + ty;
+    TILE_FOR(UH, UW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
         if (gy < 0 || gy >= n) continue;
-        const int gx = wrapx(x0 + tx, m);
-        int cy[2], cx[2], hy[2], hx[2];
-        const int ny = p1d_halves(gy, n, 0, cy, hy), nx = p1d_halves(gx, m, 1, cx, hx);
-        T ax = 0, ay = 0;
-        bool inside = true;
-        for (int bq = 0; bq < ny; bq++)
-            for (int a = 0; a < nx; a++) {
-                int lx = cx[a] - (I0 - 1);
-                if (lx < 0) lx += cm;
-                if (lx >= cm) lx -= cm;
-                const int ly = cy[bq] - (J0 - 1);
-                // Points of a partial last tile far beyond its owned columns
-                // (wrapped copies that no owned output depends on) may map
-                // outside the staged coarse patch.
-                if (lx < 0 || lx >= TCX + 3 || ly < 0 || ly >= TCY + 3) {
+        int cy[2], hy[2];
+        const int ny = p1d_halves(gy, n, 0, cy, hy);
+        {
+            // even periodic line: even fine points inject, odd ones average
+            const int gx = wrapx(x0 + tx, m);
+            const int c0 = gx >> 1, c1 = (gx == m - 1) ? 0 : c0 + 1;
+            const bool odd = gx & 1;
+            int l0 = c0 - (I0 - 1), l1 = c1 - (I0 - 1);
+            l0 += l0 < 0 ? cm : (l0 >= cm ? -cm : 0);
+            l1 += l1 < 0 ? cm : (l1 >= cm ? -cm : 0);
+            T ax = 0, ay = 0;
+            bool inside = true;
+            for (int q = 0; q < ny; q++) {
+                const int ly = cy[q] - (J0 - 1);
+                if (ly < 0 || ly >= TCY + 3 || l0 < 0 || l0 >= TCX + 3 || (odd && (l1 < 0 || l1 >= TCX + 3))) {
+                    // wrapped copies far beyond a partial tile's owned columns:
+                    // no owned output depends on them
                     inside = false;
                     continue;
                 }
-                const V v = cs[ly][lx];
-                const T wgt = (T)(hx[a] * hy[bq]) * (T)0.25;
-                ax += wgt * v.x;
-                ay += wgt * v.y;
+                const T wy = (T)hy[q] * (T)0.25;
+                if (odd) {
+                    const V v0 = cs[ly][l0], v1 = cs[ly][l1];
+                    ax += wy * (v0.x + v1.x);
+                    ay += wy * (v0.y + v1.y);
+                } else {
+                    const V v0 = cs[ly][l0];
+                    ax += (T)2 * wy * v0.x;
+                    ay += (T)2 * wy * v0.y;
+                }
             }
-        if (!inside) ax = ay = 0;
-        zs[ty][tx].x += ax;
-        zs[ty][tx].y += ay;
+            if (!inside) ax = ay = 0;
+            zs[ty][tx].x += ax;
+            zs[ty][tx].y += ay;
+        }
     }
     __syncthreads();
-    tile_top_color<T, UW, UH>(op, zs, bs, x0, y0, m, n, 0, 1);
+    tile_top_color<T, UW, UH, 1>(op, zs, bs, x0, y0, n, 0);
     __syncthreads();
-    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
-        const int tx = 2 + k % (2 * TCX), ty = 2 + k / (2 * TCX);
-        const int gx = x0 + tx, gy = y0 + ty;
-        if (gx >= m || gy >= n) continue;
-        V &zcur = zs[ty][tx];
-        const V bb = bs[ty][tx];
-        const bool xc = ((gx + gy) & 1) == 1;
-        if (gy == 0 || gy == n - 1) {
-            if (xc) zcur.x = op.ibcxx * bb.x;
-            else zcur.y = op.ibcyy * bb.y;
-        } else {
-            const V l = zs[ty][tx - 1], r = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
-            const V dl = zs[ty - 1][tx - 1], ur = zs[ty + 1][tx + 1], dr = zs[ty - 1][tx + 1], ul = zs[ty + 1][tx - 1];
-            if (xc) {
-                T a = op.Kmx * (l.x + r.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
-                zcur.x = op.icxx * (bb.x - a);
-            } else {
-                T a = op.mx * (l.y + r.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
-                zcur.y = op.icyy * (bb.y - a);
-            }
-        }
-        z[(size_t)gy * m + gx] = zcur;
+    tile_top_color<T, UW, UH, 2>(op, zs, bs, x0, y0, n, 1);
+    __syncthreads();
+    TILE_FOR(2 * TCY, 2 * TCX, 2, 2, ty, tx) {
+        const int gy = y0 + ty, gx = x0 + tx;
+        if (gy < n && gx < m) z[(size_t)gy * m + gx] = zs[ty][tx];
     }
 }
 
@@ -971,29 +1004,44 @@ __global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename
 constexpr int LDW = 2 * TCX + 11, LDH = 2 * TCY + 11;  // down: fine x in [2I0-6, 2I1+4]
 constexpr int LUW = 2 * TCX + 8, LUH = 2 * TCY + 8;    // up:   fine x in [2I0-4, 2I1+3]
 
-template <typename T, int W, int H>
-__device__ inline void tile_lev_color(const level_view<T> &L, typename vec2_t<T>::type (*zs)[W],
-                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int cx, int cy, int lo) {
+template <typename T, int W>
+__device__ __forceinline__ typename vec2_t<T>::type lev_offdiag_tile(const stencil9<T> &s,
+                                                                     typename vec2_t<T>::type (*zs)[W], int ty, int tx,
+                                                                     bool has_d, bool has_u) {
     typedef typename vec2_t<T>::type V;
-    // points of colour (cx, cy) inside [lo, W-1-lo] x [lo, H-1-lo]
-    const int txs = lo + (((cx - (x0 + lo)) % 2) + 2) % 2, tys = lo + (((cy - (y0 + lo)) % 2) + 2) % 2;
-    const int nx = (W - 1 - lo - txs) / 2 + 1, ny = (H - 1 - lo - tys) / 2 + 1;
-    if (nx <= 0 || ny <= 0) return;
-    for (int k = threadIdx.x; k < nx * ny; k += blockDim.x) {
-        const int tx = txs + 2 * (k % nx), ty = tys + 2 * (k / nx);
+    V a;
+    a.x = a.y = 0;
+    if (has_d) {
+        madd(a, s.e[0], zs[ty - 1][tx - 1]);
+        madd(a, s.e[1], zs[ty - 1][tx]);
+        madd(a, s.e[2], zs[ty - 1][tx + 1]);
+    }
+    madd(a, s.e[3], zs[ty][tx - 1]);
+    madd(a, s.e[5], zs[ty][tx + 1]);
+    if (has_u) {
+        madd(a, s.e[6], zs[ty + 1][tx - 1]);
+        madd(a, s.e[7], zs[ty + 1][tx]);
+        madd(a, s.e[8], zs[ty + 1][tx + 1]);
+    }
+    return a;
+}
+
+// Colour (cx, cy) on tile rows/columns [LO, H-1-LO] x [LO, W-1-LO]; the
+// colour's rows and columns are enumerated with compile-time strides.
+template <typename T, int W, int H, int LO>
+__device__ inline void tile_lev_color(const level_view<T> &L, typename vec2_t<T>::type (*zs)[W],
+                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int cx, int cy) {
+    typedef typename vec2_t<T>::type V;
+    constexpr int NC = (W - 2 * LO + 1) / 2, NRW = (H - 2 * LO + 1) / 2;
+    const int ty0 = LO + ((cy - (y0 + LO)) & 1), tx0 = LO + ((cx - (x0 + LO)) & 1);
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int k = tid; k < NRW * NC; k += nth) {
+        const int ty = ty0 + 2 * (k / NC), tx = tx0 + 2 * (k % NC);
+        if (ty > H - 1 - LO || tx > W - 1 - LO) continue;
         const int gy = y0 + ty;
         if (gy < 0 || gy >= L.n) continue;
-        const int gx = wrapx(x0 + tx, L.m);
-        const stencil9<T> &s = stencil_at(L, gx, gy);
-        V a;
-        a.x = a.y = 0;
-        if (gy > 0) {
-            madd(a, s.e[0], zs[ty - 1][tx - 1]); madd(a, s.e[1], zs[ty - 1][tx]); madd(a, s.e[2], zs[ty - 1][tx + 1]);
-        }
-        madd(a, s.e[3], zs[ty][tx - 1]); madd(a, s.e[5], zs[ty][tx + 1]);
-        if (gy < L.n - 1) {
-            madd(a, s.e[6], zs[ty + 1][tx - 1]); madd(a, s.e[7], zs[ty + 1][tx]); madd(a, s.e[8], zs[ty + 1][tx + 1]);
-        }
+        const stencil9<T> &s = stencil_at(L, wrapx(x0 + tx, L.m), gy);
+        const V a = lev_offdiag_tile<T, W>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
         const V bb = bs[ty][tx];
         const T rx = bb.x - a.x, ry = bb.y - a.y;
         V o;
@@ -1010,8 +1058,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, lev
     __shared__ V bs[LDH][LDW];
     const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
     const int x0 = 2 * I0 - 6, y0 = 2 * J0 - 6;
-    for (int k = threadIdx.x; k < LDH * LDW; k += blockDim.x) {
-        const int ty = k / LDW, tx = k % LDW, gy = y0 + ty;
+    TILE_FOR(LDH, LDW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
         V bb, zz;
         bb.x = bb.y = zz.x = zz.y = 0;
         if (gy >= 0 && gy < L.n) bb = L.b[(size_t)gy * L.m + wrapx(x0 + tx, L.m)];
@@ -1019,62 +1067,33 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, lev
         bs[ty][tx] = bb;
     }
     __syncthreads();
-    for (int p = 0; p < 4; p++) {
-        tile_lev_color<T, LDW, LDH>(L, zs, bs, x0, y0, p & 1, p >> 1, 1 + p);
-        __syncthreads();
-    }
-    // residual on [5, W-6], over b
-    {
-        const int lo = 5, w = LDW - 2 * lo, h = LDH - 2 * lo;
-        for (int k = threadIdx.x; k < w * h; k += blockDim.x) {
-            const int ty = lo + k / w, tx = lo + k % w, gy = y0 + ty;
-            if (gy < 0 || gy >= L.n) continue;
-            const int gx = wrapx(x0 + tx, L.m);
-            const stencil9<T> &s = stencil_at(L, gx, gy);
-            V a;
-            a.x = a.y = 0;
-            if (gy > 0) {
-                madd(a, s.e[0], zs[ty - 1][tx - 1]); madd(a, s.e[1], zs[ty - 1][tx]); madd(a, s.e[2], zs[ty - 1][tx + 1]);
-            }
-            madd(a, s.e[3], zs[ty][tx - 1]); madd(a, s.e[4], zs[ty][tx]); madd(a, s.e[5], zs[ty][tx + 1]);
-            if (gy < L.n - 1) {
-                madd(a, s.e[6], zs[ty + 1][tx - 1]); madd(a, s.e[7], zs[ty + 1][tx]); madd(a, s.e[8], zs[ty + 1][tx + 1]);
-            }
-            V r;
-            r.x = bs[ty][tx].x - a.x;
-            r.y = bs[ty][tx].y - a.y;
-            bs[ty][tx] = r;
-        }
+    tile_lev_color<T, LDW, LDH, 1>(L, zs, bs, x0, y0, 0, 0);
+    __syncthreads();
+    tile_lev_color<T, LDW, LDH, 2>(L, zs, bs, x0, y0, 1, 0);
+    __syncthreads();
+    tile_lev_color<T, LDW, LDH, 3>(L, zs, bs, x0, y0, 0, 1);
+    __syncthreads();
+    tile_lev_color<T, LDW, LDH, 4>(L, zs, bs, x0, y0, 1, 1);
+    __syncthreads();
+    TILE_FOR(LDH - 10, LDW - 10, 5, 5, ty, tx) {
+        const int gy = y0 + ty;
+        if (gy < 0 || gy >= L.n) continue;
+        const stencil9<T> &s = stencil_at(L, wrapx(x0 + tx, L.m), gy);
+        V a = lev_offdiag_tile<T, LDW>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
+        madd(a, s.e[4], zs[ty][tx]);
+        V r;
+        r.x = bs[ty][tx].x - a.x;
+        r.y = bs[ty][tx].y - a.y;
+        bs[ty][tx] = r;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < TCX * TCY; k += blockDim.x) {
-        const int cI = k % TCX, cJ = k / TCX, I = I0 + cI, J = J0 + cJ;
-        if (I >= C.m || J >= C.n) continue;
-        T ax = 0, ay = 0;
-        for (int dy = -1; dy <= 1; dy++) {
-            const int fy = 2 * J + dy;
-            if (fy < 0 || fy >= L.n) continue;
-            const int hy = halves_of(fy, L.n, 0, J);
-            if (!hy) continue;
-            for (int dx = -1; dx <= 1; dx++) {
-                const int hx = halves_of(wrapx(2 * I + dx, L.m), L.m, 1, I);
-                if (!hx) continue;
-                const V r = bs[2 * cJ + 6 + dy][2 * cI + 6 + dx];
-                const T wgt = (T)(hx * hy) * (T)0.25;
-                ax += wgt * r.x;
-                ay += wgt * r.y;
-            }
-        }
-        V o;
-        o.x = ax;
-        o.y = ay;
-        C.b[(size_t)J * C.m + I] = o;
+    {
+        const int cI = threadIdx.x, cJ = threadIdx.y, I = I0 + cI, J = J0 + cJ;
+        if (I < C.m && J < C.n) C.b[(size_t)J * C.m + I] = restrict_at<T, LDW>(bs, I, J, L.n, 2 * cI + 6, 2 * cJ + 6);
     }
-    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
-        const int tx = 6 + k % (2 * TCX), ty = 6 + k / (2 * TCX);
-        const int gx = x0 + tx, gy = y0 + ty;
-        if (gx >= L.m || gy >= L.n) continue;
-        L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
+    TILE_FOR(2 * TCY, 2 * TCX, 6, 6, ty, tx) {
+        const int gy = y0 + ty, gx = x0 + tx;
+        if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
     }
 }
 
@@ -1086,8 +1105,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
     __shared__ V cs[TCY + 5][TCX + 5];
     const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
     const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
-    for (int k = threadIdx.x; k < LUH * LUW; k += blockDim.x) {
-        const int ty = k / LUW, tx = k % LUW, gy = y0 + ty;
+    TILE_FOR(LUH, LUW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
         V zz, bb;
         zz.x = zz.y = bb.x = bb.y = 0;
         if (gy >= 0 && gy < L.n) {
@@ -1098,59 +1117,71 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
         zs[ty][tx] = zz;
         bs[ty][tx] = bb;
     }
-    for (int k = threadIdx.x; k < (TCY + 5) * (TCX + 5); k += blockDim.x) {
-        const int ly = k / (TCX + 5), lx = k % (TCX + 5), J = J0 - 2 + ly;
+    TILE_FOR(TCY + 5, TCX + 5, 0, 0, ly, lx) {
+        const int J = J0 - 2 + ly;
         V v;
         v.x = v.y = 0;
         if (J >= 0 && J < C.n) v = C.z[(size_t)J * C.m + wrapx(I0 - 2 + lx, C.m)];
         cs[ly][lx] = v;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < LUH * LUW; k += blockDim.x) {
-        const int ty = k / LUW, tx = k % LUW, gy = y0 + ty;
+    TILE_FOR(LUH, LUW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
         if (gy < 0 || gy >= L.n) continue;
-        const int gx = wrapx(x0 + tx, L.m);
-        int cy[2], cx[2], hy[2], hx[2];
-        const int ny = p1d_halves(gy, L.n, 0, cy, hy), nx = p1d_halves(gx, L.m, 1, cx, hx);
-        T ax = 0, ay = 0;
-        bool inside = true;
-        for (int bq = 0; bq < ny; bq++)
-            for (int a = 0; a < nx; a++) {
-                int lx = cx[a] - (I0 - 2);
-                if (lx < 0) lx += C.m;
-                if (lx >= C.m) lx -= C.m;
-                const int ly = cy[bq] - (J0 - 2);
-                if (lx < 0 || lx >= TCX + 5 || ly < 0 || ly >= TCY + 5) {
+        int cy[2], hy[2];
+        const int ny = p1d_halves(gy, L.n, 0, cy, hy);
+        {
+            const int gx = wrapx(x0 + tx, L.m);
+            const int c0 = gx >> 1, c1 = (gx == L.m - 1) ? 0 : c0 + 1;
+            const bool odd = gx & 1;
+            int l0 = c0 - (I0 - 2), l1 = c1 - (I0 - 2);
+            l0 += l0 < 0 ? C.m : (l0 >= C.m ? -C.m : 0);
+            l1 += l1 < 0 ? C.m : (l1 >= C.m ? -C.m : 0);
+            T ax = 0, ay = 0;
+            bool inside = true;
+            for (int q = 0; q < ny; q++) {
+                const int ly = cy[q] - (J0 - 2);
+                if (ly < 0 || ly >= TCY + 5 || l0 < 0 || l0 >= TCX + 5 || (odd && (l1 < 0 || l1 >= TCX + 5))) {
                     inside = false;
                     continue;
                 }
-                const V v = cs[ly][lx];
-                const T wgt = (T)(hx[a] * hy[bq]) * (T)0.25;
-                ax += wgt * v.x;
-                ay += wgt * v.y;
+                const T wy = (T)hy[q] * (T)0.25;
+                if (odd) {
+                    const V v0 = cs[ly][l0], v1 = cs[ly][l1];
+                    ax += wy * (v0.x + v1.x);
+                    ay += wy * (v0.y + v1.y);
+                } else {
+                    const V v0 = cs[ly][l0];
+                    ax += (T)2 * wy * v0.x;
+                    ay += (T)2 * wy * v0.y;
+                }
             }
-        if (!inside) ax = ay = 0;
-        zs[ty][tx].x += ax;
-        zs[ty][tx].y += ay;
+            if (!inside) ax = ay = 0;
+            zs[ty][tx].x += ax;
+            zs[ty][tx].y += ay;
+        }
     }
     __syncthreads();
-    for (int p = 0; p < 4; p++) {
-        tile_lev_color<T, LUW, LUH>(L, zs, bs, x0, y0, p & 1, p >> 1, 1 + p);
-        __syncthreads();
-    }
-    for (int k = threadIdx.x; k < 4 * TCX * TCY; k += blockDim.x) {
-        const int tx = 4 + k % (2 * TCX), ty = 4 + k / (2 * TCX);
-        const int gx = x0 + tx, gy = y0 + ty;
-        if (gx >= L.m || gy >= L.n) continue;
-        L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
+    tile_lev_color<T, LUW, LUH, 1>(L, zs, bs, x0, y0, 0, 0);
+    __syncthreads();
+    tile_lev_color<T, LUW, LUH, 2>(L, zs, bs, x0, y0, 1, 0);
+    __syncthreads();
+    tile_lev_color<T, LUW, LUH, 3>(L, zs, bs, x0, y0, 0, 1);
+    __syncthreads();
+    tile_lev_color<T, LUW, LUH, 4>(L, zs, bs, x0, y0, 1, 1);
+    __syncthreads();
+    TILE_FOR(2 * TCY, 2 * TCX, 4, 4, ty, tx) {
+        const int gy = y0 + ty, gx = x0 + tx;
+        if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
     }
 }
 
 // ---------------------------------------------------------------------------
-// Tail of the V-cycle on small levels, one block: levels t..ml-1 go down
-// (clear, sweep, residual, restriction), the coarsest level is solved, and
-// the levels come back up to t (prolongation, sweep).  Phases are separated by
-// __syncthreads; the data stays in L1/L2.
+// Tail of the V-cycle on small levels, one block of 32 x 32 threads: levels
+// t..ml-1 go down (clear, sweep, residual, restriction), the coarsest level
+// is solved, and the levels come back up to t (prolongation, sweep).  All
+// levels live in shared memory; level t exchanges b and z with its global
+// arrays.  Phases are separated by __syncthreads.
 
 struct tail_levels {
     int t, ml;
@@ -1161,30 +1192,22 @@ struct tail_levels {
 template <typename T>
 __device__ void tail_sweep(const level_view<T> &L) {
     typedef typename vec2_t<T>::type V;
-    const int hm = (L.m + 1) >> 1, hn = (L.n + 1) >> 1;
     for (int cy = 0; cy < 2; cy++)
         for (int cx = 0; cx < L.colors_x; cx++) {
-            const int cnt = cx == 2 ? hn : hm * hn;
-            for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-                int i, j;
-                if (cx == 2) {
-                    i = L.m - 1;
-                    j = 2 * k + cy;
-                } else {
-                    i = 2 * (k % hm) + cx;
-                    j = 2 * (k / hm) + cy;
-                    if (L.colors_x == 3 && i == L.m - 1) continue;
+            for (int j = cy + 2 * threadIdx.y; j < L.n; j += 2 * blockDim.y) {
+                const int ist = cx == 2 ? L.m - 1 + 2 * threadIdx.x : cx + 2 * threadIdx.x;
+                for (int i = ist; i < L.m; i += 2 * blockDim.x) {
+                    if (cx < 2 && L.colors_x == 3 && i == L.m - 1) continue;
+                    const stencil9<T> &s = stencil_at(L, i, j);
+                    const size_t ij = (size_t)j * L.m + i;
+                    V a = lev_offdiag<T, V>(L, s, L.z, i, j);
+                    V r, o;
+                    r.x = L.b[ij].x - a.x;
+                    r.y = L.b[ij].y - a.y;
+                    o.x = s.e[9].a * r.x + s.e[9].b * r.y;
+                    o.y = s.e[9].c * r.x + s.e[9].d * r.y;
+                    L.z[ij] = o;
                 }
-                if (i >= L.m || j >= L.n) continue;
-                const stencil9<T> &s = stencil_at(L, i, j);
-                const size_t ij = (size_t)j * L.m + i;
-                V a = lev_offdiag<T, V>(L, s, L.z, i, j);
-                V r, o;
-                r.x = L.b[ij].x - a.x;
-                r.y = L.b[ij].y - a.y;
-                o.x = s.e[9].a * r.x + s.e[9].b * r.y;
-                o.y = s.e[9].c * r.x + s.e[9].d * r.y;
-                L.z[ij] = o;
             }
             __syncthreads();
         }
@@ -1196,8 +1219,6 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
     extern __shared__ __align__(16) unsigned char tail_raw[];
     double *tsh = (double *)tail_raw;
     V *p = (V *)(tail_raw + ((sizeof(double) * tl.inv_n + 15) & ~(size_t)15));
-    // every level of the tail lives in shared memory; level t exchanges b
-    // and z with its global arrays
     level_view<T> S[17];
     for (int l = tl.t; l <= tl.ml; l++) {
         S[l] = H.lv[l];
@@ -1209,66 +1230,70 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
         S[l].r = p;
         p += mn;
     }
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
     {
         const int mn = S[tl.t].m * S[tl.t].n;
-        for (int k = threadIdx.x; k < mn; k += blockDim.x) S[tl.t].b[k] = H.lv[tl.t].b[k];
+        for (int k = tid; k < mn; k += nth) S[tl.t].b[k] = H.lv[tl.t].b[k];
     }
     __syncthreads();
     for (int i = tl.t; i < tl.ml; i++) {
         const level_view<T> &L = S[i];
         const int mn = L.m * L.n;
-        for (int k = threadIdx.x; k < mn; k += blockDim.x) {
+        for (int k = tid; k < mn; k += nth) {
             L.z[k].x = 0;
             L.z[k].y = 0;
         }
         __syncthreads();
         tail_sweep(L);
-        for (int k = threadIdx.x; k < mn; k += blockDim.x) {
-            const int ii = k % L.m, jj = k / L.m;
-            const stencil9<T> &s = stencil_at(L, ii, jj);
-            V a = lev_offdiag<T, V>(L, s, L.z, ii, jj);
-            madd(a, s.e[4], L.z[k]);
-            V r;
-            r.x = L.b[k].x - a.x;
-            r.y = L.b[k].y - a.y;
-            L.r[k] = r;
-        }
+        for (int jj = threadIdx.y; jj < L.n; jj += blockDim.y)
+            for (int ii = threadIdx.x; ii < L.m; ii += blockDim.x) {
+                const size_t k = (size_t)jj * L.m + ii;
+                const stencil9<T> &s = stencil_at(L, ii, jj);
+                V a = lev_offdiag<T, V>(L, s, L.z, ii, jj);
+                madd(a, s.e[4], L.z[k]);
+                V r;
+                r.x = L.b[k].x - a.x;
+                r.y = L.b[k].y - a.y;
+                L.r[k] = r;
+            }
         __syncthreads();
         const level_view<T> &C = S[i + 1];
-        for (int k = threadIdx.x; k < C.m * C.n; k += blockDim.x) {
-            const int I = k % C.m, J = k / C.m;
-            T ax = 0, ay = 0;
-            for (int dy = -1; dy <= 1; dy++) {
-                const int fy = 2 * J + dy;
-                if (fy < 0 || fy >= L.n) continue;
-                const int hy = halves_of(fy, L.n, 0, J);
-                if (!hy) continue;
-                for (int dx = -1; dx <= 1; dx++) {
-                    const int fx = wrapx(2 * I + dx, L.m);
-                    const int hx = halves_of(fx, L.m, 1, I);
-                    if (!hx) continue;
-                    const V v = L.r[(size_t)fy * L.m + fx];
-                    const T wgt = (T)(hx * hy) * (T)0.25;
-                    ax += wgt * v.x;
-                    ay += wgt * v.y;
+        for (int J = threadIdx.y; J < C.n; J += blockDim.y)
+            for (int I = threadIdx.x; I < C.m; I += blockDim.x) {
+                T ax = 0, ay = 0;
+                for (int dy = -1; dy <= 1; dy++) {
+                    const int fy = 2 * J + dy;
+                    if (fy < 0 || fy >= L.n) continue;
+                    const int hy = halves_of(fy, L.n, 0, J);
+                    if (!hy) continue;
+                    for (int dx = -1; dx <= 1; dx++) {
+                        const int fx = wrapx(2 * I + dx, L.m);
+                        const int hx = halves_of(fx, L.m, 1, I);
+                        if (!hx) continue;
+                        const V v = L.r[(size_t)fy * L.m + fx];
+                        const T wgt = (T)(hx * hy) * (T)0.25;
+                        ax += wgt * v.x;
+                        ay += wgt * v.y;
+                    }
                 }
+                V o;
+                o.x = ax;
+                o.y = ay;
+                C.b[(size_t)J * C.m + I] = o;
             }
-            C.b[k].x = ax;
-            C.b[k].y = ay;
-        }
         __syncthreads();
     }
     // coarsest level: z = A^-1 b in FP64
     {
         const level_view<T> &B = S[tl.ml];
         const int N = tl.inv_n;
-        for (int k = threadIdx.x; k < N / 2; k += blockDim.x) {
+        for (int k = tid; k < N / 2; k += nth) {
             tsh[2 * k] = (double)B.b[k].x;
             tsh[2 * k + 1] = (double)B.b[k].y;
         }
         __syncthreads();
         T *zz = (T *)B.z;
-        for (int r = threadIdx.x; r < N; r += blockDim.x) {
+        for (int r = tid; r < N; r += nth) {
             const double *row = tl.inv + (size_t)r * N;
             double a = 0;
             for (int k = 0; k < N; k++) a += row[k] * tsh[k];
@@ -1278,27 +1303,31 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
     }
     for (int i = tl.ml; i > tl.t; i--) {
         const level_view<T> &C = S[i], &F = S[i - 1];
-        for (int k = threadIdx.x; k < F.m * F.n; k += blockDim.x) {
-            const int ii = k % F.m, jj = k / F.m;
-            int cy[2], cx[2], hy[2], hx[2];
-            const int ny = p1d_halves(jj, F.n, 0, cy, hy), nx = p1d_halves(ii, F.m, 1, cx, hx);
-            T ax = 0, ay = 0;
-            for (int bq = 0; bq < ny; bq++)
-                for (int a = 0; a < nx; a++) {
-                    const V v = C.z[(size_t)cy[bq] * C.m + cx[a]];
-                    const T wgt = (T)(hx[a] * hy[bq]) * (T)0.25;
-                    ax += wgt * v.x;
-                    ay += wgt * v.y;
-                }
-            F.z[k].x += ax;
-            F.z[k].y += ay;
+        for (int jj = threadIdx.y; jj < F.n; jj += blockDim.y) {
+            int cy[2], hy[2];
+            const int ny = p1d_halves(jj, F.n, 0, cy, hy);
+            for (int ii = threadIdx.x; ii < F.m; ii += blockDim.x) {
+                int cx[2], hx[2];
+                const int nx = p1d_halves(ii, F.m, 1, cx, hx);
+                T ax = 0, ay = 0;
+                for (int bq = 0; bq < ny; bq++)
+                    for (int a = 0; a < nx; a++) {
+                        const V v = C.z[(size_t)cy[bq] * C.m + cx[a]];
+                        const T wgt = (T)(hx[a] * hy[bq]) * (T)0.25;
+                        ax += wgt * v.x;
+                        ay += wgt * v.y;
+                    }
+                const size_t k = (size_t)jj * F.m + ii;
+                F.z[k].x += ax;
+                F.z[k].y += ay;
+            }
         }
         __syncthreads();
         tail_sweep(F);
     }
     {
         const int mn = S[tl.t].m * S[tl.t].n;
-        for (int k = threadIdx.x; k < mn; k += blockDim.x) H.lv[tl.t].z[k] = S[tl.t].z[k];
+        for (int k = tid; k < mn; k += nth) H.lv[tl.t].z[k] = S[tl.t].z[k];
     }
 }
 
@@ -1335,7 +1364,7 @@ template <typename T> void top_sweep(hierarchy<T> &h, cudaStream_t st) {
     level_view<T> &L = h.lv[0];
     dim3 blk(32, 8);
     for (int c = 0; c < 2; c++) {
-        k_top_color<T><<<grid2(L.m, L.n, blk), blk, 0, st>>>(h.op, L.z, L.b, L.m, L.n, c);
+        k_top_color<T><<<grid2((L.m + 1) / 2, L.n, blk), blk, 0, st>>>(h.op, L.z, L.b, L.m, L.n, c);
         note_launch();
     }
 }
@@ -1382,7 +1411,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     const int t = tail_start(h);
     if (fused) {
         dim3 g(ceil_div(h.lv[1].m, TCX), ceil_div(h.lv[1].n, TCY));
-        k_top_down<T><<<g, kFusedThreads, 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].b, h.lv[1].m, h.lv[1].n);
+        k_top_down<T><<<g, dim3(32, 8), 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].b, h.lv[1].m, h.lv[1].n);
         note_launch();
     } else {
         top_sweep(h, st);
@@ -1398,7 +1427,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         level_view<T> &C = h.lv[i + 1];
         if (tile_level(L)) {
             dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
-            k_lev_down<T><<<g, kFusedThreads, 0, st>>>(L, C);
+            k_lev_down<T><<<g, dim3(32, 8), 0, st>>>(L, C);
             note_launch();
             continue;
         }
@@ -1415,7 +1444,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         for (int l = 0; l < h.nl; l++) hv.lv[l] = h.lv[l];
         tail_levels tl{t, ml, h.bottom_inv, h.bottom_unknowns};
         const size_t smem = tail_smem_bytes(h, t);
-        k_tail<T><<<1, 1024, smem, st>>>(tl, hv);
+        k_tail<T><<<1, dim3(32, 32), smem, st>>>(tl, hv);
         note_launch();
         up_from = t;
     } else {
@@ -1434,7 +1463,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         level_view<T> &C = h.lv[i], &F = h.lv[i - 1];
         if (tile_level(F)) {
             dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
-            k_lev_up<T><<<g, kFusedThreads, 0, st>>>(F, C);
+            k_lev_up<T><<<g, dim3(32, 8), 0, st>>>(F, C);
             note_launch();
             continue;
         }
@@ -1444,7 +1473,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     }
     if (fused) {
         dim3 g(ceil_div(h.lv[1].m, TCX), ceil_div(h.lv[1].n, TCY));
-        k_top_up<T><<<g, kFusedThreads, 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].z, h.lv[1].m, h.lv[1].n);
+        k_top_up<T><<<g, dim3(32, 8), 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].z, h.lv[1].m, h.lv[1].n);
         note_launch();
     } else {
         k_prolong_add<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.lv[1].z, h.lv[1].m, h.lv[1].n, T0.z, T0.m,
