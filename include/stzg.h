@@ -175,6 +175,40 @@ int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
 int stzg_residual_norms_noalloc(const stz_params *p, double dt, const double *z_dev, const double *b_dev,
                                 double *out_dev, void *stream);
 
+/* ---- batches -----------------------------------------------------------
+ * No single counterpart in the reference, whose drivers run one shear_sim
+ * per process (the UQ harness, esim/coord_transforms/simple_shear/pfn.py,
+ * launches one process per sample).  A batch owns `count` independent
+ * simulations (params[k] each; grids may differ) and runs them together in
+ * one CUDA graph: per instance a device-side loop over time steps, each step
+ * with a device-side multigrid loop (same stopping rule as stzg_step_qs,
+ * bounded at 400 passes).  stzg_batch_sim exposes instance k as an ordinary
+ * handle (set_state, get_field, ...; do not destroy it). */
+typedef struct stzg_batch stzg_batch;
+typedef struct {
+    long instances, steps, cell_steps;
+    long vcycles, passes, failed;
+    double seconds;          /* device time of the graph launch (CUDA events) */
+    long graph_kernels;      /* kernel nodes in the graph */
+    long kernel_launches;    /* kernels executed (loop bodies counted per iteration) */
+} stzg_batch_stats;
+
+int stzg_batch_create(int count, const stz_params *params, const stzg_options *opt, stzg_batch **out);
+int stzg_batch_destroy(stzg_batch *b);
+int stzg_batch_size(stzg_batch *b, int *count);
+int stzg_batch_sim(stzg_batch *b, int k, stzg_sim **s);
+/* Schedule knobs for instances of grid m x n (cells): FP32 V-cycles per
+ * refinement pass, largest level (points) solved by the single-block tail
+ * (<0: default), fused single-precision tile kernels on/off. */
+int stzg_batch_set_tuning(stzg_batch *b, int m, int n, int inner, long tail_limit, int fuse);
+/* Times the candidate knobs on the GPU for every grid size of the batch
+ * (`steps` steps each, on scratch instances) and installs the fastest. */
+int stzg_batch_autotune(stzg_batch *b, double dt, int steps);
+int stzg_batch_get_tuning(stzg_batch *b, int m, int n, int *inner, long *tail_limit, int *fuse);
+/* Replaces: shear_sim::step_forward_quasistatic (shear_sim.cc:280-291)
+ * nsteps times on every instance, in one graph launch. */
+int stzg_batch_run(stzg_batch *b, double dt, int nsteps, stzg_batch_stats *stats);
+
 /* Replaces: shear_sim::l2_comparison (shear_sim.cc:460-502) between two
  * handles of the same grid: l2[4] = velocity, stress, chi, reference map. */
 int stzg_l2_comparison(stzg_sim *a, stzg_sim *b, double *l2);

@@ -30,6 +30,8 @@ EXPORTS = [
     "stzg_mg_solve", "stzg_mg_vcycle", "stzg_mg_l2_error", "stzg_mg_levels", "stzg_mg_stencil",
     "stzg_l2_comparison", "stzg_random_chi", "stzg_upload", "stzg_download", "stzg_time_kernel",
     "stzg_residual_norms_noalloc",
+    "stzg_batch_create", "stzg_batch_destroy", "stzg_batch_size", "stzg_batch_sim", "stzg_batch_set_tuning",
+    "stzg_batch_autotune", "stzg_batch_get_tuning", "stzg_batch_run",
 ]
 
 
@@ -45,6 +47,15 @@ class StzgStats(ctypes.Structure):
                 ("refinements", ctypes.c_long), ("checks", ctypes.c_long), ("last_error", ctypes.c_double),
                 ("seconds", ctypes.c_double), ("substeps_max", ctypes.c_long),
                 ("kernel_launches", ctypes.c_long)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class StzgBatchStats(ctypes.Structure):
+    _fields_ = [("instances", ctypes.c_long), ("steps", ctypes.c_long), ("cell_steps", ctypes.c_long),
+                ("vcycles", ctypes.c_long), ("passes", ctypes.c_long), ("failed", ctypes.c_long),
+                ("seconds", ctypes.c_double), ("graph_kernels", ctypes.c_long), ("kernel_launches", ctypes.c_long)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -99,6 +110,14 @@ def load(path=None):
         "stzg_time_kernel": (I, [V, D, I, I, _P]),
         "stzg_residual_norms_noalloc": (I, [ctypes.POINTER(StzParams), D, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_void_p]),
+        "stzg_batch_create": (I, [I, ctypes.POINTER(StzParams), ctypes.POINTER(StzgOptions), ctypes.POINTER(V)]),
+        "stzg_batch_destroy": (I, [V]),
+        "stzg_batch_size": (I, [V, ctypes.POINTER(I)]),
+        "stzg_batch_sim": (I, [V, I, ctypes.POINTER(V)]),
+        "stzg_batch_set_tuning": (I, [V, I, I, I, ctypes.c_long, I]),
+        "stzg_batch_autotune": (I, [V, D, I]),
+        "stzg_batch_get_tuning": (I, [V, I, I, ctypes.POINTER(I), ctypes.POINTER(ctypes.c_long), ctypes.POINTER(I)]),
+        "stzg_batch_run": (I, [V, D, I, ctypes.POINTER(StzgBatchStats)]),
     }
     for name, (res, args) in decl.items():
         f = getattr(lib, name)

@@ -18,6 +18,7 @@ static std::atomic<long> g_launches(0);
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void discount_launches(long k) { g_launches.fetch_sub(k, std::memory_order_relaxed); }
 
 int fail(int status, const std::string &msg) {
     g_msg = msg;
@@ -34,41 +35,9 @@ int cuda_fail(cudaError_t e, const char *what) {
 
 using namespace stzg;
 
-struct stzg_sim {
-    stz_params P;
-    stzg_options O;
-    int m, n;
-    double time = 0;
-    double bv_state = 0;  // wall speed of the stored state (u=-bv on row 0, +bv on row n)
-    cudaStream_t st = nullptr;
-    step_consts sc;
-    fields_dev F;
-    int cur = 0;
-    std::vector<void *> owned;
-    // multigrid
-    qs_constants q;
-    double viscdt = -1;
-    std::vector<level_ops> ops;
-    hierarchy<double> h64;
-    hierarchy<float> h32;
-    double *partials = nullptr;  // device, 2 per block
-    double *dnorm = nullptr;     // device: [r2, b2]
-    double *hnorm = nullptr;     // pinned host copy
-    int npart = 0;
-    // tgmg_predict state (tgmg_predict.hh:6-33, tgmg_config.hh:26-45)
-    int lim = 16 * 8, mult = 16, decay = 32, max_thresh = 16 * 2048, extra_iters = 1;
-    long avg_vcount = 0, avg_solves = 0;
-    stzg_stats acc{};
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // captured graphs: one FP64 V-cycle; mixed: initial residual, one pass
-    cudaGraphExec_t g_vc64 = nullptr, g_res32 = nullptr, g_pass32 = nullptr;
-    long n_vc64 = 0, n_res32 = 0, n_pass32 = 0;  // kernel nodes per graph
-    int g_inner = 0;
-    double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)
-    bool have_prev = false;
-};
+#include "sim.cuh"
 
-namespace {
+namespace stzg {
 
 int dev_alloc(stzg_sim *s, void **p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes);
@@ -322,7 +291,7 @@ int check_flags(stzg_sim *s) {
 
 size_t cell_count(const stzg_sim *s) { return (size_t)s->m * (s->n + 2); }
 
-}  // namespace
+}  // namespace stzg
 
 extern "C" {
 

@@ -50,6 +50,8 @@ inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 // while a stream is being captured belong to the captured graph).
 void note_launch();
 long launch_count();
+// Removes launches that were recorded while capturing a graph.
+void discount_launches(long k);
 
 // Device-wide numbers used for grid sizing.
 struct device_info {

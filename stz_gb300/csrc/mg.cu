@@ -1384,7 +1384,7 @@ template <typename T> static void lev_sweep(level_view<T> &L, cudaStream_t st) {
 template <typename T> static int tail_start(const hierarchy<T> &h) {
     const int ml = h.nl - 1;
     if (ml < 1 || !h.bottom_inv) return ml + 1;
-    const long limit = sizeof(T) == 4 ? 4400 : 300;
+    const long limit = h.tail_limit >= 0 ? h.tail_limit : (sizeof(T) == 4 ? 4400 : 300);
     int t = ml;
     while (t > 1 && (long)h.lv[t - 1].m * h.lv[t - 1].n <= limit && tail_smem_bytes(h, t - 1) <= kTailSmem) t--;
     if (tail_smem_bytes(h, t) > kTailSmem) return ml + 1;
@@ -1393,8 +1393,8 @@ template <typename T> static int tail_start(const hierarchy<T> &h) {
 
 // Levels wide enough for the single-precision tile kernels (an even periodic
 // line that the halo cannot wrap onto itself).
-template <typename T> static bool tile_level(const level_view<T> &L) {
-    return sizeof(T) == 4 && L.colors_x == 2 && L.m >= kFusedMinWidth;
+template <typename T> static bool tile_level(const hierarchy<T> &h, const level_view<T> &L) {
+    return h.fuse && sizeof(T) == 4 && L.colors_x == 2 && L.m >= kFusedMinWidth;
 }
 
 template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64) {
@@ -1402,7 +1402,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     dim3 blk(32, 8);
     const int ml = h.nl - 1;
     level_view<T> &T0 = h.lv[0];
-    const bool fused = sizeof(T) == 4 && ml > 0 && T0.m >= kFusedMinWidth;
+    const bool fused = h.fuse && sizeof(T) == 4 && ml > 0 && T0.m >= kFusedMinWidth;
     if (ml == 0) {
         top_sweep(h, st);
         top_sweep(h, st);
@@ -1425,7 +1425,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     for (int i = 1; i < down_end; i++) {
         level_view<T> &L = h.lv[i];
         level_view<T> &C = h.lv[i + 1];
-        if (tile_level(L)) {
+        if (tile_level(h, L)) {
             dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
             k_lev_down<T><<<g, dim3(32, 8), 0, st>>>(L, C);
             note_launch();
@@ -1461,7 +1461,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     }
     for (int i = up_from; i >= 2; i--) {
         level_view<T> &C = h.lv[i], &F = h.lv[i - 1];
-        if (tile_level(F)) {
+        if (tile_level(h, F)) {
             dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
             k_lev_up<T><<<g, dim3(32, 8), 0, st>>>(F, C);
             note_launch();

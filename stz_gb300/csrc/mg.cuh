@@ -89,6 +89,11 @@ template <typename T> class hierarchy {
     // exact coarsest solve z = A^-1 b in FP64 (nullptr: Gauss-Seidel sweeps)
     const double *bottom_inv = nullptr;
     int bottom_unknowns = 0;
+    // schedule knobs (autotuned per grid size for batches): largest level
+    // (points) handled by the single-block tail (<0: default by precision),
+    // and whether wide single-precision levels use the fused tile kernels
+    long tail_limit = -1;
+    int fuse = 1;
     void release();
     ~hierarchy() { release(); }
     size_t device_bytes() const { return bytes_; }

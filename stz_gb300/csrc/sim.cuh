@@ -1,0 +1,58 @@
+// The simulation handle behind the C ABI and the internal operations that
+// the single-simulation path (api.cu) and the batched graph (batch.cu) share.
+#pragma once
+
+#include <vector>
+
+#include "mg.cuh"
+#include "step.cuh"
+
+struct stzg_sim {
+    stz_params P;
+    stzg_options O;
+    int m, n;
+    double time = 0;
+    double bv_state = 0;  // wall speed of the stored state (u=-bv on row 0, +bv on row n)
+    cudaStream_t st = nullptr;
+    stzg::step_consts sc;
+    stzg::fields_dev F;
+    int cur = 0;
+    std::vector<void *> owned;
+    // multigrid
+    stzg::qs_constants q;
+    double viscdt = -1;
+    std::vector<stzg::level_ops> ops;
+    stzg::hierarchy<double> h64;
+    stzg::hierarchy<float> h32;
+    double *partials = nullptr;  // device, 2 per block
+    double *dnorm = nullptr;     // device: [r2, b2]
+    double *hnorm = nullptr;     // pinned host copy
+    int npart = 0;
+    // tgmg_predict state (tgmg_predict.hh:6-33, tgmg_config.hh:26-45)
+    int lim = 16 * 8, mult = 16, decay = 32, max_thresh = 16 * 2048, extra_iters = 1;
+    long avg_vcount = 0, avg_solves = 0;
+    stzg_stats acc{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // captured graphs: one FP64 V-cycle; mixed: initial residual, one pass
+    cudaGraphExec_t g_vc64 = nullptr, g_res32 = nullptr, g_pass32 = nullptr;
+    long n_vc64 = 0, n_res32 = 0, n_pass32 = 0;  // kernel nodes per graph
+    int g_inner = 0;
+    double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)
+    bool have_prev = false;
+};
+
+
+namespace stzg {
+
+int dev_alloc(stzg_sim *s, void **p, size_t bytes);
+double bdry_vel(const stzg_sim *s, double t);
+double bdry_pos(const stzg_sim *s, double t);
+int validate(const stz_params *p);
+void drop_graphs(stzg_sim *s);
+int ensure_ops(stzg_sim *s, double dt);
+void launch_norms(stzg_sim *s, bool mixed);
+int read_check(stzg_sim *s, double *err, bool *ok);
+int check_flags(stzg_sim *s);
+size_t cell_count(const stzg_sim *s);
+
+}  // namespace stzg

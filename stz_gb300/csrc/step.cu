@@ -35,6 +35,8 @@ step_consts make_step_consts(const stz_params &p) {
     c.chi_len = p.chi_len;
     c.track_plastic = 0;
     c.substep_cap = 1 << 22;
+    c.clock = nullptr;
+    c.xbc = 0;
     return c;
 }
 
@@ -161,12 +163,14 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= m || j >= n) return;
+    if (c.clock) cur = (int)c.clock[CLK_CUR];
     const double *__restrict__ const *A = F.f[cur];
     double *const *B = F.f[cur ^ 1];
     const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt, lx = c.lx;
     const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
     const int il2 = i <= 1 ? i + m - 2 : i - 2, ir2 = i >= m - 2 ? i + 2 - m : i + 2;
     const size_t ci = IDX(i, j);
+    if (c.clock) bv = c.clock[CLK_BV_STATE];
     velo V{F.vel, m, n, bv};
     double uc, vc;
     // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
@@ -280,6 +284,7 @@ __global__ void k_precombine(step_consts c, fields_dev F, int cur, double xf, do
 // chi_diffusion (shear_sim.cc:364-386): B.chi holds cchi; old chi in A.
 __global__ void k_chi_diffusion(step_consts c, fields_dev F, int cur, double dt) {
     const int m = c.m, n = c.n;
+    if (c.clock) cur = (int)c.clock[CLK_CUR];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= m || j >= n) return;
@@ -304,6 +309,7 @@ __global__ void k_chi_diffusion(step_consts c, fields_dev F, int cur, double dt)
 // walls.
 __global__ void k_source(step_consts c, fields_dev F, double xbc_bv) {
     const int m = c.m, n = c.n;
+    if (c.clock) xbc_bv = c.xbc * c.clock[CLK_BV];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= m || j > n) return;
@@ -327,6 +333,7 @@ __global__ void k_source(step_consts c, fields_dev F, double xbc_bv) {
 // Stress correction from the solved velocity (shear_sim.cc:418-434).
 __global__ void k_project(step_consts c, fields_dev F, int cur, double hx, double hy) {
     const int m = c.m, n = c.n;
+    if (c.clock) cur = (int)c.clock[CLK_CUR] ^ 1;  // the state the advection wrote
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= m || j >= n) return;
@@ -349,6 +356,10 @@ __global__ void k_project(step_consts c, fields_dev F, int cur, double hx, doubl
 // advection kernel takes them as arguments.
 __global__ void k_boundaries(step_consts c, fields_dev F, int cur, double bp) {
     const int m = c.m, n = c.n;
+    if (c.clock) {
+        bp = c.clock[CLK_BP];
+        cur = (int)c.clock[CLK_CUR] ^ 1;
+    }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     double *const *S = F.f[cur];

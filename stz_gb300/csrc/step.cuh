@@ -35,7 +35,16 @@ struct step_consts {
     double chi_diff, chi_len;
     int track_plastic;
     int substep_cap;
+    // Device clock of a graph-driven run (nullptr: wall quantities come as
+    // kernel arguments from the host).  Layout: CLK_* below.
+    const double *clock;
+    double xbc;  // bcs*cxx of the projection operator (wall source = -+xbc*bv)
 };
+
+// Device clock slots: time, wall speed of the stored state, wall speed and
+// wall position at `time` (shear_sim.hh:120-124).
+// CLK_CUR holds the state buffer index at the start of the step.
+enum { CLK_TIME = 0, CLK_BV_STATE = 1, CLK_BV = 2, CLK_BP = 3, CLK_CUR = 4, CLK_COUNT = 5 };
 
 step_consts make_step_consts(const stz_params &p);
 

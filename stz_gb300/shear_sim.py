@@ -53,11 +53,24 @@ class ShearSim:
         if chi is not None:
             self.set_state(chi)
 
+    @classmethod
+    def view(cls, handle, params):
+        """Non-owning wrapper of a handle that belongs to a batch."""
+        self = cls.__new__(cls)
+        self.lib = _lib.load()
+        self.params = params.copy()
+        self.m, self.n = params.m, params.n
+        self.h = handle
+        self.cycles = 0
+        self.stats = _lib.StzgStats()
+        self._owned = False
+        return self
+
     # -- lifetime ---------------------------------------------------------
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "_owned", True):
             self.lib.stzg_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
