@@ -1,6 +1,7 @@
 // Time-step kernels: fused ENO advection + STZ plasticity, chi diffusion,
 // projection source, stress correction and boundaries.
 #include "step.cuh"
+#include "stz_law.cuh"
 
 namespace stzg {
 
@@ -45,101 +46,6 @@ namespace {
 __device__ __forceinline__ double eno2(double p0, double p1, double p2, double p3) {
     // shear_sim::eno2, shear_sim.cc:653-655
     return fabs(p0 - 2 * p1 + p2) > fabs(p1 - 2 * p2 + p3) ? 3 * p1 - 4 * p2 + p3 : p0 - p2;
-}
-
-// STZ plastic rate (stz_model.hh:9-207) with the yield stress s_y in place
-// of the reference's unit s0 and `sbar<1`.
-__device__ double dplastic(const step_consts &c, double sbar, double chi, double &dchi1, double &dchi2) {
-    const double s0 = c.s_y, thetainv = 1 / c.theta;
-    const double Om = c.Omegaeps0, De = c.Delta, tau0 = c.tau0;
-    if (c.stz_model == 0 || c.stz_model == 1) {
-        double sC1, sC2, sC, sT;
-        if (c.stz_model == 0) {  // stz_model.hh:58-67
-            sC1 = exp(-De * thetainv);
-            sC2 = cosh(Om * sbar * thetainv);
-            sC = sC1 * sC2;
-            sT = tanh(Om * sbar * thetainv);
-        } else {  // stz_model.hh:76-87
-            double x = Om * sbar / De;
-            sC1 = exp(-De * thetainv);
-            sC = exp(-De * cosh(x) * thetainv) * cosh(De * sinh(x) * thetainv);
-            sC2 = sC / sC1;
-            sT = tanh(De * sinh(x) * thetainv);
-        }
-        // Dplastic_common, stz_model.hh:30-48
-        double sbart = sbar > 1e-12 ? sbar : 1e-12, bfac = exp(-1 / chi);
-        double pM = 1 + sbart * sT / s0 + c.rho / (2 * sC2);
-        double M = s0 / (2 * sbart) * (pM - sqrt(pM * pM - 4 * sbart * sT / s0));
-        double Dpl = bfac * sC * (sT - M) / tau0;
-        double Gamma = 2 * tau0 * Dpl * sbar / (s0 * bfac);
-        bfac /= tau0 * c.c0;
-        dchi1 = bfac * Gamma;
-        dchi2 = bfac * c.kappa * sC1 * c.rho;
-        return Dpl;
-    }
-    dchi2 = 0;
-    if (sbar < s0) {
-        dchi1 = 0;
-        return 0;
-    }
-    double sC, sT;
-    if (c.stz_model == 3) {  // stz_model.hh:179-206
-        double x = Om * sbar / De;
-        sC = 0.5 * (exp(-De * thetainv * exp(x)) + exp(-De * thetainv * exp(-x)));
-        sT = tanh(De * sinh(x) * thetainv);
-    } else {  // stz_model.hh:103-151
-        const int tm = c.t_model;
-        if (tm == -1 || De >= Om * sbar) {
-            sC = 0.5 * (exp((Om * sbar - De) * thetainv) + exp((-Om * sbar - De) * thetainv));
-        } else {
-            double tmp;
-            switch (tm) {
-                case 0: sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + 1); break;
-                case 1: tmp = Om * sbar / De;
-                        sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + sqrt(0.5 * (1 + tmp * tmp))); break;
-                case 2: tmp = Om * sbar / De;
-                        sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + (0.5 * (1 + tmp * tmp))); break;
-                case 3: sC = sbar * (0.5 * Om / De); break;  // t_icpt=0, t_grad=Omegaeps0/(2 Delta)
-                case 4: sC = 0.5 * (exp((-Om * sbar - De) * thetainv) + (Om * sbar - De) * thetainv + 1); break;
-                default: sC = 0;
-            }
-        }
-        sT = tm != 3 ? tanh(Om * sbar * thetainv) : 1;
-    }
-    double bfac = exp(-1 / chi);
-    double Dpl = bfac * sC * (sT - s0 / sbar) / tau0;
-    double Gamma = 2 * tau0 * Dpl * sbar / (s0 * bfac);
-    dchi1 = bfac * Gamma / (tau0 * c.c0);
-    return Dpl;
-}
-
-// shear_sim::adaptive_plastic_term, shear_sim.cc:513-548, with an iteration
-// cap (the reference loop has none and never ends in stiff regimes).
-__device__ double adaptive_plastic(const step_consts &c, double sbar, double &chiv, double &ddev, double dt,
-                                   int &iters) {
-    const double theta_loc = 0;
-    iters = 0;
-    if (sbar < 1e-12) {
-        ddev = 0;
-        return 0;
-    }
-    double dtl = dt, osbar = sbar, dplas, dchi1, dchi2, adt;
-    bool adapt = true;
-    do {
-        dplas = 2 * c.t_scale * c.mu * dplastic(c, sbar, chiv, dchi1, dchi2);
-        if (fabs(dtl * dplas) > c.adapt_fac) {
-            adt = c.adapt_fac / fabs(dplas);
-            dtl -= adt;
-        } else {
-            adapt = false;
-            adt = dtl;
-        }
-        sbar -= adt * dplas;
-        chiv += (dchi1 * (c.chi_inf - chiv) + dchi2 * (theta_loc - chiv)) * c.t_scale * adt;
-        if (++iters >= c.substep_cap) break;
-    } while (adapt);
-    ddev = osbar - sbar;
-    return ddev == 0 ? 0.0 : ddev / osbar;
 }
 
 struct velo {
@@ -242,7 +148,8 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
         dtmp = 0;
     } else {
         int iters;
-        dtmp = adaptive_plastic(c, sqrt(devsq), cchi, ddev, dt, iters);
+        const stz_law_params<double> lp = law_params(c);
+        dtmp = adaptive_plastic(lp, sqrt(devsq), cchi, ddev, dt, iters);
         if (iters >= c.substep_cap) atomicExch(&F.flags[0], 1);
         if (iters > 1) atomicMax(&F.flags[1], iters);
     }
