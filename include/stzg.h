@@ -209,6 +209,26 @@ int stzg_batch_get_tuning(stzg_batch *b, int m, int n, int *inner, long *tail_li
  * nsteps times on every instance, in one graph launch. */
 int stzg_batch_run(stzg_batch *b, double dt, int nsteps, stzg_batch_stats *stats);
 
+/* ---- adjoint -----------------------------------------------------------
+ * No counterpart in the reference, which has no gradients.  A forward/
+ * backward pair shaped like torch.autograd.Function around `nsteps`
+ * quasi-static steps (shear_sim::step_forward_quasistatic, shear_sim.cc:
+ * 280-291) from the handle's current state, with the loss
+ *     L = dx dy sum_cells (eps_pl - target)^2
+ * on the plastic strain after the last step (target: m*n doubles on the
+ * host).  The forward pass steps the handle, stores a checkpoint every
+ * `checkpoint_every` steps and writes L.  The backward pass recomputes each
+ * segment from its checkpoint, runs the hand-written adjoint of every step
+ * in reverse and writes dloss * dL/dp for p = (c0, Omega*eps0, chi_inf,
+ * s_y) into grad_params[4] and dloss * dL/d chi(t=0) (m*n) into grad_chi0
+ * (either may be NULL); the handle is left at the forward run's end state.
+ * Requires track_plastic and no chi diffusion (chi_diff = chi_len = 0);
+ * branch decisions (ENO stencils, upwind sides, yield, sub-step counts) are
+ * those of the forward run. */
+int stzg_adjoint_forward(stzg_sim *s, double dt, int nsteps, int checkpoint_every, const double *target,
+                         double *loss);
+int stzg_adjoint_backward(stzg_sim *s, double dloss, double *grad_params, double *grad_chi0);
+
 /* Replaces: shear_sim::l2_comparison (shear_sim.cc:460-502) between two
  * handles of the same grid: l2[4] = velocity, stress, chi, reference map. */
 int stzg_l2_comparison(stzg_sim *a, stzg_sim *b, double *l2);

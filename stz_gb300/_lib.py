@@ -32,6 +32,7 @@ EXPORTS = [
     "stzg_residual_norms_noalloc",
     "stzg_batch_create", "stzg_batch_destroy", "stzg_batch_size", "stzg_batch_sim", "stzg_batch_set_tuning",
     "stzg_batch_autotune", "stzg_batch_get_tuning", "stzg_batch_run",
+    "stzg_adjoint_forward", "stzg_adjoint_backward",
 ]
 
 
@@ -118,6 +119,8 @@ def load(path=None):
         "stzg_batch_autotune": (I, [V, D, I]),
         "stzg_batch_get_tuning": (I, [V, I, I, ctypes.POINTER(I), ctypes.POINTER(ctypes.c_long), ctypes.POINTER(I)]),
         "stzg_batch_run": (I, [V, D, I, ctypes.POINTER(StzgBatchStats)]),
+        "stzg_adjoint_forward": (I, [V, D, I, I, _P, _P]),
+        "stzg_adjoint_backward": (I, [V, D, _P, _P]),
     }
     for name, (res, args) in decl.items():
         f = getattr(lib, name)

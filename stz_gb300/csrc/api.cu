@@ -382,6 +382,7 @@ int stzg_destroy(stzg_sim *s) {
     if (!s) return STZG_OK;
     if (s->st) cudaStreamSynchronize(s->st);
     drop_graphs(s);
+    adjoint_release(s);
     for (void *p : s->owned) cudaFree(p);
     s->h64.release();
     s->h32.release();

@@ -7,6 +7,8 @@
 #include "mg.cuh"
 #include "step.cuh"
 
+struct stzg_adjoint;
+
 struct stzg_sim {
     stz_params P;
     stzg_options O;
@@ -39,6 +41,7 @@ struct stzg_sim {
     int g_inner = 0;
     double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)
     bool have_prev = false;
+    stzg_adjoint *adj = nullptr;  // adjoint workspace (adjoint.cu), created on first use
 };
 
 
@@ -54,5 +57,6 @@ void launch_norms(stzg_sim *s, bool mixed);
 int read_check(stzg_sim *s, double *err, bool *ok);
 int check_flags(stzg_sim *s);
 size_t cell_count(const stzg_sim *s);
+void adjoint_release(stzg_sim *s);
 
 }  // namespace stzg

@@ -90,6 +90,33 @@ def plastic_shear(N, M=None, **kw):
     return simple_shear(N, M, **kw)
 
 
+def adjoint_shear(N, M=None, **kw):
+    """Plastic-active shear for gradient checks: 100 steps of ADJOINT_DT.
+
+    Linear thermal STZ law (stz_model.hh:58-67), which has no yield kink.
+    Walls at +-8 with the ramp u = 8 t reach a CFL number of 0.41 at t = 0.2
+    on a 256-cell line; the stress scale s_y = 0.1 is passed at t ~ 0.14 and
+    t_scale = 3e5 makes the plastic strain reach ~3e-2 in the most active
+    cells.  adapt_fac = 0.02 keeps every cell at one plastic sub-step per
+    step (the largest stress drop per step is ~1.4e-2), so the loss is smooth
+    in c0, Omega*eps0, chi_inf, s_y and chi at the scale of a 1e-6 relative
+    finite-difference step.  With the sub-stepping active (adapt_fac 0.002,
+    or the athermal law at t_scale 1e9 with hundreds of sub-steps) the step
+    count of some cell changes under parameter changes of 1e-7 and the
+    discrete map is only piecewise smooth at that scale.  At the reference
+    wall speed 1e-4 the layer never yields and every gradient is zero.
+    """
+    kw.setdefault("u_bdry", 8.0)
+    kw.setdefault("s_y", 0.1)
+    kw.setdefault("t_scale", 3e5)
+    kw.setdefault("stz_model", STZ_LINEAR)
+    kw.setdefault("adapt_fac", 0.02)
+    return simple_shear(N, M, **kw)
+
+
+ADJOINT_DT = 2e-3
+
+
 def default_dt(N):
     """Time step of the reference-like configurations (dt=1e-2)."""
     return 1e-2
@@ -100,5 +127,5 @@ def cfl(p, dt):
     return abs(p.u_bdry) * dt * p.m / (p.bx - p.ax)
 
 
-__all__ = ["StzParams", "simple_shear", "plastic_shear", "default_dt", "cfl",
+__all__ = ["StzParams", "simple_shear", "plastic_shear", "adjoint_shear", "ADJOINT_DT", "default_dt", "cfl",
            "STZ_LINEAR", "STZ_NONLINEAR", "STZ_LINEAR_ATHERMAL", "STZ_NONLINEAR_ATHERMAL"]
