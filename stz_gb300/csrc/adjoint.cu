@@ -146,9 +146,8 @@ namespace {
 
 #define IDX(i, j) ((size_t)((j) + 1) * m + (i))
 
-__device__ __forceinline__ bool eno_a(double p0, double p1, double p2, double p3) {
-    return ::fabs(p0 - 2 * p1 + p2) > ::fabs(p1 - 2 * p2 + p3);
-}
+// the forward kernel's branch decision (eno2 in step.cuh)
+__device__ __forceinline__ bool eno_a(double p0, double p1, double p2, double p3) { return eno2_pick(p0, p1, p2, p3); }
 __device__ __forceinline__ double eno_val(bool a, double p0, double p1, double p2, double p3) {
     return a ? 3 * p1 - 4 * p2 + p3 : p0 - p2;
 }

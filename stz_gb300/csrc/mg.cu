@@ -669,10 +669,12 @@ __global__ void k_top_sqnorm(top_op<T> op, const typename vec2_t<T>::type *__res
                              const typename vec2_t<T>::type *__restrict__ b, int m, int n, double *partials) {
     typedef typename vec2_t<T>::type V;
     __shared__ double sh[32];
-    const long total = (long)m * n;
+    // 32-bit indices (grids are limited to 2^30 points): the division by m
+    // is a short unsigned sequence instead of a 64-bit division routine
+    const unsigned total = (unsigned)m * (unsigned)n;
     double sr = 0, sb = 0;
-    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (long)gridDim.x * blockDim.x) {
-        int i = (int)(k % m), j = (int)(k / m);
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        const int j = (int)(k / (unsigned)m), i = (int)k - j * m;
         V r = top_res<T>(op, z, b, m, n, i, j);
         sr += (double)r.x * r.x + (double)r.y * r.y;
         V bb = b[k];
@@ -705,10 +707,10 @@ __global__ void k_final_sum(const double *partials, int npart, double *out, doub
 __global__ void k_mixed_residual(top_op<double> op, const double2 *__restrict__ z, const double2 *__restrict__ b,
                                  int m, int n, float2 *__restrict__ r32, double *partials) {
     __shared__ double sh[32];
-    const long total = (long)m * n;
+    const unsigned total = (unsigned)m * (unsigned)n;
     double sr = 0, sb = 0;
-    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (long)gridDim.x * blockDim.x) {
-        int i = (int)(k % m), j = (int)(k / m);
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        const int j = (int)(k / (unsigned)m), i = (int)k - j * m;
         double2 r = top_res<double>(op, z, b, m, n, i, j);
         r32[k] = make_float2((float)r.x, (float)r.y);
         sr += r.x * r.x + r.y * r.y;

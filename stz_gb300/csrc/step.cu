@@ -43,11 +43,6 @@ step_consts make_step_consts(const stz_params &p) {
 
 namespace {
 
-__device__ __forceinline__ double eno2(double p0, double p1, double p2, double p3) {
-    // shear_sim::eno2, shear_sim.cc:653-655
-    return fabs(p0 - 2 * p1 + p2) > fabs(p1 - 2 * p2 + p3) ? 3 * p1 - 4 * p2 + p3 : p0 - p2;
-}
-
 struct velo {
     const double2 *vel;
     int m, n;
@@ -78,65 +73,66 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     const size_t ci = IDX(i, j);
     if (c.clock) bv = c.clock[CLK_BV_STATE];
     velo V{F.vel, m, n, bv};
-    double uc, vc;
+    // Upwind ENO values without the factor hs = +-dt/(2 dx); it is folded
+    // into the velocity: -u * (hs * eno) = -(u * hs) * eno.
     // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
     if (j > 0) {
         const double *X = A[F_X], *Y = A[F_Y];
-        double Xx, Xy, Yx, Yy;
-        uc = V.u(i, j);
-        vc = V.v(i, j);
-        if (uc > 0) {
-            Xx = hx * eno2(X[IDX(ir, j)] + (i == m - 1 ? lx : 0), X[ci], X[IDX(il, j)] + (i == 0 ? -lx : 0),
-                           X[IDX(il2, j)] + (i <= 1 ? -lx : 0));
-            Yx = hx * eno2(Y[IDX(ir, j)], Y[ci], Y[IDX(il, j)], Y[IDX(il2, j)]);
+        double ex_X, ex_Y, ey_X, ey_Y;
+        const double un = V.u(i, j), vn = V.v(i, j);
+        const double uh = un * (un > 0 ? hx : -hx), vh = vn * (vn > 0 ? hy : -hy);
+        if (un > 0) {
+            ex_X = eno2(X[IDX(ir, j)] + (i == m - 1 ? lx : 0), X[ci], X[IDX(il, j)] + (i == 0 ? -lx : 0),
+                        X[IDX(il2, j)] + (i <= 1 ? -lx : 0));
+            ex_Y = eno2(Y[IDX(ir, j)], Y[ci], Y[IDX(il, j)], Y[IDX(il2, j)]);
         } else {
-            Xx = -hx * eno2(X[IDX(il, j)] + (i == 0 ? -lx : 0), X[ci], X[IDX(ir, j)] + (i == m - 1 ? lx : 0),
-                            X[IDX(ir2, j)] + (i >= m - 2 ? lx : 0));
-            Yx = -hx * eno2(Y[IDX(il, j)], Y[ci], Y[IDX(ir, j)], Y[IDX(ir2, j)]);
+            ex_X = eno2(X[IDX(il, j)] + (i == 0 ? -lx : 0), X[ci], X[IDX(ir, j)] + (i == m - 1 ? lx : 0),
+                        X[IDX(ir2, j)] + (i >= m - 2 ? lx : 0));
+            ex_Y = eno2(Y[IDX(il, j)], Y[ci], Y[IDX(ir, j)], Y[IDX(ir2, j)]);
         }
-        if (vc > 0) {
+        if (vn > 0) {
             if (j > 1) {
-                Xy = hy * eno2(X[IDX(i, j + 1)], X[ci], X[IDX(i, j - 1)], X[IDX(i, j - 2)]);
-                Yy = hy * eno2(Y[IDX(i, j + 1)], Y[ci], Y[IDX(i, j - 1)], Y[IDX(i, j - 2)]);
+                ey_X = eno2(X[IDX(i, j + 1)], X[ci], X[IDX(i, j - 1)], X[IDX(i, j - 2)]);
+                ey_Y = eno2(Y[IDX(i, j + 1)], Y[ci], Y[IDX(i, j - 1)], Y[IDX(i, j - 2)]);
             } else {
-                Xy = 2 * hy * (X[ci] - X[IDX(i, j - 1)]);
-                Yy = 2 * hy * (Y[ci] - Y[IDX(i, j - 1)]);
+                ey_X = 2 * (X[ci] - X[IDX(i, j - 1)]);
+                ey_Y = 2 * (Y[ci] - Y[IDX(i, j - 1)]);
             }
         } else {
             if (j < n - 1) {
-                Xy = -hy * eno2(X[IDX(i, j - 1)], X[ci], X[IDX(i, j + 1)], X[IDX(i, j + 2)]);
-                Yy = -hy * eno2(Y[IDX(i, j - 1)], Y[ci], Y[IDX(i, j + 1)], Y[IDX(i, j + 2)]);
+                ey_X = eno2(X[IDX(i, j - 1)], X[ci], X[IDX(i, j + 1)], X[IDX(i, j + 2)]);
+                ey_Y = eno2(Y[IDX(i, j - 1)], Y[ci], Y[IDX(i, j + 1)], Y[IDX(i, j + 2)]);
             } else {
-                Xy = 2 * -hy * (X[ci] - X[IDX(i, j + 1)]);
-                Yy = 2 * -hy * (Y[ci] - Y[IDX(i, j + 1)]);
+                ey_X = 2 * (X[ci] - X[IDX(i, j + 1)]);
+                ey_Y = 2 * (Y[ci] - Y[IDX(i, j + 1)]);
             }
         }
-        B[F_X][ci] = X[ci] + (-uc * Xx - vc * Xy);
-        B[F_Y][ci] = Y[ci] + (-uc * Yx - vc * Yy);
+        B[F_X][ci] = X[ci] + fma(-vh, ey_X, -uh * ex_X);
+        B[F_Y][ci] = Y[ci] + fma(-vh, ey_Y, -uh * ex_Y);
     }
     // staggered velocity and spin (shear_sim.cc:330-333)
     const double u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
     const double v00 = V.v(i, j), v10 = V.v(ir, j), v01 = V.v(i, j + 1), v11 = V.v(ir, j + 1);
-    uc = 0.25 * (u00 + u10 + u01 + u11);
-    vc = 0.25 * (v00 + v10 + v01 + v11);
+    const double uc = 0.25 * (u00 + u10 + u01 + u11), vc = 0.25 * (v00 + v10 + v01 + v11);
     const double two_omega = hx * (-v00 + v10 - v01 + v11) - hy * (-u00 - u10 + u01 + u11);
+    const double uh = uc * (uc > 0 ? hx : -hx), vh = vc * (vc > 0 ? hy : -hy);
     // ENO derivatives of p, q, s, tau, chi (shear_sim.cc:336-338)
     double f1[5], f2[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
         const double *G = A[k];
-        if (uc > 0) f1[k] = hx * eno2(G[IDX(ir, j)], G[ci], G[IDX(il, j)], G[IDX(il2, j)]);
-        else f1[k] = -hx * eno2(G[IDX(il, j)], G[ci], G[IDX(ir, j)], G[IDX(ir2, j)]);
+        if (uc > 0) f1[k] = eno2(G[IDX(ir, j)], G[ci], G[IDX(il, j)], G[IDX(il2, j)]);
+        else f1[k] = eno2(G[IDX(il, j)], G[ci], G[IDX(ir, j)], G[IDX(ir2, j)]);
         if (vc > 0) {
-            if (j > 0) f2[k] = hy * eno2(G[IDX(i, j + 1)], G[ci], G[IDX(i, j - 1)], G[IDX(i, j - 2)]);
-            else f2[k] = 2 * hy * (G[ci] - G[IDX(i, j - 1)]);
+            if (j > 0) f2[k] = eno2(G[IDX(i, j + 1)], G[ci], G[IDX(i, j - 1)], G[IDX(i, j - 2)]);
+            else f2[k] = 2 * (G[ci] - G[IDX(i, j - 1)]);
         } else {
-            if (j < n - 1) f2[k] = -hy * eno2(G[IDX(i, j - 1)], G[ci], G[IDX(i, j + 1)], G[IDX(i, j + 2)]);
-            else f2[k] = 2 * -hy * (G[ci] - G[IDX(i, j + 1)]);
+            if (j < n - 1) f2[k] = eno2(G[IDX(i, j - 1)], G[ci], G[IDX(i, j + 1)], G[IDX(i, j + 2)]);
+            else f2[k] = 2 * (G[ci] - G[IDX(i, j + 1)]);
         }
     }
     const double p = A[F_P][ci], q = A[F_Q][ci], s = A[F_S][ci], t = A[F_TAU][ci];
-    double cchi = A[F_CHI][ci] - uc * f1[4] - vc * f2[4], ddev, dtmp;
+    double cchi = A[F_CHI][ci] + fma(-vh, f2[4], -uh * f1[4]), ddev, dtmp;
     const double devsq = 3 * q * q + s * s + t * t;
     // Cells far enough below the cut-offs return exactly ddev = 0 and leave
     // chi unchanged in the reference loop (sbar < 1e-12, or an athermal law
@@ -156,10 +152,10 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     B[F_CHI][ci] = cchi;
     F.ddev[ci] = ddev;
     if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
-    const double pn = p + (-uc * f1[0] - vc * f2[0]);
-    const double qn = q + (-uc * f1[1] - vc * f2[1] - dtmp * q);
-    const double sn = s + (-uc * f1[2] - vc * f2[2] + two_omega * t - dtmp * s);
-    const double tn = t + (-uc * f1[3] - vc * f2[3] - two_omega * s - dtmp * t);
+    const double pn = p + fma(-vh, f2[0], -uh * f1[0]);
+    const double qn = q + (fma(-vh, f2[1], -uh * f1[1]) - dtmp * q);
+    const double sn = s + (fma(-vh, f2[2], -uh * f1[2]) + two_omega * t - dtmp * s);
+    const double tn = t + (fma(-vh, f2[3], -uh * f1[3]) - two_omega * s - dtmp * t);
     B[F_P][ci] = pn;
     B[F_Q][ci] = qn;
     B[F_S][ci] = sn;

@@ -48,6 +48,29 @@ enum { CLK_TIME = 0, CLK_BV_STATE = 1, CLK_BV = 2, CLK_BP = 3, CLK_CUR = 4, CLK_
 
 step_consts make_step_consts(const stz_params &p);
 
+// |a| > |b| for finite doubles, compared as the magnitudes of their IEEE bit
+// patterns on the integer pipe (same result as fabs(a) > fabs(b)).
+__device__ __forceinline__ bool mag_gt(double a, double b) {
+    const unsigned long long ma = (unsigned long long)__double_as_longlong(a) & 0x7fffffffffffffffull;
+    const unsigned long long mb = (unsigned long long)__double_as_longlong(b) & 0x7fffffffffffffffull;
+    return ma > mb;
+}
+
+// ENO2 choice and value (shear_sim::eno2, shear_sim.cc:653-655): with the
+// second differences d1 = p0 - 2p1 + p2 and d2 = p1 - 2p2 + p3, |d1| > |d2|
+// selects 3p1 - 4p2 + p3 = d2 + 2(p1 - p2), otherwise p0 - p2 = d1 + 2(p1 - p2).
+// Written through first differences: six FP64 operations and an integer
+// compare.  The adjoint takes its branch decisions from eno2_pick, so both
+// see the same choice.
+__device__ __forceinline__ bool eno2_pick(double p0, double p1, double p2, double p3) {
+    const double e = p1 - p2;
+    return mag_gt((p0 - p1) - e, e - (p2 - p3));
+}
+__device__ __forceinline__ double eno2(double p0, double p1, double p2, double p3) {
+    const double e = p1 - p2, d1 = (p0 - p1) - e, d2 = e - (p2 - p3);
+    return fma(2.0, e, mag_gt(d1, d2) ? d2 : d1);
+}
+
 // shear_sim::advection_step + chi_diffusion + the field update
 // (shear_sim.cc:296-386, fields.hh:61-80).  bv is the wall speed of the
 // current state (u = -bv on row 0 and +bv on row n, set_boundaries).
