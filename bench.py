@@ -40,7 +40,7 @@ ADVECT_BYTES_PER_CELL = 128      # read u,v,p,q,s,tau,chi,X,Y; write p,q,s,tau,c
 VCYCLE32_BYTES_PER_NODE = 69.3   # 17.3 words of 4 B: 13 W on the top level x (1 + 1/4 + 1/16 + ...)
 VCYCLE64_BYTES_PER_NODE = 138.7
 SWEEP32_BYTES_PER_NODE = 24      # one Gauss-Seidel sweep: read z, b; write z (float2)
-RESID64_BYTES_PER_NODE = 40      # read z, b (double2); write r (float2)
+RESIDFF_BYTES_PER_NODE = 40      # read z, b as float-float (hi, lo float2 each); write r (float2)
 
 
 def parse():
@@ -288,10 +288,10 @@ def run_ours(args, dist):
     rows = {"advect": (t_adv, ADVECT_BYTES_PER_CELL * N * N, 1.0)}
     if prec == _lib.MIXED:
         t_v32 = sim.time_kernel(DT, 4, 10)
-        t_r64 = sim.time_kernel(DT, 5, 10)
+        t_rff = sim.time_kernel(DT, 5, 10)
         vc = st.vcycles / args.steps
         rows["vcycle_fp32"] = (t_v32, VCYCLE32_BYTES_PER_NODE * nn, vc)
-        rows["residual_fp64"] = (t_r64, RESID64_BYTES_PER_NODE * nn, st.refinements / args.steps + 1)
+        rows["residual_ff"] = (t_rff, RESIDFF_BYTES_PER_NODE * nn, st.refinements / args.steps + 1)
     else:
         t_v64 = sim.time_kernel(DT, 3, 10)
         rows["vcycle_fp64"] = (t_v64, VCYCLE64_BYTES_PER_NODE * nn, st.vcycles / args.steps)

@@ -153,7 +153,8 @@ int stzg_mg_stencil(stzg_sim *s, double dt, int level, double *out);
  * measured with CUDA events.  kernel: 0 advection (writes the spare buffer,
  * state unchanged), 1 FP64 top-level sweep (changes the velocity iterate),
  * 2 FP32 top-level sweep (scratch), 3 FP64 V-cycle, 4 FP32 V-cycle
- * (scratch), 5 FP64 residual + FP32 copy + norms. */
+ * (scratch), 5 outer residual of the mixed solve (float-float) + FP32 copy +
+ * norms. */
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
 
 /* No counterpart in the reference.  Squared residual norms of the

@@ -115,11 +115,17 @@ int ensure_ops(stzg_sim *s, double dt) {
 void launch_norms(stzg_sim *s, bool mixed) {
     const int M = s->m, N = s->n + 1;
     if (mixed)
-        mixed_residual(s->q.op<double>(), s->F.vel, s->F.src, M, N, s->h32.lv[0].b, s->partials, s->npart,
-                       s->dnorm, s->dnorm + 1, s->st);
+        ff_residual(s->q.op<double>(), s->zhi, s->zlo, s->bhi, s->blo, M, N, s->h32.lv[0].b, s->partials, s->npart,
+                    s->dnorm, s->dnorm + 1, s->st);
     else
         top_residual_sqnorm(s->h64, s->partials, s->npart, s->dnorm, s->dnorm + 1, s->st);
 }
+
+void mixed_begin(stzg_sim *s) {
+    ff_split(s->F.vel, s->zhi, s->zlo, s->F.src, s->bhi, s->blo, (long)s->m * (s->n + 1), s->st);
+}
+
+void mixed_end(stzg_sim *s) { ff_merge(s->zhi, s->zlo, s->F.vel, (long)s->m * (s->n + 1), s->st); }
 
 // Reads dnorm and evaluates the stopping rule.
 int read_check(stzg_sim *s, double *err, bool *ok) {
@@ -199,7 +205,7 @@ int run_passes(stzg_sim *s, int k) {
     auto pass = [&] {
         cudaMemsetAsync(s->h32.lv[0].z, 0, sizeof(float2) * count, s->st);
         for (int c = 0; c < inner; c++) vcycle<float>(s->h32, s->st, 10, 1);
-        mixed_correct(s->F.vel, s->h32.lv[0].z, count, s->st);
+        ff_correct(s->zhi, s->zlo, s->h32.lv[0].z, count, s->st);
         launch_norms(s, true);
     };
     if (k <= 0) return STZG_OK;
@@ -223,6 +229,7 @@ int solve_mixed(stzg_sim *s, int *ncyc) {
         s->g_pass32 = nullptr;
     }
     s->g_inner = inner;
+    mixed_begin(s);
     launch_norms(s, true);  // initial residual of the warm start
     int np = s->lim / s->mult;
     STZG_CHECK(run_passes(s, np));
@@ -241,6 +248,7 @@ int solve_mixed(stzg_sim *s, int *ncyc) {
             STZG_CHECK(read_check(s, &err, &ok));
         } while (!ok);
     }
+    mixed_end(s);
     const int cycles = np * inner;
     s->acc.vcycles += cycles;
     s->acc.solves++;
@@ -369,8 +377,12 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if (cudaMallocHost(&s->hnorm, 2 * sizeof(double)) != cudaSuccess) return bail(fail(STZG_ENOMEM, "pinned alloc"));
     // FP64 hierarchy over vel/src; FP32 hierarchy with its own top arrays
     if ((st = s->h64.allocate(s->m, s->n + 1, s->F.vel, s->F.src)) != STZG_OK) return bail(st);
-    if (o.precision == STZG_MIXED)
+    if (o.precision == STZG_MIXED) {
         if ((st = s->h32.allocate(s->m, s->n + 1, nullptr, nullptr)) != STZG_OK) return bail(st);
+        float2 **ffa[4] = {&s->zhi, &s->zlo, &s->bhi, &s->blo};
+        for (int k = 0; k < 4; k++)
+            if ((st = dev_alloc(s, (void **)ffa[k], nn * sizeof(float2))) != STZG_OK) return bail(st);
+    }
     cudaEventCreate(&s->ev0);
     cudaEventCreate(&s->ev1);
     if (cudaStreamSynchronize(s->st) != cudaSuccess) return bail(fail(STZG_ECUDA, "set-up failed"));

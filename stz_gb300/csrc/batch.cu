@@ -161,7 +161,10 @@ int add_instance(stzg_batch *b, cudaGraph_t root, int k, double dt, int nsteps, 
     advection(sc, s->F, 0, dt, 0.0, s->st);
     projection_source(sc, s->F, 0, dt, 0.0, s->st);
     if (s->O.extrapolate) extrapolate_guess(s->F.vel, s->vel_prev, count, s->st);
-    if (mixed) launch_norms(s, true);
+    if (mixed) {
+        mixed_begin(s);
+        launch_norms(s, true);
+    }
     k_solve_reset<<<1, 32, 0, s->st>>>(ctr, hsolve);
     note_launch();
     cudaStreamCaptureStatus cs;
@@ -177,6 +180,7 @@ int add_instance(stzg_batch *b, cudaGraph_t root, int k, double dt, int nsteps, 
     cudaGraphNode_t snode;
     STZG_CUDA(cudaGraphAddNode(&snode, cg, deps, nullptr, ndeps, &sp));
     STZG_CUDA(cudaStreamUpdateCaptureDependencies(s->st, &snode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    if (mixed) mixed_end(s);
     projection_apply(sc, s->F, 0, dt, 0.0, 0.0, s->st);
     k_step_end<<<1, 32, 0, s->st>>>(clk, ctr, nsteps, hstep);
     note_launch();
@@ -192,7 +196,7 @@ int add_instance(stzg_batch *b, cudaGraph_t root, int k, double dt, int nsteps, 
         per_pass = tn.inner;
         cudaMemsetAsync(s->h32.lv[0].z, 0, sizeof(float2) * count, s->st);
         for (int c = 0; c < tn.inner; c++) vcycle<float>(s->h32, s->st, 10, 1);
-        mixed_correct(s->F.vel, s->h32.lv[0].z, count, s->st);
+        ff_correct(s->zhi, s->zlo, s->h32.lv[0].z, count, s->st);
         launch_norms(s, true);
     } else {
         vcycle<double>(s->h64, s->st, 10, 1);

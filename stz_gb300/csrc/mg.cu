@@ -744,6 +744,197 @@ __global__ void k_extrapolate(double2 *__restrict__ z, double2 *__restrict__ pre
 }
 
 // ---------------------------------------------------------------------------
+// Float-float iterates of the mixed-precision solve.  GB300 issues FP64 at
+// 1/57 of the FP32 rate, so the outer residual b - A z, computed in FP64,
+// was ALU-bound.  Here z and b are kept as unevaluated sums hi + lo of two
+// floats (~48 significant bits) and the residual is evaluated with
+// error-free transformations in FP32: Knuth's TwoSum, Dekker's
+// Fast2Sum and the FMA product error (a*b - p exactly = fmaf(a, b, -p)).
+// The additions are the "sloppy" double-float sum, whose error is bounded
+// by ~2^-44 (|x| + |y|): the residual's error is then ~1e-13 |b|, three
+// orders below the 1e-10 stopping tolerance, while the FP32 value handed to
+// the V-cycles needs only single precision.
+
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_fast2sum(float a, float b) {
+    const float s = a + b;
+    return ff{s, b - (s - a)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    return ff_fast2sum(s, e);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return ff_fast2sum(p, e);
+}
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+    const float s = a.hi + b, bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b - bb);
+    e += a.lo;
+    return ff_fast2sum(s, e);
+}
+
+// double -> hi + lo on the integer pipe: hi keeps the sign, the exponent and
+// the leading 24 significant bits, lo the remaining 29 bits rounded to a
+// float.  |d| below 2^-126 gives 0; below 2^-74 lo is dropped (an absolute
+// error under 2^-98).  NaN and infinity pass through in hi.
+__device__ __forceinline__ void ff_split_d(double d, float &hi, float &lo) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const unsigned sign = (unsigned)(u >> 63) << 31;
+    const int ex = (int)((u >> 52) & 0x7ff);
+    const int ef = ex - 1023 + 127;
+    lo = 0.f;
+    if (ex == 0x7ff) {
+        hi = (u & 0xfffffffffffffull) ? __uint_as_float(0x7fc00000u) : __uint_as_float(sign | 0x7f800000u);
+        return;
+    }
+    if (ef <= 0) {
+        hi = __uint_as_float(sign);
+        return;
+    }
+    if (ef >= 255) {
+        hi = __uint_as_float(sign | 0x7f800000u);
+        return;
+    }
+    hi = __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)((u >> 29) & 0x7fffffu));
+    const int es = ex - 1075 + 127;  // float exponent field of 2^(ex - 1075)
+    if (es > 0) {
+        const float r = __uint2float_rn((unsigned)(u & 0x1fffffffu)) * __uint_as_float((unsigned)es << 23);
+        lo = sign ? -r : r;
+    }
+}
+
+// float -> double on the integer pipe (exact for normal floats; zero and
+// subnormal floats give a signed zero, infinity and NaN convert normally).
+__device__ __forceinline__ double ff_f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xff;
+    if (e == 255) return (double)f;
+    unsigned long long r = (unsigned long long)(u >> 31) << 63;
+    if (e != 0) r |= ((unsigned long long)(e - 127 + 1023) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)r);
+}
+
+__global__ void k_ff_split(const double2 *__restrict__ a, float2 *__restrict__ hi, float2 *__restrict__ lo,
+                           const double2 *__restrict__ a2, float2 *__restrict__ hi2, float2 *__restrict__ lo2,
+                           long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        float2 h, l;
+        const double2 v = a[k];
+        ff_split_d(v.x, h.x, l.x);
+        ff_split_d(v.y, h.y, l.y);
+        hi[k] = h;
+        lo[k] = l;
+        if (a2) {
+            const double2 w = a2[k];
+            ff_split_d(w.x, h.x, l.x);
+            ff_split_d(w.y, h.y, l.y);
+            hi2[k] = h;
+            lo2[k] = l;
+        }
+    }
+}
+
+__global__ void k_ff_merge(const float2 *__restrict__ hi, const float2 *__restrict__ lo, double2 *__restrict__ a,
+                           long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        const float2 h = hi[k], l = lo[k];
+        a[k] = make_double2(ff_f2d(h.x) + ff_f2d(l.x), ff_f2d(h.y) + ff_f2d(l.y));
+    }
+}
+
+__global__ void k_ff_correct(float2 *__restrict__ hi, float2 *__restrict__ lo, const float2 *__restrict__ e,
+                             long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        const float2 h = hi[k], l = lo[k], d = e[k];
+        const ff x = ff_add_f(ff{h.x, l.x}, d.x), y = ff_add_f(ff{h.y, l.y}, d.y);
+        hi[k] = make_float2(x.hi, y.hi);
+        lo[k] = make_float2(x.lo, y.lo);
+    }
+}
+
+// Constants of the top-level operator as float-float pairs.
+struct ff_op {
+    ff Kmx, Kmy, mx, my, qK, bcxx, bcyy;
+    ff dxx, dyy;  // cxx + 2 (Kmx + my), cyy + 2 (mx + Kmy): zero up to rounding
+};
+
+// r = b - A z (qs_multi::mul_a + a_cc) in float-float; r is stored in FP32
+// as the next right-hand side; sum r^2 and sum b^2 go to the partials
+// (FP32 per thread, FP64 across threads).
+__global__ void k_ff_residual(ff_op op, const float2 *__restrict__ zh, const float2 *__restrict__ zl,
+                              const float2 *__restrict__ bh, const float2 *__restrict__ bl, int m, int n,
+                              float2 *__restrict__ r32, double *partials) {
+    __shared__ double sh[32];
+    const unsigned total = (unsigned)m * (unsigned)n;
+    float sr = 0.f, sb = 0.f;
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        const int j = (int)(k / (unsigned)m), i = (int)k - j * m;
+        const float2 b0h = bh[k], b0l = bl[k];
+        const ff bx{b0h.x, b0l.x}, by{b0h.y, b0l.y};
+        const float2 ch = zh[k], cl = zl[k];
+        const ff cx{ch.x, cl.x}, cy{ch.y, cl.y};
+        ff rx, ry;
+        if (j == 0 || j == n - 1) {
+            rx = ff_sub(bx, ff_mul(op.bcxx, cx));
+            ry = ff_sub(by, ff_mul(op.bcyy, cy));
+        } else {
+            const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+            const unsigned rd = k - (unsigned)m, ru = k + (unsigned)m;
+            auto ld = [&](unsigned q, ff &x, ff &y) {
+                const float2 h = zh[q], l = zl[q];
+                x = ff{h.x, l.x};
+                y = ff{h.y, l.y};
+            };
+            ff lx, ly, rrx, rry, dx, dy, ux, uy, dlx, dly, urx, ury, drx, dry, ulx, uly;
+            ld(k - i + il, lx, ly);
+            ld(k - i + ir, rrx, rry);
+            ld(rd, dx, dy);
+            ld(ru, ux, uy);
+            ld(rd - i + il, dlx, dly);
+            ld(ru - i + ir, urx, ury);
+            ld(rd - i + ir, drx, dry);
+            ld(ru - i + il, ulx, uly);
+            // cxx = -2 (Kmx + my) and cyy = -2 (mx + Kmy) up to rounding
+            // (qs_multi.cc:31-55), so A z is evaluated on differences from
+            // the centre value, which are small for smooth z: the float-float
+            // rounding then scales with them rather than with z itself.
+            const ff axx = ff_add(
+                ff_add(ff_mul(op.Kmx, ff_add(ff_sub(lx, cx), ff_sub(rrx, cx))),
+                       ff_mul(op.my, ff_add(ff_sub(dx, cx), ff_sub(ux, cx)))),
+                ff_add(ff_mul(op.qK, ff_add(ff_sub(dly, dry), ff_sub(ury, uly))), ff_mul(op.dxx, cx)));
+            const ff ayy = ff_add(
+                ff_add(ff_mul(op.mx, ff_add(ff_sub(ly, cy), ff_sub(rry, cy))),
+                       ff_mul(op.Kmy, ff_add(ff_sub(dy, cy), ff_sub(uy, cy)))),
+                ff_add(ff_mul(op.qK, ff_add(ff_sub(dlx, drx), ff_sub(urx, ulx))), ff_mul(op.dyy, cy)));
+            rx = ff_sub(bx, axx);
+            ry = ff_sub(by, ayy);
+        }
+        const float2 r = make_float2(rx.hi + rx.lo, ry.hi + ry.lo);
+        r32[k] = r;
+        sr = fmaf(r.x, r.x, fmaf(r.y, r.y, sr));
+        sb = fmaf(b0h.x, b0h.x, fmaf(b0h.y, b0h.y, sb));
+    }
+    const double a = block_sum((double)sr, sh);
+    const double c = block_sum((double)sb, sh);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = a;
+        partials[2 * blockIdx.x + 1] = c;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Fused top-level kernels (single precision).  A block (32 x 8 threads) owns a
 // tile of TCX x TCY coarse points and the 2TCX x 2TCY fine points below them.
 // It stages z and b of the tile plus a halo in shared memory, runs both
@@ -1496,6 +1687,35 @@ void top_residual_sqnorm(hierarchy<T> &h, double *partials, int npart, double *o
 void mixed_residual(const top_op<double> &op64, const double2 *z64, const double2 *b64, int m, int n, float2 *r32,
                     double *partials, int npart, double *out, double *out_b, cudaStream_t st) {
     k_mixed_residual<<<npart, kRedThreads, 0, st>>>(op64, z64, b64, m, n, r32, partials); note_launch();
+    k_final_sum<<<1, 256, 0, st>>>(partials, npart, out, out_b); note_launch();
+}
+
+static ff ff_of(double d) {
+    const float hi = (float)d;
+    return ff{hi, (float)(d - (double)hi)};
+}
+
+void ff_split(const double2 *a, float2 *hi, float2 *lo, const double2 *a2, float2 *hi2, float2 *lo2, long count,
+              cudaStream_t st) {
+    k_ff_split<<<4 * 152, 256, 0, st>>>(a, hi, lo, a2, hi2, lo2, count); note_launch();
+}
+
+void ff_merge(const float2 *hi, const float2 *lo, double2 *a, long count, cudaStream_t st) {
+    k_ff_merge<<<4 * 152, 256, 0, st>>>(hi, lo, a, count); note_launch();
+}
+
+void ff_correct(float2 *hi, float2 *lo, const float2 *e32, long count, cudaStream_t st) {
+    k_ff_correct<<<4 * 152, 256, 0, st>>>(hi, lo, e32, count); note_launch();
+}
+
+void ff_residual(const top_op<double> &o, const float2 *zhi, const float2 *zlo, const float2 *bhi, const float2 *blo,
+                 int m, int n, float2 *r32, double *partials, int npart, double *out, double *out_b, cudaStream_t st) {
+    ff_op f;
+    f.Kmx = ff_of(o.Kmx); f.Kmy = ff_of(o.Kmy); f.mx = ff_of(o.mx); f.my = ff_of(o.my); f.qK = ff_of(o.qK);
+    f.bcxx = ff_of(o.bcxx); f.bcyy = ff_of(o.bcyy);
+    f.dxx = ff_of(o.cxx + 2 * (o.Kmx + o.my));
+    f.dyy = ff_of(o.cyy + 2 * (o.mx + o.Kmy));
+    k_ff_residual<<<npart, kRedThreads, 0, st>>>(f, zhi, zlo, bhi, blo, m, n, r32, partials); note_launch();
     k_final_sum<<<1, 256, 0, st>>>(partials, npart, out, out_b); note_launch();
 }
 

@@ -121,6 +121,17 @@ void mixed_residual(const top_op<double> &op64, const double2 *z64, const double
                     float2 *r32, double *partials, int npart, double *out, double *out_b, cudaStream_t st);
 // z64 += e32
 void mixed_correct(double2 *z64, const float2 *e32, long count, cudaStream_t st);
+// Float-float iterates (hi + lo pairs of FP32 vectors) of the mixed solve:
+// split FP64 vectors (a, and a2 unless null), merge back, add an FP32
+// correction, and the residual r32 = b - A z in float-float arithmetic with
+// squared norms like top_residual_sqnorm.
+void ff_split(const double2 *a, float2 *hi, float2 *lo, const double2 *a2, float2 *hi2, float2 *lo2, long count,
+              cudaStream_t st);
+void ff_merge(const float2 *hi, const float2 *lo, double2 *a, long count, cudaStream_t st);
+void ff_correct(float2 *hi, float2 *lo, const float2 *e32, long count, cudaStream_t st);
+void ff_residual(const top_op<double> &op64, const float2 *zhi, const float2 *zlo, const float2 *bhi,
+                 const float2 *blo, int m, int n, float2 *r32, double *partials, int npart, double *out,
+                 double *out_b, cudaStream_t st);
 // Linear extrapolation of the initial guess: z <- 2 z - prev, prev <- old z.
 void extrapolate_guess(double2 *z, double2 *prev, long count, cudaStream_t st);
 

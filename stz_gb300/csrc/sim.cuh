@@ -40,6 +40,9 @@ struct stzg_sim {
     long n_vc64 = 0, n_res32 = 0, n_pass32 = 0;  // kernel nodes per graph
     int g_inner = 0;
     double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)
+    // mixed precision: float-float copies (hi + lo) of the iterate and of the
+    // right-hand side for the duration of a solve
+    float2 *zhi = nullptr, *zlo = nullptr, *bhi = nullptr, *blo = nullptr;
     bool have_prev = false;
     stzg_adjoint *adj = nullptr;  // adjoint workspace (adjoint.cu), created on first use
 };
@@ -54,6 +57,9 @@ int validate(const stz_params *p);
 void drop_graphs(stzg_sim *s);
 int ensure_ops(stzg_sim *s, double dt);
 void launch_norms(stzg_sim *s, bool mixed);
+// Mixed solve: vel, src -> float-float iterate and right-hand side, and back.
+void mixed_begin(stzg_sim *s);
+void mixed_end(stzg_sim *s);
 int read_check(stzg_sim *s, double *err, bool *ok);
 int check_flags(stzg_sim *s);
 size_t cell_count(const stzg_sim *s);
