@@ -935,7 +935,7 @@ __global__ void k_ff_residual(ff_op op, const float2 *__restrict__ zh, const flo
 }
 
 // ---------------------------------------------------------------------------
-// Fused top-level kernels (single precision).  A block (32 x 8 threads) owns a
+// Fused top-level kernels (single precision).  A block (256 threads) owns a
 // tile of TCX x TCY coarse points and the 2TCX x 2TCY fine points below them.
 // It stages z and b of the tile plus a halo in shared memory, runs both
 // colours of the Gauss-Seidel sweep there (recomputing the halo points that
@@ -943,10 +943,18 @@ __global__ void k_ff_residual(ff_op op, const float2 *__restrict__ zh, const flo
 // and then either restricts the residual (down) or, after adding the
 // prolongation, writes the swept tile (up).  One launch replaces the five or
 // three launches of the colour-by-colour path; HBM sees z and b once per
-// sweep.  Loops are two-dimensional (no division), and in each colour a
-// thread updates a horizontal pair of nodes: the x component of the one whose
-// parity matches the colour and the y component of the other, so the warps
-// do not diverge.
+// sweep.
+//
+// Shared-memory layout: the x and y components of z and b live in four
+// separate planes (row stride W floats, plane stride a multiple of 32
+// floats).  In a colour a lane updates one component of one node, the x
+// component where (i+j)&1 equals the colour and the y component elsewhere,
+// with consecutive lanes on consecutive nodes of a row: the lanes alternate
+// between the x and the y plane at consecutive columns, so each load of a
+// warp touches 32 distinct banks (one wavefront).  A node's colour-1
+// component has a zero residual after the sweep (up to rounding: it was the
+// last unknown updated and none of its neighbours changed since), so the
+// residual is evaluated for the colour-0 component only.
 
 constexpr int TCX = 32, TCY = 8;
 constexpr int DW = 2 * TCX + 7, DH = 2 * TCY + 7;   // down: fine x in [2I0-4, 2I1+2]
@@ -961,74 +969,210 @@ __device__ __forceinline__ int wrapx(int x, int m) { return x < 0 ? x + m : (x >
     for (int k_ = threadIdx.y * blockDim.x + threadIdx.x; k_ < (RH) * (RW); k_ += blockDim.x * blockDim.y) \
         if (const int ty = (R0) + k_ / (RW), tx = (C0) + k_ % (RW); true)
 
-template <typename T, int W>
-__device__ __forceinline__ void top_x_update(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
-                                             typename vec2_t<T>::type (*bs)[W], int ty, int tx, bool wall) {
-    if (wall) {
-        zs[ty][tx].x = op.ibcxx * bs[ty][tx].x;
-        return;
-    }
-    const T l = zs[ty][tx - 1].x, r = zs[ty][tx + 1].x, d = zs[ty - 1][tx].x, u = zs[ty + 1][tx].x;
-    const T dl = zs[ty - 1][tx - 1].y, ur = zs[ty + 1][tx + 1].y, dr = zs[ty - 1][tx + 1].y,
-            ul = zs[ty + 1][tx - 1].y;
-    const T a = op.Kmx * (l + r) + op.my * (d + u) + op.qK * (dl + ur - dr - ul);
-    zs[ty][tx].x = op.icxx * (bs[ty][tx].x - a);
-}
-
-template <typename T, int W>
-__device__ __forceinline__ void top_y_update(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
-                                             typename vec2_t<T>::type (*bs)[W], int ty, int tx, bool wall) {
-    if (wall) {
-        zs[ty][tx].y = op.ibcyy * bs[ty][tx].y;
-        return;
-    }
-    const T l = zs[ty][tx - 1].y, r = zs[ty][tx + 1].y, d = zs[ty - 1][tx].y, u = zs[ty + 1][tx].y;
-    const T dl = zs[ty - 1][tx - 1].x, ur = zs[ty + 1][tx + 1].x, dr = zs[ty - 1][tx + 1].x,
-            ul = zs[ty + 1][tx - 1].x;
-    const T a = op.mx * (l + r) + op.Kmy * (d + u) + op.qK * (dl + ur - dr - ul);
-    zs[ty][tx].y = op.icyy * (bs[ty][tx].y - a);
-}
+// Plane stride of a W x H tile, padded to whole 32-float bank rows.
+template <int W, int H> __host__ __device__ constexpr int plane_stride() { return ((W * H + 31) / 32) * 32; }
 
 // One colour of the top-level sweep on tile rows/columns [LO, H-1-LO] x
-// [LO, W-1-LO]: colour c updates x where (i+j)&1 == c and y elsewhere.  The
-// (row, pair) index is flattened with compile-time divisors so that every
-// lane has work.
+// [LO, W-1-LO]; planes v = (zx, zy, bx, by).
 template <typename T, int W, int H, int LO>
-__device__ inline void tile_top_color(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
-                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int n, int color) {
-    constexpr int HI = W - 1 - LO, NPR = (HI - LO + 2) >> 1, NR = H - 2 * LO;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
-    for (int k = tid; k < NR * NPR; k += nth) {
-        const int ty = LO + k / NPR, ta = LO + 2 * (k % NPR);
+__device__ inline void plane_top_color(const top_op<T> &op, T *v, int x0, int y0, int n, int color) {
+    constexpr int P = plane_stride<W, H>(), RW = W - 2 * LO, RH = H - 2 * LO;
+    TILE_FOR(RH, RW, LO, LO, ty, tx) {
         const int gy = y0 + ty;
         if (gy < 0 || gy >= n) continue;
-        const bool wall = gy == 0 || gy == n - 1;
-        const bool a_is_x = ((x0 + ta + gy) & 1) == color;
-        const int tx_x = a_is_x ? ta : ta + 1, tx_y = a_is_x ? ta + 1 : ta;
-        if (tx_x <= HI) top_x_update<T, W>(op, zs, bs, ty, tx_x, wall);
-        if (tx_y <= HI) top_y_update<T, W>(op, zs, bs, ty, tx_y, wall);
+        const bool ux = ((x0 + tx + gy) & 1) == color;  // this lane updates x (else y)
+        const int o = ty * W + tx;
+        T *S = v + (ux ? 0 : P);
+        const T *O = v + (ux ? P : 0);
+        const T bb = v[(ux ? 2 * P : 3 * P) + o];
+        if (gy == 0 || gy == n - 1) {
+            S[o] = (ux ? op.ibcxx : op.ibcyy) * bb;
+            continue;
+        }
+        const T cl = ux ? op.Kmx : op.mx, cd = ux ? op.my : op.Kmy;
+        const T a = cl * (S[o - 1] + S[o + 1]) + cd * (S[o - W] + S[o + W]) +
+                    op.qK * (O[o - W - 1] + O[o + W + 1] - O[o - W + 1] - O[o + W - 1]);
+        S[o] = (ux ? op.icxx : op.icyy) * (bb - a);
     }
 }
 
-// Residual b - A z of the top level at a tile point (written over b).
-template <typename T, int W>
-__device__ __forceinline__ void top_residual_at(const top_op<T> &op, typename vec2_t<T>::type (*zs)[W],
-                                                typename vec2_t<T>::type (*bs)[W], int ty, int tx, bool wall) {
+// Pre-smooth + residual + restriction of the top level (apply_r after one
+// gauss_seidel, tgmg.in.cc:313-320).
+template <typename T>
+__global__ void __launch_bounds__(kFusedThreads) k_top_down(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
+                                                         const typename vec2_t<T>::type *__restrict__ b, int m,
+                                                         int n, typename vec2_t<T>::type *__restrict__ bc, int cm,
+                                                         int cn) {
     typedef typename vec2_t<T>::type V;
-    const V c = zs[ty][tx], bb = bs[ty][tx];
-    V r;
-    if (wall) {
-        r.x = bb.x - op.bcxx * c.x;
-        r.y = bb.y - op.bcyy * c.y;
-    } else {
-        const V l = zs[ty][tx - 1], rr = zs[ty][tx + 1], d = zs[ty - 1][tx], u = zs[ty + 1][tx];
-        const V dl = zs[ty - 1][tx - 1], ur = zs[ty + 1][tx + 1], dr = zs[ty - 1][tx + 1], ul = zs[ty + 1][tx - 1];
-        const T ax = op.Kmx * (l.x + rr.x) + op.my * (d.x + u.x) + op.qK * (dl.y + ur.y - dr.y - ul.y);
-        const T ay = op.mx * (l.y + rr.y) + op.Kmy * (d.y + u.y) + op.qK * (dl.x + ur.x - dr.x - ul.x);
-        r.x = bb.x - ax - op.cxx * c.x;
-        r.y = bb.y - ay - op.cyy * c.y;
+    constexpr int P = plane_stride<DW, DH>();
+    __shared__ T v[4 * P];
+    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
+    TILE_FOR(DH, DW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
+        V zz, bb;
+        zz.x = zz.y = bb.x = bb.y = 0;
+        if (gy >= 0 && gy < n) {
+            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
+            zz = z[g];
+            bb = b[g];
+        }
+        const int o = ty * DW + tx;
+        v[o] = zz.x;
+        v[P + o] = zz.y;
+        v[2 * P + o] = bb.x;
+        v[3 * P + o] = bb.y;
     }
-    bs[ty][tx] = r;
+    __syncthreads();
+    plane_top_color<T, DW, DH, 1>(op, v, x0, y0, n, 0);
+    __syncthreads();
+    plane_top_color<T, DW, DH, 2>(op, v, x0, y0, n, 1);
+    __syncthreads();
+    // residual of the colour-0 component over b; the colour-1 one is zero
+    TILE_FOR(DH - 6, DW - 6, 3, 3, ty, tx) {
+        const int gy = y0 + ty;
+        if (gy < 0 || gy >= n) continue;
+        const int o = ty * DW + tx;
+        const bool ux = ((x0 + tx + gy) & 1) == 0;
+        T r = 0;
+        if (gy != 0 && gy != n - 1) {
+            const T *S = v + (ux ? 0 : P), *O = v + (ux ? P : 0);
+            const T cl = ux ? op.Kmx : op.mx, cd = ux ? op.my : op.Kmy, cc = ux ? op.cxx : op.cyy;
+            const T a = cl * (S[o - 1] + S[o + 1]) + cd * (S[o - DW] + S[o + DW]) +
+                        op.qK * (O[o - DW - 1] + O[o + DW + 1] - O[o - DW + 1] - O[o + DW - 1]);
+            r = v[(ux ? 2 * P : 3 * P) + o] - a - cc * S[o];
+        }
+        v[(ux ? 2 * P : 3 * P) + o] = r;
+        v[(ux ? 3 * P : 2 * P) + o] = 0;
+    }
+    __syncthreads();
+    {
+        // full weighting (1,2,1)x(1,2,1)/4 on the periodic even line,
+        // rows through halves_of for the walls
+        const int cI = threadIdx.x, cJ = threadIdx.y, I = I0 + cI, J = J0 + cJ;
+        if (I < cm && J < cn) {
+            T ax = 0, ay = 0;
+#pragma unroll
+            for (int dy = -1; dy <= 1; dy++) {
+                const int fy = 2 * J + dy;
+                if (fy < 0 || fy >= n) continue;
+                const int hy = halves_of(fy, n, 0, J);
+                if (!hy) continue;
+                const int o = (2 * cJ + 4 + dy) * DW + 2 * cI + 4;
+#pragma unroll
+                for (int dx = -1; dx <= 1; dx++) {
+                    const T wgt = (T)((dx == 0 ? 2 : 1) * hy) * (T)0.25;
+                    ax += wgt * v[2 * P + o + dx];
+                    ay += wgt * v[3 * P + o + dx];
+                }
+            }
+            V w;
+            w.x = ax;
+            w.y = ay;
+            bc[(size_t)J * cm + I] = w;
+        }
+    }
+    TILE_FOR(2 * TCY, 2 * TCX, 4, 4, ty, tx) {
+        const int gy = y0 + ty, gx = x0 + tx;
+        if (gy < n && gx < m) {
+            const int o = ty * DW + tx;
+            V w;
+            w.x = v[o];
+            w.y = v[P + o];
+            z[(size_t)gy * m + gx] = w;
+        }
+    }
+}
+
+// Prolongation + post-smooth of the top level (apply_t of level 0, then
+// up_gs_iterations, tgmg.in.cc:323-327).
+template <typename T>
+__global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
+                                                       const typename vec2_t<T>::type *__restrict__ b, int m, int n,
+                                                       const typename vec2_t<T>::type *__restrict__ zc, int cm,
+                                                       int cn) {
+    typedef typename vec2_t<T>::type V;
+    constexpr int P = plane_stride<UW, UH>();
+    constexpr int CW = TCX + 3, CH = TCY + 3, CP = plane_stride<CW, CH>();
+    __shared__ T v[4 * P];
+    __shared__ T cs[2 * CP];
+    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int x0 = 2 * I0 - 2, y0 = 2 * J0 - 2;
+    TILE_FOR(UH, UW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
+        V zz, bb;
+        zz.x = zz.y = bb.x = bb.y = 0;
+        if (gy >= 0 && gy < n) {
+            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
+            zz = z[g];
+            bb = b[g];
+        }
+        const int o = ty * UW + tx;
+        v[o] = zz.x;
+        v[P + o] = zz.y;
+        v[2 * P + o] = bb.x;
+        v[3 * P + o] = bb.y;
+    }
+    TILE_FOR(CH, CW, 0, 0, ly, lx) {
+        const int J = J0 - 1 + ly;
+        V w;
+        w.x = w.y = 0;
+        if (J >= 0 && J < cn) w = zc[(size_t)J * cm + wrapx(I0 - 1 + lx, cm)];
+        cs[ly * CW + lx] = w.x;
+        cs[CP + ly * CW + lx] = w.y;
+    }
+    __syncthreads();
+    TILE_FOR(UH, UW, 0, 0, ty, tx) {
+        const int gy = y0 + ty;
+        if (gy < 0 || gy >= n) continue;
+        int cy[2], hy[2];
+        const int ny = p1d_halves(gy, n, 0, cy, hy);
+        // even periodic line: even fine points inject, odd ones average
+        const int gx = wrapx(x0 + tx, m);
+        const int c0 = gx >> 1, c1 = (gx == m - 1) ? 0 : c0 + 1;
+        const bool odd = gx & 1;
+        int l0 = c0 - (I0 - 1), l1 = c1 - (I0 - 1);
+        l0 += l0 < 0 ? cm : (l0 >= cm ? -cm : 0);
+        l1 += l1 < 0 ? cm : (l1 >= cm ? -cm : 0);
+        T ax = 0, ay = 0;
+        bool inside = true;
+        for (int q = 0; q < ny; q++) {
+            const int ly = cy[q] - (J0 - 1);
+            if (ly < 0 || ly >= CH || l0 < 0 || l0 >= CW || (odd && (l1 < 0 || l1 >= CW))) {
+                // wrapped copies far beyond a partial tile's owned columns:
+                // no owned output depends on them
+                inside = false;
+                continue;
+            }
+            const T wy = (T)hy[q] * (T)0.25;
+            if (odd) {
+                ax += wy * (cs[ly * CW + l0] + cs[ly * CW + l1]);
+                ay += wy * (cs[CP + ly * CW + l0] + cs[CP + ly * CW + l1]);
+            } else {
+                ax += (T)2 * wy * cs[ly * CW + l0];
+                ay += (T)2 * wy * cs[CP + ly * CW + l0];
+            }
+        }
+        if (!inside) ax = ay = 0;
+        const int o = ty * UW + tx;
+        v[o] += ax;
+        v[P + o] += ay;
+    }
+    __syncthreads();
+    plane_top_color<T, UW, UH, 1>(op, v, x0, y0, n, 0);
+    __syncthreads();
+    plane_top_color<T, UW, UH, 2>(op, v, x0, y0, n, 1);
+    __syncthreads();
+    TILE_FOR(2 * TCY, 2 * TCX, 2, 2, ty, tx) {
+        const int gy = y0 + ty, gx = x0 + tx;
+        if (gy < n && gx < m) {
+            const int o = ty * UW + tx;
+            V w;
+            w.x = v[o];
+            w.y = v[P + o];
+            z[(size_t)gy * m + gx] = w;
+        }
+    }
 }
 
 // Full weighting of the residual held in rs at coarse point (I, J); the fine
@@ -1058,133 +1202,6 @@ __device__ __forceinline__ typename vec2_t<T>::type restrict_at(typename vec2_t<
     o.y = ay;
     (void)I;
     return o;
-}
-
-// Pre-smooth + residual + restriction of the top level (apply_r after one
-// gauss_seidel, tgmg.in.cc:313-320).
-template <typename T>
-__global__ void __launch_bounds__(kFusedThreads) k_top_down(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
-                                                         const typename vec2_t<T>::type *__restrict__ b, int m,
-                                                         int n, typename vec2_t<T>::type *__restrict__ bc, int cm,
-                                                         int cn) {
-    typedef typename vec2_t<T>::type V;
-    __shared__ V zs[DH][DW];
-    __shared__ V bs[DH][DW];
-    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
-    const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
-    TILE_FOR(DH, DW, 0, 0, ty, tx) {
-        const int gy = y0 + ty;
-        V zz, bb;
-        zz.x = zz.y = bb.x = bb.y = 0;
-        if (gy >= 0 && gy < n) {
-            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
-            zz = z[g];
-            bb = b[g];
-        }
-        zs[ty][tx] = zz;
-        bs[ty][tx] = bb;
-    }
-    __syncthreads();
-    tile_top_color<T, DW, DH, 1>(op, zs, bs, x0, y0, n, 0);
-    __syncthreads();
-    tile_top_color<T, DW, DH, 2>(op, zs, bs, x0, y0, n, 1);
-    __syncthreads();
-    TILE_FOR(DH - 6, DW - 6, 3, 3, ty, tx) {
-        const int gy = y0 + ty;
-        if (gy >= 0 && gy < n) top_residual_at<T, DW>(op, zs, bs, ty, tx, gy == 0 || gy == n - 1);
-    }
-    __syncthreads();
-    {
-        const int cI = threadIdx.x, cJ = threadIdx.y, I = I0 + cI, J = J0 + cJ;
-        if (I < cm && J < cn) bc[(size_t)J * cm + I] = restrict_at<T, DW>(bs, I, J, n, 2 * cI + 4, 2 * cJ + 4);
-    }
-    TILE_FOR(2 * TCY, 2 * TCX, 4, 4, ty, tx) {
-        const int gy = y0 + ty, gx = x0 + tx;
-        if (gy < n && gx < m) z[(size_t)gy * m + gx] = zs[ty][tx];
-    }
-}
-
-// Prolongation + post-smooth of the top level (apply_t of level 0, then
-// up_gs_iterations, tgmg.in.cc:323-327).
-template <typename T>
-__global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
-                                                       const typename vec2_t<T>::type *__restrict__ b, int m, int n,
-                                                       const typename vec2_t<T>::type *__restrict__ zc, int cm,
-                                                       int cn) {
-    typedef typename vec2_t<T>::type V;
-    __shared__ V zs[UH][UW];
-    __shared__ V bs[UH][UW];
-    __shared__ V cs[TCY + 3][TCX + 3];
-    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
-    const int x0 = 2 * I0 - 2, y0 = 2 * J0 - 2;
-    TILE_FOR(UH, UW, 0, 0, ty, tx) {
-        const int gy = y0 + ty;
-        V zz, bb;
-        zz.x = zz.y = bb.x = bb.y = 0;
-        if (gy >= 0 && gy < n) {
-            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
-            zz = z[g];
-            bb = b[g];
-        }
-        zs[ty][tx] = zz;
-        bs[ty][tx] = bb;
-    }
-    TILE_FOR(TCY + 3, TCX + 3, 0, 0, ly, lx) {
-        const int J = J0 - 1 + ly;
-        V v;
-        v.x = v.y = 0;
-        if (J >= 0 && J < cn) v = zc[(size_t)J * cm + wrapx(I0 - 1 + lx, cm)];
-        cs[ly][lx] = v;
-    }
-    __syncthreads();
-    TILE_FOR(UH, UW, 0, 0, ty, tx) {
-        const int gy = y0 + ty;
-        if (gy < 0 || gy >= n) continue;
-        int cy[2], hy[2];
-        const int ny = p1d_halves(gy, n, 0, cy, hy);
-        {
-            // even periodic line: even fine points inject, odd ones average
-            const int gx = wrapx(x0 + tx, m);
-            const int c0 = gx >> 1, c1 = (gx == m - 1) ? 0 : c0 + 1;
-            const bool odd = gx & 1;
-            int l0 = c0 - (I0 - 1), l1 = c1 - (I0 - 1);
-            l0 += l0 < 0 ? cm : (l0 >= cm ? -cm : 0);
-            l1 += l1 < 0 ? cm : (l1 >= cm ? -cm : 0);
-            T ax = 0, ay = 0;
-            bool inside = true;
-            for (int q = 0; q < ny; q++) {
-                const int ly = cy[q] - (J0 - 1);
-                if (ly < 0 || ly >= TCY + 3 || l0 < 0 || l0 >= TCX + 3 || (odd && (l1 < 0 || l1 >= TCX + 3))) {
-                    // wrapped copies far beyond a partial tile's owned columns:
-                    // no owned output depends on them
-                    inside = false;
-                    continue;
-                }
-                const T wy = (T)hy[q] * (T)0.25;
-                if (odd) {
-                    const V v0 = cs[ly][l0], v1 = cs[ly][l1];
-                    ax += wy * (v0.x + v1.x);
-                    ay += wy * (v0.y + v1.y);
-                } else {
-                    const V v0 = cs[ly][l0];
-                    ax += (T)2 * wy * v0.x;
-                    ay += (T)2 * wy * v0.y;
-                }
-            }
-            if (!inside) ax = ay = 0;
-            zs[ty][tx].x += ax;
-            zs[ty][tx].y += ay;
-        }
-    }
-    __syncthreads();
-    tile_top_color<T, UW, UH, 1>(op, zs, bs, x0, y0, n, 0);
-    __syncthreads();
-    tile_top_color<T, UW, UH, 2>(op, zs, bs, x0, y0, n, 1);
-    __syncthreads();
-    TILE_FOR(2 * TCY, 2 * TCX, 2, 2, ty, tx) {
-        const int gy = y0 + ty, gx = x0 + tx;
-        if (gy < n && gx < m) z[(size_t)gy * m + gx] = zs[ty][tx];
-    }
 }
 
 // ---------------------------------------------------------------------------
