@@ -355,6 +355,8 @@ template <typename T> int hierarchy<T>::upload_ops(const std::vector<level_ops> 
                 tab[k].e[e].c = (T)L.table[k].e[e].c; tab[k].e[e].d = (T)L.table[k].e[e].d;
             }
         STZG_CHECK(grow(l, tab.size(), L.cls.size()));
+        D.nst = (int)tab.size();
+        D.ncls = (int)L.cls.size();
         STZG_CUDA(cudaMemcpy((void *)D.st, tab.data(), sizeof(stencil9<T>) * tab.size(), cudaMemcpyHostToDevice));
         STZG_CUDA(cudaMemcpy((void *)D.cls, L.cls.data(), sizeof(int) * L.cls.size(), cudaMemcpyHostToDevice));
     }
@@ -1236,11 +1238,32 @@ __device__ __forceinline__ typename vec2_t<T>::type lev_offdiag_tile(const stenc
     return a;
 }
 
+// Stencils of the tile's rows: on an x-homogeneous level the stencil depends
+// on the row only, and the tile's H rows are copied to shared memory once;
+// otherwise each point reads its own class from global memory.
+template <typename T, int H>
+__device__ inline void stage_row_stencils(const level_view<T> &L, stencil9<T> *rows, int y0) {
+    if (!L.homog) return;
+    constexpr int NE = (int)(sizeof(stencil9<T>) / sizeof(T));
+    T *dst = (T *)rows;
+    for (int k = threadIdx.y * blockDim.x + threadIdx.x; k < H * NE; k += blockDim.x * blockDim.y) {
+        const int ty = k / NE, e = k % NE, gy = y0 + ty;
+        if (gy >= 0 && gy < L.n) dst[k] = ((const T *)&L.st[L.cls[gy]])[e];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ const stencil9<T> &tile_stencil(const level_view<T> &L, const stencil9<T> *rows, int ty,
+                                                          int gx, int gy) {
+    return L.homog ? rows[ty] : stencil_at(L, gx, gy);
+}
+
 // Colour (cx, cy) on tile rows/columns [LO, H-1-LO] x [LO, W-1-LO]; the
 // colour's rows and columns are enumerated with compile-time strides.
 template <typename T, int W, int H, int LO>
-__device__ inline void tile_lev_color(const level_view<T> &L, typename vec2_t<T>::type (*zs)[W],
-                                      typename vec2_t<T>::type (*bs)[W], int x0, int y0, int cx, int cy) {
+__device__ inline void tile_lev_color(const level_view<T> &L, const stencil9<T> *rows,
+                                      typename vec2_t<T>::type (*zs)[W], typename vec2_t<T>::type (*bs)[W], int x0,
+                                      int y0, int cx, int cy) {
     typedef typename vec2_t<T>::type V;
     constexpr int NC = (W - 2 * LO + 1) / 2, NRW = (H - 2 * LO + 1) / 2;
     const int ty0 = LO + ((cy - (y0 + LO)) & 1), tx0 = LO + ((cx - (x0 + LO)) & 1);
@@ -1250,7 +1273,7 @@ __device__ inline void tile_lev_color(const level_view<T> &L, typename vec2_t<T>
         if (ty > H - 1 - LO || tx > W - 1 - LO) continue;
         const int gy = y0 + ty;
         if (gy < 0 || gy >= L.n) continue;
-        const stencil9<T> &s = stencil_at(L, wrapx(x0 + tx, L.m), gy);
+        const stencil9<T> &s = tile_stencil(L, rows, ty, wrapx(x0 + tx, L.m), gy);
         const V a = lev_offdiag_tile<T, W>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
         const V bb = bs[ty][tx];
         const T rx = bb.x - a.x, ry = bb.y - a.y;
@@ -1266,8 +1289,10 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, lev
     typedef typename vec2_t<T>::type V;
     __shared__ V zs[LDH][LDW];
     __shared__ V bs[LDH][LDW];
+    __shared__ stencil9<T> rows[LDH];
     const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
     const int x0 = 2 * I0 - 6, y0 = 2 * J0 - 6;
+    stage_row_stencils<T, LDH>(L, rows, y0);
     TILE_FOR(LDH, LDW, 0, 0, ty, tx) {
         const int gy = y0 + ty;
         V bb, zz;
@@ -1277,18 +1302,18 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, lev
         bs[ty][tx] = bb;
     }
     __syncthreads();
-    tile_lev_color<T, LDW, LDH, 1>(L, zs, bs, x0, y0, 0, 0);
+    tile_lev_color<T, LDW, LDH, 1>(L, rows, zs, bs, x0, y0, 0, 0);
     __syncthreads();
-    tile_lev_color<T, LDW, LDH, 2>(L, zs, bs, x0, y0, 1, 0);
+    tile_lev_color<T, LDW, LDH, 2>(L, rows, zs, bs, x0, y0, 1, 0);
     __syncthreads();
-    tile_lev_color<T, LDW, LDH, 3>(L, zs, bs, x0, y0, 0, 1);
+    tile_lev_color<T, LDW, LDH, 3>(L, rows, zs, bs, x0, y0, 0, 1);
     __syncthreads();
-    tile_lev_color<T, LDW, LDH, 4>(L, zs, bs, x0, y0, 1, 1);
+    tile_lev_color<T, LDW, LDH, 4>(L, rows, zs, bs, x0, y0, 1, 1);
     __syncthreads();
     TILE_FOR(LDH - 10, LDW - 10, 5, 5, ty, tx) {
         const int gy = y0 + ty;
         if (gy < 0 || gy >= L.n) continue;
-        const stencil9<T> &s = stencil_at(L, wrapx(x0 + tx, L.m), gy);
+        const stencil9<T> &s = tile_stencil(L, rows, ty, wrapx(x0 + tx, L.m), gy);
         V a = lev_offdiag_tile<T, LDW>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
         madd(a, s.e[4], zs[ty][tx]);
         V r;
@@ -1313,8 +1338,10 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
     __shared__ V zs[LUH][LUW];
     __shared__ V bs[LUH][LUW];
     __shared__ V cs[TCY + 5][TCX + 5];
+    __shared__ stencil9<T> rows[LUH];
     const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
     const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
+    stage_row_stencils<T, LUH>(L, rows, y0);
     TILE_FOR(LUH, LUW, 0, 0, ty, tx) {
         const int gy = y0 + ty;
         V zz, bb;
@@ -1372,13 +1399,13 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
         }
     }
     __syncthreads();
-    tile_lev_color<T, LUW, LUH, 1>(L, zs, bs, x0, y0, 0, 0);
+    tile_lev_color<T, LUW, LUH, 1>(L, rows, zs, bs, x0, y0, 0, 0);
     __syncthreads();
-    tile_lev_color<T, LUW, LUH, 2>(L, zs, bs, x0, y0, 1, 0);
+    tile_lev_color<T, LUW, LUH, 2>(L, rows, zs, bs, x0, y0, 1, 0);
     __syncthreads();
-    tile_lev_color<T, LUW, LUH, 3>(L, zs, bs, x0, y0, 0, 1);
+    tile_lev_color<T, LUW, LUH, 3>(L, rows, zs, bs, x0, y0, 0, 1);
     __syncthreads();
-    tile_lev_color<T, LUW, LUH, 4>(L, zs, bs, x0, y0, 1, 1);
+    tile_lev_color<T, LUW, LUH, 4>(L, rows, zs, bs, x0, y0, 1, 1);
     __syncthreads();
     TILE_FOR(2 * TCY, 2 * TCX, 4, 4, ty, tx) {
         const int gy = y0 + ty, gx = x0 + tx;
@@ -1423,37 +1450,64 @@ __device__ void tail_sweep(const level_view<T> &L) {
         }
 }
 
+// Stencil tables and class arrays of the tail levels are copied into shared
+// memory when they are small (x-homogeneous levels: a few stencils and one
+// class per row), so that the sweeps' stencil reads do not wait on L2.
+constexpr size_t kTailStageMax = 16 * 1024;
+
+template <typename T> __host__ __device__ inline size_t tail_stage_bytes(int nst, int ncls) {
+    return sizeof(stencil9<T>) * (size_t)nst + sizeof(int) * (size_t)ncls;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T> H) {
     typedef typename vec2_t<T>::type V;
-    extern __shared__ __align__(16) unsigned char tail_raw[];
+    extern __shared__ __align__(32) unsigned char tail_raw[];
+    __shared__ level_view<T> S[17];  // the levels' views, read by every phase
     double *tsh = (double *)tail_raw;
-    V *p = (V *)(tail_raw + ((sizeof(double) * tl.inv_n + 15) & ~(size_t)15));
-    level_view<T> S[17];
-    for (int l = tl.t; l <= tl.ml; l++) {
-        S[l] = H.lv[l];
-        const int mn = S[l].m * S[l].n;
-        S[l].z = p;
-        p += mn;
-        S[l].b = p;
-        p += mn;
-        S[l].r = p;
-        p += mn;
-    }
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    if (tid == 0) {
+        size_t off = (sizeof(double) * tl.inv_n + 15) & ~(size_t)15;
+        for (int l = tl.t; l <= tl.ml; l++) {
+            S[l] = H.lv[l];
+            const size_t mn = (size_t)S[l].m * S[l].n;
+            S[l].z = (V *)(tail_raw + off);
+            S[l].b = S[l].z + mn;
+            S[l].r = S[l].b + mn;
+            off += 3 * sizeof(V) * mn;
+        }
+        for (int l = tl.t; l < tl.ml; l++) {
+            if (tail_stage_bytes<T>(S[l].nst, S[l].ncls) > kTailStageMax) continue;
+            off = (off + 31) & ~(size_t)31;
+            S[l].st = (const stencil9<T> *)(tail_raw + off);
+            off += sizeof(stencil9<T>) * (size_t)S[l].nst;
+            S[l].cls = (const int *)(tail_raw + off);
+            off += sizeof(int) * (size_t)S[l].ncls;
+        }
+    }
+    __syncthreads();
+    for (int l = tl.t; l < tl.ml; l++) {
+        if (S[l].st == H.lv[l].st) continue;  // not staged
+        T *st = (T *)S[l].st;
+        const T *src = (const T *)H.lv[l].st;
+        const int nt = S[l].nst * (int)(sizeof(stencil9<T>) / sizeof(T));
+        for (int k = tid; k < nt; k += nth) st[k] = src[k];
+        int *cl = (int *)S[l].cls;
+        for (int k = tid; k < S[l].ncls; k += nth) cl[k] = H.lv[l].cls[k];
+    }
     {
+        // the down sweeps start from z = 0 (gauss_seidel_from_zero); coarser
+        // levels get their zero z with their b in the restriction below
         const int mn = S[tl.t].m * S[tl.t].n;
-        for (int k = tid; k < mn; k += nth) S[tl.t].b[k] = H.lv[tl.t].b[k];
+        for (int k = tid; k < mn; k += nth) {
+            S[tl.t].b[k] = H.lv[tl.t].b[k];
+            S[tl.t].z[k].x = 0;
+            S[tl.t].z[k].y = 0;
+        }
     }
     __syncthreads();
     for (int i = tl.t; i < tl.ml; i++) {
         const level_view<T> &L = S[i];
-        const int mn = L.m * L.n;
-        for (int k = tid; k < mn; k += nth) {
-            L.z[k].x = 0;
-            L.z[k].y = 0;
-        }
-        __syncthreads();
         tail_sweep(L);
         for (int jj = threadIdx.y; jj < L.n; jj += blockDim.y)
             for (int ii = threadIdx.x; ii < L.m; ii += blockDim.x) {
@@ -1490,6 +1544,8 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
                 o.x = ax;
                 o.y = ay;
                 C.b[(size_t)J * C.m + I] = o;
+                o.x = o.y = 0;
+                C.z[(size_t)J * C.m + I] = o;
             }
         __syncthreads();
     }
@@ -1543,9 +1599,14 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
 
 constexpr size_t kTailSmem = 200 * 1024;
 
+// Shared memory of the tail from level t: the same partition as k_tail.
 template <typename T> size_t tail_smem_bytes(const hierarchy<T> &h, int t) {
     size_t b = ((sizeof(double) * h.bottom_unknowns + 15) & ~(size_t)15);
     for (int l = t; l < h.nl; l++) b += 3 * sizeof(typename vec2_t<T>::type) * (size_t)h.lv[l].m * h.lv[l].n;
+    for (int l = t; l < h.nl - 1; l++) {
+        const size_t sb = tail_stage_bytes<T>(h.lv[l].nst, h.lv[l].ncls);
+        if (sb <= kTailStageMax) b = ((b + 31) & ~(size_t)31) + sb;
+    }
     return b;
 }
 

@@ -42,6 +42,7 @@ template <typename T> struct level_view {
     const int *cls;       // class index per row or per point (coarse levels)
     const stencil9<T> *st;// stencil table (coarse levels)
     V *z, *b, *r;
+    int nst, ncls;        // entries of st and cls
 };
 
 // All levels by value, for kernels that walk several levels.
