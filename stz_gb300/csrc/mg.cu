@@ -1213,8 +1213,8 @@ __device__ __forceinline__ typename vec2_t<T>::type restrict_at(typename vec2_t<
 // (down_gs_iterations, tgmg.hh:273-279), so only b is read; the residual is
 // restricted to the child.  Up: prolongation of the child plus one sweep.
 
-constexpr int LDW = 2 * TCX + 11, LDH = 2 * TCY + 11;  // down: fine x in [2I0-6, 2I1+4]
-constexpr int LUW = 2 * TCX + 8, LUH = 2 * TCY + 8;    // up:   fine x in [2I0-4, 2I1+3]
+// Coarse tiles of TX x TY points; smaller levels take smaller tiles (more
+// blocks, shorter phases), see lev_tile below.
 
 template <typename T, int W>
 __device__ __forceinline__ typename vec2_t<T>::type lev_offdiag_tile(const stencil9<T> &s,
@@ -1284,13 +1284,14 @@ __device__ inline void tile_lev_color(const level_view<T> &L, const stencil9<T> 
     }
 }
 
-template <typename T>
+template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, level_view<T> C) {
     typedef typename vec2_t<T>::type V;
+    constexpr int LDW = 2 * TX + 11, LDH = 2 * TY + 11;  // fine x in [2I0-6, 2I1+4]
     __shared__ V zs[LDH][LDW];
     __shared__ V bs[LDH][LDW];
     __shared__ stencil9<T> rows[LDH];
-    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int I0 = blockIdx.x * TX, J0 = blockIdx.y * TY;
     const int x0 = 2 * I0 - 6, y0 = 2 * J0 - 6;
     stage_row_stencils<T, LDH>(L, rows, y0);
     TILE_FOR(LDH, LDW, 0, 0, ty, tx) {
@@ -1322,24 +1323,25 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, lev
         bs[ty][tx] = r;
     }
     __syncthreads();
-    {
-        const int cI = threadIdx.x, cJ = threadIdx.y, I = I0 + cI, J = J0 + cJ;
+    TILE_FOR(TY, TX, 0, 0, cJ, cI) {
+        const int I = I0 + cI, J = J0 + cJ;
         if (I < C.m && J < C.n) C.b[(size_t)J * C.m + I] = restrict_at<T, LDW>(bs, I, J, L.n, 2 * cI + 6, 2 * cJ + 6);
     }
-    TILE_FOR(2 * TCY, 2 * TCX, 6, 6, ty, tx) {
+    TILE_FOR(2 * TY, 2 * TX, 6, 6, ty, tx) {
         const int gy = y0 + ty, gx = x0 + tx;
         if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
     }
 }
 
-template <typename T>
+template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level_view<T> C) {
     typedef typename vec2_t<T>::type V;
+    constexpr int LUW = 2 * TX + 8, LUH = 2 * TY + 8;    // fine x in [2I0-4, 2I1+3]
     __shared__ V zs[LUH][LUW];
     __shared__ V bs[LUH][LUW];
-    __shared__ V cs[TCY + 5][TCX + 5];
+    __shared__ V cs[TY + 5][TX + 5];
     __shared__ stencil9<T> rows[LUH];
-    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
+    const int I0 = blockIdx.x * TX, J0 = blockIdx.y * TY;
     const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
     stage_row_stencils<T, LUH>(L, rows, y0);
     TILE_FOR(LUH, LUW, 0, 0, ty, tx) {
@@ -1354,7 +1356,7 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
         zs[ty][tx] = zz;
         bs[ty][tx] = bb;
     }
-    TILE_FOR(TCY + 5, TCX + 5, 0, 0, ly, lx) {
+    TILE_FOR(TY + 5, TX + 5, 0, 0, ly, lx) {
         const int J = J0 - 2 + ly;
         V v;
         v.x = v.y = 0;
@@ -1378,7 +1380,7 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
             bool inside = true;
             for (int q = 0; q < ny; q++) {
                 const int ly = cy[q] - (J0 - 2);
-                if (ly < 0 || ly >= TCY + 5 || l0 < 0 || l0 >= TCX + 5 || (odd && (l1 < 0 || l1 >= TCX + 5))) {
+                if (ly < 0 || ly >= TY + 5 || l0 < 0 || l0 >= TX + 5 || (odd && (l1 < 0 || l1 >= TX + 5))) {
                     inside = false;
                     continue;
                 }
@@ -1407,7 +1409,7 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
     __syncthreads();
     tile_lev_color<T, LUW, LUH, 4>(L, rows, zs, bs, x0, y0, 1, 1);
     __syncthreads();
-    TILE_FOR(2 * TCY, 2 * TCX, 4, 4, ty, tx) {
+    TILE_FOR(2 * TY, 2 * TX, 4, 4, ty, tx) {
         const int gy = y0 + ty, gx = x0 + tx;
         if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
     }
@@ -1668,6 +1670,34 @@ template <typename T> static bool tile_level(const hierarchy<T> &h, const level_
     return h.fuse && sizeof(T) == 4 && L.colors_x == 2 && L.m >= kFusedMinWidth;
 }
 
+// Coarse tile of a tile-kernel level: the largest of 32x8, 16x4 and 8x4
+// coarse points that still gives two blocks per SM; the coarse levels are
+// latency-bound, and a smaller tile shortens every phase of a block.
+inline int lev_tile(int cm, int cn) {
+    const long want = 2L * 152;
+    if ((long)ceil_div(cm, 32) * ceil_div(cn, 8) >= want) return 0;
+    if ((long)ceil_div(cm, 16) * ceil_div(cn, 4) >= want) return 1;
+    return 2;
+}
+
+template <typename T> void launch_lev_down(level_view<T> &L, level_view<T> &C, cudaStream_t st) {
+    switch (lev_tile(C.m, C.n)) {
+        case 0: k_lev_down<T, 32, 8><<<dim3(ceil_div(C.m, 32), ceil_div(C.n, 8)), dim3(32, 8), 0, st>>>(L, C); break;
+        case 1: k_lev_down<T, 16, 4><<<dim3(ceil_div(C.m, 16), ceil_div(C.n, 4)), dim3(32, 8), 0, st>>>(L, C); break;
+        default: k_lev_down<T, 8, 4><<<dim3(ceil_div(C.m, 8), ceil_div(C.n, 4)), dim3(32, 8), 0, st>>>(L, C);
+    }
+    note_launch();
+}
+
+template <typename T> void launch_lev_up(level_view<T> &F, level_view<T> &C, cudaStream_t st) {
+    switch (lev_tile(C.m, C.n)) {
+        case 0: k_lev_up<T, 32, 8><<<dim3(ceil_div(C.m, 32), ceil_div(C.n, 8)), dim3(32, 8), 0, st>>>(F, C); break;
+        case 1: k_lev_up<T, 16, 4><<<dim3(ceil_div(C.m, 16), ceil_div(C.n, 4)), dim3(32, 8), 0, st>>>(F, C); break;
+        default: k_lev_up<T, 8, 4><<<dim3(ceil_div(C.m, 8), ceil_div(C.n, 4)), dim3(32, 8), 0, st>>>(F, C);
+    }
+    note_launch();
+}
+
 template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64) {
     typedef typename vec2_t<T>::type V;
     dim3 blk(32, 8);
@@ -1697,9 +1727,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         level_view<T> &L = h.lv[i];
         level_view<T> &C = h.lv[i + 1];
         if (tile_level(h, L)) {
-            dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
-            k_lev_down<T><<<g, dim3(32, 8), 0, st>>>(L, C);
-            note_launch();
+            launch_lev_down(L, C, st);
             continue;
         }
         cudaMemsetAsync(L.z, 0, sizeof(V) * (size_t)L.m * L.n, st);
@@ -1733,9 +1761,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     for (int i = up_from; i >= 2; i--) {
         level_view<T> &C = h.lv[i], &F = h.lv[i - 1];
         if (tile_level(h, F)) {
-            dim3 g(ceil_div(C.m, TCX), ceil_div(C.n, TCY));
-            k_lev_up<T><<<g, dim3(32, 8), 0, st>>>(F, C);
-            note_launch();
+            launch_lev_up(F, C, st);
             continue;
         }
         k_prolong_add<T><<<grid2(F.m, F.n, blk), blk, 0, st>>>(C.z, C.m, C.n, F.z, F.m, F.n);
