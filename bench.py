@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--size", type=int, default=GRID)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-extrapolate", action="store_true")
+    ap.add_argument("--extrapolate-order", type=int, default=1, choices=[1, 2],
+                    help="initial guess: 1 linear, 2 quadratic extrapolation of the last solutions")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--fp64-steps", type=int, default=0, help="FP64 comparison steps (0: = steps+warmup, capped)")
     ap.add_argument("--skip-cpu", action="store_true")
@@ -225,7 +227,7 @@ def run_ours(args, dist):
     P = make_params(N)
     chi = random_chi(N, N, CHI["l"], CHI["tem_avg"], CHI["tem_std"], P.TZ, 2 + dist.rank)
     prec = _lib.MIXED if args.precision == "mixed" else _lib.FP64
-    extrap = not args.no_extrapolate
+    extrap = 0 if args.no_extrapolate else args.extrapolate_order
     sim = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, device=dist.local,
                    extrapolate=extrap, inner_cycles=args.inner)
     sim.steps(DT, args.warmup)

@@ -59,8 +59,9 @@ typedef struct {
     int device;        /* CUDA device ordinal */
     int inner_cycles;  /* mixed precision: FP32 V-cycles per refinement pass (0: auto) */
     int use_graphs;    /* capture the V-cycle in a CUDA graph (1 default) */
-    int extrapolate;   /* initial guess of each solve: 2 v(n) - v(n-1) instead of the
-                          previous solution v(n) (tgmg keeps z between solves) */
+    int extrapolate;   /* initial guess of each solve instead of the previous solution
+                          v(n) (tgmg keeps z between solves): 1 = linear, 2v(n) - v(n-1);
+                          2 = quadratic, 3v(n) - 3v(n-1) + v(n-2) */
     int substep_cap;   /* iteration cap of the plastic sub-stepping per cell and step
                           (0: 4194304); reaching it returns STZG_ESUBSTEP */
     int reserved[6];
@@ -114,7 +115,9 @@ int stzg_get_time(stzg_sim *s, double *time);
  * p, q, s, tau, chi (m*(n+2) with ghost rows), X, Y (m*(n+1)), vel
  * (m*(n+1) x,y pairs, the solver array).  down[9]: the same plus eps_pl
  * (m*n).  Entries may be NULL to skip a field.  Time and wall speed are
- * kept.  Pinned host memory gives full copy bandwidth. */
+ * kept.  An uploaded vel that is bit-identical to the device's keeps the
+ * solver's history for extrapolated initial guesses; any other vel restarts
+ * it.  Pinned host memory gives full copy bandwidth. */
 int stzg_upload(stzg_sim *s, const double *const *up);
 int stzg_download(stzg_sim *s, double *const *down);
 

@@ -494,7 +494,7 @@ namespace stzg {
 struct host_state {
     double time = 0, bv = 0;
     int lim = 0;
-    bool have_prev = false;
+    bool have_prev = false, have_prev2 = false;
 };
 }  // namespace stzg
 
@@ -553,7 +553,7 @@ int adj_alloc(stzg_sim *s, stzg_adjoint *a, void *p, size_t bytes) {
 // repeats the forward run bit for bit.
 size_t slab_doubles(const stzg_sim *s) {
     const size_t nc = cell_count(s), nn = (size_t)s->m * (s->n + 1);
-    return 7 * nc + 2 * nn + (size_t)s->m * s->n + (s->vel_prev ? 2 * nn : 0);
+    return 7 * nc + 2 * nn + (size_t)s->m * s->n + (s->vel_prev ? 2 * nn : 0) + (s->vel_prev2 ? 2 * nn : 0);
 }
 
 host_state save_state(stzg_sim *s, double *slab, int *status) {
@@ -566,12 +566,15 @@ host_state save_state(stzg_sim *s, double *slab, int *status) {
         e = cudaMemcpyAsync(slab + 7 * nc + 2 * nn, s->F.eps_pl, mn * 8, cudaMemcpyDeviceToDevice, s->st);
     if (e == cudaSuccess && s->vel_prev)
         e = cudaMemcpyAsync(slab + 7 * nc + 2 * nn + mn, s->vel_prev, nn * 16, cudaMemcpyDeviceToDevice, s->st);
+    if (e == cudaSuccess && s->vel_prev2)
+        e = cudaMemcpyAsync(slab + 7 * nc + 4 * nn + mn, s->vel_prev2, nn * 16, cudaMemcpyDeviceToDevice, s->st);
     *status = e == cudaSuccess ? STZG_OK : cuda_fail(e, "cudaMemcpyAsync(checkpoint)");
     host_state h;
     h.time = s->time;
     h.bv = s->bv_state;
     h.lim = s->lim;
     h.have_prev = s->have_prev;
+    h.have_prev2 = s->have_prev2;
     return h;
 }
 
@@ -584,11 +587,14 @@ int load_state(stzg_sim *s, const double *slab, const host_state &h) {
     STZG_CUDA(cudaMemcpyAsync(s->F.eps_pl, slab + 7 * nc + 2 * nn, mn * 8, cudaMemcpyDeviceToDevice, s->st));
     if (s->vel_prev)
         STZG_CUDA(cudaMemcpyAsync(s->vel_prev, slab + 7 * nc + 2 * nn + mn, nn * 16, cudaMemcpyDeviceToDevice, s->st));
+    if (s->vel_prev2)
+        STZG_CUDA(cudaMemcpyAsync(s->vel_prev2, slab + 7 * nc + 4 * nn + mn, nn * 16, cudaMemcpyDeviceToDevice, s->st));
     s->cur = 0;
     s->time = h.time;
     s->bv_state = h.bv;
     s->lim = h.lim;
     s->have_prev = h.have_prev;
+    s->have_prev2 = h.have_prev2;
     return STZG_OK;
 }
 

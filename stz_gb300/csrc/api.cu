@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "mg.cuh"
@@ -269,7 +270,14 @@ int do_projection(stzg_sim *s, double dt, bool fresh_combinations) {
     projection_source(s->sc, s->F, s->cur, dt, s->q.bcs * s->q.cxx * bv, s->st);
     if (s->O.extrapolate) {
         const long cnt = (long)s->m * (s->n + 1);
-        if (s->have_prev) {
+        if (s->have_prev && s->O.extrapolate >= 2 && s->have_prev2) {
+            extrapolate_guess2(s->F.vel, s->vel_prev, s->vel_prev2, cnt, s->st);
+        } else if (s->have_prev) {
+            if (s->O.extrapolate >= 2) {
+                STZG_CUDA(cudaMemcpyAsync(s->vel_prev2, s->vel_prev, cnt * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                          s->st));
+                s->have_prev2 = true;
+            }
             extrapolate_guess(s->F.vel, s->vel_prev, cnt, s->st);
         } else {
             STZG_CUDA(cudaMemcpyAsync(s->vel_prev, s->F.vel, cnt * sizeof(double2), cudaMemcpyDeviceToDevice, s->st));
@@ -371,6 +379,8 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
         if ((st = dev_alloc(s, (void **)&s->F.pre[k], nc * sizeof(double))) != STZG_OK) return bail(st);
     if (o.extrapolate)
         if ((st = dev_alloc(s, (void **)&s->vel_prev, nn * sizeof(double2))) != STZG_OK) return bail(st);
+    if (o.extrapolate >= 2)
+        if ((st = dev_alloc(s, (void **)&s->vel_prev2, nn * sizeof(double2))) != STZG_OK) return bail(st);
     s->npart = reduction_blocks();
     if ((st = dev_alloc(s, (void **)&s->partials, 2 * s->npart * sizeof(double))) != STZG_OK) return bail(st);
     if ((st = dev_alloc(s, (void **)&s->dnorm, 2 * sizeof(double))) != STZG_OK) return bail(st);
@@ -395,6 +405,11 @@ int stzg_destroy(stzg_sim *s) {
     if (s->st) cudaStreamSynchronize(s->st);
     drop_graphs(s);
     adjoint_release(s);
+    for (int k = 0; k < stzg_sim::kCopyStreams; k++) {
+        if (s->cst[k]) cudaStreamDestroy(s->cst[k]);
+        if (s->cev[k]) cudaEventDestroy(s->cev[k]);
+    }
+    if (s->cev_ready) cudaEventDestroy(s->cev_ready);
     for (void *p : s->owned) cudaFree(p);
     s->h64.release();
     s->h32.release();
@@ -438,7 +453,7 @@ int stzg_set_state(stzg_sim *s, const double *chi) {
     s->time = 0;
     s->bv_state = 0;
     s->cur = 0;
-    s->have_prev = false;
+    s->have_prev = s->have_prev2 = false;
     return STZG_OK;
 }
 
@@ -503,7 +518,7 @@ int stzg_set_field(stzg_sim *s, int field, const double *host) {
         STZG_CUDA(cudaMemcpy(v.data(), s->F.vel, nn * sizeof(double2), cudaMemcpyDeviceToHost));
         for (size_t k = 0; k < nn; k++) (field == STZG_U ? v[k].x : v[k].y) = host[k];
         STZG_CUDA(cudaMemcpy(s->F.vel, v.data(), nn * sizeof(double2), cudaMemcpyHostToDevice));
-        s->have_prev = false;
+        s->have_prev = s->have_prev2 = false;
         // walls carry +-bv on u and 0 on v (set_boundaries, shear_sim.cc:557-572)
         if (field == STZG_U) s->bv_state = host[(size_t)n * m];
         return STZG_OK;
@@ -570,10 +585,68 @@ int stzg_step_qs(stzg_sim *s, double dt, int nsteps, stzg_stats *stats) {
     return STZG_OK;
 }
 
+// Bulk transfers: the field copies are spread over kCopyStreams streams so
+// that several copy engines move data at once; they start after the work
+// already queued on the handle's stream and the call returns when all are
+// done.
+static int copy_streams(stzg_sim *s) {
+    if (s->cev_ready) return STZG_OK;
+    for (int k = 0; k < stzg_sim::kCopyStreams; k++) {
+        STZG_CUDA(cudaStreamCreateWithFlags(&s->cst[k], cudaStreamNonBlocking));
+        STZG_CUDA(cudaEventCreateWithFlags(&s->cev[k], cudaEventDisableTiming));
+    }
+    STZG_CUDA(cudaEventCreateWithFlags(&s->cev_ready, cudaEventDisableTiming));
+    return STZG_OK;
+}
+
+struct copy_job {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+
+static int run_copies(stzg_sim *s, const std::vector<copy_job> &jobs, cudaMemcpyKind kind) {
+    STZG_CHECK(copy_streams(s));
+    STZG_CUDA(cudaEventRecord(s->cev_ready, s->st));
+    const int ns = stzg_sim::kCopyStreams;
+    for (int k = 0; k < ns; k++) STZG_CUDA(cudaStreamWaitEvent(s->cst[k], s->cev_ready, 0));
+    // every copy in ns pieces of whole 8-byte words, one per stream
+    for (const copy_job &j : jobs) {
+        const size_t words = j.bytes / 8, per = (words + ns - 1) / ns;
+        for (int k = 0; k < ns; k++) {
+            const size_t w0 = (size_t)k * per, w1 = std::min(words, w0 + per);
+            if (w1 <= w0) continue;
+            STZG_CUDA(cudaMemcpyAsync((char *)j.dst + 8 * w0, (const char *)j.src + 8 * w0, 8 * (w1 - w0), kind,
+                                      s->cst[k]));
+        }
+    }
+    for (int k = 0; k < ns; k++) {
+        STZG_CUDA(cudaEventRecord(s->cev[k], s->cst[k]));
+        STZG_CUDA(cudaStreamWaitEvent(s->st, s->cev[k], 0));
+    }
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+// Installs an uploaded velocity (staged in src, which every step rewrites)
+// and flags whether it differs bitwise from the velocity it replaces.
+__global__ void k_accept_vel(const double2 *__restrict__ staged, double2 *__restrict__ vel, long count,
+                             int *changed) {
+    int diff = 0;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        const double2 a = staged[k], b = vel[k];
+        diff |= (__double_as_longlong(a.x) != __double_as_longlong(b.x)) |
+                (__double_as_longlong(a.y) != __double_as_longlong(b.y));
+        vel[k] = a;
+    }
+    if (__syncthreads_or(diff) && threadIdx.x == 0) atomicExch(changed, 1);
+}
+
 int stzg_upload(stzg_sim *s, const double *const *up) {
     if (!s || !up) return fail(STZG_EINVAL, "null argument");
     const int m = s->m;
     const size_t nn = (size_t)m * (s->n + 1), nc = cell_count(s);
+    std::vector<copy_job> jobs;
     for (int k = 0; k < 7; k++) {
         if (!up[k]) continue;
         double *dst = s->F.f[s->cur][k];
@@ -582,13 +655,23 @@ int stzg_upload(stzg_sim *s, const double *const *up) {
             dst += m;
             cnt = nn;
         }
-        STZG_CUDA(cudaMemcpyAsync(dst, up[k], cnt * 8, cudaMemcpyHostToDevice, s->st));
+        jobs.push_back({dst, up[k], cnt * 8});
     }
+    // The velocity goes through a staging copy: when it is bit-identical to
+    // the one on the device (a caller that downloads and uploads the state
+    // around every step), the solver keeps its history for the extrapolated
+    // initial guess; any other velocity restarts that history.
+    if (up[7]) jobs.push_back({s->F.src, up[7], nn * sizeof(double2)});
+    STZG_CHECK(run_copies(s, jobs, cudaMemcpyHostToDevice));
     if (up[7]) {
-        STZG_CUDA(cudaMemcpyAsync(s->F.vel, up[7], nn * sizeof(double2), cudaMemcpyHostToDevice, s->st));
-        s->have_prev = false;
+        STZG_CUDA(cudaMemsetAsync(s->F.flags + 2, 0, sizeof(int), s->st));
+        k_accept_vel<<<4 * 152, 256, 0, s->st>>>(s->F.src, s->F.vel, (long)nn, s->F.flags + 2);
+        note_launch();
+        int changed = 0;
+        STZG_CUDA(cudaMemcpyAsync(&changed, s->F.flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+        if (changed) s->have_prev = s->have_prev2 = false;
     }
-    STZG_CUDA(cudaStreamSynchronize(s->st));
     return STZG_OK;
 }
 
@@ -596,6 +679,7 @@ int stzg_download(stzg_sim *s, double *const *down) {
     if (!s || !down) return fail(STZG_EINVAL, "null argument");
     const int m = s->m;
     const size_t nn = (size_t)m * (s->n + 1), nc = cell_count(s);
+    std::vector<copy_job> jobs;
     for (int k = 0; k < 7; k++) {
         if (!down[k]) continue;
         const double *src = s->F.f[s->cur][k];
@@ -604,13 +688,11 @@ int stzg_download(stzg_sim *s, double *const *down) {
             src += m;
             cnt = nn;
         }
-        STZG_CUDA(cudaMemcpyAsync(down[k], src, cnt * 8, cudaMemcpyDeviceToHost, s->st));
+        jobs.push_back({down[k], src, cnt * 8});
     }
-    if (down[7]) STZG_CUDA(cudaMemcpyAsync(down[7], s->F.vel, nn * sizeof(double2), cudaMemcpyDeviceToHost, s->st));
-    if (down[8])
-        STZG_CUDA(cudaMemcpyAsync(down[8], s->F.eps_pl, (size_t)m * s->n * 8, cudaMemcpyDeviceToHost, s->st));
-    STZG_CUDA(cudaStreamSynchronize(s->st));
-    return STZG_OK;
+    if (down[7]) jobs.push_back({down[7], s->F.vel, nn * sizeof(double2)});
+    if (down[8]) jobs.push_back({down[8], s->F.eps_pl, (size_t)m * s->n * 8});
+    return run_copies(s, jobs, cudaMemcpyDeviceToHost);
 }
 
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {

@@ -737,6 +737,18 @@ __global__ void k_mixed_correct(double2 *__restrict__ z, const float2 *__restric
     }
 }
 
+// Quadratic extrapolation through the last three solutions:
+// z <- 3 z - 3 prev + prev2, prev2 <- prev, prev <- old z.
+__global__ void k_extrapolate2(double2 *__restrict__ z, double2 *__restrict__ prev, double2 *__restrict__ prev2,
+                               long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        const double2 a = z[k], p = prev[k], q = prev2[k];
+        prev2[k] = p;
+        prev[k] = a;
+        z[k] = make_double2(3 * (a.x - p.x) + q.x, 3 * (a.y - p.y) + q.y);
+    }
+}
+
 __global__ void k_extrapolate(double2 *__restrict__ z, double2 *__restrict__ prev, long count) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
         double2 a = z[k], p = prev[k];
@@ -1825,6 +1837,10 @@ void ff_residual(const top_op<double> &o, const float2 *zhi, const float2 *zlo, 
 
 void mixed_correct(double2 *z64, const float2 *e32, long count, cudaStream_t st) {
     k_mixed_correct<<<4 * 152, 256, 0, st>>>(z64, e32, count); note_launch();
+}
+
+void extrapolate_guess2(double2 *z, double2 *prev, double2 *prev2, long count, cudaStream_t st) {
+    k_extrapolate2<<<4 * 152, 256, 0, st>>>(z, prev, prev2, count); note_launch();
 }
 
 void extrapolate_guess(double2 *z, double2 *prev, long count, cudaStream_t st) {

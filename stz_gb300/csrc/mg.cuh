@@ -135,6 +135,8 @@ void ff_residual(const top_op<double> &op64, const float2 *zhi, const float2 *zl
                  double *out_b, cudaStream_t st);
 // Linear extrapolation of the initial guess: z <- 2 z - prev, prev <- old z.
 void extrapolate_guess(double2 *z, double2 *prev, long count, cudaStream_t st);
+// Quadratic: z <- 3 z - 3 prev + prev2, prev2 <- prev, prev <- old z.
+void extrapolate_guess2(double2 *z, double2 *prev, double2 *prev2, long count, cudaStream_t st);
 
 int reduction_blocks();
 

@@ -40,11 +40,17 @@ struct stzg_sim {
     long n_vc64 = 0, n_res32 = 0, n_pass32 = 0;  // kernel nodes per graph
     int g_inner = 0;
     double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)
+    double2 *vel_prev2 = nullptr; // the one before (quadratic extrapolation)
+    bool have_prev2 = false;
     // mixed precision: float-float copies (hi + lo) of the iterate and of the
     // right-hand side for the duration of a solve
     float2 *zhi = nullptr, *zlo = nullptr, *bhi = nullptr, *blo = nullptr;
     bool have_prev = false;
     stzg_adjoint *adj = nullptr;  // adjoint workspace (adjoint.cu), created on first use
+    // bulk host transfers: copies spread over several streams (copy engines)
+    static constexpr int kCopyStreams = 4;
+    cudaStream_t cst[kCopyStreams] = {};
+    cudaEvent_t cev_ready = nullptr, cev[kCopyStreams] = {};
 };
 
 

@@ -172,6 +172,31 @@ def test_upload_download_roundtrip_and_launch_count():
     assert a.stats.kernel_launches > 0
 
 
+def test_state_roundtrip_keeps_extrapolation_history():
+    """A caller that downloads and re-uploads the whole state around every
+    step (host-owned fields) gets the same steps, V-cycle for V-cycle, as one
+    that leaves the state on the device."""
+    N = 64
+    P = simple_shear(N)
+    chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, 4)
+    kw = dict(tol_mode=_lib.TOL_RELATIVE, tol=1e-11, extrapolate=True)
+    a, b = ShearSim(P, chi, **kw), ShearSim(P, chi, **kw)
+    a.steps(0.01, 5)
+    b.steps(0.01, 5)
+    cells, nodes = N * (N + 2), N * (N + 1)
+    bufs = [np.zeros(cells) for _ in range(5)] + [np.zeros(nodes) for _ in range(2)] + [np.zeros(2 * nodes),
+                                                                                       np.zeros(N * N)]
+    ca = cb = 0
+    for _ in range(10):
+        ca += a.steps(0.01, 1)
+        b.download([x.ctypes.data for x in bufs])
+        b.upload([x.ctypes.data for x in bufs[:8]])
+        cb += b.steps(0.01, 1)
+    assert ca == cb
+    err = group_errors(a.fields(), b.fields(), N, fields=("p", "q", "s", "tau", "chi", "X", "Y", "u", "v"))
+    assert max(err.values()) == 0.0, err
+
+
 def test_extrapolated_guess_same_answer_fewer_cycles():
     N = 64
     P = simple_shear(N)
@@ -183,6 +208,20 @@ def test_extrapolated_guess_same_answer_fewer_cycles():
     err = group_errors(a.fields(), b.fields(), N)
     assert max(err.values()) < 1e-9, err
     assert b.cycles < a.cycles
+
+def test_quadratic_guess_same_answer():
+    """extrapolate = 2 (3v(n) - 3v(n-1) + v(n-2)) converges to the same
+    solutions as the linear guess."""
+    N = 64
+    P = simple_shear(N)
+    chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, 4)
+    a = ShearSim(P, chi, tol_mode=_lib.TOL_RELATIVE, tol=1e-11, extrapolate=1)
+    b = ShearSim(P, chi, tol_mode=_lib.TOL_RELATIVE, tol=1e-11, extrapolate=2)
+    a.steps(0.01, 40)
+    b.steps(0.01, 40)
+    err = group_errors(a.fields(), b.fields(), N)
+    assert max(err.values()) < 1e-9, err
+    assert b.cycles <= a.cycles
 
 
 def test_substep_cap_reports_status():
