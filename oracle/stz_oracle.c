@@ -58,7 +58,7 @@ struct stzo_sim {
     double lx, ly, dx, dy, xsp, ysp, mu_inv, bcs;
     double time;
     double *u, *v, *p, *q, *s, *tau, *chi, *X, *Y, *ddev;
-    double *cp, *cq, *cs, *ctau, *cchi, *cX, *cY;
+    double *cp, *cq, *cs, *ctau, *cchi, *cX, *cY, *cu, *cv;
     v2 *vel, *src;
     /* qs_multi constants (qs_multi.cc:9-15, 31-55) */
     double Kq, qK, Kmu, xsp2, ysp2, xyfac, tmufac1, tmufac2;
@@ -177,6 +177,32 @@ static inline double eno2(double p0, double p1, double p2, double p3) {
     return fabs(p0 - 2 * p1 + p2) > fabs(p1 - 2 * p2 + p3) ? 3 * p1 - 4 * p2 + p3 : p0 - p2;
 }
 
+/* chi diffusion, shear_sim::chi_diffusion, shear_sim.cc:364-386: added to
+ * cchi from the old chi and the step's ddev (adds exact zeros when both
+ * coefficients vanish, so it is skipped then) */
+static void chi_diffusion(stzo_sim *S, double dt) {
+    const int m = S->m, n = S->n;
+    const double hx = 0.5 * S->xsp * dt, hy = 0.5 * S->ysp * dt;
+    if (S->P.chi_diff != 0 || S->P.chi_len != 0) {
+        const double hxxcd = 2 * S->xsp * hx * S->P.chi_diff, hyycd = 2 * S->ysp * hy * S->P.chi_diff,
+                     hccd = 2 * (hxxcd + hyycd);
+        const double dfac = 0.25 * S->P.chi_len * S->P.chi_len * S->mu_inv, dfacx = dfac * S->xsp * S->xsp,
+                     dfacy = dfac * S->ysp * S->ysp;
+        const double *ch = S->chi, *dd = S->ddev;
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < m; i++) {
+                const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+                size_t c = CI(S, i, j), cl = CI(S, il, j), cr = CI(S, ir, j), cd = CI(S, i, j - 1),
+                       cu = CI(S, i, j + 1);
+                double Dd = dd[c] + dd[cd], Dl = dd[c] + dd[cl], Dr = dd[c] + dd[cr], Du = dd[c] + dd[cu];
+                S->cchi[c] += hxxcd * (ch[cr] + ch[cl]) + hyycd * (ch[cu] + ch[cd]) - hccd * ch[c]
+                              + dfacx * (Dr * ch[cr] - (Dr + Dl) * ch[c] + Dl * ch[cl])
+                              + dfacy * (Du * ch[cu] - (Du + Dd) * ch[c] + Dd * ch[cd]);
+            }
+    }
+}
+
 /* ---------------------------------------------------------------------- */
 /* Advection + plasticity, shear_sim::advection_step, shear_sim.cc:296-361 */
 
@@ -254,32 +280,159 @@ static void advection_step(stzo_sim *S, double dt) {
             (void)pv;
         }
     }
-    /* chi diffusion, shear_sim.cc:364-386 (adds exact zeros when both
-     * coefficients vanish, so it is skipped then) */
-    if (S->P.chi_diff != 0 || S->P.chi_len != 0) {
-        const double hxxcd = 2 * S->xsp * hx * S->P.chi_diff, hyycd = 2 * S->ysp * hy * S->P.chi_diff,
-                     hccd = 2 * (hxxcd + hyycd);
-        const double dfac = 0.25 * S->P.chi_len * S->P.chi_len * S->mu_inv, dfacx = dfac * S->xsp * S->xsp,
-                     dfacy = dfac * S->ysp * S->ysp;
-        const double *ch = S->chi, *dd = S->ddev;
-#pragma omp parallel for schedule(static)
-        for (int j = 0; j < n; j++)
-            for (int i = 0; i < m; i++) {
-                const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
-                size_t c = CI(S, i, j), cl = CI(S, il, j), cr = CI(S, ir, j), cd = CI(S, i, j - 1),
-                       cu = CI(S, i, j + 1);
-                double Dd = dd[c] + dd[cd], Dl = dd[c] + dd[cl], Dr = dd[c] + dd[cr], Du = dd[c] + dd[cu];
-                S->cchi[c] += hxxcd * (ch[cr] + ch[cl]) + hyycd * (ch[cu] + ch[cd]) - hccd * ch[c]
-                              + dfacx * (Dr * ch[cr] - (Dr + Dl) * ch[c] + Dl * ch[cl])
-                              + dfacy * (Du * ch[cu] - (Du + Dd) * ch[c] + Dd * ch[cd]);
-            }
-    }
+    chi_diffusion(S, dt);
     /* apply the updates, shear_sim.cc:356-360 and fields.hh:61-80 */
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < n; j++)
         for (int i = 0; i < m; i++) {
             size_t c = CI(S, i, j);
             if (j > 0) { S->X[c] += S->cX[c]; S->Y[c] += S->cY[c]; }
+            S->p[c] += S->cp[c];
+            S->q[c] += S->cq[c];
+            S->s[c] += S->cs[c];
+            S->tau[c] += S->ctau[c];
+            S->chi[c] = S->cchi[c];
+        }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Explicit (direct) step, shear_sim::step_forward, shear_sim.cc:185-276:
+ * velocity and reference map advected with ENO2 at the nodes, plus the net
+ * force of the stress (net_force, shear_sim.cc:447-453, prefactors -hx,-hy)
+ * and a 5-point viscous term; the cells take the advection, the elastic
+ * rate from the velocity gradient and the plastic term.  The constant chi
+ * diffusion enters cchi before the plastic term and again in chi_diffusion
+ * (the reference adds it twice), and ddev is stored times the old |s|.
+ * The raw stress drop is returned per cell in raw_ddev for eps_pl. */
+
+static void direct_step(stzo_sim *S, double dt, double *raw_ddev) {
+    const int m = S->m, n = S->n;
+    const double third = 1. / 3;
+    const double hx = 0.5 * S->xsp * dt, hy = 0.5 * S->ysp * dt, lx = S->lx;
+    const double visc = S->P.viscosity;
+    const double hxxv = 2 * S->xsp * hx * visc, hyyv = 2 * S->ysp * hy * visc, hcv = 2 * (hxxv + hyyv);
+    const double hxxcd = 2 * S->xsp * hx * S->P.chi_diff, hyycd = 2 * S->ysp * hy * S->P.chi_diff,
+                 hccd = 2 * (hxxcd + hyycd);
+    const double K = S->P.K, mu = S->P.mu, mu_inv = S->mu_inv;
+    const double *u = S->u, *v = S->v, *X = S->X, *Y = S->Y;
+    const double *fld[5] = {S->p, S->q, S->s, S->tau, S->chi};
+    double *cu = S->cu, *cv = S->cv;
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < n; j++) {
+        for (int i = 0; i < m; i++) {
+            const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+            const int il2 = i <= 1 ? i + m - 2 : i - 2, ir2 = i >= m - 2 ? i + 2 - m : i + 2;
+            const size_t c = CI(S, i, j);
+            double uc, vc;
+            if (j > 0) {
+                double ux, vx, uy, vy, Xx, Yx, Xy, Yy;
+                uc = u[c]; vc = v[c];
+                if (uc > 0) {
+                    ux = hx * eno2(u[CI(S, ir, j)], u[c], u[CI(S, il, j)], u[CI(S, il2, j)]);
+                    vx = hx * eno2(v[CI(S, ir, j)], v[c], v[CI(S, il, j)], v[CI(S, il2, j)]);
+                    Xx = hx * eno2(X[CI(S, ir, j)] + (i == m - 1 ? lx : 0), X[c],
+                                   X[CI(S, il, j)] + (i == 0 ? -lx : 0), X[CI(S, il2, j)] + (i <= 1 ? -lx : 0));
+                    Yx = hx * eno2(Y[CI(S, ir, j)], Y[c], Y[CI(S, il, j)], Y[CI(S, il2, j)]);
+                } else {
+                    ux = -hx * eno2(u[CI(S, il, j)], u[c], u[CI(S, ir, j)], u[CI(S, ir2, j)]);
+                    vx = -hx * eno2(v[CI(S, il, j)], v[c], v[CI(S, ir, j)], v[CI(S, ir2, j)]);
+                    Xx = -hx * eno2(X[CI(S, il, j)] + (i == 0 ? -lx : 0), X[c],
+                                    X[CI(S, ir, j)] + (i == m - 1 ? lx : 0), X[CI(S, ir2, j)] + (i >= m - 2 ? lx : 0));
+                    Yx = -hx * eno2(Y[CI(S, il, j)], Y[c], Y[CI(S, ir, j)], Y[CI(S, ir2, j)]);
+                }
+                if (vc > 0) {
+                    if (j > 1) {
+                        const size_t a = CI(S, i, j + 1), b = CI(S, i, j - 1), d = CI(S, i, j - 2);
+                        uy = hy * eno2(u[a], u[c], u[b], u[d]);
+                        vy = hy * eno2(v[a], v[c], v[b], v[d]);
+                        Xy = hy * eno2(X[a], X[c], X[b], X[d]);
+                        Yy = hy * eno2(Y[a], Y[c], Y[b], Y[d]);
+                    } else {
+                        const size_t b = CI(S, i, j - 1);
+                        uy = 2 * hy * (u[c] - u[b]);
+                        vy = 2 * hy * (v[c] - v[b]);
+                        Xy = 2 * hy * (X[c] - X[b]);
+                        Yy = 2 * hy * (Y[c] - Y[b]);
+                    }
+                } else {
+                    if (j < n - 1) {
+                        const size_t a = CI(S, i, j - 1), b = CI(S, i, j + 1), d = CI(S, i, j + 2);
+                        uy = -hy * eno2(u[a], u[c], u[b], u[d]);
+                        vy = -hy * eno2(v[a], v[c], v[b], v[d]);
+                        Xy = -hy * eno2(X[a], X[c], X[b], X[d]);
+                        Yy = -hy * eno2(Y[a], Y[c], Y[b], Y[d]);
+                    } else {
+                        const size_t b = CI(S, i, j + 1);
+                        uy = 2 * -hy * (u[c] - u[b]);
+                        vy = 2 * -hy * (v[c] - v[b]);
+                        Xy = 2 * -hy * (X[c] - X[b]);
+                        Yy = 2 * -hy * (Y[c] - Y[b]);
+                    }
+                }
+                /* net force from the cells (i-1,j-1), (i,j-1), (i-1,j), (i,j) */
+                const size_t c0 = CI(S, il, j - 1), c1 = CI(S, i, j - 1), c2 = CI(S, il, j), c3 = c;
+                const double *P = S->p, *Q = S->q, *SS = S->s, *T = S->tau;
+                const double xf = -hx, yf = -hy;
+                const double fx = (-P[c0] + P[c1] - P[c2] + P[c3] - Q[c0] + Q[c1] - Q[c2] + Q[c3] + SS[c0] - SS[c1] +
+                                   SS[c2] - SS[c3]) * xf + (T[c0] + T[c1] - T[c2] - T[c3]) * yf;
+                const double fy = (T[c0] - T[c1] + T[c2] - T[c3]) * xf +
+                                  (-P[c0] - P[c1] + P[c2] + P[c3] - Q[c0] - Q[c1] + Q[c2] + Q[c3] - SS[c0] - SS[c1] +
+                                   SS[c2] + SS[c3]) * yf;
+                const size_t cr = CI(S, ir, j), cl = CI(S, il, j), cup = CI(S, i, j + 1), cdn = CI(S, i, j - 1);
+                const double uvisc = hxxv * (u[cr] + u[cl]) + hyyv * (u[cup] + u[cdn]) - hcv * uc;
+                const double vvisc = hxxv * (v[cr] + v[cl]) + hyyv * (v[cup] + v[cdn]) - hcv * vc;
+                cu[c] = -uc * ux - vc * uy + mu_inv * (fx + uvisc);
+                cv[c] = -uc * vx - vc * vy + mu_inv * (fy + vvisc);
+                S->cX[c] = -uc * Xx - vc * Xy;
+                S->cY[c] = -uc * Yx - vc * Yy;
+            }
+            /* deformation rate, staggered velocity, spin */
+            const size_t cr = CI(S, ir, j), cup = CI(S, i, j + 1), cur = CI(S, ir, j + 1);
+            uc = 0.25 * (u[c] + u[cr] + u[cup] + u[cur]);
+            vc = 0.25 * (v[c] + v[cr] + v[cup] + v[cur]);
+            const double ux = hx * (-u[c] + u[cr] - u[cup] + u[cur]), uy = hy * (-u[c] - u[cr] + u[cup] + u[cur]);
+            const double vx = hx * (-v[c] + v[cr] - v[cup] + v[cur]), vy = hy * (-v[c] - v[cr] + v[cup] + v[cur]);
+            const double two_omega = vx - uy;
+            double f1[5], f2[5];
+            for (int k = 0; k < 5; k++) {
+                const double *F = fld[k];
+                if (uc > 0) f1[k] = hx * eno2(F[CI(S, ir, j)], F[c], F[CI(S, il, j)], F[CI(S, il2, j)]);
+                else f1[k] = -hx * eno2(F[CI(S, il, j)], F[c], F[CI(S, ir, j)], F[CI(S, ir2, j)]);
+                if (vc > 0) {
+                    if (j > 0) f2[k] = hy * eno2(F[CI(S, i, j + 1)], F[c], F[CI(S, i, j - 1)], F[CI(S, i, j - 2)]);
+                    else f2[k] = 2 * hy * (F[c] - F[CI(S, i, j - 1)]);
+                } else {
+                    if (j < n - 1) f2[k] = -hy * eno2(F[CI(S, i, j - 1)], F[c], F[CI(S, i, j + 1)], F[CI(S, i, j + 2)]);
+                    else f2[k] = 2 * -hy * (F[c] - F[CI(S, i, j + 1)]);
+                }
+            }
+            const double *ch = S->chi;
+            const double qv = S->q[c], sv = S->s[c], tv = S->tau[c];
+            const double sbar = sqrt(3 * qv * qv + sv * sv + tv * tv);
+            double cchi = ch[c] - uc * f1[4] - vc * f2[4] + hxxcd * (ch[cr] + ch[CI(S, il, j)]) +
+                          hyycd * (ch[cup] + ch[CI(S, i, j - 1)]) - hccd * ch[c];
+            double ddev;
+            const double dtmp = adaptive_plastic_term(&S->P, sbar, &cchi, &ddev, dt);
+            S->cchi[c] = cchi;
+            S->cp[c] = -uc * f1[0] - vc * f2[0] - K * (ux + vy);
+            S->cq[c] = -uc * f1[1] - vc * f2[1] - mu * third * (ux + vy) - dtmp * qv;
+            S->cs[c] = -uc * f1[2] - vc * f2[2] + two_omega * tv + mu * (ux - vy) - dtmp * sv;
+            S->ctau[c] = -uc * f1[3] - vc * f2[3] - two_omega * sv + mu * (vx + uy) - dtmp * tv;
+            if (raw_ddev) raw_ddev[(size_t)j * m + i] = ddev;
+            S->ddev[c] = ddev * sbar;
+        }
+    }
+    chi_diffusion(S, dt);
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            size_t c = CI(S, i, j);
+            if (j > 0) {
+                S->u[c] += cu[c];
+                S->v[c] += cv[c];
+                S->X[c] += S->cX[c];
+                S->Y[c] += S->cY[c];
+            }
             S->p[c] += S->cp[c];
             S->q[c] += S->cq[c];
             S->s[c] += S->cs[c];
@@ -704,9 +857,9 @@ stzo_sim *stzo_create(const stzo_params *p) {
     S->mu_inv = 1 / p->mu;
     S->bcs = 4;
     size_t np = (size_t)(n + 2) * m;
-    double **arr[17] = {&S->u, &S->v, &S->p, &S->q, &S->s, &S->tau, &S->chi, &S->X, &S->Y, &S->ddev,
-                        &S->cp, &S->cq, &S->cs, &S->ctau, &S->cchi, &S->cX, &S->cY};
-    for (int k = 0; k < 17; k++) *arr[k] = (double *)calloc(np, sizeof(double));
+    double **arr[19] = {&S->u, &S->v, &S->p, &S->q, &S->s, &S->tau, &S->chi, &S->X, &S->Y, &S->ddev,
+                        &S->cp, &S->cq, &S->cs, &S->ctau, &S->cchi, &S->cX, &S->cY, &S->cu, &S->cv};
+    for (int k = 0; k < 19; k++) *arr[k] = (double *)calloc(np, sizeof(double));
     S->vel = (v2 *)calloc((size_t)m * (n + 1), sizeof(v2));
     S->src = (v2 *)calloc((size_t)m * (n + 1), sizeof(v2));
     /* qs_multi constructor, qs_multi.cc:9-15 */
@@ -748,9 +901,9 @@ stzo_sim *stzo_create(const stzo_params *p) {
 }
 
 void stzo_destroy(stzo_sim *S) {
-    double *arr[17] = {S->u, S->v, S->p, S->q, S->s, S->tau, S->chi, S->X, S->Y, S->ddev,
-                       S->cp, S->cq, S->cs, S->ctau, S->cchi, S->cX, S->cY};
-    for (int k = 0; k < 17; k++) free(arr[k]);
+    double *arr[19] = {S->u, S->v, S->p, S->q, S->s, S->tau, S->chi, S->X, S->Y, S->ddev,
+                       S->cp, S->cq, S->cs, S->ctau, S->cchi, S->cX, S->cY, S->cu, S->cv};
+    for (int k = 0; k < 19; k++) free(arr[k]);
     free(S->vel); free(S->src); free(S->lv[0].r);
     for (int l = 1; l < S->nl; l++) { free(S->lv[l].b); free(S->lv[l].z); free(S->lv[l].r); free(S->lv[l].st); }
     free(S);
@@ -809,6 +962,34 @@ long stzo_steps(stzo_sim *S, double dt, int nsteps, double *eps_pl, double *seco
     }
     if (seconds) *seconds = t;
     return S->vcount - c0;
+}
+
+/* shear_sim::step_forward, shear_sim.cc:185-276, nsteps times; eps_pl
+ * accumulates the raw stress drop / (2 mu) */
+void stzo_steps_direct(stzo_sim *S, double dt, int nsteps, double *eps_pl) {
+    const size_t mn = (size_t)S->m * S->n;
+    double *raw = eps_pl ? (double *)malloc(mn * sizeof(double)) : NULL;
+    for (int k = 0; k < nsteps; k++) {
+        S->time += dt;
+        direct_step(S, dt, raw);
+        set_boundaries(S);
+        if (eps_pl)
+            for (size_t c = 0; c < mn; c++) eps_pl[c] += raw[c] / (2 * S->P.mu);
+    }
+    free(raw);
+}
+
+/* The frame loop of shear_sim::solve (shear_sim.cc:120-140) without output:
+ * steps of dt while they stay short of target (relative margin 1e-8), then
+ * one step of the remaining time.  Returns the number of steps. */
+long stzo_advance_direct(stzo_sim *S, double dt, double target, double *eps_pl) {
+    long k = 0;
+    while (S->time + dt * (1 + 1e-8) < target) {
+        stzo_steps_direct(S, dt, 1, eps_pl);
+        k++;
+    }
+    stzo_steps_direct(S, target - S->time, 1, eps_pl);
+    return k + 1;
 }
 
 double stzo_time(stzo_sim *S) { return S->time; }

@@ -39,6 +39,10 @@ void stzo_set_state(stzo_sim *s, const double *chi);
  * ||r||_2 <= tol*||b||_2. */
 void stzo_set_tolerance(stzo_sim *s, int mode, double value);
 long stzo_steps(stzo_sim *s, double dt, int nsteps, double *eps_pl, double *seconds);
+/* Explicit steps (shear_sim::step_forward) and the frame loop of
+ * shear_sim::solve up to a target time. */
+void stzo_steps_direct(stzo_sim *s, double dt, int nsteps, double *eps_pl);
+long stzo_advance_direct(stzo_sim *s, double dt, double target, double *eps_pl);
 double stzo_time(stzo_sim *s);
 /* Field ids as oracle/ref_driver.cc: 0 u,1 v,7 X,8 Y node (m*(n+1));
  * 2 p,3 q,4 s,5 tau,6 chi,9 ddev cell with ghost rows (m*(n+2)). */
