@@ -65,6 +65,9 @@ def _load(path, prefix):
     f("set_state").argtypes = [ctypes.c_void_p, _P]
     f("steps").restype = ctypes.c_long
     f("steps").argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, _P, _P]
+    f("steps_direct").argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_int, _P]
+    f("advance_direct").restype = ctypes.c_long
+    f("advance_direct").argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, _P]
     f("time").restype = ctypes.c_double
     f("time").argtypes = [ctypes.c_void_p]
     f("get").argtypes = [ctypes.c_void_p, ctypes.c_int, _P]
@@ -132,6 +135,14 @@ class _Sim:
         self.cycles += c
         self.seconds += sec.value
         return c
+
+    def steps_direct(self, dt, nsteps):
+        """Explicit steps (shear_sim::step_forward)."""
+        self._f("steps_direct")(self.h, dt, nsteps, _ptr(self.eps_pl))
+
+    def advance_direct(self, dt, target):
+        """Explicit steps of dt up to target time (the frame loop of shear_sim::solve)."""
+        return self._f("advance_direct")(self.h, dt, target, _ptr(self.eps_pl))
 
     @property
     def time(self):

@@ -13,6 +13,8 @@
 // oracle with a tighter tolerance, and to read its coarse-grid stencils, this
 // translation unit opens the private members.  It never changes the
 // reference's arithmetic.
+#include <vector>
+
 #define private public
 #include "shear_sim.hh"
 #undef private
@@ -125,6 +127,35 @@ long stzref_steps(void *vh, double dt, int nsteps, double *eps_pl, double *secon
     (void)t0;
     if (seconds) *seconds = acc;
     return cycles;
+}
+
+// Runs nsteps explicit steps (shear_sim::step_forward, shear_sim.cc:185-276).
+// The reference stores ddev times the old |s| there (shear_sim.cc:265); when
+// eps_pl is non-NULL it accumulates the raw stress drop / (2 mu), recovered
+// with the |s| of each cell before the step.
+void stzref_steps_direct(void *vh, double dt, int nsteps, double *eps_pl) {
+    shear_sim &s = *((ref_handle *)vh)->sim;
+    std::vector<double> dev(eps_pl ? (size_t)s.m * s.n : 0);
+    for (int k = 0; k < nsteps; k++) {
+        if (eps_pl)
+            for (int c = 0; c < s.m * s.n; c++) dev[c] = s.fm[c].dev();
+        s.step_forward(dt);
+        if (eps_pl)
+            for (int c = 0; c < s.m * s.n; c++)
+                if (dev[c] > 0) eps_pl[c] += s.fm[c].ddev / dev[c] / (2 * s.mu);
+    }
+}
+
+// The frame loop of shear_sim::solve (shear_sim.cc:120-140) up to target.
+long stzref_advance_direct(void *vh, double dt, double target, double *eps_pl) {
+    shear_sim &s = *((ref_handle *)vh)->sim;
+    long k = 0;
+    while (s.time + dt * (1 + 1e-8) < target) {
+        stzref_steps_direct(vh, dt, 1, eps_pl);
+        k++;
+    }
+    stzref_steps_direct(vh, target - s.time, 1, eps_pl);
+    return k + 1;
 }
 
 double stzref_time(void *vh) { return ((ref_handle *)vh)->sim->time; }

@@ -20,8 +20,11 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 (runs the CUDA path)")
 
 
-def golden_names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+def golden_names(kind="quasistatic"):
+    """Fixture names of one kind: "quasistatic" (step_forward_quasistatic)
+    or "direct" (the explicit step_forward)."""
+    names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    return [n for n in names if n.startswith("direct_") == (kind == "direct")]
 
 
 def load_golden(name):
@@ -37,4 +40,9 @@ def load_golden(name):
 
 @pytest.fixture(params=golden_names())
 def golden(request):
+    return (request.param,) + load_golden(request.param)
+
+
+@pytest.fixture(params=golden_names("direct"))
+def golden_direct(request):
     return (request.param,) + load_golden(request.param)

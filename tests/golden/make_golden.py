@@ -7,9 +7,10 @@ Run in a checkout that has the SURGroup/STZ tree available (default
 
 It builds oracle/_ref/libstzref.so from the reference sources
 (oracle/build_ref.sh), runs the reference's own
-shear_sim::step_forward_quasistatic (esim/sb/main/shear_sim.cc:280) on seeded
-inputs, and stores inputs and outputs as compressed .npz files next to this
-script.  The chi inputs come from the oracle's seeded random-field generator;
+shear_sim::step_forward_quasistatic (esim/sb/main/shear_sim.cc:280) and
+shear_sim::step_forward (shear_sim.cc:185) on seeded inputs, and stores
+inputs and outputs as compressed .npz files next to this script.  Names given
+on the command line restrict it to those fixtures.  The chi inputs come from the oracle's seeded random-field generator;
 they are stored in the fixture, so the fixtures do not depend on it.
 """
 import json
@@ -49,6 +50,35 @@ CASES = {
 }
 
 
+# Explicit (direct) steps, shear_sim::step_forward (shear_sim.cc:185-276),
+# through the frame loop of shear_sim::solve (shear_sim.cc:120-140) with
+# dt = dx^2 * tmult up to the target time:
+# name -> (params, chi (l, std, seed), tmult, target time)
+DIRECT_CASES = {
+    "direct_elastic32": (simple_shear(32, viscosity=0.05, chi_diff=1e-3, chi_len=0.02), (4, 30, 12), 0.5, 0.3),
+    "direct_plastic24": (plastic_shear(24, u_bdry=1.0, viscosity=0.02), (3, 30, 13), 0.5, 0.4),
+    "direct_rect40x24": (plastic_shear(40, 24, u_bdry=2.0, viscosity=0.01, chi_diff=5e-4), (3, 30, 14), 0.4,
+                         0.25),
+}
+
+
+def make_direct(name, spec):
+    P, (l, std, seed), tmult, target = spec
+    chi = random_chi(P.m, P.n, l, 600.0, std, P.TZ, seed)
+    sim = ReferenceSim(P, chi)
+    dx = (P.bx - P.ax) / P.m
+    dt = dx * dx * tmult
+    nsteps = sim.advance_direct(dt, target)
+    f = sim.fields()
+    out = {k: v for k, v in f.items()}
+    out["chi0"] = chi
+    meta = {"kind": "direct", "params": P.as_dict(), "dt": dt, "tmult": tmult, "target": target,
+            "steps": int(nsteps), "time": sim.time,
+            "source": "reference shear_sim::step_forward in the frame loop of shear_sim::solve, built from source"}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **out)
+    return nsteps
+
+
 def make(name, spec):
     P, (l, std, seed), dt, steps, mult = spec
     chi = random_chi(P.m, P.n, l, 600.0, std, P.TZ, seed)
@@ -67,9 +97,17 @@ def make(name, spec):
 
 
 def main():
+    only = sys.argv[1:]
     for name, spec in CASES.items():
+        if only and name not in only:
+            continue
         c = make(name, spec)
         print(f"{name}: {c} V-cycles")
+    for name, spec in DIRECT_CASES.items():
+        if only and name not in only:
+            continue
+        k = make_direct(name, spec)
+        print(f"{name}: {k} explicit steps")
 
 
 if __name__ == "__main__":

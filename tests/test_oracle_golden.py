@@ -32,3 +32,18 @@ def test_golden_plastic_cases_are_plastic(golden):
     elif name not in ("thermal_nonlinear16",):
         # plastic-active variants: a large share of cells yields by the end
         assert np.mean(ref["ddev"][1:-1] > 0) > 0.1 or np.max(ref["eps_pl"]) > 0
+
+
+def test_oracle_direct_step_matches_reference_golden(golden_direct):
+    """The explicit step (shear_sim::step_forward, shear_sim.cc:185-276) in
+    the frame loop of shear_sim::solve: the restatement repeats the
+    reference's arithmetic operation for operation."""
+    name, P, meta, ref = golden_direct
+    sim = OracleSim(P, ref["chi0"])
+    steps = sim.advance_direct(meta["dt"], meta["target"])
+    got = sim.fields()
+    err = group_errors(ref, got, P.n)
+    assert max(err.values()) < 1e-13, (name, err)
+    scale = max(np.abs(ref["ddev"]).max(), 1e-300)
+    assert np.abs(got["ddev"] - ref["ddev"]).max() <= 1e-13 * scale
+    assert steps == meta["steps"] and sim.time == meta["time"]
