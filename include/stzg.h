@@ -124,6 +124,17 @@ int stzg_download(stzg_sim *s, double *const *down);
 /* Replaces: shear_sim::step_forward_quasistatic (shear_sim.cc:280-291),
  * called nsteps times; stats may be NULL. */
 int stzg_step_qs(stzg_sim *s, double dt, int nsteps, stzg_stats *stats);
+/* Replaces: shear_sim::step_forward (shear_sim.cc:185-276), the explicit
+ * (direct) step: velocity and reference map advected with ENO2 and driven by
+ * the net force of the stress and a viscous term, stresses advected and
+ * loaded elastically by the velocity gradient, STZ plasticity, chi diffusion,
+ * set_boundaries; nsteps steps of dt; stats may be NULL. */
+int stzg_step_direct(stzg_sim *s, double dt, int nsteps, stzg_stats *stats);
+/* Replaces: the frame loop of shear_sim::solve (shear_sim.cc:120-140)
+ * without file output: explicit steps of dt while time + dt(1+1e-8) stays
+ * below target, then one step of the remaining time; *nsteps (may be NULL)
+ * receives the number of steps.  The reference uses dt = dx^2 * tmult. */
+int stzg_advance_direct(stzg_sim *s, double dt, double target, long *nsteps);
 /* Replaces: shear_sim::advection_step + chi_diffusion (shear_sim.cc:296-386),
  * one call, time not advanced. */
 int stzg_advection_step(stzg_sim *s, double dt);

@@ -33,15 +33,15 @@ inline void check_or_exit(int st) {
 class shear_sim {
   public:
     const int m, n;
-    const double ax, bx, ay, by, dx, dy, mu, K, viscosity, chi_diff, chi_len, t_scale, adapt_fac, u_bdry;
+    const double ax, bx, ay, by, dx, dy, mu, K, viscosity, chi_diff, chi_len, t_scale, tmult, adapt_fac, u_bdry;
 
     template <class STZ>
     shear_sim(int m_, int n_, double ax_, double bx_, double ay_, double by_, double mu_, double K_, double visc_,
-              double chi_diff_, double chi_len_, double t_scale_, double /*tmult*/, double adapt_fac_,
+              double chi_diff_, double chi_len_, double t_scale_, double tmult_, double adapt_fac_,
               double u_bdry_, const STZ *stz, const char * /*filename*/, int model = 2, int t_model = -1,
               const stzg_options *opt = nullptr)
         : m(m_), n(n_), ax(ax_), bx(bx_), ay(ay_), by(by_), dx((bx_ - ax_) / m_), dy((by_ - ay_) / n_), mu(mu_),
-          K(K_), viscosity(visc_), chi_diff(chi_diff_), chi_len(chi_len_), t_scale(t_scale_),
+          K(K_), viscosity(visc_), chi_diff(chi_diff_), chi_len(chi_len_), t_scale(t_scale_), tmult(tmult_),
           adapt_fac(adapt_fac_), u_bdry(u_bdry_), h(nullptr) {
         stz_params p;
         p.m = m_;
@@ -70,6 +70,20 @@ class shear_sim {
     void set_chi(const double *chi) { check_or_exit(stzg_set_state(h, chi)); }
 
     void step_forward_quasistatic(double dt) { check_or_exit(stzg_step_qs(h, dt, 1, nullptr)); }
+    // shear_sim::step_forward (shear_sim.cc:185-276), the explicit step.
+    void step_forward(double dt) { check_or_exit(stzg_step_direct(h, dt, 1, nullptr)); }
+    // shear_sim::solve (shear_sim.cc:120-140) without file output: steps of
+    // dx*dx*tmult landing exactly on every frame time; frame(k) after each.
+    template <class F> void solve(double duration, int frames, F frame) {
+        const double dt = dx * dx * tmult, t_start = time();
+        for (int k = 1; k <= frames; k++) {
+            check_or_exit(stzg_advance_direct(h, dt, t_start + duration / frames * k, nullptr));
+            frame(k);
+        }
+    }
+    void solve(double duration, int frames) {
+        solve(duration, frames, [](int) {});
+    }
     void advection_step(double dt) { check_or_exit(stzg_advection_step(h, dt)); }
     void projection_step(double dt) { check_or_exit(stzg_projection_step(h, dt, nullptr)); }
     // shear_sim::solve_quasistatic (shear_sim.cc:159-181) without file output;

@@ -33,6 +33,7 @@ EXPORTS = [
     "stzg_batch_create", "stzg_batch_destroy", "stzg_batch_size", "stzg_batch_sim", "stzg_batch_set_tuning",
     "stzg_batch_autotune", "stzg_batch_get_tuning", "stzg_batch_run",
     "stzg_adjoint_forward", "stzg_adjoint_backward",
+    "stzg_step_direct", "stzg_advance_direct",
 ]
 
 
@@ -121,6 +122,8 @@ def load(path=None):
         "stzg_batch_run": (I, [V, D, I, ctypes.POINTER(StzgBatchStats)]),
         "stzg_adjoint_forward": (I, [V, D, I, I, _P, _P]),
         "stzg_adjoint_backward": (I, [V, D, _P, _P]),
+        "stzg_step_direct": (I, [V, D, I, ctypes.POINTER(StzgStats)]),
+        "stzg_advance_direct": (I, [V, D, D, ctypes.POINTER(ctypes.c_long)]),
     }
     for name, (res, args) in decl.items():
         f = getattr(lib, name)

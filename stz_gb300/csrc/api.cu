@@ -195,10 +195,10 @@ int solve_fp64(stzg_sim *s, int *ncyc) {
     return STZG_OK;
 }
 
-// FP32 V-cycles inside FP64 iterative refinement.  One pass: e = 0,
-// `inner` FP32 V-cycles on A e = r (coarsest level solved in FP64), z += e in
-// FP64, then the FP64 residual r = b - A z (kept in FP32 for the next pass)
-// and its norm.  The number of passes between host checks follows the
+// FP32 V-cycles inside iterative refinement.  One pass: e = 0, `inner` FP32
+// V-cycles on A e = r (coarsest level solved in FP64), z += e on the
+// float-float iterate, then the float-float residual r = b - A z (kept in
+// FP32 for the next pass) and its norm.  The number of passes between host checks follows the
 // tgmg_predict policy (tgmg.in.cc:266-301) applied to passes.
 int run_passes(stzg_sim *s, int k) {
     const long count = (long)s->m * (s->n + 1);
@@ -720,6 +720,60 @@ int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {
     float t = 0;
     cudaEventElapsedTime(&t, s->ev0, s->ev1);
     *ms = t / reps;
+    return STZG_OK;
+}
+
+// One explicit step (shear_sim::step_forward, shear_sim.cc:185-276): time
+// first, the fused update, the new interior velocities from the staging
+// array, then set_boundaries at the new time.
+static int do_direct(stzg_sim *s, double dt) {
+    s->time += dt;
+    direct_step(s->sc, s->P.viscosity, s->F, s->cur, dt, s->bv_state, s->st);
+    const size_t m = s->m;
+    if (s->n > 1)
+        STZG_CUDA(cudaMemcpyAsync(s->F.vel + m, s->F.src + m, (size_t)(s->n - 1) * m * sizeof(double2),
+                                  cudaMemcpyDeviceToDevice, s->st));
+    s->cur ^= 1;
+    const double bv = bdry_vel(s, s->time), bp = bdry_pos(s, s->time);
+    set_boundaries(s->sc, s->F, s->cur, bp, s->st);
+    s->bv_state = bv;
+    // the velocity no longer comes from a solve: restart the guess history
+    s->have_prev = s->have_prev2 = false;
+    return STZG_OK;
+}
+
+int stzg_step_direct(stzg_sim *s, double dt, int nsteps, stzg_stats *stats) {
+    if (!s || nsteps < 0 || !(dt > 0)) return fail(STZG_EINVAL, "bad step arguments");
+    const long l0 = launch_count();
+    STZG_CUDA(cudaEventRecord(s->ev0, s->st));
+    for (int k = 0; k < nsteps; k++) STZG_CHECK(do_direct(s, dt));
+    STZG_CUDA(cudaEventRecord(s->ev1, s->st));
+    STZG_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->acc.seconds += ms * 1e-3;
+    STZG_CHECK(check_flags(s));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->seconds = ms * 1e-3;
+        stats->substeps_max = s->acc.substeps_max;
+        stats->kernel_launches = launch_count() - l0;
+    }
+    return STZG_OK;
+}
+
+int stzg_advance_direct(stzg_sim *s, double dt, double target, long *nsteps) {
+    if (!s || !(dt > 0)) return fail(STZG_EINVAL, "bad step arguments");
+    if (!(target > s->time)) return fail(STZG_EINVAL, "target time not after the current time");
+    long k = 0;
+    while (s->time + dt * (1 + 1e-8) < target) {
+        STZG_CHECK(do_direct(s, dt));
+        if (++k % 64 == 0) STZG_CHECK(check_flags(s));
+    }
+    STZG_CHECK(do_direct(s, target - s->time));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    STZG_CHECK(check_flags(s));
+    if (nsteps) *nsteps = k + 1;
     return STZG_OK;
 }
 

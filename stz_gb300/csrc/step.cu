@@ -170,6 +170,129 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     }
 }
 
+// Explicit step (shear_sim::step_forward, shear_sim.cc:185-276) per cell
+// (i,j) and its lower-left node: the node velocity and reference map are
+// advected with ENO2 and the velocity takes the net force of the old stress
+// (net_force with prefactors -hx,-hy, shear_sim.cc:447-453) and a 5-point
+// viscous term, divided by mu as the reference's mu_inv; the cell fields are
+// advected and take the elastic rate of the old velocity gradient and the
+// plastic term.  The constant chi diffusion enters cchi before the plastic
+// term (and again in k_chi_diffusion, as the reference adds it twice); ddev
+// is stored times the old |s| (shear_sim.cc:265).  New node velocities go to
+// F.src (rows 1..n-1), the other fields to buffer cur^1.
+struct direct_consts {
+    double hxxv, hyyv, hcv, hxxcd, hyycd, hccd;
+};
+
+__global__ void __launch_bounds__(256) k_direct(step_consts c, direct_consts d, fields_dev F, int cur, double dt,
+                                                double bv) {
+    const int m = c.m, n = c.n;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const double *__restrict__ const *A = F.f[cur];
+    double *const *B = F.f[cur ^ 1];
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt, lx = c.lx, mu_inv = 1 / c.mu;
+    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
+    const int il2 = i <= 1 ? i + m - 2 : i - 2, ir2 = i >= m - 2 ? i + 2 - m : i + 2;
+    const size_t ci = IDX(i, j);
+    velo V{F.vel, m, n, bv};
+    const double *P = A[F_P], *Q = A[F_Q], *S = A[F_S], *T = A[F_TAU];
+    if (j > 0) {
+        const double *X = A[F_X], *Y = A[F_Y];
+        const double un = V.u(i, j), vn = V.v(i, j);
+        const double hsx = un > 0 ? hx : -hx, hsy = vn > 0 ? hy : -hy;
+        double ux, vx, Xx, Yx, uy, vy, Xy, Yy;
+        if (un > 0) {
+            ux = eno2(V.u(ir, j), un, V.u(il, j), V.u(il2, j));
+            vx = eno2(V.v(ir, j), vn, V.v(il, j), V.v(il2, j));
+            Xx = eno2(X[IDX(ir, j)] + (i == m - 1 ? lx : 0), X[ci], X[IDX(il, j)] + (i == 0 ? -lx : 0),
+                      X[IDX(il2, j)] + (i <= 1 ? -lx : 0));
+            Yx = eno2(Y[IDX(ir, j)], Y[ci], Y[IDX(il, j)], Y[IDX(il2, j)]);
+        } else {
+            ux = eno2(V.u(il, j), un, V.u(ir, j), V.u(ir2, j));
+            vx = eno2(V.v(il, j), vn, V.v(ir, j), V.v(ir2, j));
+            Xx = eno2(X[IDX(il, j)] + (i == 0 ? -lx : 0), X[ci], X[IDX(ir, j)] + (i == m - 1 ? lx : 0),
+                      X[IDX(ir2, j)] + (i >= m - 2 ? lx : 0));
+            Yx = eno2(Y[IDX(il, j)], Y[ci], Y[IDX(ir, j)], Y[IDX(ir2, j)]);
+        }
+        const int jn = vn > 0 ? j - 1 : j + 1;  // upwind neighbour row
+        if ((vn > 0 && j > 1) || (vn <= 0 && j < n - 1)) {
+            const int j0 = vn > 0 ? j + 1 : j - 1, j3 = vn > 0 ? j - 2 : j + 2;
+            uy = eno2(V.u(i, j0), un, V.u(i, jn), V.u(i, j3));
+            vy = eno2(V.v(i, j0), vn, V.v(i, jn), V.v(i, j3));
+            Xy = eno2(X[IDX(i, j0)], X[ci], X[IDX(i, jn)], X[IDX(i, j3)]);
+            Yy = eno2(Y[IDX(i, j0)], Y[ci], Y[IDX(i, jn)], Y[IDX(i, j3)]);
+        } else {
+            uy = 2 * (un - V.u(i, jn));
+            vy = 2 * (vn - V.v(i, jn));
+            Xy = 2 * (X[ci] - X[IDX(i, jn)]);
+            Yy = 2 * (Y[ci] - Y[IDX(i, jn)]);
+        }
+        ux *= hsx; vx *= hsx; Xx *= hsx; Yx *= hsx;
+        uy *= hsy; vy *= hsy; Xy *= hsy; Yy *= hsy;
+        // net force from the cells (i-1,j-1), (i,j-1), (i-1,j), (i,j)
+        const size_t c0 = IDX(il, j - 1), c1 = IDX(i, j - 1), c2 = IDX(il, j), c3 = ci;
+        const double xf = -hx, yf = -hy;
+        const double fx = (-P[c0] + P[c1] - P[c2] + P[c3] - Q[c0] + Q[c1] - Q[c2] + Q[c3] + S[c0] - S[c1] + S[c2] -
+                           S[c3]) * xf + (T[c0] + T[c1] - T[c2] - T[c3]) * yf;
+        const double fy = (T[c0] - T[c1] + T[c2] - T[c3]) * xf +
+                          (-P[c0] - P[c1] + P[c2] + P[c3] - Q[c0] - Q[c1] + Q[c2] + Q[c3] - S[c0] - S[c1] + S[c2] +
+                           S[c3]) * yf;
+        const double uvisc = d.hxxv * (V.u(ir, j) + V.u(il, j)) + d.hyyv * (V.u(i, j + 1) + V.u(i, j - 1)) - d.hcv * un;
+        const double vvisc = d.hxxv * (V.v(ir, j) + V.v(il, j)) + d.hyyv * (V.v(i, j + 1) + V.v(i, j - 1)) - d.hcv * vn;
+        F.src[(size_t)j * m + i] = make_double2(un + (-un * ux - vn * uy + mu_inv * (fx + uvisc)),
+                                                vn + (-un * vx - vn * vy + mu_inv * (fy + vvisc)));
+        B[F_X][ci] = X[ci] + (-un * Xx - vn * Xy);
+        B[F_Y][ci] = Y[ci] + (-un * Yx - vn * Yy);
+    }
+    // deformation rate, staggered velocity and spin
+    const double u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
+    const double v00 = V.v(i, j), v10 = V.v(ir, j), v01 = V.v(i, j + 1), v11 = V.v(ir, j + 1);
+    const double uc = 0.25 * (u00 + u10 + u01 + u11), vc = 0.25 * (v00 + v10 + v01 + v11);
+    const double ux = hx * (-u00 + u10 - u01 + u11), uy = hy * (-u00 - u10 + u01 + u11);
+    const double vx = hx * (-v00 + v10 - v01 + v11), vy = hy * (-v00 - v10 + v01 + v11);
+    const double two_omega = vx - uy;
+    const double uh = uc * (uc > 0 ? hx : -hx), vh = vc * (vc > 0 ? hy : -hy);
+    double f1[5], f2[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const double *G = A[k];
+        if (uc > 0) f1[k] = eno2(G[IDX(ir, j)], G[ci], G[IDX(il, j)], G[IDX(il2, j)]);
+        else f1[k] = eno2(G[IDX(il, j)], G[ci], G[IDX(ir, j)], G[IDX(ir2, j)]);
+        if (vc > 0) {
+            if (j > 0) f2[k] = eno2(G[IDX(i, j + 1)], G[ci], G[IDX(i, j - 1)], G[IDX(i, j - 2)]);
+            else f2[k] = 2 * (G[ci] - G[IDX(i, j - 1)]);
+        } else {
+            if (j < n - 1) f2[k] = eno2(G[IDX(i, j - 1)], G[ci], G[IDX(i, j + 1)], G[IDX(i, j + 2)]);
+            else f2[k] = 2 * (G[ci] - G[IDX(i, j + 1)]);
+        }
+    }
+    const double *CH = A[F_CHI];
+    const double p = P[ci], q = Q[ci], s = S[ci], t = T[ci];
+    double cchi = CH[ci] + fma(-vh, f2[4], -uh * f1[4]) + d.hxxcd * (CH[IDX(ir, j)] + CH[IDX(il, j)]) +
+                  d.hyycd * (CH[IDX(i, j + 1)] + CH[IDX(i, j - 1)]) - d.hccd * CH[ci];
+    const double devsq = 3 * q * q + s * s + t * t;
+    double ddev = 0, dtmp = 0, sbar = 0;
+    const bool athermal = c.stz_model >= 2;
+    if (!(devsq < 0.999e-24 || (athermal && devsq < c.s_y * c.s_y * (1 - 1e-12)))) {
+        int iters;
+        const stz_law_params<double> lp = law_params(c);
+        sbar = sqrt(devsq);
+        dtmp = adaptive_plastic(lp, sbar, cchi, ddev, dt, iters);
+        if (iters >= c.substep_cap) atomicExch(&F.flags[0], 1);
+        if (iters > 1) atomicMax(&F.flags[1], iters);
+    }
+    B[F_CHI][ci] = cchi;
+    F.ddev[ci] = ddev * sbar;
+    if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
+    const double third = 1 / 3.0;
+    B[F_P][ci] = p + (fma(-vh, f2[0], -uh * f1[0]) - c.K * (ux + vy));
+    B[F_Q][ci] = q + (fma(-vh, f2[1], -uh * f1[1]) - c.mu * third * (ux + vy) - dtmp * q);
+    B[F_S][ci] = s + (fma(-vh, f2[2], -uh * f1[2]) + two_omega * t + c.mu * (ux - vy) - dtmp * s);
+    B[F_TAU][ci] = t + (fma(-vh, f2[3], -uh * f1[3]) - two_omega * s + c.mu * (vx + uy) - dtmp * t);
+}
+
 __global__ void k_precombine(step_consts c, fields_dev F, int cur, double xf, double yf) {
     const int m = c.m, n = c.n;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -287,6 +410,25 @@ inline dim3 g2(int m, int n, dim3 b) { return dim3(ceil_div(m, b.x), ceil_div(n,
 void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st) {
     dim3 blk(32, 8);
     k_advect<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt, bv, 1); note_launch();
+    if (c.chi_diff != 0 || c.chi_len != 0) {
+        k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);
+        note_launch();
+    }
+}
+
+void direct_step(const step_consts &c, double viscosity, fields_dev &F, int cur, double dt, double bv,
+                 cudaStream_t st) {
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
+    direct_consts d;
+    d.hxxv = 2 * c.xsp * hx * viscosity;
+    d.hyyv = 2 * c.ysp * hy * viscosity;
+    d.hcv = 2 * (d.hxxv + d.hyyv);
+    d.hxxcd = 2 * c.xsp * hx * c.chi_diff;
+    d.hyycd = 2 * c.ysp * hy * c.chi_diff;
+    d.hccd = 2 * (d.hxxcd + d.hyycd);
+    dim3 blk(32, 8);
+    k_direct<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, d, F, cur, dt, bv);
+    note_launch();
     if (c.chi_diff != 0 || c.chi_len != 0) {
         k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);
         note_launch();

@@ -150,6 +150,31 @@ class ShearSim:
         self.cycles += st.vcycles
         return st.vcycles
 
+    def step_forward(self, dt, nsteps=1):
+        """shear_sim::step_forward (shear_sim.cc:185-276): explicit steps."""
+        st = _lib.StzgStats()
+        _lib.check(self.lib.stzg_step_direct(self.h, float(dt), int(nsteps), ctypes.byref(st)))
+        self.stats = st
+
+    def advance_direct(self, dt, target):
+        """Explicit steps of dt up to target time (the frame loop of
+        shear_sim::solve, shear_sim.cc:120-140); returns the step count."""
+        k = ctypes.c_long()
+        _lib.check(self.lib.stzg_advance_direct(self.h, float(dt), float(target), ctypes.byref(k)))
+        return k.value
+
+    def solve(self, duration, frames, tmult=0.5, frame_callback=None):
+        """shear_sim::solve (shear_sim.cc:120-140) without the file output:
+        explicit steps of dt = dx^2 * tmult, landing exactly on each frame
+        time; frame_callback(k, sim) is called after each frame."""
+        dx = (self.params.bx - self.params.ax) / self.m
+        dt = dx * dx * tmult
+        t_start = self.time
+        for k in range(1, frames + 1):
+            self.advance_direct(dt, t_start + duration / frames * k)
+            if frame_callback:
+                frame_callback(k, self)
+
     def advection_step(self, dt):
         _lib.check(self.lib.stzg_advection_step(self.h, float(dt)))
 

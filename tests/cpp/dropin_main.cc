@@ -2,8 +2,11 @@
 // drivers drive shear_sim (esim/sb/main/shear_test.cc:30-72): construct with
 // the reference's arguments and an STZ law object, step, read fields.
 // Writes chi0, then p, q, s, tau, chi, X, Y, u, v, eps_pl as raw doubles.
+// Usage: dropin <out> <tol> [direct]; "direct" runs shear_sim::solve (the
+// explicit step, two frames of 0.05) instead of quasi-static steps.
 #include <cmath>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "stzg_shear_sim.hh"
@@ -25,7 +28,13 @@ int main(int argc, char **argv) {
     std::vector<double> chi((size_t)N * N);
     stzg_random_chi(N, N, 4, 600, 30, TZ, 11, chi.data());
     sim.set_chi(chi.data());
-    for (int k = 0; k < steps; k++) sim.step_forward_quasistatic(0.01);
+    if (argc > 3 && std::string(argv[3]) == "direct") {
+        int frames = 0;
+        sim.solve(0.1, 2, [&](int) { frames++; });
+        if (frames != 2) return 3;
+    } else {
+        for (int k = 0; k < steps; k++) sim.step_forward_quasistatic(0.01);
+    }
     std::FILE *f = std::fopen(argv[1], "wb");
     std::fwrite(chi.data(), sizeof(double), chi.size(), f);
     const int ids[] = {STZG_P, STZG_Q, STZG_S, STZG_TAU, STZG_CHI, STZG_X, STZG_Y, STZG_U, STZG_V, STZG_EPS_PL};
