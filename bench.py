@@ -40,6 +40,7 @@ ADVECT_BYTES_PER_CELL = 128      # read u,v,p,q,s,tau,chi,X,Y; write p,q,s,tau,c
 VCYCLE32_BYTES_PER_NODE = 69.3   # 17.3 words of 4 B: 13 W on the top level x (1 + 1/4 + 1/16 + ...)
 VCYCLE64_BYTES_PER_NODE = 138.7
 SWEEP32_BYTES_PER_NODE = 24      # one Gauss-Seidel sweep: read z, b; write z (float2)
+DIRECT_BYTES_PER_CELL = 160      # explicit step: read u,v,p,q,s,tau,chi,X,Y; write them, ddev (8 B each)
 RESIDFF_BYTES_PER_NODE = 40      # read z, b as float-float (hi, lo float2 each); write r (float2)
 
 
@@ -282,6 +283,20 @@ def run_ours(args, dist):
         line["rel_err_mixed_vs_fp64"] = {"steps": nsteps, **{k: float(v) for k, v in err.items()}}
         for h in (a, b, a2):
             h.close()
+
+    # the explicit step (shear_sim::step_forward) on the same grid and state
+    # shape, dt = dx^2/2 as the reference's solve with tmult = 0.5
+    if prec == _lib.MIXED:
+        d = ShearSim(P, chi, precision=_lib.FP64)
+        ddt = 0.5 * (2.0 / N) ** 2
+        d.step_forward(ddt, 3)
+        kd = 50
+        d.step_forward(ddt, kd)
+        line["direct"] = {"value": N * N * kd / d.stats.seconds, "unit": METRIC,
+                          "ms_per_step": 1e3 * d.stats.seconds / kd, "steps": kd, "dt": ddt,
+                          "GBs": DIRECT_BYTES_PER_CELL * N * N / (d.stats.seconds / kd) / 1e9,
+                          "api": "stzg_step_direct (explicit step)"}
+        d.close()
 
     # roofline of the dominant kernels, timed in isolation on the library's stream
     peak, peak_kind = measured_peaks()
