@@ -86,6 +86,11 @@ def _load(path, prefix):
                                         ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong, _P]
         lib.stzo_threads.restype = ctypes.c_int
     else:
+        lib.stzref_output.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+        lib.stzref_qs_measure.argtypes = [ctypes.c_void_p, ctypes.c_int, _P, _P]
+        lib.stzref_tractions.argtypes = [ctypes.c_void_p, _P]
+        lib.stzref_compute_strain.argtypes = [ctypes.c_void_p, _P]
+        lib.stzref_clear_cu.argtypes = [ctypes.c_void_p]
         lib.stzref_set_acc_mult.argtypes = [ctypes.c_void_p, ctypes.c_double]
         lib.stzref_get_acc.restype = ctypes.c_double
         lib.stzref_get_acc.argtypes = [ctypes.c_void_p]
@@ -218,6 +223,33 @@ class ReferenceSim(_Sim):
             raise ValueError("the reference hard-wires the yield stress to 1")
         self.lib = _load(path, "stzref_")
         super().__init__(params, chi)
+
+    def output(self, mode, tmpdir):
+        """shear_sim::output of one mode, read back as the float32 matrix."""
+        self.lib.stzref_output(self.h, str(tmpdir).encode(), b"f", int(mode), 0)
+        path = os.path.join(str(tmpdir), "f.0")
+        a = np.fromfile(path, dtype=np.float32)
+        os.remove(path)
+        w = int(a[0]) + 1
+        return a.reshape(-1, w)
+
+    def qs_measure(self, staggered=False):
+        q, mx = ctypes.c_double(), ctypes.c_double()
+        self.lib.stzref_qs_measure(self.h, int(staggered), ctypes.byref(q), ctypes.byref(mx))
+        return q.value, mx.value
+
+    def tractions(self):
+        out = np.zeros(4)
+        self.lib.stzref_tractions(self.h, _ptr(out))
+        return out
+
+    def compute_strain(self):
+        out = np.zeros(self.m * self.n)
+        self.lib.stzref_compute_strain(self.h, _ptr(out))
+        return out.reshape(self.n, self.m)
+
+    def clear_cu(self):
+        self.lib.stzref_clear_cu(self.h)
 
     def set_acc_mult(self, mult):
         self.lib.stzref_set_acc_mult(self.h, mult)

@@ -158,6 +158,39 @@ long stzref_advance_direct(void *vh, double dt, double target, double *eps_pl) {
     return k + 1;
 }
 
+// shear_sim::output (shear_sim.cc:684-720): writes <dir>/<prefix>.<sn>.
+void stzref_output(void *vh, const char *dir, const char *prefix, int mode, int sn) {
+    shear_sim &s = *((ref_handle *)vh)->sim;
+    const char *old = s.filename;
+    s.filename = dir;
+    s.output(prefix, mode, sn);
+    s.filename = old;
+}
+
+// shear_sim::qs_measure (shear_sim.cc:733-775); the integrand stays in cu.
+void stzref_qs_measure(void *vh, int staggered, double *Q, double *max_qs) {
+    ((ref_handle *)vh)->sim->qs_measure(*Q, *max_qs, staggered != 0);
+}
+
+// shear_sim::tractions (shear_sim.cc:1003-1028): out = bx, by, tx, ty.
+void stzref_tractions(void *vh, double *out) {
+    ((ref_handle *)vh)->sim->tractions(out[0], out[1], out[2], out[3]);
+}
+
+// shear_sim::compute_strain (shear_sim.cc:778-824): out = cu of rows 0..n-1.
+void stzref_compute_strain(void *vh, double *out) {
+    shear_sim &s = *((ref_handle *)vh)->sim;
+    s.compute_strain();
+    for (int c = 0; c < s.m * s.n; c++) out[c] = s.fm[c].cu;
+}
+
+// Zeroes the cu slots (rows -1..n) so that the rows qs_measure leaves alone
+// read 0 in an output of mode 11.
+void stzref_clear_cu(void *vh) {
+    shear_sim &s = *((ref_handle *)vh)->sim;
+    for (int c = -s.m; c < s.m * (s.n + 1); c++) s.fm[c].cu = 0;
+}
+
 double stzref_time(void *vh) { return ((ref_handle *)vh)->sim->time; }
 
 // Field ids: 0 u, 1 v, 7 X, 8 Y are node fields with rows 0..n (m*(n+1));
