@@ -244,6 +244,31 @@ int stzg_adjoint_forward(stzg_sim *s, double dt, int nsteps, int checkpoint_ever
                          double *loss);
 int stzg_adjoint_backward(stzg_sim *s, double dloss, double *grad_params, double *grad_chi0);
 
+/* ---- frame export and diagnostics ---------------------------------------
+ * Replaces: shear_sim::output (shear_sim.cc:684-720): the Gnuplot binary
+ * matrix (float32) of one field, the bytes the reference writes to
+ * <dir>/<prefix>.<frame>.  mode: 0 u, 1 v, 2 p, 3 q, 4 s, 5 tau, 6 chi,
+ * 7 chi*TZ ("tem"), 8 |s| ("dev"), 9 X, 10 Y, 11 the last qs_measure
+ * integrand ("proj").  Cell fields (2-8): (n+1) rows of m+1 floats; node
+ * fields: (n+2) rows of m+2.  *count (may be NULL) receives the number of
+ * floats; out == NULL only queries it. */
+int stzg_output_field(stzg_sim *s, int mode, float *out, long *count);
+/* Replaces: shear_sim::write_files (shear_sim.cc:659-676) with the field
+ * selection as flags (bit k = mode k, the reference writes 4|128|256|512|1024;
+ * bit 11 first runs qs_measure and returns Q, max in qs[2], may be NULL). */
+int stzg_write_frame(stzg_sim *s, const char *dir, int frame, unsigned flags, double *qs);
+/* Replaces: shear_sim::qs_measure (shear_sim.cc:733-775): Q over the
+ * interior rows and its maximum integrand; the integrand per node is kept
+ * for output mode 11. */
+int stzg_qs_measure(stzg_sim *s, int staggered, double *Q, double *max_qs);
+/* Replaces: shear_sim::tractions (shear_sim.cc:1003-1028): out[4] = bottom
+ * (x, y), top (x, y). */
+int stzg_tractions(stzg_sim *s, double *out);
+/* Replaces: shear_sim::compute_strain (shear_sim.cc:778-824): the Hencky
+ * strain magnitude per cell, out[m*n] (rows 0..n-1), restating the
+ * reference's y differences as they are (interior rows give 0). */
+int stzg_compute_strain(stzg_sim *s, double *out);
+
 /* Replaces: shear_sim::l2_comparison (shear_sim.cc:460-502) between two
  * handles of the same grid: l2[4] = velocity, stress, chi, reference map. */
 int stzg_l2_comparison(stzg_sim *a, stzg_sim *b, double *l2);

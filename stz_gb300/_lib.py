@@ -34,6 +34,7 @@ EXPORTS = [
     "stzg_batch_autotune", "stzg_batch_get_tuning", "stzg_batch_run",
     "stzg_adjoint_forward", "stzg_adjoint_backward",
     "stzg_step_direct", "stzg_advance_direct",
+    "stzg_output_field", "stzg_write_frame", "stzg_qs_measure", "stzg_tractions", "stzg_compute_strain",
 ]
 
 
@@ -124,6 +125,11 @@ def load(path=None):
         "stzg_adjoint_backward": (I, [V, D, _P, _P]),
         "stzg_step_direct": (I, [V, D, I, ctypes.POINTER(StzgStats)]),
         "stzg_advance_direct": (I, [V, D, D, ctypes.POINTER(ctypes.c_long)]),
+        "stzg_output_field": (I, [V, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_long)]),
+        "stzg_write_frame": (I, [V, ctypes.c_char_p, I, ctypes.c_uint, _P]),
+        "stzg_qs_measure": (I, [V, I, _P, _P]),
+        "stzg_tractions": (I, [V, _P]),
+        "stzg_compute_strain": (I, [V, _P]),
     }
     for name, (res, args) in decl.items():
         f = getattr(lib, name)

@@ -47,6 +47,7 @@ struct stzg_sim {
     float2 *zhi = nullptr, *zlo = nullptr, *bhi = nullptr, *blo = nullptr;
     bool have_prev = false;
     stzg_adjoint *adj = nullptr;  // adjoint workspace (adjoint.cu), created on first use
+    double *proj = nullptr;       // qs_measure integrand per node (output.cu), created on first use
     // bulk host transfers: copies spread over several streams (copy engines)
     static constexpr int kCopyStreams = 4;
     cudaStream_t cst[kCopyStreams] = {};

@@ -175,6 +175,41 @@ class ShearSim:
             if frame_callback:
                 frame_callback(k, self)
 
+    # -- frame export and diagnostics --------------------------------------
+    def output(self, mode):
+        """shear_sim::output (shear_sim.cc:684-720): the Gnuplot binary
+        matrix of one field as a float32 array (rows x width)."""
+        n = ctypes.c_long()
+        _lib.check(self.lib.stzg_output_field(self.h, int(mode), None, ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.float32)
+        _lib.check(self.lib.stzg_output_field(self.h, int(mode), out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                              ctypes.byref(n)))
+        return out.reshape(-1, int(out[0]) + 1)
+
+    def write_files(self, directory, frame, flags=4 | 128 | 256 | 512 | 1024):
+        """shear_sim::write_files (shear_sim.cc:659-676) into directory."""
+        qs = np.zeros(2)
+        _lib.check(self.lib.stzg_write_frame(self.h, str(directory).encode(), int(frame), int(flags), _ptr(qs)))
+        return qs
+
+    def qs_measure(self, staggered=False):
+        """shear_sim::qs_measure (shear_sim.cc:733-775): (Q, max integrand)."""
+        q, mx = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self.lib.stzg_qs_measure(self.h, int(staggered), ctypes.byref(q), ctypes.byref(mx)))
+        return q.value, mx.value
+
+    def tractions(self):
+        """shear_sim::tractions (shear_sim.cc:1003-1028): bottom x, y, top x, y."""
+        out = np.zeros(4)
+        _lib.check(self.lib.stzg_tractions(self.h, _ptr(out)))
+        return out
+
+    def compute_strain(self):
+        """shear_sim::compute_strain (shear_sim.cc:778-824): (n, m)."""
+        out = np.zeros(self.m * self.n)
+        _lib.check(self.lib.stzg_compute_strain(self.h, _ptr(out)))
+        return out.reshape(self.n, self.m)
+
     def advection_step(self, dt):
         _lib.check(self.lib.stzg_advection_step(self.h, float(dt)))
 

@@ -21,10 +21,14 @@ def pytest_configure(config):
 
 
 def golden_names(kind="quasistatic"):
-    """Fixture names of one kind: "quasistatic" (step_forward_quasistatic)
-    or "direct" (the explicit step_forward)."""
+    """Fixture names of one kind: "quasistatic" (step_forward_quasistatic),
+    "direct" (the explicit step_forward) or "frames" (output and
+    diagnostics of a quasi-static state)."""
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-    return [n for n in names if n.startswith("direct_") == (kind == "direct")]
+    prefix = {"direct": "direct_", "frames": "frames_"}
+    if kind in prefix:
+        return [n for n in names if n.startswith(prefix[kind])]
+    return [n for n in names if not any(n.startswith(p) for p in prefix.values())]
 
 
 def load_golden(name):
@@ -45,4 +49,9 @@ def golden(request):
 
 @pytest.fixture(params=golden_names("direct"))
 def golden_direct(request):
+    return (request.param,) + load_golden(request.param)
+
+
+@pytest.fixture(params=golden_names("frames"))
+def golden_frames(request):
     return (request.param,) + load_golden(request.param)

@@ -8,7 +8,9 @@ Run in a checkout that has the SURGroup/STZ tree available (default
 It builds oracle/_ref/libstzref.so from the reference sources
 (oracle/build_ref.sh), runs the reference's own
 shear_sim::step_forward_quasistatic (esim/sb/main/shear_sim.cc:280) and
-shear_sim::step_forward (shear_sim.cc:185) on seeded inputs, and stores
+shear_sim::step_forward (shear_sim.cc:185) and the frame export and
+diagnostics (output, qs_measure, tractions, compute_strain) on seeded
+inputs, and stores
 inputs and outputs as compressed .npz files next to this script.  Names given
 on the command line restrict it to those fixtures.  The chi inputs come from the oracle's seeded random-field generator;
 they are stored in the fixture, so the fixtures do not depend on it.
@@ -79,6 +81,40 @@ def make_direct(name, spec):
     return nsteps
 
 
+# Frame export and diagnostics (shear_sim::output, qs_measure, tractions,
+# compute_strain) on the state of a quasi-static run:
+# name -> (params, chi (l, std, seed), dt, steps, tolerance multiplier)
+FRAME_CASES = {
+    "frames_plastic24": (plastic_shear(24), (3, 30, 15), 0.01, 90, 10.0),
+}
+
+
+def make_frames(name, spec):
+    import tempfile
+    P, (l, std, seed), dt, steps, mult = spec
+    chi = random_chi(P.m, P.n, l, 600.0, std, P.TZ, seed)
+    sim = ReferenceSim(P, chi)
+    sim.set_acc_mult(mult)
+    sim.steps(dt, steps)
+    out = {k: v for k, v in sim.fields().items()}
+    out["chi0"] = chi
+    with tempfile.TemporaryDirectory() as tmp:
+        for mode in range(11):
+            out[f"output{mode}"] = sim.output(mode, tmp)
+        sim.clear_cu()
+        q, mx = sim.qs_measure(False)
+        out["output11"] = sim.output(11, tmp)
+        qs_stag = sim.qs_measure(True)
+    out["qs"] = np.array([q, mx])
+    out["qs_staggered"] = np.array(qs_stag)
+    out["tractions"] = sim.tractions()
+    out["strain"] = sim.compute_strain()
+    meta = {"kind": "frames", "params": P.as_dict(), "dt": dt, "steps": steps, "acc_mult": mult, "time": sim.time,
+            "source": "reference shear_sim::output, qs_measure, tractions, compute_strain after "
+                      "step_forward_quasistatic, built from source"}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **out)
+
+
 def make(name, spec):
     P, (l, std, seed), dt, steps, mult = spec
     chi = random_chi(P.m, P.n, l, 600.0, std, P.TZ, seed)
@@ -103,6 +139,11 @@ def main():
             continue
         c = make(name, spec)
         print(f"{name}: {c} V-cycles")
+    for name, spec in FRAME_CASES.items():
+        if only and name not in only:
+            continue
+        make_frames(name, spec)
+        print(f"{name}: frames and diagnostics")
     for name, spec in DIRECT_CASES.items():
         if only and name not in only:
             continue
