@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(128) k_adj_advect(step_consts c, adj_fields A,
         double ddev = 0, dtmp = 0, J_ddev[ND] = {0}, J_dtmp[ND] = {0}, J_chi[ND] = {0};
         J_chi[1] = 1;  // chi_out = cchi where there is no plastic flow
         const bool athermal = c.stz_model >= 2;
-        if (!(devsq < 0.999e-24 || (athermal && devsq < c.s_y * c.s_y * (1 - 1e-12)))) {
+        if (!(devsq < 0.999e-24 || (athermal && devsq < c.yield_cut2))) {
             stz_law_params<dual> lp;
             lp.stz_model = c.stz_model; lp.t_model = c.t_model; lp.substep_cap = c.substep_cap;
             lp.t_scale = c.t_scale; lp.adapt_fac = c.adapt_fac; lp.theta = c.theta; lp.Delta = c.Delta;

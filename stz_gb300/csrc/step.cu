@@ -36,6 +36,7 @@ step_consts make_step_consts(const stz_params &p) {
     c.chi_len = p.chi_len;
     c.track_plastic = 0;
     c.substep_cap = 1 << 22;
+    c.yield_cut2 = p.s_y * p.s_y * (1 - 1e-12);
     c.clock = nullptr;
     c.xbc = 0;
     return c;
@@ -138,8 +139,10 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     // chi unchanged in the reference loop (sbar < 1e-12, or an athermal law
     // below yield); they skip the FP64 square root and the loop.  The margin
     // keeps the test exact under the rounding of sqrt.
+    // devsq >= 0, so the cut-offs compare as integers on the bit patterns
     const bool athermal = c.stz_model >= 2;
-    if (devsq < 0.999e-24 || (athermal && devsq < c.s_y * c.s_y * (1 - 1e-12))) {
+    const long long dbits = __double_as_longlong(devsq);
+    if (dbits < __double_as_longlong(0.999e-24) || (athermal && dbits < __double_as_longlong(c.yield_cut2))) {
         ddev = 0;
         dtmp = 0;
     } else {
@@ -153,9 +156,18 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     F.ddev[ci] = ddev;
     if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
     const double pn = p + fma(-vh, f2[0], -uh * f1[0]);
-    const double qn = q + (fma(-vh, f2[1], -uh * f1[1]) - dtmp * q);
-    const double sn = s + (fma(-vh, f2[2], -uh * f1[2]) + two_omega * t - dtmp * s);
-    const double tn = t + (fma(-vh, f2[3], -uh * f1[3]) - two_omega * s - dtmp * t);
+    // dtmp is exactly 0 outside plastic flow; the terms - dtmp * (q, s, t)
+    // then add exact zeros and are skipped
+    double qn, sn, tn;
+    if (dtmp != 0) {
+        qn = q + (fma(-vh, f2[1], -uh * f1[1]) - dtmp * q);
+        sn = s + (fma(-vh, f2[2], -uh * f1[2]) + two_omega * t - dtmp * s);
+        tn = t + (fma(-vh, f2[3], -uh * f1[3]) - two_omega * s - dtmp * t);
+    } else {
+        qn = q + fma(-vh, f2[1], -uh * f1[1]);
+        sn = s + (fma(-vh, f2[2], -uh * f1[2]) + two_omega * t);
+        tn = t + (fma(-vh, f2[3], -uh * f1[3]) - two_omega * s);
+    }
     B[F_P][ci] = pn;
     B[F_Q][ci] = qn;
     B[F_S][ci] = sn;
@@ -275,7 +287,7 @@ __global__ void __launch_bounds__(256) k_direct(step_consts c, direct_consts d, 
     const double devsq = 3 * q * q + s * s + t * t;
     double ddev = 0, dtmp = 0, sbar = 0;
     const bool athermal = c.stz_model >= 2;
-    if (!(devsq < 0.999e-24 || (athermal && devsq < c.s_y * c.s_y * (1 - 1e-12)))) {
+    if (!(devsq < 0.999e-24 || (athermal && devsq < c.yield_cut2))) {
         int iters;
         const stz_law_params<double> lp = law_params(c);
         sbar = sqrt(devsq);

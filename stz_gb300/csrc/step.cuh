@@ -35,6 +35,7 @@ struct step_consts {
     double chi_diff, chi_len;
     int track_plastic;
     int substep_cap;
+    double yield_cut2;  // s_y^2 (1 - 1e-12): athermal cells below it skip the plastic loop
     // Device clock of a graph-driven run (nullptr: wall quantities come as
     // kernel arguments from the host).  Layout: CLK_* below.
     const double *clock;
