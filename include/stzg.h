@@ -120,6 +120,12 @@ int stzg_get_time(stzg_sim *s, double *time);
  * it.  Pinned host memory gives full copy bandwidth. */
 int stzg_upload(stzg_sim *s, const double *const *up);
 int stzg_download(stzg_sim *s, double *const *down);
+/* Replaces: shear_sim::step_forward_quasistatic (shear_sim.cc:280-291) on
+ * host-owned fields, as the reference holds them: stzg_upload(up), one step,
+ * stzg_download(down) in one call.  The parts of the new state that the
+ * projection leaves alone (chi rows, interior rows of X and Y, eps_pl) are
+ * copied back while the multigrid solve runs. */
+int stzg_step_qs_host(stzg_sim *s, double dt, const double *const *up, double *const *down, stzg_stats *stats);
 
 /* Replaces: shear_sim::step_forward_quasistatic (shear_sim.cc:280-291),
  * called nsteps times; stats may be NULL. */

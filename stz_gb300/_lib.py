@@ -35,6 +35,7 @@ EXPORTS = [
     "stzg_adjoint_forward", "stzg_adjoint_backward",
     "stzg_step_direct", "stzg_advance_direct",
     "stzg_output_field", "stzg_write_frame", "stzg_qs_measure", "stzg_tractions", "stzg_compute_strain",
+    "stzg_step_qs_host",
 ]
 
 
@@ -130,6 +131,8 @@ def load(path=None):
         "stzg_qs_measure": (I, [V, I, _P, _P]),
         "stzg_tractions": (I, [V, _P]),
         "stzg_compute_strain": (I, [V, _P]),
+        "stzg_step_qs_host": (I, [V, D, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                  ctypes.POINTER(StzgStats)]),
     }
     for name, (res, args) in decl.items():
         f = getattr(lib, name)

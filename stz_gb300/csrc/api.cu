@@ -605,7 +605,9 @@ struct copy_job {
     size_t bytes;
 };
 
-static int run_copies(stzg_sim *s, const std::vector<copy_job> &jobs, cudaMemcpyKind kind) {
+// Enqueues the copies on the copy streams after the work queued so far on
+// the handle's stream; returns without waiting.
+static int enqueue_copies(stzg_sim *s, const std::vector<copy_job> &jobs, cudaMemcpyKind kind) {
     STZG_CHECK(copy_streams(s));
     STZG_CUDA(cudaEventRecord(s->cev_ready, s->st));
     const int ns = stzg_sim::kCopyStreams;
@@ -620,10 +622,21 @@ static int run_copies(stzg_sim *s, const std::vector<copy_job> &jobs, cudaMemcpy
                                       s->cst[k]));
         }
     }
-    for (int k = 0; k < ns; k++) {
+    return STZG_OK;
+}
+
+// Makes the handle's stream wait for every copy enqueued so far.
+static int join_copies(stzg_sim *s) {
+    for (int k = 0; k < stzg_sim::kCopyStreams; k++) {
         STZG_CUDA(cudaEventRecord(s->cev[k], s->cst[k]));
         STZG_CUDA(cudaStreamWaitEvent(s->st, s->cev[k], 0));
     }
+    return STZG_OK;
+}
+
+static int run_copies(stzg_sim *s, const std::vector<copy_job> &jobs, cudaMemcpyKind kind) {
+    STZG_CHECK(enqueue_copies(s, jobs, kind));
+    STZG_CHECK(join_copies(s));
     STZG_CUDA(cudaStreamSynchronize(s->st));
     return STZG_OK;
 }
@@ -671,6 +684,62 @@ int stzg_upload(stzg_sim *s, const double *const *up) {
         STZG_CUDA(cudaMemcpyAsync(&changed, s->F.flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s->st));
         STZG_CUDA(cudaStreamSynchronize(s->st));
         if (changed) s->have_prev = s->have_prev2 = false;
+    }
+    return STZG_OK;
+}
+
+// One quasi-static step on host-owned fields: upload, step, download.  The
+// parts of the new state that the projection does not change (the rows of
+// chi, the interior rows of X and Y, eps_pl) are copied back while the
+// multigrid solve runs; the rest follows the projection.
+int stzg_step_qs_host(stzg_sim *s, double dt, const double *const *up, double *const *down, stzg_stats *stats) {
+    if (!s || !up || !down || !(dt > 0)) return fail(STZG_EINVAL, "bad step arguments");
+    STZG_CHECK(stzg_upload(s, up));
+    stzg_stats before = s->acc;
+    const long l0 = launch_count();
+    STZG_CHECK(ensure_ops(s, dt));
+    STZG_CUDA(cudaEventRecord(s->ev0, s->st));
+    s->time += dt;  // shear_sim.cc:283
+    STZG_CHECK(do_advection(s, dt));
+    const int m = s->m, n = s->n;
+    const size_t nn = (size_t)m * (n + 1), nc = cell_count(s), row = (size_t)m * 8;
+    double *const *f = s->F.f[s->cur];
+    std::vector<copy_job> early, late;
+    if (down[F_CHI]) {
+        early.push_back({down[F_CHI] + m, f[F_CHI] + m, n * row});
+        late.push_back({down[F_CHI], f[F_CHI], row});
+        late.push_back({down[F_CHI] + (size_t)(n + 1) * m, f[F_CHI] + (size_t)(n + 1) * m, row});
+    }
+    for (int k : {F_X, F_Y}) {
+        if (!down[k]) continue;
+        // node rows 0..n live at offset m of the cell-layout array
+        early.push_back({down[k] + m, f[k] + 2 * (size_t)m, (n - 1) * row});
+        late.push_back({down[k], f[k] + m, row});
+        late.push_back({down[k] + (size_t)n * m, f[k] + (size_t)(n + 1) * m, row});
+    }
+    if (down[8]) early.push_back({down[8], s->F.eps_pl, (size_t)m * n * 8});
+    STZG_CHECK(enqueue_copies(s, early, cudaMemcpyDeviceToHost));
+    STZG_CHECK(do_projection(s, dt, true));
+    for (int k = 0; k < F_CHI; k++)
+        if (down[k]) late.push_back({down[k], f[k], nc * 8});
+    if (down[7]) late.push_back({down[7], s->F.vel, nn * sizeof(double2)});
+    STZG_CUDA(cudaEventRecord(s->ev1, s->st));
+    STZG_CHECK(enqueue_copies(s, late, cudaMemcpyDeviceToHost));
+    STZG_CHECK(join_copies(s));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->acc.seconds += ms * 1e-3;
+    STZG_CHECK(check_flags(s));
+    if (stats) {
+        *stats = s->acc;
+        stats->vcycles -= before.vcycles;
+        stats->extra_vcycles -= before.extra_vcycles;
+        stats->solves -= before.solves;
+        stats->refinements -= before.refinements;
+        stats->checks -= before.checks;
+        stats->seconds -= before.seconds;
+        stats->kernel_launches = launch_count() - l0;
     }
     return STZG_OK;
 }

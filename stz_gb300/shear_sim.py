@@ -132,6 +132,17 @@ class ShearSim:
         arr = (ctypes.c_void_p * 9)(*[p or None for p in ptrs[:9]])
         _lib.check(self.lib.stzg_download(self.h, arr))
 
+    def step_host(self, dt, up_ptrs, down_ptrs):
+        """One quasi-static step on host-owned fields (stzg_step_qs_host):
+        upload p,q,s,tau,chi,X,Y,vel, step, download them and eps_pl."""
+        up = (ctypes.c_void_p * 8)(*[p or None for p in up_ptrs[:8]])
+        down = (ctypes.c_void_p * 9)(*[p or None for p in down_ptrs[:9]])
+        st = _lib.StzgStats()
+        _lib.check(self.lib.stzg_step_qs_host(self.h, float(dt), up, down, ctypes.byref(st)))
+        self.stats = st
+        self.cycles += st.vcycles
+        return st.vcycles
+
     def time_kernel(self, dt, kernel, reps=10):
         """Average ms per launch of one kernel group (stzg_time_kernel)."""
         ms = ctypes.c_double()

@@ -197,6 +197,34 @@ def test_state_roundtrip_keeps_extrapolation_history():
     assert max(err.values()) == 0.0, err
 
 
+def test_step_host_matches_three_calls():
+    """stzg_step_qs_host (upload, step, download with the early copies
+    overlapping the solve) gives the bytes of upload + step + download."""
+    N = 48
+    P = plastic_shear(N)
+    chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, 6)
+    cells, nodes = N * (N + 2), N * (N + 1)
+
+    def bufs():
+        return [np.zeros(cells) for _ in range(5)] + [np.zeros(nodes) for _ in range(2)] + \
+               [np.zeros(2 * nodes), np.zeros(N * N)]
+
+    a, b = ShearSim(P, chi, extrapolate=True), ShearSim(P, chi, extrapolate=True)
+    a.steps(0.01, 60)
+    b.steps(0.01, 60)
+    ha, hb = bufs(), bufs()
+    a.download([x.ctypes.data for x in ha])
+    b.download([x.ctypes.data for x in hb])
+    for _ in range(8):
+        a.step_host(0.01, [x.ctypes.data for x in ha], [x.ctypes.data for x in ha])
+        b.upload([x.ctypes.data for x in hb[:8]])
+        b.steps(0.01, 1)
+        b.download([x.ctypes.data for x in hb])
+    for k in range(9):
+        np.testing.assert_array_equal(ha[k], hb[k], err_msg=str(k))
+    assert a.stats.kernel_launches > 0
+
+
 def test_extrapolated_guess_same_answer_fewer_cycles():
     N = 64
     P = simple_shear(N)
