@@ -23,6 +23,7 @@ def main(argv=None):
     ap.add_argument("--std", type=float, default=40.0)
     ap.add_argument("--corr", type=float, default=16.0)
     ap.add_argument("--no-extrapolate", action="store_true")
+    ap.add_argument("--direct", action="store_true", help="explicit steps (dt = dx^2/2) instead of quasi-static")
     a = ap.parse_args(argv)
     N = a.size
     P = simple_shear(N)
@@ -30,6 +31,15 @@ def main(argv=None):
     prec = _lib.MIXED if a.precision == "mixed" else _lib.FP64
     sim = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=a.tol,
                    extrapolate=not a.no_extrapolate)
+    if a.direct:
+        ddt = 0.5 * (2.0 / N) ** 2
+        sim.step_forward(ddt, a.warmup)
+        t0 = time.time()
+        sim.step_forward(ddt, a.steps)
+        t = time.time() - t0
+        print(f"N={N} explicit: {1e3 * t / max(a.steps, 1):.2f} ms/step, {sim.stats.kernel_launches} kernels")
+        sim.close()
+        return
     sim.steps(1e-2, a.warmup)
     t0 = time.time()
     sim.steps(1e-2, a.steps)
