@@ -350,6 +350,7 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(STZG_ENODEV, "no CUDA device");
     if (o.device < 0 || o.device >= ndev) return fail(STZG_EINVAL, "device ordinal out of range");
     STZG_CUDA(cudaSetDevice(o.device));
+    STZG_CUDA(prepare_step_kernels());
     stzg_sim *s = new stzg_sim;
     s->P = *p;
     s->O = o;

@@ -58,20 +58,153 @@ struct velo {
 
 #define IDX(i, j) ((size_t)((j) + 1) * m + (i))
 
-// Fused advection + STZ step per cell (i,j) and its lower-left node.
-__global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int cur, double dt, double bv,
-                                                int emit_source) {
+// Fused advection + STZ step over a tile of ATX x ATY cells (i,j) and their
+// lower-left nodes.
+//
+// ENO2 through shared differences: on a line f, the first differences
+// D(c+1/2) = f(c+1) - f(c) and second differences S(c) = D(c+1/2) - D(c-1/2)
+// are computed once per tile (with a halo) into shared memory, and each
+// point's ENO2 value is one FMA on them:
+//   upwind from the left:  eno2 = 2 D(i-1/2) + (|S(i)| > |S(i-1)| ? S(i-1) : S(i))
+//   upwind from the right: eno2 = -2 D(i+1/2) + (|S(i)| > |S(i+1)| ? S(i+1) : S(i))
+// These are the values of eno2(p0..p3) in step.cuh operation for operation
+// (p0 - p1, p1 - p2 and p2 - p3 are the D's up to exact negations, and
+// (-a) - (-b) rounds as b - a), so the result is the same double.  A point
+// costs three FP64 operations per direction plus its share of the tile's
+// halo instead of six.  The reference map X is unwrapped across the periodic
+// seam by the column's offset (+-lx) before differencing, as the per-point
+// form adds it to each shifted value.
+constexpr int ATX = 32, ATY = 8;
+constexpr int ADXW = ATX + 3;  // D(c+1/2), tile columns c = -2..ATX
+constexpr int ASXW = ATX + 2;  // S(c), c = -1..ATX
+constexpr int ADYH = ATY + 3;  // D(r+1/2), tile rows r = -2..ATY
+constexpr int ASYH = ATY + 2;  // S(r), r = -1..ATY
+constexpr int ACOLS = ATX + 4; // tile columns -2..ATX+1
+
+__device__ __forceinline__ double eno_left(const double *d, const double *s, int k) {
+    // d[k] = D(i-1/2), s[k] = S(i), s[k-1] = S(i-1)
+    const double s0 = s[k], s1 = s[k - 1];
+    return fma(2.0, d[k], mag_gt(s0, s1) ? s1 : s0);
+}
+__device__ __forceinline__ double eno_right(const double *d, const double *s, int k) {
+    // d[k+1] = D(i+1/2), s[k] = S(i), s[k+1] = S(i+1)
+    const double s0 = s[k], s1 = s[k + 1];
+    return fma(-2.0, d[k + 1], mag_gt(s0, s1) ? s1 : s0);
+}
+
+template <int NF> struct eno_tile {
+    double dx[NF][ATY][ADXW];
+    double dy[NF][ADYH][ATX];
+    double sx[NF][ATY][ASXW];
+    double sy[NF][ASYH][ATX];
+    double xo[ACOLS];  // X offset of the unwrapped column
+    int col[ACOLS];    // storage column of tile column c-2
+};
+typedef eno_tile<F_COUNT> adv_tile;
+
+// Fills the tile's first and second differences of NF fields over cell rows
+// j0..j0+ATY-1 (x) and rows j0-2..j0+ATY+1 (y).  get(f, row, col) reads field
+// f at row -1..n and storage column col; rows below low(f) (-1 for the stored
+// fields, 0 for the node velocity) and above n hold no value, and the
+// differences that would need them are never used.  Field xf (the reference
+// map X) is unwrapped across the periodic seam.  Ends with __syncthreads.
+template <int NF, typename Get, typename Low>
+__device__ __forceinline__ void fill_eno_tile(eno_tile<NF> &T, int i0, int j0, int m, int n, double lx, int xf,
+                                              Get get, Low low) {
+    const int tid = threadIdx.y * ATX + threadIdx.x;
+    if (tid < ACOLS) {
+        const int u = i0 + tid - 2;  // unwrapped column
+        int w = u % m;
+        if (w < 0) w += m;
+        T.col[tid] = w;
+        T.xo[tid] = u < 0 ? -lx : (u >= m ? lx : 0.0);
+    }
+    __syncthreads();
+    for (int k = tid; k < NF * ATY * ADXW; k += ATX * ATY) {
+        const int f = k / (ATY * ADXW), rem = k - f * (ATY * ADXW), r = rem / ADXW, cc = rem - r * ADXW;
+        const int jj = j0 + r;
+        double d = 0;
+        if (jj < n) {
+            double hi = get(f, jj, T.col[cc + 1]), lo = get(f, jj, T.col[cc]);
+            if (f == xf) {
+                if (T.xo[cc + 1] != 0) hi += T.xo[cc + 1];
+                if (T.xo[cc] != 0) lo += T.xo[cc];
+            }
+            d = hi - lo;
+        }
+        T.dx[f][r][cc] = d;
+    }
+    for (int k = tid; k < NF * ADYH * ATX; k += ATX * ATY) {
+        const int f = k / (ADYH * ATX), rem = k - f * (ADYH * ATX), r = rem / ATX, cc = rem - r * ATX;
+        const int jj = j0 + r - 2, ii = i0 + cc;
+        double d = 0;
+        if (jj >= low(f) && jj + 1 <= n && ii < m) d = get(f, jj + 1, ii) - get(f, jj, ii);
+        T.dy[f][r][cc] = d;
+    }
+    __syncthreads();
+    for (int k = tid; k < NF * ATY * ASXW; k += ATX * ATY) {
+        const int f = k / (ATY * ASXW), rem = k - f * (ATY * ASXW), r = rem / ASXW, cc = rem - r * ASXW;
+        T.sx[f][r][cc] = T.dx[f][r][cc + 1] - T.dx[f][r][cc];
+    }
+    for (int k = tid; k < NF * ASYH * ATX; k += ATX * ATY) {
+        const int f = k / (ASYH * ATX), rem = k - f * (ASYH * ATX), r = rem / ATX, cc = rem - r * ATX;
+        T.sy[f][r][cc] = T.dy[f][r + 1][cc] - T.dy[f][r][cc];
+    }
+    __syncthreads();
+}
+
+// ENO2 values of a point at tile column tx / row ty from the tile (the
+// factor hs is applied by the caller).
+template <int NF>
+__device__ __forceinline__ double tile_eno_x(const eno_tile<NF> &T, int f, int ty, int tx, bool from_left) {
+    const double *d = T.dx[f][ty], *s = T.sx[f][ty];
+    const int k = tx + 1;
+    return from_left ? eno_left(d, s, k) : eno_right(d, s, k);
+}
+// y direction with the one-sided wall rows: `inner` is false on the last row
+// before the wall on the upwind side.
+template <int NF>
+__device__ __forceinline__ double tile_eno_y(const eno_tile<NF> &T, int f, int ty, int tx, bool from_below,
+                                             bool inner) {
+    const int ky = ty + 1;
+    const double s0 = T.sy[f][ky][tx];
+    if (from_below) {
+        const double d = T.dy[f][ky][tx];
+        if (!inner) return 2 * d;
+        const double s1 = T.sy[f][ky - 1][tx];
+        return fma(2.0, d, mag_gt(s0, s1) ? s1 : s0);
+    }
+    const double d = T.dy[f][ky + 1][tx];
+    if (!inner) return -2 * d;
+    const double s1 = T.sy[f][ky + 1][tx];
+    return fma(-2.0, d, mag_gt(s0, s1) ? s1 : s0);
+}
+
+// Per-launch constants of the step that depend on dt (computed on the host
+// with the same operations the per-thread code used).
+struct advect_consts {
+    double hx, hy;  // dt/(2 dx), dt/(2 dy)
+    double xf, yf;  // 1/(2 dt dx), 1/(2 dt dy) of projection_step
+};
+
+__global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_consts a, fields_dev F, int cur,
+                                                      double dt, double bv, int emit_source) {
+    extern __shared__ __align__(16) unsigned char adv_smem[];
+    adv_tile &T = *reinterpret_cast<adv_tile *>(adv_smem);
     const int m = c.m, n = c.n;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= m || j >= n) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY;
+    const int i = i0 + tx, j = j0 + ty;
     if (c.clock) cur = (int)c.clock[CLK_CUR];
     const double *__restrict__ const *A = F.f[cur];
     double *const *B = F.f[cur ^ 1];
-    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt, lx = c.lx;
-    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
-    const int il2 = i <= 1 ? i + m - 2 : i - 2, ir2 = i >= m - 2 ? i + 2 - m : i + 2;
-    const size_t ci = IDX(i, j);
+    fill_eno_tile<F_COUNT>(
+        T, i0, j0, m, n, c.lx, F_X,
+        [&](int f, int row, int col) { return A[f][(size_t)(row + 1) * m + col]; }, [](int) { return -1; });
+    if (i >= m || j >= n) return;
+    const double hx = a.hx, hy = a.hy;
+    const size_t ci = (size_t)(j + 1) * m + i;
+    const int ir = T.col[tx + 3];
     if (c.clock) bv = c.clock[CLK_BV_STATE];
     velo V{F.vel, m, n, bv};
     // Upwind ENO values without the factor hs = +-dt/(2 dx); it is folded
@@ -82,32 +215,11 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
         double ex_X, ex_Y, ey_X, ey_Y;
         const double un = V.u(i, j), vn = V.v(i, j);
         const double uh = un * (un > 0 ? hx : -hx), vh = vn * (vn > 0 ? hy : -hy);
-        if (un > 0) {
-            ex_X = eno2(X[IDX(ir, j)] + (i == m - 1 ? lx : 0), X[ci], X[IDX(il, j)] + (i == 0 ? -lx : 0),
-                        X[IDX(il2, j)] + (i <= 1 ? -lx : 0));
-            ex_Y = eno2(Y[IDX(ir, j)], Y[ci], Y[IDX(il, j)], Y[IDX(il2, j)]);
-        } else {
-            ex_X = eno2(X[IDX(il, j)] + (i == 0 ? -lx : 0), X[ci], X[IDX(ir, j)] + (i == m - 1 ? lx : 0),
-                        X[IDX(ir2, j)] + (i >= m - 2 ? lx : 0));
-            ex_Y = eno2(Y[IDX(il, j)], Y[ci], Y[IDX(ir, j)], Y[IDX(ir2, j)]);
-        }
-        if (vn > 0) {
-            if (j > 1) {
-                ey_X = eno2(X[IDX(i, j + 1)], X[ci], X[IDX(i, j - 1)], X[IDX(i, j - 2)]);
-                ey_Y = eno2(Y[IDX(i, j + 1)], Y[ci], Y[IDX(i, j - 1)], Y[IDX(i, j - 2)]);
-            } else {
-                ey_X = 2 * (X[ci] - X[IDX(i, j - 1)]);
-                ey_Y = 2 * (Y[ci] - Y[IDX(i, j - 1)]);
-            }
-        } else {
-            if (j < n - 1) {
-                ey_X = eno2(X[IDX(i, j - 1)], X[ci], X[IDX(i, j + 1)], X[IDX(i, j + 2)]);
-                ey_Y = eno2(Y[IDX(i, j - 1)], Y[ci], Y[IDX(i, j + 1)], Y[IDX(i, j + 2)]);
-            } else {
-                ey_X = 2 * (X[ci] - X[IDX(i, j + 1)]);
-                ey_Y = 2 * (Y[ci] - Y[IDX(i, j + 1)]);
-            }
-        }
+        ex_X = tile_eno_x(T, F_X, ty, tx, un > 0);
+        ex_Y = tile_eno_x(T, F_Y, ty, tx, un > 0);
+        const bool inner = vn > 0 ? j > 1 : j < n - 1;
+        ey_X = tile_eno_y(T, F_X, ty, tx, vn > 0, inner);
+        ey_Y = tile_eno_y(T, F_Y, ty, tx, vn > 0, inner);
         B[F_X][ci] = X[ci] + fma(-vh, ey_X, -uh * ex_X);
         B[F_Y][ci] = Y[ci] + fma(-vh, ey_Y, -uh * ex_Y);
     }
@@ -119,18 +231,11 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     const double uh = uc * (uc > 0 ? hx : -hx), vh = vc * (vc > 0 ? hy : -hy);
     // ENO derivatives of p, q, s, tau, chi (shear_sim.cc:336-338)
     double f1[5], f2[5];
+    const bool inner = vc > 0 ? j > 0 : j < n - 1;
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const double *G = A[k];
-        if (uc > 0) f1[k] = eno2(G[IDX(ir, j)], G[ci], G[IDX(il, j)], G[IDX(il2, j)]);
-        else f1[k] = eno2(G[IDX(il, j)], G[ci], G[IDX(ir, j)], G[IDX(ir2, j)]);
-        if (vc > 0) {
-            if (j > 0) f2[k] = eno2(G[IDX(i, j + 1)], G[ci], G[IDX(i, j - 1)], G[IDX(i, j - 2)]);
-            else f2[k] = 2 * (G[ci] - G[IDX(i, j - 1)]);
-        } else {
-            if (j < n - 1) f2[k] = eno2(G[IDX(i, j - 1)], G[ci], G[IDX(i, j + 1)], G[IDX(i, j + 2)]);
-            else f2[k] = 2 * (G[ci] - G[IDX(i, j + 1)]);
-        }
+        f1[k] = tile_eno_x(T, k, ty, tx, uc > 0);
+        f2[k] = tile_eno_y(T, k, ty, tx, vc > 0, inner);
     }
     const double p = A[F_P][ci], q = A[F_Q][ci], s = A[F_S][ci], t = A[F_TAU][ci];
     double cchi = A[F_CHI][ci] + fma(-vh, f2[4], -uh * f1[4]), ddev, dtmp;
@@ -173,12 +278,11 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
     B[F_S][ci] = sn;
     B[F_TAU][ci] = tn;
     if (emit_source) {
-        const double xf = 0.5 / dt * c.xsp, yf = 0.5 / dt * c.ysp;
         const double pq = pn + qn, Aa = pq - sn, Bb = pq + sn;
-        F.pre[0][ci] = xf * Aa + yf * tn;
-        F.pre[1][ci] = xf * Aa - yf * tn;
-        F.pre[2][ci] = xf * tn - yf * Bb;
-        F.pre[3][ci] = xf * tn + yf * Bb;
+        F.pre[0][ci] = a.xf * Aa + a.yf * tn;
+        F.pre[1][ci] = a.xf * Aa - a.yf * tn;
+        F.pre[2][ci] = a.xf * tn - a.yf * Bb;
+        F.pre[3][ci] = a.xf * tn + a.yf * Bb;
     }
 }
 
@@ -194,53 +298,45 @@ __global__ void __launch_bounds__(256) k_advect(step_consts c, fields_dev F, int
 // F.src (rows 1..n-1), the other fields to buffer cur^1.
 struct direct_consts {
     double hxxv, hyyv, hcv, hxxcd, hyycd, hccd;
+    double hx, hy, mu_inv;
 };
 
-__global__ void __launch_bounds__(256) k_direct(step_consts c, direct_consts d, fields_dev F, int cur, double dt,
-                                                double bv) {
+// Tile fields of the explicit step: the seven stored fields, then the node
+// velocity components u and v (rows 0..n, walls substituted).
+enum { DF_U = F_COUNT, DF_V, DF_COUNT };
+typedef eno_tile<DF_COUNT> direct_tile;
+
+__global__ void __launch_bounds__(ATX * ATY) k_direct(step_consts c, direct_consts d, fields_dev F, int cur,
+                                                      double dt, double bv) {
+    extern __shared__ __align__(16) unsigned char dir_smem[];
+    direct_tile &TT = *reinterpret_cast<direct_tile *>(dir_smem);
     const int m = c.m, n = c.n;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= m || j >= n) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY;
+    const int i = i0 + tx, j = j0 + ty;
     const double *__restrict__ const *A = F.f[cur];
     double *const *B = F.f[cur ^ 1];
-    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt, lx = c.lx, mu_inv = 1 / c.mu;
-    const int il = i == 0 ? m - 1 : i - 1, ir = i == m - 1 ? 0 : i + 1;
-    const int il2 = i <= 1 ? i + m - 2 : i - 2, ir2 = i >= m - 2 ? i + 2 - m : i + 2;
-    const size_t ci = IDX(i, j);
     velo V{F.vel, m, n, bv};
+    fill_eno_tile<DF_COUNT>(
+        TT, i0, j0, m, n, c.lx, F_X,
+        [&](int f, int row, int col) {
+            return f == DF_U ? V.u(col, row) : (f == DF_V ? V.v(col, row) : A[f][(size_t)(row + 1) * m + col]);
+        },
+        [](int f) { return f >= DF_U ? 0 : -1; });
+    if (i >= m || j >= n) return;
+    const double hx = d.hx, hy = d.hy, mu_inv = d.mu_inv;
+    const int il = TT.col[tx + 1], ir = TT.col[tx + 3];
+    const size_t ci = IDX(i, j);
     const double *P = A[F_P], *Q = A[F_Q], *S = A[F_S], *T = A[F_TAU];
     if (j > 0) {
         const double *X = A[F_X], *Y = A[F_Y];
         const double un = V.u(i, j), vn = V.v(i, j);
         const double hsx = un > 0 ? hx : -hx, hsy = vn > 0 ? hy : -hy;
-        double ux, vx, Xx, Yx, uy, vy, Xy, Yy;
-        if (un > 0) {
-            ux = eno2(V.u(ir, j), un, V.u(il, j), V.u(il2, j));
-            vx = eno2(V.v(ir, j), vn, V.v(il, j), V.v(il2, j));
-            Xx = eno2(X[IDX(ir, j)] + (i == m - 1 ? lx : 0), X[ci], X[IDX(il, j)] + (i == 0 ? -lx : 0),
-                      X[IDX(il2, j)] + (i <= 1 ? -lx : 0));
-            Yx = eno2(Y[IDX(ir, j)], Y[ci], Y[IDX(il, j)], Y[IDX(il2, j)]);
-        } else {
-            ux = eno2(V.u(il, j), un, V.u(ir, j), V.u(ir2, j));
-            vx = eno2(V.v(il, j), vn, V.v(ir, j), V.v(ir2, j));
-            Xx = eno2(X[IDX(il, j)] + (i == 0 ? -lx : 0), X[ci], X[IDX(ir, j)] + (i == m - 1 ? lx : 0),
-                      X[IDX(ir2, j)] + (i >= m - 2 ? lx : 0));
-            Yx = eno2(Y[IDX(il, j)], Y[ci], Y[IDX(ir, j)], Y[IDX(ir2, j)]);
-        }
-        const int jn = vn > 0 ? j - 1 : j + 1;  // upwind neighbour row
-        if ((vn > 0 && j > 1) || (vn <= 0 && j < n - 1)) {
-            const int j0 = vn > 0 ? j + 1 : j - 1, j3 = vn > 0 ? j - 2 : j + 2;
-            uy = eno2(V.u(i, j0), un, V.u(i, jn), V.u(i, j3));
-            vy = eno2(V.v(i, j0), vn, V.v(i, jn), V.v(i, j3));
-            Xy = eno2(X[IDX(i, j0)], X[ci], X[IDX(i, jn)], X[IDX(i, j3)]);
-            Yy = eno2(Y[IDX(i, j0)], Y[ci], Y[IDX(i, jn)], Y[IDX(i, j3)]);
-        } else {
-            uy = 2 * (un - V.u(i, jn));
-            vy = 2 * (vn - V.v(i, jn));
-            Xy = 2 * (X[ci] - X[IDX(i, jn)]);
-            Yy = 2 * (Y[ci] - Y[IDX(i, jn)]);
-        }
+        double ux = tile_eno_x(TT, DF_U, ty, tx, un > 0), vx = tile_eno_x(TT, DF_V, ty, tx, un > 0);
+        double Xx = tile_eno_x(TT, F_X, ty, tx, un > 0), Yx = tile_eno_x(TT, F_Y, ty, tx, un > 0);
+        const bool inner = vn > 0 ? j > 1 : j < n - 1;
+        double uy = tile_eno_y(TT, DF_U, ty, tx, vn > 0, inner), vy = tile_eno_y(TT, DF_V, ty, tx, vn > 0, inner);
+        double Xy = tile_eno_y(TT, F_X, ty, tx, vn > 0, inner), Yy = tile_eno_y(TT, F_Y, ty, tx, vn > 0, inner);
         ux *= hsx; vx *= hsx; Xx *= hsx; Yx *= hsx;
         uy *= hsy; vy *= hsy; Xy *= hsy; Yy *= hsy;
         // net force from the cells (i-1,j-1), (i,j-1), (i-1,j), (i,j)
@@ -267,18 +363,11 @@ __global__ void __launch_bounds__(256) k_direct(step_consts c, direct_consts d, 
     const double two_omega = vx - uy;
     const double uh = uc * (uc > 0 ? hx : -hx), vh = vc * (vc > 0 ? hy : -hy);
     double f1[5], f2[5];
+    const bool inner = vc > 0 ? j > 0 : j < n - 1;
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-        const double *G = A[k];
-        if (uc > 0) f1[k] = eno2(G[IDX(ir, j)], G[ci], G[IDX(il, j)], G[IDX(il2, j)]);
-        else f1[k] = eno2(G[IDX(il, j)], G[ci], G[IDX(ir, j)], G[IDX(ir2, j)]);
-        if (vc > 0) {
-            if (j > 0) f2[k] = eno2(G[IDX(i, j + 1)], G[ci], G[IDX(i, j - 1)], G[IDX(i, j - 2)]);
-            else f2[k] = 2 * (G[ci] - G[IDX(i, j - 1)]);
-        } else {
-            if (j < n - 1) f2[k] = eno2(G[IDX(i, j - 1)], G[ci], G[IDX(i, j + 1)], G[IDX(i, j + 2)]);
-            else f2[k] = 2 * (G[ci] - G[IDX(i, j + 1)]);
-        }
+        f1[k] = tile_eno_x(TT, k, ty, tx, uc > 0);
+        f2[k] = tile_eno_y(TT, k, ty, tx, vc > 0, inner);
     }
     const double *CH = A[F_CHI];
     const double p = P[ci], q = Q[ci], s = S[ci], t = T[ci];
@@ -419,9 +508,29 @@ inline dim3 g2(int m, int n, dim3 b) { return dim3(ceil_div(m, b.x), ceil_div(n,
 
 }  // namespace
 
+cudaError_t prepare_step_kernels() {
+    static unsigned long long done = 0;  // per device ordinal
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 64 && (done >> dev & 1)) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_advect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(adv_tile));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_direct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(direct_tile));
+    if (e == cudaSuccess && dev < 64) done |= 1ull << dev;
+    return e;
+}
+
 void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st) {
     dim3 blk(32, 8);
-    k_advect<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt, bv, 1); note_launch();
+    advect_consts a;
+    a.hx = 0.5 * c.xsp * dt;
+    a.hy = 0.5 * c.ysp * dt;
+    a.xf = 0.5 / dt * c.xsp;
+    a.yf = 0.5 / dt * c.ysp;
+    k_advect<<<dim3(ceil_div(c.m, ATX), ceil_div(c.n, ATY)), dim3(ATX, ATY), sizeof(adv_tile), st>>>(c, a, F, cur,
+                                                                                                      dt, bv, 1);
+    note_launch();
     if (c.chi_diff != 0 || c.chi_len != 0) {
         k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);
         note_launch();
@@ -432,14 +541,17 @@ void direct_step(const step_consts &c, double viscosity, fields_dev &F, int cur,
                  cudaStream_t st) {
     const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
     direct_consts d;
+    d.hx = hx;
+    d.hy = hy;
+    d.mu_inv = 1 / c.mu;
     d.hxxv = 2 * c.xsp * hx * viscosity;
     d.hyyv = 2 * c.ysp * hy * viscosity;
     d.hcv = 2 * (d.hxxv + d.hyyv);
     d.hxxcd = 2 * c.xsp * hx * c.chi_diff;
     d.hyycd = 2 * c.ysp * hy * c.chi_diff;
     d.hccd = 2 * (d.hxxcd + d.hyycd);
-    dim3 blk(32, 8);
-    k_direct<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, d, F, cur, dt, bv);
+    dim3 blk(ATX, ATY);
+    k_direct<<<g2(c.m, c.n, blk), blk, sizeof(direct_tile), st>>>(c, d, F, cur, dt, bv);
     note_launch();
     if (c.chi_diff != 0 || c.chi_len != 0) {
         k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);

@@ -76,6 +76,9 @@ __device__ __forceinline__ double eno2(double p0, double p1, double p2, double p
 // (shear_sim.cc:296-386, fields.hh:61-80).  bv is the wall speed of the
 // current state (u = -bv on row 0 and +bv on row n, set_boundaries).
 void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st);
+// Opts the advection kernel into the shared memory its tile needs (once per
+// process, outside any stream capture).
+cudaError_t prepare_step_kernels();
 // shear_sim::step_forward (shear_sim.cc:185-276) up to set_boundaries:
 // explicit update of buffer cur into cur^1, new interior node velocities in
 // F.src (rows 1..n-1), chi diffusion.  bv is the wall speed of the state.
