@@ -1,6 +1,8 @@
 #!/bin/sh
-# Builds the reference's own quasi-static shear step from its sources, read in
-# place under the reference tree, into oracle/_ref/libstzref.so (test-only).
+# Builds the reference's own quasi-static shear step and its general multigrid
+# on the poisson_fd problem class from their sources, read in place under the
+# reference tree, into oracle/_ref/libstzref.so and oracle/_ref/libtgmgref.so
+# (test-only).
 #
 #   oracle/build_ref.sh [REFERENCE_ROOT]     (default: /root/reference)
 #
@@ -12,7 +14,10 @@
 #   2. g++ compiles esim/sb/main/{shear_sim,qs_multi,common}.cc and
 #      esim/shared/mat.cc with the reference's flags (esim/config/
 #      config.mk.linux:4: -Wall -ansi -pedantic -fopenmp -O3) plus -fPIC,
-#      together with oracle/ref_driver.cc, into one shared library.
+#      together with oracle/ref_driver.cc, into one shared library;
+#   3. g++ compiles esim/tgmg/poisson_fd.cc (which includes the generated
+#      tgmg.cc and instantiates tgmg<poisson_fd,double,double>) with
+#      oracle/ref_tgmg_driver.cc into a second one.
 # Only x86/Arm-neutral flags are used; nothing here runs on the GPU.
 set -e
 REF=${1:-/root/reference}
@@ -39,7 +44,12 @@ $CXX $FLAGS $INC -c "$ESIM/sb/main/qs_multi.cc" -o "$OBJ/qs_multi.o" &
 $CXX $FLAGS $INC -c "$ESIM/sb/main/common.cc" -o "$OBJ/common.o" &
 $CXX $FLAGS $INC -c "$ESIM/shared/mat.cc" -o "$OBJ/mat.o" &
 $CXX $FLAGS $INC -c "$HERE/ref_driver.cc" -o "$OBJ/ref_driver.o" &
+TG="$OUT/objtg"
+mkdir -p "$TG"
+$CXX $FLAGS $INC -c "$ESIM/tgmg/poisson_fd.cc" -o "$TG/poisson_fd.o" &
+$CXX $FLAGS $INC -c "$HERE/ref_tgmg_driver.cc" -o "$TG/ref_tgmg_driver.o" &
 wait
 $CXX -shared -fopenmp -o "$OUT/libstzref.so" "$OBJ"/*.o
-rm -rf "$GEN" "$OBJ"
-echo "build_ref: wrote $OUT/libstzref.so"
+$CXX -shared -fopenmp -o "$OUT/libtgmgref.so" "$TG"/*.o
+rm -rf "$GEN" "$OBJ" "$TG"
+echo "build_ref: wrote $OUT/libstzref.so $OUT/libtgmgref.so"

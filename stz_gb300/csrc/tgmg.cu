@@ -1,0 +1,892 @@
+// General scalar geometric multigrid on one GPU (include/stzg_tgmg.h): the
+// tgmg<S,double,double> template of esim/tgmg (tgmg.hh:42-495,
+// tgmg.in.cc:11-856) for problem classes such as poisson_fd
+// (esim/tgmg/poisson_fd.hh:7-61).
+//
+// Layout: every level keeps z, b and a residual buffer r (FP64, row-major,
+// index j*m+i) and its operator as a table of distinct 9-point stencils plus
+// the reciprocal centre, with a stencil index per point; the top level uses
+// the problem's own table.  Coarse operators are the Galerkin products
+// P^T A P of tgmg_base::rat (tgmg.in.cc:667-736) with the reference's
+// one-dimensional interpolation in each direction (apply_t / t_line,
+// tgmg.in.cc:552-621; restriction is its transpose, apply_r :626-647).
+// Gauss-Seidel runs in four colours ((i&1),(j&1)), a true Gauss-Seidel
+// ordering for 9-point stencils, with a third colour for the last line of an
+// odd periodic direction; the reference sweeps zebra-lexicographically
+// (tgmg.in.cc:128-208), so iterates differ and converged solutions agree.
+// The coarsest level (more than 10 points, the next coarsening would have
+// at most 10, tgmg_config.hh:23) is solved exactly with a dense inverse
+// where it has at most 1024 points, else smoothed like the reference.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "common.cuh"
+#include "stzg_tgmg.h"
+#include "transfer1d.cuh"
+
+namespace stzg {
+namespace {
+
+struct gst {
+    double e[10];  // dl dc dr cl cc cr ul uc ur, 1/cc (tgmg_level::s, tgmg.hh:256-265)
+};
+
+struct glevel {
+    int m, n, xp, yp;
+    int cx_n, cy_n;  // colours per direction: 2, or 3 on an odd periodic line
+    const int *cls;
+    const gst *st;
+    double *z, *b, *r;
+};
+
+constexpr int kMaxLevels = 17;
+constexpr int kGridMin = 10;        // tgmg_grid_min, tgmg_config.hh:23
+constexpr int kBottomDirect = 1024; // largest coarsest level solved by a dense inverse
+constexpr int kRedBlocks = 4 * 152;
+constexpr int kRedThreads = 256;
+
+// Neighbour index on a line of m points, or -1 outside a non-periodic line.
+__host__ __device__ inline int nbr(int i, int d, int m, int prd) {
+    const int k = i + d;
+    if (k < 0) return prd ? k + m : -1;
+    if (k >= m) return prd ? k - m : -1;
+    return k;
+}
+
+// Off-diagonal product sum_k a_k z_k at (i, j) (tgmg_level::mul_a,
+// tgmg.in.cc:536-547); neighbours outside a non-periodic grid are skipped.
+__device__ __forceinline__ double offdiag(const glevel &L, const gst &s, int i, int j) {
+    const int il = nbr(i, -1, L.m, L.xp), ir = nbr(i, 1, L.m, L.xp);
+    const int jd = nbr(j, -1, L.n, L.yp), ju = nbr(j, 1, L.n, L.yp);
+    double a = 0;
+    if (jd >= 0) {
+        const double *zr = L.z + (size_t)jd * L.m;
+        if (il >= 0) a += s.e[0] * zr[il];
+        a += s.e[1] * zr[i];
+        if (ir >= 0) a += s.e[2] * zr[ir];
+    }
+    {
+        const double *zr = L.z + (size_t)j * L.m;
+        if (il >= 0) a += s.e[3] * zr[il];
+        if (ir >= 0) a += s.e[5] * zr[ir];
+    }
+    if (ju >= 0) {
+        const double *zr = L.z + (size_t)ju * L.m;
+        if (il >= 0) a += s.e[6] * zr[il];
+        a += s.e[7] * zr[i];
+        if (ir >= 0) a += s.e[8] * zr[ir];
+    }
+    return a;
+}
+
+// k-th line of colour c on a line of m points with cn colours: colour 0 the
+// even lines, 1 the odd ones, 2 the last line of an odd periodic direction
+// (a neighbour of line 0); -1 when there is none.
+__device__ __forceinline__ int color_line(int k, int c, int m, int cn) {
+    if (c == 2) return k == 0 ? m - 1 : -1;
+    const int i = c + 2 * k;
+    if (i >= m || (cn == 3 && i == m - 1)) return -1;
+    return i;
+}
+
+// One colour of Gauss-Seidel (omega = 1) or SOR: z += omega (D^-1 (b - A'z) - z)
+// (gauss_seidel, sor: tgmg.in.cc:128-230).
+__global__ void k_tg_color(glevel L, int cx, int cy, double omega) {
+    const int i = color_line(blockIdx.x * blockDim.x + threadIdx.x, cx, L.m, L.cx_n);
+    const int j = color_line(blockIdx.y * blockDim.y + threadIdx.y, cy, L.n, L.cy_n);
+    if (i < 0 || j < 0) return;
+    const size_t ij = (size_t)j * L.m + i;
+    const gst &s = L.st[L.cls[ij]];
+    const double t = s.e[9] * (L.b[ij] - offdiag(L, s, i, j));
+    L.z[ij] = omega == 1.0 ? t : L.z[ij] + omega * (t - L.z[ij]);
+}
+
+// Jacobi update into r (jacobi, tgmg.in.cc:69-85); the caller copies r to z.
+__global__ void k_tg_jacobi(glevel L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= L.m || j >= L.n) return;
+    const size_t ij = (size_t)j * L.m + i;
+    const gst &s = L.st[L.cls[ij]];
+    L.r[ij] = s.e[9] * (L.b[ij] - offdiag(L, s, i, j));
+}
+
+// r = b - A z (tgmg_base::res, tgmg.hh:197-199).
+__global__ void k_tg_residual(glevel L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= L.m || j >= L.n) return;
+    const size_t ij = (size_t)j * L.m + i;
+    const gst &s = L.st[L.cls[ij]];
+    L.r[ij] = L.b[ij] - offdiag(L, s, i, j) - s.e[4] * L.z[ij];
+}
+
+// Fine line index 2I+d, wrapped on a periodic line; -1 outside.
+__device__ __forceinline__ int fine_at(int I, int d, int m, int prd) {
+    int f = 2 * I + d;
+    if (f < 0 || f >= m) {
+        if (!prd) return -1;
+        f = f < 0 ? f + m : f - m;
+    }
+    return f;
+}
+
+// Child b = P^T r (apply_r, tgmg.in.cc:626-647): weights 1, 1/2, 1/4 from
+// the interpolation's halves in each direction.
+__global__ void k_tg_restrict(glevel F, glevel C) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y;
+    if (I >= C.m || J >= C.n) return;
+    double a = 0;
+#pragma unroll
+    for (int dy = -1; dy <= 1; dy++) {
+        const int fy = fine_at(J, dy, F.n, F.yp);
+        if (fy < 0) continue;
+        const int hy = halves_of(fy, F.n, F.yp, J);
+        if (!hy) continue;
+#pragma unroll
+        for (int dx = -1; dx <= 1; dx++) {
+            const int fx = fine_at(I, dx, F.m, F.xp);
+            if (fx < 0) continue;
+            const int hx = halves_of(fx, F.m, F.xp, I);
+            if (!hx) continue;
+            a += (double)(hx * hy) * 0.25 * F.r[(size_t)fy * F.m + fx];
+        }
+    }
+    C.b[(size_t)J * C.m + I] = a;
+}
+
+// Parent z += P z_child (apply_t, tgmg.in.cc:552-606).
+__global__ void k_tg_prolong(glevel C, glevel F) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= F.m || j >= F.n) return;
+    int cy[2], hy[2], cx[2], hx[2];
+    const int ny = p1d_halves(j, F.n, F.yp, cy, hy), nx = p1d_halves(i, F.m, F.xp, cx, hx);
+    double a = 0;
+    for (int q = 0; q < ny; q++)
+        for (int p = 0; p < nx; p++) a += (double)(hx[p] * hy[q]) * 0.25 * C.z[(size_t)cy[q] * C.m + cx[p]];
+    F.z[(size_t)j * F.m + i] += a;
+}
+
+// Coarsest level: z = A^-1 b with the dense FP64 inverse.
+__global__ void k_tg_bottom(glevel B, const double *__restrict__ inv, int N) {
+    __shared__ double bb[kBottomDirect];
+    for (int k = threadIdx.x; k < N; k += blockDim.x) bb[k] = B.b[k];
+    __syncthreads();
+    for (int r = threadIdx.x; r < N; r += blockDim.x) {
+        const double *row = inv + (size_t)r * N;
+        double a = 0;
+        for (int k = 0; k < N; k++) a += row[k] * bb[k];
+        B.z[r] = a;
+    }
+}
+
+// Deterministic sum of squared residuals (mds, tgmg.in.cc:55-65): per-block
+// partial sums in a fixed order, then one block adds the partials in order.
+__device__ __forceinline__ double block_reduce(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
+    return t;
+}
+
+__global__ void k_tg_sqnorm(glevel L, double *partials) {
+    __shared__ double sh[32];
+    const long mn = (long)L.m * L.n;
+    double acc = 0;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += (long)gridDim.x * blockDim.x) {
+        const int j = (int)(k / L.m), i = (int)(k - (long)j * L.m);
+        const gst &s = L.st[L.cls[k]];
+        const double r = L.b[k] - offdiag(L, s, i, j) - s.e[4] * L.z[k];
+        acc += r * r;
+    }
+    const double t = block_reduce(acc, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+__global__ void k_tg_sum(const double *partials, int np, double *out) {
+    __shared__ double sh[32];
+    double a = 0;
+    for (int k = threadIdx.x; k < np; k += blockDim.x) a += partials[k];
+    const double t = block_reduce(a, sh);
+    if (threadIdx.x == 0) *out = t;
+}
+
+// ---------------------------------------------------------------------------
+// Host side: hierarchy sizes, Galerkin products, dense coarsest inverse.
+
+struct host_level {
+    int m, n;
+    std::vector<int> cls;
+    std::vector<gst> table;
+};
+
+// Child sizes (tgmg_base constructor, tgmg.hh:108-110) while the child has
+// more than tgmg_grid_min points (tgmg.in.cc:17-31).  A periodic line
+// shorter than 3 would alias its own neighbours; coarsening stops there
+// (the reference collapses such lines, tgmg.in.cc:738-781).
+std::vector<std::pair<int, int>> level_sizes(int m, int n, int xp, int yp) {
+    std::vector<std::pair<int, int>> out;
+    out.push_back(std::make_pair(m, n));
+    int am = (m + (xp ? 1 : 2)) >> 1, an = (n + (yp ? 1 : 2)) >> 1;
+    while ((long)am * an > kGridMin && (int)out.size() < kMaxLevels && (!xp || am >= 3) && (!yp || an >= 3)) {
+        out.push_back(std::make_pair(am, an));
+        const int nm = (am + (xp ? 1 : 2)) >> 1, nn = (an + (yp ? 1 : 2)) >> 1;
+        am = nm;
+        an = nn;
+    }
+    return out;
+}
+
+inline int wrap_line(int f, int m, int prd) {
+    if (f >= 0 && f < m) return f;
+    if (!prd) return -1;
+    return f < 0 ? f + m : f - m;
+}
+
+// Coarse offset -1..1 of coarse index c relative to C on a line of cm points.
+inline int coarse_offset(int c, int C, int cm, int prd) {
+    int o = c - C;
+    if (prd) {
+        if (o > 1) o -= cm;
+        if (o < -1) o += cm;
+    }
+    return o;
+}
+
+// Galerkin stencil at coarse point (I, J): sum over fine points k near
+// (2I, 2J) and their neighbours l of P(k, (I,J)) A(k, l) P(l, neighbour).
+gst rap_point(const host_level &F, int xp, int yp, int cm, int cn, int I, int J) {
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int dy = -1; dy <= 1; dy++) {
+        const int fy = wrap_line(2 * J + dy, F.n, yp);
+        if (fy < 0) continue;
+        const double wy = pw(fy, F.n, yp, J);
+        if (wy == 0) continue;
+        for (int dx = -1; dx <= 1; dx++) {
+            const int fx = wrap_line(2 * I + dx, F.m, xp);
+            if (fx < 0) continue;
+            const double wx = pw(fx, F.m, xp, I);
+            if (wx == 0) continue;
+            const gst &s = F.table[F.cls[(size_t)fy * F.m + fx]];
+            for (int sy = -1; sy <= 1; sy++) {
+                const int ly = wrap_line(fy + sy, F.n, yp);
+                if (ly < 0) continue;
+                for (int sx = -1; sx <= 1; sx++) {
+                    const int lx = wrap_line(fx + sx, F.m, xp);
+                    if (lx < 0) continue;
+                    const double a = s.e[(sy + 1) * 3 + sx + 1];
+                    if (a == 0) continue;
+                    int cy[2], cx[2];
+                    double wyl[2], wxl[2];
+                    const int ny = p1d(ly, F.n, yp, cy, wyl), nx = p1d(lx, F.m, xp, cx, wxl);
+                    for (int q = 0; q < ny; q++)
+                        for (int p = 0; p < nx; p++) {
+                            const int oy = coarse_offset(cy[q], J, cn, yp), ox = coarse_offset(cx[p], I, cm, xp);
+                            acc[(oy + 1) * 3 + ox + 1] += wx * wy * a * wxl[p] * wyl[q];
+                        }
+                }
+            }
+        }
+    }
+    gst out;
+    for (int k = 0; k < 9; k++) out.e[k] = acc[k];
+    out.e[9] = 1. / acc[4];
+    return out;
+}
+
+struct gst_hash {
+    size_t operator()(const gst &s) const {
+        uint64_t h = 1469598103934665603ull;
+        const unsigned char *p = (const unsigned char *)&s;
+        for (size_t k = 0; k < sizeof(gst); k++) h = (h ^ p[k]) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+struct gst_eq {
+    bool operator()(const gst &a, const gst &b) const { return std::memcmp(&a, &b, sizeof(gst)) == 0; }
+};
+
+host_level coarsen(const host_level &F, int xp, int yp, int cm, int cn) {
+    host_level C;
+    C.m = cm;
+    C.n = cn;
+    std::vector<gst> all((size_t)cm * cn);
+#pragma omp parallel for schedule(static)
+    for (int J = 0; J < cn; J++)
+        for (int I = 0; I < cm; I++) all[(size_t)J * cm + I] = rap_point(F, xp, yp, cm, cn, I, J);
+    std::unordered_map<gst, int, gst_hash, gst_eq> index;
+    C.cls.resize(all.size());
+    for (size_t k = 0; k < all.size(); k++) {
+        auto it = index.find(all[k]);
+        if (it == index.end()) {
+            it = index.emplace(all[k], (int)C.table.size()).first;
+            C.table.push_back(all[k]);
+        }
+        C.cls[k] = it->second;
+    }
+    return C;
+}
+
+// Dense inverse by Gauss-Jordan elimination with partial pivoting; empty if
+// singular.
+std::vector<double> dense_inverse(const host_level &L, int xp, int yp) {
+    const int N = L.m * L.n;
+    std::vector<double> A((size_t)N * N, 0.0), X((size_t)N * N, 0.0);
+    for (int j = 0; j < L.n; j++)
+        for (int i = 0; i < L.m; i++) {
+            const int r = j * L.m + i;
+            const gst &s = L.table[L.cls[r]];
+            for (int sy = -1; sy <= 1; sy++) {
+                const int ly = wrap_line(j + sy, L.n, yp);
+                if (ly < 0) continue;
+                for (int sx = -1; sx <= 1; sx++) {
+                    const int lx = wrap_line(i + sx, L.m, xp);
+                    if (lx < 0) continue;
+                    A[(size_t)r * N + ly * L.m + lx] += s.e[(sy + 1) * 3 + sx + 1];
+                }
+            }
+        }
+    for (int r = 0; r < N; r++) X[(size_t)r * N + r] = 1;
+    for (int c = 0; c < N; c++) {
+        int p = c;
+        for (int r = c + 1; r < N; r++)
+            if (std::fabs(A[(size_t)r * N + c]) > std::fabs(A[(size_t)p * N + c])) p = r;
+        if (A[(size_t)p * N + c] == 0) return std::vector<double>();
+        if (p != c)
+            for (int k = 0; k < N; k++) {
+                std::swap(A[(size_t)p * N + k], A[(size_t)c * N + k]);
+                std::swap(X[(size_t)p * N + k], X[(size_t)c * N + k]);
+            }
+        const double d = 1. / A[(size_t)c * N + c];
+        for (int k = 0; k < N; k++) {
+            A[(size_t)c * N + k] *= d;
+            X[(size_t)c * N + k] *= d;
+        }
+        for (int r = 0; r < N; r++) {
+            if (r == c) continue;
+            const double f = A[(size_t)r * N + c];
+            if (f == 0) continue;
+            for (int k = 0; k < N; k++) {
+                A[(size_t)r * N + k] -= f * A[(size_t)c * N + k];
+                X[(size_t)r * N + k] -= f * X[(size_t)c * N + k];
+            }
+        }
+    }
+    return X;
+}
+
+inline dim3 grid_of(int m, int n, dim3 b) { return dim3(ceil_div(m, b.x), ceil_div(n, b.y)); }
+
+}  // namespace
+}  // namespace stzg
+
+using namespace stzg;
+
+struct stzg_tgmg {
+    int device = 0;
+    int xp = 0, yp = 0;
+    double acc = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int nl = 0;
+    glevel lv[kMaxLevels];
+    std::vector<host_level> host;
+    std::vector<void *> owned;
+    double *inv = nullptr;
+    int inv_n = 0;
+    double *partials = nullptr, *dsum = nullptr, *hsum = nullptr;
+    // graph of one iteration of the last (type, omega, cycles) used
+    cudaGraphExec_t gexec = nullptr;
+    int gkey[5] = {-1, 0, 0, 0, 0};
+    double gomega = 0;
+    long gnodes = 0;
+    double last_ms = 0;
+    long last_kernels = 0;
+    long kernels = 0;
+};
+
+namespace {
+
+int g_alloc(stzg_tgmg *g, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    g->owned.push_back(*p);
+    STZG_CUDA(cudaMemsetAsync(*p, 0, bytes, g->st));
+    return STZG_OK;
+}
+
+void launch_note(stzg_tgmg *g) {
+    g->kernels++;
+    note_launch();
+}
+
+const dim3 kBlk(32, 8);
+
+void sweep(stzg_tgmg *g, const glevel &L, bool reverse, double omega) {
+    const int nc = L.cx_n * L.cy_n;
+    for (int q = 0; q < nc; q++) {
+        const int c = reverse ? nc - 1 - q : q;
+        const int cy = c / L.cx_n, cx = c % L.cx_n;
+        k_tg_color<<<grid_of((L.m + 1) / 2, (L.n + 1) / 2, kBlk), kBlk, 0, g->st>>>(L, cx, cy, omega);
+        launch_note(g);
+    }
+}
+
+void clear_z(stzg_tgmg *g, const glevel &L) {
+    cudaMemsetAsync(L.z, 0, sizeof(double) * (size_t)L.m * L.n, g->st);
+}
+
+// down_gs_iterations (tgmg.hh:273-279): clear z, then cyc sweeps (the first
+// from zero).
+void down_gs(stzg_tgmg *g, const glevel &L, int cyc) {
+    clear_z(g, L);
+    for (int c = 0; c < cyc; c++) sweep(g, L, false, 1.0);
+}
+
+// up_gs_iterations (tgmg.hh:183-187): cyc sweeps, reversed when symmetric.
+void up_gs(stzg_tgmg *g, const glevel &L, int cyc, bool sym) {
+    for (int c = 0; c < cyc; c++) sweep(g, L, sym, 1.0);
+}
+
+void restrict_to(stzg_tgmg *g, const glevel &F, const glevel &C) {
+    k_tg_residual<<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(F);
+    launch_note(g);
+    k_tg_restrict<<<grid_of(C.m, C.n, kBlk), kBlk, 0, g->st>>>(F, C);
+    launch_note(g);
+}
+
+void prolong(stzg_tgmg *g, const glevel &C, const glevel &F) {
+    k_tg_prolong<<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(C, F);
+    launch_note(g);
+}
+
+// Coarsest level: the reference's hcyc_bottom sweeps down and up
+// (tgmg.in.cc:350-352), replaced by the exact solve where it is available.
+void bottom(stzg_tgmg *g, const glevel &B, int hcyc, bool sym) {
+    if (g->inv) {
+        k_tg_bottom<<<1, 256, 0, g->st>>>(B, g->inv, g->inv_n);
+        launch_note(g);
+    } else {
+        down_gs(g, B, hcyc);
+        up_gs(g, B, hcyc, sym);
+    }
+}
+
+// v_cycle_internal (tgmg.in.cc:341-359) from level lv (>= 1), whose z has
+// had its down sweeps.
+void internal(stzg_tgmg *g, int level, int cd, int cu, int hb, bool sym) {
+    const int L = g->nl - 1;
+    for (int i = level; i < L; i++) {
+        if (i > level) down_gs(g, g->lv[i], cd);
+        restrict_to(g, g->lv[i], g->lv[i + 1]);
+    }
+    bottom(g, g->lv[L], hb, sym);
+    for (int i = L; i > level; i--) {
+        prolong(g, g->lv[i], g->lv[i - 1]);
+        up_gs(g, g->lv[i - 1], cu, sym);
+    }
+}
+
+// tgmg::v_cycle (tgmg.in.cc:313-328).
+void v_cycle(stzg_tgmg *g, int cd, int cu, int hb, bool sym) {
+    for (int c = 0; c < cd; c++) sweep(g, g->lv[0], false, 1.0);
+    if (g->nl > 1) {
+        restrict_to(g, g->lv[0], g->lv[1]);
+        if (g->nl - 1 > 1) {
+            down_gs(g, g->lv[1], cd);
+            internal(g, 1, cd, cu, hb, sym);
+        } else {
+            bottom(g, g->lv[1], hb, sym);
+        }
+        prolong(g, g->lv[1], g->lv[0]);
+    }
+    up_gs(g, g->lv[0], cu, sym);
+}
+
+// tgmg::fmg_pre (tgmg.in.cc:369-402).
+void fmg_pre(stzg_tgmg *g, int cd, int cu, int hb, bool sym) {
+    const int L = g->nl - 1;
+    for (int c = 0; c < cd; c++) sweep(g, g->lv[0], false, 1.0);
+    if (L > 0) {
+        restrict_to(g, g->lv[0], g->lv[1]);
+        for (int i = 1; i < L; i++) {
+            down_gs(g, g->lv[i], cd);
+            restrict_to(g, g->lv[i], g->lv[i + 1]);
+        }
+        bottom(g, g->lv[L], hb, sym);
+        for (int i = L; i > 1; i--) {
+            prolong(g, g->lv[i], g->lv[i - 1]);
+            up_gs(g, g->lv[i - 1], cu, sym);
+            for (int c = 0; c < cd; c++) sweep(g, g->lv[i - 1], false, 1.0);
+            internal(g, i - 1, cd, cu, hb, sym);
+        }
+        prolong(g, g->lv[1], g->lv[0]);
+    }
+    up_gs(g, g->lv[0], cu, sym);
+}
+
+// One iteration of a solver type (tgmg::iters, tgmg.hh:457-466).
+void one_iteration(stzg_tgmg *g, int type, double omega, int cd, int cu, int hb) {
+    const glevel &T = g->lv[0];
+    switch (type) {
+        case STZG_TGMG_JACOBI:
+            k_tg_jacobi<<<grid_of(T.m, T.n, kBlk), kBlk, 0, g->st>>>(T);
+            launch_note(g);
+            cudaMemcpyAsync(T.z, T.r, sizeof(double) * (size_t)T.m * T.n, cudaMemcpyDeviceToDevice, g->st);
+            break;
+        case STZG_TGMG_GS: sweep(g, T, false, 1.0); break;
+        case STZG_TGMG_SOR: sweep(g, T, false, omega); break;
+        case STZG_TGMG_FMG:
+            fmg_pre(g, cd, cu, hb, false);
+            v_cycle(g, cd, cu, hb, false);
+            break;
+        case STZG_TGMG_VCYCLE: v_cycle(g, cd, cu, hb, false); break;
+        default: v_cycle(g, cd, cu, hb, true); break;
+    }
+}
+
+int run_iterations(stzg_tgmg *g, int type, int count, double omega, int cd, int cu, int hb) {
+    if (count <= 0) return STZG_OK;
+    const int key[5] = {type, cd, cu, hb, 1};
+    if (!g->gexec || std::memcmp(key, g->gkey, sizeof(key)) != 0 || g->gomega != omega) {
+        if (g->gexec) {
+            cudaGraphExecDestroy(g->gexec);
+            g->gexec = nullptr;
+        }
+        const long k0 = g->kernels;
+        const long n0 = launch_count();
+        cudaGraph_t graph;
+        STZG_CUDA(cudaStreamBeginCapture(g->st, cudaStreamCaptureModeThreadLocal));
+        one_iteration(g, type, omega, cd, cu, hb);
+        STZG_CUDA(cudaStreamEndCapture(g->st, &graph));
+        discount_launches(launch_count() - n0);
+        g->gnodes = g->kernels - k0;
+        g->kernels = k0;
+        cudaError_t e = cudaGraphInstantiate(&g->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        std::memcpy(g->gkey, key, sizeof(key));
+        g->gomega = omega;
+    }
+    for (int c = 0; c < count; c++) {
+        STZG_CUDA(cudaGraphLaunch(g->gexec, g->st));
+        g->kernels += g->gnodes;
+        for (long k = 0; k < g->gnodes; k++) note_launch();
+    }
+    return STZG_OK;
+}
+
+// l2_error = mds / mn (tgmg.hh:146).
+int l2_error(stzg_tgmg *g, double *err) {
+    const glevel &T = g->lv[0];
+    k_tg_sqnorm<<<kRedBlocks, kRedThreads, 0, g->st>>>(T, g->partials);
+    launch_note(g);
+    k_tg_sum<<<1, 256, 0, g->st>>>(g->partials, kRedBlocks, g->dsum);
+    launch_note(g);
+    STZG_CUDA(cudaMemcpyAsync(g->hsum, g->dsum, sizeof(double), cudaMemcpyDeviceToHost, g->st));
+    STZG_CUDA(cudaStreamSynchronize(g->st));
+    *err = g->hsum[0] / ((double)T.m * T.n);
+    return STZG_OK;
+}
+
+bool valid_type(int t) { return t >= STZG_TGMG_JACOBI && t <= STZG_TGMG_SYM_VCYCLE; }
+
+struct timed {
+    stzg_tgmg *g;
+    long k0;
+    explicit timed(stzg_tgmg *g_) : g(g_), k0(g_->kernels) { cudaEventRecord(g->ev0, g->st); }
+    void done() {
+        cudaEventRecord(g->ev1, g->st);
+        cudaEventSynchronize(g->ev1);
+        float t = 0;
+        cudaEventElapsedTime(&t, g->ev0, g->ev1);
+        g->last_ms = t;
+        g->last_kernels = g->kernels - k0;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+void stzg_tgmg_predict_init(stzg_tgmg_predict *tp) {
+    if (!tp) return;
+    tp->mult = 16;
+    tp->decay = 32;
+    tp->max_thresh = 16 * 2048;
+    tp->extra_iters = 1;
+    tp->lim = 16 * 8;
+    tp->solves = 0;
+    tp->vcount = 0;
+}
+
+int stzg_poisson_fd(int m, int n, double ax, double bx, double ay, double by, double *table, int *cls,
+                    double *acc) {
+    if (m < 2 || n < 2 || !table || !cls || !acc) return fail(STZG_EINVAL, "poisson_fd needs m,n >= 2");
+    // poisson_fd::poisson_fd (poisson_fd.cc:12-16)
+    const double dx = (bx - ax) / (m - 1), dy = (by - ay) / (n - 1);
+    const double hcc = -2 / (dx * dx) - 2 / (dy * dy), hxx = 1. / (dx * dx), hyy = 1. / (dy * dy);
+    const double a = DBL_EPSILON * 1e4 * hcc;  // tgmg_accuracy(hcc, 1e4), tgmg.hh:42-45
+    *acc = a * a;
+    const double interior[9] = {0, hyy, 0, hxx, hcc, hxx, 0, hyy, 0};
+    for (int k = 0; k < 9; k++) {
+        table[k] = interior[k];
+        table[9 + k] = k == 4 ? hcc : 0;
+    }
+    // edge() (poisson_fd.hh:38): i==0 || i==m-1 || first or last row
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) cls[(size_t)j * m + i] = (i == 0 || i == m - 1 || j == 0 || j == n - 1) ? 1 : 0;
+    return STZG_OK;
+}
+
+int stzg_tgmg_create(int m, int n, int x_prd, int y_prd, const double *table, int ntable, const int *cls,
+                     double acc, int device, stzg_tgmg **out) {
+    if (!out) return fail(STZG_EINVAL, "null handle pointer");
+    *out = nullptr;
+    if (m < 1 || n < 1 || !table || ntable < 1 || !cls) return fail(STZG_EINVAL, "bad grid or operator");
+    if ((x_prd && m < 3) || (y_prd && n < 3)) return fail(STZG_EINVAL, "a periodic direction needs >= 3 points");
+    if (!(acc >= 0)) return fail(STZG_EINVAL, "acc must be >= 0");
+    const size_t mn = (size_t)m * n;
+    for (size_t k = 0; k < mn; k++)
+        if (cls[k] < 0 || cls[k] >= ntable) return fail(STZG_EINVAL, "stencil index out of range");
+    for (int c = 0; c < ntable; c++)
+        if (table[9 * c + 4] == 0) return fail(STZG_EINVAL, "zero diagonal entry");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(STZG_ENODEV, "no CUDA device");
+    if (device < 0 || device >= ndev) return fail(STZG_EINVAL, "device ordinal out of range");
+    STZG_CUDA(cudaSetDevice(device));
+    stzg_tgmg *g = new stzg_tgmg;
+    g->device = device;
+    g->xp = x_prd ? 1 : 0;
+    g->yp = y_prd ? 1 : 0;
+    g->acc = acc;
+    auto bail = [&](int st) {
+        stzg_tgmg_destroy(g);
+        return st;
+    };
+    if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess)
+        return bail(fail(STZG_ECUDA, "stream/event creation failed"));
+    // host hierarchy: the problem's operator, then Galerkin products
+    host_level top;
+    top.m = m;
+    top.n = n;
+    top.cls.assign(cls, cls + mn);
+    top.table.resize(ntable);
+    for (int c = 0; c < ntable; c++) {
+        for (int k = 0; k < 9; k++) top.table[c].e[k] = table[9 * c + k];
+        top.table[c].e[9] = 1. / table[9 * c + 4];
+    }
+    g->host.push_back(top);
+    const std::vector<std::pair<int, int>> sizes = level_sizes(m, n, g->xp, g->yp);
+    for (size_t l = 1; l < sizes.size(); l++)
+        g->host.push_back(coarsen(g->host[l - 1], g->xp, g->yp, sizes[l].first, sizes[l].second));
+    g->nl = (int)g->host.size();
+    for (int l = 0; l < g->nl; l++) {
+        const host_level &H = g->host[l];
+        glevel &L = g->lv[l];
+        L.m = H.m;
+        L.n = H.n;
+        L.xp = g->xp;
+        L.yp = g->yp;
+        L.cx_n = (g->xp && (H.m & 1)) ? 3 : 2;
+        L.cy_n = (g->yp && (H.n & 1)) ? 3 : 2;
+        const size_t pts = (size_t)H.m * H.n;
+        void *p;
+        int st;
+        if ((st = g_alloc(g, &p, pts * sizeof(double))) != STZG_OK) return bail(st);
+        L.z = (double *)p;
+        if ((st = g_alloc(g, &p, pts * sizeof(double))) != STZG_OK) return bail(st);
+        L.b = (double *)p;
+        if ((st = g_alloc(g, &p, pts * sizeof(double))) != STZG_OK) return bail(st);
+        L.r = (double *)p;
+        if ((st = g_alloc(g, &p, pts * sizeof(int))) != STZG_OK) return bail(st);
+        L.cls = (const int *)p;
+        if (cudaMemcpy(p, H.cls.data(), pts * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(STZG_ECUDA, "upload of stencil indices failed"));
+        if ((st = g_alloc(g, &p, H.table.size() * sizeof(gst))) != STZG_OK) return bail(st);
+        L.st = (const gst *)p;
+        if (cudaMemcpy(p, H.table.data(), H.table.size() * sizeof(gst), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(STZG_ECUDA, "upload of stencils failed"));
+    }
+    const host_level &B = g->host.back();
+    if (g->nl > 1 && (long)B.m * B.n <= kBottomDirect) {
+        std::vector<double> inv = dense_inverse(B, g->xp, g->yp);
+        if (!inv.empty()) {
+            void *p;
+            int st;
+            if ((st = g_alloc(g, &p, inv.size() * sizeof(double))) != STZG_OK) return bail(st);
+            g->inv = (double *)p;
+            g->inv_n = B.m * B.n;
+            if (cudaMemcpy(p, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+                return bail(fail(STZG_ECUDA, "upload of the coarsest inverse failed"));
+        }
+    }
+    {
+        void *p;
+        int st;
+        if ((st = g_alloc(g, &p, kRedBlocks * sizeof(double))) != STZG_OK) return bail(st);
+        g->partials = (double *)p;
+        if ((st = g_alloc(g, &p, sizeof(double))) != STZG_OK) return bail(st);
+        g->dsum = (double *)p;
+        if (cudaMallocHost(&p, sizeof(double)) != cudaSuccess) return bail(fail(STZG_ENOMEM, "pinned allocation"));
+        g->hsum = (double *)p;
+    }
+    if (cudaStreamSynchronize(g->st) != cudaSuccess) return bail(fail(STZG_ECUDA, "setup failed"));
+    *out = g;
+    return STZG_OK;
+}
+
+int stzg_tgmg_destroy(stzg_tgmg *g) {
+    if (!g) return STZG_OK;
+    cudaSetDevice(g->device);
+    if (g->st) cudaStreamSynchronize(g->st);
+    if (g->gexec) cudaGraphExecDestroy(g->gexec);
+    for (void *p : g->owned) cudaFree(p);
+    if (g->hsum) cudaFreeHost(g->hsum);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->st) cudaStreamDestroy(g->st);
+    delete g;
+    return STZG_OK;
+}
+
+static int copy_top(stzg_tgmg *g, double *dev, const double *src, double *dst) {
+    if (!g || (!src && !dst)) return fail(STZG_EINVAL, "null argument");
+    STZG_CUDA(cudaSetDevice(g->device));
+    const size_t bytes = sizeof(double) * (size_t)g->lv[0].m * g->lv[0].n;
+    if (src) STZG_CUDA(cudaMemcpyAsync(dev, src, bytes, cudaMemcpyHostToDevice, g->st));
+    else STZG_CUDA(cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, g->st));
+    STZG_CUDA(cudaStreamSynchronize(g->st));
+    return STZG_OK;
+}
+
+int stzg_tgmg_set_b(stzg_tgmg *g, const double *b) { return copy_top(g, g ? g->lv[0].b : nullptr, b, nullptr); }
+int stzg_tgmg_get_b(stzg_tgmg *g, double *b) { return copy_top(g, g ? g->lv[0].b : nullptr, nullptr, b); }
+int stzg_tgmg_set_z(stzg_tgmg *g, const double *z) { return copy_top(g, g ? g->lv[0].z : nullptr, z, nullptr); }
+int stzg_tgmg_get_z(stzg_tgmg *g, double *z) { return copy_top(g, g ? g->lv[0].z : nullptr, nullptr, z); }
+
+int stzg_tgmg_clear_z(stzg_tgmg *g) {
+    if (!g) return fail(STZG_EINVAL, "null handle");
+    STZG_CUDA(cudaSetDevice(g->device));
+    clear_z(g, g->lv[0]);
+    STZG_CUDA(cudaStreamSynchronize(g->st));
+    return STZG_OK;
+}
+
+int stzg_tgmg_l2_error(stzg_tgmg *g, double *err) {
+    if (!g || !err) return fail(STZG_EINVAL, "null argument");
+    STZG_CUDA(cudaSetDevice(g->device));
+    return l2_error(g, err);
+}
+
+int stzg_tgmg_iterate(stzg_tgmg *g, int type, int count, double omega, int cyc_down, int cyc_up, int hcyc_bottom) {
+    if (!g || !valid_type(type) || count < 0 || cyc_down < 0 || cyc_up < 0 || hcyc_bottom < 0)
+        return fail(STZG_EINVAL, "bad iterate arguments");
+    STZG_CUDA(cudaSetDevice(g->device));
+    timed t(g);
+    STZG_CHECK(run_iterations(g, type, count, omega, cyc_down, cyc_up, hcyc_bottom));
+    t.done();
+    STZG_CUDA(cudaGetLastError());
+    return STZG_OK;
+}
+
+int stzg_tgmg_solve(stzg_tgmg *g, int type, stzg_tgmg_predict *tp, double omega, int cyc_down, int cyc_up,
+                    int hcyc_bottom, int *iters, double *l2) {
+    if (!g || !tp || !valid_type(type) || tp->mult < 1 || cyc_down < 0 || cyc_up < 0 || hcyc_bottom < 0)
+        return fail(STZG_EINVAL, "bad solve arguments");
+    STZG_CUDA(cudaSetDevice(g->device));
+    timed t(g);
+    // tgmg::solve(type, tgmg_predict&, ...), tgmg.in.cc:266-301
+    int nit = tp->lim / tp->mult;
+    STZG_CHECK(run_iterations(g, type, nit, omega, cyc_down, cyc_up, hcyc_bottom));
+    double acc;
+    STZG_CHECK(l2_error(g, &acc));
+    if (acc < g->acc) {
+        if (tp->lim > 0) tp->lim -= 1 + tp->lim / tp->decay;
+    } else {
+        int k = 0;
+        do {
+            tp->lim += ++k * tp->mult;
+            if (tp->lim > tp->max_thresh) {
+                t.done();
+                if (l2) *l2 = acc;
+                return fail(STZG_ENOTCONV, "tgmg did not converge");
+            }
+            nit += k;
+            STZG_CHECK(run_iterations(g, type, k, omega, cyc_down, cyc_up, hcyc_bottom));
+            STZG_CHECK(l2_error(g, &acc));
+        } while (acc >= g->acc && !std::isnan(acc));
+    }
+    tp->solves++;
+    tp->vcount += nit;
+    STZG_CHECK(run_iterations(g, type, tp->extra_iters, omega, cyc_down, cyc_up, hcyc_bottom));
+    t.done();
+    if (iters) *iters = nit;
+    if (l2) *l2 = acc;
+    if (std::isnan(acc)) return fail(STZG_ENAN, "NaN residual");
+    return STZG_OK;
+}
+
+int stzg_tgmg_solve_fixed(stzg_tgmg *g, int type, int per_loop, int max_loops, double omega, int cyc_down,
+                          int cyc_up, int hcyc_bottom, int *iters, double *l2) {
+    if (!g || !valid_type(type) || per_loop < 1 || max_loops < 1 || cyc_down < 0 || cyc_up < 0 ||
+        hcyc_bottom < 0)
+        return fail(STZG_EINVAL, "bad solve arguments");
+    STZG_CUDA(cudaSetDevice(g->device));
+    timed t(g);
+    // tgmg::solve(type, per_loop, max_loops, ...), tgmg.in.cc:182-197
+    double acc = 0;
+    int nloop = 0;
+    do {
+        if (++nloop == max_loops) {
+            t.done();
+            if (iters) *iters = nloop * per_loop;
+            if (l2) *l2 = acc;
+            return fail(STZG_ENOTCONV, "tgmg did not converge");
+        }
+        STZG_CHECK(run_iterations(g, type, per_loop, omega, cyc_down, cyc_up, hcyc_bottom));
+        STZG_CHECK(l2_error(g, &acc));
+    } while (acc > g->acc && !std::isnan(acc));
+    t.done();
+    if (iters) *iters = nloop * per_loop;
+    if (l2) *l2 = acc;
+    if (std::isnan(acc)) return fail(STZG_ENAN, "NaN residual");
+    return STZG_OK;
+}
+
+int stzg_tgmg_levels(stzg_tgmg *g, int *nlevels, int *dims) {
+    if (!g || !nlevels) return fail(STZG_EINVAL, "null argument");
+    *nlevels = g->nl;
+    if (dims)
+        for (int l = 0; l < g->nl; l++) {
+            dims[2 * l] = g->host[l].m;
+            dims[2 * l + 1] = g->host[l].n;
+        }
+    return STZG_OK;
+}
+
+int stzg_tgmg_stencil(stzg_tgmg *g, int level, double *out) {
+    if (!g || !out || level < 1 || level >= g->nl) return fail(STZG_EINVAL, "bad level");
+    const host_level &H = g->host[level];
+    const size_t pts = (size_t)H.m * H.n;
+    for (size_t k = 0; k < pts; k++) std::memcpy(out + 10 * k, H.table[H.cls[k]].e, sizeof(gst));
+    return STZG_OK;
+}
+
+int stzg_tgmg_last_timing(stzg_tgmg *g, double *ms, long *kernels) {
+    if (!g) return fail(STZG_EINVAL, "null handle");
+    if (ms) *ms = g->last_ms;
+    if (kernels) *kernels = g->last_kernels;
+    return STZG_OK;
+}
+
+}  // extern "C"

@@ -22,10 +22,11 @@ def pytest_configure(config):
 
 def golden_names(kind="quasistatic"):
     """Fixture names of one kind: "quasistatic" (step_forward_quasistatic),
-    "direct" (the explicit step_forward) or "frames" (output and
-    diagnostics of a quasi-static state)."""
+    "direct" (the explicit step_forward), "frames" (output and
+    diagnostics of a quasi-static state) or "tgmg" (the general multigrid on
+    poisson_fd)."""
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-    prefix = {"direct": "direct_", "frames": "frames_"}
+    prefix = {"direct": "direct_", "frames": "frames_", "tgmg": "tgmg_"}
     if kind in prefix:
         return [n for n in names if n.startswith(prefix[kind])]
     return [n for n in names if not any(n.startswith(p) for p in prefix.values())]
@@ -55,3 +56,14 @@ def golden_direct(request):
 @pytest.fixture(params=golden_names("frames"))
 def golden_frames(request):
     return (request.param,) + load_golden(request.param)
+
+
+def load_tgmg_golden(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(d["meta"]))
+    return meta, {k: d[k] for k in d.files if k != "meta"}
+
+
+@pytest.fixture(params=golden_names("tgmg"))
+def golden_tgmg(request):
+    return (request.param,) + load_tgmg_golden(request.param)

@@ -13,8 +13,8 @@ from stz_gb300.params import simple_shear
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_symbols():
-    txt = open(os.path.join(ROOT, "include", "stzg.h")).read()
+def header_symbols(header="stzg.h"):
+    txt = open(os.path.join(ROOT, "include", header)).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     return sorted(set(re.findall(r"\b(stzg_\w+)\s*\(", txt)))
 
@@ -32,6 +32,42 @@ def test_exports_every_declared_symbol(lib):
     for name in names:
         assert hasattr(lib, name), name
     assert sorted(_lib.EXPORTS) == names
+
+
+def test_exports_every_general_multigrid_symbol(lib):
+    from stz_gb300 import tgmg
+    names = header_symbols("stzg_tgmg.h")
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+    assert sorted(tgmg.EXPORTS) == names
+    tgmg.load()
+
+
+def test_general_multigrid_without_gpu_returns_status(lib):
+    import ctypes
+    from stz_gb300 import tgmg
+    tgmg.load()
+    P = ctypes.POINTER(ctypes.c_double)
+    IP = ctypes.POINTER(ctypes.c_int)
+    table = np.zeros(18)
+    cls = np.zeros(9 * 7, dtype=np.int32)
+    acc = ctypes.c_double()
+    assert lib.stzg_poisson_fd(9, 7, -1.0, 1.0, -1.0, 1.0, table.ctypes.data_as(P), cls.ctypes.data_as(IP),
+                               ctypes.byref(acc)) == 0
+    from oracle import tgmg_oracle
+    t2, c2, a2 = tgmg_oracle.poisson_fd(9, 7, -1.0, 1.0, -1.0, 1.0)
+    assert np.array_equal(table.reshape(2, 9), t2) and np.array_equal(cls.reshape(7, 9), c2) and acc.value == a2
+    tp = tgmg.Predict()
+    assert (tp.lim, tp.mult, tp.decay, tp.max_thresh, tp.extra_iters) == (128, 16, 32, 16 * 2048, 1)
+    h = ctypes.c_void_p()
+    st = lib.stzg_tgmg_create(9, 7, 0, 0, table.ctypes.data_as(P), 2, cls.ctypes.data_as(IP), acc.value, 0,
+                              ctypes.byref(h))
+    if not _has_gpu():
+        assert st == 7 and not h.value
+    else:
+        assert st == 0
+        lib.stzg_tgmg_destroy(h)
 
 
 def test_status_strings(lib):

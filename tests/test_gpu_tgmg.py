@@ -1,0 +1,221 @@
+"""Parity of the general GPU multigrid (include/stzg_tgmg.h) with the
+reference's tgmg<poisson_fd,double,double> (golden fixtures) and with the CPU
+restatement of its operator algebra (oracle/tgmg_oracle.py): hierarchy sizes,
+Galerkin stencils, converged solutions of every solver type, periodic
+variants, the predictor's failure path and argument errors."""
+import numpy as np
+import pytest
+
+from oracle import tgmg_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _tg():
+    from stz_gb300 import tgmg
+    return tgmg
+
+
+def _pfd(meta):
+    tg = _tg()
+    q = tg.PoissonFD(meta["m"], meta["n"], meta["ax"], meta["bx"], meta["ay"], meta["by"])
+    return q
+
+
+def test_hierarchy_and_stencils_match_reference(golden_tgmg):
+    name, meta, arr = golden_tgmg
+    tg = _tg()
+    q = _pfd(meta)
+    assert q.acc == meta["acc"]
+    g = tg.Tgmg(q)
+    assert [list(s) for s in g.levels()] == meta["levels"]
+    for l in range(1, len(meta["levels"])):
+        key = "stencil%d" % l
+        if key not in arr:
+            continue
+        mine, ref = g.stencil(l), arr[key]
+        scale = np.abs(ref[..., :9]).max()
+        assert np.abs(mine[..., :9] - ref[..., :9]).max() <= 1e-15 * scale, (name, l)
+    g.close()
+
+
+def test_vcycle_solve_matches_reference(golden_tgmg):
+    """solve_v_cycle(tgmg_predict&) from z = 0 on the reference's source:
+    converged under acc, and the solution agrees with the reference's and with
+    the exact discrete solution."""
+    name, meta, arr = golden_tgmg
+    tg = _tg()
+    q = _pfd(meta)
+    q.b[...] = arr["b"]
+    g = tg.Tgmg(q)
+    tp = tg.Predict()
+    assert g.solve_v_cycle(tp)
+    assert g.l2_error() < q.acc
+    table, cls, acc = O.poisson_fd(meta["m"], meta["n"], meta["ax"], meta["bx"], meta["ay"], meta["by"])
+    zx = O.solve(O.operator(meta["m"], meta["n"], 0, 0, table, cls), arr["b"])
+    scale = np.abs(zx).max()
+    assert np.abs(q.z - zx).max() <= 1e-9 * scale
+    assert np.abs(q.z - arr["z"]).max() <= 1e-9 * scale
+    # the GPU's four-colour V-cycle needs about as many cycles as the
+    # reference's zebra ordering
+    assert g.iterations <= meta["vcycles"] + 2
+    g.close()
+
+
+def test_vcycle_contraction_from_zero(golden_tgmg):
+    name, meta, arr = golden_tgmg
+    tg = _tg()
+    q = _pfd(meta)
+    q.b[...] = arr["b"]
+    g = tg.Tgmg(q)
+    hist = []
+    for _ in range(6):
+        g.v_cycle()
+        hist.append(g.l2_error())
+    ref = meta["l2_history_from_zero"]
+    # l2_error is squared: the reference contracts it by 0.003-0.015 a cycle
+    for k in range(1, 4):
+        assert hist[k] <= 0.05 * hist[k - 1] or hist[k] < q.acc
+        assert hist[k] <= 10 * ref[k] or hist[k] < q.acc
+    g.close()
+
+
+@pytest.mark.parametrize("kind", ["fmg", "sym", "fixed_v", "fixed_fmg"])
+def test_other_multigrid_solvers(kind):
+    tg = _tg()
+    q = tg.PoissonFD(40, 30, -4.0, 4.0, -3.0, 3.0)
+    q.gaussian_source_term(0.3, -0.2, 0.8, 1.0)
+    b = q.b.copy()
+    g = tg.Tgmg(q)
+    tp = tg.Predict()
+    ok = {"fmg": lambda: g.solve_full_multigrid(tp), "sym": lambda: g.solve_sym_v_cycle(tp),
+          "fixed_v": lambda: g.solve_v_cycle(), "fixed_fmg": lambda: g.solve_full_multigrid()}[kind]()
+    assert ok and g.l2_error() < q.acc
+    zx = O.solve(O.operator(40, 30, 0, 0, q.table, q.cls), b)
+    assert np.abs(q.z - zx).max() <= 1e-9 * np.abs(zx).max()
+    g.close()
+
+
+@pytest.mark.parametrize("kind", ["jacobi", "gs", "sor"])
+def test_relaxation_solvers(kind):
+    tg = _tg()
+    q = tg.PoissonFD(9, 8, -1.0, 1.0, -1.0, 1.0)
+    q.gaussian_source_term(0.0, 0.0, 0.5, 1.0)
+    b = q.b.copy()
+    g = tg.Tgmg(q)
+    ok = {"jacobi": lambda: g.solve_jacobi(), "gs": lambda: g.solve_gauss_seidel(),
+          "sor": lambda: g.solve_sor(1.5)}[kind]()
+    assert ok and g.l2_error() <= q.acc
+    zx = O.solve(O.operator(9, 8, 0, 0, q.table, q.cls), b)
+    assert np.abs(q.z - zx).max() <= 1e-8 * np.abs(zx).max()
+    g.close()
+
+
+def _helmholtz(m, n, xp, yp, rows_vary=False, seed=0):
+    """A 9-point operator with a shifted diagonal (nonsingular on periodic
+    grids), optionally with per-row coefficients and corner entries."""
+    rng = np.random.default_rng(seed)
+    if rows_vary:
+        table = []
+        for j in range(n):
+            a = 1.0 + 0.5 * rng.random()
+            c = 0.1 * rng.random()
+            table.append([c, a, c, 1.0, -(2 * a + 2 + 4 * c) - 0.3, 1.0, c, a, c])
+        table = np.array(table)
+        cls = np.repeat(np.arange(n, dtype=np.int32)[:, None], m, axis=1)
+    else:
+        table = np.array([[0, 1.0, 0, 1.0, -4.3, 1.0, 0, 1.0, 0]])
+        cls = np.zeros((n, m), dtype=np.int32)
+    return table, cls
+
+
+@pytest.mark.parametrize("m,n,xp,yp,vary", [(32, 24, 1, 0, False), (33, 25, 1, 0, False), (24, 32, 0, 1, False),
+                                            (27, 21, 1, 1, False), (40, 36, 1, 1, True), (31, 17, 0, 0, True)])
+def test_periodic_and_variable_operators(m, n, xp, yp, vary):
+    tg = _tg()
+    table, cls = _helmholtz(m, n, xp, yp, vary, seed=m * n)
+    ops, sizes = O.hierarchy(m, n, xp, yp, table, cls)
+    q = tg.Problem(m, n, table, cls, 1e-26, x_prd=xp, y_prd=yp)
+    rng = np.random.default_rng(1)
+    q.b[...] = rng.standard_normal((n, m))
+    b = q.b.copy()
+    g = tg.Tgmg(q)
+    assert g.levels() == sizes
+    for l in range(1, len(sizes)):
+        mine = g.stencil(l)
+        ref = O.stencils(ops[l], sizes[l][0], sizes[l][1], xp, yp)
+        assert np.abs(mine[..., :9] - ref[..., :9]).max() <= 1e-14 * np.abs(ref[..., :9]).max(), l
+    tp = tg.Predict()
+    assert g.solve_v_cycle(tp)
+    zx = O.solve(ops[0], b)
+    assert np.abs(q.z - zx).max() <= 1e-10 * np.abs(zx).max()
+    g.close()
+
+
+def test_predictor_threshold_returns_false():
+    """The reference returns false once lim exceeds max_thresh; so does the
+    mirror, with a status and no fault."""
+    tg = _tg()
+    q = tg.PoissonFD(33, 33, -8.0, 8.0, -8.0, 8.0)
+    q.gaussian_source_term(0, 0, 1, 1)
+    q.acc = 0.0  # unreachable
+    g = tg.Tgmg(q)
+    tp = tg.Predict()
+    tp.max_thresh = tp.lim + 3 * tp.mult
+    assert g.solve_v_cycle(tp) is False
+    g.close()
+
+
+def test_bad_arguments_are_statuses():
+    import ctypes
+    tg = _tg()
+    lib = tg.load()
+    h = ctypes.c_void_p()
+    table = np.array([0, 1, 0, 1, -4, 1, 0, 1, 0], dtype=np.float64)
+    cls = np.zeros(4, dtype=np.int32)
+    P = ctypes.POINTER(ctypes.c_double)
+    IP = ctypes.POINTER(ctypes.c_int)
+    # periodic line of 2 points
+    assert lib.stzg_tgmg_create(2, 2, 1, 0, table.ctypes.data_as(P), 1, cls.ctypes.data_as(IP), 0.0, 0,
+                                ctypes.byref(h)) == 1
+    cls[1] = 3  # index out of range
+    assert lib.stzg_tgmg_create(2, 2, 0, 0, table.ctypes.data_as(P), 1, cls.ctypes.data_as(IP), 0.0, 0,
+                                ctypes.byref(h)) == 1
+    assert not h.value
+
+
+def test_reports_device_time_and_kernels():
+    tg = _tg()
+    q = tg.PoissonFD(129, 129, -8.0, 8.0, -8.0, 8.0)
+    q.gaussian_source_term(1, 1, 1, 1)
+    g = tg.Tgmg(q)
+    g.v_cycle()
+    ms, k = g.last_timing()
+    assert ms > 0 and k > 10
+    g.close()
+
+
+def test_cpp_dropin_header(tmp_path):
+    """include/stzg_tgmg.hh with a problem class of the reference's concept,
+    compiled into a small driver, reproduces the reference's solution."""
+    import json
+    import os
+    import subprocess
+    from conftest import GOLDEN
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = os.path.join(root, "stz_gb300", "_build")
+    exe = tmp_path / "tgmg_main"
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", os.path.join(root, "include"),
+                           os.path.join(root, "tests", "cpp", "tgmg_main.cc"), "-o", str(exe), "-L", lib, "-lstzg",
+                           f"-Wl,-rpath,{lib}"])
+    d = np.load(os.path.join(GOLDEN, "tgmg_pfd65x49.npz"))
+    meta = json.loads(str(d["meta"]))
+    bfile, zfile = tmp_path / "b.bin", tmp_path / "z.bin"
+    d["b"].astype(np.float64).tofile(bfile)
+    r = subprocess.run([str(exe), str(meta["m"]), str(meta["n"]), repr(meta["ax"]), repr(meta["bx"]),
+                        repr(meta["ay"]), repr(meta["by"]), str(bfile), str(zfile)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    z = np.fromfile(zfile).reshape(meta["n"], meta["m"])
+    assert np.abs(z - d["z"]).max() <= 1e-9 * np.abs(d["z"]).max()
+    assert "levels %d" % len(meta["levels"]) in r.stdout
