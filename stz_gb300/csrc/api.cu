@@ -291,16 +291,17 @@ int do_projection(stzg_sim *s, double dt, bool fresh_combinations) {
 }
 
 int do_advection(stzg_sim *s, double dt) {
-    advection(s->sc, s->F, s->cur, dt, s->bv_state, s->st);
+    advection(s->sc, *s->maps, s->F, s->cur, dt, s->bv_state, s->st);
     s->cur ^= 1;
     return STZG_OK;
 }
 
 int check_flags(stzg_sim *s) {
-    int h[2];
+    int h[4];
     STZG_CUDA(cudaMemcpyAsync(h, s->F.flags, sizeof(h), cudaMemcpyDeviceToHost, s->st));
     STZG_CUDA(cudaStreamSynchronize(s->st));
     if (h[1] > s->acc.substeps_max) s->acc.substeps_max = h[1];
+    if (h[3]) return fail(STZG_ECUDA, "an advection tile copy did not complete in time");
     if (h[0]) return fail(STZG_ESUBSTEP, "plastic sub-stepping reached its iteration cap");
     return STZG_OK;
 }
@@ -378,6 +379,8 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if ((st = dev_alloc(s, (void **)&s->F.flags, 4 * sizeof(int))) != STZG_OK) return bail(st);
     for (int k = 0; k < 4; k++)
         if ((st = dev_alloc(s, (void **)&s->F.pre[k], nc * sizeof(double))) != STZG_OK) return bail(st);
+    s->maps = new field_maps;
+    if ((st = make_field_maps(s->sc, s->F, s->maps)) != STZG_OK) return bail(st);
     if (o.extrapolate)
         if ((st = dev_alloc(s, (void **)&s->vel_prev, nn * sizeof(double2))) != STZG_OK) return bail(st);
     if (o.extrapolate >= 2)
@@ -412,6 +415,7 @@ int stzg_destroy(stzg_sim *s) {
     }
     if (s->cev_ready) cudaEventDestroy(s->cev_ready);
     for (void *p : s->owned) cudaFree(p);
+    delete s->maps;
     s->h64.release();
     s->h32.release();
     if (s->hnorm) cudaFreeHost(s->hnorm);
@@ -772,7 +776,7 @@ int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {
         return fail(STZG_EINVAL, "FP32 kernels need a mixed-precision handle");
     auto one = [&]() -> int {
         switch (kernel) {
-            case 0: advection(s->sc, s->F, s->cur, dt, s->bv_state, s->st); break;
+            case 0: advection(s->sc, *s->maps, s->F, s->cur, dt, s->bv_state, s->st); break;
             case 1: top_sweep<double>(s->h64, s->st); break;
             case 2: top_sweep<float>(s->h32, s->st); break;
             case 3: vcycle<double>(s->h64, s->st, 10, 1); break;

@@ -158,7 +158,7 @@ int add_instance(stzg_batch *b, cudaGraph_t root, int k, double dt, int nsteps, 
     STZG_CUDA(cudaStreamBeginCaptureToGraph(s->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     k_step_begin<<<1, 32, 0, s->st>>>(clk, dt, s->P.u_bdry);
     note_launch();
-    advection(sc, s->F, 0, dt, 0.0, s->st);
+    advection(sc, *s->maps, s->F, 0, dt, 0.0, s->st);
     projection_source(sc, s->F, 0, dt, 0.0, s->st);
     if (s->O.extrapolate) extrapolate_guess(s->F.vel, s->vel_prev, count, s->st);
     if (mixed) {

@@ -18,6 +18,7 @@ struct stzg_sim {
     cudaStream_t st = nullptr;
     stzg::step_consts sc;
     stzg::fields_dev F;
+    stzg::field_maps *maps = nullptr;  // TMA descriptors of F's advected fields
     int cur = 0;
     std::vector<void *> owned;
     // multigrid

@@ -102,15 +102,9 @@ template <int NF> struct eno_tile {
 };
 typedef eno_tile<F_COUNT> adv_tile;
 
-// Fills the tile's first and second differences of NF fields over cell rows
-// j0..j0+ATY-1 (x) and rows j0-2..j0+ATY+1 (y).  get(f, row, col) reads field
-// f at row -1..n and storage column col; rows below low(f) (-1 for the stored
-// fields, 0 for the node velocity) and above n hold no value, and the
-// differences that would need them are never used.  Field xf (the reference
-// map X) is unwrapped across the periodic seam.  Ends with __syncthreads.
-template <int NF, typename Get, typename Low>
-__device__ __forceinline__ void fill_eno_tile(eno_tile<NF> &T, int i0, int j0, int m, int n, double lx, int xf,
-                                              Get get, Low low) {
+// Storage column and X offset of every tile column (unwrapped column
+// i0 + t - 2 for t = 0..ACOLS-1); threads 0..ACOLS-1 write them.
+template <int NF> __device__ __forceinline__ void tile_columns(eno_tile<NF> &T, int i0, int m, double lx) {
     const int tid = threadIdx.y * ATX + threadIdx.x;
     if (tid < ACOLS) {
         const int u = i0 + tid - 2;  // unwrapped column
@@ -119,13 +113,25 @@ __device__ __forceinline__ void fill_eno_tile(eno_tile<NF> &T, int i0, int j0, i
         T.col[tid] = w;
         T.xo[tid] = u < 0 ? -lx : (u >= m ? lx : 0.0);
     }
-    __syncthreads();
+}
+
+// Fills the tile's first and second differences of NF fields over cell rows
+// j0..j0+ATY-1 (x) and rows j0-2..j0+ATY+1 (y), after tile_columns and a
+// barrier.  get(f, row, t) reads field f at row -1..n and tile column t;
+// rows below low(f) (-1 for the stored fields, 0 for the node velocity) and
+// above n hold no value, and the differences that would need them are never
+// used.  Field xf (the reference map X) is unwrapped across the periodic
+// seam.  Ends with __syncthreads.
+template <int NF, typename Get, typename Low>
+__device__ __forceinline__ void tile_differences(eno_tile<NF> &T, int i0, int j0, int m, int n, int xf, Get get,
+                                                 Low low) {
+    const int tid = threadIdx.y * ATX + threadIdx.x;
     for (int k = tid; k < NF * ATY * ADXW; k += ATX * ATY) {
         const int f = k / (ATY * ADXW), rem = k - f * (ATY * ADXW), r = rem / ADXW, cc = rem - r * ADXW;
         const int jj = j0 + r;
         double d = 0;
         if (jj < n) {
-            double hi = get(f, jj, T.col[cc + 1]), lo = get(f, jj, T.col[cc]);
+            double hi = get(f, jj, cc + 1), lo = get(f, jj, cc);
             if (f == xf) {
                 if (T.xo[cc + 1] != 0) hi += T.xo[cc + 1];
                 if (T.xo[cc] != 0) lo += T.xo[cc];
@@ -138,7 +144,7 @@ __device__ __forceinline__ void fill_eno_tile(eno_tile<NF> &T, int i0, int j0, i
         const int f = k / (ADYH * ATX), rem = k - f * (ADYH * ATX), r = rem / ATX, cc = rem - r * ATX;
         const int jj = j0 + r - 2, ii = i0 + cc;
         double d = 0;
-        if (jj >= low(f) && jj + 1 <= n && ii < m) d = get(f, jj + 1, ii) - get(f, jj, ii);
+        if (jj >= low(f) && jj + 1 <= n && ii < m) d = get(f, jj + 1, cc + 2) - get(f, jj, cc + 2);
         T.dy[f][r][cc] = d;
     }
     __syncthreads();
@@ -180,6 +186,53 @@ __device__ __forceinline__ double tile_eno_y(const eno_tile<NF> &T, int f, int t
     return fma(-2.0, d, mag_gt(s0, s1) ? s1 : s0);
 }
 
+// ---- TMA staging of the field tiles -----------------------------------------
+// Rows of the staged tile: cell rows j0-2..j0+ATY+1 (storage rows j0-1..).
+constexpr int AROWS = ATY + 4;
+constexpr unsigned kTileBytes = F_COUNT * AROWS * ACOLS * sizeof(double);
+// Iterations of the bounded wait on the tile copies (each try_wait itself
+// suspends for a while); past it the block flags F.flags[3].
+constexpr int kTmaWaitIters = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 2D tiled TMA load of box (x, y) of `map` into dst, completing on bar.
+// x (the column) must be even for FP64 (16-byte rule); it and y may lie
+// outside the tensor, whose missing elements arrive as zeros.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_addr(dst)), "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Bounded wait for phase 0 of bar; false when it ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar) {
+    for (int it = 0; it < kTmaWaitIters; it++)
+        if (mbar_try_wait(bar, 0)) return true;
+    return false;
+}
+
 // Per-launch constants of the step that depend on dt (computed on the host
 // with the same operations the per-thread code used).
 struct advect_consts {
@@ -187,20 +240,50 @@ struct advect_consts {
     double xf, yf;  // 1/(2 dt dx), 1/(2 dt dy) of projection_step
 };
 
-__global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_consts a, fields_dev F, int cur,
-                                                      double dt, double bv, int emit_source) {
-    extern __shared__ __align__(16) unsigned char adv_smem[];
-    adv_tile &T = *reinterpret_cast<adv_tile *>(adv_smem);
+struct adv_smem {
+    double tile[F_COUNT][AROWS][ACOLS];  // staged fields, first: 128-byte aligned
+    adv_tile T;
+    uint64_t bar;
+};
+
+__global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_consts a, const __grid_constant__ field_maps maps,
+                                                      fields_dev F, int cur, double dt, double bv, int emit_source) {
+    extern __shared__ __align__(128) unsigned char adv_raw[];
+    adv_smem &Sm = *reinterpret_cast<adv_smem *>(adv_raw + ((128 - (smem_addr(adv_raw) & 127)) & 127));
+    adv_tile &T = Sm.T;
     const int m = c.m, n = c.n;
-    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * ATX + tx;
     const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY;
     const int i = i0 + tx, j = j0 + ty;
     if (c.clock) cur = (int)c.clock[CLK_CUR];
     const double *__restrict__ const *A = F.f[cur];
     double *const *B = F.f[cur ^ 1];
-    fill_eno_tile<F_COUNT>(
-        T, i0, j0, m, n, c.lx, F_X,
-        [&](int f, int row, int col) { return A[f][(size_t)(row + 1) * m + col]; }, [](int) { return -1; });
+    // One thread copies the seven field tiles (columns i0-2.., storage rows
+    // j0-1..) by TMA while the block sets up the column tables.
+    if (tid == 0) mbar_init(&Sm.bar, 1);
+    tile_columns(T, i0, m, c.lx);
+    __syncthreads();
+    if (tid == 0) {
+        mbar_expect_tx(&Sm.bar, kTileBytes);
+        for (int f = 0; f < F_COUNT; f++) tma_load_2d(&Sm.tile[f][0][0], &maps.f[cur][f], i0 - 2, j0 - 1, &Sm.bar);
+    }
+    if (!mbar_wait_bounded(&Sm.bar)) {
+        if (tid == 0) atomicExch(&F.flags[3], 1);
+        mbar_wait_bounded(&Sm.bar);  // the copies in flight, once more, then go on with what is there
+    }
+    // Columns across the periodic seam arrive as zeros: blocks at either end
+    // fetch them from their wrapped columns.
+    if (i0 == 0 || i0 + ACOLS - 2 > m) {
+        for (int k = tid; k < F_COUNT * AROWS * ACOLS; k += ATX * ATY) {
+            const int f = k / (AROWS * ACOLS), rem = k - f * (AROWS * ACOLS), r = rem / ACOLS, t = rem - r * ACOLS;
+            const int u = i0 + t - 2, sr = j0 - 1 + r;
+            if ((u < 0 || u >= m) && sr >= 0 && sr <= n + 1) Sm.tile[f][r][t] = A[f][(size_t)sr * m + T.col[t]];
+        }
+        __syncthreads();
+    }
+    tile_differences<F_COUNT>(
+        T, i0, j0, m, n, F_X, [&](int f, int row, int t) { return Sm.tile[f][row - j0 + 2][t]; },
+        [](int) { return -1; });
     if (i >= m || j >= n) return;
     const double hx = a.hx, hy = a.hy;
     const size_t ci = (size_t)(j + 1) * m + i;
@@ -211,7 +294,7 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
     // into the velocity: -u * (hs * eno) = -(u * hs) * eno.
     // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
     if (j > 0) {
-        const double *X = A[F_X], *Y = A[F_Y];
+        const double Xc = Sm.tile[F_X][ty + 2][tx + 2], Yc = Sm.tile[F_Y][ty + 2][tx + 2];
         double ex_X, ex_Y, ey_X, ey_Y;
         const double un = V.u(i, j), vn = V.v(i, j);
         const double uh = un * (un > 0 ? hx : -hx), vh = vn * (vn > 0 ? hy : -hy);
@@ -220,8 +303,8 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
         const bool inner = vn > 0 ? j > 1 : j < n - 1;
         ey_X = tile_eno_y(T, F_X, ty, tx, vn > 0, inner);
         ey_Y = tile_eno_y(T, F_Y, ty, tx, vn > 0, inner);
-        B[F_X][ci] = X[ci] + fma(-vh, ey_X, -uh * ex_X);
-        B[F_Y][ci] = Y[ci] + fma(-vh, ey_Y, -uh * ex_Y);
+        B[F_X][ci] = Xc + fma(-vh, ey_X, -uh * ex_X);
+        B[F_Y][ci] = Yc + fma(-vh, ey_Y, -uh * ex_Y);
     }
     // staggered velocity and spin (shear_sim.cc:330-333)
     const double u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
@@ -237,8 +320,9 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
         f1[k] = tile_eno_x(T, k, ty, tx, uc > 0);
         f2[k] = tile_eno_y(T, k, ty, tx, vc > 0, inner);
     }
-    const double p = A[F_P][ci], q = A[F_Q][ci], s = A[F_S][ci], t = A[F_TAU][ci];
-    double cchi = A[F_CHI][ci] + fma(-vh, f2[4], -uh * f1[4]), ddev, dtmp;
+    const double p = Sm.tile[F_P][ty + 2][tx + 2], q = Sm.tile[F_Q][ty + 2][tx + 2];
+    const double s = Sm.tile[F_S][ty + 2][tx + 2], t = Sm.tile[F_TAU][ty + 2][tx + 2];
+    double cchi = Sm.tile[F_CHI][ty + 2][tx + 2] + fma(-vh, f2[4], -uh * f1[4]), ddev, dtmp;
     const double devsq = 3 * q * q + s * s + t * t;
     // Cells far enough below the cut-offs return exactly ddev = 0 and leave
     // chi unchanged in the reference loop (sbar < 1e-12, or an athermal law
@@ -317,9 +401,12 @@ __global__ void __launch_bounds__(ATX * ATY) k_direct(step_consts c, direct_cons
     const double *__restrict__ const *A = F.f[cur];
     double *const *B = F.f[cur ^ 1];
     velo V{F.vel, m, n, bv};
-    fill_eno_tile<DF_COUNT>(
-        TT, i0, j0, m, n, c.lx, F_X,
-        [&](int f, int row, int col) {
+    tile_columns(TT, i0, m, c.lx);
+    __syncthreads();
+    tile_differences<DF_COUNT>(
+        TT, i0, j0, m, n, F_X,
+        [&](int f, int row, int t) {
+            const int col = TT.col[t];
             return f == DF_U ? V.u(col, row) : (f == DF_V ? V.v(col, row) : A[f][(size_t)(row + 1) * m + col]);
         },
         [](int f) { return f >= DF_U ? 0 : -1; });
@@ -514,22 +601,54 @@ cudaError_t prepare_step_kernels() {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 64 && (done >> dev & 1)) return cudaSuccess;
-    e = cudaFuncSetAttribute(k_advect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(adv_tile));
+    e = cudaFuncSetAttribute(k_advect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(adv_smem) + 128));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_direct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(direct_tile));
     if (e == cudaSuccess && dev < 64) done |= 1ull << dev;
     return e;
 }
 
-void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st) {
+int make_field_maps(const step_consts &c, const fields_dev &F, field_maps *out) {
+    typedef CUresult (*encode_fn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static encode_fn encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return fail(STZG_ECUDA, "cuTensorMapEncodeTiled is not available");
+        encode = (encode_fn)fn;
+    }
+    // 16-byte rules: row stride m*8 and the box's inner extent ACOLS*8
+    if ((c.m * sizeof(double)) % 16 != 0) return fail(STZG_EINVAL, "tile copies need an even m");
+    const cuuint64_t dims[2] = {(cuuint64_t)c.m, (cuuint64_t)c.n + 2};
+    const cuuint64_t strides[1] = {(cuuint64_t)c.m * sizeof(double)};
+    const cuuint32_t box[2] = {ACOLS, AROWS};
+    const cuuint32_t estr[2] = {1, 1};
+    for (int b = 0; b < 2; b++)
+        for (int f = 0; f < F_COUNT; f++) {
+            if (((uintptr_t)F.f[b][f]) % 16 != 0) return fail(STZG_EINVAL, "field not 16-byte aligned");
+            const CUresult r = encode(&out->f[b][f], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void *)F.f[b][f], dims,
+                                      strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(STZG_ECUDA, "cuTensorMapEncodeTiled failed");
+        }
+    return STZG_OK;
+}
+
+void advection(const step_consts &c, const field_maps &maps, fields_dev &F, int cur, double dt, double bv,
+               cudaStream_t st) {
     dim3 blk(32, 8);
     advect_consts a;
     a.hx = 0.5 * c.xsp * dt;
     a.hy = 0.5 * c.ysp * dt;
     a.xf = 0.5 / dt * c.xsp;
     a.yf = 0.5 / dt * c.ysp;
-    k_advect<<<dim3(ceil_div(c.m, ATX), ceil_div(c.n, ATY)), dim3(ATX, ATY), sizeof(adv_tile), st>>>(c, a, F, cur,
-                                                                                                      dt, bv, 1);
+    k_advect<<<dim3(ceil_div(c.m, ATX), ceil_div(c.n, ATY)), dim3(ATX, ATY), sizeof(adv_smem) + 128, st>>>(
+        c, a, maps, F, cur, dt, bv, 1);
     note_launch();
     if (c.chi_diff != 0 || c.chi_len != 0) {
         k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);

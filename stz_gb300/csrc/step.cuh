@@ -1,6 +1,8 @@
 // Time-step kernels of the quasi-static STZ simulation.
 #pragma once
 
+#include <cuda.h>
+
 #include "common.cuh"
 
 namespace stzg {
@@ -17,7 +19,8 @@ struct fields_dev {
     double *eps_pl;  // accumulated plastic strain (cells, m*n)
     double2 *vel;    // node velocity, rows 0..n, index j*m+i (solver array)
     double2 *src;    // projection right-hand side, same layout
-    int *flags;      // [0]: plastic sub-step cap reached, [1]: max sub-steps
+    int *flags;      // [0]: plastic sub-step cap reached, [1]: max sub-steps, [2]: scratch of
+                     // the velocity upload, [3]: an advection tile copy wait ran out
     // Per-cell combinations of the advected stress that the nodal net force
     // (shear_sim::net_force, shear_sim.cc:447-453) sums with +-1 weights:
     // U = xf A + yf tau, W = xf A - yf tau, Y1 = xf tau - yf B,
@@ -75,7 +78,17 @@ __device__ __forceinline__ double eno2(double p0, double p1, double p2, double p
 // shear_sim::advection_step + chi_diffusion + the field update
 // (shear_sim.cc:296-386, fields.hh:61-80).  bv is the wall speed of the
 // current state (u = -bv on row 0 and +bv on row n, set_boundaries).
-void advection(const step_consts &c, fields_dev &F, int cur, double dt, double bv, cudaStream_t st);
+// TMA descriptors of the seven advected fields in both state buffers: 2D
+// FP64 tensors of m x (n+2) (rows -1..n), box of the advection tile (36
+// columns x 12 rows).  Built once per simulation; the pointers of F must not
+// change afterwards.
+struct field_maps {
+    CUtensorMap f[2][F_COUNT];
+};
+int make_field_maps(const step_consts &c, const fields_dev &F, field_maps *out);
+// F.flags[3] is set when a tile's copy wait runs out (status, no fault).
+void advection(const step_consts &c, const field_maps &maps, fields_dev &F, int cur, double dt, double bv,
+               cudaStream_t st);
 // Opts the advection kernel into the shared memory its tile needs (once per
 // process, outside any stream capture).
 cudaError_t prepare_step_kernels();

@@ -33,6 +33,8 @@ namespace {
 
 struct gst {
     double e[10];  // dl dc dr cl cc cr ul uc ur, 1/cc (tgmg_level::s, tgmg.hh:256-265)
+    int nz;        // bit k set where off-diagonal entry k is nonzero
+    int pad;
 };
 
 struct glevel {
@@ -47,6 +49,8 @@ constexpr int kMaxLevels = 17;
 constexpr int kGridMin = 10;        // tgmg_grid_min, tgmg_config.hh:23
 constexpr int kBottomDirect = 1024; // largest coarsest level solved by a dense inverse
 constexpr int kRedBlocks = 4 * 152;
+constexpr size_t kTailSmem = 200 * 1024; // shared memory of the single-block tail
+constexpr long kTailPoints = 4400;       // largest level the tail takes
 constexpr int kRedThreads = 256;
 
 // Neighbour index on a line of m points, or -1 outside a non-periodic line.
@@ -58,27 +62,30 @@ __host__ __device__ inline int nbr(int i, int d, int m, int prd) {
 }
 
 // Off-diagonal product sum_k a_k z_k at (i, j) (tgmg_level::mul_a,
-// tgmg.in.cc:536-547); neighbours outside a non-periodic grid are skipped.
+// tgmg.in.cc:536-547); neighbours outside a non-periodic grid are skipped, and
+// so are zero entries (an integer test on the stencil's mask: the FP64 pipe,
+// GB300's scarce one, only sees the nonzero products).
 __device__ __forceinline__ double offdiag(const glevel &L, const gst &s, int i, int j) {
     const int il = nbr(i, -1, L.m, L.xp), ir = nbr(i, 1, L.m, L.xp);
     const int jd = nbr(j, -1, L.n, L.yp), ju = nbr(j, 1, L.n, L.yp);
+    const int nz = s.nz;
     double a = 0;
     if (jd >= 0) {
         const double *zr = L.z + (size_t)jd * L.m;
-        if (il >= 0) a += s.e[0] * zr[il];
-        a += s.e[1] * zr[i];
-        if (ir >= 0) a += s.e[2] * zr[ir];
+        if ((nz & 1) && il >= 0) a = fma(s.e[0], zr[il], a);
+        if (nz & 2) a = fma(s.e[1], zr[i], a);
+        if ((nz & 4) && ir >= 0) a = fma(s.e[2], zr[ir], a);
     }
     {
         const double *zr = L.z + (size_t)j * L.m;
-        if (il >= 0) a += s.e[3] * zr[il];
-        if (ir >= 0) a += s.e[5] * zr[ir];
+        if ((nz & 8) && il >= 0) a = fma(s.e[3], zr[il], a);
+        if ((nz & 32) && ir >= 0) a = fma(s.e[5], zr[ir], a);
     }
     if (ju >= 0) {
         const double *zr = L.z + (size_t)ju * L.m;
-        if (il >= 0) a += s.e[6] * zr[il];
-        a += s.e[7] * zr[i];
-        if (ir >= 0) a += s.e[8] * zr[ir];
+        if ((nz & 64) && il >= 0) a = fma(s.e[6], zr[il], a);
+        if (nz & 128) a = fma(s.e[7], zr[i], a);
+        if ((nz & 256) && ir >= 0) a = fma(s.e[8], zr[ir], a);
     }
     return a;
 }
@@ -95,6 +102,7 @@ __device__ __forceinline__ int color_line(int k, int c, int m, int cn) {
 
 // One colour of Gauss-Seidel (omega = 1) or SOR: z += omega (D^-1 (b - A'z) - z)
 // (gauss_seidel, sor: tgmg.in.cc:128-230).
+template <bool Relax>
 __global__ void k_tg_color(glevel L, int cx, int cy, double omega) {
     const int i = color_line(blockIdx.x * blockDim.x + threadIdx.x, cx, L.m, L.cx_n);
     const int j = color_line(blockIdx.y * blockDim.y + threadIdx.y, cy, L.n, L.cy_n);
@@ -102,7 +110,7 @@ __global__ void k_tg_color(glevel L, int cx, int cy, double omega) {
     const size_t ij = (size_t)j * L.m + i;
     const gst &s = L.st[L.cls[ij]];
     const double t = s.e[9] * (L.b[ij] - offdiag(L, s, i, j));
-    L.z[ij] = omega == 1.0 ? t : L.z[ij] + omega * (t - L.z[ij]);
+    L.z[ij] = Relax ? L.z[ij] + omega * (t - L.z[ij]) : t;
 }
 
 // Jacobi update into r (jacobi, tgmg.in.cc:69-85); the caller copies r to z.
@@ -133,28 +141,48 @@ __device__ __forceinline__ int fine_at(int I, int d, int m, int prd) {
     return f;
 }
 
-// Child b = P^T r (apply_r, tgmg.in.cc:626-647): weights 1, 1/2, 1/4 from
-// the interpolation's halves in each direction.
-__global__ void k_tg_restrict(glevel F, glevel C) {
-    const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y;
-    if (I >= C.m || J >= C.n) return;
-    double a = 0;
+// Child b = P^T r at (I, J) (apply_r, tgmg.in.cc:626-647): weights 1, 1/2,
+// 1/4 from the interpolation's halves in each direction, summed as
+// (sum over rows of hy * (sum over columns of hx * r)) / 4 with the factors 2
+// applied as additions.
+__device__ __forceinline__ double restrict_at(const glevel &F, const double *r, int I, int J) {
+    double acc = 0;
 #pragma unroll
     for (int dy = -1; dy <= 1; dy++) {
         const int fy = fine_at(J, dy, F.n, F.yp);
         if (fy < 0) continue;
         const int hy = halves_of(fy, F.n, F.yp, J);
         if (!hy) continue;
+        const double *rr = r + (size_t)fy * F.m;
+        double row = 0;
 #pragma unroll
         for (int dx = -1; dx <= 1; dx++) {
             const int fx = fine_at(I, dx, F.m, F.xp);
             if (fx < 0) continue;
             const int hx = halves_of(fx, F.m, F.xp, I);
             if (!hx) continue;
-            a += (double)(hx * hy) * 0.25 * F.r[(size_t)fy * F.m + fx];
+            row += hx == 2 ? rr[fx] + rr[fx] : rr[fx];
         }
+        acc += hy == 2 ? row + row : row;
     }
-    C.b[(size_t)J * C.m + I] = a;
+    return 0.25 * acc;
+}
+
+__global__ void k_tg_restrict(glevel F, glevel C) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y;
+    if (I >= C.m || J >= C.n) return;
+    C.b[(size_t)J * C.m + I] = restrict_at(F, F.r, I, J);
+}
+
+// Interpolated child value at a parent point from the coarse indices of
+// p1d_halves: injection, the mean of two, or the mean of four (exact weights
+// 1, 1/2, 1/4 applied as one multiplication).
+__device__ __forceinline__ double interp_at(const glevel &C, int ny, const int *cy, int nx, const int *cx) {
+    const double *r0 = C.z + (size_t)cy[0] * C.m;
+    if (ny == 1) return nx == 1 ? r0[cx[0]] : 0.5 * (r0[cx[0]] + r0[cx[1]]);
+    const double *r1 = C.z + (size_t)cy[1] * C.m;
+    if (nx == 1) return 0.5 * (r0[cx[0]] + r1[cx[0]]);
+    return 0.25 * ((r0[cx[0]] + r0[cx[1]]) + (r1[cx[0]] + r1[cx[1]]));
 }
 
 // Parent z += P z_child (apply_t, tgmg.in.cc:552-606).
@@ -163,10 +191,7 @@ __global__ void k_tg_prolong(glevel C, glevel F) {
     if (i >= F.m || j >= F.n) return;
     int cy[2], hy[2], cx[2], hx[2];
     const int ny = p1d_halves(j, F.n, F.yp, cy, hy), nx = p1d_halves(i, F.m, F.xp, cx, hx);
-    double a = 0;
-    for (int q = 0; q < ny; q++)
-        for (int p = 0; p < nx; p++) a += (double)(hx[p] * hy[q]) * 0.25 * C.z[(size_t)cy[q] * C.m + cx[p]];
-    F.z[(size_t)j * F.m + i] += a;
+    F.z[(size_t)j * F.m + i] += interp_at(C, ny, cy, nx, cx);
 }
 
 // Coarsest level: z = A^-1 b with the dense FP64 inverse.
@@ -220,6 +245,117 @@ __global__ void k_tg_sum(const double *partials, int np, double *out) {
 }
 
 // ---------------------------------------------------------------------------
+// Tail of the cycle on the small levels, one block of 32 x 32 threads: the
+// recursive V-cycle below level t (down sweeps from zero, residual and
+// restriction level by level, the coarsest solve, prolongation and up sweeps)
+// with z, b and r of levels t..L in shared memory; b of level t comes from
+// and z of level t goes to global memory.  Phases are separated by
+// __syncthreads.
+
+struct tail_args {
+    int t, L, cd, cu, hb, sym;
+    const double *inv;
+    int inv_n;
+    glevel lv[kMaxLevels];
+};
+
+__device__ void tail_sweep(const glevel &L, bool reverse) {
+    const int nc = L.cx_n * L.cy_n;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    const int kx = (L.m + 1) / 2, ky = (L.n + 1) / 2;
+    for (int q = 0; q < nc; q++) {
+        const int c = reverse ? nc - 1 - q : q;
+        const int cy = c / L.cx_n, cx = c % L.cx_n;
+        for (int k = tid; k < kx * ky; k += nth) {
+            const int i = color_line(k % kx, cx, L.m, L.cx_n), j = color_line(k / kx, cy, L.n, L.cy_n);
+            if (i < 0 || j < 0) continue;
+            const size_t ij = (size_t)j * L.m + i;
+            const gst &s = L.st[L.cls[ij]];
+            L.z[ij] = s.e[9] * (L.b[ij] - offdiag(L, s, i, j));
+        }
+        __syncthreads();
+    }
+}
+
+__device__ void tail_clear(const glevel &L) {
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int k = tid; k < L.m * L.n; k += nth) L.z[k] = 0;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_tg_tail(tail_args a) {
+    extern __shared__ __align__(16) double tsm[];
+    __shared__ glevel S[kMaxLevels];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    if (tid == 0) {
+        size_t off = 0;
+        for (int l = a.t; l <= a.L; l++) {
+            S[l] = a.lv[l];
+            const size_t mn = (size_t)S[l].m * S[l].n;
+            S[l].z = tsm + off;
+            S[l].b = tsm + off + mn;
+            S[l].r = tsm + off + 2 * mn;
+            off += 3 * mn;
+        }
+    }
+    __syncthreads();
+    {
+        const glevel &T = S[a.t];
+        for (int k = tid; k < T.m * T.n; k += nth) T.b[k] = a.lv[a.t].b[k];
+        __syncthreads();
+    }
+    // down: levels t..L-1 (down_gs_iterations, then residual and restriction)
+    for (int i = a.t; i < a.L; i++) {
+        const glevel &L = S[i], &C = S[i + 1];
+        tail_clear(L);
+        for (int c = 0; c < a.cd; c++) tail_sweep(L, false);
+        for (int k = tid; k < L.m * L.n; k += nth) {
+            const int j = k / L.m, ii = k - j * L.m;
+            const gst &s = L.st[L.cls[k]];
+            L.r[k] = L.b[k] - offdiag(L, s, ii, j) - s.e[4] * L.z[k];
+        }
+        __syncthreads();
+        for (int k = tid; k < C.m * C.n; k += nth) {
+            const int J = k / C.m, I = k - J * C.m;
+            C.b[k] = restrict_at(L, L.r, I, J);
+        }
+        __syncthreads();
+    }
+    // coarsest level
+    {
+        const glevel &B = S[a.L];
+        if (a.inv) {
+            for (int r = tid; r < a.inv_n; r += nth) {
+                const double *row = a.inv + (size_t)r * a.inv_n;
+                double acc = 0;
+                for (int k = 0; k < a.inv_n; k++) acc += row[k] * B.b[k];
+                B.z[r] = acc;
+            }
+            __syncthreads();
+        } else {
+            tail_clear(B);
+            for (int c = 0; c < 2 * a.hb; c++) tail_sweep(B, a.sym && c >= a.hb);
+        }
+    }
+    // up: prolongation and up_gs_iterations on levels L-1..t
+    for (int i = a.L; i > a.t; i--) {
+        const glevel &C = S[i], &F = S[i - 1];
+        for (int k = tid; k < F.m * F.n; k += nth) {
+            const int j = k / F.m, ii = k - j * F.m;
+            int cy[2], hy[2], cx[2], hx[2];
+            const int ny = p1d_halves(j, F.n, F.yp, cy, hy), nx = p1d_halves(ii, F.m, F.xp, cx, hx);
+            F.z[k] += interp_at(C, ny, cy, nx, cx);
+        }
+        __syncthreads();
+        for (int c = 0; c < a.cu; c++) tail_sweep(F, a.sym != 0);
+    }
+    {
+        const glevel &T = S[a.t];
+        for (int k = tid; k < T.m * T.n; k += nth) a.lv[a.t].z[k] = T.z[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host side: hierarchy sizes, Galerkin products, dense coarsest inverse.
 
 struct host_level {
@@ -261,6 +397,13 @@ inline int coarse_offset(int c, int C, int cm, int prd) {
     return o;
 }
 
+int nonzero_mask(const gst &s) {
+    int nz = 0;
+    for (int k = 0; k < 9; k++)
+        if (k != 4 && s.e[k] != 0) nz |= 1 << k;
+    return nz;
+}
+
 // Galerkin stencil at coarse point (I, J): sum over fine points k near
 // (2I, 2J) and their neighbours l of P(k, (I,J)) A(k, l) P(l, neighbour).
 gst rap_point(const host_level &F, int xp, int yp, int cm, int cn, int I, int J) {
@@ -296,9 +439,10 @@ gst rap_point(const host_level &F, int xp, int yp, int cm, int cn, int I, int J)
             }
         }
     }
-    gst out;
+    gst out = {};
     for (int k = 0; k < 9; k++) out.e[k] = acc[k];
     out.e[9] = 1. / acc[4];
+    out.nz = nonzero_mask(out);
     return out;
 }
 
@@ -402,6 +546,8 @@ struct stzg_tgmg {
     std::vector<void *> owned;
     double *inv = nullptr;
     int inv_n = 0;
+    int tail_start = 1 << 30;  // first level handled by k_tg_tail (none if > nl-1)
+    size_t tail_smem = 0;
     double *partials = nullptr, *dsum = nullptr, *hsum = nullptr;
     // graph of one iteration of the last (type, omega, cycles) used
     cudaGraphExec_t gexec = nullptr;
@@ -435,7 +581,9 @@ void sweep(stzg_tgmg *g, const glevel &L, bool reverse, double omega) {
     for (int q = 0; q < nc; q++) {
         const int c = reverse ? nc - 1 - q : q;
         const int cy = c / L.cx_n, cx = c % L.cx_n;
-        k_tg_color<<<grid_of((L.m + 1) / 2, (L.n + 1) / 2, kBlk), kBlk, 0, g->st>>>(L, cx, cy, omega);
+        const dim3 gr = grid_of((L.m + 1) / 2, (L.n + 1) / 2, kBlk);
+        if (omega == 1.0) k_tg_color<false><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
+        else k_tg_color<true><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
         launch_note(g);
     }
 }
@@ -480,19 +628,51 @@ void bottom(stzg_tgmg *g, const glevel &B, int hcyc, bool sym) {
     }
 }
 
-// v_cycle_internal (tgmg.in.cc:341-359) from level lv (>= 1), whose z has
-// had its down sweeps.
-void internal(stzg_tgmg *g, int level, int cd, int cu, int hb, bool sym) {
+void tail(stzg_tgmg *g, int i, int cd, int cu, int hb, bool sym) {
+    tail_args a;
+    a.t = i;
+    a.L = g->nl - 1;
+    a.cd = cd;
+    a.cu = cu;
+    a.hb = hb;
+    a.sym = sym ? 1 : 0;
+    a.inv = g->inv;
+    a.inv_n = g->inv_n;
+    for (int l = 0; l < g->nl; l++) a.lv[l] = g->lv[l];
+    size_t smem = 0;
+    for (int l = i; l < g->nl; l++) smem += 3 * sizeof(double) * (size_t)g->lv[l].m * g->lv[l].n;
+    k_tg_tail<<<1, dim3(32, 32), smem, g->st>>>(a);
+    launch_note(g);
+}
+
+// The V-cycle from level i (>= 1) on its b: down_gs, restriction, the cycle
+// below, prolongation, up_gs; the coarsest level is the bottom solve.  This
+// is v_cycle_internal (tgmg.in.cc:341-359) written recursively; levels from
+// tail_start down run in one k_tg_tail launch.
+void vc(stzg_tgmg *g, int i, int cd, int cu, int hb, bool sym) {
     const int L = g->nl - 1;
-    for (int i = level; i < L; i++) {
-        if (i > level) down_gs(g, g->lv[i], cd);
-        restrict_to(g, g->lv[i], g->lv[i + 1]);
+    if (i == L) {
+        bottom(g, g->lv[L], hb, sym);
+        return;
     }
-    bottom(g, g->lv[L], hb, sym);
-    for (int i = L; i > level; i--) {
-        prolong(g, g->lv[i], g->lv[i - 1]);
-        up_gs(g, g->lv[i - 1], cu, sym);
+    if (i >= g->tail_start) {
+        tail(g, i, cd, cu, hb, sym);
+        return;
     }
+    down_gs(g, g->lv[i], cd);
+    restrict_to(g, g->lv[i], g->lv[i + 1]);
+    vc(g, i + 1, cd, cu, hb, sym);
+    prolong(g, g->lv[i + 1], g->lv[i]);
+    up_gs(g, g->lv[i], cu, sym);
+}
+
+// v_cycle_internal from a level whose z has had its down sweeps: restrict,
+// cycle below, prolong, up sweeps.
+void internal(stzg_tgmg *g, int level, int cd, int cu, int hb, bool sym) {
+    restrict_to(g, g->lv[level], g->lv[level + 1]);
+    vc(g, level + 1, cd, cu, hb, sym);
+    prolong(g, g->lv[level + 1], g->lv[level]);
+    up_gs(g, g->lv[level], cu, sym);
 }
 
 // tgmg::v_cycle (tgmg.in.cc:313-328).
@@ -500,12 +680,7 @@ void v_cycle(stzg_tgmg *g, int cd, int cu, int hb, bool sym) {
     for (int c = 0; c < cd; c++) sweep(g, g->lv[0], false, 1.0);
     if (g->nl > 1) {
         restrict_to(g, g->lv[0], g->lv[1]);
-        if (g->nl - 1 > 1) {
-            down_gs(g, g->lv[1], cd);
-            internal(g, 1, cd, cu, hb, sym);
-        } else {
-            bottom(g, g->lv[1], hb, sym);
-        }
+        vc(g, 1, cd, cu, hb, sym);
         prolong(g, g->lv[1], g->lv[0]);
     }
     up_gs(g, g->lv[0], cu, sym);
@@ -680,10 +855,11 @@ int stzg_tgmg_create(int m, int n, int x_prd, int y_prd, const double *table, in
     top.m = m;
     top.n = n;
     top.cls.assign(cls, cls + mn);
-    top.table.resize(ntable);
+    top.table.assign(ntable, gst{});
     for (int c = 0; c < ntable; c++) {
         for (int k = 0; k < 9; k++) top.table[c].e[k] = table[9 * c + k];
         top.table[c].e[9] = 1. / table[9 * c + 4];
+        top.table[c].nz = nonzero_mask(top.table[c]);
     }
     g->host.push_back(top);
     const std::vector<std::pair<int, int>> sizes = level_sizes(m, n, g->xp, g->yp);
@@ -728,6 +904,26 @@ int stzg_tgmg_create(int m, int n, int x_prd, int y_prd, const double *table, in
             g->inv_n = B.m * B.n;
             if (cudaMemcpy(p, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
                 return bail(fail(STZG_ECUDA, "upload of the coarsest inverse failed"));
+        }
+    }
+    // single-block tail: the small levels that fit in its shared memory
+    // together, if they are at least two (the coarsest alone is the bottom)
+    {
+        size_t bytes = 0;
+        int t = g->nl;
+        for (int l = g->nl - 1; l >= 1; l--) {
+            const long pts = (long)g->host[l].m * g->host[l].n;
+            const size_t b = 3 * sizeof(double) * (size_t)pts;
+            if (pts > kTailPoints || bytes + b > kTailSmem) break;
+            bytes += b;
+            t = l;
+        }
+        if (t <= g->nl - 2) {
+            if (cudaFuncSetAttribute(k_tg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
+                cudaSuccess)
+                return bail(fail(STZG_ECUDA, "tail kernel attribute"));
+            g->tail_start = t;
+            g->tail_smem = bytes;
         }
     }
     {
@@ -878,7 +1074,7 @@ int stzg_tgmg_stencil(stzg_tgmg *g, int level, double *out) {
     if (!g || !out || level < 1 || level >= g->nl) return fail(STZG_EINVAL, "bad level");
     const host_level &H = g->host[level];
     const size_t pts = (size_t)H.m * H.n;
-    for (size_t k = 0; k < pts; k++) std::memcpy(out + 10 * k, H.table[H.cls[k]].e, sizeof(gst));
+    for (size_t k = 0; k < pts; k++) std::memcpy(out + 10 * k, H.table[H.cls[k]].e, 10 * sizeof(double));
     return STZG_OK;
 }
 

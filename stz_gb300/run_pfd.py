@@ -41,7 +41,7 @@ def main(argv=None):
     for k in range(args.warmup):
         q.gaussian_source_term(6 * math.cos(h * k), 6 * math.sin(h * k), 1, 1)
         assert g.solve_v_cycle(tp)
-    tp.avg_iters()
+    tp.solves = tp.vcount = 0
     wall = dev = 0.0
     kernels = 0
     for k in range(args.trials):

@@ -42,7 +42,9 @@ class Predict(ctypes.Structure):
         load().stzg_tgmg_predict_init(ctypes.byref(self))
 
     def avg_iters(self):
-        ans = float(self.vcount) / float(self.solves)
+        """Average count per solve since the last call, then reset (NaN
+        before any solve, as the reference's float division gives)."""
+        ans = float(self.vcount) / self.solves if self.solves else float("nan")
         self.solves = self.vcount = 0
         return ans
 
