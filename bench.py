@@ -41,7 +41,7 @@ VCYCLE32_BYTES_PER_NODE = 69.3   # 17.3 words of 4 B: 13 W on the top level x (1
 VCYCLE64_BYTES_PER_NODE = 138.7
 SWEEP32_BYTES_PER_NODE = 24      # one Gauss-Seidel sweep: read z, b; write z (float2)
 # DRAM bytes (read + write) of one launch at 2048x2048 from the committed ncu capture
-NCU_TRAFFIC_2048 = {"advect": 659.5e6, "residual_ff": 153.0e6}
+NCU_TRAFFIC_2048 = {"advect": 659.8e6, "residual_ff": 153.0e6}
 DIRECT_BYTES_PER_CELL = 160      # explicit step: read u,v,p,q,s,tau,chi,X,Y; write them, ddev (8 B each)
 RESIDFF_BYTES_PER_NODE = 40      # read z, b as float-float (hi, lo float2 each); write r (float2)
 
@@ -330,7 +330,7 @@ def run_ours(args, dist):
                         "ms_per_launch": t, "algorithmic_bytes": b,
                         "share_of_step": shares[dom] / (1e3 * dev_s / args.steps)}
     if dom == "advect":
-        line["roofline"]["note"] = "FP64-ALU-bound (FP64 pipe 80% active under ncu); HBM is not the limit"
+        line["roofline"]["note"] = "FP64-ALU-bound (FP64 pipe 83% active under ncu); HBM is not the limit"
 
     line["kernels"] = {k: {"ms": t, "per_step": c, "GBs": b / (t * 1e-3) / 1e9} for k, (t, b, c) in rows.items()}
     line["mg_hbm_gbs"] = line["kernels"].get("vcycle_fp32", line["kernels"].get("vcycle_fp64"))["GBs"]

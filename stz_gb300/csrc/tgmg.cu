@@ -50,7 +50,9 @@ constexpr int kGridMin = 10;        // tgmg_grid_min, tgmg_config.hh:23
 constexpr int kBottomDirect = 1024; // largest coarsest level solved by a dense inverse
 constexpr int kRedBlocks = 4 * 152;
 constexpr size_t kTailSmem = 200 * 1024; // shared memory of the single-block tail
-constexpr long kTailPoints = 4400;       // largest level the tail takes
+// Largest level the tail takes: one SM's FP64 pipe is slow (a 65 x 65
+// level alone kept the tail at ~120 us a cycle), so the tail starts at 33 x 33.
+constexpr long kTailPoints = 1200;
 constexpr int kRedThreads = 256;
 
 // Neighbour index on a line of m points, or -1 outside a non-periodic line.
