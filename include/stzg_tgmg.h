@@ -5,7 +5,8 @@
  * (the concept of esim/tgmg/poisson_fd.hh:7-61: grid m x n, periodicity
  * x_prd/y_prd, nine stencil functions a_dl..a_ur, a_cc, inv_cc, mul_a and the
  * squared-L2 threshold acc).  The operator is passed as a table of distinct
- * 9-point stencils plus the stencil index of every grid point; coarse levels
+ * 9-point stencils (scalar or 2x2 blocks) plus the stencil index of every
+ * grid point; coarse levels
  * are Galerkin products with the reference's restriction and interpolation
  * (tgmg.in.cc:552-736).  One handle owns the hierarchy in device memory, a
  * CUDA stream and the captured cycle graphs.  Statuses and the last message
@@ -45,13 +46,28 @@ enum { STZG_TGMG_JACOBI = 0, STZG_TGMG_GS = 1, STZG_TGMG_SOR = 2, STZG_TGMG_FMG 
  * device: CUDA ordinal.  A periodic direction needs at least 3 points. */
 int stzg_tgmg_create(int m, int n, int x_prd, int y_prd, const double *table, int ntable, const int *cls,
                      double acc, int device, stzg_tgmg **out);
+/* tgmg<S,vec,mat> (2-vector values, 2x2 blocks, as the reference's qs_multi
+ * classes, esim/sb/main/qs_multi.hh:11-57): block = 2, the table holds 9
+ * row-major 2x2 blocks per stencil (36 doubles) and b, z hold (x, y) per
+ * point; block = 1 is stzg_tgmg_create. */
+int stzg_tgmg_create_block(int m, int n, int x_prd, int y_prd, int block, const double *table, int ntable,
+                           const int *cls, double acc, int device, stzg_tgmg **out);
+/* New operator values on the same grid: the problem class's stencil
+ * changed, e.g. qs_multi::init before each solve (coord_transforms
+ * qs_multi.cc:31-46).  Rebuilds the Galerkin hierarchy (tgmg::setup). */
+int stzg_tgmg_set_operator(stzg_tgmg *g, const double *table, int ntable, const int *cls);
 int stzg_tgmg_destroy(stzg_tgmg *g);
 
-/* The source b and solution z (m*n doubles, row-major), copied in and out. */
+/* The source b and solution z (block*m*n doubles, row-major), copied in and out. */
 int stzg_tgmg_set_b(stzg_tgmg *g, const double *b);
 int stzg_tgmg_get_b(stzg_tgmg *g, double *b);
 int stzg_tgmg_set_z(stzg_tgmg *g, const double *z);
 int stzg_tgmg_get_z(stzg_tgmg *g, double *z);
+/* Device addresses of the top level's b and z (block*m*n doubles each, on
+ * the handle's device), for callers that keep the solve's data on the GPU;
+ * valid until stzg_tgmg_destroy.  Work on them must be ordered before the
+ * next call on the handle (the handle's calls synchronize its stream). */
+int stzg_tgmg_device_arrays(stzg_tgmg *g, double **b, double **z);
 /* tgmg_base::clear_z (tgmg.in.cc:792). */
 int stzg_tgmg_clear_z(stzg_tgmg *g);
 
@@ -77,8 +93,8 @@ int stzg_tgmg_l2_error(stzg_tgmg *g, double *err);
 /* Hierarchy: nlevels including the top; dims gets (m, n) per level. */
 int stzg_tgmg_levels(stzg_tgmg *g, int *nlevels, int *dims);
 /* Galerkin stencils of coarse level `level` (1 = first child) in the layout
- * of tgmg_level::s (tgmg.hh:235): 10 doubles per point (9 entries and the
- * reciprocal of the centre), m*n points of that level. */
+ * of tgmg_level::s (tgmg.hh:235): 10 blocks per point (9 entries and the
+ * inverse of the centre), block*block doubles each, m*n points of that level. */
 int stzg_tgmg_stencil(stzg_tgmg *g, int level, double *out);
 /* Device time (ms, CUDA events) of the last solve/iterate call and the
  * kernels it launched. */

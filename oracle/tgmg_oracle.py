@@ -64,10 +64,12 @@ def _nbr(i, d, m, prd):
     return k + m if k < 0 else k - m
 
 
-def operator(m, n, xp, yp, table, cls):
-    """Sparse (m n) x (m n) operator from a stencil table (dl dc dr cl cc cr
-    ul uc ur per row) and a stencil index per point (index j*m+i)."""
-    table = np.asarray(table, dtype=np.float64).reshape(-1, 9)
+def operator(m, n, xp, yp, table, cls, block=1):
+    """Sparse (B m n) x (B m n) operator from a stencil table (dl dc dr cl cc
+    cr ul uc ur per row; 2x2 row-major blocks when block = 2) and a stencil
+    index per point (index j*m+i); unknown B*(j*m+i)+c."""
+    B = block
+    table = np.asarray(table, dtype=np.float64).reshape(-1, 9, B, B)
     cls = np.asarray(cls).reshape(-1)
     rows, cols, vals = [], [], []
     ii, jj = np.meshgrid(np.arange(m), np.arange(n))
@@ -76,29 +78,33 @@ def operator(m, n, xp, yp, table, cls):
         ly = np.array([_nbr(j, sy, n, yp) for j in range(n)])[jj]
         for sx in (-1, 0, 1):
             lx = np.array([_nbr(i, sx, m, xp) for i in range(m)])[ii]
-            a = table[cls, (sy + 1) * 3 + sx + 1]
-            ok = (lx >= 0) & (ly >= 0) & (a != 0)
-            rows.append((jj * m + ii)[ok])
-            cols.append((ly * m + lx)[ok])
-            vals.append(a[ok])
+            for r in range(B):
+                for c in range(B):
+                    a = table[cls, (sy + 1) * 3 + sx + 1, r, c]
+                    ok = (lx >= 0) & (ly >= 0) & (a != 0)
+                    rows.append(B * (jj * m + ii)[ok] + r)
+                    cols.append(B * (ly * m + lx)[ok] + c)
+                    vals.append(a[ok])
     rows, cols, vals = np.concatenate(rows), np.concatenate(cols), np.concatenate(vals)
-    return sp.csr_matrix((vals, (rows, cols)), shape=(m * n, m * n))
+    return sp.csr_matrix((vals, (rows, cols)), shape=(B * m * n, B * m * n))
 
 
-def galerkin(A, m, n, xp, yp):
-    """P^T A P and the child size."""
+def galerkin(A, m, n, xp, yp, block=1):
+    """P^T A P and the child size (P acts on every block component)."""
     Px, Py = interp_1d(m, xp), interp_1d(n, yp)
-    P = sp.kron(Py, Px, format="csr")
+    P = sp.kron(sp.kron(Py, Px), sp.identity(block), format="csr")
     return (P.T @ A @ P).tocsr(), (Px.shape[1], Py.shape[1])
 
 
-def stencils(A, m, n, xp, yp):
-    """(n, m, 10) stencils of a level's operator: the 9 entries and 1/centre."""
+def stencils(A, m, n, xp, yp, block=1):
+    """Stencils of a level's operator: (n, m, 10) with the 9 entries and
+    1/centre, or (n, m, 10, 2, 2) with the blocks and the inverse centre."""
+    B = block
     A = A.tocsr()
-    out = np.zeros((n, m, 10))
+    out = np.zeros((n, m, 10, B, B))
     for j in range(n):
         for i in range(m):
-            r = j * m + i
+            p = j * m + i
             for sy in (-1, 0, 1):
                 ly = _nbr(j, sy, n, yp)
                 if ly < 0:
@@ -107,17 +113,18 @@ def stencils(A, m, n, xp, yp):
                     lx = _nbr(i, sx, m, xp)
                     if lx < 0:
                         continue
-                    out[j, i, (sy + 1) * 3 + sx + 1] = A[r, ly * m + lx]
-            out[j, i, 9] = 1.0 / out[j, i, 4]
-    return out
+                    q = ly * m + lx
+                    out[j, i, (sy + 1) * 3 + sx + 1] = A[B * p:B * p + B, B * q:B * q + B].toarray()
+            out[j, i, 9] = np.linalg.inv(out[j, i, 4])
+    return out[..., 0, 0] if B == 1 else out
 
 
-def hierarchy(m, n, xp, yp, table, cls):
+def hierarchy(m, n, xp, yp, table, cls, block=1):
     """Operators of every level, top first, and their sizes."""
     sizes = level_sizes(m, n, xp, yp)
-    ops = [operator(m, n, xp, yp, table, cls)]
+    ops = [operator(m, n, xp, yp, table, cls, block)]
     for l in range(1, len(sizes)):
-        Ac, csz = galerkin(ops[-1], sizes[l - 1][0], sizes[l - 1][1], xp, yp)
+        Ac, csz = galerkin(ops[-1], sizes[l - 1][0], sizes[l - 1][1], xp, yp, block)
         assert csz == sizes[l]
         ops.append(Ac)
     return ops, sizes
@@ -147,11 +154,12 @@ def gaussian_source(m, n, ax, bx, ay, by, gx, gy, r, amp):
     return b
 
 
-def l2_error(A, z, b):
+def l2_error(A, z, b, block=1):
+    """mds/mn: squared residual summed over components, per grid point."""
     r = b.ravel() - A @ z.ravel()
-    return float(r @ r) / r.size
+    return float(r @ r) / (r.size // block)
 
 
 def solve(A, b):
-    """Exact discrete solution."""
+    """Exact discrete solution (b in the unknowns' order, any shape)."""
     return spla.spsolve(A.tocsc(), b.ravel()).reshape(b.shape)

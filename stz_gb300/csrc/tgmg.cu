@@ -1,22 +1,24 @@
-// General scalar geometric multigrid on one GPU (include/stzg_tgmg.h): the
-// tgmg<S,double,double> template of esim/tgmg (tgmg.hh:42-495,
-// tgmg.in.cc:11-856) for problem classes such as poisson_fd
-// (esim/tgmg/poisson_fd.hh:7-61).
+// General geometric multigrid on one GPU (include/stzg_tgmg.h): the
+// tgmg<S,V,M> template of esim/tgmg (tgmg.hh:42-495, tgmg.in.cc:11-856) for
+// problem classes with scalar values (V = M = double, e.g. poisson_fd,
+// esim/tgmg/poisson_fd.hh:7-61) or 2-vectors with 2x2 blocks (V = vec,
+// M = mat, e.g. the qs_multi classes of esim/sb and esim/coord_transforms).
 //
 // Layout: every level keeps z, b and a residual buffer r (FP64, row-major,
-// index j*m+i) and its operator as a table of distinct 9-point stencils plus
-// the reciprocal centre, with a stencil index per point; the top level uses
-// the problem's own table.  Coarse operators are the Galerkin products
-// P^T A P of tgmg_base::rat (tgmg.in.cc:667-736) with the reference's
-// one-dimensional interpolation in each direction (apply_t / t_line,
-// tgmg.in.cc:552-621; restriction is its transpose, apply_r :626-647).
+// index j*m+i, B components per point) and its operator as a table of
+// distinct 9-point block stencils plus the inverse centre block, with a
+// stencil index per point; the top level uses the problem's own table.
+// Coarse operators are the Galerkin products P^T A P of tgmg_base::rat
+// (tgmg.in.cc:667-736) with the reference's one-dimensional interpolation in
+// each direction (apply_t / t_line, tgmg.in.cc:552-621; restriction is its
+// transpose, apply_r :626-647), applied to every block component.
 // Gauss-Seidel runs in four colours ((i&1),(j&1)), a true Gauss-Seidel
 // ordering for 9-point stencils, with a third colour for the last line of an
 // odd periodic direction; the reference sweeps zebra-lexicographically
 // (tgmg.in.cc:128-208), so iterates differ and converged solutions agree.
 // The coarsest level (more than 10 points, the next coarsening would have
 // at most 10, tgmg_config.hh:23) is solved exactly with a dense inverse
-// where it has at most 1024 points, else smoothed like the reference.
+// where it has at most 1024 unknowns, else smoothed like the reference.
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -31,29 +33,69 @@
 namespace stzg {
 namespace {
 
-struct gst {
-    double e[10];  // dl dc dr cl cc cr ul uc ur, 1/cc (tgmg_level::s, tgmg.hh:256-265)
-    int nz;        // bit k set where off-diagonal entry k is nonzero
+// Value of a point (B components) and a block (B x B, row-major: the
+// reference's vec and mat, vec.hh / mat.hh).
+template <int B> struct bv {
+    double c[B];
+};
+template <int B> struct bm {
+    double c[B * B];
+};
+
+template <int B> __host__ __device__ __forceinline__ bv<B> vzero() {
+    bv<B> r;
+#pragma unroll
+    for (int k = 0; k < B; k++) r.c[k] = 0;
+    return r;
+}
+// a += M x
+template <int B> __device__ __forceinline__ void madd(bv<B> &a, const bm<B> &M, const bv<B> &x) {
+#pragma unroll
+    for (int r = 0; r < B; r++)
+#pragma unroll
+        for (int c = 0; c < B; c++) a.c[r] = fma(M.c[r * B + c], x.c[c], a.c[r]);
+}
+template <int B> __device__ __forceinline__ bv<B> mul(const bm<B> &M, const bv<B> &x) {
+    bv<B> r;
+#pragma unroll
+    for (int i = 0; i < B; i++) {
+        double a = M.c[i * B] * x.c[0];
+#pragma unroll
+        for (int c = 1; c < B; c++) a = fma(M.c[i * B + c], x.c[c], a);
+        r.c[i] = a;
+    }
+    return r;
+}
+template <int B> __device__ __forceinline__ bv<B> vsub(const bv<B> &a, const bv<B> &b) {
+    bv<B> r;
+#pragma unroll
+    for (int k = 0; k < B; k++) r.c[k] = a.c[k] - b.c[k];
+    return r;
+}
+
+template <int B> struct gst {
+    bm<B> e[10];  // dl dc dr cl cc cr ul uc ur, inverse of cc (tgmg_level::s, tgmg.hh:256-265)
+    int nz;       // bit k set where off-diagonal block k is nonzero
     int pad;
 };
 
-struct glevel {
+template <int B> struct glevel {
     int m, n, xp, yp;
     int cx_n, cy_n;  // colours per direction: 2, or 3 on an odd periodic line
     const int *cls;
-    const gst *st;
-    double *z, *b, *r;
+    const gst<B> *st;
+    bv<B> *z, *b, *r;
 };
 
 constexpr int kMaxLevels = 17;
 constexpr int kGridMin = 10;        // tgmg_grid_min, tgmg_config.hh:23
-constexpr int kBottomDirect = 1024; // largest coarsest level solved by a dense inverse
+constexpr int kBottomDirect = 1024; // most unknowns of a coarsest level solved by a dense inverse
 constexpr int kRedBlocks = 4 * 152;
+constexpr int kRedThreads = 256;
 constexpr size_t kTailSmem = 200 * 1024; // shared memory of the single-block tail
 // Largest level the tail takes: one SM's FP64 pipe is slow (a 65 x 65
 // level alone kept the tail at ~120 us a cycle), so the tail starts at 33 x 33.
 constexpr long kTailPoints = 1200;
-constexpr int kRedThreads = 256;
 
 // Neighbour index on a line of m points, or -1 outside a non-periodic line.
 __host__ __device__ inline int nbr(int i, int d, int m, int prd) {
@@ -63,33 +105,42 @@ __host__ __device__ inline int nbr(int i, int d, int m, int prd) {
     return k;
 }
 
-// Off-diagonal product sum_k a_k z_k at (i, j) (tgmg_level::mul_a,
+// Off-diagonal product sum_k A_k z_k at (i, j) (tgmg_level::mul_a,
 // tgmg.in.cc:536-547); neighbours outside a non-periodic grid are skipped, and
-// so are zero entries (an integer test on the stencil's mask: the FP64 pipe,
+// so are zero blocks (an integer test on the stencil's mask: the FP64 pipe,
 // GB300's scarce one, only sees the nonzero products).
-__device__ __forceinline__ double offdiag(const glevel &L, const gst &s, int i, int j) {
+template <int B>
+__device__ __forceinline__ bv<B> offdiag(const glevel<B> &L, const gst<B> &s, int i, int j) {
     const int il = nbr(i, -1, L.m, L.xp), ir = nbr(i, 1, L.m, L.xp);
     const int jd = nbr(j, -1, L.n, L.yp), ju = nbr(j, 1, L.n, L.yp);
     const int nz = s.nz;
-    double a = 0;
+    bv<B> a = vzero<B>();
     if (jd >= 0) {
-        const double *zr = L.z + (size_t)jd * L.m;
-        if ((nz & 1) && il >= 0) a = fma(s.e[0], zr[il], a);
-        if (nz & 2) a = fma(s.e[1], zr[i], a);
-        if ((nz & 4) && ir >= 0) a = fma(s.e[2], zr[ir], a);
+        const bv<B> *zr = L.z + (size_t)jd * L.m;
+        if ((nz & 1) && il >= 0) madd(a, s.e[0], zr[il]);
+        if (nz & 2) madd(a, s.e[1], zr[i]);
+        if ((nz & 4) && ir >= 0) madd(a, s.e[2], zr[ir]);
     }
     {
-        const double *zr = L.z + (size_t)j * L.m;
-        if ((nz & 8) && il >= 0) a = fma(s.e[3], zr[il], a);
-        if ((nz & 32) && ir >= 0) a = fma(s.e[5], zr[ir], a);
+        const bv<B> *zr = L.z + (size_t)j * L.m;
+        if ((nz & 8) && il >= 0) madd(a, s.e[3], zr[il]);
+        if ((nz & 32) && ir >= 0) madd(a, s.e[5], zr[ir]);
     }
     if (ju >= 0) {
-        const double *zr = L.z + (size_t)ju * L.m;
-        if ((nz & 64) && il >= 0) a = fma(s.e[6], zr[il], a);
-        if (nz & 128) a = fma(s.e[7], zr[i], a);
-        if ((nz & 256) && ir >= 0) a = fma(s.e[8], zr[ir], a);
+        const bv<B> *zr = L.z + (size_t)ju * L.m;
+        if ((nz & 64) && il >= 0) madd(a, s.e[6], zr[il]);
+        if (nz & 128) madd(a, s.e[7], zr[i]);
+        if ((nz & 256) && ir >= 0) madd(a, s.e[8], zr[ir]);
     }
     return a;
+}
+
+// r = b - A z at (i, j)
+template <int B>
+__device__ __forceinline__ bv<B> residual_at(const glevel<B> &L, const gst<B> &s, size_t ij, int i, int j) {
+    bv<B> a = offdiag(L, s, i, j);
+    madd(a, s.e[4], L.z[ij]);
+    return vsub(L.b[ij], a);
 }
 
 // k-th line of colour c on a line of m points with cn colours: colour 0 the
@@ -102,35 +153,41 @@ __device__ __forceinline__ int color_line(int k, int c, int m, int cn) {
     return i;
 }
 
-// One colour of Gauss-Seidel (omega = 1) or SOR: z += omega (D^-1 (b - A'z) - z)
+// One colour of Gauss-Seidel or SOR: z += omega (D^-1 (b - A'z) - z)
 // (gauss_seidel, sor: tgmg.in.cc:128-230).
-template <bool Relax>
-__global__ void k_tg_color(glevel L, int cx, int cy, double omega) {
+template <int B, bool Relax>
+__global__ void k_tg_color(glevel<B> L, int cx, int cy, double omega) {
     const int i = color_line(blockIdx.x * blockDim.x + threadIdx.x, cx, L.m, L.cx_n);
     const int j = color_line(blockIdx.y * blockDim.y + threadIdx.y, cy, L.n, L.cy_n);
     if (i < 0 || j < 0) return;
     const size_t ij = (size_t)j * L.m + i;
-    const gst &s = L.st[L.cls[ij]];
-    const double t = s.e[9] * (L.b[ij] - offdiag(L, s, i, j));
-    L.z[ij] = Relax ? L.z[ij] + omega * (t - L.z[ij]) : t;
+    const gst<B> &s = L.st[L.cls[ij]];
+    const bv<B> t = mul(s.e[9], vsub(L.b[ij], offdiag(L, s, i, j)));
+    if (Relax) {
+        bv<B> z = L.z[ij];
+#pragma unroll
+        for (int k = 0; k < B; k++) z.c[k] += omega * (t.c[k] - z.c[k]);
+        L.z[ij] = z;
+    } else {
+        L.z[ij] = t;
+    }
 }
 
 // Jacobi update into r (jacobi, tgmg.in.cc:69-85); the caller copies r to z.
-__global__ void k_tg_jacobi(glevel L) {
+template <int B> __global__ void k_tg_jacobi(glevel<B> L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= L.m || j >= L.n) return;
     const size_t ij = (size_t)j * L.m + i;
-    const gst &s = L.st[L.cls[ij]];
-    L.r[ij] = s.e[9] * (L.b[ij] - offdiag(L, s, i, j));
+    const gst<B> &s = L.st[L.cls[ij]];
+    L.r[ij] = mul(s.e[9], vsub(L.b[ij], offdiag(L, s, i, j)));
 }
 
 // r = b - A z (tgmg_base::res, tgmg.hh:197-199).
-__global__ void k_tg_residual(glevel L) {
+template <int B> __global__ void k_tg_residual(glevel<B> L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= L.m || j >= L.n) return;
     const size_t ij = (size_t)j * L.m + i;
-    const gst &s = L.st[L.cls[ij]];
-    L.r[ij] = L.b[ij] - offdiag(L, s, i, j) - s.e[4] * L.z[ij];
+    L.r[ij] = residual_at(L, L.st[L.cls[ij]], ij, i, j);
 }
 
 // Fine line index 2I+d, wrapped on a periodic line; -1 outside.
@@ -147,30 +204,35 @@ __device__ __forceinline__ int fine_at(int I, int d, int m, int prd) {
 // 1/4 from the interpolation's halves in each direction, summed as
 // (sum over rows of hy * (sum over columns of hx * r)) / 4 with the factors 2
 // applied as additions.
-__device__ __forceinline__ double restrict_at(const glevel &F, const double *r, int I, int J) {
-    double acc = 0;
+template <int B>
+__device__ __forceinline__ bv<B> restrict_at(const glevel<B> &F, const bv<B> *r, int I, int J) {
+    bv<B> acc = vzero<B>();
 #pragma unroll
     for (int dy = -1; dy <= 1; dy++) {
         const int fy = fine_at(J, dy, F.n, F.yp);
         if (fy < 0) continue;
         const int hy = halves_of(fy, F.n, F.yp, J);
         if (!hy) continue;
-        const double *rr = r + (size_t)fy * F.m;
-        double row = 0;
+        const bv<B> *rr = r + (size_t)fy * F.m;
+        bv<B> row = vzero<B>();
 #pragma unroll
         for (int dx = -1; dx <= 1; dx++) {
             const int fx = fine_at(I, dx, F.m, F.xp);
             if (fx < 0) continue;
             const int hx = halves_of(fx, F.m, F.xp, I);
             if (!hx) continue;
-            row += hx == 2 ? rr[fx] + rr[fx] : rr[fx];
+#pragma unroll
+            for (int k = 0; k < B; k++) row.c[k] += hx == 2 ? rr[fx].c[k] + rr[fx].c[k] : rr[fx].c[k];
         }
-        acc += hy == 2 ? row + row : row;
+#pragma unroll
+        for (int k = 0; k < B; k++) acc.c[k] += hy == 2 ? row.c[k] + row.c[k] : row.c[k];
     }
-    return 0.25 * acc;
+#pragma unroll
+    for (int k = 0; k < B; k++) acc.c[k] *= 0.25;
+    return acc;
 }
 
-__global__ void k_tg_restrict(glevel F, glevel C) {
+template <int B> __global__ void k_tg_restrict(glevel<B> F, glevel<B> C) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y;
     if (I >= C.m || J >= C.n) return;
     C.b[(size_t)J * C.m + I] = restrict_at(F, F.r, I, J);
@@ -179,33 +241,43 @@ __global__ void k_tg_restrict(glevel F, glevel C) {
 // Interpolated child value at a parent point from the coarse indices of
 // p1d_halves: injection, the mean of two, or the mean of four (exact weights
 // 1, 1/2, 1/4 applied as one multiplication).
-__device__ __forceinline__ double interp_at(const glevel &C, int ny, const int *cy, int nx, const int *cx) {
-    const double *r0 = C.z + (size_t)cy[0] * C.m;
-    if (ny == 1) return nx == 1 ? r0[cx[0]] : 0.5 * (r0[cx[0]] + r0[cx[1]]);
-    const double *r1 = C.z + (size_t)cy[1] * C.m;
-    if (nx == 1) return 0.5 * (r0[cx[0]] + r1[cx[0]]);
-    return 0.25 * ((r0[cx[0]] + r0[cx[1]]) + (r1[cx[0]] + r1[cx[1]]));
+template <int B>
+__device__ __forceinline__ bv<B> interp_at(const glevel<B> &C, int ny, const int *cy, int nx, const int *cx) {
+    const bv<B> *r0 = C.z + (size_t)cy[0] * C.m, *r1 = C.z + (size_t)cy[ny - 1] * C.m;
+    bv<B> o;
+#pragma unroll
+    for (int k = 0; k < B; k++) {
+        if (ny == 1) o.c[k] = nx == 1 ? r0[cx[0]].c[k] : 0.5 * (r0[cx[0]].c[k] + r0[cx[1]].c[k]);
+        else if (nx == 1) o.c[k] = 0.5 * (r0[cx[0]].c[k] + r1[cx[0]].c[k]);
+        else o.c[k] = 0.25 * ((r0[cx[0]].c[k] + r0[cx[1]].c[k]) + (r1[cx[0]].c[k] + r1[cx[1]].c[k]));
+    }
+    return o;
 }
 
 // Parent z += P z_child (apply_t, tgmg.in.cc:552-606).
-__global__ void k_tg_prolong(glevel C, glevel F) {
+template <int B> __global__ void k_tg_prolong(glevel<B> C, glevel<B> F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= F.m || j >= F.n) return;
     int cy[2], hy[2], cx[2], hx[2];
     const int ny = p1d_halves(j, F.n, F.yp, cy, hy), nx = p1d_halves(i, F.m, F.xp, cx, hx);
-    F.z[(size_t)j * F.m + i] += interp_at(C, ny, cy, nx, cx);
+    const bv<B> a = interp_at(C, ny, cy, nx, cx);
+    bv<B> &z = F.z[(size_t)j * F.m + i];
+#pragma unroll
+    for (int k = 0; k < B; k++) z.c[k] += a.c[k];
 }
 
-// Coarsest level: z = A^-1 b with the dense FP64 inverse.
-__global__ void k_tg_bottom(glevel B, const double *__restrict__ inv, int N) {
+// Coarsest level: z = A^-1 b with the dense FP64 inverse over its N unknowns.
+template <int B> __global__ void k_tg_bottom(glevel<B> L, const double *__restrict__ inv, int N) {
     __shared__ double bb[kBottomDirect];
-    for (int k = threadIdx.x; k < N; k += blockDim.x) bb[k] = B.b[k];
+    const double *b = (const double *)L.b;
+    double *z = (double *)L.z;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) bb[k] = b[k];
     __syncthreads();
     for (int r = threadIdx.x; r < N; r += blockDim.x) {
         const double *row = inv + (size_t)r * N;
         double a = 0;
         for (int k = 0; k < N; k++) a += row[k] * bb[k];
-        B.z[r] = a;
+        z[r] = a;
     }
 }
 
@@ -224,15 +296,15 @@ __device__ __forceinline__ double block_reduce(double v, double *sh) {
     return t;
 }
 
-__global__ void k_tg_sqnorm(glevel L, double *partials) {
+template <int B> __global__ void k_tg_sqnorm(glevel<B> L, double *partials) {
     __shared__ double sh[32];
     const long mn = (long)L.m * L.n;
     double acc = 0;
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += (long)gridDim.x * blockDim.x) {
         const int j = (int)(k / L.m), i = (int)(k - (long)j * L.m);
-        const gst &s = L.st[L.cls[k]];
-        const double r = L.b[k] - offdiag(L, s, i, j) - s.e[4] * L.z[k];
-        acc += r * r;
+        const bv<B> r = residual_at(L, L.st[L.cls[k]], (size_t)k, i, j);
+#pragma unroll
+        for (int c = 0; c < B; c++) acc += r.c[c] * r.c[c];
     }
     const double t = block_reduce(acc, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = t;
@@ -254,14 +326,14 @@ __global__ void k_tg_sum(const double *partials, int np, double *out) {
 // and z of level t goes to global memory.  Phases are separated by
 // __syncthreads.
 
-struct tail_args {
+template <int B> struct tail_args {
     int t, L, cd, cu, hb, sym;
     const double *inv;
     int inv_n;
-    glevel lv[kMaxLevels];
+    glevel<B> lv[kMaxLevels];
 };
 
-__device__ void tail_sweep(const glevel &L, bool reverse) {
+template <int B> __device__ void tail_sweep(const glevel<B> &L, bool reverse) {
     const int nc = L.cx_n * L.cy_n;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
     const int kx = (L.m + 1) / 2, ky = (L.n + 1) / 2;
@@ -272,49 +344,49 @@ __device__ void tail_sweep(const glevel &L, bool reverse) {
             const int i = color_line(k % kx, cx, L.m, L.cx_n), j = color_line(k / kx, cy, L.n, L.cy_n);
             if (i < 0 || j < 0) continue;
             const size_t ij = (size_t)j * L.m + i;
-            const gst &s = L.st[L.cls[ij]];
-            L.z[ij] = s.e[9] * (L.b[ij] - offdiag(L, s, i, j));
+            const gst<B> &s = L.st[L.cls[ij]];
+            L.z[ij] = mul(s.e[9], vsub(L.b[ij], offdiag(L, s, i, j)));
         }
         __syncthreads();
     }
 }
 
-__device__ void tail_clear(const glevel &L) {
+template <int B> __device__ void tail_clear(const glevel<B> &L) {
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
-    for (int k = tid; k < L.m * L.n; k += nth) L.z[k] = 0;
+    for (int k = tid; k < L.m * L.n; k += nth) L.z[k] = vzero<B>();
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) k_tg_tail(tail_args a) {
+template <int B> __global__ void __launch_bounds__(1024) k_tg_tail(tail_args<B> a) {
     extern __shared__ __align__(16) double tsm[];
-    __shared__ glevel S[kMaxLevels];
+    __shared__ glevel<B> S[kMaxLevels];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
     if (tid == 0) {
         size_t off = 0;
+        bv<B> *base = (bv<B> *)tsm;
         for (int l = a.t; l <= a.L; l++) {
             S[l] = a.lv[l];
             const size_t mn = (size_t)S[l].m * S[l].n;
-            S[l].z = tsm + off;
-            S[l].b = tsm + off + mn;
-            S[l].r = tsm + off + 2 * mn;
+            S[l].z = base + off;
+            S[l].b = base + off + mn;
+            S[l].r = base + off + 2 * mn;
             off += 3 * mn;
         }
     }
     __syncthreads();
     {
-        const glevel &T = S[a.t];
+        const glevel<B> &T = S[a.t];
         for (int k = tid; k < T.m * T.n; k += nth) T.b[k] = a.lv[a.t].b[k];
         __syncthreads();
     }
     // down: levels t..L-1 (down_gs_iterations, then residual and restriction)
     for (int i = a.t; i < a.L; i++) {
-        const glevel &L = S[i], &C = S[i + 1];
+        const glevel<B> &L = S[i], &C = S[i + 1];
         tail_clear(L);
         for (int c = 0; c < a.cd; c++) tail_sweep(L, false);
         for (int k = tid; k < L.m * L.n; k += nth) {
             const int j = k / L.m, ii = k - j * L.m;
-            const gst &s = L.st[L.cls[k]];
-            L.r[k] = L.b[k] - offdiag(L, s, ii, j) - s.e[4] * L.z[k];
+            L.r[k] = residual_at(L, L.st[L.cls[k]], (size_t)k, ii, j);
         }
         __syncthreads();
         for (int k = tid; k < C.m * C.n; k += nth) {
@@ -325,34 +397,38 @@ __global__ void __launch_bounds__(1024) k_tg_tail(tail_args a) {
     }
     // coarsest level
     {
-        const glevel &B = S[a.L];
+        const glevel<B> &Bt = S[a.L];
         if (a.inv) {
+            const double *b = (const double *)Bt.b;
+            double *z = (double *)Bt.z;
             for (int r = tid; r < a.inv_n; r += nth) {
                 const double *row = a.inv + (size_t)r * a.inv_n;
                 double acc = 0;
-                for (int k = 0; k < a.inv_n; k++) acc += row[k] * B.b[k];
-                B.z[r] = acc;
+                for (int k = 0; k < a.inv_n; k++) acc += row[k] * b[k];
+                z[r] = acc;
             }
             __syncthreads();
         } else {
-            tail_clear(B);
-            for (int c = 0; c < 2 * a.hb; c++) tail_sweep(B, a.sym && c >= a.hb);
+            tail_clear(Bt);
+            for (int c = 0; c < 2 * a.hb; c++) tail_sweep(Bt, a.sym && c >= a.hb);
         }
     }
     // up: prolongation and up_gs_iterations on levels L-1..t
     for (int i = a.L; i > a.t; i--) {
-        const glevel &C = S[i], &F = S[i - 1];
+        const glevel<B> &C = S[i], &F = S[i - 1];
         for (int k = tid; k < F.m * F.n; k += nth) {
             const int j = k / F.m, ii = k - j * F.m;
             int cy[2], hy[2], cx[2], hx[2];
             const int ny = p1d_halves(j, F.n, F.yp, cy, hy), nx = p1d_halves(ii, F.m, F.xp, cx, hx);
-            F.z[k] += interp_at(C, ny, cy, nx, cx);
+            const bv<B> v = interp_at(C, ny, cy, nx, cx);
+#pragma unroll
+            for (int q = 0; q < B; q++) F.z[k].c[q] += v.c[q];
         }
         __syncthreads();
         for (int c = 0; c < a.cu; c++) tail_sweep(F, a.sym != 0);
     }
     {
-        const glevel &T = S[a.t];
+        const glevel<B> &T = S[a.t];
         for (int k = tid; k < T.m * T.n; k += nth) a.lv[a.t].z[k] = T.z[k];
     }
 }
@@ -360,10 +436,11 @@ __global__ void __launch_bounds__(1024) k_tg_tail(tail_args a) {
 // ---------------------------------------------------------------------------
 // Host side: hierarchy sizes, Galerkin products, dense coarsest inverse.
 
-struct host_level {
+template <int B> struct host_level {
     int m, n;
+    bool rows;  // the stencil depends on the row only
     std::vector<int> cls;
-    std::vector<gst> table;
+    std::vector<gst<B>> table;
 };
 
 // Child sizes (tgmg_base constructor, tgmg.hh:108-110) while the child has
@@ -399,17 +476,43 @@ inline int coarse_offset(int c, int C, int cm, int prd) {
     return o;
 }
 
-int nonzero_mask(const gst &s) {
+template <int B> bool block_zero(const bm<B> &a) {
+    for (int q = 0; q < B * B; q++)
+        if (a.c[q] != 0) return false;
+    return true;
+}
+
+template <int B> int nonzero_mask(const gst<B> &s) {
     int nz = 0;
     for (int k = 0; k < 9; k++)
-        if (k != 4 && s.e[k] != 0) nz |= 1 << k;
+        if (k != 4 && !block_zero(s.e[k])) nz |= 1 << k;
     return nz;
+}
+
+// Inverse of a block (the reference's operator/(double,mat), mat.hh).
+template <int B> bm<B> block_inverse(const bm<B> &a);
+template <> bm<1> block_inverse<1>(const bm<1> &a) {
+    bm<1> r;
+    r.c[0] = 1. / a.c[0];
+    return r;
+}
+template <> bm<2> block_inverse<2>(const bm<2> &f) {
+    const double idet = 1. / (f.c[0] * f.c[3] - f.c[1] * f.c[2]);
+    bm<2> r;
+    r.c[0] = f.c[3] * idet;
+    r.c[1] = -f.c[1] * idet;
+    r.c[2] = -f.c[2] * idet;
+    r.c[3] = f.c[0] * idet;
+    return r;
 }
 
 // Galerkin stencil at coarse point (I, J): sum over fine points k near
 // (2I, 2J) and their neighbours l of P(k, (I,J)) A(k, l) P(l, neighbour).
-gst rap_point(const host_level &F, int xp, int yp, int cm, int cn, int I, int J) {
-    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+template <int B>
+gst<B> rap_point(const host_level<B> &F, int xp, int yp, int cm, int cn, int I, int J) {
+    bm<B> acc[9];
+    for (int k = 0; k < 9; k++)
+        for (int q = 0; q < B * B; q++) acc[k].c[q] = 0;
     for (int dy = -1; dy <= 1; dy++) {
         const int fy = wrap_line(2 * J + dy, F.n, yp);
         if (fy < 0) continue;
@@ -420,83 +523,106 @@ gst rap_point(const host_level &F, int xp, int yp, int cm, int cn, int I, int J)
             if (fx < 0) continue;
             const double wx = pw(fx, F.m, xp, I);
             if (wx == 0) continue;
-            const gst &s = F.table[F.cls[(size_t)fy * F.m + fx]];
+            const gst<B> &s = F.table[F.cls[(size_t)fy * F.m + fx]];
             for (int sy = -1; sy <= 1; sy++) {
                 const int ly = wrap_line(fy + sy, F.n, yp);
                 if (ly < 0) continue;
                 for (int sx = -1; sx <= 1; sx++) {
                     const int lx = wrap_line(fx + sx, F.m, xp);
                     if (lx < 0) continue;
-                    const double a = s.e[(sy + 1) * 3 + sx + 1];
-                    if (a == 0) continue;
+                    const bm<B> &a = s.e[(sy + 1) * 3 + sx + 1];
+                    if (block_zero(a)) continue;
                     int cy[2], cx[2];
                     double wyl[2], wxl[2];
                     const int ny = p1d(ly, F.n, yp, cy, wyl), nx = p1d(lx, F.m, xp, cx, wxl);
                     for (int q = 0; q < ny; q++)
                         for (int p = 0; p < nx; p++) {
                             const int oy = coarse_offset(cy[q], J, cn, yp), ox = coarse_offset(cx[p], I, cm, xp);
-                            acc[(oy + 1) * 3 + ox + 1] += wx * wy * a * wxl[p] * wyl[q];
+                            bm<B> &t = acc[(oy + 1) * 3 + ox + 1];
+                            for (int e = 0; e < B * B; e++) t.c[e] += wx * wy * a.c[e] * wxl[p] * wyl[q];
                         }
                 }
             }
         }
     }
-    gst out = {};
+    gst<B> out;
+    std::memset(&out, 0, sizeof(out));
     for (int k = 0; k < 9; k++) out.e[k] = acc[k];
-    out.e[9] = 1. / acc[4];
+    out.e[9] = block_inverse<B>(acc[4]);
     out.nz = nonzero_mask(out);
     return out;
 }
 
-struct gst_hash {
-    size_t operator()(const gst &s) const {
+template <int B> struct gst_hash {
+    size_t operator()(const gst<B> &s) const {
         uint64_t h = 1469598103934665603ull;
         const unsigned char *p = (const unsigned char *)&s;
-        for (size_t k = 0; k < sizeof(gst); k++) h = (h ^ p[k]) * 1099511628211ull;
+        for (size_t k = 0; k < sizeof(gst<B>); k++) h = (h ^ p[k]) * 1099511628211ull;
         return (size_t)h;
     }
 };
-struct gst_eq {
-    bool operator()(const gst &a, const gst &b) const { return std::memcmp(&a, &b, sizeof(gst)) == 0; }
+template <int B> struct gst_eq {
+    bool operator()(const gst<B> &a, const gst<B> &b) const { return std::memcmp(&a, &b, sizeof(gst<B>)) == 0; }
 };
 
-host_level coarsen(const host_level &F, int xp, int yp, int cm, int cn) {
-    host_level C;
+// Child level.  A fine level whose stencil depends on the row only, on an
+// even periodic x line, coarsens uniformly: its child depends on the row
+// only too and one Galerkin product per row suffices.
+template <int B> host_level<B> coarsen(const host_level<B> &F, int xp, int yp, int cm, int cn) {
+    host_level<B> C;
     C.m = cm;
     C.n = cn;
-    std::vector<gst> all((size_t)cm * cn);
+    C.rows = F.rows && xp && (F.m % 2 == 0);
+    std::vector<gst<B>> all;
+    if (C.rows) {
+        all.resize(cn);
 #pragma omp parallel for schedule(static)
-    for (int J = 0; J < cn; J++)
-        for (int I = 0; I < cm; I++) all[(size_t)J * cm + I] = rap_point(F, xp, yp, cm, cn, I, J);
-    std::unordered_map<gst, int, gst_hash, gst_eq> index;
-    C.cls.resize(all.size());
+        for (int J = 0; J < cn; J++) all[J] = rap_point(F, xp, yp, cm, cn, 0, J);
+    } else {
+        all.resize((size_t)cm * cn);
+#pragma omp parallel for schedule(static)
+        for (int J = 0; J < cn; J++)
+            for (int I = 0; I < cm; I++) all[(size_t)J * cm + I] = rap_point(F, xp, yp, cm, cn, I, J);
+    }
+    std::unordered_map<gst<B>, int, gst_hash<B>, gst_eq<B>> index;
+    std::vector<int> ids(all.size());
     for (size_t k = 0; k < all.size(); k++) {
         auto it = index.find(all[k]);
         if (it == index.end()) {
             it = index.emplace(all[k], (int)C.table.size()).first;
             C.table.push_back(all[k]);
         }
-        C.cls[k] = it->second;
+        ids[k] = it->second;
+    }
+    if (C.rows) {
+        C.cls.resize((size_t)cm * cn);
+        for (int J = 0; J < cn; J++)
+            for (int I = 0; I < cm; I++) C.cls[(size_t)J * cm + I] = ids[J];
+    } else {
+        C.cls.swap(ids);
     }
     return C;
 }
 
 // Dense inverse by Gauss-Jordan elimination with partial pivoting; empty if
-// singular.
-std::vector<double> dense_inverse(const host_level &L, int xp, int yp) {
-    const int N = L.m * L.n;
+// singular.  Unknown B*(j*m+i)+c.
+template <int B> std::vector<double> dense_inverse(const host_level<B> &L, int xp, int yp) {
+    const int N = B * L.m * L.n;
     std::vector<double> A((size_t)N * N, 0.0), X((size_t)N * N, 0.0);
     for (int j = 0; j < L.n; j++)
         for (int i = 0; i < L.m; i++) {
-            const int r = j * L.m + i;
-            const gst &s = L.table[L.cls[r]];
+            const int p = j * L.m + i;
+            const gst<B> &s = L.table[L.cls[p]];
             for (int sy = -1; sy <= 1; sy++) {
                 const int ly = wrap_line(j + sy, L.n, yp);
                 if (ly < 0) continue;
                 for (int sx = -1; sx <= 1; sx++) {
                     const int lx = wrap_line(i + sx, L.m, xp);
                     if (lx < 0) continue;
-                    A[(size_t)r * N + ly * L.m + lx] += s.e[(sy + 1) * 3 + sx + 1];
+                    const bm<B> &a = s.e[(sy + 1) * 3 + sx + 1];
+                    const int q = ly * L.m + lx;
+                    for (int r = 0; r < B; r++)
+                        for (int c = 0; c < B; c++) A[(size_t)(B * p + r) * N + B * q + c] += a.c[r * B + c];
                 }
             }
         }
@@ -531,25 +657,24 @@ std::vector<double> dense_inverse(const host_level &L, int xp, int yp) {
 
 inline dim3 grid_of(int m, int n, dim3 b) { return dim3(ceil_div(m, b.x), ceil_div(n, b.y)); }
 
-}  // namespace
-}  // namespace stzg
+// ---------------------------------------------------------------------------
+// The solver state of one handle, for B components per point.
 
-using namespace stzg;
-
-struct stzg_tgmg {
+template <int B> struct tg {
     int device = 0;
     int xp = 0, yp = 0;
     double acc = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int nl = 0;
-    glevel lv[kMaxLevels];
-    std::vector<host_level> host;
+    glevel<B> lv[kMaxLevels];
+    std::vector<host_level<B>> host;
     std::vector<void *> owned;
-    double *inv = nullptr;
+    size_t st_cap[kMaxLevels] = {0};
+    double *inv = nullptr, *inv_buf = nullptr;
     int inv_n = 0;
+    size_t inv_cap = 0;
     int tail_start = 1 << 30;  // first level handled by k_tg_tail (none if > nl-1)
-    size_t tail_smem = 0;
     double *partials = nullptr, *dsum = nullptr, *hsum = nullptr;
     // graph of one iteration of the last (type, omega, cycles) used
     cudaGraphExec_t gexec = nullptr;
@@ -561,9 +686,7 @@ struct stzg_tgmg {
     long kernels = 0;
 };
 
-namespace {
-
-int g_alloc(stzg_tgmg *g, void **p, size_t bytes) {
+template <int B> int g_alloc(tg<B> *g, void **p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
     g->owned.push_back(*p);
@@ -571,67 +694,73 @@ int g_alloc(stzg_tgmg *g, void **p, size_t bytes) {
     return STZG_OK;
 }
 
-void launch_note(stzg_tgmg *g) {
+template <int B> void launch_note(tg<B> *g) {
     g->kernels++;
     note_launch();
 }
 
 const dim3 kBlk(32, 8);
 
-void sweep(stzg_tgmg *g, const glevel &L, bool reverse, double omega) {
+template <int B> void sweep(tg<B> *g, const glevel<B> &L, bool reverse, double omega) {
     const int nc = L.cx_n * L.cy_n;
     for (int q = 0; q < nc; q++) {
         const int c = reverse ? nc - 1 - q : q;
         const int cy = c / L.cx_n, cx = c % L.cx_n;
         const dim3 gr = grid_of((L.m + 1) / 2, (L.n + 1) / 2, kBlk);
-        if (omega == 1.0) k_tg_color<false><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
-        else k_tg_color<true><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
+        if (omega == 1.0) k_tg_color<B, false><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
+        else k_tg_color<B, true><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
         launch_note(g);
     }
 }
 
-void clear_z(stzg_tgmg *g, const glevel &L) {
-    cudaMemsetAsync(L.z, 0, sizeof(double) * (size_t)L.m * L.n, g->st);
+template <int B> void clear_z(tg<B> *g, const glevel<B> &L) {
+    cudaMemsetAsync(L.z, 0, sizeof(bv<B>) * (size_t)L.m * L.n, g->st);
 }
 
 // down_gs_iterations (tgmg.hh:273-279): clear z, then cyc sweeps (the first
 // from zero).
-void down_gs(stzg_tgmg *g, const glevel &L, int cyc) {
+template <int B> void down_gs(tg<B> *g, const glevel<B> &L, int cyc) {
     clear_z(g, L);
     for (int c = 0; c < cyc; c++) sweep(g, L, false, 1.0);
 }
 
 // up_gs_iterations (tgmg.hh:183-187): cyc sweeps, reversed when symmetric.
-void up_gs(stzg_tgmg *g, const glevel &L, int cyc, bool sym) {
+template <int B> void up_gs(tg<B> *g, const glevel<B> &L, int cyc, bool sym) {
     for (int c = 0; c < cyc; c++) sweep(g, L, sym, 1.0);
 }
 
-void restrict_to(stzg_tgmg *g, const glevel &F, const glevel &C) {
-    k_tg_residual<<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(F);
+template <int B> void restrict_to(tg<B> *g, const glevel<B> &F, const glevel<B> &C) {
+    k_tg_residual<B><<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(F);
     launch_note(g);
-    k_tg_restrict<<<grid_of(C.m, C.n, kBlk), kBlk, 0, g->st>>>(F, C);
+    k_tg_restrict<B><<<grid_of(C.m, C.n, kBlk), kBlk, 0, g->st>>>(F, C);
     launch_note(g);
 }
 
-void prolong(stzg_tgmg *g, const glevel &C, const glevel &F) {
-    k_tg_prolong<<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(C, F);
+template <int B> void prolong(tg<B> *g, const glevel<B> &C, const glevel<B> &F) {
+    k_tg_prolong<B><<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(C, F);
     launch_note(g);
 }
 
 // Coarsest level: the reference's hcyc_bottom sweeps down and up
 // (tgmg.in.cc:350-352), replaced by the exact solve where it is available.
-void bottom(stzg_tgmg *g, const glevel &B, int hcyc, bool sym) {
+template <int B> void bottom(tg<B> *g, const glevel<B> &Bt, int hcyc, bool sym) {
     if (g->inv) {
-        k_tg_bottom<<<1, 256, 0, g->st>>>(B, g->inv, g->inv_n);
+        k_tg_bottom<B><<<1, 256, 0, g->st>>>(Bt, g->inv, g->inv_n);
         launch_note(g);
     } else {
-        down_gs(g, B, hcyc);
-        up_gs(g, B, hcyc, sym);
+        down_gs(g, Bt, hcyc);
+        up_gs(g, Bt, hcyc, sym);
     }
 }
 
-void tail(stzg_tgmg *g, int i, int cd, int cu, int hb, bool sym) {
-    tail_args a;
+template <int B> size_t tail_bytes(const tg<B> *g, int i) {
+    size_t smem = 0;
+    for (int l = i; l < g->nl; l++) smem += 3 * sizeof(bv<B>) * (size_t)g->lv[l].m * g->lv[l].n;
+    return smem;
+}
+
+template <int B> void tail(tg<B> *g, int i, int cd, int cu, int hb, bool sym) {
+    tail_args<B> a;
     a.t = i;
     a.L = g->nl - 1;
     a.cd = cd;
@@ -641,9 +770,7 @@ void tail(stzg_tgmg *g, int i, int cd, int cu, int hb, bool sym) {
     a.inv = g->inv;
     a.inv_n = g->inv_n;
     for (int l = 0; l < g->nl; l++) a.lv[l] = g->lv[l];
-    size_t smem = 0;
-    for (int l = i; l < g->nl; l++) smem += 3 * sizeof(double) * (size_t)g->lv[l].m * g->lv[l].n;
-    k_tg_tail<<<1, dim3(32, 32), smem, g->st>>>(a);
+    k_tg_tail<B><<<1, dim3(32, 32), tail_bytes(g, i), g->st>>>(a);
     launch_note(g);
 }
 
@@ -651,7 +778,7 @@ void tail(stzg_tgmg *g, int i, int cd, int cu, int hb, bool sym) {
 // below, prolongation, up_gs; the coarsest level is the bottom solve.  This
 // is v_cycle_internal (tgmg.in.cc:341-359) written recursively; levels from
 // tail_start down run in one k_tg_tail launch.
-void vc(stzg_tgmg *g, int i, int cd, int cu, int hb, bool sym) {
+template <int B> void vc(tg<B> *g, int i, int cd, int cu, int hb, bool sym) {
     const int L = g->nl - 1;
     if (i == L) {
         bottom(g, g->lv[L], hb, sym);
@@ -670,7 +797,7 @@ void vc(stzg_tgmg *g, int i, int cd, int cu, int hb, bool sym) {
 
 // v_cycle_internal from a level whose z has had its down sweeps: restrict,
 // cycle below, prolong, up sweeps.
-void internal(stzg_tgmg *g, int level, int cd, int cu, int hb, bool sym) {
+template <int B> void internal(tg<B> *g, int level, int cd, int cu, int hb, bool sym) {
     restrict_to(g, g->lv[level], g->lv[level + 1]);
     vc(g, level + 1, cd, cu, hb, sym);
     prolong(g, g->lv[level + 1], g->lv[level]);
@@ -678,7 +805,7 @@ void internal(stzg_tgmg *g, int level, int cd, int cu, int hb, bool sym) {
 }
 
 // tgmg::v_cycle (tgmg.in.cc:313-328).
-void v_cycle(stzg_tgmg *g, int cd, int cu, int hb, bool sym) {
+template <int B> void v_cycle(tg<B> *g, int cd, int cu, int hb, bool sym) {
     for (int c = 0; c < cd; c++) sweep(g, g->lv[0], false, 1.0);
     if (g->nl > 1) {
         restrict_to(g, g->lv[0], g->lv[1]);
@@ -689,7 +816,7 @@ void v_cycle(stzg_tgmg *g, int cd, int cu, int hb, bool sym) {
 }
 
 // tgmg::fmg_pre (tgmg.in.cc:369-402).
-void fmg_pre(stzg_tgmg *g, int cd, int cu, int hb, bool sym) {
+template <int B> void fmg_pre(tg<B> *g, int cd, int cu, int hb, bool sym) {
     const int L = g->nl - 1;
     for (int c = 0; c < cd; c++) sweep(g, g->lv[0], false, 1.0);
     if (L > 0) {
@@ -711,13 +838,13 @@ void fmg_pre(stzg_tgmg *g, int cd, int cu, int hb, bool sym) {
 }
 
 // One iteration of a solver type (tgmg::iters, tgmg.hh:457-466).
-void one_iteration(stzg_tgmg *g, int type, double omega, int cd, int cu, int hb) {
-    const glevel &T = g->lv[0];
+template <int B> void one_iteration(tg<B> *g, int type, double omega, int cd, int cu, int hb) {
+    const glevel<B> &T = g->lv[0];
     switch (type) {
         case STZG_TGMG_JACOBI:
-            k_tg_jacobi<<<grid_of(T.m, T.n, kBlk), kBlk, 0, g->st>>>(T);
+            k_tg_jacobi<B><<<grid_of(T.m, T.n, kBlk), kBlk, 0, g->st>>>(T);
             launch_note(g);
-            cudaMemcpyAsync(T.z, T.r, sizeof(double) * (size_t)T.m * T.n, cudaMemcpyDeviceToDevice, g->st);
+            cudaMemcpyAsync(T.z, T.r, sizeof(bv<B>) * (size_t)T.m * T.n, cudaMemcpyDeviceToDevice, g->st);
             break;
         case STZG_TGMG_GS: sweep(g, T, false, 1.0); break;
         case STZG_TGMG_SOR: sweep(g, T, false, omega); break;
@@ -730,14 +857,17 @@ void one_iteration(stzg_tgmg *g, int type, double omega, int cd, int cu, int hb)
     }
 }
 
-int run_iterations(stzg_tgmg *g, int type, int count, double omega, int cd, int cu, int hb) {
+template <int B> void drop_graph(tg<B> *g) {
+    if (g->gexec) cudaGraphExecDestroy(g->gexec);
+    g->gexec = nullptr;
+    g->gkey[0] = -1;
+}
+
+template <int B> int run_iterations(tg<B> *g, int type, int count, double omega, int cd, int cu, int hb) {
     if (count <= 0) return STZG_OK;
     const int key[5] = {type, cd, cu, hb, 1};
     if (!g->gexec || std::memcmp(key, g->gkey, sizeof(key)) != 0 || g->gomega != omega) {
-        if (g->gexec) {
-            cudaGraphExecDestroy(g->gexec);
-            g->gexec = nullptr;
-        }
+        drop_graph(g);
         const long k0 = g->kernels;
         const long n0 = launch_count();
         cudaGraph_t graph;
@@ -762,9 +892,9 @@ int run_iterations(stzg_tgmg *g, int type, int count, double omega, int cd, int 
 }
 
 // l2_error = mds / mn (tgmg.hh:146).
-int l2_error(stzg_tgmg *g, double *err) {
-    const glevel &T = g->lv[0];
-    k_tg_sqnorm<<<kRedBlocks, kRedThreads, 0, g->st>>>(T, g->partials);
+template <int B> int l2_error(tg<B> *g, double *err) {
+    const glevel<B> &T = g->lv[0];
+    k_tg_sqnorm<B><<<kRedBlocks, kRedThreads, 0, g->st>>>(T, g->partials);
     launch_note(g);
     k_tg_sum<<<1, 256, 0, g->st>>>(g->partials, kRedBlocks, g->dsum);
     launch_note(g);
@@ -776,10 +906,10 @@ int l2_error(stzg_tgmg *g, double *err) {
 
 bool valid_type(int t) { return t >= STZG_TGMG_JACOBI && t <= STZG_TGMG_SYM_VCYCLE; }
 
-struct timed {
-    stzg_tgmg *g;
+template <int B> struct timed {
+    tg<B> *g;
     long k0;
-    explicit timed(stzg_tgmg *g_) : g(g_), k0(g_->kernels) { cudaEventRecord(g->ev0, g->st); }
+    explicit timed(tg<B> *g_) : g(g_), k0(g_->kernels) { cudaEventRecord(g->ev0, g->st); }
     void done() {
         cudaEventRecord(g->ev1, g->st);
         cudaEventSynchronize(g->ev1);
@@ -789,6 +919,290 @@ struct timed {
         g->last_kernels = g->kernels - k0;
     }
 };
+
+// Top level from the problem's table (9 blocks per stencil, B*B doubles each).
+template <int B> int top_level(int m, int n, const double *table, int ntable, const int *cls, host_level<B> &top) {
+    const size_t mn = (size_t)m * n;
+    for (size_t k = 0; k < mn; k++)
+        if (cls[k] < 0 || cls[k] >= ntable) return fail(STZG_EINVAL, "stencil index out of range");
+    top.m = m;
+    top.n = n;
+    top.cls.assign(cls, cls + mn);
+    top.table.resize(ntable);
+    std::memset(top.table.data(), 0, sizeof(gst<B>) * ntable);
+    for (int c = 0; c < ntable; c++) {
+        for (int k = 0; k < 9; k++)
+            for (int q = 0; q < B * B; q++) top.table[c].e[k].c[q] = table[((size_t)c * 9 + k) * B * B + q];
+        if (block_zero(top.table[c].e[4])) return fail(STZG_EINVAL, "zero diagonal block");
+        top.table[c].e[9] = block_inverse<B>(top.table[c].e[4]);
+        top.table[c].nz = nonzero_mask(top.table[c]);
+    }
+    top.rows = true;
+    for (int j = 0; j < n && top.rows; j++)
+        for (int i = 1; i < m; i++)
+            if (cls[(size_t)j * m + i] != cls[(size_t)j * m]) {
+                top.rows = false;
+                break;
+            }
+    return STZG_OK;
+}
+
+// Galerkin hierarchy below the top and its upload (tables grow as needed;
+// sizes and z/b/r stay).  Also the dense coarsest inverse.
+template <int B> int build_hierarchy(tg<B> *g) {
+    const std::vector<std::pair<int, int>> sizes = level_sizes(g->host[0].m, g->host[0].n, g->xp, g->yp);
+    g->host.resize(1);
+    for (size_t l = 1; l < sizes.size(); l++)
+        g->host.push_back(coarsen(g->host[l - 1], g->xp, g->yp, sizes[l].first, sizes[l].second));
+    for (int l = 0; l < g->nl; l++) {
+        const host_level<B> &H = g->host[l];
+        glevel<B> &L = g->lv[l];
+        const size_t pts = (size_t)H.m * H.n;
+        STZG_CUDA(cudaMemcpyAsync((void *)L.cls, H.cls.data(), pts * sizeof(int), cudaMemcpyHostToDevice, g->st));
+        if (H.table.size() > g->st_cap[l]) {
+            void *p;
+            STZG_CHECK(g_alloc(g, &p, H.table.size() * sizeof(gst<B>)));
+            L.st = (const gst<B> *)p;
+            g->st_cap[l] = H.table.size();
+        }
+        STZG_CUDA(cudaMemcpyAsync((void *)L.st, H.table.data(), H.table.size() * sizeof(gst<B>),
+                                  cudaMemcpyHostToDevice, g->st));
+    }
+    const host_level<B> &Bt = g->host.back();
+    g->inv = nullptr;
+    g->inv_n = 0;
+    if (g->nl > 1 && (long)B * Bt.m * Bt.n <= kBottomDirect) {
+        std::vector<double> inv = dense_inverse(Bt, g->xp, g->yp);
+        if (!inv.empty()) {
+            if (inv.size() > g->inv_cap) {
+                void *p;
+                STZG_CHECK(g_alloc(g, &p, inv.size() * sizeof(double)));
+                g->inv_buf = (double *)p;
+                g->inv_cap = inv.size();
+            }
+            g->inv = g->inv_buf;
+            g->inv_n = B * Bt.m * Bt.n;
+            STZG_CUDA(cudaMemcpyAsync(g->inv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                      g->st));
+        }
+    }
+    STZG_CUDA(cudaStreamSynchronize(g->st));  // the host vectors are uploaded before they go
+    return STZG_OK;
+}
+
+}  // namespace
+}  // namespace stzg
+
+using namespace stzg;
+
+struct stzg_tgmg {
+    int B = 1;
+    tg<1> *s1 = nullptr;
+    tg<2> *s2 = nullptr;
+};
+
+namespace {
+
+template <int B> void tg_destroy(tg<B> *g) {
+    if (!g) return;
+    cudaSetDevice(g->device);
+    if (g->st) cudaStreamSynchronize(g->st);
+    drop_graph(g);
+    for (void *p : g->owned) cudaFree(p);
+    if (g->hsum) cudaFreeHost(g->hsum);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->st) cudaStreamDestroy(g->st);
+    delete g;
+}
+
+template <int B>
+int tg_create(int m, int n, int xp, int yp, const double *table, int ntable, const int *cls, double acc, int device,
+              tg<B> **out) {
+    tg<B> *g = new tg<B>;
+    g->device = device;
+    g->xp = xp ? 1 : 0;
+    g->yp = yp ? 1 : 0;
+    g->acc = acc;
+    auto bail = [&](int st) {
+        tg_destroy(g);
+        return st;
+    };
+    if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess)
+        return bail(fail(STZG_ECUDA, "stream/event creation failed"));
+    host_level<B> top;
+    int st;
+    if ((st = top_level<B>(m, n, table, ntable, cls, top)) != STZG_OK) return bail(st);
+    g->host.push_back(top);
+    const std::vector<std::pair<int, int>> sizes = level_sizes(m, n, g->xp, g->yp);
+    g->nl = (int)sizes.size();
+    for (int l = 0; l < g->nl; l++) {
+        glevel<B> &L = g->lv[l];
+        L.m = sizes[l].first;
+        L.n = sizes[l].second;
+        L.xp = g->xp;
+        L.yp = g->yp;
+        L.cx_n = (g->xp && (L.m & 1)) ? 3 : 2;
+        L.cy_n = (g->yp && (L.n & 1)) ? 3 : 2;
+        const size_t pts = (size_t)L.m * L.n;
+        void *p;
+        if ((st = g_alloc(g, &p, pts * sizeof(bv<B>))) != STZG_OK) return bail(st);
+        L.z = (bv<B> *)p;
+        if ((st = g_alloc(g, &p, pts * sizeof(bv<B>))) != STZG_OK) return bail(st);
+        L.b = (bv<B> *)p;
+        if ((st = g_alloc(g, &p, pts * sizeof(bv<B>))) != STZG_OK) return bail(st);
+        L.r = (bv<B> *)p;
+        if ((st = g_alloc(g, &p, pts * sizeof(int))) != STZG_OK) return bail(st);
+        L.cls = (const int *)p;
+        L.st = nullptr;
+    }
+    if ((st = build_hierarchy(g)) != STZG_OK) return bail(st);
+    // single-block tail: the small levels that fit in its shared memory
+    // together, if they are at least two (the coarsest alone is the bottom)
+    {
+        size_t bytes = 0;
+        int t = g->nl;
+        for (int l = g->nl - 1; l >= 1; l--) {
+            const long pts = (long)g->lv[l].m * g->lv[l].n;
+            const size_t b = 3 * sizeof(bv<B>) * (size_t)pts;
+            if (pts > kTailPoints || bytes + b > kTailSmem) break;
+            bytes += b;
+            t = l;
+        }
+        if (t <= g->nl - 2) {
+            if (cudaFuncSetAttribute(k_tg_tail<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
+                cudaSuccess)
+                return bail(fail(STZG_ECUDA, "tail kernel attribute"));
+            g->tail_start = t;
+        }
+    }
+    {
+        void *p;
+        if ((st = g_alloc(g, &p, kRedBlocks * sizeof(double))) != STZG_OK) return bail(st);
+        g->partials = (double *)p;
+        if ((st = g_alloc(g, &p, sizeof(double))) != STZG_OK) return bail(st);
+        g->dsum = (double *)p;
+        if (cudaMallocHost(&p, sizeof(double)) != cudaSuccess) return bail(fail(STZG_ENOMEM, "pinned allocation"));
+        g->hsum = (double *)p;
+    }
+    if (cudaStreamSynchronize(g->st) != cudaSuccess) return bail(fail(STZG_ECUDA, "setup failed"));
+    *out = g;
+    return STZG_OK;
+}
+
+template <int B> int tg_set_operator(tg<B> *g, const double *table, int ntable, const int *cls) {
+    host_level<B> top;
+    STZG_CHECK(top_level<B>(g->host[0].m, g->host[0].n, table, ntable, cls, top));
+    STZG_CUDA(cudaStreamSynchronize(g->st));
+    g->host[0] = top;
+    drop_graph(g);  // table pointers and the coarsest inverse may have moved
+    return build_hierarchy(g);
+}
+
+template <int B> int tg_copy(tg<B> *g, bv<B> *dev, const double *src, double *dst) {
+    const size_t bytes = sizeof(bv<B>) * (size_t)g->lv[0].m * g->lv[0].n;
+    if (src) STZG_CUDA(cudaMemcpyAsync(dev, src, bytes, cudaMemcpyHostToDevice, g->st));
+    else STZG_CUDA(cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, g->st));
+    STZG_CUDA(cudaStreamSynchronize(g->st));
+    return STZG_OK;
+}
+
+template <int B>
+int tg_solve(tg<B> *g, int type, stzg_tgmg_predict *tp, double omega, int cd, int cu, int hb, int *iters,
+             double *l2) {
+    timed<B> t(g);
+    // tgmg::solve(type, tgmg_predict&, ...), tgmg.in.cc:266-301
+    int nit = tp->lim / tp->mult;
+    STZG_CHECK(run_iterations(g, type, nit, omega, cd, cu, hb));
+    double acc;
+    STZG_CHECK(l2_error(g, &acc));
+    if (acc < g->acc) {
+        if (tp->lim > 0) tp->lim -= 1 + tp->lim / tp->decay;
+    } else {
+        int k = 0;
+        do {
+            tp->lim += ++k * tp->mult;
+            if (tp->lim > tp->max_thresh) {
+                t.done();
+                if (l2) *l2 = acc;
+                return fail(STZG_ENOTCONV, "tgmg did not converge");
+            }
+            nit += k;
+            STZG_CHECK(run_iterations(g, type, k, omega, cd, cu, hb));
+            STZG_CHECK(l2_error(g, &acc));
+        } while (acc >= g->acc && !std::isnan(acc));
+    }
+    tp->solves++;
+    tp->vcount += nit;
+    STZG_CHECK(run_iterations(g, type, tp->extra_iters, omega, cd, cu, hb));
+    t.done();
+    if (iters) *iters = nit;
+    if (l2) *l2 = acc;
+    if (std::isnan(acc)) return fail(STZG_ENAN, "NaN residual");
+    return STZG_OK;
+}
+
+template <int B>
+int tg_solve_fixed(tg<B> *g, int type, int per_loop, int max_loops, double omega, int cd, int cu, int hb,
+                   int *iters, double *l2) {
+    timed<B> t(g);
+    // tgmg::solve(type, per_loop, max_loops, ...), tgmg.in.cc:182-197
+    double acc = 0;
+    int nloop = 0;
+    do {
+        if (++nloop == max_loops) {
+            t.done();
+            if (iters) *iters = nloop * per_loop;
+            if (l2) *l2 = acc;
+            return fail(STZG_ENOTCONV, "tgmg did not converge");
+        }
+        STZG_CHECK(run_iterations(g, type, per_loop, omega, cd, cu, hb));
+        STZG_CHECK(l2_error(g, &acc));
+    } while (acc > g->acc && !std::isnan(acc));
+    t.done();
+    if (iters) *iters = nloop * per_loop;
+    if (l2) *l2 = acc;
+    if (std::isnan(acc)) return fail(STZG_ENAN, "NaN residual");
+    return STZG_OK;
+}
+
+template <int B> int tg_iterate(tg<B> *g, int type, int count, double omega, int cd, int cu, int hb) {
+    timed<B> t(g);
+    STZG_CHECK(run_iterations(g, type, count, omega, cd, cu, hb));
+    t.done();
+    STZG_CUDA(cudaGetLastError());
+    return STZG_OK;
+}
+
+template <int B> int tg_levels(tg<B> *g, int *nlevels, int *dims) {
+    *nlevels = g->nl;
+    if (dims)
+        for (int l = 0; l < g->nl; l++) {
+            dims[2 * l] = g->lv[l].m;
+            dims[2 * l + 1] = g->lv[l].n;
+        }
+    return STZG_OK;
+}
+
+template <int B> int tg_stencil(tg<B> *g, int level, double *out) {
+    if (level < 1 || level >= g->nl) return fail(STZG_EINVAL, "bad level");
+    const host_level<B> &H = g->host[level];
+    const size_t pts = (size_t)H.m * H.n, per = 10 * B * B;
+    for (size_t k = 0; k < pts; k++) std::memcpy(out + per * k, H.table[H.cls[k]].e, per * sizeof(double));
+    return STZG_OK;
+}
+
+// Calls f on the handle's state with its block size.
+template <typename F> int dispatch(stzg_tgmg *g, F f) {
+    if (!g) return fail(STZG_EINVAL, "null handle");
+    if (g->B == 1) {
+        STZG_CUDA(cudaSetDevice(g->s1->device));
+        return f(g->s1);
+    }
+    STZG_CUDA(cudaSetDevice(g->s2->device));
+    return f(g->s2);
+}
 
 }  // namespace
 
@@ -824,266 +1238,132 @@ int stzg_poisson_fd(int m, int n, double ax, double bx, double ay, double by, do
     return STZG_OK;
 }
 
-int stzg_tgmg_create(int m, int n, int x_prd, int y_prd, const double *table, int ntable, const int *cls,
-                     double acc, int device, stzg_tgmg **out) {
+int stzg_tgmg_create_block(int m, int n, int x_prd, int y_prd, int block, const double *table, int ntable,
+                           const int *cls, double acc, int device, stzg_tgmg **out) {
     if (!out) return fail(STZG_EINVAL, "null handle pointer");
     *out = nullptr;
+    if (block != 1 && block != 2) return fail(STZG_EINVAL, "block must be 1 or 2");
     if (m < 1 || n < 1 || !table || ntable < 1 || !cls) return fail(STZG_EINVAL, "bad grid or operator");
     if ((x_prd && m < 3) || (y_prd && n < 3)) return fail(STZG_EINVAL, "a periodic direction needs >= 3 points");
     if (!(acc >= 0)) return fail(STZG_EINVAL, "acc must be >= 0");
     const size_t mn = (size_t)m * n;
     for (size_t k = 0; k < mn; k++)
         if (cls[k] < 0 || cls[k] >= ntable) return fail(STZG_EINVAL, "stencil index out of range");
-    for (int c = 0; c < ntable; c++)
-        if (table[9 * c + 4] == 0) return fail(STZG_EINVAL, "zero diagonal entry");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(STZG_ENODEV, "no CUDA device");
     if (device < 0 || device >= ndev) return fail(STZG_EINVAL, "device ordinal out of range");
     STZG_CUDA(cudaSetDevice(device));
     stzg_tgmg *g = new stzg_tgmg;
-    g->device = device;
-    g->xp = x_prd ? 1 : 0;
-    g->yp = y_prd ? 1 : 0;
-    g->acc = acc;
-    auto bail = [&](int st) {
-        stzg_tgmg_destroy(g);
+    g->B = block;
+    const int st = block == 1 ? tg_create<1>(m, n, x_prd, y_prd, table, ntable, cls, acc, device, &g->s1)
+                              : tg_create<2>(m, n, x_prd, y_prd, table, ntable, cls, acc, device, &g->s2);
+    if (st != STZG_OK) {
+        delete g;
         return st;
-    };
-    if (cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&g->ev0) != cudaSuccess || cudaEventCreate(&g->ev1) != cudaSuccess)
-        return bail(fail(STZG_ECUDA, "stream/event creation failed"));
-    // host hierarchy: the problem's operator, then Galerkin products
-    host_level top;
-    top.m = m;
-    top.n = n;
-    top.cls.assign(cls, cls + mn);
-    top.table.assign(ntable, gst{});
-    for (int c = 0; c < ntable; c++) {
-        for (int k = 0; k < 9; k++) top.table[c].e[k] = table[9 * c + k];
-        top.table[c].e[9] = 1. / table[9 * c + 4];
-        top.table[c].nz = nonzero_mask(top.table[c]);
     }
-    g->host.push_back(top);
-    const std::vector<std::pair<int, int>> sizes = level_sizes(m, n, g->xp, g->yp);
-    for (size_t l = 1; l < sizes.size(); l++)
-        g->host.push_back(coarsen(g->host[l - 1], g->xp, g->yp, sizes[l].first, sizes[l].second));
-    g->nl = (int)g->host.size();
-    for (int l = 0; l < g->nl; l++) {
-        const host_level &H = g->host[l];
-        glevel &L = g->lv[l];
-        L.m = H.m;
-        L.n = H.n;
-        L.xp = g->xp;
-        L.yp = g->yp;
-        L.cx_n = (g->xp && (H.m & 1)) ? 3 : 2;
-        L.cy_n = (g->yp && (H.n & 1)) ? 3 : 2;
-        const size_t pts = (size_t)H.m * H.n;
-        void *p;
-        int st;
-        if ((st = g_alloc(g, &p, pts * sizeof(double))) != STZG_OK) return bail(st);
-        L.z = (double *)p;
-        if ((st = g_alloc(g, &p, pts * sizeof(double))) != STZG_OK) return bail(st);
-        L.b = (double *)p;
-        if ((st = g_alloc(g, &p, pts * sizeof(double))) != STZG_OK) return bail(st);
-        L.r = (double *)p;
-        if ((st = g_alloc(g, &p, pts * sizeof(int))) != STZG_OK) return bail(st);
-        L.cls = (const int *)p;
-        if (cudaMemcpy(p, H.cls.data(), pts * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(fail(STZG_ECUDA, "upload of stencil indices failed"));
-        if ((st = g_alloc(g, &p, H.table.size() * sizeof(gst))) != STZG_OK) return bail(st);
-        L.st = (const gst *)p;
-        if (cudaMemcpy(p, H.table.data(), H.table.size() * sizeof(gst), cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(fail(STZG_ECUDA, "upload of stencils failed"));
-    }
-    const host_level &B = g->host.back();
-    if (g->nl > 1 && (long)B.m * B.n <= kBottomDirect) {
-        std::vector<double> inv = dense_inverse(B, g->xp, g->yp);
-        if (!inv.empty()) {
-            void *p;
-            int st;
-            if ((st = g_alloc(g, &p, inv.size() * sizeof(double))) != STZG_OK) return bail(st);
-            g->inv = (double *)p;
-            g->inv_n = B.m * B.n;
-            if (cudaMemcpy(p, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
-                return bail(fail(STZG_ECUDA, "upload of the coarsest inverse failed"));
-        }
-    }
-    // single-block tail: the small levels that fit in its shared memory
-    // together, if they are at least two (the coarsest alone is the bottom)
-    {
-        size_t bytes = 0;
-        int t = g->nl;
-        for (int l = g->nl - 1; l >= 1; l--) {
-            const long pts = (long)g->host[l].m * g->host[l].n;
-            const size_t b = 3 * sizeof(double) * (size_t)pts;
-            if (pts > kTailPoints || bytes + b > kTailSmem) break;
-            bytes += b;
-            t = l;
-        }
-        if (t <= g->nl - 2) {
-            if (cudaFuncSetAttribute(k_tg_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
-                cudaSuccess)
-                return bail(fail(STZG_ECUDA, "tail kernel attribute"));
-            g->tail_start = t;
-            g->tail_smem = bytes;
-        }
-    }
-    {
-        void *p;
-        int st;
-        if ((st = g_alloc(g, &p, kRedBlocks * sizeof(double))) != STZG_OK) return bail(st);
-        g->partials = (double *)p;
-        if ((st = g_alloc(g, &p, sizeof(double))) != STZG_OK) return bail(st);
-        g->dsum = (double *)p;
-        if (cudaMallocHost(&p, sizeof(double)) != cudaSuccess) return bail(fail(STZG_ENOMEM, "pinned allocation"));
-        g->hsum = (double *)p;
-    }
-    if (cudaStreamSynchronize(g->st) != cudaSuccess) return bail(fail(STZG_ECUDA, "setup failed"));
     *out = g;
     return STZG_OK;
 }
 
+int stzg_tgmg_create(int m, int n, int x_prd, int y_prd, const double *table, int ntable, const int *cls,
+                     double acc, int device, stzg_tgmg **out) {
+    return stzg_tgmg_create_block(m, n, x_prd, y_prd, 1, table, ntable, cls, acc, device, out);
+}
+
 int stzg_tgmg_destroy(stzg_tgmg *g) {
     if (!g) return STZG_OK;
-    cudaSetDevice(g->device);
-    if (g->st) cudaStreamSynchronize(g->st);
-    if (g->gexec) cudaGraphExecDestroy(g->gexec);
-    for (void *p : g->owned) cudaFree(p);
-    if (g->hsum) cudaFreeHost(g->hsum);
-    if (g->ev0) cudaEventDestroy(g->ev0);
-    if (g->ev1) cudaEventDestroy(g->ev1);
-    if (g->st) cudaStreamDestroy(g->st);
+    tg_destroy(g->s1);
+    tg_destroy(g->s2);
     delete g;
     return STZG_OK;
 }
 
-static int copy_top(stzg_tgmg *g, double *dev, const double *src, double *dst) {
-    if (!g || (!src && !dst)) return fail(STZG_EINVAL, "null argument");
-    STZG_CUDA(cudaSetDevice(g->device));
-    const size_t bytes = sizeof(double) * (size_t)g->lv[0].m * g->lv[0].n;
-    if (src) STZG_CUDA(cudaMemcpyAsync(dev, src, bytes, cudaMemcpyHostToDevice, g->st));
-    else STZG_CUDA(cudaMemcpyAsync(dst, dev, bytes, cudaMemcpyDeviceToHost, g->st));
-    STZG_CUDA(cudaStreamSynchronize(g->st));
+int stzg_tgmg_set_operator(stzg_tgmg *g, const double *table, int ntable, const int *cls) {
+    if (!table || ntable < 1 || !cls) return fail(STZG_EINVAL, "bad operator");
+    return dispatch(g, [&](auto *s) { return tg_set_operator(s, table, ntable, cls); });
+}
+
+int stzg_tgmg_set_b(stzg_tgmg *g, const double *b) {
+    if (!b) return fail(STZG_EINVAL, "null argument");
+    return dispatch(g, [&](auto *s) { return tg_copy(s, s->lv[0].b, b, nullptr); });
+}
+int stzg_tgmg_get_b(stzg_tgmg *g, double *b) {
+    if (!b) return fail(STZG_EINVAL, "null argument");
+    return dispatch(g, [&](auto *s) { return tg_copy(s, s->lv[0].b, nullptr, b); });
+}
+int stzg_tgmg_set_z(stzg_tgmg *g, const double *z) {
+    if (!z) return fail(STZG_EINVAL, "null argument");
+    return dispatch(g, [&](auto *s) { return tg_copy(s, s->lv[0].z, z, nullptr); });
+}
+int stzg_tgmg_get_z(stzg_tgmg *g, double *z) {
+    if (!z) return fail(STZG_EINVAL, "null argument");
+    return dispatch(g, [&](auto *s) { return tg_copy(s, s->lv[0].z, nullptr, z); });
+}
+
+int stzg_tgmg_device_arrays(stzg_tgmg *g, double **b, double **z) {
+    if (!g || !b || !z) return fail(STZG_EINVAL, "null argument");
+    if (g->B == 1) {
+        *b = (double *)g->s1->lv[0].b;
+        *z = (double *)g->s1->lv[0].z;
+    } else {
+        *b = (double *)g->s2->lv[0].b;
+        *z = (double *)g->s2->lv[0].z;
+    }
     return STZG_OK;
 }
 
-int stzg_tgmg_set_b(stzg_tgmg *g, const double *b) { return copy_top(g, g ? g->lv[0].b : nullptr, b, nullptr); }
-int stzg_tgmg_get_b(stzg_tgmg *g, double *b) { return copy_top(g, g ? g->lv[0].b : nullptr, nullptr, b); }
-int stzg_tgmg_set_z(stzg_tgmg *g, const double *z) { return copy_top(g, g ? g->lv[0].z : nullptr, z, nullptr); }
-int stzg_tgmg_get_z(stzg_tgmg *g, double *z) { return copy_top(g, g ? g->lv[0].z : nullptr, nullptr, z); }
-
 int stzg_tgmg_clear_z(stzg_tgmg *g) {
-    if (!g) return fail(STZG_EINVAL, "null handle");
-    STZG_CUDA(cudaSetDevice(g->device));
-    clear_z(g, g->lv[0]);
-    STZG_CUDA(cudaStreamSynchronize(g->st));
-    return STZG_OK;
+    return dispatch(g, [&](auto *s) -> int {
+        clear_z(s, s->lv[0]);
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+        return STZG_OK;
+    });
 }
 
 int stzg_tgmg_l2_error(stzg_tgmg *g, double *err) {
-    if (!g || !err) return fail(STZG_EINVAL, "null argument");
-    STZG_CUDA(cudaSetDevice(g->device));
-    return l2_error(g, err);
+    if (!err) return fail(STZG_EINVAL, "null argument");
+    return dispatch(g, [&](auto *s) { return l2_error(s, err); });
 }
 
 int stzg_tgmg_iterate(stzg_tgmg *g, int type, int count, double omega, int cyc_down, int cyc_up, int hcyc_bottom) {
-    if (!g || !valid_type(type) || count < 0 || cyc_down < 0 || cyc_up < 0 || hcyc_bottom < 0)
+    if (!valid_type(type) || count < 0 || cyc_down < 0 || cyc_up < 0 || hcyc_bottom < 0)
         return fail(STZG_EINVAL, "bad iterate arguments");
-    STZG_CUDA(cudaSetDevice(g->device));
-    timed t(g);
-    STZG_CHECK(run_iterations(g, type, count, omega, cyc_down, cyc_up, hcyc_bottom));
-    t.done();
-    STZG_CUDA(cudaGetLastError());
-    return STZG_OK;
+    return dispatch(g, [&](auto *s) { return tg_iterate(s, type, count, omega, cyc_down, cyc_up, hcyc_bottom); });
 }
 
 int stzg_tgmg_solve(stzg_tgmg *g, int type, stzg_tgmg_predict *tp, double omega, int cyc_down, int cyc_up,
                     int hcyc_bottom, int *iters, double *l2) {
-    if (!g || !tp || !valid_type(type) || tp->mult < 1 || cyc_down < 0 || cyc_up < 0 || hcyc_bottom < 0)
+    if (!tp || !valid_type(type) || tp->mult < 1 || cyc_down < 0 || cyc_up < 0 || hcyc_bottom < 0)
         return fail(STZG_EINVAL, "bad solve arguments");
-    STZG_CUDA(cudaSetDevice(g->device));
-    timed t(g);
-    // tgmg::solve(type, tgmg_predict&, ...), tgmg.in.cc:266-301
-    int nit = tp->lim / tp->mult;
-    STZG_CHECK(run_iterations(g, type, nit, omega, cyc_down, cyc_up, hcyc_bottom));
-    double acc;
-    STZG_CHECK(l2_error(g, &acc));
-    if (acc < g->acc) {
-        if (tp->lim > 0) tp->lim -= 1 + tp->lim / tp->decay;
-    } else {
-        int k = 0;
-        do {
-            tp->lim += ++k * tp->mult;
-            if (tp->lim > tp->max_thresh) {
-                t.done();
-                if (l2) *l2 = acc;
-                return fail(STZG_ENOTCONV, "tgmg did not converge");
-            }
-            nit += k;
-            STZG_CHECK(run_iterations(g, type, k, omega, cyc_down, cyc_up, hcyc_bottom));
-            STZG_CHECK(l2_error(g, &acc));
-        } while (acc >= g->acc && !std::isnan(acc));
-    }
-    tp->solves++;
-    tp->vcount += nit;
-    STZG_CHECK(run_iterations(g, type, tp->extra_iters, omega, cyc_down, cyc_up, hcyc_bottom));
-    t.done();
-    if (iters) *iters = nit;
-    if (l2) *l2 = acc;
-    if (std::isnan(acc)) return fail(STZG_ENAN, "NaN residual");
-    return STZG_OK;
+    return dispatch(g, [&](auto *s) { return tg_solve(s, type, tp, omega, cyc_down, cyc_up, hcyc_bottom, iters, l2); });
 }
 
 int stzg_tgmg_solve_fixed(stzg_tgmg *g, int type, int per_loop, int max_loops, double omega, int cyc_down,
                           int cyc_up, int hcyc_bottom, int *iters, double *l2) {
-    if (!g || !valid_type(type) || per_loop < 1 || max_loops < 1 || cyc_down < 0 || cyc_up < 0 ||
-        hcyc_bottom < 0)
+    if (!valid_type(type) || per_loop < 1 || max_loops < 1 || cyc_down < 0 || cyc_up < 0 || hcyc_bottom < 0)
         return fail(STZG_EINVAL, "bad solve arguments");
-    STZG_CUDA(cudaSetDevice(g->device));
-    timed t(g);
-    // tgmg::solve(type, per_loop, max_loops, ...), tgmg.in.cc:182-197
-    double acc = 0;
-    int nloop = 0;
-    do {
-        if (++nloop == max_loops) {
-            t.done();
-            if (iters) *iters = nloop * per_loop;
-            if (l2) *l2 = acc;
-            return fail(STZG_ENOTCONV, "tgmg did not converge");
-        }
-        STZG_CHECK(run_iterations(g, type, per_loop, omega, cyc_down, cyc_up, hcyc_bottom));
-        STZG_CHECK(l2_error(g, &acc));
-    } while (acc > g->acc && !std::isnan(acc));
-    t.done();
-    if (iters) *iters = nloop * per_loop;
-    if (l2) *l2 = acc;
-    if (std::isnan(acc)) return fail(STZG_ENAN, "NaN residual");
-    return STZG_OK;
+    return dispatch(g, [&](auto *s) {
+        return tg_solve_fixed(s, type, per_loop, max_loops, omega, cyc_down, cyc_up, hcyc_bottom, iters, l2);
+    });
 }
 
 int stzg_tgmg_levels(stzg_tgmg *g, int *nlevels, int *dims) {
-    if (!g || !nlevels) return fail(STZG_EINVAL, "null argument");
-    *nlevels = g->nl;
-    if (dims)
-        for (int l = 0; l < g->nl; l++) {
-            dims[2 * l] = g->host[l].m;
-            dims[2 * l + 1] = g->host[l].n;
-        }
-    return STZG_OK;
+    if (!nlevels) return fail(STZG_EINVAL, "null argument");
+    if (!g) return fail(STZG_EINVAL, "null handle");
+    return g->B == 1 ? tg_levels(g->s1, nlevels, dims) : tg_levels(g->s2, nlevels, dims);
 }
 
 int stzg_tgmg_stencil(stzg_tgmg *g, int level, double *out) {
-    if (!g || !out || level < 1 || level >= g->nl) return fail(STZG_EINVAL, "bad level");
-    const host_level &H = g->host[level];
-    const size_t pts = (size_t)H.m * H.n;
-    for (size_t k = 0; k < pts; k++) std::memcpy(out + 10 * k, H.table[H.cls[k]].e, 10 * sizeof(double));
-    return STZG_OK;
+    if (!out || !g) return fail(STZG_EINVAL, "null argument");
+    return g->B == 1 ? tg_stencil(g->s1, level, out) : tg_stencil(g->s2, level, out);
 }
 
 int stzg_tgmg_last_timing(stzg_tgmg *g, double *ms, long *kernels) {
     if (!g) return fail(STZG_EINVAL, "null handle");
-    if (ms) *ms = g->last_ms;
-    if (kernels) *kernels = g->last_kernels;
+    const double t = g->B == 1 ? g->s1->last_ms : g->s2->last_ms;
+    const long k = g->B == 1 ? g->s1->last_kernels : g->s2->last_kernels;
+    if (ms) *ms = t;
+    if (kernels) *kernels = k;
     return STZG_OK;
 }
 

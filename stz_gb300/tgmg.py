@@ -17,8 +17,9 @@ from . import _lib
 
 # Every symbol include/stzg_tgmg.h declares.
 EXPORTS = [
-    "stzg_tgmg_predict_init", "stzg_tgmg_create", "stzg_tgmg_destroy", "stzg_tgmg_set_b", "stzg_tgmg_get_b",
-    "stzg_tgmg_set_z", "stzg_tgmg_get_z", "stzg_tgmg_clear_z", "stzg_tgmg_solve", "stzg_tgmg_solve_fixed",
+    "stzg_tgmg_predict_init", "stzg_tgmg_create", "stzg_tgmg_create_block", "stzg_tgmg_set_operator",
+    "stzg_tgmg_destroy", "stzg_tgmg_set_b", "stzg_tgmg_get_b",
+    "stzg_tgmg_set_z", "stzg_tgmg_get_z", "stzg_tgmg_device_arrays", "stzg_tgmg_clear_z", "stzg_tgmg_solve", "stzg_tgmg_solve_fixed",
     "stzg_tgmg_iterate", "stzg_tgmg_l2_error", "stzg_tgmg_levels", "stzg_tgmg_stencil", "stzg_tgmg_last_timing",
     "stzg_poisson_fd",
 ]
@@ -58,11 +59,14 @@ def load():
     decl = {
         "stzg_tgmg_predict_init": (None, [PP]),
         "stzg_tgmg_create": (I, [I, I, I, I, _P, I, _IP, D, I, ctypes.POINTER(V)]),
+        "stzg_tgmg_create_block": (I, [I, I, I, I, I, _P, I, _IP, D, I, ctypes.POINTER(V)]),
+        "stzg_tgmg_set_operator": (I, [V, _P, I, _IP]),
         "stzg_tgmg_destroy": (I, [V]),
         "stzg_tgmg_set_b": (I, [V, _P]),
         "stzg_tgmg_get_b": (I, [V, _P]),
         "stzg_tgmg_set_z": (I, [V, _P]),
         "stzg_tgmg_get_z": (I, [V, _P]),
+        "stzg_tgmg_device_arrays": (I, [V, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p)]),
         "stzg_tgmg_clear_z": (I, [V]),
         "stzg_tgmg_solve": (I, [V, I, PP, D, I, I, I, _IP, _P]),
         "stzg_tgmg_solve_fixed": (I, [V, I, I, I, D, I, I, I, _IP, _P]),
@@ -86,19 +90,21 @@ def _dp(a):
 
 
 class Problem:
-    """A problem class in the sense of tgmg's template argument S: an m x n
-    grid with periodicity flags, its 9-point operator as a table of stencils
-    (dl dc dr cl cc cr ul uc ur) with a stencil index per point, the squared
-    residual threshold acc, and the arrays b and z (n rows of m)."""
+    """A problem class in the sense of tgmg's template arguments S, V, M: an
+    m x n grid with periodicity flags, its 9-point operator as a table of
+    stencils (dl dc dr cl cc cr ul uc ur; scalars, or row-major 2x2 blocks when
+    block = 2) with a stencil index per point, the squared residual threshold
+    acc, and the arrays b and z (n rows of m, times block components)."""
 
-    def __init__(self, m, n, table, cls, acc, x_prd=False, y_prd=False):
-        self.m, self.n = int(m), int(n)
+    def __init__(self, m, n, table, cls, acc, x_prd=False, y_prd=False, block=1):
+        self.m, self.n, self.block = int(m), int(n), int(block)
         self.x_prd, self.y_prd = bool(x_prd), bool(y_prd)
-        self.table = np.ascontiguousarray(np.asarray(table, dtype=np.float64).reshape(-1, 9))
+        self.table = np.ascontiguousarray(np.asarray(table, dtype=np.float64).reshape(-1, 9 * self.block ** 2))
         self.cls = np.ascontiguousarray(np.asarray(cls, dtype=np.int32).reshape(self.n, self.m))
         self.acc = float(acc)
-        self.b = np.zeros((self.n, self.m))
-        self.z = np.zeros((self.n, self.m))
+        shape = (self.n, self.m) if self.block == 1 else (self.n, self.m, self.block)
+        self.b = np.zeros(shape)
+        self.z = np.zeros(shape)
 
 
 class PoissonFD(Problem):
@@ -140,10 +146,19 @@ class Tgmg:
         self.q = q
         self.verbose = 0
         h = ctypes.c_void_p()
-        _lib.check(self.lib.stzg_tgmg_create(q.m, q.n, int(q.x_prd), int(q.y_prd), _dp(q.table),
-                                             q.table.shape[0], q.cls.ctypes.data_as(_IP), q.acc, device,
-                                             ctypes.byref(h)))
+        _lib.check(self.lib.stzg_tgmg_create_block(q.m, q.n, int(q.x_prd), int(q.y_prd), getattr(q, "block", 1),
+                                                   _dp(q.table), q.table.shape[0], q.cls.ctypes.data_as(_IP), q.acc,
+                                                   device, ctypes.byref(h)))
         self.h = h
+
+    def set_operator(self, table, cls=None):
+        """New stencil values on the same grid (qs_multi::init + setup)."""
+        q = self.q
+        q.table = np.ascontiguousarray(np.asarray(table, dtype=np.float64).reshape(-1, q.table.shape[1]))
+        if cls is not None:
+            q.cls = np.ascontiguousarray(np.asarray(cls, dtype=np.int32).reshape(q.n, q.m))
+        _lib.check(self.lib.stzg_tgmg_set_operator(self.h, _dp(q.table), q.table.shape[0],
+                                                   q.cls.ctypes.data_as(_IP)))
 
     def close(self):
         if getattr(self, "h", None):
@@ -167,7 +182,7 @@ class Tgmg:
         _lib.check(self.lib.stzg_tgmg_set_z(self.h, _dp(z)))
 
     def _pull(self):
-        z = np.empty((self.q.n, self.q.m))
+        z = np.empty(self.q.z.shape)
         _lib.check(self.lib.stzg_tgmg_get_z(self.h, _dp(z)))
         self.q.z[...] = z
 
@@ -243,9 +258,10 @@ class Tgmg:
 
     def stencil(self, level):
         """Galerkin stencils of coarse level `level` (1 = first child), shape
-        (n, m, 10) as tgmg_level::s."""
+        (n, m, 10) as tgmg_level::s, or (n, m, 10, 2, 2) for 2x2 blocks."""
         m, n = self.levels()[level]
-        out = np.empty((n, m, 10))
+        B = getattr(self.q, "block", 1)
+        out = np.empty((n, m, 10) if B == 1 else (n, m, 10, B, B))
         _lib.check(self.lib.stzg_tgmg_stencil(self.h, level, _dp(out)))
         return out
 

@@ -219,3 +219,90 @@ def test_cpp_dropin_header(tmp_path):
     z = np.fromfile(zfile).reshape(meta["n"], meta["m"])
     assert np.abs(z - d["z"]).max() <= 1e-9 * np.abs(d["z"]).max()
     assert "levels %d" % len(meta["levels"]) in r.stdout
+
+
+def _block_operator(m, n, xp, yp, lt=0.3, seed=0, walls=True):
+    """2x2-block operators of the qs_multi kind: horizontal, vertical and
+    corner blocks (the transformed operator of coord_transforms qs_multi.cc
+    with shear lt, preconditioned by the inverse centre) and, unless y is
+    periodic, wall rows that carry only the identity (qs_multi.hh:31-42)."""
+    K, mu, h = 2.5, 1.0, 1.0
+    L = K - 2. / 3. * mu
+    ltsq = lt * lt
+    regh = np.array([[(L + 2 * mu + ltsq * mu), (lt * mu + lt * ltsq * mu)], [-lt * (L + mu), mu * (1 + ltsq)]]) / h
+    regv = np.array([[mu, lt * mu], [0, (L + 2 * mu)]]) / h
+    regc = -2 * (regh + regv)
+    regd = np.array([[-0.5 * lt * mu, 0.25 * (L + mu - 2 * ltsq * mu)],
+                     [0.25 * (L + mu), -0.25 * lt * (L + 3 * mu)]]) / h
+    ci = np.linalg.inv(regc)
+    regh, regv, regd = ci @ regh, ci @ regv, ci @ regd
+    I2 = np.eye(2)
+    inner = np.stack([regd, regv, -regd, regh, I2, regh, -regd, regv, regd])
+    wall = np.stack([np.zeros((2, 2))] * 4 + [I2] + [np.zeros((2, 2))] * 4)
+    table = np.stack([inner, wall])
+    cls = np.zeros((n, m), dtype=np.int32)
+    if walls and not yp:
+        cls[0, :] = cls[-1, :] = 1
+    return table, cls
+
+
+@pytest.mark.parametrize("m,n,xp,yp", [(32, 17, 1, 0), (40, 24, 1, 1), (33, 27, 1, 1), (24, 19, 0, 0)])
+def test_block_operators(m, n, xp, yp):
+    """tgmg<S,vec,mat>: Galerkin blocks and the converged solution of
+    qs_multi-type 2x2-block operators, periodic or walled in y."""
+    tg = _tg()
+    table, cls = _block_operator(m, n, xp, yp, seed=m)
+    ops, sizes = O.hierarchy(m, n, xp, yp, table, cls, 2)
+    q = tg.Problem(m, n, table, cls, 1e-26, x_prd=xp, y_prd=yp, block=2)
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal((n, m, 2))
+    if yp:
+        # periodic in both directions the operator annihilates rigid
+        # translations: the source must be consistent (zero mean), as the
+        # divergence of a stress is
+        b -= b.mean(axis=(0, 1))
+    q.b[...] = b
+    g = tg.Tgmg(q)
+    assert g.levels() == sizes
+    for l in range(1, len(sizes)):
+        mine = g.stencil(l)
+        ref = O.stencils(ops[l], sizes[l][0], sizes[l][1], xp, yp, 2)
+        assert np.abs(mine[:, :, :9] - ref[:, :, :9]).max() <= 1e-13 * np.abs(ref[:, :, :9]).max(), l
+    tp = tg.Predict()
+    assert g.solve_v_cycle(tp)
+    assert g.l2_error() < q.acc
+    if yp:
+        zx = np.linalg.lstsq(ops[0].toarray(), b.ravel(), rcond=None)[0].reshape(b.shape)
+        got = q.z - q.z.mean(axis=(0, 1))
+        zx -= zx.mean(axis=(0, 1))
+    else:
+        zx, got = O.solve(ops[0], b), q.z
+    assert np.abs(got - zx).max() <= 1e-10 * np.abs(zx).max()
+    assert g.l2_error() == pytest.approx(O.l2_error(ops[0], q.z, b, 2), rel=1e-3, abs=1e-28)
+    g.close()
+
+
+def test_block_operator_update():
+    """set_operator (qs_multi::init + setup on a new shear): the rebuilt
+    hierarchy equals a fresh one, and solves keep converging."""
+    tg = _tg()
+    m, n = 40, 24
+    t0, cls = _block_operator(m, n, 1, 0, lt=0.1)
+    t1, _ = _block_operator(m, n, 1, 0, lt=0.45)
+    q = tg.Problem(m, n, t0, cls, 1e-26, x_prd=True, y_prd=False, block=2)
+    q.cls[0, :] = q.cls[-1, :] = 1
+    cls = q.cls.copy()
+    q.b[...] = np.random.default_rng(5).standard_normal((n, m, 2))
+    b = q.b.copy()
+    g = tg.Tgmg(q)
+    tp = tg.Predict()
+    assert g.solve_v_cycle(tp)
+    g.set_operator(t1)
+    q.z[...] = 0
+    assert g.solve_v_cycle(tp)
+    ops, sizes = O.hierarchy(m, n, 1, 0, t1, cls, 2)
+    zx = O.solve(ops[0], b)
+    assert np.abs(q.z - zx).max() <= 1e-10 * np.abs(zx).max()
+    ref = O.stencils(ops[1], sizes[1][0], sizes[1][1], 1, 0, 2)
+    assert np.abs(g.stencil(1)[:, :, :9] - ref[:, :, :9]).max() <= 1e-13 * np.abs(ref[:, :, :9]).max()
+    g.close()
