@@ -1,0 +1,61 @@
+/* stzg_ct.h - C ABI of the quasi-static STZ step in sheared coordinates on one GPU.
+ *
+ * Stands in for the coord_transforms variant of the simulation
+ * (esim/coord_transforms/simple_shear/shear_sim.{hh,cc}): the grid follows a
+ * simple shear of rate lamb (lt = lamb * time enters the stress equations,
+ * the deviatoric norm and the elasticity operator), x is periodic and y is
+ * periodic (y_prd) or bounded by walls moving at +-u_bdry.  One handle owns
+ * the fields in device memory with the reference's two ghost layers, the
+ * 2x2-block multigrid of stzg_tgmg.h for the projection (its operator rebuilt
+ * every step, as qs_multi::init does) and a CUDA stream.  Statuses and
+ * messages are those of stzg.h.
+ */
+#ifndef STZG_CT_H
+#define STZG_CT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* shear_sim constructor arguments (shear_sim.hh:157-161) and the STZ law
+ * (stz_model.hh: stz_model 0 linear, 1 nonlinear, 2 linear athermal,
+ * 3 nonlinear athermal; s0 = 1 in this variant). */
+typedef struct {
+    int m, n, y_prd, stz_model, t_model;
+    double ax, bx, ay, by;
+    double mu, K, viscosity, chi_len, t_scale, adapt_fac, u_bdry, lamb;
+    double TZ, c0, tau0, kappa, Delta, Omegaeps0, chi_inf, theta, rho;
+} stzg_ct_params;
+
+typedef struct stzg_ct stzg_ct;
+
+/* Field ids for stzg_ct_set_field / stzg_ct_get_field: the c_field members
+ * (fields.hh:15-35).  Arrays hold rows 0..n (n+1 rows of m): nodes (u, v, X,
+ * Y) at the grid corners, cells (p, q, s, tau, chi, ddev) at the centres; a
+ * cell row n is the first ghost row. */
+enum { STZG_CT_U = 0, STZG_CT_V, STZG_CT_P, STZG_CT_Q, STZG_CT_S, STZG_CT_TAU, STZG_CT_CHI, STZG_CT_X, STZG_CT_Y,
+       STZG_CT_DDEV, STZG_CT_FIELDS };
+
+int stzg_ct_create(const stzg_ct_params *p, int device, stzg_ct **out);
+int stzg_ct_destroy(stzg_ct *s);
+/* shear_sim::init_fields(chi_case, tem_base, tem_delta) (shear_sim.cc:59-131). */
+int stzg_ct_init_fields(stzg_ct *s, int chi_case, double tem_base, double tem_delta);
+/* Copies one field in or out (rows 0..n).  set_field re-applies the
+ * boundary conditions (set_boundaries, shear_sim.cc:778-811). */
+int stzg_ct_set_field(stzg_ct *s, int field, const double *host);
+int stzg_ct_get_field(stzg_ct *s, int field, double *host);
+int stzg_ct_set_time(stzg_ct *s, double time);
+int stzg_ct_get_time(stzg_ct *s, double *time);
+/* nsteps of shear_sim::step_forward_quasistatic(dt) (shear_sim.cc:352-360):
+ * advection_step (ENO2 advection, STZ plasticity, chi diffusion, updates,
+ * time, boundaries), projection_step (operator for the new lt, source,
+ * multigrid solve, stress correction, velocities, boundaries).  vcycles
+ * (optional) receives the V-cycles counted by the solver's tgmg_predict;
+ * seconds (optional) the device time. */
+int stzg_ct_step_qs(stzg_ct *s, double dt, int nsteps, long *vcycles, double *seconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STZG_CT_H */

@@ -1,8 +1,8 @@
 #!/bin/sh
-# Builds the reference's own quasi-static shear step and its general multigrid
-# on the poisson_fd problem class from their sources, read in place under the
-# reference tree, into oracle/_ref/libstzref.so and oracle/_ref/libtgmgref.so
-# (test-only).
+# Builds the reference's own quasi-static shear step, its general multigrid
+# on the poisson_fd problem class and the coord_transforms variant of the
+# step from their sources, read in place under the reference tree, into
+# oracle/_ref/libstzref.so, libtgmgref.so and libctref.so (test-only).
 #
 #   oracle/build_ref.sh [REFERENCE_ROOT]     (default: /root/reference)
 #
@@ -17,7 +17,11 @@
 #      together with oracle/ref_driver.cc, into one shared library;
 #   3. g++ compiles esim/tgmg/poisson_fd.cc (which includes the generated
 #      tgmg.cc and instantiates tgmg<poisson_fd,double,double>) with
-#      oracle/ref_tgmg_driver.cc into a second one.
+#      oracle/ref_tgmg_driver.cc into a second one;
+#   4. g++ compiles esim/coord_transforms/simple_shear/{shear_sim,qs_multi,
+#      common,extra,bi_interp}.cc and esim/shared/mat.cc with
+#      oracle/ref_ct_driver.cc into a third one (that directory first on the
+#      include path: its headers share names with esim/sb/main's).
 # Only x86/Arm-neutral flags are used; nothing here runs on the GPU.
 set -e
 REF=${1:-/root/reference}
@@ -48,8 +52,18 @@ TG="$OUT/objtg"
 mkdir -p "$TG"
 $CXX $FLAGS $INC -c "$ESIM/tgmg/poisson_fd.cc" -o "$TG/poisson_fd.o" &
 $CXX $FLAGS $INC -c "$HERE/ref_tgmg_driver.cc" -o "$TG/ref_tgmg_driver.o" &
+CT="$OUT/objct"
+CTD="$ESIM/coord_transforms/simple_shear"
+CTINC="-I$CTD -I$GEN -I$ESIM/tgmg -I$ESIM/shared"
+mkdir -p "$CT"
+for f in shear_sim qs_multi common extra bi_interp; do
+    $CXX $FLAGS $CTINC -c "$CTD/$f.cc" -o "$CT/$f.o" &
+done
+$CXX $FLAGS $CTINC -c "$ESIM/shared/mat.cc" -o "$CT/mat.o" &
+$CXX $FLAGS $CTINC -c "$HERE/ref_ct_driver.cc" -o "$CT/ref_ct_driver.o" &
 wait
 $CXX -shared -fopenmp -o "$OUT/libstzref.so" "$OBJ"/*.o
 $CXX -shared -fopenmp -o "$OUT/libtgmgref.so" "$TG"/*.o
-rm -rf "$GEN" "$OBJ" "$TG"
-echo "build_ref: wrote $OUT/libstzref.so $OUT/libtgmgref.so"
+$CXX -shared -fopenmp -o "$OUT/libctref.so" "$CT"/*.o
+rm -rf "$GEN" "$OBJ" "$TG" "$CT"
+echo "build_ref: wrote $OUT/libstzref.so $OUT/libtgmgref.so $OUT/libctref.so"

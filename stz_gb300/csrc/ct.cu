@@ -1,0 +1,609 @@
+// Quasi-static STZ step in sheared coordinates (include/stzg_ct.h): the
+// coord_transforms variant of the simulation
+// (esim/coord_transforms/simple_shear/shear_sim.cc:352-546, fields.hh,
+// qs_multi.{hh,cc}) on one GPU.
+//
+// Layout: each field of the reference's c_field (u, v, p, q, s, tau, chi, X,
+// Y) is an FP64 array of (m+4) x (n+4) points with the reference's two ghost
+// layers, index (j+2)*(m+4) + (i+2), in two buffers: the advection kernel
+// reads buffer cur and writes buffer cur^1.  ddev is one array of the same
+// shape whose ghost points stay zero (the reference never writes them).  The
+// projection solves with the 2x2-block multigrid of tgmg.cu on m x lsn nodes
+// (lsn = n rows when y is periodic, n+1 with walls), its operator rebuilt
+// every step for the new shear lt = lamb*time as qs_multi::init does
+// (qs_multi.cc:31-46); source and velocities stay on the GPU.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "step.cuh"
+#include "stz_law.cuh"
+#include "stzg_ct.h"
+#include "stzg_tgmg.h"
+
+namespace stzg {
+namespace {
+
+enum { CU = 0, CV, CP, CQ, CS, CTAU, CCHI, CX, CY, CF };
+
+struct ct_consts {
+    int m, n, gm, yp, lsn;
+    double ax, ay, bx, by, lx, ly, dx, dy, xsp, ysp;
+    double mu, mu_inv, K, chi_len, lamb, u_bdry;
+    stz_law_params<double> law;
+};
+
+struct ct_fields {
+    double *f[2][CF];
+    double *ddev;
+};
+
+__device__ __forceinline__ size_t gidx(const ct_consts &c, int i, int j) { return (size_t)(j + 2) * c.gm + (i + 2); }
+
+// shear_sim::eno2 (shear_sim.cc:886-888)
+__device__ __forceinline__ double eno2_ct(double p0, double p1, double p2, double p3) {
+    return fabs(p0 - 2 * p1 + p2) > fabs(p1 - 2 * p2 + p3) ? 3 * p1 - 4 * p2 + p3 : p0 - p2;
+}
+
+// hs * eno2 along step d from point k (rm_eno2 / st_eno2, shear_sim.cc:864-884)
+__device__ __forceinline__ double eno_d(const double *f, size_t k, long d, double hs) {
+    return hs * eno2_ct(f[k - d], f[k], f[k + d], f[k + 2 * d]);
+}
+
+// Advection and plasticity per cell (i,j) and its lower-left node
+// (shear_sim::advection_step, shear_sim.cc:365-417); the new values go to
+// buffer cur^1 (chi without its diffusion).
+__global__ void k_ct_advect(ct_consts c, ct_fields F, int cur, double dt, double time) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= c.m || j >= c.n) return;
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
+    const double third = 1. / 3., lt = c.lamb * time, ltsq = lt * lt;
+    const double *const *A = F.f[cur];
+    double *const *B = F.f[cur ^ 1];
+    const size_t k = gidx(c, i, j);
+    const long gm = c.gm;
+    const double *U = A[CU], *V = A[CV];
+    B[CU][k] = U[k];
+    B[CV][k] = V[k];
+    // reference map at the node
+    if (j > 0 || c.yp) {
+        const double uc = U[k], vc = V[k];
+        double Xx, Yx, Xy, Yy;
+        if (uc > 0) {
+            Xx = eno_d(A[CX], k, -1, hx);
+            Yx = eno_d(A[CY], k, -1, hx);
+        } else {
+            Xx = eno_d(A[CX], k, 1, -hx);
+            Yx = eno_d(A[CY], k, 1, -hx);
+        }
+        if (vc > 0) {
+            Xy = eno_d(A[CX], k, -gm, hy);
+            Yy = eno_d(A[CY], k, -gm, hy);
+        } else {
+            Xy = eno_d(A[CX], k, gm, -hy);
+            Yy = eno_d(A[CY], k, gm, -hy);
+        }
+        const double cX = -uc * Xx - vc * Xy, cY = -uc * Yx - vc * Yy;
+        B[CX][k] = A[CX][k] + cX;
+        B[CY][k] = A[CY][k] + cY;
+    } else {
+        B[CX][k] = A[CX][k];
+        B[CY][k] = A[CY][k];
+    }
+    // deformation rate, staggered velocity and spin
+    const double u0 = U[k], ur = U[k + 1], uu = U[k + gm], uru = U[k + gm + 1];
+    const double v0 = V[k], vr = V[k + 1], vu = V[k + gm], vru = V[k + gm + 1];
+    const double uc = 0.25 * (u0 + ur + uu + uru), vc = 0.25 * (v0 + vr + vu + vru);
+    const double ux = hx * (-u0 + ur - uu + uru), uy = hy * (-u0 - ur + uu + uru);
+    const double vx = hx * (-v0 + vr - vu + vru), vy = hy * (-v0 - vr + vu + vru);
+    const double p = A[CP][k], q = A[CQ][k], s = A[CS][k], tau = A[CTAU][k], chi = A[CCHI][k];
+    // calc_p (shear_sim.hh:182-184)
+    const double old_p = p + (1. / 3) * c.lamb * time * (-2 * tau + c.lamb * time * (p + q + s));
+    const long dx1 = uc > 0 ? -1 : 1, dy1 = vc > 0 ? -gm : gm;
+    const double hsx = uc > 0 ? hx : -hx, hsy = vc > 0 ? hy : -hy;
+    double f1[5], f2[5];
+#pragma unroll
+    for (int f = 0; f < 5; f++) {
+        f1[f] = eno_d(A[CP + f], k, dx1, hsx);
+        f2[f] = eno_d(A[CP + f], k, dy1, hsy);
+    }
+    // adaptive_plastic_term (shear_sim.cc:739-776) of the deviatoric norm in
+    // the untransformed frame (c_field::devsq, fields.hh:108-141)
+    const double pqs = p + q + s;
+    const double unt_tau = tau - lt * pqs;
+    const double unt_q = q + lt * (1 / 3.) * (-tau + lt * .5 * pqs);
+    const double unt_s = s + lt * (tau - lt * .5 * pqs);
+    const double sbar = sqrt(3 * unt_q * unt_q + unt_s * unt_s + unt_tau * unt_tau);
+    double cchi = chi, dtmp = 0;
+    if (sbar >= 1e-12) {  // below it the reference returns 0 and keeps the previous ddev
+        const bool athermal = c.law.stz_model >= 2;
+        if (athermal && sbar < c.law.s_y) {
+            F.ddev[k] = 0;  // exactly what the sub-stepping gives below yield
+        } else {
+            double ddev;
+            int iters;
+            dtmp = adaptive_plastic(c.law, sbar, cchi, ddev, dt, iters);
+            F.ddev[k] = ddev;
+        }
+    }
+    cchi -= uc * f1[4] + vc * f2[4];
+    const double cp = -uc * f1[0] - vc * f2[0] - third * dtmp * (2 * lt * tau - ltsq * (p + q + s) - ltsq * old_p) -
+                      2 * third * tau * (uy + vx) - third * (p - 2 * q) * (ux + vy) + 2 * third * s * (vy - ux);
+    const double cq = -uc * f1[1] - vc * f2[1] - dtmp * (q - ltsq / 6 * old_p) - third * tau * (uy + vx) +
+                      third * (p - 2 * q) * (ux + vy) + third * s * (vy - ux);
+    const double cs = -uc * f1[2] - vc * f2[2] - dtmp * (s + ltsq / 2 * old_p) - tau * (vx - uy) + (p + q) * (vy - ux);
+    const double ctau = -uc * f1[3] - vc * f2[3] - dtmp * (tau - lt * old_p) - (p + q) * (uy + vx) + s * (vx - uy);
+    B[CP][k] = p + cp;
+    B[CQ][k] = q + cq;
+    B[CS][k] = s + cs;
+    B[CTAU][k] = tau + ctau;
+    B[CCHI][k] = cchi;
+}
+
+// Dpl-mediated chi diffusion in sheared coordinates (shear_sim::chi_diffusion,
+// shear_sim.cc:437-460), from the old chi of buffer `old` into the new chi.
+__global__ void k_ct_chi_diffusion(ct_consts c, ct_fields F, int old, double lt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= c.m || j >= c.n) return;
+    const double dfac = 0.25 * c.chi_len * c.chi_len * c.mu_inv, dfacx = dfac * c.xsp * c.xsp,
+                 dfacy = dfac * c.ysp * c.ysp, lfac = c.dy * c.xsp * lt * 0.25;
+    const size_t k = gidx(c, i, j);
+    const long gm = c.gm;
+    const double *X = F.f[old][CCHI], *D = F.ddev;
+    const double Dd = D[k] + D[k - gm], Dl = D[k] + D[k - 1], Dr = D[k] + D[k + 1], Du = D[k] + D[k + gm];
+    const double Td = Dd * (X[k] - X[k - gm] - lfac * (X[k + 1] + X[k + 1 - gm] - X[k - 1] - X[k - 1 - gm]));
+    const double Tl = Dl * (X[k] - X[k - 1]), Tr = Dr * (X[k + 1] - X[k]);
+    const double Tu = Du * (X[k + gm] - X[k] - lfac * (X[k + 1 + gm] + X[k + 1] - X[k - 1 + gm] - X[k - 1]));
+    const double diffx = dfacx * (Tr - Tl), diffy = dfacy * (Tu - Td);
+    F.f[old ^ 1][CCHI][k] += (1 - lt) * diffx + diffy;
+}
+
+// set_boundaries, rows (shear_sim.cc:778-802): periodic copies with Y
+// shifted by -+ly, or the walls' corner values and extrapolated cells.
+__global__ void k_ct_rows(ct_consts c, ct_fields F, int b, double time) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.m) return;
+    double *const *G = F.f[b];
+    auto at = [&](int row) { return gidx(c, i, row); };
+    if (c.yp) {
+        const int n = c.n;
+        const int dst[4] = {-2, -1, n, n + 1}, src[4] = {n - 2, n - 1, 0, 1};
+        const double dY[4] = {-c.ly, -c.ly, c.ly, c.ly};
+        for (int r = 0; r < 4; r++) {
+            const size_t d = at(dst[r]), s = at(src[r]);
+            for (int f = CU; f <= CCHI; f++) G[f][d] = G[f][s];
+            G[CX][d] = G[CX][s] + 0.0;
+            G[CY][d] = G[CY][s] + dY[r];
+        }
+        return;
+    }
+    const double U = c.u_bdry;  // bdry_vel (shear_sim.hh:170-173)
+    const double bp = time < 1 ? c.u_bdry * time * time * 0.5 : c.u_bdry * (time - 0.5);
+    const double xl = c.ax + bp + i * c.dx, xu = c.ax - bp + i * c.dx;
+    auto corner = [&](size_t k, double u, double v, double Xv, double Yv) {
+        G[CU][k] = u;
+        G[CV][k] = v;
+        G[CX][k] = Xv;
+        G[CY][k] = Yv;
+    };
+    auto extrap = [&](size_t k, size_t k0, size_t k1) {
+        for (int f = CP; f <= CCHI; f++) G[f][k] = 2 * G[f][k0] - G[f][k1];
+    };
+    const int n = c.n;
+    corner(at(0), -U, 0, xl, c.ay);
+    extrap(at(-1), at(0), at(1));
+    corner(at(-1), -U, 0, xl, c.ay - c.dy);
+    extrap(at(-2), at(-1), at(0));
+    corner(at(n), U, 0, xu, c.by);
+    extrap(at(n), at(n - 1), at(n - 2));
+    corner(at(n + 1), U, 0, xu, c.by + c.dy);
+    extrap(at(n + 1), at(n), at(n - 1));
+}
+
+// set_boundaries, ghost columns of every row (shear_sim.cc:804-810).
+__global__ void k_ct_cols(ct_consts c, ct_fields F, int b) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x - 2;  // rows -2..n+1
+    if (r > c.n + 1) return;
+    double *const *G = F.f[b];
+    const int m = c.m;
+    const int dst[4] = {-2, -1, m, m + 1}, src[4] = {m - 2, m - 1, 0, 1};
+    const double dX[4] = {-c.lx, -c.lx, c.lx, c.lx};
+    for (int q = 0; q < 4; q++) {
+        const size_t d = gidx(c, dst[q], r), s = gidx(c, src[q], r);
+        for (int f = CU; f <= CCHI; f++) G[f][d] = G[f][s];
+        G[CX][d] = G[CX][s] + dX[q];
+        G[CY][d] = G[CY][s] + 0.0;
+    }
+}
+
+// Projection source at node (i,j) (shear_sim::projection_step,
+// shear_sim.cc:477-507, net_force :547-559): pre * net force, or -+(U, 0) on
+// the wall rows.
+__global__ void k_ct_source(ct_consts c, ct_fields F, int cur, double xfac, double yfac, double pa, double pb,
+                            double pc, double pd, double2 *b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= c.m || j >= c.lsn) return;
+    double2 out;
+    if (!c.yp && (j == 0 || j == c.n)) {
+        const double U = c.u_bdry;
+        out = j == 0 ? make_double2(-U, -0.) : make_double2(U, 0.);
+    } else {
+        const double *const *A = F.f[cur];
+        const size_t k3 = gidx(c, i, j), k2 = k3 - 1, k1 = k3 - c.gm, k0 = k1 - 1;
+        const double *P = A[CP], *Q = A[CQ], *S = A[CS], *T = A[CTAU];
+        const double fx = (-P[k0] + P[k1] - P[k2] + P[k3] - Q[k0] + Q[k1] - Q[k2] + Q[k3] + S[k0] - S[k1] + S[k2] -
+                           S[k3]) * xfac + (T[k0] + T[k1] - T[k2] - T[k3]) * yfac;
+        const double fy = (T[k0] - T[k1] + T[k2] - T[k3]) * xfac +
+                          (-P[k0] - P[k1] + P[k2] + P[k3] - Q[k0] - Q[k1] + Q[k2] + Q[k3] - S[k0] - S[k1] + S[k2] +
+                           S[k3]) * yfac;
+        out = make_double2(pa * fx + pb * fy, pc * fx + pd * fy);
+    }
+    b[(size_t)j * c.m + i] = out;
+}
+
+// Stress correction and velocities per cell (shear_sim.cc:509-543).
+__global__ void k_ct_project(ct_consts c, ct_fields F, int cur, const double2 *vel, double dt, double lt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= c.m || j >= c.n) return;
+    const double third = 1. / 3, L = c.K - 2 * third * c.mu, ltsq = lt * lt, mu = c.mu, lamb = c.lamb;
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
+    const int m = c.m, lsn = c.lsn;
+    const int d = i == m - 1 ? 1 - m : 1, e = j == lsn - 1 ? m * (1 - lsn) : m;
+    const double2 *vp = vel + (i + (size_t)m * j);
+    double *const *G = F.f[cur];
+    const size_t k = gidx(c, i, j);
+    G[CU][k] = vp->x;
+    G[CV][k] = vp->y;
+    const double ux = hx * (-vp->x + vp[d].x - vp[e].x + vp[d + e].x),
+                 uy = hy * (-vp->x - vp[d].x + vp[e].x + vp[d + e].x),
+                 vx = hx * (-vp->y + vp[d].y - vp[e].y + vp[d + e].y),
+                 vy = hy * (-vp->y - vp[d].y + vp[e].y + vp[d + e].y);
+    G[CP][k] += 2 * third * lt * lamb * mu * dt + 2 * third * lt * mu * uy -
+                (L + third * L * ltsq + 2 * third * mu) * (vy + ux) - 2 * third * mu * ltsq * ux +
+                2 * third * mu * lt * vx;
+    G[CQ][k] += third * lt * lamb * mu * dt + third * lt * mu * uy - (L * ltsq / 6 + third * mu) * (vy + ux) -
+                third * ltsq * mu * ux + third * lt * mu * vx;
+    G[CS][k] += -lamb * lt * mu * dt + lt * mu * (vx - uy) + (L * ltsq / 2 - mu) * vy +
+                (L * ltsq / 2 + mu + ltsq * mu) * ux;
+    G[CTAU][k] += lamb * mu * dt + mu * uy - lt * (L + mu) * (vy + ux) + mu * (1 + ltsq) * vx;
+}
+
+// The reference's mat (mat.hh): row-major 2x2 with its product and inverse.
+struct m22 {
+    double a, b, c, d;
+};
+inline m22 mmul(const m22 &x, const m22 &e) {
+    return m22{x.a * e.a + x.b * e.c, x.a * e.b + x.b * e.d, x.c * e.a + x.d * e.c, x.c * e.b + x.d * e.d};
+}
+inline m22 minv(const m22 &x) {
+    const double idet = 1.0 / (x.a * x.d - x.b * x.c);
+    return m22{idet * x.d, -idet * x.b, -idet * x.c, idet * x.a};
+}
+
+}  // namespace
+}  // namespace stzg
+
+using namespace stzg;
+
+struct stzg_ct {
+    stzg_ct_params P;
+    ct_consts c;
+    ct_fields F;
+    int cur = 0;
+    double time = 0;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<void *> owned;
+    stzg_tgmg *mg = nullptr;
+    stzg_tgmg_predict tp;
+    double2 *mg_b = nullptr, *mg_z = nullptr;
+    std::vector<double> table;
+    std::vector<int> cls;
+};
+
+namespace {
+
+int ct_alloc(stzg_ct *s, double **p, size_t count) {
+    void *q;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    s->owned.push_back(q);
+    STZG_CUDA(cudaMemsetAsync(q, 0, count * sizeof(double), s->st));
+    *p = (double *)q;
+    return STZG_OK;
+}
+
+const dim3 kB2(32, 8);
+inline dim3 g2(int m, int n) { return dim3(ceil_div(m, 32), ceil_div(n, 8)); }
+
+void boundaries(stzg_ct *s, int b) {
+    k_ct_rows<<<ceil_div(s->c.m, 128), 128, 0, s->st>>>(s->c, s->F, b, s->time);
+    note_launch();
+    k_ct_cols<<<ceil_div(s->c.n + 4, 128), 128, 0, s->st>>>(s->c, s->F, b);
+    note_launch();
+}
+
+// qs_multi::init(viscdt, lt) (coord_transforms qs_multi.cc:31-46): the
+// preconditioned blocks, as a two-stencil table (interior; wall rows that
+// carry only the identity) for the block multigrid, and the source's
+// preconditioner pre = regci * (1 lt; 0 1) (shear_sim.cc:476).
+void operator_for(stzg_ct *s, double lt, m22 &pre) {
+    const ct_consts &c = s->c;
+    const double ltsq = lt * lt, L = c.K - 2. / 3. * c.mu, mu = c.mu;
+    const double xsp2 = c.xsp * c.xsp, ysp2 = c.ysp * c.ysp, xsp = c.xsp, ysp = c.ysp;
+    m22 regh{(L + 2 * mu + ltsq * mu) * xsp2, (lt * mu + lt * ltsq * mu) * xsp2, -lt * (L + mu) * xsp2,
+             mu * (1 + ltsq) * xsp2};
+    m22 regv{mu * ysp2, lt * mu * ysp2, 0, (L + 2 * mu) * ysp2};
+    const m22 sum{regh.a + regv.a, regh.b + regv.b, regh.c + regv.c, regh.d + regv.d};
+    const m22 regc{-2. * sum.a, -2. * sum.b, -2. * sum.c, -2. * sum.d};
+    const m22 regci = minv(regc);
+    m22 regd{-0.5 * xsp * ysp * lt * mu, 0.25 * xsp * ysp * (L + mu - 2 * ltsq * mu), 0.25 * xsp * ysp * (L + mu),
+             -0.25 * xsp * ysp * lt * (L + 3 * mu)};
+    regh = mmul(regci, regh);
+    regv = mmul(regci, regv);
+    regd = mmul(regci, regd);
+    pre = mmul(regci, m22{1., lt, 0, 1.});
+    const m22 nd{-regd.a, -regd.b, -regd.c, -regd.d};
+    const m22 blocks[9] = {regd, regv, nd, regh, m22{1, 0, 0, 1}, regh, nd, regv, regd};
+    s->table.assign(2 * 36, 0.0);
+    for (int k = 0; k < 9; k++) {
+        s->table[4 * k + 0] = blocks[k].a;
+        s->table[4 * k + 1] = blocks[k].b;
+        s->table[4 * k + 2] = blocks[k].c;
+        s->table[4 * k + 3] = blocks[k].d;
+    }
+    s->table[36 + 16] = 1;  // wall stencil: identity centre (regz elsewhere, rego)
+    s->table[36 + 19] = 1;
+}
+
+int advection_step(stzg_ct *s, double dt) {
+    k_ct_advect<<<g2(s->c.m, s->c.n), kB2, 0, s->st>>>(s->c, s->F, s->cur, dt, s->time);
+    note_launch();
+    if (s->c.chi_len != 0) {
+        k_ct_chi_diffusion<<<g2(s->c.m, s->c.n), kB2, 0, s->st>>>(s->c, s->F, s->cur, s->c.lamb * s->time);
+        note_launch();
+    }
+    s->cur ^= 1;
+    s->time += dt;
+    boundaries(s, s->cur);
+    return STZG_OK;
+}
+
+int projection_step(stzg_ct *s, double dt, long *vcycles) {
+    const double lt = s->c.lamb * s->time;
+    m22 pre;
+    operator_for(s, lt, pre);
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    STZG_CHECK(stzg_tgmg_set_operator(s->mg, s->table.data(), 2, s->cls.data()));
+    const double xfac = 0.5 / dt * s->c.xsp, yfac = 0.5 / dt * s->c.ysp;
+    k_ct_source<<<g2(s->c.m, s->c.lsn), kB2, 0, s->st>>>(s->c, s->F, s->cur, xfac, yfac, pre.a, pre.b, pre.c,
+                                                        pre.d, s->mg_b);
+    note_launch();
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    int it = 0;
+    const int st = stzg_tgmg_solve(s->mg, STZG_TGMG_VCYCLE, &s->tp, 1.0, 1, 1, 10, &it, nullptr);
+    if (st != STZG_OK) return st;
+    if (vcycles) *vcycles += it;
+    k_ct_project<<<g2(s->c.m, s->c.n), kB2, 0, s->st>>>(s->c, s->F, s->cur, s->mg_z, dt, lt);
+    note_launch();
+    boundaries(s, s->cur);
+    return STZG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int stzg_ct_create(const stzg_ct_params *p, int device, stzg_ct **out) {
+    if (!out || !p) return fail(STZG_EINVAL, "null argument");
+    *out = nullptr;
+    if (p->m < 4 || p->n < 4 || (p->m & 1)) return fail(STZG_EINVAL, "grid needs m >= 4 even and n >= 4");
+    if (p->stz_model < 0 || p->stz_model > 3) return fail(STZG_EINVAL, "unknown STZ law");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(STZG_ENODEV, "no CUDA device");
+    if (device < 0 || device >= ndev) return fail(STZG_EINVAL, "device ordinal out of range");
+    STZG_CUDA(cudaSetDevice(device));
+    stzg_ct *s = new stzg_ct;
+    s->P = *p;
+    s->device = device;
+    auto bail = [&](int st) {
+        stzg_ct_destroy(s);
+        return st;
+    };
+    ct_consts &c = s->c;
+    c.m = p->m;
+    c.n = p->n;
+    c.gm = p->m + 4;
+    c.yp = p->y_prd ? 1 : 0;
+    c.lsn = c.yp ? p->n : p->n + 1;
+    c.ax = p->ax;
+    c.ay = p->ay;
+    c.bx = p->bx;
+    c.by = p->by;
+    c.lx = p->bx - p->ax;
+    c.ly = p->by - p->ay;
+    c.dx = c.lx / p->m;
+    c.dy = c.ly / p->n;
+    c.xsp = 1. / c.dx;
+    c.ysp = 1. / c.dy;
+    c.mu = p->mu;
+    c.mu_inv = 1. / p->mu;
+    c.K = p->K;
+    c.chi_len = p->chi_len;
+    c.lamb = p->lamb;
+    c.u_bdry = p->u_bdry;
+    stz_law_params<double> &L = c.law;
+    L.stz_model = p->stz_model;
+    L.t_model = p->t_model;
+    L.substep_cap = 1 << 22;
+    L.t_scale = p->t_scale;
+    L.adapt_fac = p->adapt_fac;
+    L.theta = p->theta;
+    L.Delta = p->Delta;
+    L.tau0 = p->tau0;
+    L.kappa = p->kappa;
+    L.rho = p->rho;
+    L.mu = p->mu;
+    L.c0 = p->c0;
+    L.Omegaeps0 = p->Omegaeps0;
+    L.chi_inf = p->chi_inf;
+    L.s_y = 1;  // s0 of this variant's stz_dynamics (stz_model.hh:20)
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess)
+        return bail(fail(STZG_ECUDA, "stream/event creation failed"));
+    const size_t pts = (size_t)(p->m + 4) * (p->n + 4);
+    int st;
+    for (int b = 0; b < 2; b++)
+        for (int f = 0; f < CF; f++)
+            if ((st = ct_alloc(s, &s->F.f[b][f], pts)) != STZG_OK) return bail(st);
+    if ((st = ct_alloc(s, &s->F.ddev, pts)) != STZG_OK) return bail(st);
+    // the block multigrid on the m x lsn nodes; wall rows carry the identity
+    s->cls.assign((size_t)p->m * c.lsn, 0);
+    if (!c.yp)
+        for (int i = 0; i < p->m; i++) s->cls[i] = s->cls[(size_t)p->n * p->m + i] = 1;
+    m22 pre;
+    operator_for(s, 0.0, pre);
+    const double a = DBL_EPSILON * 1e4 * 2.;  // acc = tgmg_accuracy(2., 1e4), qs_multi.cc:11
+    if ((st = stzg_tgmg_create_block(p->m, c.lsn, 1, c.yp, 2, s->table.data(), 2, s->cls.data(), a * a, device,
+                                     &s->mg)) != STZG_OK)
+        return bail(st);
+    stzg_tgmg_predict_init(&s->tp);
+    double *b, *z;
+    if ((st = stzg_tgmg_device_arrays(s->mg, &b, &z)) != STZG_OK) return bail(st);
+    s->mg_b = (double2 *)b;
+    s->mg_z = (double2 *)z;
+    if (cudaStreamSynchronize(s->st) != cudaSuccess) return bail(fail(STZG_ECUDA, "setup failed"));
+    *out = s;
+    return STZG_OK;
+}
+
+int stzg_ct_destroy(stzg_ct *s) {
+    if (!s) return STZG_OK;
+    cudaSetDevice(s->device);
+    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->mg) stzg_tgmg_destroy(s->mg);
+    for (void *p : s->owned) cudaFree(p);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return STZG_OK;
+}
+
+int stzg_ct_init_fields(stzg_ct *s, int chi_case, double tem_base, double tem_delta) {
+    if (!s || chi_case < 0 || chi_case > 2) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CUDA(cudaSetDevice(s->device));
+    const ct_consts &c = s->c;
+    const stzg_ct_params &P = s->P;
+    const double chi0 = tem_base / P.TZ, chi1 = tem_delta / P.TZ;
+    double sx[16], sy[16];
+    if (chi_case == 2)
+        for (int i = 0; i < 16; i++) {
+            sx[i] = c.ax + c.lx * (i + 0.5) * 0.0625;
+            sy[i] = 0.2 * sin(M_PI * 0.0625 * (2 * i + 1));
+        }
+    const size_t pts = (size_t)c.gm * (c.n + 4);
+    std::vector<double> h[CF];
+    for (int f = 0; f < CF; f++) h[f].assign(pts, 0.0);
+    // shear_sim::init_fields (shear_sim.cc:59-131)
+    for (int j = 0; j < (c.yp ? c.n : c.n + 1); j++) {
+        const double Y = c.ay + j * c.dy, Ys = Y + 0.5 * c.dy;
+        for (int i = 0; i < c.m; i++) {
+            const size_t k = (size_t)(j + 2) * c.gm + (i + 2);
+            const double X = c.ax + i * c.dx, Xs = X + 0.5 * c.dx;
+            h[CU][k] = Y * c.u_bdry;
+            h[CV][k] = 0;
+            double chi;
+            if (chi_case == 0) {
+                chi = chi0 + chi1 * exp(-200 * (Xs * Xs + Ys * Ys));
+            } else if (chi_case == 1) {
+                const double csa = cos(30 * M_PI / 180.), sia = sin(30 * M_PI / 180.);
+                double Xr = csa * Xs + sia * Ys, Yr = -sia * Xs + csa * Ys;
+                Xr = (Xr < -1) ? Xr + 1 : ((Xr > 1) ? Xr - 1 : 0);
+                chi = chi0 + chi1 * exp(-200 * (Xr * Xr + Yr * Yr));
+            } else {
+                double R = 1e100, Rt, Xr, Yr;
+                for (int q = 0; q < 16; q++) {
+                    Xr = sx[q] - Xs;
+                    if (Xr < -c.lx * 0.5) Xr += c.lx;
+                    if (Xr > c.lx * 0.5) Xr -= c.lx;
+                    Yr = sy[q] - Ys;
+                    Rt = Xr * Xr + Yr * Yr;
+                    if (Rt < R) R = Rt;
+                }
+                chi = chi0 + chi1 * exp(-200 * R);
+            }
+            h[CCHI][k] = chi;
+            h[CX][k] = X;
+            h[CY][k] = Y;
+        }
+    }
+    for (int f = 0; f < CF; f++)
+        STZG_CUDA(cudaMemcpyAsync(s->F.f[s->cur][f], h[f].data(), pts * sizeof(double), cudaMemcpyHostToDevice,
+                                  s->st));
+    boundaries(s, s->cur);
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+static double *ct_field_ptr(stzg_ct *s, int field) {
+    return field == STZG_CT_DDEV ? s->F.ddev : s->F.f[s->cur][field];
+}
+
+int stzg_ct_set_field(stzg_ct *s, int field, const double *host) {
+    if (!s || !host || field < 0 || field >= STZG_CT_FIELDS) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CUDA(cudaSetDevice(s->device));
+    const ct_consts &c = s->c;
+    double *d = ct_field_ptr(s, field);
+    STZG_CUDA(cudaMemcpy2DAsync(d + 2 * c.gm + 2, c.gm * sizeof(double), host, c.m * sizeof(double),
+                                c.m * sizeof(double), c.n + 1, cudaMemcpyHostToDevice, s->st));
+    if (field != STZG_CT_DDEV) boundaries(s, s->cur);
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+int stzg_ct_get_field(stzg_ct *s, int field, double *host) {
+    if (!s || !host || field < 0 || field >= STZG_CT_FIELDS) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CUDA(cudaSetDevice(s->device));
+    const ct_consts &c = s->c;
+    const double *d = ct_field_ptr(s, field);
+    STZG_CUDA(cudaMemcpy2DAsync(host, c.m * sizeof(double), d + 2 * c.gm + 2, c.gm * sizeof(double),
+                                c.m * sizeof(double), c.n + 1, cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+int stzg_ct_set_time(stzg_ct *s, double time) {
+    if (!s) return fail(STZG_EINVAL, "null handle");
+    s->time = time;
+    return STZG_OK;
+}
+
+int stzg_ct_get_time(stzg_ct *s, double *time) {
+    if (!s || !time) return fail(STZG_EINVAL, "null argument");
+    *time = s->time;
+    return STZG_OK;
+}
+
+int stzg_ct_step_qs(stzg_ct *s, double dt, int nsteps, long *vcycles, double *seconds) {
+    if (!s || !(dt > 0) || nsteps < 0) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CUDA(cudaSetDevice(s->device));
+    if (vcycles) *vcycles = 0;
+    STZG_CUDA(cudaEventRecord(s->ev0, s->st));
+    for (int k = 0; k < nsteps; k++) {
+        STZG_CHECK(advection_step(s, dt));
+        STZG_CHECK(projection_step(s, dt, vcycles));
+    }
+    STZG_CUDA(cudaEventRecord(s->ev1, s->st));
+    STZG_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    if (seconds) *seconds = 1e-3 * ms;
+    STZG_CUDA(cudaGetLastError());
+    return STZG_OK;
+}
+
+}  // extern "C"

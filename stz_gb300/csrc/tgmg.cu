@@ -19,6 +19,7 @@
 // The coarsest level (more than 10 points, the next coarsening would have
 // at most 10, tgmg_config.hh:23) is solved exactly with a dense inverse
 // where it has at most 1024 unknowns, else smoothed like the reference.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -627,11 +628,16 @@ template <int B> std::vector<double> dense_inverse(const host_level<B> &L, int x
             }
         }
     for (int r = 0; r < N; r++) X[(size_t)r * N + r] = 1;
+    // a pivot at rounding level means a singular level (a periodic operator
+    // that annihilates constants): no inverse, the bottom is smoothed
+    double amax = 0;
+    for (double v : A) amax = std::max(amax, std::fabs(v));
+    const double tiny = 1e-12 * amax;
     for (int c = 0; c < N; c++) {
         int p = c;
         for (int r = c + 1; r < N; r++)
             if (std::fabs(A[(size_t)r * N + c]) > std::fabs(A[(size_t)p * N + c])) p = r;
-        if (A[(size_t)p * N + c] == 0) return std::vector<double>();
+        if (!(std::fabs(A[(size_t)p * N + c]) > tiny)) return std::vector<double>();
         if (p != c)
             for (int k = 0; k < N; k++) {
                 std::swap(A[(size_t)p * N + k], A[(size_t)c * N + k]);

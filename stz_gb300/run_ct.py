@@ -1,0 +1,44 @@
+"""Timing harness of the step in sheared coordinates (include/stzg_ct.h): the
+reference driver's configuration (shear_coord_transform.cc:20-89: Vitreloy-1
+constants, linear athermal law, y periodic with lamb = 1e-3, chi_case 0)
+scaled to a larger grid; warm-up steps, then timed steps of the driver's
+dt = tf/600.  Prints one JSON line.
+
+    python -m stz_gb300.run_ct [--m 2048] [--n 1024] [--steps 20] [--warmup 3] [--walls]
+"""
+import argparse
+import json
+import time
+
+from .ct_sim import CtSim, transform_shear
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--m", type=int, default=2048)
+    ap.add_argument("--n", type=int, default=1024)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--walls", action="store_true")
+    args = ap.parse_args(argv)
+    yp = not args.walls
+    P = transform_shear(args.m, args.n, y_prd=yp)
+    dt = (0.5 / 1e-3 if yp else 3e6 / 2e4) / 600
+    sim = CtSim(P)
+    sim.init_fields(0, 580.0, 220.0)
+    sim.step_forward_quasistatic(dt, args.warmup)
+    t0 = time.perf_counter()
+    sim.step_forward_quasistatic(dt, args.steps)
+    wall = time.perf_counter() - t0
+    line = {"workload": "coord_transforms simple shear %dx%d, %s, quasi-static steps of dt %.6g" %
+                        (args.m, args.n, "y periodic, lamb 1e-3" if yp else "walls", dt),
+            "metric": "cell-steps/s", "value": args.m * args.n * args.steps / sim.seconds,
+            "ms_per_step": 1e3 * sim.seconds / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
+            "vcycles_per_step": sim.vcycles / args.steps, "steps": args.steps, "warmup": args.warmup}
+    print(json.dumps(line))
+    sim.close()
+    return line
+
+
+if __name__ == "__main__":
+    main()

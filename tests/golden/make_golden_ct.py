@@ -1,0 +1,82 @@
+"""Regenerates the golden fixtures of the coord_transforms step from the
+reference itself.
+
+Run where the SURGroup/STZ tree is available (default /root/reference,
+override with STZ_REFERENCE_ROOT):
+
+    python tests/golden/make_golden_ct.py
+
+It builds oracle/_ref/libctref.so (oracle/build_ref.sh: the reference's
+esim/coord_transforms/simple_shear sources with oracle/ref_ct_driver.cc), sets
+up the driver's Vitreloy configuration (shear_coord_transform.cc:20-89) on a
+small grid with shear_sim::init_fields, runs step_forward_quasistatic, and
+stores the initial and final fields (rows 0..n), the time and the V-cycle
+count as tests/golden/ct_*.npz.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.bind_ct import FIELDS, ReferenceCt  # noqa: E402
+from stz_gb300.ct_sim import transform_shear  # noqa: E402
+
+# name -> (m, n, y_prd, chi_case, tem_base, tem_delta, dt, steps, lead, extra params)
+# dt: the driver's frame interval over its 5 steps (tf/600); past about 40
+# steps on these grids the periodic case's solve stops converging in the
+# reference (exit 1), so the runs end before.  Stress passes yield (plastic
+# flow) in each case.  With y periodic the elasticity operator annihilates
+# rigid translations and the reference's velocity keeps whatever translation
+# its own Gauss-Seidel iterates leave, which then moves the fields; those
+# fixtures record one step (`steps` = 1) from the state after `lead` steps,
+# so that a solver of another ordering can be compared field by field.
+CASES = {
+    "ct_prd64x32": (64, 32, True, 0, 580.0, 220.0, 0.5 / 1e-3 / 600, 1, 39, {}),
+    "ct_prd48x24_line": (48, 24, True, 1, 580.0, 220.0, 0.5 / 1e-3 / 600, 1, 37, {}),
+    "ct_wall64x32": (64, 32, False, 0, 580.0, 220.0, 3e6 / 2e4 / 600, 60, 0, {}),
+    "ct_prd32x32_nodiff": (32, 32, True, 2, 580.0, 220.0, 0.5 / 1e-3 / 600, 1, 39, {"chi_len": 0.0}),
+    "ct_prd64x32_elastic": (64, 32, True, 0, 580.0, 220.0, 0.5 / 1e-3 / 600, 1, 12, {}),
+}
+
+
+def make(name, case):
+    m, n, yp, cc, base, delta, dt, steps, lead, extra = case
+    P = transform_shear(m, n, y_prd=yp, **extra)
+    ref = ReferenceCt(P)
+    ref.init_fields(cc, base, delta)
+    ref.steps(dt, lead)
+    time0 = ref.time
+    init = ref.fields()
+    ref.steps(dt, steps)
+    final = ref.fields()
+    out = {"init_" + k: v for k, v in init.items()}
+    out.update({"final_" + k: v for k, v in final.items()})
+    params = {k: getattr(P, k) for k, _ in P._fields_}
+    meta = {"params": params, "chi_case": cc, "dt": dt, "steps": steps, "lead": lead, "time0": time0,
+            "time": ref.time, "vcount": ref.vcount}
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    dev = np.sqrt(3 * final["q"] ** 2 + final["s"] ** 2 + final["tau"] ** 2)[:-1]
+    print(name, "time", ref.time, "vcount", ref.vcount, "max dev", dev.max(), "ddev", np.abs(final["ddev"]).max())
+    ref.close()
+
+
+def main(argv):
+    names = argv[1:] or list(CASES)
+    if len(names) == 1:
+        make(names[0], CASES[names[0]])
+        return
+    # one process per case: the reference reads never-written ghost values
+    # (ddev) and fresh allocations, which are zero only in a fresh process
+    import subprocess
+    for name in names:
+        subprocess.check_call([sys.executable, os.path.abspath(__file__), name])
+
+
+if __name__ == "__main__":
+    main(sys.argv)

@@ -44,6 +44,16 @@ def test_exports_every_general_multigrid_symbol(lib):
     tgmg.load()
 
 
+def test_exports_every_sheared_step_symbol(lib):
+    from stz_gb300 import ct_sim
+    names = header_symbols("stzg_ct.h")
+    assert len(names) >= 8
+    for name in names:
+        assert hasattr(lib, name), name
+    assert sorted(ct_sim.EXPORTS) == names
+    ct_sim.load()
+
+
 def test_general_multigrid_without_gpu_returns_status(lib):
     import ctypes
     from stz_gb300 import tgmg
