@@ -914,32 +914,26 @@ __global__ void k_ff_residual(ff_op op, const float2 *__restrict__ zh, const flo
 }
 
 // ---------------------------------------------------------------------------
-// Fused top-level kernels (single precision).  A block (256 threads) owns a
-// tile of TCX x TCY coarse points and the 2TCX x 2TCY fine points below them.
-// It stages z and b of the tile plus a halo in shared memory, runs both
-// colours of the Gauss-Seidel sweep there (recomputing the halo points that
-// neighbouring blocks own, with the same arithmetic, so every copy agrees),
-// and then either restricts the residual (down) or, after adding the
-// prolongation, writes the swept tile (up).  One launch replaces the five or
-// three launches of the colour-by-colour path; HBM sees z and b once per
-// sweep.
+// Streaming top-level kernels (single precision).  A warp owns a strip of 64
+// fine columns and marches down the rows of its tile with a register
+// window: lane L holds the node pair (xs + 2L, xs + 2L + 1) of each row as a
+// float4 (x and y of the even node, x and y of the odd node), neighbours in
+// x come from the adjacent lanes by shuffles and neighbours in y from the
+// window.  Each row step takes one new row of z and b (loaded two steps
+// ahead), sweeps colour 0 one row behind it and colour 1 two rows behind
+// (down: and evaluates the residual three rows behind), so that a warp
+// reads every node of its strip once and writes it once.  The outer lanes
+// and rows are halo: a colour update is exact one node further in than the
+// values it reads, and the owned columns and rows are those the two colours
+// (and the residual) still reach exactly.  The sweep reads z_in and writes
+// z_out, different arrays, so the halo a warp recomputes never sees another
+// warp's results.
 //
-// Shared-memory layout: the x and y components of z and b live in four
-// separate planes (row stride W floats, plane stride a multiple of 32
-// floats).  In a colour a lane updates one component of one node, the x
-// component where (i+j)&1 equals the colour and the y component elsewhere,
-// with consecutive lanes on consecutive nodes of a row: the lanes alternate
-// between the x and the y plane at consecutive columns, so each load of a
-// warp touches 32 distinct banks (one wavefront).  A node's colour-1
-// component has a zero residual after the sweep (up to rounding: it was the
-// last unknown updated and none of its neighbours changed since), so the
-// residual is evaluated for the colour-0 component only.
-
-constexpr int TCX = 32, TCY = 8;
-constexpr int DW = 2 * TCX + 7, DH = 2 * TCY + 7;   // down: fine x in [2I0-4, 2I1+2]
-constexpr int UW = 2 * TCX + 4, UH = 2 * TCY + 4;   // up:   fine x in [2I0-2, 2I1+1]
-constexpr int kFusedThreads = 256;                 // blockDim (32, 8)
-constexpr int kFusedMinWidth = 2 * TCX + 16;       // no self-aliasing of the periodic halo
+// Colour c updates the x component of nodes with (i + j) & 1 == c and the y
+// component of the others (qs_multi::mul_a couples x to x on edge
+// neighbours and to y on corners only, qs_multi.hh:41-50, so each colour is
+// a set of independent unknowns); with xs even, the even node of a pair
+// updates x in colour c exactly when (j & 1) == c.
 
 __device__ __forceinline__ int wrapx(int x, int m) { return x < 0 ? x + m : (x >= m ? x - m : x); }
 
@@ -948,208 +942,242 @@ __device__ __forceinline__ int wrapx(int x, int m) { return x < 0 ? x + m : (x >
     for (int k_ = threadIdx.y * blockDim.x + threadIdx.x; k_ < (RH) * (RW); k_ += blockDim.x * blockDim.y) \
         if (const int ty = (R0) + k_ / (RW), tx = (C0) + k_ % (RW); true)
 
-// Plane stride of a W x H tile, padded to whole 32-float bank rows.
-template <int W, int H> __host__ __device__ constexpr int plane_stride() { return ((W * H + 31) / 32) * 32; }
+constexpr int kFusedThreads = 256;     // blockDim of the coarse tile kernels
+constexpr int kFusedMinWidth = 80;     // narrowest even periodic line of the tile and strip kernels
+constexpr int kMarchWarps = 4;         // warps (row tiles) per block of the top-level kernels
+constexpr int kMarchRows = 16;         // coarse rows per warp tile
+constexpr int kDownCols = 28;          // coarse columns per strip (down): fine [xs + 4, xs + 60)
+constexpr int kUpCols = 30;            // coarse columns per strip (up):   fine [xs + 2, xs + 62)
 
-// One colour of the top-level sweep on tile rows/columns [LO, H-1-LO] x
-// [LO, W-1-LO]; planes v = (zx, zy, bx, by).
-template <typename T, int W, int H, int LO>
-__device__ inline void plane_top_color(const top_op<T> &op, T *v, int x0, int y0, int n, int color) {
-    constexpr int P = plane_stride<W, H>(), RW = W - 2 * LO, RH = H - 2 * LO;
-    TILE_FOR(RH, RW, LO, LO, ty, tx) {
-        const int gy = y0 + ty;
-        if (gy < 0 || gy >= n) continue;
-        const bool ux = ((x0 + tx + gy) & 1) == color;  // this lane updates x (else y)
-        const int o = ty * W + tx;
-        T *S = v + (ux ? 0 : P);
-        const T *O = v + (ux ? P : 0);
-        const T bb = v[(ux ? 2 * P : 3 * P) + o];
-        if (gy == 0 || gy == n - 1) {
-            S[o] = (ux ? op.ibcxx : op.ibcyy) * bb;
-            continue;
+// Off-diagonal sums of the two equations a pair updates in one colour, in
+// the association of the per-node form (x - the 4 edge terms - the 4 corner
+// terms).  ex: the even node's equation is the x one (and the odd node's
+// the y one); d, c, u: the rows below, at and above.
+struct pair_sums {
+    float a0, a1;
+};
+
+__device__ __forceinline__ pair_sums march_offdiag(const top_op<float> &op, const float4 &d, const float4 &c,
+                                                   const float4 &u, bool ex) {
+    constexpr unsigned F = 0xffffffffu;
+    pair_sums s;
+    if (ex) {
+        const float xl = __shfl_up_sync(F, c.z, 1);    // x(a-1, j)
+        const float dl = __shfl_up_sync(F, d.w, 1);    // y(a-1, j-1)
+        const float ul = __shfl_up_sync(F, u.w, 1);    // y(a-1, j+1)
+        const float yr = __shfl_down_sync(F, c.y, 1);  // y(b+1, j)
+        const float ur = __shfl_down_sync(F, u.x, 1);  // x(b+1, j+1)
+        const float dr = __shfl_down_sync(F, d.x, 1);  // x(b+1, j-1)
+        s.a0 = op.Kmx * (xl + c.z) + op.my * (d.x + u.x) + op.qK * (dl + u.w - d.w - ul);
+        s.a1 = op.mx * (c.y + yr) + op.Kmy * (d.w + u.w) + op.qK * (d.x + ur - dr - u.x);
+    } else {
+        const float yl = __shfl_up_sync(F, c.w, 1);    // y(a-1, j)
+        const float dl = __shfl_up_sync(F, d.z, 1);    // x(a-1, j-1)
+        const float ul = __shfl_up_sync(F, u.z, 1);    // x(a-1, j+1)
+        const float xr = __shfl_down_sync(F, c.x, 1);  // x(b+1, j)
+        const float ur = __shfl_down_sync(F, u.y, 1);  // y(b+1, j+1)
+        const float dr = __shfl_down_sync(F, d.y, 1);  // y(b+1, j-1)
+        s.a0 = op.mx * (yl + c.w) + op.Kmy * (d.y + u.y) + op.qK * (dl + u.z - d.z - ul);
+        s.a1 = op.Kmx * (c.x + xr) + op.my * (d.z + u.z) + op.qK * (d.y + ur - dr - u.y);
+    }
+    return s;
+}
+
+// One colour on row j of the pair (the Dirichlet wall rows take z = regcbi*b).
+__device__ __forceinline__ void march_color(const top_op<float> &op, const float4 &d, float4 &c, const float4 &u,
+                                            const float4 &bb, int j, int n, int color) {
+    const bool ex = (j & 1) == color;
+    if (j == 0 || j == n - 1) {
+        if (ex) {
+            c.x = op.ibcxx * bb.x;
+            c.w = op.ibcyy * bb.w;
+        } else {
+            c.y = op.ibcyy * bb.y;
+            c.z = op.ibcxx * bb.z;
         }
-        const T cl = ux ? op.Kmx : op.mx, cd = ux ? op.my : op.Kmy;
-        const T a = cl * (S[o - 1] + S[o + 1]) + cd * (S[o - W] + S[o + W]) +
-                    op.qK * (O[o - W - 1] + O[o + W + 1] - O[o - W + 1] - O[o + W - 1]);
-        S[o] = (ux ? op.icxx : op.icyy) * (bb - a);
+        return;
+    }
+    const pair_sums s = march_offdiag(op, d, c, u, ex);
+    if (ex) {
+        c.x = op.icxx * (bb.x - s.a0);
+        c.w = op.icyy * (bb.w - s.a1);
+    } else {
+        c.y = op.icyy * (bb.y - s.a0);
+        c.z = op.icxx * (bb.z - s.a1);
     }
 }
 
+// Residual of the colour-0 equations of the pair on row j after the sweep
+// (the colour-1 ones are zero up to rounding: their unknowns were updated
+// last and none of their neighbours changed since).  .x belongs to the even
+// node, .y to the odd one; the x component of the even node when j is even.
+__device__ __forceinline__ float2 march_residual(const top_op<float> &op, const float4 &d, const float4 &c,
+                                                 const float4 &u, const float4 &bb, int j, int n) {
+    float2 r = make_float2(0.f, 0.f);
+    if (j <= 0 || j >= n - 1) return r;
+    const bool ex = (j & 1) == 0;
+    const pair_sums s = march_offdiag(op, d, c, u, ex);
+    if (ex) {
+        r.x = bb.x - s.a0 - op.cxx * c.x;
+        r.y = bb.w - s.a1 - op.cyy * c.w;
+    } else {
+        r.x = bb.y - s.a0 - op.cyy * c.y;
+        r.y = bb.z - s.a1 - op.cxx * c.z;
+    }
+    return r;
+}
+
+// Row j of a strip (pairs at xs + 2 lane, wrapped); zero outside the grid.
+__device__ __forceinline__ float4 march_load(const float2 *__restrict__ a, int j, int m, int n, int gx) {
+    if (j < 0 || j >= n) return make_float4(0.f, 0.f, 0.f, 0.f);
+    return __ldg(reinterpret_cast<const float4 *>(a + (size_t)j * m + gx));
+}
+
+// Full weighting (1,2,1)x(1,2,1)/4 of the residual rows 2J-1, 2J, 2J+1 (r0,
+// r1, r2) at the coarse point under the lane's even node, y rows through
+// halves_of for the walls.
+__device__ __forceinline__ float2 march_restrict(const float2 &r0, const float2 &r1, const float2 &r2, int J, int n) {
+    constexpr unsigned F = 0xffffffffu;
+    const float2 rr[3] = {r0, r1, r2};
+    float ax = 0, ay = 0;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float left = __shfl_up_sync(F, rr[q].y, 1);  // odd node of the lane to the left
+        const int fy = 2 * J + q - 1;
+        if (fy < 0 || fy >= n) continue;
+        const int hy = halves_of(fy, n, 0, J);
+        if (!hy) continue;
+        const float w1 = (float)hy * 0.25f, w2 = (float)(2 * hy) * 0.25f;
+        if (!(fy & 1)) {
+            // even row: x residual on the even nodes, y on the odd ones
+            ax += w2 * rr[q].x;
+            ay += w1 * left;
+            ay += w1 * rr[q].y;
+        } else {
+            ax += w1 * left;
+            ax += w1 * rr[q].y;
+            ay += w2 * rr[q].x;
+        }
+    }
+    return make_float2(ax, ay);
+}
+
 // Pre-smooth + residual + restriction of the top level (apply_r after one
-// gauss_seidel, tgmg.in.cc:313-320).
-template <typename T>
-__global__ void __launch_bounds__(kFusedThreads) k_top_down(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
-                                                         const typename vec2_t<T>::type *__restrict__ b, int m,
-                                                         int n, typename vec2_t<T>::type *__restrict__ bc, int cm,
-                                                         int cn) {
-    typedef typename vec2_t<T>::type V;
-    constexpr int P = plane_stride<DW, DH>();
-    __shared__ T v[4 * P];
-    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
-    const int x0 = 2 * I0 - 4, y0 = 2 * J0 - 4;
-    TILE_FOR(DH, DW, 0, 0, ty, tx) {
-        const int gy = y0 + ty;
-        V zz, bb;
-        zz.x = zz.y = bb.x = bb.y = 0;
-        if (gy >= 0 && gy < n) {
-            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
-            zz = z[g];
-            bb = b[g];
-        }
-        const int o = ty * DW + tx;
-        v[o] = zz.x;
-        v[P + o] = zz.y;
-        v[2 * P + o] = bb.x;
-        v[3 * P + o] = bb.y;
-    }
-    __syncthreads();
-    plane_top_color<T, DW, DH, 1>(op, v, x0, y0, n, 0);
-    __syncthreads();
-    plane_top_color<T, DW, DH, 2>(op, v, x0, y0, n, 1);
-    __syncthreads();
-    // residual of the colour-0 component over b; the colour-1 one is zero
-    TILE_FOR(DH - 6, DW - 6, 3, 3, ty, tx) {
-        const int gy = y0 + ty;
-        if (gy < 0 || gy >= n) continue;
-        const int o = ty * DW + tx;
-        const bool ux = ((x0 + tx + gy) & 1) == 0;
-        T r = 0;
-        if (gy != 0 && gy != n - 1) {
-            const T *S = v + (ux ? 0 : P), *O = v + (ux ? P : 0);
-            const T cl = ux ? op.Kmx : op.mx, cd = ux ? op.my : op.Kmy, cc = ux ? op.cxx : op.cyy;
-            const T a = cl * (S[o - 1] + S[o + 1]) + cd * (S[o - DW] + S[o + DW]) +
-                        op.qK * (O[o - DW - 1] + O[o + DW + 1] - O[o - DW + 1] - O[o + DW - 1]);
-            r = v[(ux ? 2 * P : 3 * P) + o] - a - cc * S[o];
-        }
-        v[(ux ? 2 * P : 3 * P) + o] = r;
-        v[(ux ? 3 * P : 2 * P) + o] = 0;
-    }
-    __syncthreads();
-    {
-        // full weighting (1,2,1)x(1,2,1)/4 on the periodic even line,
-        // rows through halves_of for the walls
-        const int cI = threadIdx.x, cJ = threadIdx.y, I = I0 + cI, J = J0 + cJ;
-        if (I < cm && J < cn) {
-            T ax = 0, ay = 0;
+// gauss_seidel, tgmg.in.cc:313-320): z_out = one sweep of z_in, bc = R(b - A z_out).
+__global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op, const float2 *__restrict__ zin,
+                                                               const float2 *__restrict__ b, int m, int n,
+                                                               float2 *__restrict__ zout, float2 *__restrict__ bc,
+                                                               int cm, int cn) {
+    const int lane = threadIdx.x & 31;
+    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kMarchRows;
+    if (J0 >= cn) return;
+    const int I0 = blockIdx.x * kDownCols;
+    const int xs = 2 * I0 - 4, y0 = 2 * J0;
+    const int gx = wrapx(xs + 2 * lane, m);
+    const int I = I0 + lane - 2;
+    const bool own = lane >= 2 && lane < 2 + kDownCols && I < cm;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 Z0 = zero, Z1 = zero, Z2 = zero, Z3 = zero, Z4 = zero;  // rows k-4 .. k
+    float4 B0 = zero, B1 = zero, B2 = zero, B3 = zero;             // rows k-3 .. k
+    float2 R0 = make_float2(0.f, 0.f), R1 = R0, R2 = R0;           // residual rows k-5 .. k-3
+    const int kb = y0 - 4, ke = y0 + 2 * kMarchRows + 2;
+    // two prefetch slots, used on alternate steps (no move of a pending load)
+    float4 pz[2], pb[2];
+    pz[0] = march_load(zin, kb, m, n, gx);
+    pb[0] = march_load(b, kb, m, n, gx);
+    pz[1] = march_load(zin, kb + 1, m, n, gx);
+    pb[1] = march_load(b, kb + 1, m, n, gx);
+    for (int k0 = kb; k0 <= ke; k0 += 2) {
 #pragma unroll
-            for (int dy = -1; dy <= 1; dy++) {
-                const int fy = 2 * J + dy;
-                if (fy < 0 || fy >= n) continue;
-                const int hy = halves_of(fy, n, 0, J);
-                if (!hy) continue;
-                const int o = (2 * cJ + 4 + dy) * DW + 2 * cI + 4;
-#pragma unroll
-                for (int dx = -1; dx <= 1; dx++) {
-                    const T wgt = (T)((dx == 0 ? 2 : 1) * hy) * (T)0.25;
-                    ax += wgt * v[2 * P + o + dx];
-                    ay += wgt * v[3 * P + o + dx];
+        for (int h = 0; h < 2; h++) {
+            const int k = k0 + h;
+            if (k > ke) break;
+            Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = Z4; Z4 = pz[h];
+            B0 = B1; B1 = B2; B2 = B3; B3 = pb[h];
+            if (k + 2 <= ke) {
+                pz[h] = march_load(zin, k + 2, m, n, gx);
+                pb[h] = march_load(b, k + 2, m, n, gx);
+            }
+            const int j0 = k - 1, j1 = k - 2, j2 = k - 3;
+            if (j0 >= y0 - 3 && j0 >= 0 && j0 < n) march_color(op, Z2, Z3, Z4, B2, j0, n, 0);
+            if (j1 >= y0 - 2 && j1 >= 0 && j1 < n) {
+                march_color(op, Z1, Z2, Z3, B1, j1, n, 1);
+                if (j1 >= y0 && j1 < y0 + 2 * kMarchRows && own && gx == xs + 2 * lane)
+                    *reinterpret_cast<float4 *>(zout + (size_t)j1 * m + gx) = Z2;
+            }
+            if (j2 >= y0 - 1) {
+                R0 = R1; R1 = R2;
+                R2 = march_residual(op, Z0, Z1, Z2, B0, j2, n);
+                if ((j2 & 1) && j2 >= y0 + 1) {
+                    const int J = (j2 - 1) >> 1;
+                    const float2 w = march_restrict(R0, R1, R2, J, n);
+                    if (own && J < cn) bc[(size_t)J * cm + I] = w;
                 }
             }
-            V w;
-            w.x = ax;
-            w.y = ay;
-            bc[(size_t)J * cm + I] = w;
-        }
-    }
-    TILE_FOR(2 * TCY, 2 * TCX, 4, 4, ty, tx) {
-        const int gy = y0 + ty, gx = x0 + tx;
-        if (gy < n && gx < m) {
-            const int o = ty * DW + tx;
-            V w;
-            w.x = v[o];
-            w.y = v[P + o];
-            z[(size_t)gy * m + gx] = w;
         }
     }
 }
 
 // Prolongation + post-smooth of the top level (apply_t of level 0, then
-// up_gs_iterations, tgmg.in.cc:323-327).
-template <typename T>
-__global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename vec2_t<T>::type *__restrict__ z,
-                                                       const typename vec2_t<T>::type *__restrict__ b, int m, int n,
-                                                       const typename vec2_t<T>::type *__restrict__ zc, int cm,
-                                                       int cn) {
-    typedef typename vec2_t<T>::type V;
-    constexpr int P = plane_stride<UW, UH>();
-    constexpr int CW = TCX + 3, CH = TCY + 3, CP = plane_stride<CW, CH>();
-    __shared__ T v[4 * P];
-    __shared__ T cs[2 * CP];
-    const int I0 = blockIdx.x * TCX, J0 = blockIdx.y * TCY;
-    const int x0 = 2 * I0 - 2, y0 = 2 * J0 - 2;
-    TILE_FOR(UH, UW, 0, 0, ty, tx) {
-        const int gy = y0 + ty;
-        V zz, bb;
-        zz.x = zz.y = bb.x = bb.y = 0;
-        if (gy >= 0 && gy < n) {
-            const size_t g = (size_t)gy * m + wrapx(x0 + tx, m);
-            zz = z[g];
-            bb = b[g];
-        }
-        const int o = ty * UW + tx;
-        v[o] = zz.x;
-        v[P + o] = zz.y;
-        v[2 * P + o] = bb.x;
-        v[3 * P + o] = bb.y;
-    }
-    TILE_FOR(CH, CW, 0, 0, ly, lx) {
-        const int J = J0 - 1 + ly;
-        V w;
-        w.x = w.y = 0;
-        if (J >= 0 && J < cn) w = zc[(size_t)J * cm + wrapx(I0 - 1 + lx, cm)];
-        cs[ly * CW + lx] = w.x;
-        cs[CP + ly * CW + lx] = w.y;
-    }
-    __syncthreads();
-    TILE_FOR(UH, UW, 0, 0, ty, tx) {
-        const int gy = y0 + ty;
-        if (gy < 0 || gy >= n) continue;
-        int cy[2], hy[2];
-        const int ny = p1d_halves(gy, n, 0, cy, hy);
-        // even periodic line: even fine points inject, odd ones average
-        const int gx = wrapx(x0 + tx, m);
-        const int c0 = gx >> 1, c1 = (gx == m - 1) ? 0 : c0 + 1;
-        const bool odd = gx & 1;
-        int l0 = c0 - (I0 - 1), l1 = c1 - (I0 - 1);
-        l0 += l0 < 0 ? cm : (l0 >= cm ? -cm : 0);
-        l1 += l1 < 0 ? cm : (l1 >= cm ? -cm : 0);
-        T ax = 0, ay = 0;
-        bool inside = true;
-        for (int q = 0; q < ny; q++) {
-            const int ly = cy[q] - (J0 - 1);
-            if (ly < 0 || ly >= CH || l0 < 0 || l0 >= CW || (odd && (l1 < 0 || l1 >= CW))) {
-                // wrapped copies far beyond a partial tile's owned columns:
-                // no owned output depends on them
-                inside = false;
-                continue;
+// up_gs_iterations, tgmg.in.cc:323-327): z_out = one sweep of z_in + P zc.
+// Fine node i takes coarse i/2 (even) or the mean of (i-1)/2 and (i+1)/2
+// (odd, wrapping on the even periodic line); rows through p1d_halves.
+__global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, const float2 *__restrict__ zin,
+                                                             const float2 *__restrict__ b, int m, int n,
+                                                             const float2 *__restrict__ zc, int cm, int cn,
+                                                             float2 *__restrict__ zout) {
+    const int lane = threadIdx.x & 31;
+    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kMarchRows;
+    if (J0 >= cn) return;
+    const int I0 = blockIdx.x * kUpCols;
+    const int xs = 2 * I0 - 2, y0 = 2 * J0;
+    const int gx = wrapx(xs + 2 * lane, m);
+    const int c0 = gx >> 1, c1 = c0 + 1 == cm ? 0 : c0 + 1;  // coarse columns of the pair
+    const bool own = lane >= 1 && lane < 1 + kUpCols && xs + 2 * lane < m;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 Z0 = zero, Z1 = zero, Z2 = zero, Z3 = zero;  // rows k-3 .. k
+    float4 B0 = zero, B1 = zero, B2 = zero;            // rows k-2 .. k
+    const int kb = y0 - 2, ke = y0 + 2 * kMarchRows + 1;
+    float4 pz[2], pb[2];
+    pz[0] = march_load(zin, kb, m, n, gx);
+    pb[0] = march_load(b, kb, m, n, gx);
+    pz[1] = march_load(zin, kb + 1, m, n, gx);
+    pb[1] = march_load(b, kb + 1, m, n, gx);
+    for (int k0 = kb; k0 <= ke; k0 += 2) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int k = k0 + h;
+            if (k > ke) break;
+            float4 zn = pz[h];
+            B0 = B1; B1 = B2; B2 = pb[h];
+            if (k + 2 <= ke) {
+                pz[h] = march_load(zin, k + 2, m, n, gx);
+                pb[h] = march_load(b, k + 2, m, n, gx);
             }
-            const T wy = (T)hy[q] * (T)0.25;
-            if (odd) {
-                ax += wy * (cs[ly * CW + l0] + cs[ly * CW + l1]);
-                ay += wy * (cs[CP + ly * CW + l0] + cs[CP + ly * CW + l1]);
-            } else {
-                ax += (T)2 * wy * cs[ly * CW + l0];
-                ay += (T)2 * wy * cs[CP + ly * CW + l0];
+            if (k >= 0 && k < n) {
+                int cy[2], hy[2];
+                const int ny = p1d_halves(k, n, 0, cy, hy);
+                float ax = 0, ay = 0, bx = 0, by = 0;
+                for (int q = 0; q < ny; q++) {
+                    const float wy = (float)hy[q] * 0.25f;
+                    const float2 v0 = __ldg(zc + (size_t)cy[q] * cm + c0), v1 = __ldg(zc + (size_t)cy[q] * cm + c1);
+                    ax += 2.f * wy * v0.x;
+                    ay += 2.f * wy * v0.y;
+                    bx += wy * (v0.x + v1.x);
+                    by += wy * (v0.y + v1.y);
+                }
+                zn.x += ax;
+                zn.y += ay;
+                zn.z += bx;
+                zn.w += by;
             }
-        }
-        if (!inside) ax = ay = 0;
-        const int o = ty * UW + tx;
-        v[o] += ax;
-        v[P + o] += ay;
-    }
-    __syncthreads();
-    plane_top_color<T, UW, UH, 1>(op, v, x0, y0, n, 0);
-    __syncthreads();
-    plane_top_color<T, UW, UH, 2>(op, v, x0, y0, n, 1);
-    __syncthreads();
-    TILE_FOR(2 * TCY, 2 * TCX, 2, 2, ty, tx) {
-        const int gy = y0 + ty, gx = x0 + tx;
-        if (gy < n && gx < m) {
-            const int o = ty * UW + tx;
-            V w;
-            w.x = v[o];
-            w.y = v[P + o];
-            z[(size_t)gy * m + gx] = w;
+            Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = zn;
+            const int j0 = k - 1, j1 = k - 2;
+            if (j0 >= y0 - 1 && j0 >= 0 && j0 < n) march_color(op, Z1, Z2, Z3, B1, j0, n, 0);
+            if (j1 >= y0 && j1 < n) {
+                march_color(op, Z0, Z1, Z2, B0, j1, n, 1);
+                if (own) *reinterpret_cast<float4 *>(zout + (size_t)j1 * m + xs + 2 * lane) = Z1;
+            }
         }
     }
 }
@@ -1157,9 +1185,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_top_up(top_op<T> op, typename
 // Full weighting of the residual held in rs at coarse point (I, J); the fine
 // point 2I+dx sits at tile column cx0 + dx.  Periodic x with an even line
 // always has the weights (1, 2, 1)/2.
-template <typename T, int W>
-__device__ __forceinline__ typename vec2_t<T>::type restrict_at(typename vec2_t<T>::type (*rs)[W], int I, int J,
-                                                                int n, int cx0, int cy0) {
+template <typename T, typename Tile>
+__device__ __forceinline__ typename vec2_t<T>::type restrict_at(Tile &rs, int I, int J, int n, int cx0, int cy0) {
     typedef typename vec2_t<T>::type V;
     T ax = 0, ay = 0;
 #pragma unroll
@@ -1171,7 +1198,7 @@ __device__ __forceinline__ typename vec2_t<T>::type restrict_at(typename vec2_t<
 #pragma unroll
         for (int dx = -1; dx <= 1; dx++) {
             const T wgt = (T)((dx == 0 ? 2 : 1) * hy) * (T)0.25;
-            const V r = rs[cy0 + dy][cx0 + dx];
+            const V r = rs(cy0 + dy, cx0 + dx);
             ax += wgt * r.x;
             ay += wgt * r.y;
         }
@@ -1193,24 +1220,35 @@ __device__ __forceinline__ typename vec2_t<T>::type restrict_at(typename vec2_t<
 // Coarse tiles of TX x TY points; smaller levels take smaller tiles (more
 // blocks, shorter phases), see lev_tile below.
 
-template <typename T, int W>
-__device__ __forceinline__ typename vec2_t<T>::type lev_offdiag_tile(const stencil9<T> &s,
-                                                                     typename vec2_t<T>::type (*zs)[W], int ty, int tx,
+// A W x H shared-memory tile of (x, y) pairs with each row stored
+// parity-major: the even tile columns first, then the odd ones.  A colour of
+// the four-colour sweep takes every other column; in this layout the points
+// of one colour, and their neighbours at tx - 1 and tx + 1, lie at
+// consecutive addresses, so a warp's 8-byte loads need two shared-memory
+// wavefronts instead of the four of the natural layout (stride 16 bytes).
+template <typename V, int W, int H> struct ptile {
+    static constexpr int HALF = (W + 1) / 2;
+    V d[H][2 * HALF];
+    __device__ __forceinline__ V &operator()(int ty, int tx) { return d[ty][(tx & 1) * HALF + (tx >> 1)]; }
+};
+
+template <typename T, typename Tile>
+__device__ __forceinline__ typename vec2_t<T>::type lev_offdiag_tile(const stencil9<T> &s, Tile &zs, int ty, int tx,
                                                                      bool has_d, bool has_u) {
     typedef typename vec2_t<T>::type V;
     V a;
     a.x = a.y = 0;
     if (has_d) {
-        madd(a, s.e[0], zs[ty - 1][tx - 1]);
-        madd(a, s.e[1], zs[ty - 1][tx]);
-        madd(a, s.e[2], zs[ty - 1][tx + 1]);
+        madd(a, s.e[0], zs(ty - 1, tx - 1));
+        madd(a, s.e[1], zs(ty - 1, tx));
+        madd(a, s.e[2], zs(ty - 1, tx + 1));
     }
-    madd(a, s.e[3], zs[ty][tx - 1]);
-    madd(a, s.e[5], zs[ty][tx + 1]);
+    madd(a, s.e[3], zs(ty, tx - 1));
+    madd(a, s.e[5], zs(ty, tx + 1));
     if (has_u) {
-        madd(a, s.e[6], zs[ty + 1][tx - 1]);
-        madd(a, s.e[7], zs[ty + 1][tx]);
-        madd(a, s.e[8], zs[ty + 1][tx + 1]);
+        madd(a, s.e[6], zs(ty + 1, tx - 1));
+        madd(a, s.e[7], zs(ty + 1, tx));
+        madd(a, s.e[8], zs(ty + 1, tx + 1));
     }
     return a;
 }
@@ -1239,8 +1277,8 @@ __device__ __forceinline__ const stencil9<T> &tile_stencil(const level_view<T> &
 // colour's rows and columns are enumerated with compile-time strides.
 template <typename T, int W, int H, int LO>
 __device__ inline void tile_lev_color(const level_view<T> &L, const stencil9<T> *rows,
-                                      typename vec2_t<T>::type (*zs)[W], typename vec2_t<T>::type (*bs)[W], int x0,
-                                      int y0, int cx, int cy) {
+                                      ptile<typename vec2_t<T>::type, W, H> &zs,
+                                      ptile<typename vec2_t<T>::type, W, H> &bs, int x0, int y0, int cx, int cy) {
     typedef typename vec2_t<T>::type V;
     constexpr int NC = (W - 2 * LO + 1) / 2, NRW = (H - 2 * LO + 1) / 2;
     const int ty0 = LO + ((cy - (y0 + LO)) & 1), tx0 = LO + ((cx - (x0 + LO)) & 1);
@@ -1251,13 +1289,13 @@ __device__ inline void tile_lev_color(const level_view<T> &L, const stencil9<T> 
         const int gy = y0 + ty;
         if (gy < 0 || gy >= L.n) continue;
         const stencil9<T> &s = tile_stencil(L, rows, ty, wrapx(x0 + tx, L.m), gy);
-        const V a = lev_offdiag_tile<T, W>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
-        const V bb = bs[ty][tx];
+        const V a = lev_offdiag_tile<T>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
+        const V bb = bs(ty, tx);
         const T rx = bb.x - a.x, ry = bb.y - a.y;
         V o;
         o.x = s.e[9].a * rx + s.e[9].b * ry;
         o.y = s.e[9].c * rx + s.e[9].d * ry;
-        zs[ty][tx] = o;
+        zs(ty, tx) = o;
     }
 }
 
@@ -1265,8 +1303,7 @@ template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, level_view<T> C) {
     typedef typename vec2_t<T>::type V;
     constexpr int LDW = 2 * TX + 11, LDH = 2 * TY + 11;  // fine x in [2I0-6, 2I1+4]
-    __shared__ V zs[LDH][LDW];
-    __shared__ V bs[LDH][LDW];
+    __shared__ ptile<V, LDW, LDH> zs, bs;
     __shared__ stencil9<T> rows[LDH];
     const int I0 = blockIdx.x * TX, J0 = blockIdx.y * TY;
     const int x0 = 2 * I0 - 6, y0 = 2 * J0 - 6;
@@ -1276,8 +1313,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, lev
         V bb, zz;
         bb.x = bb.y = zz.x = zz.y = 0;
         if (gy >= 0 && gy < L.n) bb = L.b[(size_t)gy * L.m + wrapx(x0 + tx, L.m)];
-        zs[ty][tx] = zz;
-        bs[ty][tx] = bb;
+        zs(ty, tx) = zz;
+        bs(ty, tx) = bb;
     }
     __syncthreads();
     tile_lev_color<T, LDW, LDH, 1>(L, rows, zs, bs, x0, y0, 0, 0);
@@ -1292,21 +1329,21 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_down(level_view<T> L, lev
         const int gy = y0 + ty;
         if (gy < 0 || gy >= L.n) continue;
         const stencil9<T> &s = tile_stencil(L, rows, ty, wrapx(x0 + tx, L.m), gy);
-        V a = lev_offdiag_tile<T, LDW>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
-        madd(a, s.e[4], zs[ty][tx]);
+        V a = lev_offdiag_tile<T>(s, zs, ty, tx, gy > 0, gy < L.n - 1);
+        madd(a, s.e[4], zs(ty, tx));
         V r;
-        r.x = bs[ty][tx].x - a.x;
-        r.y = bs[ty][tx].y - a.y;
-        bs[ty][tx] = r;
+        r.x = bs(ty, tx).x - a.x;
+        r.y = bs(ty, tx).y - a.y;
+        bs(ty, tx) = r;
     }
     __syncthreads();
     TILE_FOR(TY, TX, 0, 0, cJ, cI) {
         const int I = I0 + cI, J = J0 + cJ;
-        if (I < C.m && J < C.n) C.b[(size_t)J * C.m + I] = restrict_at<T, LDW>(bs, I, J, L.n, 2 * cI + 6, 2 * cJ + 6);
+        if (I < C.m && J < C.n) C.b[(size_t)J * C.m + I] = restrict_at<T>(bs, I, J, L.n, 2 * cI + 6, 2 * cJ + 6);
     }
     TILE_FOR(2 * TY, 2 * TX, 6, 6, ty, tx) {
         const int gy = y0 + ty, gx = x0 + tx;
-        if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
+        if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs(ty, tx);
     }
 }
 
@@ -1314,8 +1351,7 @@ template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level_view<T> C) {
     typedef typename vec2_t<T>::type V;
     constexpr int LUW = 2 * TX + 8, LUH = 2 * TY + 8;    // fine x in [2I0-4, 2I1+3]
-    __shared__ V zs[LUH][LUW];
-    __shared__ V bs[LUH][LUW];
+    __shared__ ptile<V, LUW, LUH> zs, bs;
     __shared__ V cs[TY + 5][TX + 5];
     __shared__ stencil9<T> rows[LUH];
     const int I0 = blockIdx.x * TX, J0 = blockIdx.y * TY;
@@ -1330,8 +1366,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
             zz = L.z[g];
             bb = L.b[g];
         }
-        zs[ty][tx] = zz;
-        bs[ty][tx] = bb;
+        zs(ty, tx) = zz;
+        bs(ty, tx) = bb;
     }
     TILE_FOR(TY + 5, TX + 5, 0, 0, ly, lx) {
         const int J = J0 - 2 + ly;
@@ -1373,8 +1409,8 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
                 }
             }
             if (!inside) ax = ay = 0;
-            zs[ty][tx].x += ax;
-            zs[ty][tx].y += ay;
+            zs(ty, tx).x += ax;
+            zs(ty, tx).y += ay;
         }
     }
     __syncthreads();
@@ -1388,7 +1424,243 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
     __syncthreads();
     TILE_FOR(2 * TY, 2 * TX, 4, 4, ty, tx) {
         const int gy = y0 + ty, gx = x0 + tx;
-        if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs[ty][tx];
+        if (gy < L.n && gx < L.m) L.z[(size_t)gy * L.m + gx] = zs(ty, tx);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Streaming coarse-level kernels (single precision, levels with one stencil
+// class per row and an even periodic line).  The strip-and-window scheme of
+// the top level with the four-colour block Gauss-Seidel of the stored
+// Galerkin stencils: an even row takes colours (0,0) and (1,0) while both of
+// its odd neighbour rows still hold their values from before the sweep, and
+// the odd row below it then takes (0,1) and (1,1) between two finished even
+// rows, so a warp advances two rows per iteration.  Within a row the even
+// node of a pair is updated first (it reads the odd node of the lane to the
+// left), then the odd node (it reads the new even node of the lane to the
+// right).  Down: the sweep starts from z = 0 (down_gs_iterations,
+// tgmg.hh:273-279), so only b is read; the swept z goes to the level's r
+// array and the restricted residual to the child's b.  Up: z is taken from
+// r, the child's correction added, and the sweep written back to z.  The
+// outer four columns and the last two of a strip are halo, as are the rows
+// before y0 and after the owned block.
+
+constexpr int kLevDownCols = 27;  // coarse columns per strip (down): lanes 3..29
+constexpr int kLevUpCols = 29;    // coarse columns per strip (up): lanes 2..30
+
+__device__ __forceinline__ float4 st_e(const stencil9<float> *s, int e) {
+    return __ldg(reinterpret_cast<const float4 *>(s->e + e));
+}
+
+__device__ __forceinline__ void madd4(float2 &acc, const float4 &A, float zx, float zy) {
+    acc.x += A.x * zx + A.y * zy;
+    acc.y += A.z * zx + A.w * zy;
+}
+
+// Off-diagonal products at the even node of the pair (tgmg_level::mul_a,
+// tgmg.in.cc:536-547, in the order of lev_offdiag).
+__device__ __forceinline__ float2 offdiag_even(const stencil9<float> *s, const float4 &d, const float4 &c,
+                                               const float4 &u, bool has_d, bool has_u) {
+    constexpr unsigned F = 0xffffffffu;
+    const float dlx = __shfl_up_sync(F, d.z, 1), dly = __shfl_up_sync(F, d.w, 1);
+    const float clx = __shfl_up_sync(F, c.z, 1), cly = __shfl_up_sync(F, c.w, 1);
+    const float ulx = __shfl_up_sync(F, u.z, 1), uly = __shfl_up_sync(F, u.w, 1);
+    float2 a = make_float2(0.f, 0.f);
+    if (has_d) {
+        madd4(a, st_e(s, 0), dlx, dly);
+        madd4(a, st_e(s, 1), d.x, d.y);
+        madd4(a, st_e(s, 2), d.z, d.w);
+    }
+    madd4(a, st_e(s, 3), clx, cly);
+    madd4(a, st_e(s, 5), c.z, c.w);
+    if (has_u) {
+        madd4(a, st_e(s, 6), ulx, uly);
+        madd4(a, st_e(s, 7), u.x, u.y);
+        madd4(a, st_e(s, 8), u.z, u.w);
+    }
+    return a;
+}
+
+// The same at the odd node of the pair.
+__device__ __forceinline__ float2 offdiag_odd(const stencil9<float> *s, const float4 &d, const float4 &c,
+                                              const float4 &u, bool has_d, bool has_u) {
+    constexpr unsigned F = 0xffffffffu;
+    const float drx = __shfl_down_sync(F, d.x, 1), dry = __shfl_down_sync(F, d.y, 1);
+    const float crx = __shfl_down_sync(F, c.x, 1), cry = __shfl_down_sync(F, c.y, 1);
+    const float urx = __shfl_down_sync(F, u.x, 1), ury = __shfl_down_sync(F, u.y, 1);
+    float2 a = make_float2(0.f, 0.f);
+    if (has_d) {
+        madd4(a, st_e(s, 0), d.x, d.y);
+        madd4(a, st_e(s, 1), d.z, d.w);
+        madd4(a, st_e(s, 2), drx, dry);
+    }
+    madd4(a, st_e(s, 3), c.x, c.y);
+    madd4(a, st_e(s, 5), crx, cry);
+    if (has_u) {
+        madd4(a, st_e(s, 6), u.x, u.y);
+        madd4(a, st_e(s, 7), u.z, u.w);
+        madd4(a, st_e(s, 8), urx, ury);
+    }
+    return a;
+}
+
+// Both colours of row j that touch the pair: even node, then odd node.
+__device__ __forceinline__ void lev_row_sweep(const level_view<float> &L, int j, const float4 &d, float4 &c,
+                                              const float4 &u, const float4 &bb) {
+    const stencil9<float> *s = L.st + __ldg(L.cls + j);
+    const bool hd = j > 0, hu = j < L.n - 1;
+    const float4 iv = st_e(s, 9);
+    float2 a = offdiag_even(s, d, c, u, hd, hu);
+    float rx = bb.x - a.x, ry = bb.y - a.y;
+    c.x = iv.x * rx + iv.y * ry;
+    c.y = iv.z * rx + iv.w * ry;
+    a = offdiag_odd(s, d, c, u, hd, hu);
+    rx = bb.z - a.x;
+    ry = bb.w - a.y;
+    c.z = iv.x * rx + iv.y * ry;
+    c.w = iv.z * rx + iv.w * ry;
+}
+
+// Residual b - A z of the pair on row j (even node .x .y, odd node .z .w).
+__device__ __forceinline__ float4 lev_pair_residual(const level_view<float> &L, int j, const float4 &d,
+                                                    const float4 &c, const float4 &u, const float4 &bb) {
+    const stencil9<float> *s = L.st + __ldg(L.cls + j);
+    const bool hd = j > 0, hu = j < L.n - 1;
+    const float4 cc = st_e(s, 4);
+    float2 a = offdiag_even(s, d, c, u, hd, hu);
+    madd4(a, cc, c.x, c.y);
+    float2 e = offdiag_odd(s, d, c, u, hd, hu);
+    madd4(e, cc, c.z, c.w);
+    return make_float4(bb.x - a.x, bb.y - a.y, bb.z - e.x, bb.w - e.y);
+}
+
+// Full weighting of the residual rows 2J-1, 2J, 2J+1 at the coarse point
+// under the lane's even node (restrict_at).
+__device__ __forceinline__ float2 lev_restrict(const float4 &r0, const float4 &r1, const float4 &r2, int J, int n) {
+    constexpr unsigned F = 0xffffffffu;
+    const float4 rr[3] = {r0, r1, r2};
+    float ax = 0, ay = 0;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float lx = __shfl_up_sync(F, rr[q].z, 1), ly = __shfl_up_sync(F, rr[q].w, 1);
+        const int fy = 2 * J + q - 1;
+        if (fy < 0 || fy >= n) continue;
+        const int hy = halves_of(fy, n, 0, J);
+        if (!hy) continue;
+        const float w1 = (float)hy * 0.25f, w2 = (float)(2 * hy) * 0.25f;
+        ax += w1 * lx;
+        ay += w1 * ly;
+        ax += w2 * rr[q].x;
+        ay += w2 * rr[q].y;
+        ax += w1 * rr[q].z;
+        ay += w1 * rr[q].w;
+    }
+    return make_float2(ax, ay);
+}
+
+// Adds the child's correction to row j of the pair (apply_t / t_line,
+// tgmg.in.cc:552-621): the even node takes coarse c0, the odd node the mean
+// of c0 and c1; rows through p1d_halves.
+__device__ __forceinline__ void march_prolong(float4 &z, const float2 *__restrict__ zc, int cm, int c0, int c1, int j,
+                                              int n) {
+    if (j < 0 || j >= n) return;
+    int cy[2], hy[2];
+    const int ny = p1d_halves(j, n, 0, cy, hy);
+    float ax = 0, ay = 0, bx = 0, by = 0;
+    for (int q = 0; q < ny; q++) {
+        const float wy = (float)hy[q] * 0.25f;
+        const float2 v0 = __ldg(zc + (size_t)cy[q] * cm + c0), v1 = __ldg(zc + (size_t)cy[q] * cm + c1);
+        ax += 2.f * wy * v0.x;
+        ay += 2.f * wy * v0.y;
+        bx += wy * (v0.x + v1.x);
+        by += wy * (v0.y + v1.y);
+    }
+    z.x += ax;
+    z.y += ay;
+    z.z += bx;
+    z.w += by;
+}
+
+template <int TCH>
+__global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<float> L, level_view<float> C) {
+    const int lane = threadIdx.x & 31;
+    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
+    if (J0 >= C.n) return;
+    const int m = L.m, n = L.n;
+    const int I0 = blockIdx.x * kLevDownCols;
+    const int xs = 2 * I0 - 6, y0 = 2 * J0;
+    const int gx = wrapx(xs + 2 * lane, m);
+    const int I = I0 + lane - 3;
+    const bool own = lane >= 3 && lane < 3 + kLevDownCols && I < C.m;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 W0 = zero, W1 = zero, W2 = zero, W3 = zero, W4 = zero;  // z rows k-4 .. k
+    float4 B0 = zero, B1 = zero, B2 = zero, B3 = zero;             // b rows k-3 .. k
+    float4 Rp = zero;                                              // residual row k-4
+    const int kb = y0 - 4, ke = y0 + 2 * TCH + 1;
+    float4 nb0 = march_load(L.b, kb, m, n, gx), nb1 = march_load(L.b, kb + 1, m, n, gx);
+    for (int k = kb + 1; k <= ke; k += 2) {
+        W0 = W2; W1 = W3; W2 = W4; W3 = zero; W4 = zero;
+        B0 = B2; B1 = B3; B2 = nb0; B3 = nb1;
+        if (k + 2 <= ke) {
+            nb0 = march_load(L.b, k + 1, m, n, gx);
+            nb1 = march_load(L.b, k + 2, m, n, gx);
+        }
+        const int je = k - 1, jo = k - 2;
+        if (je >= 0 && je < n) lev_row_sweep(L, je, W2, W3, W4, B2);
+        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(L, jo, W1, W2, W3, B1);
+        if (own) {
+            if (je >= y0 && je < y0 + 2 * TCH && je < n) *reinterpret_cast<float4 *>(L.r + (size_t)je * m + gx) = W3;
+            if (jo >= y0 && jo < y0 + 2 * TCH && jo < n) *reinterpret_cast<float4 *>(L.r + (size_t)jo * m + gx) = W2;
+        }
+        const int j3 = k - 3, j2 = k - 2;
+        float4 R3 = zero, R2 = zero;
+        if (j3 >= y0 - 1 && j3 >= 0 && j3 < n) R3 = lev_pair_residual(L, j3, W0, W1, W2, B0);
+        if (j2 >= y0 - 1 && j2 >= 0 && j2 < n) R2 = lev_pair_residual(L, j2, W1, W2, W3, B1);
+        const int J = j3 >> 1;  // rows 2J-1, 2J, 2J+1 = k-4, k-3, k-2
+        if (j3 >= y0) {
+            const float2 w = lev_restrict(Rp, R3, R2, J, n);
+            if (own && J < C.n) C.b[(size_t)J * C.m + I] = w;
+        }
+        Rp = R2;
+    }
+}
+
+template <int TCH>
+__global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float> L, level_view<float> C) {
+    const int lane = threadIdx.x & 31;
+    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
+    if (J0 >= C.n) return;
+    const int m = L.m, n = L.n;
+    const int I0 = blockIdx.x * kLevUpCols;
+    const int xs = 2 * I0 - 4, y0 = 2 * J0;
+    const int gx = wrapx(xs + 2 * lane, m);
+    const int c0 = gx >> 1, c1 = c0 + 1 == C.m ? 0 : c0 + 1;
+    const bool own = lane >= 2 && lane < 2 + kLevUpCols && xs + 2 * lane < m;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 W0 = zero, W1 = zero, W2 = zero, W3 = zero;  // z rows k-3 .. k
+    float4 B0 = zero, B1 = zero, B2 = zero;             // b rows k-2 .. k
+    const int kb = y0 - 2, ke = y0 + 2 * TCH + 1;
+    float4 nz0 = march_load(L.r, kb, m, n, gx), nz1 = march_load(L.r, kb + 1, m, n, gx);
+    float4 nb0 = march_load(L.b, kb, m, n, gx), nb1 = march_load(L.b, kb + 1, m, n, gx);
+    for (int k = kb + 1; k <= ke; k += 2) {
+        float4 z0 = nz0, z1 = nz1;
+        B0 = B2; B1 = nb0; B2 = nb1;
+        if (k + 2 <= ke) {
+            nz0 = march_load(L.r, k + 1, m, n, gx);
+            nz1 = march_load(L.r, k + 2, m, n, gx);
+            nb0 = march_load(L.b, k + 1, m, n, gx);
+            nb1 = march_load(L.b, k + 2, m, n, gx);
+        }
+        march_prolong(z0, C.z, C.m, c0, c1, k - 1, n);
+        march_prolong(z1, C.z, C.m, c0, c1, k, n);
+        W0 = W2; W1 = W3; W2 = z0; W3 = z1;
+        const int je = k - 1, jo = k - 2;
+        if (je >= 0 && je < n) lev_row_sweep(L, je, W1, W2, W3, B1);
+        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(L, jo, W0, W1, W2, B0);
+        if (own) {
+            if (je >= y0 && je < y0 + 2 * TCH && je < n) *reinterpret_cast<float4 *>(L.z + (size_t)je * m + gx) = W2;
+            if (jo >= y0 && jo < y0 + 2 * TCH && jo < n) *reinterpret_cast<float4 *>(L.z + (size_t)jo * m + gx) = W1;
+        }
     }
 }
 
@@ -1647,6 +1919,52 @@ template <typename T> static bool tile_level(const hierarchy<T> &h, const level_
     return h.fuse && sizeof(T) == 4 && L.colors_x == 2 && L.m >= kFusedMinWidth;
 }
 
+// Levels for the streaming coarse kernels: tile levels with one stencil
+// class per row.
+template <typename T> static bool march_level(const hierarchy<T> &h, const level_view<T> &L) {
+    return tile_level(h, L) && L.homog;
+}
+
+// Coarse rows per warp of a streaming coarse kernel: the largest of 16, 8
+// and 4 that still gives eight warps per SM, else 2 (small levels are
+// latency-bound: shorter marches finish sooner).
+inline int march_rows(int strips, int cn) {
+    const long want = 8L * 152;
+    for (int t = 16; t >= 4; t >>= 1)
+        if ((long)strips * ceil_div(cn, t) >= want) return t;
+    return 2;
+}
+
+template <typename T> void launch_lev_down_m(level_view<T> &L, level_view<T> &C, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4) {
+        const int strips = ceil_div(C.m, kLevDownCols);
+        const int t = march_rows(strips, C.n);
+        const dim3 g(strips, ceil_div(ceil_div(C.n, t), kMarchWarps)), blk(32 * kMarchWarps);
+        switch (t) {
+            case 16: k_lev_down_m<16><<<g, blk, 0, st>>>(L, C); break;
+            case 8: k_lev_down_m<8><<<g, blk, 0, st>>>(L, C); break;
+            case 4: k_lev_down_m<4><<<g, blk, 0, st>>>(L, C); break;
+            default: k_lev_down_m<2><<<g, blk, 0, st>>>(L, C);
+        }
+        note_launch();
+    }
+}
+
+template <typename T> void launch_lev_up_m(level_view<T> &F, level_view<T> &C, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4) {
+        const int strips = ceil_div(C.m, kLevUpCols);
+        const int t = march_rows(strips, C.n);
+        const dim3 g(strips, ceil_div(ceil_div(C.n, t), kMarchWarps)), blk(32 * kMarchWarps);
+        switch (t) {
+            case 16: k_lev_up_m<16><<<g, blk, 0, st>>>(F, C); break;
+            case 8: k_lev_up_m<8><<<g, blk, 0, st>>>(F, C); break;
+            case 4: k_lev_up_m<4><<<g, blk, 0, st>>>(F, C); break;
+            default: k_lev_up_m<2><<<g, blk, 0, st>>>(F, C);
+        }
+        note_launch();
+    }
+}
+
 // Coarse tile of a tile-kernel level: the largest of 32x8, 16x4 and 8x4
 // coarse points that still gives two blocks per SM; the coarse levels are
 // latency-bound, and a smaller tile shortens every phase of a block.
@@ -1675,12 +1993,32 @@ template <typename T> void launch_lev_up(level_view<T> &F, level_view<T> &C, cud
     note_launch();
 }
 
+// The streaming top-level kernels (single precision only): the swept z goes
+// to the level's r array on the way down and back to z on the way up.
+template <typename T> void launch_top_down(hierarchy<T> &h, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4) {
+        level_view<T> &T0 = h.lv[0], &C = h.lv[1];
+        dim3 g(ceil_div(C.m, kDownCols), ceil_div(ceil_div(C.n, kMarchRows), kMarchWarps));
+        k_top_down<<<g, 32 * kMarchWarps, 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, T0.r, C.b, C.m, C.n);
+        note_launch();
+    }
+}
+
+template <typename T> void launch_top_up(hierarchy<T> &h, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4) {
+        level_view<T> &T0 = h.lv[0], &C = h.lv[1];
+        dim3 g(ceil_div(C.m, kUpCols), ceil_div(ceil_div(C.n, kMarchRows), kMarchWarps));
+        k_top_up<<<g, 32 * kMarchWarps, 0, st>>>(h.op, T0.r, T0.b, T0.m, T0.n, C.z, C.m, C.n, T0.z);
+        note_launch();
+    }
+}
+
 template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64) {
     typedef typename vec2_t<T>::type V;
     dim3 blk(32, 8);
     const int ml = h.nl - 1;
     level_view<T> &T0 = h.lv[0];
-    const bool fused = h.fuse && sizeof(T) == 4 && ml > 0 && T0.m >= kFusedMinWidth;
+    const bool fused = h.fuse && sizeof(T) == 4 && ml > 0 && T0.colors_x == 2 && T0.m >= kFusedMinWidth;
     if (ml == 0) {
         top_sweep(h, st);
         top_sweep(h, st);
@@ -1688,9 +2026,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     }
     const int t = tail_start(h);
     if (fused) {
-        dim3 g(ceil_div(h.lv[1].m, TCX), ceil_div(h.lv[1].n, TCY));
-        k_top_down<T><<<g, dim3(32, 8), 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].b, h.lv[1].m, h.lv[1].n);
-        note_launch();
+        launch_top_down(h, st);
     } else {
         top_sweep(h, st);
         k_top_residual<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.op, T0.z, T0.b, T0.r, T0.m, T0.n);
@@ -1703,6 +2039,10 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     for (int i = 1; i < down_end; i++) {
         level_view<T> &L = h.lv[i];
         level_view<T> &C = h.lv[i + 1];
+        if (march_level(h, L)) {
+            launch_lev_down_m(L, C, st);
+            continue;
+        }
         if (tile_level(h, L)) {
             launch_lev_down(L, C, st);
             continue;
@@ -1737,6 +2077,10 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     }
     for (int i = up_from; i >= 2; i--) {
         level_view<T> &C = h.lv[i], &F = h.lv[i - 1];
+        if (march_level(h, F)) {
+            launch_lev_up_m(F, C, st);
+            continue;
+        }
         if (tile_level(h, F)) {
             launch_lev_up(F, C, st);
             continue;
@@ -1746,9 +2090,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         lev_sweep(F, st);
     }
     if (fused) {
-        dim3 g(ceil_div(h.lv[1].m, TCX), ceil_div(h.lv[1].n, TCY));
-        k_top_up<T><<<g, dim3(32, 8), 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, h.lv[1].z, h.lv[1].m, h.lv[1].n);
-        note_launch();
+        launch_top_up(h, st);
     } else {
         k_prolong_add<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.lv[1].z, h.lv[1].m, h.lv[1].n, T0.z, T0.m,
                                                                  T0.n);
