@@ -1062,6 +1062,48 @@ __device__ __forceinline__ float2 march_restrict(const float2 &r0, const float2 
     return make_float2(ax, ay);
 }
 
+// Coarse z of a strip staged by one warp: columns cx0 + 0..32 (wrapped) of
+// rows Jlo .. Jlo + R - 1, zero outside the level.  Lane L's pair prolongs
+// from columns L (even node) and L, L + 1 (odd node).
+template <int R>
+__device__ __forceinline__ void stage_coarse(float2 (*cz)[33], const float2 *__restrict__ zc, int cm, int cn, int cx0,
+                                             int Jlo, int lane) {
+    for (int k = lane; k < R * 33; k += 32) {
+        const int r = k / 33, c = k - r * 33, J = Jlo + r;
+        float2 v = make_float2(0.f, 0.f);
+        if (J >= 0 && J < cn) v = __ldg(zc + (size_t)J * cm + wrapx(cx0 + c, cm));
+        cz[r][c] = v;
+    }
+    __syncwarp();
+}
+
+// Adds the child's correction to row j of the pair (apply_t / t_line,
+// tgmg.in.cc:552-621): the even node takes coarse c0, the odd node the mean
+// of c0 and c1 (wrapping on the even periodic line); rows through p1d_halves.
+__device__ __forceinline__ void prolong_staged(float4 &z, const float2 (*cz)[33], int Jlo, int lane, int j, int n) {
+    if (j < 0 || j >= n) return;
+    int cy[2], hy[2];
+    const int ny = p1d_halves(j, n, 0, cy, hy);
+    float ax = 0, ay = 0, bx = 0, by = 0;
+    for (int q = 0; q < ny; q++) {
+        const float wy = (float)hy[q] * 0.25f;
+        const float2 v0 = cz[cy[q] - Jlo][lane], v1 = cz[cy[q] - Jlo][lane + 1];
+        ax += 2.f * wy * v0.x;
+        ay += 2.f * wy * v0.y;
+        bx += wy * (v0.x + v1.x);
+        by += wy * (v0.y + v1.y);
+    }
+    z.x += ax;
+    z.y += ay;
+    z.z += bx;
+    z.w += by;
+}
+
+__device__ __forceinline__ void madd4(float2 &acc, const float4 &A, float zx, float zy) {
+    acc.x += A.x * zx + A.y * zy;
+    acc.y += A.z * zx + A.w * zy;
+}
+
 // Pre-smooth + residual + restriction of the top level (apply_r after one
 // gauss_seidel, tgmg.in.cc:313-320): z_out = one sweep of z_in, bc = R(b - A z_out).
 __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op, const float2 *__restrict__ zin,
@@ -1126,13 +1168,13 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
                                                              const float2 *__restrict__ b, int m, int n,
                                                              const float2 *__restrict__ zc, int cm, int cn,
                                                              float2 *__restrict__ zout) {
-    const int lane = threadIdx.x & 31;
-    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kMarchRows;
+    __shared__ float2 czs[kMarchWarps][kMarchRows + 3][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int J0 = (blockIdx.y * kMarchWarps + w) * kMarchRows;
     if (J0 >= cn) return;
     const int I0 = blockIdx.x * kUpCols;
     const int xs = 2 * I0 - 2, y0 = 2 * J0;
     const int gx = wrapx(xs + 2 * lane, m);
-    const int c0 = gx >> 1, c1 = c0 + 1 == cm ? 0 : c0 + 1;  // coarse columns of the pair
     const bool own = lane >= 1 && lane < 1 + kUpCols && xs + 2 * lane < m;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 Z0 = zero, Z1 = zero, Z2 = zero, Z3 = zero;  // rows k-3 .. k
@@ -1143,6 +1185,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
     pb[0] = march_load(b, kb, m, n, gx);
     pz[1] = march_load(zin, kb + 1, m, n, gx);
     pb[1] = march_load(b, kb + 1, m, n, gx);
+    stage_coarse<kMarchRows + 3>(czs[w], zc, cm, cn, xs / 2, J0 - 1, lane);
     for (int k0 = kb; k0 <= ke; k0 += 2) {
 #pragma unroll
         for (int h = 0; h < 2; h++) {
@@ -1154,23 +1197,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
                 pz[h] = march_load(zin, k + 2, m, n, gx);
                 pb[h] = march_load(b, k + 2, m, n, gx);
             }
-            if (k >= 0 && k < n) {
-                int cy[2], hy[2];
-                const int ny = p1d_halves(k, n, 0, cy, hy);
-                float ax = 0, ay = 0, bx = 0, by = 0;
-                for (int q = 0; q < ny; q++) {
-                    const float wy = (float)hy[q] * 0.25f;
-                    const float2 v0 = __ldg(zc + (size_t)cy[q] * cm + c0), v1 = __ldg(zc + (size_t)cy[q] * cm + c1);
-                    ax += 2.f * wy * v0.x;
-                    ay += 2.f * wy * v0.y;
-                    bx += wy * (v0.x + v1.x);
-                    by += wy * (v0.y + v1.y);
-                }
-                zn.x += ax;
-                zn.y += ay;
-                zn.z += bx;
-                zn.w += by;
-            }
+            prolong_staged(zn, czs[w], J0 - 1, lane, k, n);
             Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = zn;
             const int j0 = k - 1, j1 = k - 2;
             if (j0 >= y0 - 1 && j0 >= 0 && j0 < n) march_color(op, Z1, Z2, Z3, B1, j0, n, 0);
@@ -1447,14 +1474,23 @@ __global__ void __launch_bounds__(kFusedThreads) k_lev_up(level_view<T> L, level
 
 constexpr int kLevDownCols = 27;  // coarse columns per strip (down): lanes 3..29
 constexpr int kLevUpCols = 29;    // coarse columns per strip (up): lanes 2..30
+constexpr int kMarchStencils = 16; // stencil classes a streaming level may have (staged in shared memory)
 
 __device__ __forceinline__ float4 st_e(const stencil9<float> *s, int e) {
-    return __ldg(reinterpret_cast<const float4 *>(s->e + e));
+    return *reinterpret_cast<const float4 *>(s->e + e);
 }
 
-__device__ __forceinline__ void madd4(float2 &acc, const float4 &A, float zx, float zy) {
-    acc.x += A.x * zx + A.y * zy;
-    acc.y += A.z * zx + A.w * zy;
+// The level's stencil table, copied to shared memory by the whole block.
+__device__ __forceinline__ void stage_stencils(stencil9<float> *tab, const level_view<float> &L) {
+    const float4 *src = reinterpret_cast<const float4 *>(L.st);
+    float4 *dst = reinterpret_cast<float4 *>(tab);
+    for (int k = threadIdx.x; k < L.nst * 10; k += blockDim.x) dst[k] = __ldg(src + k);
+    __syncthreads();
+}
+
+// Stencil class of row j (0 outside the level; such rows are never swept).
+__device__ __forceinline__ int row_class(const level_view<float> &L, int j) {
+    return j >= 0 && j < L.n ? __ldg(L.cls + j) : 0;
 }
 
 // Off-diagonal products at the even node of the pair (tgmg_level::mul_a,
@@ -1504,11 +1540,10 @@ __device__ __forceinline__ float2 offdiag_odd(const stencil9<float> *s, const fl
     return a;
 }
 
-// Both colours of row j that touch the pair: even node, then odd node.
-__device__ __forceinline__ void lev_row_sweep(const level_view<float> &L, int j, const float4 &d, float4 &c,
+// Both colours of row j (stencil s) that touch the pair: even node, then odd node.
+__device__ __forceinline__ void lev_row_sweep(const stencil9<float> *s, int j, int n, const float4 &d, float4 &c,
                                               const float4 &u, const float4 &bb) {
-    const stencil9<float> *s = L.st + __ldg(L.cls + j);
-    const bool hd = j > 0, hu = j < L.n - 1;
+    const bool hd = j > 0, hu = j < n - 1;
     const float4 iv = st_e(s, 9);
     float2 a = offdiag_even(s, d, c, u, hd, hu);
     float rx = bb.x - a.x, ry = bb.y - a.y;
@@ -1522,10 +1557,9 @@ __device__ __forceinline__ void lev_row_sweep(const level_view<float> &L, int j,
 }
 
 // Residual b - A z of the pair on row j (even node .x .y, odd node .z .w).
-__device__ __forceinline__ float4 lev_pair_residual(const level_view<float> &L, int j, const float4 &d,
+__device__ __forceinline__ float4 lev_pair_residual(const stencil9<float> *s, int j, int n, const float4 &d,
                                                     const float4 &c, const float4 &u, const float4 &bb) {
-    const stencil9<float> *s = L.st + __ldg(L.cls + j);
-    const bool hd = j > 0, hu = j < L.n - 1;
+    const bool hd = j > 0, hu = j < n - 1;
     const float4 cc = st_e(s, 4);
     float2 a = offdiag_even(s, d, c, u, hd, hu);
     madd4(a, cc, c.x, c.y);
@@ -1558,31 +1592,10 @@ __device__ __forceinline__ float2 lev_restrict(const float4 &r0, const float4 &r
     return make_float2(ax, ay);
 }
 
-// Adds the child's correction to row j of the pair (apply_t / t_line,
-// tgmg.in.cc:552-621): the even node takes coarse c0, the odd node the mean
-// of c0 and c1; rows through p1d_halves.
-__device__ __forceinline__ void march_prolong(float4 &z, const float2 *__restrict__ zc, int cm, int c0, int c1, int j,
-                                              int n) {
-    if (j < 0 || j >= n) return;
-    int cy[2], hy[2];
-    const int ny = p1d_halves(j, n, 0, cy, hy);
-    float ax = 0, ay = 0, bx = 0, by = 0;
-    for (int q = 0; q < ny; q++) {
-        const float wy = (float)hy[q] * 0.25f;
-        const float2 v0 = __ldg(zc + (size_t)cy[q] * cm + c0), v1 = __ldg(zc + (size_t)cy[q] * cm + c1);
-        ax += 2.f * wy * v0.x;
-        ay += 2.f * wy * v0.y;
-        bx += wy * (v0.x + v1.x);
-        by += wy * (v0.y + v1.y);
-    }
-    z.x += ax;
-    z.y += ay;
-    z.z += bx;
-    z.w += by;
-}
-
 template <int TCH>
 __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<float> L, level_view<float> C) {
+    __shared__ stencil9<float> tab[kMarchStencils];
+    stage_stencils(tab, L);
     const int lane = threadIdx.x & 31;
     const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
     if (J0 >= C.n) return;
@@ -1595,27 +1608,32 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<floa
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 W0 = zero, W1 = zero, W2 = zero, W3 = zero, W4 = zero;  // z rows k-4 .. k
     float4 B0 = zero, B1 = zero, B2 = zero, B3 = zero;             // b rows k-3 .. k
+    int S0 = 0, S1 = 0, S2 = 0, S3 = 0;                            // stencil classes of rows k-3 .. k
     float4 Rp = zero;                                              // residual row k-4
     const int kb = y0 - 4, ke = y0 + 2 * TCH + 1;
     float4 nb0 = march_load(L.b, kb, m, n, gx), nb1 = march_load(L.b, kb + 1, m, n, gx);
+    int ns0 = row_class(L, kb), ns1 = row_class(L, kb + 1);
     for (int k = kb + 1; k <= ke; k += 2) {
         W0 = W2; W1 = W3; W2 = W4; W3 = zero; W4 = zero;
         B0 = B2; B1 = B3; B2 = nb0; B3 = nb1;
+        S0 = S2; S1 = S3; S2 = ns0; S3 = ns1;
         if (k + 2 <= ke) {
             nb0 = march_load(L.b, k + 1, m, n, gx);
             nb1 = march_load(L.b, k + 2, m, n, gx);
+            ns0 = row_class(L, k + 1);
+            ns1 = row_class(L, k + 2);
         }
         const int je = k - 1, jo = k - 2;
-        if (je >= 0 && je < n) lev_row_sweep(L, je, W2, W3, W4, B2);
-        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(L, jo, W1, W2, W3, B1);
+        if (je >= 0 && je < n) lev_row_sweep(tab + S2, je, n, W2, W3, W4, B2);
+        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(tab + S1, jo, n, W1, W2, W3, B1);
         if (own) {
             if (je >= y0 && je < y0 + 2 * TCH && je < n) *reinterpret_cast<float4 *>(L.r + (size_t)je * m + gx) = W3;
             if (jo >= y0 && jo < y0 + 2 * TCH && jo < n) *reinterpret_cast<float4 *>(L.r + (size_t)jo * m + gx) = W2;
         }
         const int j3 = k - 3, j2 = k - 2;
         float4 R3 = zero, R2 = zero;
-        if (j3 >= y0 - 1 && j3 >= 0 && j3 < n) R3 = lev_pair_residual(L, j3, W0, W1, W2, B0);
-        if (j2 >= y0 - 1 && j2 >= 0 && j2 < n) R2 = lev_pair_residual(L, j2, W1, W2, W3, B1);
+        if (j3 >= y0 - 1 && j3 >= 0 && j3 < n) R3 = lev_pair_residual(tab + S0, j3, n, W0, W1, W2, B0);
+        if (j2 >= y0 - 1 && j2 >= 0 && j2 < n) R2 = lev_pair_residual(tab + S1, j2, n, W1, W2, W3, B1);
         const int J = j3 >> 1;  // rows 2J-1, 2J, 2J+1 = k-4, k-3, k-2
         if (j3 >= y0) {
             const float2 w = lev_restrict(Rp, R3, R2, J, n);
@@ -1627,36 +1645,44 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<floa
 
 template <int TCH>
 __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float> L, level_view<float> C) {
-    const int lane = threadIdx.x & 31;
-    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
+    __shared__ stencil9<float> tab[kMarchStencils];
+    __shared__ float2 czs[kMarchWarps][TCH + 3][33];
+    stage_stencils(tab, L);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int J0 = (blockIdx.y * kMarchWarps + w) * TCH;
     if (J0 >= C.n) return;
     const int m = L.m, n = L.n;
     const int I0 = blockIdx.x * kLevUpCols;
     const int xs = 2 * I0 - 4, y0 = 2 * J0;
     const int gx = wrapx(xs + 2 * lane, m);
-    const int c0 = gx >> 1, c1 = c0 + 1 == C.m ? 0 : c0 + 1;
     const bool own = lane >= 2 && lane < 2 + kLevUpCols && xs + 2 * lane < m;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 W0 = zero, W1 = zero, W2 = zero, W3 = zero;  // z rows k-3 .. k
     float4 B0 = zero, B1 = zero, B2 = zero;             // b rows k-2 .. k
+    int S0 = 0, S1 = 0, S2 = 0;                         // stencil classes of rows k-2 .. k
     const int kb = y0 - 2, ke = y0 + 2 * TCH + 1;
     float4 nz0 = march_load(L.r, kb, m, n, gx), nz1 = march_load(L.r, kb + 1, m, n, gx);
     float4 nb0 = march_load(L.b, kb, m, n, gx), nb1 = march_load(L.b, kb + 1, m, n, gx);
+    int ns0 = row_class(L, kb), ns1 = row_class(L, kb + 1);
+    stage_coarse<TCH + 3>(czs[w], C.z, C.m, C.n, xs / 2, J0 - 1, lane);
     for (int k = kb + 1; k <= ke; k += 2) {
         float4 z0 = nz0, z1 = nz1;
         B0 = B2; B1 = nb0; B2 = nb1;
+        S0 = S2; S1 = ns0; S2 = ns1;
         if (k + 2 <= ke) {
             nz0 = march_load(L.r, k + 1, m, n, gx);
             nz1 = march_load(L.r, k + 2, m, n, gx);
             nb0 = march_load(L.b, k + 1, m, n, gx);
             nb1 = march_load(L.b, k + 2, m, n, gx);
+            ns0 = row_class(L, k + 1);
+            ns1 = row_class(L, k + 2);
         }
-        march_prolong(z0, C.z, C.m, c0, c1, k - 1, n);
-        march_prolong(z1, C.z, C.m, c0, c1, k, n);
+        prolong_staged(z0, czs[w], J0 - 1, lane, k - 1, n);
+        prolong_staged(z1, czs[w], J0 - 1, lane, k, n);
         W0 = W2; W1 = W3; W2 = z0; W3 = z1;
         const int je = k - 1, jo = k - 2;
-        if (je >= 0 && je < n) lev_row_sweep(L, je, W1, W2, W3, B1);
-        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(L, jo, W0, W1, W2, B0);
+        if (je >= 0 && je < n) lev_row_sweep(tab + S1, je, n, W1, W2, W3, B1);
+        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(tab + S0, jo, n, W0, W1, W2, B0);
         if (own) {
             if (je >= y0 && je < y0 + 2 * TCH && je < n) *reinterpret_cast<float4 *>(L.z + (size_t)je * m + gx) = W2;
             if (jo >= y0 && jo < y0 + 2 * TCH && jo < n) *reinterpret_cast<float4 *>(L.z + (size_t)jo * m + gx) = W1;
@@ -1809,12 +1835,15 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
             tsh[2 * k + 1] = (double)B.b[k].y;
         }
         __syncthreads();
+        // one warp per row of the inverse: coalesced reads, shuffle sum
         T *zz = (T *)B.z;
-        for (int r = tid; r < N; r += nth) {
+        const int lane = tid & 31, nw = nth >> 5;
+        for (int r = tid >> 5; r < N; r += nw) {
             const double *row = tl.inv + (size_t)r * N;
             double a = 0;
-            for (int k = 0; k < N; k++) a += row[k] * tsh[k];
-            zz[r] = (T)a;
+            for (int k = lane; k < N; k += 32) a += __ldg(row + k) * tsh[k];
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if (lane == 0) zz[r] = (T)a;
         }
         __syncthreads();
     }
@@ -1922,7 +1951,7 @@ template <typename T> static bool tile_level(const hierarchy<T> &h, const level_
 // Levels for the streaming coarse kernels: tile levels with one stencil
 // class per row.
 template <typename T> static bool march_level(const hierarchy<T> &h, const level_view<T> &L) {
-    return tile_level(h, L) && L.homog;
+    return tile_level(h, L) && L.homog && L.nst <= kMarchStencils;
 }
 
 // Coarse rows per warp of a streaming coarse kernel: the largest of 16, 8
