@@ -919,8 +919,8 @@ __global__ void k_ff_residual(ff_op op, const float2 *__restrict__ zh, const flo
 // window: lane L holds the node pair (xs + 2L, xs + 2L + 1) of each row as a
 // float4 (x and y of the even node, x and y of the odd node), neighbours in
 // x come from the adjacent lanes by shuffles and neighbours in y from the
-// window.  Each row step takes one new row of z and b (loaded two steps
-// ahead), sweeps colour 0 one row behind it and colour 1 two rows behind
+// window.  Each row step takes one new row of z and b (from a shared-memory
+// ring that cp.async fills several rows ahead), sweeps colour 0 one row behind it and colour 1 two rows behind
 // (down: and evaluates the residual three rows behind), so that a warp
 // reads every node of its strip once and writes it once.  The outer lanes
 // and rows are halo: a colour update is exact one node further in than the
@@ -1104,12 +1104,37 @@ __device__ __forceinline__ void madd4(float2 &acc, const float4 &A, float zx, fl
     acc.y += A.z * zx + A.w * zy;
 }
 
+// Per-warp ring of rows of z and b for the top-level kernels, filled by
+// cp.async kRing - 1 rows ahead of the row being consumed: row k of a march
+// sits in slot (k - kb) mod kRing.  A lane copies and later reads only its
+// own 16-byte pair, so its own cp.async.wait_group is the only
+// synchronisation; a slot is refilled one step after it was read.  Rows
+// outside the grid arrive as zeros (source size 0).
+constexpr int kRing = 6;
+
+__device__ __forceinline__ void cp_async16(float4 *dst, const float2 *src, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+
+__device__ __forceinline__ void ring_issue(float4 (*ring)[2][32], int slot, const float2 *__restrict__ z,
+                                           const float2 *__restrict__ b, int j, int m, int n, int gx, int lane) {
+    const bool v = j >= 0 && j < n;
+    const size_t o = v ? (size_t)j * m + gx : 0;
+    cp_async16(&ring[slot][0][lane], z + o, v);
+    cp_async16(&ring[slot][1][lane], b + o, v);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void ring_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(kRing - 2) : "memory"); }
+
 // Pre-smooth + residual + restriction of the top level (apply_r after one
 // gauss_seidel, tgmg.in.cc:313-320): z_out = one sweep of z_in, bc = R(b - A z_out).
 __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op, const float2 *__restrict__ zin,
                                                                const float2 *__restrict__ b, int m, int n,
                                                                float2 *__restrict__ zout, float2 *__restrict__ bc,
                                                                int cm, int cn) {
+    __shared__ __align__(16) float4 ring[kMarchWarps][kRing][2][32];
     const int lane = threadIdx.x & 31;
     const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kMarchRows;
     if (J0 >= cn) return;
@@ -1123,23 +1148,19 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op,
     float4 B0 = zero, B1 = zero, B2 = zero, B3 = zero;             // rows k-3 .. k
     float2 R0 = make_float2(0.f, 0.f), R1 = R0, R2 = R0;           // residual rows k-5 .. k-3
     const int kb = y0 - 4, ke = y0 + 2 * kMarchRows + 2;
-    // two prefetch slots, used on alternate steps (no move of a pending load)
-    float4 pz[2], pb[2];
-    pz[0] = march_load(zin, kb, m, n, gx);
-    pb[0] = march_load(b, kb, m, n, gx);
-    pz[1] = march_load(zin, kb + 1, m, n, gx);
-    pb[1] = march_load(b, kb + 1, m, n, gx);
-    for (int k0 = kb; k0 <= ke; k0 += 2) {
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int k = k0 + h;
-            if (k > ke) break;
-            Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = Z4; Z4 = pz[h];
-            B0 = B1; B1 = B2; B2 = B3; B3 = pb[h];
-            if (k + 2 <= ke) {
-                pz[h] = march_load(zin, k + 2, m, n, gx);
-                pb[h] = march_load(b, k + 2, m, n, gx);
-            }
+    float4(*rg)[2][32] = ring[threadIdx.x >> 5];
+    for (int d = 0; d < kRing - 1; d++) ring_issue(rg, d, zin, b, kb + d, m, n, gx, lane);
+    int slot = 0;
+    for (int k = kb; k <= ke; k++) {
+        {
+            ring_wait();
+            const float4 zn = rg[slot][0][lane], bn = rg[slot][1][lane];
+            const int prev = slot == 0 ? kRing - 1 : slot - 1;
+            const int jn = k + kRing - 1;
+            ring_issue(rg, prev, zin, b, jn <= ke ? jn : -1, m, n, gx, lane);
+            slot = slot == kRing - 1 ? 0 : slot + 1;
+            Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = Z4; Z4 = zn;
+            B0 = B1; B1 = B2; B2 = B3; B3 = bn;
             const int j0 = k - 1, j1 = k - 2, j2 = k - 3;
             if (j0 >= y0 - 3 && j0 >= 0 && j0 < n) march_color(op, Z2, Z3, Z4, B2, j0, n, 0);
             if (j1 >= y0 - 2 && j1 >= 0 && j1 < n) {
@@ -1168,6 +1189,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
                                                              const float2 *__restrict__ b, int m, int n,
                                                              const float2 *__restrict__ zc, int cm, int cn,
                                                              float2 *__restrict__ zout) {
+    __shared__ __align__(16) float4 ring[kMarchWarps][kRing][2][32];
     __shared__ float2 czs[kMarchWarps][kMarchRows + 3][33];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int J0 = (blockIdx.y * kMarchWarps + w) * kMarchRows;
@@ -1180,31 +1202,26 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
     float4 Z0 = zero, Z1 = zero, Z2 = zero, Z3 = zero;  // rows k-3 .. k
     float4 B0 = zero, B1 = zero, B2 = zero;            // rows k-2 .. k
     const int kb = y0 - 2, ke = y0 + 2 * kMarchRows + 1;
-    float4 pz[2], pb[2];
-    pz[0] = march_load(zin, kb, m, n, gx);
-    pb[0] = march_load(b, kb, m, n, gx);
-    pz[1] = march_load(zin, kb + 1, m, n, gx);
-    pb[1] = march_load(b, kb + 1, m, n, gx);
+    float4(*rg)[2][32] = ring[w];
+    for (int d = 0; d < kRing - 1; d++) ring_issue(rg, d, zin, b, kb + d, m, n, gx, lane);
     stage_coarse<kMarchRows + 3>(czs[w], zc, cm, cn, xs / 2, J0 - 1, lane);
-    for (int k0 = kb; k0 <= ke; k0 += 2) {
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int k = k0 + h;
-            if (k > ke) break;
-            float4 zn = pz[h];
-            B0 = B1; B1 = B2; B2 = pb[h];
-            if (k + 2 <= ke) {
-                pz[h] = march_load(zin, k + 2, m, n, gx);
-                pb[h] = march_load(b, k + 2, m, n, gx);
-            }
-            prolong_staged(zn, czs[w], J0 - 1, lane, k, n);
-            Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = zn;
-            const int j0 = k - 1, j1 = k - 2;
-            if (j0 >= y0 - 1 && j0 >= 0 && j0 < n) march_color(op, Z1, Z2, Z3, B1, j0, n, 0);
-            if (j1 >= y0 && j1 < n) {
-                march_color(op, Z0, Z1, Z2, B0, j1, n, 1);
-                if (own) *reinterpret_cast<float4 *>(zout + (size_t)j1 * m + xs + 2 * lane) = Z1;
-            }
+    int slot = 0;
+    for (int k = kb; k <= ke; k++) {
+        ring_wait();
+        float4 zn = rg[slot][0][lane];
+        const float4 bn = rg[slot][1][lane];
+        const int prev = slot == 0 ? kRing - 1 : slot - 1;
+        const int jn = k + kRing - 1;
+        ring_issue(rg, prev, zin, b, jn <= ke ? jn : -1, m, n, gx, lane);
+        slot = slot == kRing - 1 ? 0 : slot + 1;
+        B0 = B1; B1 = B2; B2 = bn;
+        prolong_staged(zn, czs[w], J0 - 1, lane, k, n);
+        Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = zn;
+        const int j0 = k - 1, j1 = k - 2;
+        if (j0 >= y0 - 1 && j0 >= 0 && j0 < n) march_color(op, Z1, Z2, Z3, B1, j0, n, 0);
+        if (j1 >= y0 && j1 < n) {
+            march_color(op, Z0, Z1, Z2, B0, j1, n, 1);
+            if (own) *reinterpret_cast<float4 *>(zout + (size_t)j1 * m + xs + 2 * lane) = Z1;
         }
     }
 }
@@ -1496,11 +1513,11 @@ __device__ __forceinline__ int row_class(const level_view<float> &L, int j) {
 // Off-diagonal products at the even node of the pair (tgmg_level::mul_a,
 // tgmg.in.cc:536-547, in the order of lev_offdiag).
 __device__ __forceinline__ float2 offdiag_even(const stencil9<float> *s, const float4 &d, const float4 &c,
-                                               const float4 &u, bool has_d, bool has_u) {
+                                               const float4 &u, bool has_d, bool has_u, int lsrc) {
     constexpr unsigned F = 0xffffffffu;
-    const float dlx = __shfl_up_sync(F, d.z, 1), dly = __shfl_up_sync(F, d.w, 1);
-    const float clx = __shfl_up_sync(F, c.z, 1), cly = __shfl_up_sync(F, c.w, 1);
-    const float ulx = __shfl_up_sync(F, u.z, 1), uly = __shfl_up_sync(F, u.w, 1);
+    const float dlx = __shfl_sync(F, d.z, lsrc), dly = __shfl_sync(F, d.w, lsrc);
+    const float clx = __shfl_sync(F, c.z, lsrc), cly = __shfl_sync(F, c.w, lsrc);
+    const float ulx = __shfl_sync(F, u.z, lsrc), uly = __shfl_sync(F, u.w, lsrc);
     float2 a = make_float2(0.f, 0.f);
     if (has_d) {
         madd4(a, st_e(s, 0), dlx, dly);
@@ -1519,11 +1536,11 @@ __device__ __forceinline__ float2 offdiag_even(const stencil9<float> *s, const f
 
 // The same at the odd node of the pair.
 __device__ __forceinline__ float2 offdiag_odd(const stencil9<float> *s, const float4 &d, const float4 &c,
-                                              const float4 &u, bool has_d, bool has_u) {
+                                              const float4 &u, bool has_d, bool has_u, int rsrc) {
     constexpr unsigned F = 0xffffffffu;
-    const float drx = __shfl_down_sync(F, d.x, 1), dry = __shfl_down_sync(F, d.y, 1);
-    const float crx = __shfl_down_sync(F, c.x, 1), cry = __shfl_down_sync(F, c.y, 1);
-    const float urx = __shfl_down_sync(F, u.x, 1), ury = __shfl_down_sync(F, u.y, 1);
+    const float drx = __shfl_sync(F, d.x, rsrc), dry = __shfl_sync(F, d.y, rsrc);
+    const float crx = __shfl_sync(F, c.x, rsrc), cry = __shfl_sync(F, c.y, rsrc);
+    const float urx = __shfl_sync(F, u.x, rsrc), ury = __shfl_sync(F, u.y, rsrc);
     float2 a = make_float2(0.f, 0.f);
     if (has_d) {
         madd4(a, st_e(s, 0), d.x, d.y);
@@ -1540,16 +1557,17 @@ __device__ __forceinline__ float2 offdiag_odd(const stencil9<float> *s, const fl
     return a;
 }
 
-// Both colours of row j (stencil s) that touch the pair: even node, then odd node.
+// Both colours of row j (stencil s) that touch the pair: even node, then odd
+// node; lsrc / rsrc: the lanes holding the pairs to the left and right.
 __device__ __forceinline__ void lev_row_sweep(const stencil9<float> *s, int j, int n, const float4 &d, float4 &c,
-                                              const float4 &u, const float4 &bb) {
+                                              const float4 &u, const float4 &bb, int lsrc, int rsrc) {
     const bool hd = j > 0, hu = j < n - 1;
     const float4 iv = st_e(s, 9);
-    float2 a = offdiag_even(s, d, c, u, hd, hu);
+    float2 a = offdiag_even(s, d, c, u, hd, hu, lsrc);
     float rx = bb.x - a.x, ry = bb.y - a.y;
     c.x = iv.x * rx + iv.y * ry;
     c.y = iv.z * rx + iv.w * ry;
-    a = offdiag_odd(s, d, c, u, hd, hu);
+    a = offdiag_odd(s, d, c, u, hd, hu, rsrc);
     rx = bb.z - a.x;
     ry = bb.w - a.y;
     c.z = iv.x * rx + iv.y * ry;
@@ -1558,25 +1576,27 @@ __device__ __forceinline__ void lev_row_sweep(const stencil9<float> *s, int j, i
 
 // Residual b - A z of the pair on row j (even node .x .y, odd node .z .w).
 __device__ __forceinline__ float4 lev_pair_residual(const stencil9<float> *s, int j, int n, const float4 &d,
-                                                    const float4 &c, const float4 &u, const float4 &bb) {
+                                                    const float4 &c, const float4 &u, const float4 &bb, int lsrc,
+                                                    int rsrc) {
     const bool hd = j > 0, hu = j < n - 1;
     const float4 cc = st_e(s, 4);
-    float2 a = offdiag_even(s, d, c, u, hd, hu);
+    float2 a = offdiag_even(s, d, c, u, hd, hu, lsrc);
     madd4(a, cc, c.x, c.y);
-    float2 e = offdiag_odd(s, d, c, u, hd, hu);
+    float2 e = offdiag_odd(s, d, c, u, hd, hu, rsrc);
     madd4(e, cc, c.z, c.w);
     return make_float4(bb.x - a.x, bb.y - a.y, bb.z - e.x, bb.w - e.y);
 }
 
 // Full weighting of the residual rows 2J-1, 2J, 2J+1 at the coarse point
 // under the lane's even node (restrict_at).
-__device__ __forceinline__ float2 lev_restrict(const float4 &r0, const float4 &r1, const float4 &r2, int J, int n) {
+__device__ __forceinline__ float2 lev_restrict(const float4 &r0, const float4 &r1, const float4 &r2, int J, int n,
+                                               int lsrc) {
     constexpr unsigned F = 0xffffffffu;
     const float4 rr[3] = {r0, r1, r2};
     float ax = 0, ay = 0;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-        const float lx = __shfl_up_sync(F, rr[q].z, 1), ly = __shfl_up_sync(F, rr[q].w, 1);
+        const float lx = __shfl_sync(F, rr[q].z, lsrc), ly = __shfl_sync(F, rr[q].w, lsrc);
         const int fy = 2 * J + q - 1;
         if (fy < 0 || fy >= n) continue;
         const int hy = halves_of(fy, n, 0, J);
@@ -1596,7 +1616,7 @@ template <int TCH>
 __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<float> L, level_view<float> C) {
     __shared__ stencil9<float> tab[kMarchStencils];
     stage_stencils(tab, L);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
     const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
     if (J0 >= C.n) return;
     const int m = L.m, n = L.n;
@@ -1624,19 +1644,19 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<floa
             ns1 = row_class(L, k + 2);
         }
         const int je = k - 1, jo = k - 2;
-        if (je >= 0 && je < n) lev_row_sweep(tab + S2, je, n, W2, W3, W4, B2);
-        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(tab + S1, jo, n, W1, W2, W3, B1);
+        if (je >= 0 && je < n) lev_row_sweep(tab + S2, je, n, W2, W3, W4, B2, lsrc, rsrc);
+        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(tab + S1, jo, n, W1, W2, W3, B1, lsrc, rsrc);
         if (own) {
             if (je >= y0 && je < y0 + 2 * TCH && je < n) *reinterpret_cast<float4 *>(L.r + (size_t)je * m + gx) = W3;
             if (jo >= y0 && jo < y0 + 2 * TCH && jo < n) *reinterpret_cast<float4 *>(L.r + (size_t)jo * m + gx) = W2;
         }
         const int j3 = k - 3, j2 = k - 2;
         float4 R3 = zero, R2 = zero;
-        if (j3 >= y0 - 1 && j3 >= 0 && j3 < n) R3 = lev_pair_residual(tab + S0, j3, n, W0, W1, W2, B0);
-        if (j2 >= y0 - 1 && j2 >= 0 && j2 < n) R2 = lev_pair_residual(tab + S1, j2, n, W1, W2, W3, B1);
+        if (j3 >= y0 - 1 && j3 >= 0 && j3 < n) R3 = lev_pair_residual(tab + S0, j3, n, W0, W1, W2, B0, lsrc, rsrc);
+        if (j2 >= y0 - 1 && j2 >= 0 && j2 < n) R2 = lev_pair_residual(tab + S1, j2, n, W1, W2, W3, B1, lsrc, rsrc);
         const int J = j3 >> 1;  // rows 2J-1, 2J, 2J+1 = k-4, k-3, k-2
         if (j3 >= y0) {
-            const float2 w = lev_restrict(Rp, R3, R2, J, n);
+            const float2 w = lev_restrict(Rp, R3, R2, J, n, lsrc);
             if (own && J < C.n) C.b[(size_t)J * C.m + I] = w;
         }
         Rp = R2;
@@ -1648,7 +1668,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float>
     __shared__ stencil9<float> tab[kMarchStencils];
     __shared__ float2 czs[kMarchWarps][TCH + 3][33];
     stage_stencils(tab, L);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
     const int J0 = (blockIdx.y * kMarchWarps + w) * TCH;
     if (J0 >= C.n) return;
     const int m = L.m, n = L.n;
@@ -1681,8 +1701,8 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float>
         prolong_staged(z1, czs[w], J0 - 1, lane, k, n);
         W0 = W2; W1 = W3; W2 = z0; W3 = z1;
         const int je = k - 1, jo = k - 2;
-        if (je >= 0 && je < n) lev_row_sweep(tab + S1, je, n, W1, W2, W3, B1);
-        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(tab + S0, jo, n, W0, W1, W2, B0);
+        if (je >= 0 && je < n) lev_row_sweep(tab + S1, je, n, W1, W2, W3, B1, lsrc, rsrc);
+        if (jo >= kb + 1 && jo >= 0 && jo < n) lev_row_sweep(tab + S0, jo, n, W0, W1, W2, B0, lsrc, rsrc);
         if (own) {
             if (je >= y0 && je < y0 + 2 * TCH && je < n) *reinterpret_cast<float4 *>(L.z + (size_t)je * m + gx) = W2;
             if (jo >= y0 && jo < y0 + 2 * TCH && jo < n) *reinterpret_cast<float4 *>(L.z + (size_t)jo * m + gx) = W1;
@@ -1736,13 +1756,14 @@ template <typename T> __host__ __device__ inline size_t tail_stage_bytes(int nst
     return sizeof(stencil9<T>) * (size_t)nst + sizeof(int) * (size_t)ncls;
 }
 
+// Prologue of the tail kernels: places every tail level (z, b, r) and the
+// small stencil tables in shared memory, copies the first level's b in and
+// clears its z (the down sweeps start from z = 0, gauss_seidel_from_zero;
+// coarser levels get their zero z with their b in the restriction).
 template <typename T>
-__global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T> H) {
+__device__ void tail_prologue(const tail_levels &tl, const hierarchy_view<T> &H, level_view<T> *S,
+                              unsigned char *tail_raw, int tid, int nth) {
     typedef typename vec2_t<T>::type V;
-    extern __shared__ __align__(32) unsigned char tail_raw[];
-    __shared__ level_view<T> S[17];  // the levels' views, read by every phase
-    double *tsh = (double *)tail_raw;
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
     if (tid == 0) {
         size_t off = (sizeof(double) * tl.inv_n + 15) & ~(size_t)15;
         for (int l = tl.t; l <= tl.ml; l++) {
@@ -1772,17 +1793,45 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
         int *cl = (int *)S[l].cls;
         for (int k = tid; k < S[l].ncls; k += nth) cl[k] = H.lv[l].cls[k];
     }
-    {
-        // the down sweeps start from z = 0 (gauss_seidel_from_zero); coarser
-        // levels get their zero z with their b in the restriction below
-        const int mn = S[tl.t].m * S[tl.t].n;
-        for (int k = tid; k < mn; k += nth) {
-            S[tl.t].b[k] = H.lv[tl.t].b[k];
-            S[tl.t].z[k].x = 0;
-            S[tl.t].z[k].y = 0;
-        }
+    const int mn = S[tl.t].m * S[tl.t].n;
+    for (int k = tid; k < mn; k += nth) {
+        S[tl.t].b[k] = H.lv[tl.t].b[k];
+        S[tl.t].z[k].x = 0;
+        S[tl.t].z[k].y = 0;
     }
     __syncthreads();
+}
+
+// Coarsest level: z = A^-1 b in FP64, one warp per row of the inverse
+// (coalesced reads, shuffle sum).
+template <typename T>
+__device__ void tail_bottom(const tail_levels &tl, const level_view<T> &B, double *tsh, int tid, int nth) {
+    const int N = tl.inv_n;
+    for (int k = tid; k < N / 2; k += nth) {
+        tsh[2 * k] = (double)B.b[k].x;
+        tsh[2 * k + 1] = (double)B.b[k].y;
+    }
+    __syncthreads();
+    T *zz = (T *)B.z;
+    const int lane = tid & 31, nw = nth >> 5;
+    for (int r = tid >> 5; r < N; r += nw) {
+        const double *row = tl.inv + (size_t)r * N;
+        double a = 0;
+        for (int k = lane; k < N; k += 32) a += __ldg(row + k) * tsh[k];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) zz[r] = (T)a;
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T> H) {
+    typedef typename vec2_t<T>::type V;
+    extern __shared__ __align__(32) unsigned char tail_raw[];
+    __shared__ level_view<T> S[17];  // the levels' views, read by every phase
+    double *tsh = (double *)tail_raw;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    tail_prologue(tl, H, S, tail_raw, tid, nth);
     for (int i = tl.t; i < tl.ml; i++) {
         const level_view<T> &L = S[i];
         tail_sweep(L);
@@ -1826,27 +1875,7 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
             }
         __syncthreads();
     }
-    // coarsest level: z = A^-1 b in FP64
-    {
-        const level_view<T> &B = S[tl.ml];
-        const int N = tl.inv_n;
-        for (int k = tid; k < N / 2; k += nth) {
-            tsh[2 * k] = (double)B.b[k].x;
-            tsh[2 * k + 1] = (double)B.b[k].y;
-        }
-        __syncthreads();
-        // one warp per row of the inverse: coalesced reads, shuffle sum
-        T *zz = (T *)B.z;
-        const int lane = tid & 31, nw = nth >> 5;
-        for (int r = tid >> 5; r < N; r += nw) {
-            const double *row = tl.inv + (size_t)r * N;
-            double a = 0;
-            for (int k = lane; k < N; k += 32) a += __ldg(row + k) * tsh[k];
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-            if (lane == 0) zz[r] = (T)a;
-        }
-        __syncthreads();
-    }
+    tail_bottom(tl, S[tl.ml], tsh, tid, nth);
     for (int i = tl.ml; i > tl.t; i--) {
         const level_view<T> &C = S[i], &F = S[i - 1];
         for (int jj = threadIdx.y; jj < F.n; jj += blockDim.y) {
@@ -1877,6 +1906,104 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
     }
 }
 
+// Tail of the V-cycle with the pair scheme of the streaming kernels (single
+// precision; every level above the coarsest of even width <= 64, one stencil
+// class per row, its table staged): a warp holds a whole row of a level,
+// lane L the node pair (2L, 2L+1), and the periodic neighbours come by
+// shuffles from lanes L-1 and L+1 modulo m/2.  A sweep is two phases (the
+// even rows with colours (0,0), (1,0), then the odd rows with (0,1),
+// (1,1)); residual, restriction and prolongation take one phase each.
+__device__ __forceinline__ void tail_pair_sweep(const level_view<float> &L, float4 *z4, const float4 *b4, int P,
+                                                int ln, int lane, int lsrc, int rsrc, int w, int nw) {
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int n = L.n;
+    for (int par = 0; par < 2; par++) {
+        for (int j = 2 * w + par; j < n; j += 2 * nw) {
+            const float4 d = j > 0 ? z4[(j - 1) * P + ln] : zero;
+            float4 c = z4[j * P + ln];
+            const float4 u = j < n - 1 ? z4[(j + 1) * P + ln] : zero;
+            lev_row_sweep(L.st + L.cls[j], j, n, d, c, u, b4[j * P + ln], lsrc, rsrc);
+            if (lane < P) z4[j * P + lane] = c;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_tail_pairs(tail_levels tl, hierarchy_view<float> H) {
+    extern __shared__ __align__(32) unsigned char tail_raw[];
+    __shared__ level_view<float> S[17];
+    double *tsh = (double *)tail_raw;
+    const int lane = threadIdx.x, w = threadIdx.y, nw = blockDim.y;
+    const int tid = w * 32 + lane, nth = 32 * nw;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    tail_prologue(tl, H, S, tail_raw, tid, nth);
+    for (int l = tl.t; l < tl.ml; l++) {
+        const level_view<float> &L = S[l];
+        const level_view<float> &C = S[l + 1];
+        const int P = L.m >> 1, n = L.n, ln = lane < P ? lane : P - 1;
+        const int lsrc = ln == 0 ? P - 1 : ln - 1, rsrc = ln + 1 == P ? 0 : ln + 1;
+        float4 *z4 = reinterpret_cast<float4 *>(L.z);
+        const float4 *b4 = reinterpret_cast<const float4 *>(L.b);
+        float4 *r4 = reinterpret_cast<float4 *>(L.r);
+        tail_pair_sweep(L, z4, b4, P, ln, lane, lsrc, rsrc, w, nw);
+        for (int j = w; j < n; j += nw) {
+            const float4 d = j > 0 ? z4[(j - 1) * P + ln] : zero, c = z4[j * P + ln];
+            const float4 u = j < n - 1 ? z4[(j + 1) * P + ln] : zero;
+            const float4 r = lev_pair_residual(L.st + L.cls[j], j, n, d, c, u, b4[j * P + ln], lsrc, rsrc);
+            if (lane < P) r4[j * P + lane] = r;
+        }
+        __syncthreads();
+        for (int J = w; J < C.n; J += nw) {
+            const int f0 = 2 * J - 1;
+            const float4 r0 = f0 >= 0 && f0 < n ? r4[f0 * P + ln] : zero;
+            const float4 r1 = f0 + 1 < n ? r4[(f0 + 1) * P + ln] : zero;
+            const float4 r2 = f0 + 2 < n ? r4[(f0 + 2) * P + ln] : zero;
+            const float2 v = lev_restrict(r0, r1, r2, J, n, lsrc);
+            if (lane < P) {
+                C.b[J * P + lane] = v;
+                C.z[J * P + lane] = make_float2(0.f, 0.f);
+            }
+        }
+        __syncthreads();
+    }
+    tail_bottom(tl, S[tl.ml], tsh, tid, nth);
+    for (int l = tl.ml - 1; l >= tl.t; l--) {
+        const level_view<float> &L = S[l];
+        const level_view<float> &C = S[l + 1];
+        const int P = L.m >> 1, n = L.n, ln = lane < P ? lane : P - 1;
+        const int lsrc = ln == 0 ? P - 1 : ln - 1, rsrc = ln + 1 == P ? 0 : ln + 1;
+        float4 *z4 = reinterpret_cast<float4 *>(L.z);
+        const float4 *b4 = reinterpret_cast<const float4 *>(L.b);
+        // the child has m/2 = P columns: the even node takes coarse ln, the
+        // odd node the mean of ln and rsrc
+        for (int j = w; j < n; j += nw) {
+            int cy[2], hy[2];
+            const int ny = p1d_halves(j, n, 0, cy, hy);
+            float ax = 0, ay = 0, bx = 0, by = 0;
+            for (int q = 0; q < ny; q++) {
+                const float wy = (float)hy[q] * 0.25f;
+                const float2 v0 = C.z[cy[q] * P + ln], v1 = C.z[cy[q] * P + rsrc];
+                ax += 2.f * wy * v0.x;
+                ay += 2.f * wy * v0.y;
+                bx += wy * (v0.x + v1.x);
+                by += wy * (v0.y + v1.y);
+            }
+            if (lane < P) {
+                float4 z = z4[j * P + lane];
+                z.x += ax;
+                z.y += ay;
+                z.z += bx;
+                z.w += by;
+                z4[j * P + lane] = z;
+            }
+        }
+        __syncthreads();
+        tail_pair_sweep(L, z4, b4, P, ln, lane, lsrc, rsrc, w, nw);
+    }
+    const int mn = S[tl.t].m * S[tl.t].n;
+    for (int k = tid; k < mn; k += nth) H.lv[tl.t].z[k] = S[tl.t].z[k];
+}
+
 constexpr size_t kTailSmem = 200 * 1024;
 
 // Shared memory of the tail from level t: the same partition as k_tail.
@@ -1898,7 +2025,10 @@ template <typename T> cudaError_t prepare_tail_kernel() {
     static bool done = false;
     if (done) return cudaSuccess;
     done = true;
-    return cudaFuncSetAttribute(k_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem + 1024);
+    cudaError_t e = cudaFuncSetAttribute(k_tail<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem + 1024);
+    if (e == cudaSuccess && sizeof(T) == 4)
+        e = cudaFuncSetAttribute(k_tail_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem + 1024);
+    return e;
 }
 template cudaError_t prepare_tail_kernel<float>();
 template cudaError_t prepare_tail_kernel<double>();
@@ -1940,6 +2070,16 @@ template <typename T> static int tail_start(const hierarchy<T> &h) {
     while (t > 1 && (long)h.lv[t - 1].m * h.lv[t - 1].n <= limit && tail_smem_bytes(h, t - 1) <= kTailSmem) t--;
     if (tail_smem_bytes(h, t) > kTailSmem) return ml + 1;
     return t;
+}
+
+// The pair tail covers levels t .. ml-1 of even width <= 64 with one
+// stencil class per row and their tables staged in shared memory.
+template <typename T> static bool pair_tail(const hierarchy<T> &h, int t) {
+    for (int l = t; l < h.nl - 1; l++) {
+        const level_view<T> &L = h.lv[l];
+        if ((L.m & 1) || L.m > 64 || !L.homog || tail_stage_bytes<T>(L.nst, L.ncls) > kTailStageMax) return false;
+    }
+    return true;
 }
 
 // Levels wide enough for the single-precision tile kernels (an even periodic
@@ -2089,7 +2229,14 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         for (int l = 0; l < h.nl; l++) hv.lv[l] = h.lv[l];
         tail_levels tl{t, ml, h.bottom_inv, h.bottom_unknowns};
         const size_t smem = tail_smem_bytes(h, t);
-        k_tail<T><<<1, dim3(32, 32), smem, st>>>(tl, hv);
+        if constexpr (sizeof(T) == 4) {
+            if (pair_tail(h, t))
+                k_tail_pairs<<<1, dim3(32, 32), smem, st>>>(tl, hv);
+            else
+                k_tail<T><<<1, dim3(32, 32), smem, st>>>(tl, hv);
+        } else {
+            k_tail<T><<<1, dim3(32, 32), smem, st>>>(tl, hv);
+        }
         note_launch();
         up_from = t;
     } else {
