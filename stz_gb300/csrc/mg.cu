@@ -1033,6 +1033,17 @@ __device__ __forceinline__ float4 march_load(const float2 *__restrict__ a, int j
     return __ldg(reinterpret_cast<const float4 *>(a + (size_t)j * m + gx));
 }
 
+// halves_of(2J + q - 1, n, 0, J) for q = 0, 1, 2 on a bounded line of n
+// points (p1d_halves: even fine rows inject, odd ones average, and an even
+// line injects its last point into the last coarse one).
+__device__ __forceinline__ int restrict_hy(int q, int J, int n) {
+    const int fy = 2 * J + q - 1;
+    if (fy < 0 || fy >= n) return 0;
+    if (q == 1) return 2;
+    if ((n & 1) || fy != n - 1) return 1;
+    return q == 0 ? 2 : 0;
+}
+
 // Full weighting (1,2,1)x(1,2,1)/4 of the residual rows 2J-1, 2J, 2J+1 (r0,
 // r1, r2) at the coarse point under the lane's even node, y rows through
 // halves_of for the walls.
@@ -1044,8 +1055,7 @@ __device__ __forceinline__ float2 march_restrict(const float2 &r0, const float2 
     for (int q = 0; q < 3; q++) {
         const float left = __shfl_up_sync(F, rr[q].y, 1);  // odd node of the lane to the left
         const int fy = 2 * J + q - 1;
-        if (fy < 0 || fy >= n) continue;
-        const int hy = halves_of(fy, n, 0, J);
+        const int hy = restrict_hy(q, J, n);
         if (!hy) continue;
         const float w1 = (float)hy * 0.25f, w2 = (float)(2 * hy) * 0.25f;
         if (!(fy & 1)) {
@@ -1128,6 +1138,49 @@ __device__ __forceinline__ void ring_issue(float4 (*ring)[2][32], int slot, cons
 
 __device__ __forceinline__ void ring_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(kRing - 2) : "memory"); }
 
+// The row windows of the top-level marches are circular arrays of kRing
+// entries indexed by (row - kb) mod kRing, the same index as the row's ring
+// slot; the step loop is unrolled kRing times so that every index is a
+// compile-time constant and no register moves shift the window.
+struct top_march {
+    top_op<float> op;
+    const float2 *zin, *b;
+    float2 *zout, *bc;
+    int m, n, cm, cn, y0, kb, ke, gx, lane, I;
+    bool own;
+    float4 (*rg)[2][32];
+};
+
+// One row step of the down march: row k arrives, colour 0 on row k-1,
+// colour 1 on row k-2 (stored when owned), the residual on row k-3, and the
+// restriction to coarse row (k-4)/2 when k-3 is odd.
+template <int U>
+__device__ __forceinline__ void top_down_step(const top_march &t, int k, float4 (&Z)[kRing], float4 (&B)[kRing],
+                                              float2 (&R)[kRing]) {
+    constexpr int P1 = (U + 5) % 6, P2 = (U + 4) % 6, P3 = (U + 3) % 6, P4 = (U + 2) % 6, P5 = (U + 1) % 6;
+    static_assert(kRing == 6, "window indices assume six slots");
+    ring_wait();
+    Z[U] = t.rg[U][0][t.lane];
+    B[U] = t.rg[U][1][t.lane];
+    const int jn = k + kRing - 1;
+    ring_issue(t.rg, P1, t.zin, t.b, jn <= t.ke ? jn : -1, t.m, t.n, t.gx, t.lane);
+    const int j0 = k - 1, j1 = k - 2, j2 = k - 3, n = t.n;
+    if (j0 >= t.y0 - 3 && j0 >= 0 && j0 < n) march_color(t.op, Z[P2], Z[P1], Z[U], B[P1], j0, n, 0);
+    if (j1 >= t.y0 - 2 && j1 >= 0 && j1 < n) {
+        march_color(t.op, Z[P3], Z[P2], Z[P1], B[P2], j1, n, 1);
+        if (j1 >= t.y0 && j1 < t.y0 + 2 * kMarchRows && t.own)
+            *reinterpret_cast<float4 *>(t.zout + (size_t)j1 * t.m + t.gx) = Z[P2];
+    }
+    if (j2 >= t.y0 - 1) {
+        R[P3] = march_residual(t.op, Z[P4], Z[P3], Z[P2], B[P3], j2, n);
+        if ((j2 & 1) && j2 >= t.y0 + 1) {
+            const int J = (j2 - 1) >> 1;
+            const float2 w = march_restrict(R[P5], R[P4], R[P3], J, n);
+            if (t.own && J < t.cn) t.bc[(size_t)J * t.cm + t.I] = w;
+        }
+    }
+}
+
 // Pre-smooth + residual + restriction of the top level (apply_r after one
 // gauss_seidel, tgmg.in.cc:313-320): z_out = one sweep of z_in, bc = R(b - A z_out).
 __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op, const float2 *__restrict__ zin,
@@ -1139,45 +1192,68 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op,
     const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kMarchRows;
     if (J0 >= cn) return;
     const int I0 = blockIdx.x * kDownCols;
-    const int xs = 2 * I0 - 4, y0 = 2 * J0;
-    const int gx = wrapx(xs + 2 * lane, m);
-    const int I = I0 + lane - 2;
-    const bool own = lane >= 2 && lane < 2 + kDownCols && I < cm;
+    top_march t;
+    t.op = op;
+    t.zin = zin;
+    t.b = b;
+    t.zout = zout;
+    t.bc = bc;
+    t.m = m;
+    t.n = n;
+    t.cm = cm;
+    t.cn = cn;
+    t.y0 = 2 * J0;
+    t.kb = t.y0 - 4;
+    t.ke = t.y0 + 2 * kMarchRows + 2;
+    const int xs = 2 * I0 - 4;
+    t.gx = wrapx(xs + 2 * lane, m);
+    t.lane = lane;
+    t.I = I0 + lane - 2;
+    t.own = lane >= 2 && lane < 2 + kDownCols && t.I < cm;  // columns [xs + 4, xs + 60)
+    t.rg = ring[threadIdx.x >> 5];
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 Z0 = zero, Z1 = zero, Z2 = zero, Z3 = zero, Z4 = zero;  // rows k-4 .. k
-    float4 B0 = zero, B1 = zero, B2 = zero, B3 = zero;             // rows k-3 .. k
-    float2 R0 = make_float2(0.f, 0.f), R1 = R0, R2 = R0;           // residual rows k-5 .. k-3
-    const int kb = y0 - 4, ke = y0 + 2 * kMarchRows + 2;
-    float4(*rg)[2][32] = ring[threadIdx.x >> 5];
-    for (int d = 0; d < kRing - 1; d++) ring_issue(rg, d, zin, b, kb + d, m, n, gx, lane);
-    int slot = 0;
-    for (int k = kb; k <= ke; k++) {
-        {
-            ring_wait();
-            const float4 zn = rg[slot][0][lane], bn = rg[slot][1][lane];
-            const int prev = slot == 0 ? kRing - 1 : slot - 1;
-            const int jn = k + kRing - 1;
-            ring_issue(rg, prev, zin, b, jn <= ke ? jn : -1, m, n, gx, lane);
-            slot = slot == kRing - 1 ? 0 : slot + 1;
-            Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = Z4; Z4 = zn;
-            B0 = B1; B1 = B2; B2 = B3; B3 = bn;
-            const int j0 = k - 1, j1 = k - 2, j2 = k - 3;
-            if (j0 >= y0 - 3 && j0 >= 0 && j0 < n) march_color(op, Z2, Z3, Z4, B2, j0, n, 0);
-            if (j1 >= y0 - 2 && j1 >= 0 && j1 < n) {
-                march_color(op, Z1, Z2, Z3, B1, j1, n, 1);
-                if (j1 >= y0 && j1 < y0 + 2 * kMarchRows && own && gx == xs + 2 * lane)
-                    *reinterpret_cast<float4 *>(zout + (size_t)j1 * m + gx) = Z2;
-            }
-            if (j2 >= y0 - 1) {
-                R0 = R1; R1 = R2;
-                R2 = march_residual(op, Z0, Z1, Z2, B0, j2, n);
-                if ((j2 & 1) && j2 >= y0 + 1) {
-                    const int J = (j2 - 1) >> 1;
-                    const float2 w = march_restrict(R0, R1, R2, J, n);
-                    if (own && J < cn) bc[(size_t)J * cm + I] = w;
-                }
-            }
-        }
+    float4 Z[kRing], B[kRing];
+    float2 R[kRing];
+#pragma unroll
+    for (int i = 0; i < kRing; i++) {
+        Z[i] = zero;
+        B[i] = zero;
+        R[i] = make_float2(0.f, 0.f);
+    }
+    for (int d = 0; d < kRing - 1; d++) ring_issue(t.rg, d, zin, b, t.kb + d, m, n, t.gx, lane);
+    for (int k = t.kb; k <= t.ke; k += kRing) {
+        top_down_step<0>(t, k, Z, B, R);
+        if (k + 1 > t.ke) break;
+        top_down_step<1>(t, k + 1, Z, B, R);
+        if (k + 2 > t.ke) break;
+        top_down_step<2>(t, k + 2, Z, B, R);
+        if (k + 3 > t.ke) break;
+        top_down_step<3>(t, k + 3, Z, B, R);
+        if (k + 4 > t.ke) break;
+        top_down_step<4>(t, k + 4, Z, B, R);
+        if (k + 5 > t.ke) break;
+        top_down_step<5>(t, k + 5, Z, B, R);
+    }
+}
+
+// One row step of the up march: row k arrives with the child's correction,
+// colour 0 on row k-1, colour 1 on row k-2 (stored when owned).
+template <int U>
+__device__ __forceinline__ void top_up_step(const top_march &t, const float2 (*czs)[33], int J0, int k,
+                                            float4 (&Z)[kRing], float4 (&B)[kRing]) {
+    constexpr int P1 = (U + 5) % 6, P2 = (U + 4) % 6, P3 = (U + 3) % 6;
+    ring_wait();
+    float4 zn = t.rg[U][0][t.lane];
+    B[U] = t.rg[U][1][t.lane];
+    const int jn = k + kRing - 1;
+    ring_issue(t.rg, P1, t.zin, t.b, jn <= t.ke ? jn : -1, t.m, t.n, t.gx, t.lane);
+    prolong_staged(zn, czs, J0 - 1, t.lane, k, t.n);
+    Z[U] = zn;
+    const int j0 = k - 1, j1 = k - 2, n = t.n;
+    if (j0 >= t.y0 - 1 && j0 >= 0 && j0 < n) march_color(t.op, Z[P2], Z[P1], Z[U], B[P1], j0, n, 0);
+    if (j1 >= t.y0 && j1 < n) {
+        march_color(t.op, Z[P3], Z[P2], Z[P1], B[P2], j1, n, 1);
+        if (t.own) *reinterpret_cast<float4 *>(t.zout + (size_t)j1 * t.m + t.gx) = Z[P2];
     }
 }
 
@@ -1195,34 +1271,46 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
     const int J0 = (blockIdx.y * kMarchWarps + w) * kMarchRows;
     if (J0 >= cn) return;
     const int I0 = blockIdx.x * kUpCols;
-    const int xs = 2 * I0 - 2, y0 = 2 * J0;
-    const int gx = wrapx(xs + 2 * lane, m);
-    const bool own = lane >= 1 && lane < 1 + kUpCols && xs + 2 * lane < m;
+    const int xs = 2 * I0 - 2;
+    top_march t;
+    t.op = op;
+    t.zin = zin;
+    t.b = b;
+    t.zout = zout;
+    t.bc = nullptr;
+    t.m = m;
+    t.n = n;
+    t.cm = cm;
+    t.cn = cn;
+    t.y0 = 2 * J0;
+    t.kb = t.y0 - 2;
+    t.ke = t.y0 + 2 * kMarchRows + 1;
+    t.gx = wrapx(xs + 2 * lane, m);
+    t.lane = lane;
+    t.I = 0;
+    t.own = lane >= 1 && lane < 1 + kUpCols && xs + 2 * lane < m;  // columns [xs + 2, xs + 62)
+    t.rg = ring[w];
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 Z0 = zero, Z1 = zero, Z2 = zero, Z3 = zero;  // rows k-3 .. k
-    float4 B0 = zero, B1 = zero, B2 = zero;            // rows k-2 .. k
-    const int kb = y0 - 2, ke = y0 + 2 * kMarchRows + 1;
-    float4(*rg)[2][32] = ring[w];
-    for (int d = 0; d < kRing - 1; d++) ring_issue(rg, d, zin, b, kb + d, m, n, gx, lane);
+    float4 Z[kRing], B[kRing];
+#pragma unroll
+    for (int i = 0; i < kRing; i++) {
+        Z[i] = zero;
+        B[i] = zero;
+    }
+    for (int d = 0; d < kRing - 1; d++) ring_issue(t.rg, d, zin, b, t.kb + d, m, n, t.gx, lane);
     stage_coarse<kMarchRows + 3>(czs[w], zc, cm, cn, xs / 2, J0 - 1, lane);
-    int slot = 0;
-    for (int k = kb; k <= ke; k++) {
-        ring_wait();
-        float4 zn = rg[slot][0][lane];
-        const float4 bn = rg[slot][1][lane];
-        const int prev = slot == 0 ? kRing - 1 : slot - 1;
-        const int jn = k + kRing - 1;
-        ring_issue(rg, prev, zin, b, jn <= ke ? jn : -1, m, n, gx, lane);
-        slot = slot == kRing - 1 ? 0 : slot + 1;
-        B0 = B1; B1 = B2; B2 = bn;
-        prolong_staged(zn, czs[w], J0 - 1, lane, k, n);
-        Z0 = Z1; Z1 = Z2; Z2 = Z3; Z3 = zn;
-        const int j0 = k - 1, j1 = k - 2;
-        if (j0 >= y0 - 1 && j0 >= 0 && j0 < n) march_color(op, Z1, Z2, Z3, B1, j0, n, 0);
-        if (j1 >= y0 && j1 < n) {
-            march_color(op, Z0, Z1, Z2, B0, j1, n, 1);
-            if (own) *reinterpret_cast<float4 *>(zout + (size_t)j1 * m + xs + 2 * lane) = Z1;
-        }
+    for (int k = t.kb; k <= t.ke; k += kRing) {
+        top_up_step<0>(t, czs[w], J0, k, Z, B);
+        if (k + 1 > t.ke) break;
+        top_up_step<1>(t, czs[w], J0, k + 1, Z, B);
+        if (k + 2 > t.ke) break;
+        top_up_step<2>(t, czs[w], J0, k + 2, Z, B);
+        if (k + 3 > t.ke) break;
+        top_up_step<3>(t, czs[w], J0, k + 3, Z, B);
+        if (k + 4 > t.ke) break;
+        top_up_step<4>(t, czs[w], J0, k + 4, Z, B);
+        if (k + 5 > t.ke) break;
+        top_up_step<5>(t, czs[w], J0, k + 5, Z, B);
     }
 }
 
@@ -1597,9 +1685,7 @@ __device__ __forceinline__ float2 lev_restrict(const float4 &r0, const float4 &r
 #pragma unroll
     for (int q = 0; q < 3; q++) {
         const float lx = __shfl_sync(F, rr[q].z, lsrc), ly = __shfl_sync(F, rr[q].w, lsrc);
-        const int fy = 2 * J + q - 1;
-        if (fy < 0 || fy >= n) continue;
-        const int hy = halves_of(fy, n, 0, J);
+        const int hy = restrict_hy(q, J, n);
         if (!hy) continue;
         const float w1 = (float)hy * 0.25f, w2 = (float)(2 * hy) * 0.25f;
         ax += w1 * lx;
@@ -1721,6 +1807,7 @@ struct tail_levels {
     int t, ml;
     const double *inv;
     int inv_n;
+    int inv_off;  // byte offset of a shared-memory copy of inv (pair tail), -1: none
 };
 
 template <typename T>
@@ -1803,9 +1890,10 @@ __device__ void tail_prologue(const tail_levels &tl, const hierarchy_view<T> &H,
 }
 
 // Coarsest level: z = A^-1 b in FP64, one warp per row of the inverse
-// (coalesced reads, shuffle sum).
+// (coalesced reads, shuffle sum); inv in global or shared memory.
 template <typename T>
-__device__ void tail_bottom(const tail_levels &tl, const level_view<T> &B, double *tsh, int tid, int nth) {
+__device__ void tail_bottom(const tail_levels &tl, const double *inv, const level_view<T> &B, double *tsh, int tid,
+                            int nth) {
     const int N = tl.inv_n;
     for (int k = tid; k < N / 2; k += nth) {
         tsh[2 * k] = (double)B.b[k].x;
@@ -1815,9 +1903,9 @@ __device__ void tail_bottom(const tail_levels &tl, const level_view<T> &B, doubl
     T *zz = (T *)B.z;
     const int lane = tid & 31, nw = nth >> 5;
     for (int r = tid >> 5; r < N; r += nw) {
-        const double *row = tl.inv + (size_t)r * N;
+        const double *row = inv + (size_t)r * N;
         double a = 0;
-        for (int k = lane; k < N; k += 32) a += __ldg(row + k) * tsh[k];
+        for (int k = lane; k < N; k += 32) a += row[k] * tsh[k];
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
         if (lane == 0) zz[r] = (T)a;
     }
@@ -1875,7 +1963,7 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
             }
         __syncthreads();
     }
-    tail_bottom(tl, S[tl.ml], tsh, tid, nth);
+    tail_bottom(tl, tl.inv, S[tl.ml], tsh, tid, nth);
     for (int i = tl.ml; i > tl.t; i--) {
         const level_view<T> &C = S[i], &F = S[i - 1];
         for (int jj = threadIdx.y; jj < F.n; jj += blockDim.y) {
@@ -1929,51 +2017,107 @@ __device__ __forceinline__ void tail_pair_sweep(const level_view<float> &L, floa
     }
 }
 
+// Shared-memory addresses of a tail level, rebuilt from byte offsets so that
+// the compiler sees the shared state space (plain shared loads and stores).
+struct pair_level {
+    float4 *z, *r;
+    const float4 *b;
+    float2 *z2, *b2;
+    const stencil9<float> *st;
+    const int *cls;
+};
+
+__device__ __forceinline__ pair_level pair_view(unsigned char *raw, const unsigned (*offs)[5], int l) {
+    pair_level v;
+    v.z = reinterpret_cast<float4 *>(raw + offs[l][0]);
+    v.b = reinterpret_cast<const float4 *>(raw + offs[l][1]);
+    v.r = reinterpret_cast<float4 *>(raw + offs[l][2]);
+    v.z2 = reinterpret_cast<float2 *>(raw + offs[l][0]);
+    v.b2 = reinterpret_cast<float2 *>(raw + offs[l][1]);
+    v.st = reinterpret_cast<const stencil9<float> *>(raw + offs[l][3]);
+    v.cls = reinterpret_cast<const int *>(raw + offs[l][4]);
+    return v;
+}
+
+__device__ __forceinline__ void tail_pair_sweep(const pair_level &V, int n, int P, int ln, int lane, int lsrc,
+                                                int rsrc, int w, int nw) {
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int par = 0; par < 2; par++) {
+        for (int j = 2 * w + par; j < n; j += 2 * nw) {
+            const float4 d = j > 0 ? V.z[(j - 1) * P + ln] : zero;
+            float4 c = V.z[j * P + ln];
+            const float4 u = j < n - 1 ? V.z[(j + 1) * P + ln] : zero;
+            lev_row_sweep(V.st + V.cls[j], j, n, d, c, u, V.b[j * P + ln], lsrc, rsrc);
+            if (lane < P) V.z[j * P + lane] = c;
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(1024) k_tail_pairs(tail_levels tl, hierarchy_view<float> H) {
     extern __shared__ __align__(32) unsigned char tail_raw[];
     __shared__ level_view<float> S[17];
+    __shared__ unsigned offs[17][5];
     double *tsh = (double *)tail_raw;
     const int lane = threadIdx.x, w = threadIdx.y, nw = blockDim.y;
     const int tid = w * 32 + lane, nth = 32 * nw;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int N = tl.inv_n;
+    if (tl.inv_off >= 0) {
+        // the coarsest inverse arrives while the down sweeps run
+        double *dst = reinterpret_cast<double *>(tail_raw + tl.inv_off);
+        for (int k = tid; k < N * N; k += nth) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + k);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(tl.inv + k) : "memory");
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
     tail_prologue(tl, H, S, tail_raw, tid, nth);
+    if (tid == 0)
+        for (int l = tl.t; l <= tl.ml; l++) {
+            offs[l][0] = (unsigned)((const unsigned char *)S[l].z - tail_raw);
+            offs[l][1] = (unsigned)((const unsigned char *)S[l].b - tail_raw);
+            offs[l][2] = (unsigned)((const unsigned char *)S[l].r - tail_raw);
+            offs[l][3] = l < tl.ml ? (unsigned)((const unsigned char *)S[l].st - tail_raw) : 0u;
+            offs[l][4] = l < tl.ml ? (unsigned)((const unsigned char *)S[l].cls - tail_raw) : 0u;
+        }
+    __syncthreads();
     for (int l = tl.t; l < tl.ml; l++) {
-        const level_view<float> &L = S[l];
-        const level_view<float> &C = S[l + 1];
-        const int P = L.m >> 1, n = L.n, ln = lane < P ? lane : P - 1;
+        const pair_level V = pair_view(tail_raw, offs, l), Cv = pair_view(tail_raw, offs, l + 1);
+        const int P = S[l].m >> 1, n = S[l].n, cn = S[l + 1].n, ln = lane < P ? lane : P - 1;
         const int lsrc = ln == 0 ? P - 1 : ln - 1, rsrc = ln + 1 == P ? 0 : ln + 1;
-        float4 *z4 = reinterpret_cast<float4 *>(L.z);
-        const float4 *b4 = reinterpret_cast<const float4 *>(L.b);
-        float4 *r4 = reinterpret_cast<float4 *>(L.r);
-        tail_pair_sweep(L, z4, b4, P, ln, lane, lsrc, rsrc, w, nw);
+        tail_pair_sweep(V, n, P, ln, lane, lsrc, rsrc, w, nw);
         for (int j = w; j < n; j += nw) {
-            const float4 d = j > 0 ? z4[(j - 1) * P + ln] : zero, c = z4[j * P + ln];
-            const float4 u = j < n - 1 ? z4[(j + 1) * P + ln] : zero;
-            const float4 r = lev_pair_residual(L.st + L.cls[j], j, n, d, c, u, b4[j * P + ln], lsrc, rsrc);
-            if (lane < P) r4[j * P + lane] = r;
+            const float4 d = j > 0 ? V.z[(j - 1) * P + ln] : zero, c = V.z[j * P + ln];
+            const float4 u = j < n - 1 ? V.z[(j + 1) * P + ln] : zero;
+            const float4 r = lev_pair_residual(V.st + V.cls[j], j, n, d, c, u, V.b[j * P + ln], lsrc, rsrc);
+            if (lane < P) V.r[j * P + lane] = r;
         }
         __syncthreads();
-        for (int J = w; J < C.n; J += nw) {
+        for (int J = w; J < cn; J += nw) {
             const int f0 = 2 * J - 1;
-            const float4 r0 = f0 >= 0 && f0 < n ? r4[f0 * P + ln] : zero;
-            const float4 r1 = f0 + 1 < n ? r4[(f0 + 1) * P + ln] : zero;
-            const float4 r2 = f0 + 2 < n ? r4[(f0 + 2) * P + ln] : zero;
+            const float4 r0 = f0 >= 0 && f0 < n ? V.r[f0 * P + ln] : zero;
+            const float4 r1 = f0 + 1 < n ? V.r[(f0 + 1) * P + ln] : zero;
+            const float4 r2 = f0 + 2 < n ? V.r[(f0 + 2) * P + ln] : zero;
             const float2 v = lev_restrict(r0, r1, r2, J, n, lsrc);
             if (lane < P) {
-                C.b[J * P + lane] = v;
-                C.z[J * P + lane] = make_float2(0.f, 0.f);
+                Cv.b2[J * P + lane] = v;
+                Cv.z2[J * P + lane] = make_float2(0.f, 0.f);
             }
         }
         __syncthreads();
     }
-    tail_bottom(tl, S[tl.ml], tsh, tid, nth);
+    if (tl.inv_off >= 0) {
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        __syncthreads();
+        tail_bottom(tl, reinterpret_cast<const double *>(tail_raw + tl.inv_off), S[tl.ml], tsh, tid, nth);
+    } else {
+        tail_bottom(tl, tl.inv, S[tl.ml], tsh, tid, nth);
+    }
     for (int l = tl.ml - 1; l >= tl.t; l--) {
-        const level_view<float> &L = S[l];
-        const level_view<float> &C = S[l + 1];
-        const int P = L.m >> 1, n = L.n, ln = lane < P ? lane : P - 1;
+        const pair_level V = pair_view(tail_raw, offs, l), Cv = pair_view(tail_raw, offs, l + 1);
+        const int P = S[l].m >> 1, n = S[l].n, ln = lane < P ? lane : P - 1;
         const int lsrc = ln == 0 ? P - 1 : ln - 1, rsrc = ln + 1 == P ? 0 : ln + 1;
-        float4 *z4 = reinterpret_cast<float4 *>(L.z);
-        const float4 *b4 = reinterpret_cast<const float4 *>(L.b);
         // the child has m/2 = P columns: the even node takes coarse ln, the
         // odd node the mean of ln and rsrc
         for (int j = w; j < n; j += nw) {
@@ -1982,26 +2126,27 @@ __global__ void __launch_bounds__(1024) k_tail_pairs(tail_levels tl, hierarchy_v
             float ax = 0, ay = 0, bx = 0, by = 0;
             for (int q = 0; q < ny; q++) {
                 const float wy = (float)hy[q] * 0.25f;
-                const float2 v0 = C.z[cy[q] * P + ln], v1 = C.z[cy[q] * P + rsrc];
+                const float2 v0 = Cv.z2[cy[q] * P + ln], v1 = Cv.z2[cy[q] * P + rsrc];
                 ax += 2.f * wy * v0.x;
                 ay += 2.f * wy * v0.y;
                 bx += wy * (v0.x + v1.x);
                 by += wy * (v0.y + v1.y);
             }
             if (lane < P) {
-                float4 z = z4[j * P + lane];
+                float4 z = V.z[j * P + lane];
                 z.x += ax;
                 z.y += ay;
                 z.z += bx;
                 z.w += by;
-                z4[j * P + lane] = z;
+                V.z[j * P + lane] = z;
             }
         }
         __syncthreads();
-        tail_pair_sweep(L, z4, b4, P, ln, lane, lsrc, rsrc, w, nw);
+        tail_pair_sweep(V, n, P, ln, lane, lsrc, rsrc, w, nw);
     }
+    const pair_level V = pair_view(tail_raw, offs, tl.t);
     const int mn = S[tl.t].m * S[tl.t].n;
-    for (int k = tid; k < mn; k += nth) H.lv[tl.t].z[k] = S[tl.t].z[k];
+    for (int k = tid; k < mn; k += nth) H.lv[tl.t].z[k] = V.z2[k];
 }
 
 constexpr size_t kTailSmem = 200 * 1024;
@@ -2227,8 +2372,17 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
     if (t <= ml) {
         hierarchy_view<T> hv;
         for (int l = 0; l < h.nl; l++) hv.lv[l] = h.lv[l];
-        tail_levels tl{t, ml, h.bottom_inv, h.bottom_unknowns};
-        const size_t smem = tail_smem_bytes(h, t);
+        tail_levels tl{t, ml, h.bottom_inv, h.bottom_unknowns, -1};
+        size_t smem = tail_smem_bytes(h, t);
+        if (sizeof(T) == 4 && pair_tail(h, t)) {
+            // room for a copy of the coarsest inverse after the levels
+            const size_t off = (smem + 15) & ~(size_t)15;
+            const size_t need = sizeof(double) * (size_t)h.bottom_unknowns * h.bottom_unknowns;
+            if (off + need <= kTailSmem) {
+                tl.inv_off = (int)off;
+                smem = off + need;
+            }
+        }
         if constexpr (sizeof(T) == 4) {
             if (pair_tail(h, t))
                 k_tail_pairs<<<1, dim3(32, 32), smem, st>>>(tl, hv);
