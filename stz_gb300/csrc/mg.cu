@@ -1114,6 +1114,31 @@ __device__ __forceinline__ void madd4(float2 &acc, const float4 &A, float zx, fl
     acc.y += A.z * zx + A.w * zy;
 }
 
+// Programmatic dependent launch within the FP32 V-cycle: each streaming
+// kernel lets the next one be scheduled as soon as it starts
+// (griddepcontrol.launch_dependents) and waits for its predecessor's results
+// (griddepcontrol.wait) only after the set-up that needs none, so launch
+// latency and set-up overlap the previous level's work.  Kernels launched
+// with the attribute all execute the wait before touching data another
+// kernel writes.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
+template <typename... K, typename... A>
+void launch_pdl(void (*kern)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // Per-warp ring of rows of z and b for the top-level kernels, filled by
 // cp.async kRing - 1 rows ahead of the row being consumed: row k of a march
 // sits in slot (k - kb) mod kRing.  A lane copies and later reads only its
@@ -1188,6 +1213,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op,
                                                                float2 *__restrict__ zout, float2 *__restrict__ bc,
                                                                int cm, int cn) {
     __shared__ __align__(16) float4 ring[kMarchWarps][kRing][2][32];
+    pdl_trigger();
     const int lane = threadIdx.x & 31;
     const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kMarchRows;
     if (J0 >= cn) return;
@@ -1220,6 +1246,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op,
         B[i] = zero;
         R[i] = make_float2(0.f, 0.f);
     }
+    pdl_wait();
     for (int d = 0; d < kRing - 1; d++) ring_issue(t.rg, d, zin, b, t.kb + d, m, n, t.gx, lane);
     for (int k = t.kb; k <= t.ke; k += kRing) {
         top_down_step<0>(t, k, Z, B, R);
@@ -1267,6 +1294,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
                                                              float2 *__restrict__ zout) {
     __shared__ __align__(16) float4 ring[kMarchWarps][kRing][2][32];
     __shared__ float2 czs[kMarchWarps][kMarchRows + 3][33];
+    pdl_trigger();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int J0 = (blockIdx.y * kMarchWarps + w) * kMarchRows;
     if (J0 >= cn) return;
@@ -1297,6 +1325,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
         Z[i] = zero;
         B[i] = zero;
     }
+    pdl_wait();
     for (int d = 0; d < kRing - 1; d++) ring_issue(t.rg, d, zin, b, t.kb + d, m, n, t.gx, lane);
     stage_coarse<kMarchRows + 3>(czs[w], zc, cm, cn, xs / 2, J0 - 1, lane);
     for (int k = t.kb; k <= t.ke; k += kRing) {
@@ -1701,10 +1730,12 @@ __device__ __forceinline__ float2 lev_restrict(const float4 &r0, const float4 &r
 template <int TCH>
 __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<float> L, level_view<float> C) {
     __shared__ stencil9<float> tab[kMarchStencils];
+    pdl_trigger();
     stage_stencils(tab, L);
     const int lane = threadIdx.x & 31, lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
     const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
     if (J0 >= C.n) return;
+    pdl_wait();
     const int m = L.m, n = L.n;
     const int I0 = blockIdx.x * kLevDownCols;
     const int xs = 2 * I0 - 6, y0 = 2 * J0;
@@ -1753,10 +1784,12 @@ template <int TCH>
 __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float> L, level_view<float> C) {
     __shared__ stencil9<float> tab[kMarchStencils];
     __shared__ float2 czs[kMarchWarps][TCH + 3][33];
+    pdl_trigger();
     stage_stencils(tab, L);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
     const int J0 = (blockIdx.y * kMarchWarps + w) * TCH;
     if (J0 >= C.n) return;
+    pdl_wait();
     const int m = L.m, n = L.n;
     const int I0 = blockIdx.x * kLevUpCols;
     const int xs = 2 * I0 - 4, y0 = 2 * J0;
@@ -2072,6 +2105,8 @@ __global__ void __launch_bounds__(1024) k_tail_pairs(tail_levels tl, hierarchy_v
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
     }
+    pdl_trigger();
+    pdl_wait();
     tail_prologue(tl, H, S, tail_raw, tid, nth);
     if (tid == 0)
         for (int l = tl.t; l <= tl.ml; l++) {
@@ -2255,10 +2290,10 @@ template <typename T> void launch_lev_down_m(level_view<T> &L, level_view<T> &C,
         const int t = march_rows(strips, C.n);
         const dim3 g(strips, ceil_div(ceil_div(C.n, t), kMarchWarps)), blk(32 * kMarchWarps);
         switch (t) {
-            case 16: k_lev_down_m<16><<<g, blk, 0, st>>>(L, C); break;
-            case 8: k_lev_down_m<8><<<g, blk, 0, st>>>(L, C); break;
-            case 4: k_lev_down_m<4><<<g, blk, 0, st>>>(L, C); break;
-            default: k_lev_down_m<2><<<g, blk, 0, st>>>(L, C);
+            case 16: launch_pdl(k_lev_down_m<16>, g, blk, 0, st, L, C); break;
+            case 8: launch_pdl(k_lev_down_m<8>, g, blk, 0, st, L, C); break;
+            case 4: launch_pdl(k_lev_down_m<4>, g, blk, 0, st, L, C); break;
+            default: launch_pdl(k_lev_down_m<2>, g, blk, 0, st, L, C);
         }
         note_launch();
     }
@@ -2270,10 +2305,10 @@ template <typename T> void launch_lev_up_m(level_view<T> &F, level_view<T> &C, c
         const int t = march_rows(strips, C.n);
         const dim3 g(strips, ceil_div(ceil_div(C.n, t), kMarchWarps)), blk(32 * kMarchWarps);
         switch (t) {
-            case 16: k_lev_up_m<16><<<g, blk, 0, st>>>(F, C); break;
-            case 8: k_lev_up_m<8><<<g, blk, 0, st>>>(F, C); break;
-            case 4: k_lev_up_m<4><<<g, blk, 0, st>>>(F, C); break;
-            default: k_lev_up_m<2><<<g, blk, 0, st>>>(F, C);
+            case 16: launch_pdl(k_lev_up_m<16>, g, blk, 0, st, F, C); break;
+            case 8: launch_pdl(k_lev_up_m<8>, g, blk, 0, st, F, C); break;
+            case 4: launch_pdl(k_lev_up_m<4>, g, blk, 0, st, F, C); break;
+            default: launch_pdl(k_lev_up_m<2>, g, blk, 0, st, F, C);
         }
         note_launch();
     }
@@ -2313,7 +2348,8 @@ template <typename T> void launch_top_down(hierarchy<T> &h, cudaStream_t st) {
     if constexpr (sizeof(T) == 4) {
         level_view<T> &T0 = h.lv[0], &C = h.lv[1];
         dim3 g(ceil_div(C.m, kDownCols), ceil_div(ceil_div(C.n, kMarchRows), kMarchWarps));
-        k_top_down<<<g, 32 * kMarchWarps, 0, st>>>(h.op, T0.z, T0.b, T0.m, T0.n, T0.r, C.b, C.m, C.n);
+        launch_pdl(k_top_down, g, dim3(32 * kMarchWarps), 0, st, h.op, (const float2 *)T0.z, (const float2 *)T0.b,
+                   T0.m, T0.n, T0.r, C.b, C.m, C.n);
         note_launch();
     }
 }
@@ -2322,7 +2358,8 @@ template <typename T> void launch_top_up(hierarchy<T> &h, cudaStream_t st) {
     if constexpr (sizeof(T) == 4) {
         level_view<T> &T0 = h.lv[0], &C = h.lv[1];
         dim3 g(ceil_div(C.m, kUpCols), ceil_div(ceil_div(C.n, kMarchRows), kMarchWarps));
-        k_top_up<<<g, 32 * kMarchWarps, 0, st>>>(h.op, T0.r, T0.b, T0.m, T0.n, C.z, C.m, C.n, T0.z);
+        launch_pdl(k_top_up, g, dim3(32 * kMarchWarps), 0, st, h.op, (const float2 *)T0.r, (const float2 *)T0.b,
+                   T0.m, T0.n, (const float2 *)C.z, C.m, C.n, T0.z);
         note_launch();
     }
 }
@@ -2385,7 +2422,7 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         }
         if constexpr (sizeof(T) == 4) {
             if (pair_tail(h, t))
-                k_tail_pairs<<<1, dim3(32, 32), smem, st>>>(tl, hv);
+                launch_pdl(k_tail_pairs, dim3(1), dim3(32, 32), smem, st, tl, hv);
             else
                 k_tail<T><<<1, dim3(32, 32), smem, st>>>(tl, hv);
         } else {
