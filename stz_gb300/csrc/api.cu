@@ -204,8 +204,7 @@ int run_passes(stzg_sim *s, int k) {
     const long count = (long)s->m * (s->n + 1);
     const int inner = s->g_inner;
     auto pass = [&] {
-        cudaMemsetAsync(s->h32.lv[0].z, 0, sizeof(float2) * count, s->st);
-        for (int c = 0; c < inner; c++) vcycle<float>(s->h32, s->st, 10, 1);
+        for (int c = 0; c < inner; c++) vcycle<float>(s->h32, s->st, 10, 1, c == 0);
         ff_correct(s->zhi, s->zlo, s->h32.lv[0].z, count, s->st);
         launch_norms(s, true);
     };

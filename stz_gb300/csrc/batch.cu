@@ -194,8 +194,7 @@ int add_instance(stzg_batch *b, cudaGraph_t root, int k, double dt, int nsteps, 
     int per_pass = 1;
     if (mixed) {
         per_pass = tn.inner;
-        cudaMemsetAsync(s->h32.lv[0].z, 0, sizeof(float2) * count, s->st);
-        for (int c = 0; c < tn.inner; c++) vcycle<float>(s->h32, s->st, 10, 1);
+        for (int c = 0; c < tn.inner; c++) vcycle<float>(s->h32, s->st, 10, 1, c == 0);
         ff_correct(s->zhi, s->zlo, s->h32.lv[0].z, count, s->st);
         launch_norms(s, true);
     } else {

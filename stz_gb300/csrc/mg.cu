@@ -1156,9 +1156,10 @@ __device__ __forceinline__ void cp_async16(float4 *dst, const float2 *src, bool 
 
 __device__ __forceinline__ void ring_issue(float4 (*ring)[2][32], int slot, const float2 *__restrict__ z,
                                            const float2 *__restrict__ b, int j, int m, int n, int gx, int lane) {
+    // z == nullptr: the iterate is zero and only b is read
     const bool v = j >= 0 && j < n;
     const size_t o = v ? (size_t)j * m + gx : 0;
-    cp_async16(&ring[slot][0][lane], z + o, v);
+    cp_async16(&ring[slot][0][lane], z ? z + o : b + o, v && z);
     cp_async16(&ring[slot][1][lane], b + o, v);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
@@ -2039,21 +2040,6 @@ __global__ void __launch_bounds__(1024) k_tail(tail_levels tl, hierarchy_view<T>
 // shuffles from lanes L-1 and L+1 modulo m/2.  A sweep is two phases (the
 // even rows with colours (0,0), (1,0), then the odd rows with (0,1),
 // (1,1)); residual, restriction and prolongation take one phase each.
-__device__ __forceinline__ void tail_pair_sweep(const level_view<float> &L, float4 *z4, const float4 *b4, int P,
-                                                int ln, int lane, int lsrc, int rsrc, int w, int nw) {
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int n = L.n;
-    for (int par = 0; par < 2; par++) {
-        for (int j = 2 * w + par; j < n; j += 2 * nw) {
-            const float4 d = j > 0 ? z4[(j - 1) * P + ln] : zero;
-            float4 c = z4[j * P + ln];
-            const float4 u = j < n - 1 ? z4[(j + 1) * P + ln] : zero;
-            lev_row_sweep(L.st + L.cls[j], j, n, d, c, u, b4[j * P + ln], lsrc, rsrc);
-            if (lane < P) z4[j * P + lane] = c;
-        }
-        __syncthreads();
-    }
-}
 
 // Shared-memory addresses of a tail level, rebuilt from byte offsets so that
 // the compiler sees the shared state space (plain shared loads and stores).
@@ -2349,11 +2335,12 @@ template <typename T> void launch_lev_up(level_view<T> &F, level_view<T> &C, cud
 
 // The streaming top-level kernels (single precision only): the swept z goes
 // to the level's r array on the way down and back to z on the way up.
-template <typename T> void launch_top_down(hierarchy<T> &h, cudaStream_t st) {
+template <typename T> void launch_top_down(hierarchy<T> &h, cudaStream_t st, bool zero_start) {
     if constexpr (sizeof(T) == 4) {
         level_view<T> &T0 = h.lv[0], &C = h.lv[1];
         dim3 g(ceil_div(C.m, kDownCols), ceil_div(ceil_div(C.n, kMarchRows), kMarchWarps));
-        launch_pdl(k_top_down, g, dim3(32 * kMarchWarps), 0, st, h.op, (const float2 *)T0.z, (const float2 *)T0.b,
+        launch_pdl(k_top_down, g, dim3(32 * kMarchWarps), 0, st, h.op,
+                   zero_start ? (const float2 *)nullptr : (const float2 *)T0.z, (const float2 *)T0.b,
                    T0.m, T0.n, T0.r, C.b, C.m, C.n);
         note_launch();
     }
@@ -2369,7 +2356,7 @@ template <typename T> void launch_top_up(hierarchy<T> &h, cudaStream_t st) {
     }
 }
 
-template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64) {
+template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64, bool zero_start) {
     typedef typename vec2_t<T>::type V;
     dim3 blk(32, 8);
     const int ml = h.nl - 1;
@@ -2381,8 +2368,9 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         return;
     }
     const int t = tail_start(h);
+    if (zero_start && !fused) cudaMemsetAsync(T0.z, 0, sizeof(V) * (size_t)T0.m * T0.n, st);
     if (fused) {
-        launch_top_down(h, st);
+        launch_top_down(h, st, zero_start);
     } else {
         top_sweep(h, st);
         k_top_residual<T><<<grid2(T0.m, T0.n, blk), blk, 0, st>>>(h.op, T0.z, T0.b, T0.r, T0.m, T0.n);
@@ -2526,8 +2514,8 @@ void extrapolate_guess(double2 *z, double2 *prev, long count, cudaStream_t st) {
     k_extrapolate<<<4 * 152, 256, 0, st>>>(z, prev, count); note_launch();
 }
 
-template void vcycle<double>(hierarchy<double> &, cudaStream_t, int, int);
-template void vcycle<float>(hierarchy<float> &, cudaStream_t, int, int);
+template void vcycle<double>(hierarchy<double> &, cudaStream_t, int, int, bool);
+template void vcycle<float>(hierarchy<float> &, cudaStream_t, int, int, bool);
 template void top_sweep<double>(hierarchy<double> &, cudaStream_t);
 template void top_sweep<float>(hierarchy<float> &, cudaStream_t);
 template void top_residual_sqnorm<double>(hierarchy<double> &, double *, int, double *, double *, cudaStream_t);

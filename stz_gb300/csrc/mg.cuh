@@ -107,7 +107,10 @@ template <typename T> class hierarchy {
 };
 
 // Kernel-level building blocks (mg.cu).
-template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64);
+// zero_start: the top-level z is taken as zero (the first cycle of a pass);
+// the V-cycle then clears it itself or never reads it.
+template <typename T>
+void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64, bool zero_start = false);
 template <typename T> void top_sweep(hierarchy<T> &h, cudaStream_t st);
 
 // Sum of squared residuals of the top level into *out (device), optional
