@@ -945,7 +945,8 @@ __device__ __forceinline__ int wrapx(int x, int m) { return x < 0 ? x + m : (x >
 constexpr int kFusedThreads = 256;     // blockDim of the coarse tile kernels
 constexpr int kFusedMinWidth = 80;     // narrowest even periodic line of the tile and strip kernels
 constexpr int kMarchWarps = 4;         // warps (row tiles) per block of the top-level kernels
-constexpr int kMarchRows = 16;         // coarse rows per warp tile
+constexpr int kMarchRows = 8;          // coarse rows per warp tile
+constexpr int kMarchMinWidth = 64;     // narrowest even periodic line of the streaming kernels
 constexpr int kDownCols = 28;          // coarse columns per strip (down): fine [xs + 4, xs + 60)
 constexpr int kUpCols = 30;            // coarse columns per strip (up):   fine [xs + 2, xs + 62)
 
@@ -2231,17 +2232,6 @@ template <typename T> static void lev_sweep(level_view<T> &L, cudaStream_t st) {
         }
 }
 
-// First level handled by the single-block tail (levels of at most
-// tail_points points, plus a direct coarsest solve); ml+1 when there is none.
-template <typename T> static int tail_start(const hierarchy<T> &h) {
-    const int ml = h.nl - 1;
-    if (ml < 1 || !h.bottom_inv) return ml + 1;
-    const long limit = h.tail_limit >= 0 ? h.tail_limit : (sizeof(T) == 4 ? 4400 : 300);
-    int t = ml;
-    while (t > 1 && (long)h.lv[t - 1].m * h.lv[t - 1].n <= limit && tail_smem_bytes(h, t - 1) <= kTailSmem) t--;
-    if (tail_smem_bytes(h, t) > kTailSmem) return ml + 1;
-    return t;
-}
 
 // The pair tail covers levels t .. ml-1 of even width <= 64 with one
 // stencil class per row and their tables staged in shared memory.
@@ -2262,14 +2252,30 @@ template <typename T> static bool tile_level(const hierarchy<T> &h, const level_
 // Levels for the streaming coarse kernels: tile levels with one stencil
 // class per row.
 template <typename T> static bool march_level(const hierarchy<T> &h, const level_view<T> &L) {
-    return tile_level(h, L) && L.homog && L.nst <= kMarchStencils;
+    return h.fuse && sizeof(T) == 4 && L.colors_x == 2 && L.m >= kMarchMinWidth && L.homog &&
+           L.nst <= kMarchStencils;
+}
+
+// First level handled by the single-block tail (levels of at most
+// tail_points points, plus a direct coarsest solve); ml+1 when there is none.
+template <typename T> static int tail_start(const hierarchy<T> &h) {
+    const int ml = h.nl - 1;
+    if (ml < 1 || !h.bottom_inv) return ml + 1;
+    const long limit = h.tail_limit >= 0 ? h.tail_limit : (sizeof(T) == 4 ? 4400 : 300);
+    int t = ml;
+    // a level the streaming kernels take stays out of the tail (they are faster)
+    while (t > 1 && (long)h.lv[t - 1].m * h.lv[t - 1].n <= limit && tail_smem_bytes(h, t - 1) <= kTailSmem &&
+           !march_level(h, h.lv[t - 1]))
+        t--;
+    if (tail_smem_bytes(h, t) > kTailSmem) return ml + 1;
+    return t;
 }
 
 // Coarse rows per warp of a streaming coarse kernel: the largest of 16, 8
-// and 4 that still gives eight warps per SM, else 2 (small levels are
+// and 4 that still gives sixteen warps per SM, else 2 (small levels are
 // latency-bound: shorter marches finish sooner).
 inline int march_rows(int strips, int cn) {
-    const long want = 8L * 152;
+    const long want = 16L * 152;
     for (int t = 16; t >= 4; t >>= 1)
         if ((long)strips * ceil_div(cn, t) >= want) return t;
     return 2;
