@@ -54,6 +54,23 @@ int stzg_ct_get_time(stzg_ct *s, double *time);
  * seconds (optional) the device time. */
 int stzg_ct_step_qs(stzg_ct *s, double dt, int nsteps, long *vcycles, double *seconds);
 
+/* Lagrangian tracers.  stzg_ct_tracers_init: shear_sim::initialize_tracers(mm,
+ * nn) (shear_sim.cc:1247-1283): mm x nn tracers at the cell centres of an
+ * mm x nn grid of the domain, their reference points equal to their
+ * positions, created at the current time.  stzg_ct_tracers_update:
+ * shear_sim::update_tracers (shear_sim.cc:1286-1316) with correct_tracer
+ * (:1322-1355): each tracer's position is predicted from its velocity
+ * estimate and corrected by Newton iterations on the bicubic interpolant of
+ * the reference map (bi_interp.cc), and the velocity estimate is (new - old
+ * position) / (time since creation); tracers whose Newton iteration fails are
+ * dropped in the reference's order and counted in *lost (optional).  A
+ * tracer whose interpolation leaves the grid (the reference stops the
+ * program) gives STZG_EINVAL.  stzg_ct_tracers_get: *count tracers, the first
+ * min(cap, count) copied to out as (x_ref, y_ref, x, y, v_x, v_y). */
+int stzg_ct_tracers_init(stzg_ct *s, int mm, int nn);
+int stzg_ct_tracers_update(stzg_ct *s, int *lost);
+int stzg_ct_tracers_get(stzg_ct *s, double *out, int cap, int *count);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,10 @@ def _load():
         L.ctref_time.argtypes = [V]
         L.ctref_vcount.restype = I
         L.ctref_vcount.argtypes = [V]
+        L.ctref_init_tracers.argtypes = [V, I, I]
+        L.ctref_update_tracers.argtypes = [V]
+        L.ctref_get_tracers.restype = I
+        L.ctref_get_tracers.argtypes = [V, _P, I]
         _lib = L
     return _lib
 
@@ -94,3 +98,16 @@ class ReferenceCt:
     @property
     def vcount(self):
         return self.L.ctref_vcount(self.h)
+
+    def initialize_tracers(self, mm, nn):
+        self.L.ctref_init_tracers(self.h, mm, nn)
+
+    def update_tracers(self):
+        self.L.ctref_update_tracers(self.h)
+
+    def tracers(self):
+        n = self.L.ctref_get_tracers(self.h, None, 0)
+        out = np.empty((n, 6))
+        if n:
+            self.L.ctref_get_tracers(self.h, out.ctypes.data_as(_P), n)
+        return out

@@ -100,4 +100,17 @@ double ctref_time(void *vh) { return ((ct_handle *)vh)->sim->time; }
 
 int ctref_vcount(void *vh) { return ((ct_handle *)vh)->sim->qsm.tp.vcount; }
 
+// Lagrangian tracers (shear_sim.cc:1247-1316).
+void ctref_init_tracers(void *vh, int mm, int nn) { ((ct_handle *)vh)->sim->initialize_tracers(mm, nn); }
+
+void ctref_update_tracers(void *vh) { ((ct_handle *)vh)->sim->update_tracers(); }
+
+// Copies min(cap, ntrace) tracers (6 doubles each); returns ntrace.
+int ctref_get_tracers(void *vh, double *out, int cap) {
+    shear_sim &s = *((ct_handle *)vh)->sim;
+    const int k = cap < s.ntrace ? cap : s.ntrace;
+    if (out && k > 0) std::memcpy(out, s.tr, sizeof(double) * 6 * (size_t)k);
+    return s.ntrace;
+}
+
 }  // extern "C"

@@ -25,8 +25,11 @@ def nvcc():
     return cand
 
 
+# Host code is compiled without floating-point contraction: GCC fuses a*b+c
+# on Arm by default and not on x86-64, and the host set-up (operators,
+# tracer grids) must give the same bits on both.
 def _flags(extra=()):
-    return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-O3", "-I", os.path.join(ROOT, "include"),
+    return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-O3,-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
             "-I", CSRC] + list(extra)
 
 

@@ -282,6 +282,100 @@ inline m22 minv(const m22 &x) {
     return m22{idet * x.d, -idet * x.b, -idet * x.c, idet * x.a};
 }
 
+// ---- Lagrangian tracers (shear_sim::initialize_tracers, update_tracers and
+// correct_tracer, shear_sim.cc:1247-1355) ----
+//
+// The reference map (X, Y) is interpolated with the bicubic convolution of
+// bicubic_interp (bi_interp.cc): on the ghosted node grid (origin two cells
+// before ax, ay), the four rows around the point are each reduced to the
+// coefficients (f1, (f2 - f0)/2, f0 - 5f1/2 + 2f2 - f3/2, (3f1 - f0 - 3f2 +
+// f3)/2) of the cubic through four samples, and the same combination is
+// taken across the rows.  A tracer keeps its reference point fixed; an update
+// predicts the position from the velocity estimate and corrects it by Newton
+// iterations on X(x) = Xref (four iterations within tolerance, at most 100).
+
+__device__ __forceinline__ void cubic_coeffs(double f0, double f1, double f2, double f3, double *a) {
+    a[0] = f1;
+    a[1] = -0.5 * f0 + 0.5 * f2;
+    a[2] = f0 - 2.5 * f1 + 2 * f2 - 0.5 * f3;
+    a[3] = -0.5 * f0 + 1.5 * f1 - 1.5 * f2 + 0.5 * f3;
+}
+
+__device__ __forceinline__ double cubic_at(const double *a, double y) { return a[0] + y * (a[1] + y * (a[2] + y * a[3])); }
+__device__ __forceinline__ double cubic_slope(const double *a, double y) { return a[1] + y * (2 * a[2] + 3 * y * a[3]); }
+
+// Value and gradient of the bicubic interpolant of node field f at (x, y);
+// false outside the grid squares the reference accepts (bi_interp.cc:17-27).
+__device__ bool bicubic_grad(const ct_consts &c, const double *__restrict__ f, double x, double y, double &v, double &fx,
+                             double &fy) {
+    const int gm = c.gm, gn = c.n + 4;
+    x = (x - (c.ax - 2 * c.dx)) * c.xsp;
+    y = (y - (c.ay - 2 * c.dy)) * c.ysp;
+    const int i = static_cast<int>(x), j = static_cast<int>(y);
+    if (i < 1 || i > gm - 2 || j < 1 || j > gn - 2) return false;
+    x -= i;
+    y -= j;
+    const double *up = f + i + (size_t)gm * j;
+    double r[4][4], a[4][4];  // r[row][k]: cubic in x of rows j-1 .. j+2
+    cubic_coeffs(up[-gm - 1], up[-gm], up[-gm + 1], up[-gm + 2], r[0]);
+    cubic_coeffs(up[-1], up[0], up[1], up[2], r[1]);
+    cubic_coeffs(up[gm - 1], up[gm], up[gm + 1], up[gm + 2], r[2]);
+    cubic_coeffs(up[2 * gm - 1], up[2 * gm], up[2 * gm + 1], up[2 * gm + 2], r[3]);
+    for (int k = 0; k < 4; k++) cubic_coeffs(r[0][k], r[1][k], r[2][k], r[3][k], a[k]);  // a[k]: cubic in y
+    fx = c.xsp * (cubic_at(a[1], y) + x * (2 * cubic_at(a[2], y) + 3 * x * cubic_at(a[3], y)));
+    fy = c.ysp * (cubic_slope(a[0], y) + x * (cubic_slope(a[1], y) + x * (cubic_slope(a[2], y) + x * cubic_slope(a[3], y))));
+    v = cubic_at(a[0], y) + x * (cubic_at(a[1], y) + x * (cubic_at(a[2], y) + x * cubic_at(a[3], y)));
+    return true;
+}
+
+// ok[t]: 1 updated, 0 Newton failed (the reference drops the tracer), -1
+// the interpolation left the grid (the reference stops the program).
+__global__ void k_ct_tracers(ct_consts c, const double *__restrict__ X, const double *__restrict__ Y,
+                             double *__restrict__ tr, int *__restrict__ ok, int ntr, double dt, double dtinv) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntr) return;
+    double *p = tr + 6 * (size_t)t;
+    const double xref = p[0], yref = p[1];
+    double xx = p[2] + dt * p[4], yy = p[3] + dt * p[5];
+    const double tol = DBL_EPSILON, tolnewt = tol * tol * 1e6;
+    const double ilx = 1 / c.lx, ily = 1 / c.ly, bigstep = c.lx * c.lx + c.ly * c.ly;
+    int count = 0, iter = 0, res = 1;
+    while (count < 4) {
+        if (iter > 100) {
+            res = 0;
+            break;
+        }
+        const double xs = floor((xx - c.ax) * ilx) * c.lx, ys = floor((yy - c.ay) * ily) * c.ly;
+        double vx, vy, fxx, fxy, fyx, fyy;
+        if (!bicubic_grad(c, X, xx - xs, yy - ys, vx, fxx, fxy) || !bicubic_grad(c, Y, xx - xs, yy - ys, vy, fyx, fyy)) {
+            res = -1;
+            break;
+        }
+        const double fx = vx - xref + xs, fy = vy - yref + ys;
+        if (fx * fx + fy * fy < tolnewt) count++;
+        const double det = fxx * fyy - fxy * fyx;
+        if (det < tol && det > -tol) {
+            res = 0;
+            break;
+        }
+        const double delx = (fyy * fx - fxy * fy) / det, dely = (-fyx * fx + fxx * fy) / det;
+        if (delx * delx + dely * dely > bigstep) {
+            res = 0;
+            break;
+        }
+        xx -= delx;
+        yy -= dely;
+        iter++;
+    }
+    ok[t] = res;
+    if (res == 1) {
+        p[4] = (xx - p[2]) * dtinv;
+        p[5] = (yy - p[3]) * dtinv;
+        p[2] = xx;
+        p[3] = yy;
+    }
+}
+
 }  // namespace
 }  // namespace stzg
 
@@ -302,6 +396,12 @@ struct stzg_ct {
     double2 *mg_b = nullptr, *mg_z = nullptr;
     std::vector<double> table;
     std::vector<int> cls;
+    // Lagrangian tracers: 6 doubles each (reference point, position,
+    // velocity estimate), their count and creation time
+    double *tr = nullptr;
+    int *tr_ok = nullptr;
+    int ntrace = 0, tr_cap = 0;
+    double tr_time = 0;
 };
 
 namespace {
@@ -318,6 +418,7 @@ int ct_alloc(stzg_ct *s, double **p, size_t count) {
 
 const dim3 kB2(32, 8);
 inline dim3 g2(int m, int n) { return dim3(ceil_div(m, 32), ceil_div(n, 8)); }
+
 
 void boundaries(stzg_ct *s, int b) {
     k_ct_rows<<<ceil_div(s->c.m, 128), 128, 0, s->st>>>(s->c, s->F, b, s->time);
@@ -585,6 +686,98 @@ int stzg_ct_set_time(stzg_ct *s, double time) {
 int stzg_ct_get_time(stzg_ct *s, double *time) {
     if (!s || !time) return fail(STZG_EINVAL, "null argument");
     *time = s->time;
+    return STZG_OK;
+}
+
+int stzg_ct_tracers_init(stzg_ct *s, int mm, int nn) {
+    if (!s || mm < 1 || nn < 1 || (long)mm * nn > (1L << 26)) return fail(STZG_EINVAL, "bad tracer grid");
+    STZG_CUDA(cudaSetDevice(s->device));
+    const int cnt = mm * nn;
+    if (cnt > s->tr_cap) {
+        void *a, *b;
+        STZG_CUDA(cudaMalloc(&a, sizeof(double) * 6 * (size_t)cnt));
+        if (cudaMalloc(&b, sizeof(int) * (size_t)cnt) != cudaSuccess) {
+            cudaFree(a);
+            return fail(STZG_ENOMEM, "cudaMalloc(tracers)");
+        }
+        s->owned.push_back(a);
+        s->owned.push_back(b);
+        s->tr = (double *)a;
+        s->tr_ok = (int *)b;
+        s->tr_cap = cnt;
+    }
+    // a regular grid of cell-centred points, at rest (shear_sim.cc:1265-1281)
+    std::vector<double> h((size_t)6 * cnt);
+    const double dxx = (s->P.bx - s->P.ax) / mm, dyy = (s->P.by - s->P.ay) / nn;
+    double *q = h.data();
+    for (int j = 0; j < nn; j++) {
+        const double yy = s->P.ay + dyy * (j + 0.5);
+        for (int i = 0; i < mm; i++) {
+            const double xx = s->P.ax + dxx * (i + 0.5);
+            *q++ = xx;
+            *q++ = yy;
+            *q++ = xx;
+            *q++ = yy;
+            *q++ = 0;
+            *q++ = 0;
+        }
+    }
+    STZG_CUDA(cudaMemcpyAsync(s->tr, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    s->ntrace = cnt;
+    s->tr_time = s->time;
+    return STZG_OK;
+}
+
+int stzg_ct_tracers_update(stzg_ct *s, int *lost) {
+    if (!s) return fail(STZG_EINVAL, "null handle");
+    if (!s->tr) return fail(STZG_EINVAL, "no tracers: call stzg_ct_tracers_init first");
+    STZG_CUDA(cudaSetDevice(s->device));
+    if (lost) *lost = 0;
+    if (s->ntrace == 0) return STZG_OK;
+    // dt runs from the tracers' creation, as in the reference (tr_time is
+    // not advanced by update_tracers)
+    const double dt = s->time - s->tr_time, dtinv = 1 / dt;
+    const int n = s->ntrace;
+    k_ct_tracers<<<ceil_div(n, 128), 128, 0, s->st>>>(s->c, s->F.f[s->cur][CX], s->F.f[s->cur][CY], s->tr, s->tr_ok,
+                                                       n, dt, dtinv);
+    STZG_CUDA(cudaGetLastError());
+    std::vector<int> ok(n);
+    STZG_CUDA(cudaMemcpyAsync(ok.data(), s->tr_ok, sizeof(int) * n, cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    int dropped = 0;
+    for (int t = 0; t < n; t++) {
+        if (ok[t] < 0) return fail(STZG_EINVAL, "a tracer left the interpolation grid");
+        dropped += ok[t] == 0;
+    }
+    if (dropped) {
+        // the reference moves the last tracer into a dropped one's slot and
+        // processes it there next (shear_sim.cc:1303-1313)
+        std::vector<double> h((size_t)6 * n), g;
+        STZG_CUDA(cudaMemcpy(h.data(), s->tr, sizeof(double) * h.size(), cudaMemcpyDeviceToHost));
+        std::vector<int> perm(n);
+        for (int t = 0; t < n; t++) perm[t] = t;
+        int i = 0, e = n;
+        while (i < e) {
+            if (ok[perm[i]]) i++;
+            else perm[i] = perm[--e];
+        }
+        g.resize((size_t)6 * e);
+        for (int t = 0; t < e; t++) std::memcpy(&g[(size_t)6 * t], &h[(size_t)6 * perm[t]], 6 * sizeof(double));
+        if (e) STZG_CUDA(cudaMemcpy(s->tr, g.data(), sizeof(double) * g.size(), cudaMemcpyHostToDevice));
+        s->ntrace = e;
+    }
+    if (lost) *lost = dropped;
+    return STZG_OK;
+}
+
+int stzg_ct_tracers_get(stzg_ct *s, double *out, int cap, int *count) {
+    if (!s || !count) return fail(STZG_EINVAL, "null argument");
+    *count = s->ntrace;
+    if (!out || s->ntrace == 0) return STZG_OK;
+    STZG_CUDA(cudaSetDevice(s->device));
+    const int k = cap < s->ntrace ? cap : s->ntrace;
+    if (k > 0) STZG_CUDA(cudaMemcpy(out, s->tr, sizeof(double) * 6 * (size_t)k, cudaMemcpyDeviceToHost));
     return STZG_OK;
 }
 

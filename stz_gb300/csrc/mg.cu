@@ -958,11 +958,12 @@ struct pair_sums {
     float a0, a1;
 };
 
+template <bool EX>
 __device__ __forceinline__ pair_sums march_offdiag(const top_op<float> &op, const float4 &d, const float4 &c,
-                                                   const float4 &u, bool ex) {
+                                                   const float4 &u) {
     constexpr unsigned F = 0xffffffffu;
     pair_sums s;
-    if (ex) {
+    if constexpr (EX) {
         const float xl = __shfl_up_sync(F, c.z, 1);    // x(a-1, j)
         const float dl = __shfl_up_sync(F, d.w, 1);    // y(a-1, j-1)
         const float ul = __shfl_up_sync(F, u.w, 1);    // y(a-1, j+1)
@@ -984,12 +985,14 @@ __device__ __forceinline__ pair_sums march_offdiag(const top_op<float> &op, cons
     return s;
 }
 
-// One colour on row j of the pair (the Dirichlet wall rows take z = regcbi*b).
+// One colour on row j of the pair (the Dirichlet wall rows take z =
+// regcbi*b).  EX = ((j & 1) == colour), known at compile time in the
+// unrolled marches (their rows start at an even index).
+template <bool EX>
 __device__ __forceinline__ void march_color(const top_op<float> &op, const float4 &d, float4 &c, const float4 &u,
-                                            const float4 &bb, int j, int n, int color) {
-    const bool ex = (j & 1) == color;
+                                            const float4 &bb, int j, int n) {
     if (j == 0 || j == n - 1) {
-        if (ex) {
+        if constexpr (EX) {
             c.x = op.ibcxx * bb.x;
             c.w = op.ibcyy * bb.w;
         } else {
@@ -998,8 +1001,8 @@ __device__ __forceinline__ void march_color(const top_op<float> &op, const float
         }
         return;
     }
-    const pair_sums s = march_offdiag(op, d, c, u, ex);
-    if (ex) {
+    const pair_sums s = march_offdiag<EX>(op, d, c, u);
+    if constexpr (EX) {
         c.x = op.icxx * (bb.x - s.a0);
         c.w = op.icyy * (bb.w - s.a1);
     } else {
@@ -1011,14 +1014,15 @@ __device__ __forceinline__ void march_color(const top_op<float> &op, const float
 // Residual of the colour-0 equations of the pair on row j after the sweep
 // (the colour-1 ones are zero up to rounding: their unknowns were updated
 // last and none of their neighbours changed since).  .x belongs to the even
-// node, .y to the odd one; the x component of the even node when j is even.
+// node, .y to the odd one; the x component of the even node when j is even
+// (EX = j even).
+template <bool EX>
 __device__ __forceinline__ float2 march_residual(const top_op<float> &op, const float4 &d, const float4 &c,
                                                  const float4 &u, const float4 &bb, int j, int n) {
     float2 r = make_float2(0.f, 0.f);
     if (j <= 0 || j >= n - 1) return r;
-    const bool ex = (j & 1) == 0;
-    const pair_sums s = march_offdiag(op, d, c, u, ex);
-    if (ex) {
+    const pair_sums s = march_offdiag<EX>(op, d, c, u);
+    if constexpr (EX) {
         r.x = bb.x - s.a0 - op.cxx * c.x;
         r.y = bb.w - s.a1 - op.cyy * c.w;
     } else {
@@ -1194,14 +1198,16 @@ __device__ __forceinline__ void top_down_step(const top_march &t, int k, float4 
     const int jn = k + kRing - 1;
     ring_issue(t.rg, P1, t.zin, t.b, jn <= t.ke ? jn : -1, t.m, t.n, t.gx, t.lane);
     const int j0 = k - 1, j1 = k - 2, j2 = k - 3, n = t.n;
-    if (j0 >= t.y0 - 3 && j0 >= 0 && j0 < n) march_color(t.op, Z[P2], Z[P1], Z[U], B[P1], j0, n, 0);
+    // k has the parity of U (kb is even): row k-1 is odd when U is even
+    constexpr bool E0 = (U & 1) == 1, E1 = (U & 1) == 1, ER = (U & 1) == 1;
+    if (j0 >= t.y0 - 3 && j0 >= 0 && j0 < n) march_color<E0>(t.op, Z[P2], Z[P1], Z[U], B[P1], j0, n);
     if (j1 >= t.y0 - 2 && j1 >= 0 && j1 < n) {
-        march_color(t.op, Z[P3], Z[P2], Z[P1], B[P2], j1, n, 1);
+        march_color<E1>(t.op, Z[P3], Z[P2], Z[P1], B[P2], j1, n);
         if (j1 >= t.y0 && j1 < t.y0 + 2 * kMarchRows && t.own)
             *reinterpret_cast<float4 *>(t.zout + (size_t)j1 * t.m + t.gx) = Z[P2];
     }
     if (j2 >= t.y0 - 1) {
-        R[P3] = march_residual(t.op, Z[P4], Z[P3], Z[P2], B[P3], j2, n);
+        R[P3] = march_residual<ER>(t.op, Z[P4], Z[P3], Z[P2], B[P3], j2, n);
         if ((j2 & 1) && j2 >= t.y0 + 1) {
             const int J = (j2 - 1) >> 1;
             const float2 w = march_restrict(R[P5], R[P4], R[P3], J, n);
@@ -1281,9 +1287,10 @@ __device__ __forceinline__ void top_up_step(const top_march &t, const float2 (*c
     prolong_staged(zn, czs, J0 - 1, t.lane, k, t.n);
     Z[U] = zn;
     const int j0 = k - 1, j1 = k - 2, n = t.n;
-    if (j0 >= t.y0 - 1 && j0 >= 0 && j0 < n) march_color(t.op, Z[P2], Z[P1], Z[U], B[P1], j0, n, 0);
+    constexpr bool E0 = (U & 1) == 1, E1 = (U & 1) == 1;  // as in top_down_step
+    if (j0 >= t.y0 - 1 && j0 >= 0 && j0 < n) march_color<E0>(t.op, Z[P2], Z[P1], Z[U], B[P1], j0, n);
     if (j1 >= t.y0 && j1 < n) {
-        march_color(t.op, Z[P3], Z[P2], Z[P1], B[P2], j1, n, 1);
+        march_color<E1>(t.op, Z[P3], Z[P2], Z[P1], B[P2], j1, n);
         if (t.own) *reinterpret_cast<float4 *>(t.zout + (size_t)j1 * t.m + t.gx) = Z[P2];
     }
 }

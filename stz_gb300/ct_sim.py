@@ -12,7 +12,8 @@ import numpy as np
 from . import _lib
 
 EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_set_field", "stzg_ct_get_field",
-           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs"]
+           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs", "stzg_ct_tracers_init",
+           "stzg_ct_tracers_update", "stzg_ct_tracers_get"]
 FIELDS = ("u", "v", "p", "q", "s", "tau", "chi", "X", "Y", "ddev")
 BOLTZMANN = 1.3806503e-23
 
@@ -74,6 +75,9 @@ def load():
         "stzg_ct_set_time": (I, [V, D]),
         "stzg_ct_get_time": (I, [V, _P]),
         "stzg_ct_step_qs": (I, [V, D, I, ctypes.POINTER(ctypes.c_long), _P]),
+        "stzg_ct_tracers_init": (I, [V, I, I]),
+        "stzg_ct_tracers_update": (I, [V, ctypes.POINTER(I)]),
+        "stzg_ct_tracers_get": (I, [V, _P, I, ctypes.POINTER(I)]),
     }
     for name, (res, args) in decl.items():
         f = getattr(lib, name)
@@ -135,3 +139,23 @@ class CtSim:
         vc, sec = ctypes.c_long(), ctypes.c_double()
         _lib.check(self.lib.stzg_ct_step_qs(self.h, float(dt), int(nsteps), ctypes.byref(vc), ctypes.byref(sec)))
         self.vcycles, self.seconds = vc.value, sec.value
+
+    # -- Lagrangian tracers (shear_sim.cc:1247-1355) ------------------------
+    def initialize_tracers(self, mm, nn):
+        """shear_sim::initialize_tracers(mm, nn)."""
+        _lib.check(self.lib.stzg_ct_tracers_init(self.h, int(mm), int(nn)))
+
+    def update_tracers(self):
+        """shear_sim::update_tracers(); returns the number of tracers dropped."""
+        lost = ctypes.c_int()
+        _lib.check(self.lib.stzg_ct_tracers_update(self.h, ctypes.byref(lost)))
+        return lost.value
+
+    def tracers(self):
+        """(count, 6) array: reference point, position, velocity estimate."""
+        cnt = ctypes.c_int()
+        _lib.check(self.lib.stzg_ct_tracers_get(self.h, None, 0, ctypes.byref(cnt)))
+        out = np.empty((cnt.value, 6))
+        if cnt.value:
+            _lib.check(self.lib.stzg_ct_tracers_get(self.h, out.ctypes.data_as(_P), cnt.value, ctypes.byref(cnt)))
+        return out

@@ -24,9 +24,12 @@ def golden_names(kind="quasistatic"):
     """Fixture names of one kind: "quasistatic" (step_forward_quasistatic),
     "direct" (the explicit step_forward), "frames" (output and
     diagnostics of a quasi-static state), "tgmg" (the general multigrid on
-    poisson_fd) or "ct" (the step in sheared coordinates)."""
+    poisson_fd), "ct" (the step in sheared coordinates) or "ct_tracers" (its
+    Lagrangian tracers)."""
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-    prefix = {"direct": "direct_", "frames": "frames_", "tgmg": "tgmg_", "ct": "ct_"}
+    prefix = {"direct": "direct_", "frames": "frames_", "tgmg": "tgmg_", "ct": "ct_", "ct_tracers": "ct_tracers_"}
+    if kind == "ct":
+        return [n for n in names if n.startswith("ct_") and not n.startswith("ct_tracers_")]
     if kind in prefix:
         return [n for n in names if n.startswith(prefix[kind])]
     return [n for n in names if not any(n.startswith(p) for p in prefix.values())]

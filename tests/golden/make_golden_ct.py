@@ -11,7 +11,8 @@ esim/coord_transforms/simple_shear sources with oracle/ref_ct_driver.cc), sets
 up the driver's Vitreloy configuration (shear_coord_transform.cc:20-89) on a
 small grid with shear_sim::init_fields, runs step_forward_quasistatic, and
 stores the initial and final fields (rows 0..n), the time and the V-cycle
-count as tests/golden/ct_*.npz.
+count as tests/golden/ct_*.npz; the tracer cases (ct_tracers_*.npz) add
+shear_sim::initialize_tracers / update_tracers.
 """
 import json
 import os
@@ -66,8 +67,51 @@ def make(name, case):
     ref.close()
 
 
+# Lagrangian tracers: name -> (m, n, y_prd, chi_case, tem_base, tem_delta, dt,
+# steps between updates, updates, tracer grid mm x nn).  The reference map
+# (X, Y, rows 0..n) and the time before each update_tracers are stored with
+# the tracers after it, so that the tracer update can be checked on the
+# reference's own fields.
+TRACER_CASES = {
+    "ct_tracers_wall64x32": (64, 32, False, 0, 580.0, 220.0, 3e6 / 2e4 / 600, 10, 3, 16, 8),
+    "ct_tracers_prd64x32": (64, 32, True, 0, 580.0, 220.0, 0.5 / 1e-3 / 600, 15, 2, 12, 6),
+}
+
+
+def make_tracers(name, case):
+    m, n, yp, cc, base, delta, dt, every, updates, mm, nn = case
+    P = transform_shear(m, n, y_prd=yp)
+    ref = ReferenceCt(P)
+    ref.init_fields(cc, base, delta)
+    # one step first: the reference allocates its solver's work arrays on
+    # the first solve and reads some of them before writing; allocating the
+    # tracers' interpolators first hands it recycled, nonzero memory
+    ref.steps(dt, 1)
+    ref.initialize_tracers(mm, nn)
+    out = {"tracers0": ref.tracers()}
+    times = [ref.time]
+    for u in range(updates):
+        ref.steps(dt, every)
+        out["X_%d" % u] = ref.get("X")
+        out["Y_%d" % u] = ref.get("Y")
+        times.append(ref.time)
+        ref.update_tracers()
+        out["tracers_%d" % u] = ref.tracers()
+    params = {k: getattr(P, k) for k, _ in P._fields_}
+    meta = {"params": params, "chi_case": cc, "dt": dt, "every": every, "updates": updates, "mm": mm, "nn": nn,
+            "times": times}
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    tr = out["tracers_%d" % (updates - 1)]
+    print(name, "tracers", len(tr), "max displacement", np.abs(tr[:, 2:4] - tr[:, 0:2]).max())
+    ref.close()
+
+
 def main(argv):
-    names = argv[1:] or list(CASES)
+    names = argv[1:] or list(CASES) + list(TRACER_CASES)
+    if len(names) == 1 and names[0] in TRACER_CASES:
+        make_tracers(names[0], TRACER_CASES[names[0]])
+        return
     if len(names) == 1:
         make(names[0], CASES[names[0]])
         return

@@ -94,3 +94,30 @@ def test_ct_init_fields_match_reference():
         for k in FIELDS:
             assert np.allclose(sim.get(k), arr["init_" + k], rtol=1e-14, atol=1e-15), (name, k)
         sim.close()
+
+
+@pytest.mark.parametrize("name", golden_names("ct_tracers"))
+def test_ct_tracers_match_reference(name):
+    """initialize_tracers / update_tracers on the reference's own reference
+    map (set before each update at the reference's time): the same tracer
+    positions (Newton on the bicubic interpolant) and velocity estimates."""
+    from stz_gb300.ct_sim import CtSim
+    meta, d = _load(name)
+    P = _params(meta)
+    g = CtSim(P)
+    times = meta["times"]
+    g.time = times[0]
+    g.initialize_tracers(meta["mm"], meta["nn"])
+    assert np.array_equal(g.tracers(), d["tracers0"])
+    L = max(P.bx - P.ax, P.by - P.ay)
+    for u in range(meta["updates"]):
+        g.time = times[u + 1]
+        g.set("X", d["X_%d" % u])
+        g.set("Y", d["Y_%d" % u])
+        assert g.update_tracers() == 0
+        got, ref = g.tracers(), d["tracers_%d" % u]
+        assert got.shape == ref.shape
+        assert np.abs(got[:, :4] - ref[:, :4]).max() < 1e-12 * L, np.abs(got[:, :4] - ref[:, :4]).max()
+        vscale = max(np.abs(ref[:, 4:]).max(), 1e-300)
+        assert np.abs(got[:, 4:] - ref[:, 4:]).max() < 1e-9 * vscale
+    g.close()
