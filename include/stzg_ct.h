@@ -54,6 +54,14 @@ int stzg_ct_get_time(stzg_ct *s, double *time);
  * seconds (optional) the device time. */
 int stzg_ct_step_qs(stzg_ct *s, double dt, int nsteps, long *vcycles, double *seconds);
 
+/* nsteps of shear_sim::step_forward(dt) (shear_sim.cc:218-349), the explicit
+ * step: upwinded ENO2 advection of velocity, reference map, stresses and chi,
+ * net force and viscous terms in sheared coordinates, the full elastic stress
+ * update with STZ plasticity, chi diffusion, then time and boundaries (row 0's
+ * nodes keep their values, as update_staggered leaves them).  seconds
+ * (optional) receives the device time. */
+int stzg_ct_step_direct(stzg_ct *s, double dt, int nsteps, double *seconds);
+
 /* Lagrangian tracers.  stzg_ct_tracers_init: shear_sim::initialize_tracers(mm,
  * nn) (shear_sim.cc:1247-1283): mm x nn tracers at the cell centres of an
  * mm x nn grid of the domain, their reference points equal to their

@@ -44,6 +44,8 @@ def _load():
         L.ctref_get_field.argtypes = [V, I, _P]
         L.ctref_set_field.argtypes = [V, I, _P]
         L.ctref_steps.argtypes = [V, D, I]
+        L.ctref_steps_direct.argtypes = [V, D, I]
+        L.ctref_set_time.argtypes = [V, D]
         L.ctref_time.restype = D
         L.ctref_time.argtypes = [V]
         L.ctref_vcount.restype = I
@@ -111,3 +113,9 @@ class ReferenceCt:
         if n:
             self.L.ctref_get_tracers(self.h, out.ctypes.data_as(_P), n)
         return out
+
+    def step_forward(self, dt, k=1):
+        self.L.ctref_steps_direct(self.h, dt, k)
+
+    def set_time(self, t):
+        self.L.ctref_set_time(self.h, t)

@@ -96,7 +96,14 @@ void ctref_steps(void *vh, double dt, int k) {
     for (int q = 0; q < k; q++) s.step_forward_quasistatic(dt);
 }
 
+void ctref_steps_direct(void *vh, double dt, int k) {
+    shear_sim &s = *((ct_handle *)vh)->sim;
+    for (int q = 0; q < k; q++) s.step_forward(dt);
+}
+
 double ctref_time(void *vh) { return ((ct_handle *)vh)->sim->time; }
+
+void ctref_set_time(void *vh, double t) { ((ct_handle *)vh)->sim->time = t; }
 
 int ctref_vcount(void *vh) { return ((ct_handle *)vh)->sim->qsm.tp.vcount; }
 

@@ -142,6 +142,117 @@ __global__ void k_ct_advect(ct_consts c, ct_fields F, int cur, double dt, double
     B[CCHI][k] = cchi;
 }
 
+// The explicit step per cell (i,j) and its lower-left node
+// (shear_sim::step_forward, shear_sim.cc:218-349): the node's velocity and
+// reference map advance by upwinded ENO2 advection, the net force of the
+// four surrounding cells and the viscous terms in sheared coordinates (a
+// node of row 0 keeps its values: the reference applies update_staggered
+// there); the cell's stresses take the full elastic update.  New values go
+// to buffer cur^1 (chi without its diffusion).
+__global__ void k_ct_direct(ct_consts c, ct_fields F, int cur, double dt, double time, double viscosity) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= c.m || j >= c.n) return;
+    const double third = 1. / 3., L = c.K - 2 * third * c.mu, lt = c.lamb * time, ltsq = lt * lt, mu = c.mu;
+    const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
+    const double hxxv = 2 * c.xsp * hx * viscosity, hyyv = 2 * c.ysp * hy * viscosity, hcv = 2 * (hxxv + hyyv);
+    const double *const *A = F.f[cur];
+    double *const *B = F.f[cur ^ 1];
+    const size_t k = gidx(c, i, j);
+    const long gm = c.gm;
+    const double *U = A[CU], *V = A[CV];
+    // velocity and reference map at the node
+    if (j > 0) {
+        const double uc = U[k], vc = V[k];
+        double ux, vx, Xx, Yx, uy, vy, Xy, Yy;
+        const long dx = uc > 0 ? -1 : 1, dy = vc > 0 ? -gm : gm;
+        const double sx = uc > 0 ? hx : -hx, sy = vc > 0 ? hy : -hy;
+        ux = eno_d(U, k, dx, sx);
+        vx = eno_d(V, k, dx, sx);
+        Xx = eno_d(A[CX], k, dx, sx);
+        Yx = eno_d(A[CY], k, dx, sx);
+        uy = eno_d(U, k, dy, sy);
+        vy = eno_d(V, k, dy, sy);
+        Xy = eno_d(A[CX], k, dy, sy);
+        Yy = eno_d(A[CY], k, dy, sy);
+        // net_force(fx, fy, -hx, -hy) of cells (i-1,j-1), (i,j-1), (i-1,j), (i,j)
+        const double *P = A[CP], *Q = A[CQ], *S = A[CS], *T = A[CTAU];
+        const size_t k0 = k - gm - 1, k1 = k - gm, k2 = k - 1, k3 = k;
+        const double xf = -hx, yf = -hy;
+        const double fx = (-P[k0] + P[k1] - P[k2] + P[k3] - Q[k0] + Q[k1] - Q[k2] + Q[k3] + S[k0] - S[k1] + S[k2] -
+                           S[k3]) * xf +
+                          (T[k0] + T[k1] - T[k2] - T[k3]) * yf;
+        const double fy = (T[k0] - T[k1] + T[k2] - T[k3]) * xf +
+                          (-P[k0] - P[k1] + P[k2] + P[k3] - Q[k0] - Q[k1] + Q[k2] + Q[k3] - S[k0] - S[k1] + S[k2] +
+                           S[k3]) * yf;
+        // viscosity, with the extra terms of the Laplacian in untransformed coordinates
+        const double uvisc = hxxv * (U[k + 1] + U[k - 1]) + hyyv * (U[k + gm] + U[k - gm]) - hcv * uc +
+                             dt * ltsq * c.xsp * c.xsp * (U[k + 1] - 2 * U[k] + U[k - 1]) -
+                             .5 * lt * dt * c.xsp * c.ysp * (U[k + 1 + gm] - U[k + 1 - gm] - U[k - 1 + gm] + U[k - 1 - gm]);
+        const double vvisc = hxxv * (V[k + 1] + V[k - 1]) + hyyv * (V[k + gm] + V[k - gm]) - hcv * vc +
+                             dt * ltsq * c.xsp * c.xsp * (V[k + 1] - 2 * V[k] + V[k - 1]) -
+                             .5 * lt * dt * c.xsp * c.ysp * (V[k + 1 + gm] - V[k + 1 - gm] - V[k - 1 + gm] + V[k - 1 - gm]);
+        B[CU][k] = uc + (-uc * ux - vc * uy + c.mu_inv * (fx + uvisc) - 2 * dt * c.lamb * vc);
+        B[CV][k] = vc + (-uc * vx - vc * vy + c.mu_inv * (fy + vvisc));
+        B[CX][k] = A[CX][k] + (-uc * Xx - vc * Xy);
+        B[CY][k] = A[CY][k] + (-uc * Yx - vc * Yy);
+    } else {
+        B[CU][k] = U[k];
+        B[CV][k] = V[k];
+        B[CX][k] = A[CX][k];
+        B[CY][k] = A[CY][k];
+    }
+    // deformation rate, staggered velocity and spin
+    const double u0 = U[k], ur = U[k + 1], uu = U[k + gm], uru = U[k + gm + 1];
+    const double v0 = V[k], vr = V[k + 1], vu = V[k + gm], vru = V[k + gm + 1];
+    const double uc = 0.25 * (u0 + ur + uu + uru), vc = 0.25 * (v0 + vr + vu + vru);
+    const double ux = hx * (-u0 + ur - uu + uru), uy = hy * (-u0 - ur + uu + uru);
+    const double vx = hx * (-v0 + vr - vu + vru), vy = hy * (-v0 - vr + vu + vru);
+    const double p = A[CP][k], q = A[CQ][k], s = A[CS][k], tau = A[CTAU][k], chi = A[CCHI][k];
+    const double old_p = p + (1. / 3) * c.lamb * time * (-2 * tau + c.lamb * time * (p + q + s));
+    const long dx1 = uc > 0 ? -1 : 1, dy1 = vc > 0 ? -gm : gm;
+    const double hsx = uc > 0 ? hx : -hx, hsy = vc > 0 ? hy : -hy;
+    double f1[5], f2[5];
+#pragma unroll
+    for (int f = 0; f < 5; f++) {
+        f1[f] = eno_d(A[CP + f], k, dx1, hsx);
+        f2[f] = eno_d(A[CP + f], k, dy1, hsy);
+    }
+    const double pqs = p + q + s;
+    const double unt_tau = tau - lt * pqs;
+    const double unt_q = q + lt * (1 / 3.) * (-tau + lt * .5 * pqs);
+    const double unt_s = s + lt * (tau - lt * .5 * pqs);
+    const double sbar = sqrt(3 * unt_q * unt_q + unt_s * unt_s + unt_tau * unt_tau);
+    double cchi = chi, dtmp = 0;
+    if (sbar >= 1e-12) {
+        const bool athermal = c.law.stz_model >= 2;
+        if (athermal && sbar < c.law.s_y) {
+            F.ddev[k] = 0;
+        } else {
+            double ddev;
+            int iters;
+            dtmp = adaptive_plastic(c.law, sbar, cchi, ddev, dt, iters);
+            F.ddev[k] = ddev;
+        }
+    }
+    cchi -= uc * f1[4] + vc * f2[4];
+    const double cp = -uc * f1[0] - vc * f2[0] + 2 * c.lamb * lt * third * mu * dt +
+                      third * (-dtmp * (2 * lt * tau - ltsq * (p + q + s + old_p)) - 2 * (tau - lt * mu) * (uy + vx) -
+                               (3 * L + 2 * mu + p - 2 * q) * (ux + vy) + 2 * s * (vy - ux) -
+                               ltsq * (L * (vy + ux) + 2 * mu * ux));
+    const double cq = -uc * f1[1] - vc * f2[1] - dtmp * (q - .5 * third * ltsq * old_p) +
+                      third * (dt * lt * c.lamb * mu - (tau - lt * mu) * (uy + vx) +
+                               (p - 2 * q - mu - .5 * ltsq * L) * (ux + vy) - ltsq * mu * ux + s * (vy - ux));
+    const double cs = -uc * f1[2] - vc * f2[2] - c.lamb * lt * mu * dt - dtmp * (s + .5 * ltsq * old_p) -
+                      (tau - lt * mu) * (vx - uy) + (p + q - mu) * (vy - ux) + .5 * ltsq * L * (ux + vy) + ltsq * mu * ux;
+    const double ctau = -uc * f1[3] - vc * f2[3] + dt * c.lamb * mu + ltsq * mu * vx - lt * (mu + L) * (ux + vy) +
+                        (vx - uy) * s + (mu - p - q) * (vx + uy) - dtmp * (tau - lt * old_p);
+    B[CP][k] = p + cp;
+    B[CQ][k] = q + cq;
+    B[CS][k] = s + cs;
+    B[CTAU][k] = tau + ctau;
+    B[CCHI][k] = cchi;
+}
+
 // Dpl-mediated chi diffusion in sheared coordinates (shear_sim::chi_diffusion,
 // shear_sim.cc:437-460), from the old chi of buffer `old` into the new chi.
 __global__ void k_ct_chi_diffusion(ct_consts c, ct_fields F, int old, double lt) {
@@ -473,6 +584,21 @@ int advection_step(stzg_ct *s, double dt) {
     return STZG_OK;
 }
 
+// shear_sim::step_forward (shear_sim.cc:218-349): the explicit update, chi
+// diffusion, time, boundaries.
+int direct_step(stzg_ct *s, double dt) {
+    k_ct_direct<<<g2(s->c.m, s->c.n), kB2, 0, s->st>>>(s->c, s->F, s->cur, dt, s->time, s->P.viscosity);
+    note_launch();
+    if (s->c.chi_len != 0) {
+        k_ct_chi_diffusion<<<g2(s->c.m, s->c.n), kB2, 0, s->st>>>(s->c, s->F, s->cur, s->c.lamb * s->time);
+        note_launch();
+    }
+    s->cur ^= 1;
+    s->time += dt;
+    boundaries(s, s->cur);
+    return STZG_OK;
+}
+
 int projection_step(stzg_ct *s, double dt, long *vcycles) {
     const double lt = s->c.lamb * s->time;
     m22 pre;
@@ -686,6 +812,20 @@ int stzg_ct_set_time(stzg_ct *s, double time) {
 int stzg_ct_get_time(stzg_ct *s, double *time) {
     if (!s || !time) return fail(STZG_EINVAL, "null argument");
     *time = s->time;
+    return STZG_OK;
+}
+
+int stzg_ct_step_direct(stzg_ct *s, double dt, int nsteps, double *seconds) {
+    if (!s || !(dt > 0) || nsteps < 0) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CUDA(cudaSetDevice(s->device));
+    STZG_CUDA(cudaEventRecord(s->ev0, s->st));
+    for (int k = 0; k < nsteps; k++) STZG_CHECK(direct_step(s, dt));
+    STZG_CUDA(cudaEventRecord(s->ev1, s->st));
+    STZG_CUDA(cudaEventSynchronize(s->ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    if (seconds) *seconds = ms * 1e-3;
+    STZG_CUDA(cudaGetLastError());
     return STZG_OK;
 }
 

@@ -12,7 +12,7 @@ import numpy as np
 from . import _lib
 
 EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_set_field", "stzg_ct_get_field",
-           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs", "stzg_ct_tracers_init",
+           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs", "stzg_ct_step_direct", "stzg_ct_tracers_init",
            "stzg_ct_tracers_update", "stzg_ct_tracers_get"]
 FIELDS = ("u", "v", "p", "q", "s", "tau", "chi", "X", "Y", "ddev")
 BOLTZMANN = 1.3806503e-23
@@ -75,6 +75,7 @@ def load():
         "stzg_ct_set_time": (I, [V, D]),
         "stzg_ct_get_time": (I, [V, _P]),
         "stzg_ct_step_qs": (I, [V, D, I, ctypes.POINTER(ctypes.c_long), _P]),
+        "stzg_ct_step_direct": (I, [V, D, I, _P]),
         "stzg_ct_tracers_init": (I, [V, I, I]),
         "stzg_ct_tracers_update": (I, [V, ctypes.POINTER(I)]),
         "stzg_ct_tracers_get": (I, [V, _P, I, ctypes.POINTER(I)]),
@@ -139,6 +140,12 @@ class CtSim:
         vc, sec = ctypes.c_long(), ctypes.c_double()
         _lib.check(self.lib.stzg_ct_step_qs(self.h, float(dt), int(nsteps), ctypes.byref(vc), ctypes.byref(sec)))
         self.vcycles, self.seconds = vc.value, sec.value
+
+    def step_forward(self, dt, nsteps=1):
+        """shear_sim::step_forward (shear_sim.cc:218-349), the explicit step."""
+        sec = ctypes.c_double()
+        _lib.check(self.lib.stzg_ct_step_direct(self.h, float(dt), int(nsteps), ctypes.byref(sec)))
+        self.seconds = sec.value
 
     # -- Lagrangian tracers (shear_sim.cc:1247-1355) ------------------------
     def initialize_tracers(self, mm, nn):

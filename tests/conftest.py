@@ -24,10 +24,11 @@ def golden_names(kind="quasistatic"):
     """Fixture names of one kind: "quasistatic" (step_forward_quasistatic),
     "direct" (the explicit step_forward), "frames" (output and
     diagnostics of a quasi-static state), "tgmg" (the general multigrid on
-    poisson_fd), "ct" (the step in sheared coordinates) or "ct_tracers" (its
-    Lagrangian tracers)."""
+    poisson_fd), "ct" (the step in sheared coordinates), "ct_tracers" (its
+    Lagrangian tracers) or "ct_direct" (its explicit step)."""
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-    prefix = {"direct": "direct_", "frames": "frames_", "tgmg": "tgmg_", "ct": "ct_", "ct_tracers": "ct_tracers_"}
+    prefix = {"direct": "direct_", "frames": "frames_", "tgmg": "tgmg_", "ct": "ct_", "ct_tracers": "ct_tracers_",
+              "ct_direct": "ctdirect_"}
     if kind == "ct":
         return [n for n in names if n.startswith("ct_") and not n.startswith("ct_tracers_")]
     if kind in prefix:

@@ -12,7 +12,8 @@ up the driver's Vitreloy configuration (shear_coord_transform.cc:20-89) on a
 small grid with shear_sim::init_fields, runs step_forward_quasistatic, and
 stores the initial and final fields (rows 0..n), the time and the V-cycle
 count as tests/golden/ct_*.npz; the tracer cases (ct_tracers_*.npz) add
-shear_sim::initialize_tracers / update_tracers.
+shear_sim::initialize_tracers / update_tracers, and the ctdirect_*.npz cases
+run the explicit shear_sim::step_forward from an advanced quasi-static state.
 """
 import json
 import os
@@ -107,10 +108,45 @@ def make_tracers(name, case):
     ref.close()
 
 
+# The explicit step: name -> (m, n, y_prd, chi_case, tem_base, tem_delta,
+# quasi-static dt, quasi-static lead steps, explicit dt, explicit steps).  The
+# state after the lead (plastic flow with y periodic, elastic with walls) and
+# the time are stored with the state after the explicit steps.
+DIRECT_CASES = {
+    "ctdirect_wall64x32": (64, 32, False, 0, 580.0, 220.0, 3e6 / 2e4 / 600, 20, 0.005, 100),
+    "ctdirect_prd64x32": (64, 32, True, 0, 580.0, 220.0, 0.5 / 1e-3 / 600, 39, 0.005, 60),
+}
+
+
+def make_direct(name, case):
+    m, n, yp, cc, base, delta, qdt, lead, dt, steps = case
+    P = transform_shear(m, n, y_prd=yp)
+    ref = ReferenceCt(P)
+    ref.init_fields(cc, base, delta)
+    ref.steps(qdt, lead)
+    time0 = ref.time
+    init = ref.fields()
+    ref.step_forward(dt, steps)
+    final = ref.fields()
+    out = {"init_" + k: v for k, v in init.items()}
+    out.update({"final_" + k: v for k, v in final.items()})
+    params = {k: getattr(P, k) for k, _ in P._fields_}
+    meta = {"params": params, "chi_case": cc, "dt": dt, "steps": steps, "lead": lead, "time0": time0,
+            "time": ref.time}
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, "time", ref.time, "max|s| change", np.abs(final["s"] - init["s"]).max(),
+          "ddev", np.abs(final["ddev"]).max())
+    ref.close()
+
+
 def main(argv):
-    names = argv[1:] or list(CASES) + list(TRACER_CASES)
+    names = argv[1:] or list(CASES) + list(TRACER_CASES) + list(DIRECT_CASES)
     if len(names) == 1 and names[0] in TRACER_CASES:
         make_tracers(names[0], TRACER_CASES[names[0]])
+        return
+    if len(names) == 1 and names[0] in DIRECT_CASES:
+        make_direct(names[0], DIRECT_CASES[names[0]])
         return
     if len(names) == 1:
         make(names[0], CASES[names[0]])

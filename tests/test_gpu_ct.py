@@ -121,3 +121,26 @@ def test_ct_tracers_match_reference(name):
         vscale = max(np.abs(ref[:, 4:]).max(), 1e-300)
         assert np.abs(got[:, 4:] - ref[:, 4:]).max() < 1e-9 * vscale
     g.close()
+
+
+@pytest.mark.parametrize("name", golden_names("ct_direct"))
+def test_ct_explicit_step_matches_reference(name):
+    """shear_sim::step_forward (the explicit step) from the reference's own
+    advanced state: the same fields after 60-100 steps (no solver, so the
+    only differences are roundings)."""
+    from stz_gb300.ct_sim import CtSim
+    meta, arr = _load(name)
+    P = _params(meta)
+    sim = CtSim(P)
+    sim.time = meta["time0"]
+    for k in FIELDS:
+        sim.set(k, arr["init_" + k])
+    sim.step_forward(meta["dt"], meta["steps"])
+    assert sim.time == pytest.approx(meta["time"], rel=1e-14)
+    ref = {k: arr["final_" + k] for k in FIELDS}
+    got = sim.fields()
+    err = ct_errors(ref, got, P)
+    assert max(err.values()) < 1e-10, err
+    # the update moved the state
+    assert np.abs(ref["s"] - arr["init_s"]).max() > 1e-4
+    sim.close()
