@@ -945,7 +945,8 @@ __device__ __forceinline__ int wrapx(int x, int m) { return x < 0 ? x + m : (x >
 constexpr int kFusedThreads = 256;     // blockDim of the coarse tile kernels
 constexpr int kFusedMinWidth = 80;     // narrowest even periodic line of the tile and strip kernels
 constexpr int kMarchWarps = 4;         // warps (row tiles) per block of the top-level kernels
-constexpr int kMarchRows = 8;          // coarse rows per warp tile
+constexpr int kDownRows = 8;  // coarse rows per warp tile (down)
+constexpr int kUpRows = 8;      // coarse rows per warp tile (up)
 constexpr int kMarchMinWidth = 64;     // narrowest even periodic line of the streaming kernels
 constexpr int kDownCols = 28;          // coarse columns per strip (down): fine [xs + 4, xs + 60)
 constexpr int kUpCols = 30;            // coarse columns per strip (up):   fine [xs + 2, xs + 62)
@@ -1203,7 +1204,7 @@ __device__ __forceinline__ void top_down_step(const top_march &t, int k, float4 
     if (j0 >= t.y0 - 3 && j0 >= 0 && j0 < n) march_color<E0>(t.op, Z[P2], Z[P1], Z[U], B[P1], j0, n);
     if (j1 >= t.y0 - 2 && j1 >= 0 && j1 < n) {
         march_color<E1>(t.op, Z[P3], Z[P2], Z[P1], B[P2], j1, n);
-        if (j1 >= t.y0 && j1 < t.y0 + 2 * kMarchRows && t.own)
+        if (j1 >= t.y0 && j1 < t.y0 + 2 * kDownRows && t.own)
             *reinterpret_cast<float4 *>(t.zout + (size_t)j1 * t.m + t.gx) = Z[P2];
     }
     if (j2 >= t.y0 - 1) {
@@ -1225,7 +1226,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op,
     __shared__ __align__(16) float4 ring[kMarchWarps][kRing][2][32];
     pdl_trigger();
     const int lane = threadIdx.x & 31;
-    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kMarchRows;
+    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * kDownRows;
     if (J0 >= cn) return;
     const int I0 = blockIdx.x * kDownCols;
     top_march t;
@@ -1240,7 +1241,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_down(top_op<float> op,
     t.cn = cn;
     t.y0 = 2 * J0;
     t.kb = t.y0 - 4;
-    t.ke = t.y0 + 2 * kMarchRows + 2;
+    t.ke = t.y0 + 2 * kDownRows + 2;
     const int xs = 2 * I0 - 4;
     t.gx = wrapx(xs + 2 * lane, m);
     t.lane = lane;
@@ -1304,10 +1305,10 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
                                                              const float2 *__restrict__ zc, int cm, int cn,
                                                              float2 *__restrict__ zout) {
     __shared__ __align__(16) float4 ring[kMarchWarps][kRing][2][32];
-    __shared__ float2 czs[kMarchWarps][kMarchRows + 3][33];
+    __shared__ float2 czs[kMarchWarps][kUpRows + 3][33];
     pdl_trigger();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int J0 = (blockIdx.y * kMarchWarps + w) * kMarchRows;
+    const int J0 = (blockIdx.y * kMarchWarps + w) * kUpRows;
     if (J0 >= cn) return;
     const int I0 = blockIdx.x * kUpCols;
     const int xs = 2 * I0 - 2;
@@ -1323,7 +1324,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
     t.cn = cn;
     t.y0 = 2 * J0;
     t.kb = t.y0 - 2;
-    t.ke = t.y0 + 2 * kMarchRows + 1;
+    t.ke = t.y0 + 2 * kUpRows + 1;
     t.gx = wrapx(xs + 2 * lane, m);
     t.lane = lane;
     t.I = 0;
@@ -1338,7 +1339,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_top_up(top_op<float> op, c
     }
     pdl_wait();
     for (int d = 0; d < kRing - 1; d++) ring_issue(t.rg, d, zin, b, t.kb + d, m, n, t.gx, lane);
-    stage_coarse<kMarchRows + 3>(czs[w], zc, cm, cn, xs / 2, J0 - 1, lane);
+    stage_coarse<kUpRows + 3>(czs[w], zc, cm, cn, xs / 2, J0 - 1, lane);
     for (int k = t.kb; k <= t.ke; k += kRing) {
         top_up_step<0>(t, czs[w], J0, k, Z, B);
         if (k + 1 > t.ke) break;
@@ -2351,7 +2352,7 @@ template <typename T> void launch_lev_up(level_view<T> &F, level_view<T> &C, cud
 template <typename T> void launch_top_down(hierarchy<T> &h, cudaStream_t st, bool zero_start) {
     if constexpr (sizeof(T) == 4) {
         level_view<T> &T0 = h.lv[0], &C = h.lv[1];
-        dim3 g(ceil_div(C.m, kDownCols), ceil_div(ceil_div(C.n, kMarchRows), kMarchWarps));
+        dim3 g(ceil_div(C.m, kDownCols), ceil_div(ceil_div(C.n, kDownRows), kMarchWarps));
         launch_pdl(k_top_down, g, dim3(32 * kMarchWarps), 0, st, h.op,
                    zero_start ? (const float2 *)nullptr : (const float2 *)T0.z, (const float2 *)T0.b,
                    T0.m, T0.n, T0.r, C.b, C.m, C.n);
@@ -2362,7 +2363,7 @@ template <typename T> void launch_top_down(hierarchy<T> &h, cudaStream_t st, boo
 template <typename T> void launch_top_up(hierarchy<T> &h, cudaStream_t st) {
     if constexpr (sizeof(T) == 4) {
         level_view<T> &T0 = h.lv[0], &C = h.lv[1];
-        dim3 g(ceil_div(C.m, kUpCols), ceil_div(ceil_div(C.n, kMarchRows), kMarchWarps));
+        dim3 g(ceil_div(C.m, kUpCols), ceil_div(ceil_div(C.n, kUpRows), kMarchWarps));
         launch_pdl(k_top_up, g, dim3(32 * kMarchWarps), 0, st, h.op, (const float2 *)T0.r, (const float2 *)T0.b,
                    T0.m, T0.n, (const float2 *)C.z, C.m, C.n, T0.z);
         note_launch();
