@@ -5,6 +5,11 @@ scaled to a larger grid; warm-up steps, then timed steps of the driver's
 dt = tf/600.  Prints one JSON line.
 
     python -m stz_gb300.run_ct [--m 2048] [--n 1024] [--steps 20] [--warmup 3] [--walls]
+                               [--direct DT] [--tracers MM NN]
+
+--direct DT times the explicit step (shear_sim::step_forward) of dt DT
+instead; --tracers MM NN adds an MM x NN tracer grid after the warm-up and
+times one update_tracers after the timed steps.
 """
 import argparse
 import json
@@ -20,21 +25,35 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--walls", action="store_true")
+    ap.add_argument("--direct", type=float, default=None)
+    ap.add_argument("--tracers", type=int, nargs=2, default=None)
     args = ap.parse_args(argv)
     yp = not args.walls
     P = transform_shear(args.m, args.n, y_prd=yp)
     dt = (0.5 / 1e-3 if yp else 3e6 / 2e4) / 600
     sim = CtSim(P)
     sim.init_fields(0, 580.0, 220.0)
-    sim.step_forward_quasistatic(dt, args.warmup)
+    kind = "quasi-static"
+    step = sim.step_forward_quasistatic
+    if args.direct:
+        dt, kind, step = args.direct, "explicit", sim.step_forward
+    step(dt, args.warmup)
+    if args.tracers:
+        sim.initialize_tracers(*args.tracers)
     t0 = time.perf_counter()
-    sim.step_forward_quasistatic(dt, args.steps)
+    step(dt, args.steps)
     wall = time.perf_counter() - t0
-    line = {"workload": "coord_transforms simple shear %dx%d, %s, quasi-static steps of dt %.6g" %
-                        (args.m, args.n, "y periodic, lamb 1e-3" if yp else "walls", dt),
+    line = {"workload": "coord_transforms simple shear %dx%d, %s, %s steps of dt %.6g" %
+                        (args.m, args.n, "y periodic, lamb 1e-3" if yp else "walls", kind, dt),
             "metric": "cell-steps/s", "value": args.m * args.n * args.steps / sim.seconds,
             "ms_per_step": 1e3 * sim.seconds / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
-            "vcycles_per_step": sim.vcycles / args.steps, "steps": args.steps, "warmup": args.warmup}
+            "vcycles_per_step": sim.vcycles / args.steps if not args.direct else 0, "steps": args.steps,
+            "warmup": args.warmup}
+    if args.tracers:
+        t0 = time.perf_counter()
+        lost = sim.update_tracers()
+        line["tracers"] = {"count": len(sim.tracers()), "lost": lost,
+                           "update_ms_wall": 1e3 * (time.perf_counter() - t0)}
     print(json.dumps(line))
     sim.close()
     return line
