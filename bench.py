@@ -37,6 +37,7 @@ CHI = dict(l=16.0, tem_avg=600.0, tem_std=40.0)
 
 # Algorithmic bytes (FP64 state, FP32 multigrid vectors), per cell or node:
 ADVECT_BYTES_PER_CELL = 128      # read u,v,p,q,s,tau,chi,X,Y; write p,q,s,tau,chi,X,Y (8 B each)
+TOP_BYTES_PER_NODE = 26.0        # one top-level streaming kernel: 6.5 words of 4 B
 VCYCLE32_BYTES_PER_NODE = 69.3   # 17.3 words of 4 B: 13 W on the top level x (1 + 1/4 + 1/16 + ...)
 VCYCLE64_BYTES_PER_NODE = 138.7
 SWEEP32_BYTES_PER_NODE = 24      # one Gauss-Seidel sweep: read z, b; write z (float2)
@@ -334,6 +335,24 @@ def run_ours(args, dist):
 
     line["kernels"] = {k: {"ms": t, "per_step": c, "GBs": b / (t * 1e-3) / 1e9} for k, (t, b, c) in rows.items()}
     line["mg_hbm_gbs"] = line["kernels"].get("vcycle_fp32", line["kernels"].get("vcycle_fp64"))["GBs"]
+    if prec == _lib.MIXED:
+        # the two top-level streaming kernels alone (the V-cycle's largest
+        # byte movers): 26 B per fine node each (z and b read, z written, a
+        # quarter node of the child's b written or z read)
+        top = {}
+        for kid, name in ((6, "down"), (7, "up")):
+            try:
+                t = sim.time_kernel(DT, kid, 20)
+            except _lib.StzgError:
+                continue
+            gbs = TOP_BYTES_PER_NODE * nn / (t * 1e-3) / 1e9
+            top[name] = {"us": 1e3 * t, "GBs": gbs, "frac": gbs / peak}
+        if top:
+            line["mg_top_level"] = {**top, "bytes_per_launch": TOP_BYTES_PER_NODE * nn, "peak": peak,
+                                    "peak_kind": peak_kind,
+                                    "l2": "back-to-back launches, no flush: z and b (8 B each per node) fit in "
+                                          "the 129 MB L2 at 2048^2, so these are warm-L2 figures; cold-cache "
+                                          "ncu figures in profiles/ncu_mg_streaming_2048_mixed.md"}
 
     # end to end through the C ABI with host buffers: upload the state, step,
     # download the state, every step; a fresh handle repeats the timed

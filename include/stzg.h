@@ -174,7 +174,9 @@ int stzg_mg_stencil(stzg_sim *s, double dt, int level, double *out);
  * state unchanged), 1 FP64 top-level sweep (changes the velocity iterate),
  * 2 FP32 top-level sweep (scratch), 3 FP64 V-cycle, 4 FP32 V-cycle
  * (scratch), 5 outer residual of the mixed solve (float-float) + FP32 copy +
- * norms. */
+ * norms, 6 / 7 the streaming FP32 top-level kernel down (sweep, residual,
+ * restriction) / up (prolongation, sweep) alone (scratch; STZG_EINVAL where
+ * the top level does not use them). */
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
 
 /* No counterpart in the reference.  Squared residual norms of the

@@ -771,7 +771,7 @@ int stzg_download(stzg_sim *s, double *const *down) {
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {
     if (!s || !ms || reps < 1 || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
     STZG_CHECK(ensure_ops(s, dt));
-    if ((kernel == 2 || kernel == 4 || kernel == 5) && s->O.precision != STZG_MIXED)
+    if ((kernel == 2 || kernel >= 4) && s->O.precision != STZG_MIXED)
         return fail(STZG_EINVAL, "FP32 kernels need a mixed-precision handle");
     auto one = [&]() -> int {
         switch (kernel) {
@@ -781,6 +781,11 @@ int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {
             case 3: vcycle<double>(s->h64, s->st, 10, 1); break;
             case 4: vcycle<float>(s->h32, s->st, 10, 1); break;
             case 5: launch_norms(s, true); break;
+            case 6:
+            case 7:
+                if (!top_level_kernel(s->h32, kernel - 6, s->st))
+                    return fail(STZG_EINVAL, "the top level does not use the streaming kernels");
+                break;
             default: return fail(STZG_EINVAL, "unknown kernel id");
         }
         return STZG_OK;

@@ -2528,6 +2528,16 @@ void extrapolate_guess(double2 *z, double2 *prev, long count, cudaStream_t st) {
     k_extrapolate<<<4 * 152, 256, 0, st>>>(z, prev, count); note_launch();
 }
 
+bool top_level_kernel(hierarchy<float> &h, int which, cudaStream_t st) {
+    const level_view<float> &T0 = h.lv[0];
+    if (!(h.fuse && h.nl > 1 && T0.colors_x == 2 && T0.m >= kFusedMinWidth)) return false;
+    if (which == 0)
+        launch_top_down(h, st, false);
+    else
+        launch_top_up(h, st);
+    return true;
+}
+
 template void vcycle<double>(hierarchy<double> &, cudaStream_t, int, int, bool);
 template void vcycle<float>(hierarchy<float> &, cudaStream_t, int, int, bool);
 template void top_sweep<double>(hierarchy<double> &, cudaStream_t);

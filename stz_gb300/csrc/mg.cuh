@@ -112,6 +112,9 @@ template <typename T> class hierarchy {
 template <typename T>
 void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64, bool zero_start = false);
 template <typename T> void top_sweep(hierarchy<T> &h, cudaStream_t st);
+// One launch of the streaming top-level kernel down (0) or up (1) of the FP32
+// V-cycle, for timing; false where the top level does not use them.
+bool top_level_kernel(hierarchy<float> &h, int which, cudaStream_t st);
 
 // Sum of squared residuals of the top level into *out (device), optional
 // sum of squared b into *out_b.  Deterministic: fixed grid, ordered final sum.
