@@ -278,3 +278,29 @@ def test_time_kernel_hook():
     after = g.fields()
     for name in ("p", "q", "s", "tau", "chi", "X", "Y"):
         assert np.array_equal(before[name], after[name])
+
+
+def test_time_kernel_top_level_streaming():
+    """Kernel ids 6 and 7 time the streaming top-level kernels alone on the
+    FP32 scratch hierarchy; grids too narrow for them (and FP64 handles)
+    report STZG_EINVAL."""
+    N = 128
+    P = simple_shear(N)
+    chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, 4)
+    g = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-10)
+    g.steps(0.01, 2)
+    before = g.fields()
+    for k in (6, 7):
+        assert g.time_kernel(0.01, k, 3) > 0
+    after = g.fields()
+    for name in before:
+        assert np.array_equal(before[name], after[name]), name
+    g.close()
+    small = ShearSim(simple_shear(64), random_chi(64, 64, 4, 600.0, 30.0, P.TZ, 4), precision=_lib.MIXED)
+    with pytest.raises(_lib.StzgError):
+        small.time_kernel(0.01, 6, 1)
+    small.close()
+    f64 = ShearSim(P, chi, precision=_lib.FP64)
+    with pytest.raises(_lib.StzgError):
+        f64.time_kernel(0.01, 7, 1)
+    f64.close()
