@@ -197,10 +197,10 @@ def test_state_roundtrip_keeps_extrapolation_history():
     assert max(err.values()) == 0.0, err
 
 
-def test_step_host_matches_three_calls():
+@pytest.mark.parametrize("N", [48, 160])
+def test_step_host_matches_three_calls(N):
     """stzg_step_qs_host (upload, step, download with the early copies
     overlapping the solve) gives the bytes of upload + step + download."""
-    N = 48
     P = plastic_shear(N)
     chi = random_chi(N, N, 4, 600.0, 30.0, P.TZ, 6)
     cells, nodes = N * (N + 2), N * (N + 1)
