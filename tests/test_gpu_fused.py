@@ -53,12 +53,15 @@ def test_inner_cycle_counts_converge(inner):
     assert max(err.values()) < 1e-8, err
 
 
-@pytest.mark.parametrize("N,M", [(256, 100), (192, 130), (128, 60), (160, 255)])
+@pytest.mark.parametrize("N,M", [(256, 100), (192, 130), (128, 60), (160, 255), (250, 90)])
 def test_streaming_kernels_non_square(N, M):
     """Non-square grids through the streaming kernels: odd and even node
     counts in y (the last row of an even line injects into the last coarse
-    row), odd periodic lines below 64 points (the single-block tail), and
-    strips that end inside the grid."""
+    row), odd periodic lines below 64 points (the single-block tail), strips
+    that end inside the grid, and an even top line with an odd child (125:
+    colour-by-colour kernels below a streaming top level).  (Odd top lines
+    are rejected at creation: the two-colour top-level smoother needs an even
+    periodic line.)"""
     P = plastic_shear(N, M, u_bdry=1.0)
     chi = random_chi(N, M, 4, 600.0, 30.0, P.TZ, N + M)
     a = ShearSim(P, chi, precision=_lib.FP64, tol_mode=_lib.TOL_RELATIVE, tol=1e-11)
