@@ -174,8 +174,9 @@ def make_params(N):
 
 def cpu_baseline(P, chi, steps, warm=1):
     """The oracle restatement of the reference step on the host cores,
-    relative residual 1e-10 like the GPU path."""
-    from oracle.bind import OracleSim, oracle_threads
+    relative residual 1e-10 like the GPU path; then one more step of the same
+    run on one thread."""
+    from oracle.bind import OracleSim, oracle_threads, set_oracle_threads
     t0 = time.time()
     o = OracleSim(P, chi)
     o.set_tolerance(1, RTOL)
@@ -183,24 +184,90 @@ def cpu_baseline(P, chi, steps, warm=1):
     o.seconds = 0.0
     o.steps(DT, steps)
     sec = o.seconds
+    cores = oracle_threads()
     n = P.m * P.n
-    return {"value": n * steps / sec, "unit": METRIC, "cores": oracle_threads(), "kind": "port",
-            "sample": f"{P.m}x{P.n}, {steps} timed steps after {warm} warm-up step(s), oracle restatement "
-                      f"(C, OpenMP) at relative residual {RTOL:g}; set-up {time.time() - t0 - sec:.1f} s untimed",
-            "ms_per_step": 1e3 * sec / steps}
+    rec = {"value": n * steps / sec, "unit": METRIC, "cores": cores, "kind": "port",
+           "sample": f"{P.m}x{P.n}, {steps} timed steps after {warm} warm-up step(s), oracle restatement "
+                     f"(C, OpenMP) at relative residual {RTOL:g}; set-up {time.time() - t0 - sec:.1f} s untimed",
+           "ms_per_step": 1e3 * sec / steps}
+    set_oracle_threads(1)
+    o.seconds = 0.0
+    o.steps(DT, 1)
+    set_oracle_threads(cores)
+    rec["one_thread"] = {"value": n / o.seconds, "unit": METRIC, "cores": 1, "ms_per_step": 1e3 * o.seconds,
+                         "sample": "the next step of the same run on one thread"}
+    o.close()
+    return rec
+
+
+PARITY_TOL = {"oracle": 1e-13, "fp64": 1e-13, "mixed": 1e-12}
+
+
+def prestress(sim, tau=1.02):
+    """Plastic-active start: uniform shear stress tau (units of the yield
+    stress) in every cell, so every cell runs the plastic sub-stepping."""
+    t = sim.get("tau")
+    t[:] = tau
+    sim.set("tau", t)
+
+
+def parity_vs_oracle(P, chi, nsteps, extrap, plastic=False):
+    """Group-normalised errors of the GPU paths against the oracle after the
+    same steps from the same state.  The oracle and the GPU solve to tight
+    relative residuals (the stresses are differences of the solved velocity
+    over one cell, so a looser solve moves them far more than the 1e-10 gate
+    in any implementation); the GPU paths at the benchmark's own tolerance
+    are reported beside them."""
+    from oracle.bind import OracleSim
+    from stz_gb300 import _lib
+    from stz_gb300.shear_sim import ShearSim
+    from parity import group_errors
+    o = OracleSim(P, chi)
+    o.set_tolerance(1, PARITY_TOL["oracle"])
+    if plastic:
+        prestress(o)
+    o.steps(DT, nsteps)
+    ref = o.fields()
+    o.close()
+    out = {"steps": nsteps, "tolerances": dict(PARITY_TOL)}
+    runs = (("fp64", _lib.FP64, PARITY_TOL["fp64"]), ("mixed", _lib.MIXED, PARITY_TOL["mixed"]),
+            ("fp64_at_bench_tolerance", _lib.FP64, RTOL), ("mixed_at_bench_tolerance", _lib.MIXED, RTOL))
+    for name, prec, tol in runs:
+        g = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=tol, extrapolate=extrap)
+        if plastic:
+            prestress(g)
+        g.steps(DT, nsteps)
+        out[name] = {k: float(v) for k, v in group_errors(ref, g.fields(), P.n).items()}
+        g.close()
+    if plastic:
+        out["eps_pl_max"] = float(ref["eps_pl"].max())
+    return out
+
+
+def bench_config(args, extrap, replicas):
+    """The workload dict both arms print (the reference arm times the same
+    workload on the host cores, in FP64)."""
+    N = args.size
+    mixed = args.precision == "mixed"
+    return {"workload": f"quasi-static STZ simple shear {N}x{N}, "
+                        f"{'FP32 V-cycles in FP64 iterative refinement' if mixed else 'FP64'} multigrid, "
+                        f"relative residual {RTOL:g}",
+            "grid": N, "dt": DT, "precision": args.precision, "chi": CHI, "extrapolated_guess": extrap,
+            "l2": "state (~0.6 GB FP64) larger than L2; no flush", "replicas": replicas}
 
 
 def run_reference(args, dist):
     """Reference arm: the reference's CPU implementation of the step on the
-    host cores.  The reference's own build is x86-only here, so the C
-    restatement of it (oracle/stz_oracle.c) is timed."""
+    host cores.  The reference's own build is compiled from its sources in
+    place and is x86-only, so the C restatement of it (oracle/stz_oracle.c)
+    is timed; chi comes from the oracle's own generator, so nothing of the
+    product library is loaded in this process."""
     if dist.rank != 0:
         return None
-    from stz_gb300.shear_sim import random_chi
-    from oracle.bind import OracleSim, oracle_threads
+    from oracle.bind import OracleSim, oracle_threads, random_chi as oracle_random_chi
     N = args.size
     P = make_params(N)
-    chi = random_chi(N, N, CHI["l"], CHI["tem_avg"], CHI["tem_std"], P.TZ, 2)
+    chi = oracle_random_chi(N, N, CHI["l"], CHI["tem_avg"], CHI["tem_std"], P.TZ, 2)
     o = OracleSim(P, chi)
     o.set_tolerance(1, RTOL)
     o.steps(DT, args.warmup)
@@ -210,15 +277,16 @@ def run_reference(args, dist):
     wall = time.time() - t0
     sec = o.seconds
     value = N * N * args.steps / sec
+    extrap = 0 if args.no_extrapolate else args.extrapolate_order
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian chi)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded Gaussian chi, mean 600 K, std 40 K, l=16 cells)",
             "impl": "reference",
-            "config": {"workload": f"quasi-static STZ simple shear {N}x{N}, FP64, relative residual {RTOL:g}",
-                       "grid": N, "dt": DT, "chi": CHI},
+            "config": bench_config(args, extrap, int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": oracle_threads(), "kind": "port",
-                             "sample": f"{args.steps} steps of {N}x{N} after {args.warmup} warm-up steps; "
-                                       f"wall {wall:.1f} s"},
+                             "sample": f"{args.steps} steps of {N}x{N} after {args.warmup} warm-up steps, "
+                                       f"FP64 at relative residual {RTOL:g}; wall {wall:.1f} s"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return line
 
@@ -252,11 +320,7 @@ def run_ours(args, dist):
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64+f32" if prec == _lib.MIXED else "f64",
             "data": "synthetic (seeded Gaussian chi, mean 600 K, std 40 K, l=16 cells)",
-            "config": {"workload": f"quasi-static STZ simple shear {N}x{N}, "
-                                   f"{'FP32 V-cycles in FP64 iterative refinement' if prec else 'FP64'} multigrid, "
-                                   f"relative residual {RTOL:g}",
-                       "grid": N, "dt": DT, "precision": args.precision, "extrapolated_guess": extrap,
-                       "l2": "state (~0.6 GB FP64) larger than L2; no flush", "replicas": dist.ws},
+            "config": bench_config(args, extrap, dist.ws),
             "clocks": clk, "gpu_launches": int(st.kernel_launches),
             "vcycles_per_step": st.vcycles / args.steps, "refinements_per_step": st.refinements / args.steps,
             "wall_ms_per_step": 1e3 * wall / args.steps}
@@ -326,8 +390,8 @@ def run_ours(args, dist):
     line["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_kind": peak_kind,
                         "traffic": traffic * (N / 2048.0) ** 2 if traffic else None,
-                        "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch, "
-                                          "profiles/ncu_full_qs_step_2048_mixed.md, scaled by cells",
+                        "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one launch under ncu "
+                                          "(cold caches), scaled by cells",
                         "ms_per_launch": t, "algorithmic_bytes": b,
                         "share_of_step": shares[dom] / (1e3 * dev_s / args.steps)}
     if dom == "advect":
@@ -351,8 +415,7 @@ def run_ours(args, dist):
             line["mg_top_level"] = {**top, "bytes_per_launch": TOP_BYTES_PER_NODE * nn, "peak": peak,
                                     "peak_kind": peak_kind,
                                     "l2": "back-to-back launches, no flush: z and b (8 B each per node) fit in "
-                                          "the 129 MB L2 at 2048^2, so these are warm-L2 figures; cold-cache "
-                                          "ncu figures in profiles/ncu_mg_streaming_2048_mixed.md"}
+                                          "the 129 MB L2 at 2048^2, so these are warm-L2 figures"}
 
     # end to end through the C ABI with host buffers: upload the state, step,
     # download the state, every step; a fresh handle repeats the timed
@@ -394,6 +457,15 @@ def run_ours(args, dist):
 
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(P, chi, args.cpu_steps)
+        # parity on the benchmark's own grid and chi, and on a plastic-active
+        # start (walls at +-0.04, CFL 0.41 at 2048^2, so the stress keeps
+        # loading past the yield stress)
+        from stz_gb300.params import simple_shear
+        line["rel_err_vs_oracle"] = {
+            "metric": "max |GPU - oracle| per field group over the group's scale",
+            "elastic": parity_vs_oracle(P, chi, 4, extrap),
+            "plastic_active": {"start": "tau = 1.02 s_y in every cell, walls at +-0.04",
+                               **parity_vs_oracle(simple_shear(N, u_bdry=0.04), chi, 3, extrap, plastic=True)}}
     return line
 
 

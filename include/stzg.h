@@ -64,8 +64,14 @@ typedef struct {
                           2 = quadratic, 3v(n) - 3v(n-1) + v(n-2) */
     int substep_cap;   /* iteration cap of the plastic sub-stepping per cell and step
                           (0: 4194304); reaching it returns STZG_ESUBSTEP */
-    int reserved[6];
+    int advection;     /* STZG_ADV_AUTO (0) and STZG_ADV_FP64: the advection runs in FP64,
+                          bit-exact with the per-point ENO2.  STZG_ADV_SPLIT (mixed-precision
+                          handles only): ENO differences and increments in FP32 from
+                          exactly split FP64 values, added to the FP64 state in FP64. */
+    int reserved[5];
 } stzg_options;
+
+enum { STZG_ADV_AUTO = 0, STZG_ADV_FP64 = 1, STZG_ADV_SPLIT = 2 };
 
 typedef struct {
     long vcycles;      /* V-cycles counted like tgmg_predict::add_iters (tgmg_predict.hh:24) */
@@ -107,6 +113,18 @@ int stzg_set_state(stzg_sim *s, const double *chi);
  * and shear_sim::time (shear_sim.hh:87).  Layouts as the field ids above. */
 int stzg_set_field(stzg_sim *s, int field, const double *host);
 int stzg_get_field(stzg_sim *s, int field, double *host);
+/* Replaces: shear_sim::init_fields (shear_sim.cc:60-114): zero velocity
+ * and stress, identity reference map, time 0, and chi from one of the
+ * reference's set-ups (0 a Gaussian blip at the origin, 1 a line at 30
+ * degrees, any other value sixteen blips along a sine wave) of height
+ * tem_delta over tem_base (Kelvin), ghost rows included. */
+int stzg_init_fields(stzg_sim *s, int chi_case, double tem_base, double tem_delta);
+/* Replaces: shear_sim::initialize_chi_bicubic (shear_sim.cc:832-909): chi
+ * of the cells = lo + sca * the bicubic interpolant of arr (mm x nn,
+ * row-major, periodic in x, nn >= 2) stretched over the domain; the other
+ * fields as stzg_init_fields.  The reference leaves chi's ghost rows as they
+ * were; here they get set_boundaries' linear extrapolation. */
+int stzg_chi_bicubic(stzg_sim *s, int mm, int nn, const double *arr, double lo, double sca);
 int stzg_set_time(stzg_sim *s, double time);
 int stzg_get_time(stzg_sim *s, double *time);
 
@@ -191,8 +209,10 @@ int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
  * in the library's static device memory, held on every GPU that loads the
  * library until exit; grids above 8,388,608 nodes are rejected with
  * STZG_EINVAL.  The first call on a device looks up that array's device
- * address (make it before capturing work on that device into a graph).
- * Calls share the array: calls that overlap on the GPU race.  Work is
+ * address (make it before capturing work on that device into a graph) and
+ * keeps it until exit, so a device must not be reset with cudaDeviceReset
+ * while it is used through this call.  Calls share the array: calls that
+ * overlap on the GPU race.  Work is
  * enqueued on `stream` (a cudaStream_t, NULL for the default stream) and
  * the call returns without synchronizing. */
 int stzg_residual_norms_noalloc(const stz_params *p, double dt, const double *z_dev, const double *b_dev,

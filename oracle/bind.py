@@ -18,7 +18,16 @@ from stz_gb300.params import StzParams
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libstzoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libstzref.so")
-REFERENCE_ROOT = os.environ.get("STZ_REFERENCE_ROOT", "/root/reference")
+_root = []
+
+
+def reference_root():
+    """The reference tree oracle/build_ref.sh resolves (STZ_REFERENCE_ROOT or
+    the recipe's default), or None where it is absent (the GPU host)."""
+    if not _root:
+        r = subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), "--root"], capture_output=True, text=True)
+        _root.append(r.stdout.strip() if r.returncode == 0 and r.stdout.strip() else None)
+    return _root[0]
 
 FIELD_IDS = {"u": 0, "v": 1, "p": 2, "q": 3, "s": 4, "tau": 5, "chi": 6, "X": 7, "Y": 8, "ddev": 9}
 NODE_FIELDS = ("u", "v", "X", "Y")
@@ -44,14 +53,15 @@ def build_reference(force=False):
     """Build oracle/_ref/libstzref.so from the reference sources if present."""
     if os.path.exists(REF_SO) and not force:
         return REF_SO
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "esim")):
+    root = reference_root()
+    if root is None:
         return None
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT])
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), root])
     return REF_SO
 
 
 def reference_available():
-    return os.path.exists(REF_SO) or os.path.isdir(os.path.join(REFERENCE_ROOT, "esim"))
+    return os.path.exists(REF_SO) or reference_root() is not None
 
 
 def _load(path, prefix):
@@ -80,11 +90,17 @@ def _load(path, prefix):
     f("mg_vcycle").argtypes = [ctypes.c_void_p, ctypes.c_double, _P, _P]
     f("mg_l2_error").restype = ctypes.c_double
     f("mg_l2_error").argtypes = [ctypes.c_void_p]
+    f("init_fields").argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+    f("chi_bicubic").argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, ctypes.c_double]
+    f("l2_comparison").argtypes = [ctypes.c_void_p, ctypes.c_void_p, _P]
     if prefix == "stzo_":
         lib.stzo_set_tolerance.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
         lib.stzo_random_chi.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_ulonglong, _P]
         lib.stzo_threads.restype = ctypes.c_int
+        lib.stzo_set.argtypes = [ctypes.c_void_p, ctypes.c_int, _P]
+        lib.stzo_set_threads.argtypes = [ctypes.c_int]
+        lib.stzo_mg_residual_sqnorms.argtypes = [ctypes.c_void_p, ctypes.c_double, _P, _P, _P]
     else:
         lib.stzref_output.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
         lib.stzref_qs_measure.argtypes = [ctypes.c_void_p, ctypes.c_int, _P, _P]
@@ -132,6 +148,24 @@ class _Sim:
         self._f("set_state")(self.h, _ptr(chi))
         self.eps_pl[:] = 0
 
+    def init_fields(self, chi_case, tem_base=600.0, tem_delta=200.0):
+        """shear_sim::init_fields (shear_sim.cc:60-114)."""
+        self._f("init_fields")(self.h, int(chi_case), float(tem_base), float(tem_delta))
+        self.eps_pl[:] = 0
+
+    def chi_bicubic(self, arr, lo=0.0, sca=1.0):
+        """shear_sim::initialize_chi_bicubic (shear_sim.cc:832-909); arr is (nn, mm)."""
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        nn, mm = a.shape
+        self._f("chi_bicubic")(self.h, mm, nn, _ptr(a), float(lo), float(sca))
+        self.eps_pl[:] = 0
+
+    def l2_comparison(self, other):
+        """shear_sim::l2_comparison (shear_sim.cc:460-502): (velocity, stress, chi, reference map)."""
+        out = np.zeros(4)
+        self._f("l2_comparison")(self.h, other.h, _ptr(out))
+        return out
+
     def steps(self, dt, nsteps):
         sec = ctypes.c_double(0)
         c = self._f("steps")(self.h, dt, nsteps, _ptr(self.eps_pl), ctypes.byref(sec))
@@ -159,6 +193,13 @@ class _Sim:
         out = np.empty(rows * self.m)
         self._f("get")(self.h, FIELD_IDS[name], _ptr(out))
         return out.reshape(rows, self.m)
+
+    def set(self, name, values):
+        """Overwrite a stored field (not u, v) in the layout of get()."""
+        if name in ("u", "v"):
+            raise ValueError("velocities are not settable")
+        a = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        self._f("set")(self.h, FIELD_IDS[name], _ptr(a))
 
     def fields(self):
         d = {k: self.get(k) for k in FIELD_IDS}
@@ -205,6 +246,15 @@ class OracleSim(_Sim):
     def __init__(self, params, chi=None):
         self.lib = _load(build_oracle(), "stzo_")
         super().__init__(params, chi)
+
+    def mg_residual_sqnorms(self, dt, src, vel):
+        """(sum of squared residuals, sum of squared sources) of the
+        quasi-static system for src and vel, each (n+1, m, 2)."""
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        out = np.zeros(2)
+        self.lib.stzo_mg_residual_sqnorms(self.h, dt, _ptr(src), _ptr(vel), _ptr(out))
+        return float(out[0]), float(out[1])
 
     def set_tolerance(self, mode, value):
         """mode 0: reference rule with multiplier ``value`` (default 1e4);
@@ -271,3 +321,9 @@ def random_chi(m, n, l, tem_avg, tem_std, TZ, seed):
 def oracle_threads():
     lib = _load(build_oracle(), "stzo_")
     return lib.stzo_threads()
+
+
+def set_oracle_threads(k):
+    """OpenMP threads of the oracle's following parallel regions."""
+    lib = _load(build_oracle(), "stzo_")
+    lib.stzo_set_threads(int(k))

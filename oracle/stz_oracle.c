@@ -928,6 +928,160 @@ void stzo_set_state(stzo_sim *S, const double *chi) {
     S->time = 0;
 }
 
+/* Resting state of every field but chi (zero velocity, stress and ddev,
+ * identity reference map), rows -1..n, and a cleared solver array. */
+static void rest_state(stzo_sim *S) {
+    const int m = S->m, n = S->n;
+    for (int j = -1; j <= n; j++)
+        for (int i = 0; i < m; i++) {
+            size_t c = CI(S, i, j);
+            S->u[c] = S->v[c] = S->ddev[c] = 0;
+            S->p[c] = S->q[c] = S->s[c] = S->tau[c] = 0;
+            S->X[c] = S->P.ax + i * S->dx;
+            S->Y[c] = S->P.ay + j * S->dy;
+        }
+    memset(S->vel, 0, sizeof(v2) * (size_t)m * (n + 1));
+    S->time = 0;
+}
+
+/* shear_sim::init_fields, shear_sim.cc:60-114: chi cases 0 (a Gaussian
+ * blip at the origin), 1 (a line at 30 degrees, wrapped), 2 (sixteen blips
+ * along a sine wave), evaluated at the cell centres of rows -1..n. */
+void stzo_init_fields(stzo_sim *S, int chi_case, double tem_base, double tem_delta) {
+    const double pi = 3.1415926535897932384626433832795;
+    const int m = S->m, n = S->n;
+    const double chi0 = tem_base / S->P.TZ, chi1 = tem_delta / S->P.TZ;
+    double sx[16], sy[16];
+    for (int k = 0; k < 16; k++) {
+        sx[k] = S->P.ax + S->lx * (k + 0.5) * 0.0625;
+        sy[k] = -0.2 * sin(pi * 0.0625 * (2 * k + 1));
+    }
+    rest_state(S);
+    for (int j = -1; j <= n; j++) {
+        const double ys = S->P.ay + j * S->dy + 0.5 * S->dy;
+        for (int i = 0; i < m; i++) {
+            const double xs = S->P.ax + i * S->dx + 0.5 * S->dx;
+            double e;
+            if (chi_case == 0) {
+                e = xs * xs + ys * ys;
+            } else if (chi_case == 1) {
+                const double ca = cos(30 * pi / 180.), sa = sin(30 * pi / 180.);
+                double xr = ca * xs + sa * ys, yr = -sa * xs + ca * ys;
+                xr = xr < -1 ? xr + 1 : (xr > 1 ? xr - 1 : 0);
+                e = xr * xr + yr * yr;
+            } else {
+                e = 1e100;
+                for (int k = 0; k < 16; k++) {
+                    double xr = sx[k] - xs, yr = sy[k] - ys;
+                    if (xr < -S->lx * 0.5) xr += S->lx;
+                    if (xr > S->lx * 0.5) xr -= S->lx;
+                    double r2 = xr * xr + yr * yr;
+                    if (r2 < e) e = r2;
+                }
+            }
+            S->chi[CI(S, i, j)] = chi0 + chi1 * exp(-200 * e);
+        }
+    }
+}
+
+/* shear_sim::initialize_chi_bicubic, shear_sim.cc:832-909: chi of rows
+ * 0..n-1 is lo + sca times the bicubic Hermite interpolant of arr (mm x nn,
+ * periodic in x) with centred-difference derivatives (one-sided on the first
+ * and last rows); the ghost rows get the linear extrapolation of
+ * set_boundaries. */
+void stzo_chi_bicubic(stzo_sim *S, int mm, int nn, const double *arr, double lo, double sca) {
+    const int m = S->m, n = S->n;
+    const size_t cnt = (size_t)mm * nn;
+    double *ax = malloc(sizeof(double) * cnt), *ay = malloc(sizeof(double) * cnt),
+           *axy = malloc(sizeof(double) * cnt);
+    for (int j = 0; j < nn; j++)
+        for (int i = 0; i < mm; i++) {
+            const int ir = i == mm - 1 ? 0 : i + 1, il = i == 0 ? mm - 1 : i - 1;
+            ax[(size_t)j * mm + i] = 0.5 * (arr[(size_t)j * mm + ir] - arr[(size_t)j * mm + il]);
+        }
+    for (int j = 0; j < nn; j++)
+        for (int i = 0; i < mm; i++) {
+            const size_t c = (size_t)j * mm + i;
+            if (j == 0) {
+                ay[c] = arr[c + mm] - arr[c];
+                axy[c] = ax[c + mm] - ax[c];
+            } else if (j == nn - 1) {
+                ay[c] = arr[c] - arr[c - mm];
+                axy[c] = ax[c] - ax[c - mm];
+            } else {
+                ay[c] = 0.5 * (arr[c + mm] - arr[c - mm]);
+                axy[c] = 0.5 * (ax[c + mm] - ax[c - mm]);
+            }
+        }
+    rest_state(S);
+    const double xsca = S->dx * mm / (S->P.bx - S->P.ax), ysca = S->dy * nn / (S->P.by - S->P.ay);
+    for (int j = 0; j < n; j++) {
+        double y = (j + 0.5) * ysca - 0.5;
+        int jj = (int)y;
+        if (jj < 0) jj = 0;
+        else if (jj > nn - 2) jj = nn - 2;
+        y -= jj;
+        const double my = 1 - y;
+        /* Hermite basis in y: derivative at 0, value at 0, value at 1, derivative at 1 */
+        const double hy0 = y * my * my, hy1 = my * my * (1 + 2 * y), hy2 = y * y * (3 - 2 * y), hy3 = -y * y * my;
+        for (int i = 0; i < m; i++) {
+            double x = (i + 0.5) * xsca - 0.5;
+            if (x < 0) x += mm;
+            int ii = (int)x;
+            if (ii >= mm) ii -= mm;
+            const size_t c0 = (size_t)jj * mm + ii, c1 = (size_t)jj * mm + (ii == mm - 1 ? 0 : ii + 1);
+            x -= ii;
+            const double mx = 1 - x;
+            const double hx0 = x * mx * mx, hx1 = mx * mx * (1 + 2 * x), hx2 = x * x * (3 - 2 * x), hx3 = -x * x * mx;
+            const double r0 = axy[c0] * hx0 + ay[c0] * hx1 + ay[c1] * hx2 + axy[c1] * hx3;
+            const double r1 = ax[c0] * hx0 + arr[c0] * hx1 + arr[c1] * hx2 + ax[c1] * hx3;
+            const double r2 = ax[c0 + mm] * hx0 + arr[c0 + mm] * hx1 + arr[c1 + mm] * hx2 + ax[c1 + mm] * hx3;
+            const double r3 = axy[c0 + mm] * hx0 + ay[c0 + mm] * hx1 + ay[c1 + mm] * hx2 + axy[c1 + mm] * hx3;
+            S->chi[CI(S, i, j)] = lo + sca * (hy0 * r0 + hy1 * r1 + hy2 * r2 + hy3 * r3);
+        }
+    }
+    for (int i = 0; i < m; i++) {
+        S->chi[CI(S, i, -1)] = 2 * S->chi[CI(S, i, 0)] - S->chi[CI(S, i, 1)];
+        S->chi[CI(S, i, n)] = 2 * S->chi[CI(S, i, n - 1)] - S->chi[CI(S, i, n - 2)];
+    }
+    free(ax); free(ay); free(axy);
+}
+
+/* shear_sim::l2_comparison, shear_sim.cc:460-502: dx dy times the sums of
+ * squared differences of (u, v) and (X, Y) over node rows 0..n with weight
+ * 1/2 on rows 0 and n, of the stresses (2 tau^2 + 2 s^2 + 3 p^2 + 6 q^2) and
+ * of chi over the cells. */
+void stzo_l2_comparison(stzo_sim *A, stzo_sim *B, double *l2) {
+    const int m = A->m, n = A->n;
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    for (int j = 0; j <= n; j++) {
+        double c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+        for (int i = 0; i < m; i++) {
+            const size_t c = CI(A, i, j);
+            const double du = A->u[c] - B->u[c], dv = A->v[c] - B->v[c];
+            const double dX = A->X[c] - B->X[c], dY = A->Y[c] - B->Y[c];
+            c0 += du * du + dv * dv;
+            c3 += dX * dX + dY * dY;
+            if (j < n) {
+                const double dp = A->p[c] - B->p[c], dq = A->q[c] - B->q[c], ds = A->s[c] - B->s[c],
+                             dt = A->tau[c] - B->tau[c], dc = A->chi[c] - B->chi[c];
+                c1 += 2 * (dt * dt + ds * ds) + 3 * dp * dp + 6 * dq * dq;
+                c2 += dc * dc;
+            }
+        }
+        const double w = (j == 0 || j == n) ? 0.5 : 1.0;
+        a0 += w * c0;
+        a3 += w * c3;
+        a1 += c1;
+        a2 += c2;
+    }
+    const double fac = A->dx * A->dy;
+    l2[0] = a0 * fac;
+    l2[1] = a1 * fac;
+    l2[2] = a2 * fac;
+    l2[3] = a3 * fac;
+}
+
 void stzo_set_tolerance(stzo_sim *S, int mode, double value) {
     S->tol_mode = mode;
     if (mode == 0) {
@@ -1008,6 +1162,22 @@ void stzo_get(stzo_sim *S, int field, double *out) {
     else memcpy(out, src, sizeof(double) * (size_t)m * (n + 2));
 }
 
+/* Overwrites a stored field (ids of stzo_get; not u, v): cell fields
+ * with their ghost rows, X and Y on node rows 0..n.  Used to start both
+ * sides of a parity run from the same prepared state. */
+void stzo_set(stzo_sim *S, int field, const double *in) {
+    const int m = S->m, n = S->n;
+    double *dst;
+    switch (field) {
+        case 2: dst = S->p; break; case 3: dst = S->q; break; case 4: dst = S->s; break;
+        case 5: dst = S->tau; break; case 6: dst = S->chi; break; case 7: dst = S->X; break;
+        case 8: dst = S->Y; break; case 9: dst = S->ddev; break;
+        default: return;
+    }
+    if (field == 7 || field == 8) memcpy(dst + CI(S, 0, 0), in, sizeof(double) * (size_t)m * (n + 1));
+    else memcpy(dst, in, sizeof(double) * (size_t)m * (n + 2));
+}
+
 void stzo_get_vel(stzo_sim *S, double *out) {
     memcpy(out, S->vel, sizeof(v2) * (size_t)S->m * (S->n + 1));
 }
@@ -1044,6 +1214,19 @@ void stzo_mg_vcycle(stzo_sim *S, double dt, const double *src, double *vel) {
 }
 
 double stzo_mg_l2_error(stzo_sim *S) { return mds(S, 0) / S->lv[0].mn; }
+
+/* Sum of squared residuals of the quasi-static system (mds, tgmg.in.cc:55-64)
+ * for the given source and velocity, and the sum of squared sources. */
+void stzo_mg_residual_sqnorms(stzo_sim *S, double dt, const double *src, const double *vel, double *out) {
+    qs_init(S, S->P.viscosity / dt);
+    size_t mn = (size_t)S->m * (S->n + 1);
+    memcpy(S->src, src, sizeof(v2) * mn);
+    memcpy(S->vel, vel, sizeof(v2) * mn);
+    out[0] = mds(S, 0);
+    double b2 = 0;
+    for (size_t k = 0; k < 2 * mn; k++) b2 += src[k] * src[k];
+    out[1] = b2;
+}
 
 /* ---------------------------------------------------------------------- */
 /* Random chi (initialize_random, shear_sim.cc:915-998).  The reference draws
@@ -1116,5 +1299,15 @@ int stzo_threads(void) {
     return omp_get_max_threads();
 #else
     return 1;
+#endif
+}
+
+/* Threads of the following parallel regions (the CPU baseline's
+ * one-thread figure). */
+void stzo_set_threads(int k) {
+#ifdef _OPENMP
+    omp_set_num_threads(k > 0 ? k : 1);
+#else
+    (void)k;
 #endif
 }

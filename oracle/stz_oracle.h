@@ -47,17 +47,26 @@ double stzo_time(stzo_sim *s);
 /* Field ids as oracle/ref_driver.cc: 0 u,1 v,7 X,8 Y node (m*(n+1));
  * 2 p,3 q,4 s,5 tau,6 chi,9 ddev cell with ghost rows (m*(n+2)). */
 void stzo_get(stzo_sim *s, int field, double *out);
+void stzo_set(stzo_sim *s, int field, const double *in);
+/* shear_sim::init_fields (chi cases 0-2) and initialize_chi_bicubic: the
+ * other fields at rest, solver array cleared, time 0. */
+void stzo_init_fields(stzo_sim *s, int chi_case, double tem_base, double tem_delta);
+void stzo_chi_bicubic(stzo_sim *s, int mm, int nn, const double *arr, double lo, double sca);
+/* shear_sim::l2_comparison: l2[4] = (velocity, stress, chi, reference map). */
+void stzo_l2_comparison(stzo_sim *a, stzo_sim *b, double *l2);
 void stzo_get_vel(stzo_sim *s, double *out);
 int stzo_mg_levels(stzo_sim *s, double dt, int *dims);
 void stzo_mg_stencil(stzo_sim *s, int level, double *out);
 int stzo_mg_solve(stzo_sim *s, double dt, const double *src, double *vel, int *ncycles);
 void stzo_mg_vcycle(stzo_sim *s, double dt, const double *src, double *vel);
 double stzo_mg_l2_error(stzo_sim *s);
+void stzo_mg_residual_sqnorms(stzo_sim *s, double dt, const double *src, const double *vel, double *out);
 /* Seeded Gaussian random chi field (initialize_random semantics,
  * shear_sim.cc:915-998) into out[m*n]. */
 void stzo_random_chi(int m, int n, double l, double tem_avg, double tem_std, double TZ,
                      unsigned long long seed, double *out);
 int stzo_threads(void);
+void stzo_set_threads(int k);
 
 #ifdef __cplusplus
 }

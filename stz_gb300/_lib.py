@@ -21,11 +21,14 @@ FP64 = 0
 MIXED = 1
 TOL_REFERENCE = 0
 TOL_RELATIVE = 1
+ADV_AUTO = 0
+ADV_FP64 = 1
+ADV_SPLIT = 2
 
 # Every symbol include/stzg.h declares.
 EXPORTS = [
     "stzg_default_options", "stzg_strerror", "stzg_last_message", "stzg_create", "stzg_destroy",
-    "stzg_set_state", "stzg_set_field", "stzg_get_field", "stzg_set_time", "stzg_get_time",
+    "stzg_set_state", "stzg_init_fields", "stzg_chi_bicubic", "stzg_set_field", "stzg_get_field", "stzg_set_time", "stzg_get_time",
     "stzg_step_qs", "stzg_advection_step", "stzg_projection_step", "stzg_avg_iters",
     "stzg_mg_solve", "stzg_mg_vcycle", "stzg_mg_l2_error", "stzg_mg_levels", "stzg_mg_stencil",
     "stzg_l2_comparison", "stzg_random_chi", "stzg_upload", "stzg_download", "stzg_time_kernel",
@@ -43,7 +46,7 @@ class StzgOptions(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("tol_mode", ctypes.c_int), ("tol", ctypes.c_double),
                 ("track_plastic", ctypes.c_int), ("device", ctypes.c_int), ("inner_cycles", ctypes.c_int),
                 ("use_graphs", ctypes.c_int), ("extrapolate", ctypes.c_int),
-                ("substep_cap", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("substep_cap", ctypes.c_int), ("advection", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class StzgStats(ctypes.Structure):
@@ -94,6 +97,8 @@ def load(path=None):
         "stzg_create": (I, [ctypes.POINTER(StzParams), ctypes.POINTER(StzgOptions), ctypes.POINTER(V)]),
         "stzg_destroy": (I, [V]),
         "stzg_set_state": (I, [V, _P]),
+        "stzg_init_fields": (I, [V, I, D, D]),
+        "stzg_chi_bicubic": (I, [V, I, I, _P, D, D]),
         "stzg_set_field": (I, [V, I, _P]),
         "stzg_get_field": (I, [V, I, _P]),
         "stzg_set_time": (I, [V, D]),

@@ -39,6 +39,12 @@ using namespace stzg;
 #include "sim.cuh"
 
 namespace stzg {
+// Host set-ups of chi (chi_init.cpp).
+void init_fields_chi(const stz_params &p, int chi_case, double tem_base, double tem_delta, double *chi);
+void bicubic_chi(const stz_params &p, int mm, int nn, const double *arr, double lo, double sca, double *chi);
+}  // namespace stzg
+
+namespace stzg {
 
 int dev_alloc(stzg_sim *s, void **p, size_t bytes) {
     cudaError_t e = cudaMalloc(p, bytes);
@@ -66,8 +72,8 @@ int validate(const stz_params *p) {
 }
 
 void drop_graphs(stzg_sim *s) {
-    cudaGraphExec_t *g[3] = {&s->g_vc64, &s->g_res32, &s->g_pass32};
-    for (int k = 0; k < 3; k++)
+    cudaGraphExec_t *g[4] = {&s->g_vc64, &s->g_res32, &s->g_pass32, &s->g_loop};
+    for (int k = 0; k < 4; k++)
         if (*g[k]) {
             cudaGraphExecDestroy(*g[k]);
             *g[k] = nullptr;
@@ -258,7 +264,176 @@ int solve_mixed(stzg_sim *s, int *ncyc) {
     return STZG_OK;
 }
 
+// Relative-tolerance solves keep their convergence loop on the device: a
+// WHILE graph node runs one pass (mixed: `inner` FP32 V-cycles, the
+// float-float correction and residual; FP64: one V-cycle and the residual
+// norm) per iteration until ||r|| <= tol ||b||, so the host neither predicts
+// a cycle count nor waits for a check between passes.  The initial residual
+// is tested first: a warm start that already meets the tolerance runs no
+// pass.  A pass cap (the tgmg_predict threshold, tgmg_config.hh:26-45, in
+// V-cycles) ends a solve that does not converge, with an error flag.
+__global__ void k_loop_start(const double *dnorm, int *flags, double tol2, cudaGraphConditionalHandle h) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double r2 = dnorm[0], b2 = dnorm[1];
+        const bool conv = b2 > 0 ? r2 <= tol2 * b2 : r2 == 0;
+        const bool nan = isnan(r2);
+        flags[FL_PASSES] = 0;
+        flags[FL_LOOP_ERR] = nan ? 2 : 0;
+        cudaGraphSetConditional(h, (!conv && !nan) ? 1u : 0u);
+    }
+}
+
+__global__ void k_loop_check(const double *dnorm, int *flags, double tol2, int cap, cudaGraphConditionalHandle h) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double r2 = dnorm[0], b2 = dnorm[1];
+        const bool conv = b2 > 0 ? r2 <= tol2 * b2 : r2 == 0;
+        const bool nan = isnan(r2);
+        const int it = ++flags[FL_PASSES];
+        if (nan) flags[FL_LOOP_ERR] = 2;
+        else if (!conv && it >= cap) flags[FL_LOOP_ERR] = 1;
+        cudaGraphSetConditional(h, (!conv && !nan && it < cap) ? 1u : 0u);
+    }
+}
+
+static int loop_cap(const stzg_sim *s, int per_pass) {
+    return std::max(1, s->max_thresh / s->mult / per_pass);
+}
+
+// Ends a capture that failed half-way, so the stream is usable again.
+static int abandon_capture(stzg_sim *s, int status) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(s->st, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return status;
+}
+
+static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
+    if (s->g_loop && s->g_loop_inner == inner) return STZG_OK;
+    if (s->g_loop) {
+        cudaGraphExecDestroy(s->g_loop);
+        s->g_loop = nullptr;
+    }
+    const long count = (long)s->m * (s->n + 1);
+    const double tol2 = s->O.tol * s->O.tol;
+    const int per_pass = mixed ? inner : 1;
+    cudaGraph_t root = nullptr;
+    STZG_CUDA(cudaGraphCreate(&root, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, root, 0, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(root);
+        return cuda_fail(e, "cudaGraphConditionalHandleCreate");
+    }
+    cudaGraphNodeParams wp = {};
+    int st = STZG_OK;
+    const long c0 = launch_count();
+    e = cudaStreamBeginCaptureToGraph(s->st, root, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(root);
+        return cuda_fail(e, "cudaStreamBeginCaptureToGraph");
+    }
+    // set-up: initial residual of the warm start, then the loop and the finish
+    if (mixed) mixed_begin(s);
+    launch_norms(s, mixed);
+    k_loop_start<<<1, 32, 0, s->st>>>(s->dnorm, s->F.flags, tol2, h);
+    note_launch();
+    {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t cg;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t ndeps = 0;
+        e = cudaStreamGetCaptureInfo(s->st, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+        cudaGraphNode_t wnode;
+        if (e == cudaSuccess) {
+            wp.type = cudaGraphNodeTypeConditional;
+            wp.conditional.handle = h;
+            wp.conditional.type = cudaGraphCondTypeWhile;
+            wp.conditional.size = 1;
+            e = cudaGraphAddNode(&wnode, cg, deps, nullptr, ndeps, &wp);
+        }
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(s->st, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) st = cuda_fail(e, "conditional node");
+    }
+    if (st != STZG_OK) {
+        cudaGraphDestroy(root);
+        return abandon_capture(s, st);
+    }
+    if (mixed) mixed_end(s);
+    else
+        for (int c = 0; c < s->extra_iters; c++) vcycle<double>(s->h64, s->st, 10, 1);
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(s->st, &got);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(root);
+        return cuda_fail(e, "cudaStreamEndCapture");
+    }
+    const long c1 = launch_count();
+    // loop body: one pass and the convergence test
+    e = cudaStreamBeginCaptureToGraph(s->st, wp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(root);
+        return cuda_fail(e, "cudaStreamBeginCaptureToGraph(body)");
+    }
+    if (mixed) {
+        for (int c = 0; c < inner; c++) vcycle<float>(s->h32, s->st, 10, 1, c == 0);
+        ff_correct(s->zhi, s->zlo, s->h32.lv[0].z, count, s->st);
+    } else {
+        vcycle<double>(s->h64, s->st, 10, 1);
+    }
+    launch_norms(s, mixed);
+    k_loop_check<<<1, 32, 0, s->st>>>(s->dnorm, s->F.flags, tol2, loop_cap(s, per_pass), h);
+    note_launch();
+    e = cudaStreamEndCapture(s->st, &got);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(root);
+        return cuda_fail(e, "cudaStreamEndCapture(body)");
+    }
+    const long c2 = launch_count();
+    discount_launches(c2 - c0);  // graph nodes, counted when they execute
+    s->n_loop_outer = c1 - c0;
+    s->n_loop_body = c2 - c1;
+    e = cudaGraphInstantiate(&s->g_loop, root, 0);
+    cudaGraphDestroy(root);
+    if (e != cudaSuccess) {
+        s->g_loop = nullptr;
+        return cuda_fail(e, "cudaGraphInstantiate(solve loop)");
+    }
+    s->g_loop_inner = inner;
+    return STZG_OK;
+}
+
+static int solve_device_loop(stzg_sim *s, int *ncyc) {
+    const bool mixed = s->O.precision == STZG_MIXED;
+    const int inner = mixed ? (s->O.inner_cycles > 0 ? s->O.inner_cycles : 3) : 1;
+    STZG_CHECK(build_loop_graph(s, mixed, inner));
+    STZG_CUDA(cudaGraphLaunch(s->g_loop, s->st));
+    STZG_CUDA(cudaMemcpyAsync(s->hflags, s->F.flags, FL_COUNT * sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaMemcpyAsync(s->hnorm, s->dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    const int passes = s->hflags[FL_PASSES], err = s->hflags[FL_LOOP_ERR];
+    g_launches.fetch_add(s->n_loop_outer + passes * s->n_loop_body);
+    const double r2 = s->hnorm[0], b2 = s->hnorm[1];
+    s->acc.checks += passes + 1;
+    s->acc.last_error = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    if (err == 2) return fail(STZG_ENAN, "NaN residual");
+    if (err == 1) return fail(STZG_ENOTCONV, mixed ? "iterative refinement did not converge"
+                                                   : "multigrid did not converge");
+    const int cycles = passes * inner;
+    s->acc.vcycles += cycles;
+    if (mixed) s->acc.refinements += passes;
+    else s->acc.extra_vcycles += s->extra_iters;
+    s->acc.solves++;
+    s->avg_vcount += cycles;
+    s->avg_solves++;
+    if (ncyc) *ncyc = cycles;
+    return STZG_OK;
+}
+
 int solve(stzg_sim *s, int *ncyc) {
+    if (s->O.tol_mode == STZG_TOL_RELATIVE && s->O.use_graphs) return solve_device_loop(s, ncyc);
     return s->O.precision == STZG_MIXED ? solve_mixed(s, ncyc) : solve_fp64(s, ncyc);
 }
 
@@ -296,12 +471,14 @@ int do_advection(stzg_sim *s, double dt) {
 }
 
 int check_flags(stzg_sim *s) {
-    int h[4];
-    STZG_CUDA(cudaMemcpyAsync(h, s->F.flags, sizeof(h), cudaMemcpyDeviceToHost, s->st));
+    int *h = s->hflags;
+    STZG_CUDA(cudaMemcpyAsync(h, s->F.flags, FL_COUNT * sizeof(int), cudaMemcpyDeviceToHost, s->st));
     STZG_CUDA(cudaStreamSynchronize(s->st));
-    if (h[1] > s->acc.substeps_max) s->acc.substeps_max = h[1];
-    if (h[3]) return fail(STZG_ECUDA, "an advection tile copy did not complete in time");
-    if (h[0]) return fail(STZG_ESUBSTEP, "plastic sub-stepping reached its iteration cap");
+    if (h[FL_SUBSTEP_MAX] > s->acc.substeps_max) s->acc.substeps_max = h[FL_SUBSTEP_MAX];
+    if (h[FL_TMA])
+        return fail(STZG_ECUDA, "an advection tile copy did not complete in time; tiles of the step were "
+                                "left unwritten, so the handle's state is undefined: recreate the handle");
+    if (h[FL_SUBSTEP_CAP]) return fail(STZG_ESUBSTEP, "plastic sub-stepping reached its iteration cap");
     return STZG_OK;
 }
 
@@ -358,6 +535,7 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     s->n = p->n;
     s->sc = make_step_consts(*p);
     s->sc.track_plastic = o.track_plastic;
+    s->sc.sp_increments = o.precision == STZG_MIXED && o.advection == STZG_ADV_SPLIT;
     if (o.substep_cap > 0) s->sc.substep_cap = o.substep_cap;
     int st = STZG_OK;
     auto bail = [&](int code) {
@@ -375,7 +553,7 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if ((st = dev_alloc(s, (void **)&s->F.eps_pl, (size_t)s->m * s->n * sizeof(double))) != STZG_OK) return bail(st);
     if ((st = dev_alloc(s, (void **)&s->F.vel, nn * sizeof(double2))) != STZG_OK) return bail(st);
     if ((st = dev_alloc(s, (void **)&s->F.src, nn * sizeof(double2))) != STZG_OK) return bail(st);
-    if ((st = dev_alloc(s, (void **)&s->F.flags, 4 * sizeof(int))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->F.flags, FL_COUNT * sizeof(int))) != STZG_OK) return bail(st);
     for (int k = 0; k < 4; k++)
         if ((st = dev_alloc(s, (void **)&s->F.pre[k], nc * sizeof(double))) != STZG_OK) return bail(st);
     s->maps = new field_maps;
@@ -388,6 +566,8 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if ((st = dev_alloc(s, (void **)&s->partials, 2 * s->npart * sizeof(double))) != STZG_OK) return bail(st);
     if ((st = dev_alloc(s, (void **)&s->dnorm, 2 * sizeof(double))) != STZG_OK) return bail(st);
     if (cudaMallocHost(&s->hnorm, 2 * sizeof(double)) != cudaSuccess) return bail(fail(STZG_ENOMEM, "pinned alloc"));
+    if (cudaMallocHost(&s->hflags, FL_COUNT * sizeof(int)) != cudaSuccess)
+        return bail(fail(STZG_ENOMEM, "pinned alloc"));
     // FP64 hierarchy over vel/src; FP32 hierarchy with its own top arrays
     if ((st = s->h64.allocate(s->m, s->n + 1, s->F.vel, s->F.src)) != STZG_OK) return bail(st);
     if (o.precision == STZG_MIXED) {
@@ -418,6 +598,7 @@ int stzg_destroy(stzg_sim *s) {
     s->h64.release();
     s->h32.release();
     if (s->hnorm) cudaFreeHost(s->hnorm);
+    if (s->hflags) cudaFreeHost(s->hflags);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->st) cudaStreamDestroy(s->st);
@@ -452,7 +633,7 @@ int stzg_set_state(stzg_sim *s, const double *chi) {
     STZG_CUDA(cudaMemsetAsync(s->F.ddev, 0, nc * 8, s->st));
     STZG_CUDA(cudaMemsetAsync(s->F.eps_pl, 0, (size_t)m * n * 8, s->st));
     STZG_CUDA(cudaMemsetAsync(s->F.vel, 0, (size_t)m * (n + 1) * sizeof(double2), s->st));
-    STZG_CUDA(cudaMemsetAsync(s->F.flags, 0, 4 * sizeof(int), s->st));
+    STZG_CUDA(cudaMemsetAsync(s->F.flags, 0, FL_COUNT * sizeof(int), s->st));
     STZG_CUDA(cudaStreamSynchronize(s->st));
     s->time = 0;
     s->bv_state = 0;
@@ -544,6 +725,23 @@ int stzg_set_field(stzg_sim *s, int field, const double *host) {
         STZG_CUDA(cudaMemcpy(dst, host, cnt * 8, cudaMemcpyHostToDevice));
     }
     return STZG_OK;
+}
+
+int stzg_init_fields(stzg_sim *s, int chi_case, double tem_base, double tem_delta) {
+    if (!s) return fail(STZG_EINVAL, "null handle");
+    const int m = s->m, n = s->n;
+    std::vector<double> full((size_t)m * (n + 2));
+    init_fields_chi(s->P, chi_case, tem_base, tem_delta, full.data());
+    STZG_CHECK(stzg_set_state(s, full.data() + m));
+    return stzg_set_field(s, STZG_CHI, full.data());  // the formula's own ghost rows
+}
+
+int stzg_chi_bicubic(stzg_sim *s, int mm, int nn, const double *arr, double lo, double sca) {
+    if (!s || !arr) return fail(STZG_EINVAL, "null argument");
+    if (mm < 1 || nn < 2) return fail(STZG_EINVAL, "the sample grid needs mm >= 1 and nn >= 2");
+    std::vector<double> chi((size_t)s->m * s->n);
+    bicubic_chi(s->P, mm, nn, arr, lo, sca, chi.data());
+    return stzg_set_state(s, chi.data());
 }
 
 int stzg_set_time(stzg_sim *s, double t) {
@@ -723,7 +921,16 @@ int stzg_step_qs_host(stzg_sim *s, double dt, const double *const *up, double *c
     }
     if (down[8]) early.push_back({down[8], s->F.eps_pl, (size_t)m * n * 8});
     STZG_CHECK(enqueue_copies(s, early, cudaMemcpyDeviceToHost));
-    STZG_CHECK(do_projection(s, dt, true));
+    {
+        // on failure, the copies already queued into the caller's buffers
+        // finish before the call returns
+        const int st = do_projection(s, dt, true);
+        if (st != STZG_OK) {
+            join_copies(s);
+            cudaStreamSynchronize(s->st);
+            return st;
+        }
+    }
     for (int k = 0; k < F_CHI; k++)
         if (down[k]) late.push_back({down[k], f[k], nc * 8});
     if (down[7]) late.push_back({down[7], s->F.vel, nn * sizeof(double2)});

@@ -78,3 +78,107 @@ extern "C" int stzg_random_chi(int m, int n, double l, double tem_avg, double te
         }
     return STZG_OK;
 }
+
+namespace stzg {
+
+// chi of shear_sim::init_fields (esim/sb/main/shear_sim.cc:60-114) at the
+// cell centres of rows -1..n (m*(n+2), row j at offset (j+1)m): case 0 a
+// Gaussian blip at the origin, case 1 a line rotated by 30 degrees (wrapped
+// back into |x_r| <= 1), any other case sixteen blips on a sine wave (the
+// nearest one, x-periodic); each of width exp(-200 r^2) over tem_base.
+void init_fields_chi(const stz_params &p, int chi_case, double tem_base, double tem_delta, double *chi) {
+    const double pi = 3.1415926535897932384626433832795;
+    const int m = p.m, n = p.n;
+    const double lx = p.bx - p.ax, dx = lx / m, dy = (p.by - p.ay) / n;
+    const double c0 = tem_base / p.TZ, c1 = tem_delta / p.TZ;
+    double bx_[16], by_[16];
+    for (int k = 0; k < 16; k++) {
+        bx_[k] = p.ax + lx * (k + 0.5) * 0.0625;
+        by_[k] = -0.2 * std::sin(pi * 0.0625 * (2 * k + 1));
+    }
+    const double ca = std::cos(30 * pi / 180.), sa = std::sin(30 * pi / 180.);
+#pragma omp parallel for schedule(static)
+    for (int j = -1; j <= n; j++) {
+        const double yc = (p.ay + j * dy) + 0.5 * dy;
+        for (int i = 0; i < m; i++) {
+            const double xc = (p.ax + i * dx) + 0.5 * dx;
+            double r2;
+            if (chi_case == 0) {
+                r2 = xc * xc + yc * yc;
+            } else if (chi_case == 1) {
+                double u = ca * xc + sa * yc;
+                const double w = -sa * xc + ca * yc;
+                u = u < -1 ? u + 1 : (u > 1 ? u - 1 : 0);
+                r2 = u * u + w * w;
+            } else {
+                r2 = 1e100;
+                for (int k = 0; k < 16; k++) {
+                    double u = bx_[k] - xc;
+                    if (u < -lx * 0.5) u += lx;
+                    if (u > lx * 0.5) u -= lx;
+                    const double w = by_[k] - yc, t = u * u + w * w;
+                    if (t < r2) r2 = t;
+                }
+            }
+            chi[(size_t)(j + 1) * m + i] = c0 + c1 * std::exp(-200 * r2);
+        }
+    }
+}
+
+// chi of shear_sim::initialize_chi_bicubic (shear_sim.cc:832-909) on rows
+// 0..n-1 (m*n): lo + sca times the bicubic Hermite interpolant of arr
+// (mm x nn samples spanning the domain, periodic in x) whose derivatives are
+// centred differences (one-sided on the first and last sample rows).
+void bicubic_chi(const stz_params &p, int mm, int nn, const double *arr, double lo, double sca, double *chi) {
+    const int m = p.m, n = p.n;
+    const size_t cnt = (size_t)mm * nn;
+    std::vector<double> dxa(cnt), dya(cnt), dxya(cnt);
+    for (int j = 0; j < nn; j++)
+        for (int i = 0; i < mm; i++) {
+            const size_t c = (size_t)j * mm;
+            dxa[c + i] = 0.5 * (arr[c + (i == mm - 1 ? 0 : i + 1)] - arr[c + (i == 0 ? mm - 1 : i - 1)]);
+        }
+    for (int j = 0; j < nn; j++)
+        for (int i = 0; i < mm; i++) {
+            const size_t c = (size_t)j * mm + i;
+            if (j == 0) {
+                dya[c] = arr[c + mm] - arr[c];
+                dxya[c] = dxa[c + mm] - dxa[c];
+            } else if (j == nn - 1) {
+                dya[c] = arr[c] - arr[c - mm];
+                dxya[c] = dxa[c] - dxa[c - mm];
+            } else {
+                dya[c] = 0.5 * (arr[c + mm] - arr[c - mm]);
+                dxya[c] = 0.5 * (dxa[c + mm] - dxa[c - mm]);
+            }
+        }
+    const double dx = (p.bx - p.ax) / m, dy = (p.by - p.ay) / n;
+    const double xs = dx * mm / (p.bx - p.ax), ys = dy * nn / (p.by - p.ay);
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < n; j++) {
+        double t = (j + 0.5) * ys - 0.5;
+        int jj = (int)t;
+        jj = jj < 0 ? 0 : (jj > nn - 2 ? nn - 2 : jj);
+        t -= jj;
+        const double u = 1 - t;
+        // Hermite weights: slope at 0, value at 0, value at 1, slope at 1
+        const double w0 = t * u * u, w1 = u * u * (1 + 2 * t), w2 = t * t * (3 - 2 * t), w3 = -t * t * u;
+        for (int i = 0; i < m; i++) {
+            double s = (i + 0.5) * xs - 0.5;
+            if (s < 0) s += mm;
+            int ii = (int)s;
+            if (ii >= mm) ii -= mm;
+            const size_t a = (size_t)jj * mm + ii, b = (size_t)jj * mm + (ii == mm - 1 ? 0 : ii + 1);
+            s -= ii;
+            const double v = 1 - s;
+            const double h0 = s * v * v, h1 = v * v * (1 + 2 * s), h2 = s * s * (3 - 2 * s), h3 = -s * s * v;
+            const double r0 = dxya[a] * h0 + dya[a] * h1 + dya[b] * h2 + dxya[b] * h3;
+            const double r1 = dxa[a] * h0 + arr[a] * h1 + arr[b] * h2 + dxa[b] * h3;
+            const double r2 = dxa[a + mm] * h0 + arr[a + mm] * h1 + arr[b + mm] * h2 + dxa[b + mm] * h3;
+            const double r3 = dxya[a + mm] * h0 + dya[a + mm] * h1 + dya[b + mm] * h2 + dxya[b + mm] * h3;
+            chi[(size_t)j * m + i] = lo + sca * (w0 * r0 + w1 * r1 + w2 * r2 + w3 * r3);
+        }
+    }
+}
+
+}  // namespace stzg

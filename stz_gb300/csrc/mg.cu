@@ -1,6 +1,7 @@
 // Multigrid kernels and hierarchy set-up (see mg.cuh for the design).
 #include "mg.cuh"
 #include "mg_device.cuh"
+#include "ff.cuh"
 #include "transfer1d.cuh"
 
 #include <algorithm>
@@ -733,77 +734,6 @@ __global__ void k_extrapolate(double2 *__restrict__ z, double2 *__restrict__ pre
 // by ~2^-44 (|x| + |y|): the residual's error is then ~1e-13 |b|, three
 // orders below the 1e-10 stopping tolerance, while the FP32 value handed to
 // the V-cycles needs only single precision.
-
-struct ff {
-    float hi, lo;
-};
-
-__device__ __forceinline__ ff ff_fast2sum(float a, float b) {
-    const float s = a + b;
-    return ff{s, b - (s - a)};
-}
-__device__ __forceinline__ ff ff_add(ff a, ff b) {
-    const float s = a.hi + b.hi, bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b.hi - bb);
-    e += a.lo + b.lo;
-    return ff_fast2sum(s, e);
-}
-__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
-__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
-__device__ __forceinline__ ff ff_mul(ff a, ff b) {
-    const float p = a.hi * b.hi;
-    float e = fmaf(a.hi, b.hi, -p);
-    e = fmaf(a.hi, b.lo, e);
-    e = fmaf(a.lo, b.hi, e);
-    return ff_fast2sum(p, e);
-}
-__device__ __forceinline__ ff ff_add_f(ff a, float b) {
-    const float s = a.hi + b, bb = s - a.hi;
-    float e = (a.hi - (s - bb)) + (b - bb);
-    e += a.lo;
-    return ff_fast2sum(s, e);
-}
-
-// double -> hi + lo on the integer pipe: hi keeps the sign, the exponent and
-// the leading 24 significant bits, lo the remaining 29 bits rounded to a
-// float.  |d| below 2^-126 gives 0; below 2^-74 lo is dropped (an absolute
-// error under 2^-98).  NaN and infinity pass through in hi.
-__device__ __forceinline__ void ff_split_d(double d, float &hi, float &lo) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
-    const unsigned sign = (unsigned)(u >> 63) << 31;
-    const int ex = (int)((u >> 52) & 0x7ff);
-    const int ef = ex - 1023 + 127;
-    lo = 0.f;
-    if (ex == 0x7ff) {
-        hi = (u & 0xfffffffffffffull) ? __uint_as_float(0x7fc00000u) : __uint_as_float(sign | 0x7f800000u);
-        return;
-    }
-    if (ef <= 0) {
-        hi = __uint_as_float(sign);
-        return;
-    }
-    if (ef >= 255) {
-        hi = __uint_as_float(sign | 0x7f800000u);
-        return;
-    }
-    hi = __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)((u >> 29) & 0x7fffffu));
-    const int es = ex - 1075 + 127;  // float exponent field of 2^(ex - 1075)
-    if (es > 0) {
-        const float r = __uint2float_rn((unsigned)(u & 0x1fffffffu)) * __uint_as_float((unsigned)es << 23);
-        lo = sign ? -r : r;
-    }
-}
-
-// float -> double on the integer pipe (exact for normal floats; zero and
-// subnormal floats give a signed zero, infinity and NaN convert normally).
-__device__ __forceinline__ double ff_f2d(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xff;
-    if (e == 255) return (double)f;
-    unsigned long long r = (unsigned long long)(u >> 31) << 63;
-    if (e != 0) r |= ((unsigned long long)(e - 127 + 1023) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)r);
-}
 
 __global__ void k_ff_split(const double2 *__restrict__ a, float2 *__restrict__ hi, float2 *__restrict__ lo,
                            const double2 *__restrict__ a2, float2 *__restrict__ hi2, float2 *__restrict__ lo2,

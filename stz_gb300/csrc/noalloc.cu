@@ -19,6 +19,12 @@
 // All calls share the array: calls whose kernels overlap on the GPU (two
 // streams, or two host threads without ordering) race on it.  Each call
 // writes every partial it reads, so nothing has to be cleared between calls.
+//
+// The array's device address is looked up once per device, on the first
+// call made with that device current, and kept for the life of the process;
+// a cudaDeviceReset while the library is loaded invalidates it (as it does
+// every handle of this library), so callers must not reset a device they
+// keep using through it.
 #include <mutex>
 
 #include "mg.cuh"

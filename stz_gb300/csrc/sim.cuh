@@ -40,6 +40,13 @@ struct stzg_sim {
     cudaGraphExec_t g_vc64 = nullptr, g_res32 = nullptr, g_pass32 = nullptr;
     long n_vc64 = 0, n_res32 = 0, n_pass32 = 0;  // kernel nodes per graph
     int g_inner = 0;
+    // relative-tolerance solve with its convergence loop on the device: one
+    // graph (set-up, WHILE node over passes, finish); kernel nodes outside
+    // and inside the loop body
+    cudaGraphExec_t g_loop = nullptr;
+    long n_loop_outer = 0, n_loop_body = 0;
+    int g_loop_inner = 0;
+    int *hflags = nullptr;  // pinned host copy of F.flags (FL_COUNT ints)
     double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)
     double2 *vel_prev2 = nullptr; // the one before (quadratic extrapolation)
     bool have_prev2 = false;

@@ -1,5 +1,6 @@
 // Time-step kernels: fused ENO advection + STZ plasticity, chi diffusion,
 // projection source, stress correction and boundaries.
+#include "ff.cuh"
 #include "step.cuh"
 #include "stz_law.cuh"
 
@@ -39,6 +40,7 @@ step_consts make_step_consts(const stz_params &p) {
     c.yield_cut2 = p.s_y * p.s_y * (1 - 1e-12);
     c.clock = nullptr;
     c.xbc = 0;
+    c.sp_increments = 0;
     return c;
 }
 
@@ -191,7 +193,7 @@ __device__ __forceinline__ double tile_eno_y(const eno_tile<NF> &T, int f, int t
 constexpr int AROWS = ATY + 4;
 constexpr unsigned kTileBytes = F_COUNT * AROWS * ACOLS * sizeof(double);
 // Iterations of the bounded wait on the tile copies (each try_wait itself
-// suspends for a while); past it the block flags F.flags[3].
+// suspends for a while); past it the block flags F.flags[FL_TMA].
 constexpr int kTmaWaitIters = 1 << 20;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -267,9 +269,12 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
         mbar_expect_tx(&Sm.bar, kTileBytes);
         for (int f = 0; f < F_COUNT; f++) tma_load_2d(&Sm.tile[f][0][0], &maps.f[cur][f], i0 - 2, j0 - 1, &Sm.bar);
     }
-    if (!mbar_wait_bounded(&Sm.bar)) {
-        if (tid == 0) atomicExch(&F.flags[3], 1);
-        mbar_wait_bounded(&Sm.bar);  // the copies in flight, once more, then go on with what is there
+    if (__syncthreads_or(!mbar_wait_bounded(&Sm.bar))) {
+        // a copy did not arrive in time: flag it, wait once more for the
+        // copies in flight, and leave this tile of the next state unwritten
+        if (tid == 0) atomicExch(&F.flags[FL_TMA], 1);
+        mbar_wait_bounded(&Sm.bar);
+        return;
     }
     // Columns across the periodic seam arrive as zeros: blocks at either end
     // fetch them from their wrapped columns.
@@ -356,6 +361,272 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
         qn = q + fma(-vh, f2[1], -uh * f1[1]);
         sn = s + (fma(-vh, f2[2], -uh * f1[2]) + two_omega * t);
         tn = t + (fma(-vh, f2[3], -uh * f1[3]) - two_omega * s);
+    }
+    B[F_P][ci] = pn;
+    B[F_Q][ci] = qn;
+    B[F_S][ci] = sn;
+    B[F_TAU][ci] = tn;
+    if (emit_source) {
+        const double pq = pn + qn, Aa = pq - sn, Bb = pq + sn;
+        F.pre[0][ci] = a.xf * Aa + a.yf * tn;
+        F.pre[1][ci] = a.xf * Aa - a.yf * tn;
+        F.pre[2][ci] = a.xf * tn - a.yf * Bb;
+        F.pre[3][ci] = a.xf * tn + a.yf * Bb;
+    }
+}
+
+// ---- single-precision increments (mixed-precision handles) ------------------
+// The same step with the ENO differences and the advective increments in
+// FP32 while the state stays FP64: every staged value is split on the
+// integer pipe into a float pair hi + lo (ff_split_d), each first difference
+// f(c+1) - f(c) is formed from the pairs by TwoSum (ff_diff: the float
+// rounding of the exact difference, however close the two values are), and
+// the second differences, the ENO choice and value, the upwind products and
+// the rotation term run in FP32 (with an exact FP64 tie-break of the ENO
+// choice, below).  Each field then takes its increment with
+// one FP64 addition, so the state carries no FP32 rounding of its own, only
+// that of the increment (relative 2^-24 of a change that is itself a small
+// part of the field per step).  The velocity differences of the spin come
+// from FP64 subtractions; the plastic law, the stress norm of the yield test
+// and the net-force combinations stay FP64.  On GB300, where FP64 issues at
+// 1/57 of the FP32 rate, this takes the kernel off the FP64 pipe.
+struct eno_tile_sp {
+    float th[F_COUNT][AROWS][ACOLS];  // hi / lo parts of the staged values (X unwrapped)
+    float tl[F_COUNT][AROWS][ACOLS];
+    float dx[F_COUNT][ATY][ADXW];
+    float dy[F_COUNT][ADYH][ATX];
+    float sx[F_COUNT][ATY][ASXW];
+    float sy[F_COUNT][ASYH][ATX];
+    double xo[ACOLS];
+    int col[ACOLS];
+};
+
+struct adv_smem_sp {
+    double tile[F_COUNT][AROWS][ACOLS];  // staged fields, first: 128-byte aligned
+    eno_tile_sp T;
+    uint64_t bar;
+};
+
+__device__ __forceinline__ bool mag_gtf(float a, float b) {
+    return (__float_as_uint(a) & 0x7fffffffu) > (__float_as_uint(b) & 0x7fffffffu);
+}
+// The ENO choice |S(i)| > |S(i-1)| (or |S(i+1)|) is taken in FP32 where the
+// two magnitudes differ by more than the FP32 differences' error bound;
+// otherwise (rare: near ties) it is recomputed in FP64 from the staged tile
+// with k_advect's operations, so the choice always equals the FP64 path's.
+// A different choice would change the ENO value by the difference of the
+// two second differences, which near an inflection is not small.
+// Bound on |s_f - s| for the FP32 second differences of three first
+// differences a, b, c (each within ~2^-24 of its value plus ~2^-47 of the
+// values differenced): generous by a factor of ~16.
+__device__ __forceinline__ float tie_margin(float a, float b, float c, float vmag) {
+    return 1e-6f * (fabsf(a) + 2.f * fabsf(b) + fabsf(c)) + 1e-13f * vmag;
+}
+// FP64 choice of k_advect in x (tile_differences with the X column
+// offsets, then eno_left / eno_right's magnitude test).
+__device__ __noinline__ bool pick_x64(const double (*tile)[AROWS][ACOLS], const double *xo, int f, int ty, int tx,
+                                      bool from_left) {
+    const int r = ty + 2, c0 = from_left ? tx : tx + 1;  // tile columns c0 .. c0+3
+    double g[4];
+    for (int q = 0; q < 4; q++) {
+        g[q] = tile[f][r][c0 + q];
+        if (f == F_X && xo[c0 + q] != 0) g[q] += xo[c0 + q];
+    }
+    const double da = g[1] - g[0], db = g[2] - g[1], dc = g[3] - g[2];
+    // from the left: s0 = S(i) = dc - db, s1 = S(i-1) = db - da;
+    // from the right: s0 = S(i) = db - da, s1 = S(i+1) = dc - db
+    return from_left ? mag_gt(dc - db, db - da) : mag_gt(db - da, dc - db);
+}
+// FP64 choice in y (rows j0+r-2 .. j0+r-1 for difference r, zero where k_advect's
+// tile_differences leaves it zero).
+__device__ __noinline__ bool pick_y64(const double (*tile)[AROWS][ACOLS], int f, int ty, int tx, bool from_below,
+                                      int j0, int n) {
+    const int r0 = from_below ? ty : ty + 1;  // differences r0 .. r0+2
+    double d[3];
+    for (int q = 0; q < 3; q++) {
+        const int r = r0 + q, jj = j0 + r - 2;
+        d[q] = (jj >= -1 && jj + 1 <= n) ? tile[f][r + 1][tx + 2] - tile[f][r][tx + 2] : 0.0;
+    }
+    // from below: s0 = S(j) = d2 - d1, s1 = S(j-1) = d1 - d0;
+    // from above: s0 = S(j) = d1 - d0, s1 = S(j+1) = d2 - d1
+    return from_below ? mag_gt(d[2] - d[1], d[1] - d[0]) : mag_gt(d[1] - d[0], d[2] - d[1]);
+}
+__device__ __forceinline__ float eno_x_sp(const adv_smem_sp &Sm, int f, int ty, int tx, bool from_left) {
+    const eno_tile_sp &T = Sm.T;
+    const float *d = T.dx[f][ty], *s = T.sx[f][ty];
+    const int k = tx + 1;
+    const int k1 = from_left ? k - 1 : k + 1;
+    const float s0 = s[k], s1 = s[k1];
+    const float gap = fabsf(fabsf(s0) - fabsf(s1));
+    const int ca = from_left ? k - 1 : k;  // first of the three differences
+    const float *h = T.th[f][ty + 2];
+    const float vmag = fabsf(h[ca]) + fabsf(h[ca + 1]) + fabsf(h[ca + 2]) + fabsf(h[ca + 3]);
+    bool outer;
+    if (gap > tie_margin(d[ca], d[ca + 1], d[ca + 2], vmag)) outer = mag_gtf(s0, s1);
+    else outer = pick_x64(Sm.tile, T.xo, f, ty, tx, from_left);
+    const float sv = outer ? s1 : s0;
+    return from_left ? fmaf(2.f, d[k], sv) : fmaf(-2.f, d[k + 1], sv);
+}
+__device__ __forceinline__ float eno_y_sp(const adv_smem_sp &Sm, int f, int ty, int tx, bool from_below, bool inner,
+                                          int j0, int n) {
+    const eno_tile_sp &T = Sm.T;
+    const int ky = ty + 1;
+    const float s0 = T.sy[f][ky][tx];
+    const float dn = from_below ? T.dy[f][ky][tx] : T.dy[f][ky + 1][tx];
+    if (!inner) return from_below ? 2.f * dn : -2.f * dn;
+    const float s1 = from_below ? T.sy[f][ky - 1][tx] : T.sy[f][ky + 1][tx];
+    const int ra = from_below ? ty : ty + 1;  // first of the three differences
+    const float gap = fabsf(fabsf(s0) - fabsf(s1));
+    const float vmag = fabsf(T.th[f][ra][tx + 2]) + fabsf(T.th[f][ra + 1][tx + 2]) + fabsf(T.th[f][ra + 2][tx + 2]) +
+                       fabsf(T.th[f][ra + 3][tx + 2]);
+    bool outer;
+    if (gap > tie_margin(T.dy[f][ra][tx], T.dy[f][ra + 1][tx], T.dy[f][ra + 2][tx], vmag)) outer = mag_gtf(s0, s1);
+    else outer = pick_y64(Sm.tile, f, ty, tx, from_below, j0, n);
+    const float sv = outer ? s1 : s0;
+    return from_below ? fmaf(2.f, dn, sv) : fmaf(-2.f, dn, sv);
+}
+// a + b for the FP64 state value a and its FP32 increment b (one FP64 add).
+__device__ __forceinline__ double add_inc(double a, float b) { return a + ff_f2d(b); }
+// u > 0 for a finite double, on the integer pipe
+__device__ __forceinline__ bool dpos(double u) { return __double_as_longlong(u) > 0; }
+
+__global__ void __launch_bounds__(ATX * ATY)
+    k_advect_sp(step_consts c, advect_consts a, const __grid_constant__ field_maps maps, fields_dev F, int cur,
+                double dt, double bv, int emit_source) {
+    extern __shared__ __align__(128) unsigned char adv_raw_sp[];
+    adv_smem_sp &Sm = *reinterpret_cast<adv_smem_sp *>(adv_raw_sp + ((128 - (smem_addr(adv_raw_sp) & 127)) & 127));
+    eno_tile_sp &T = Sm.T;
+    const int m = c.m, n = c.n;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * ATX + tx;
+    const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY;
+    const int i = i0 + tx, j = j0 + ty;
+    if (c.clock) cur = (int)c.clock[CLK_CUR];
+    const double *__restrict__ const *A = F.f[cur];
+    double *const *B = F.f[cur ^ 1];
+    if (tid == 0) mbar_init(&Sm.bar, 1);
+    if (tid < ACOLS) {
+        const int u = i0 + tid - 2;
+        int w = u % m;
+        if (w < 0) w += m;
+        T.col[tid] = w;
+        T.xo[tid] = u < 0 ? -c.lx : (u >= m ? c.lx : 0.0);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_expect_tx(&Sm.bar, kTileBytes);
+        for (int f = 0; f < F_COUNT; f++) tma_load_2d(&Sm.tile[f][0][0], &maps.f[cur][f], i0 - 2, j0 - 1, &Sm.bar);
+    }
+    if (__syncthreads_or(!mbar_wait_bounded(&Sm.bar))) {
+        if (tid == 0) atomicExch(&F.flags[FL_TMA], 1);
+        mbar_wait_bounded(&Sm.bar);
+        return;
+    }
+    constexpr int kTileVals = F_COUNT * AROWS * ACOLS;
+    // columns across the periodic seam arrive as zeros: edge blocks fetch them
+    if (i0 == 0 || i0 + ACOLS - 2 > m) {
+        for (int k = tid; k < kTileVals; k += ATX * ATY) {
+            const int f = k / (AROWS * ACOLS), rem = k - f * (AROWS * ACOLS), r = rem / ACOLS, t = rem - r * ACOLS;
+            const int u = i0 + t - 2, sr = j0 - 1 + r;
+            if ((u < 0 || u >= m) && sr >= 0 && sr <= n + 1) Sm.tile[f][r][t] = A[f][(size_t)sr * m + T.col[t]];
+        }
+        __syncthreads();
+    }
+    // split every staged value (X unwrapped across the seam first)
+    for (int k = tid; k < kTileVals; k += ATX * ATY) {
+        const int f = k / (AROWS * ACOLS), rem = k - f * (AROWS * ACOLS), r = rem / ACOLS, t = rem - r * ACOLS;
+        double v = Sm.tile[f][r][t];
+        if (f == F_X && T.xo[t] != 0) v += T.xo[t];
+        ff_split_d(v, T.th[f][r][t], T.tl[f][r][t]);
+    }
+    __syncthreads();
+    // first differences: x on cell rows j0..j0+ATY-1, y on rows j0-2..j0+ATY+1
+    for (int k = tid; k < F_COUNT * ATY * ADXW; k += ATX * ATY) {
+        const int f = k / (ATY * ADXW), rem = k - f * (ATY * ADXW), r = rem / ADXW, cc = rem - r * ADXW;
+        float d = 0.f;
+        if (j0 + r < n) d = ff_diff(T.th[f][r + 2][cc + 1], T.tl[f][r + 2][cc + 1], T.th[f][r + 2][cc], T.tl[f][r + 2][cc]);
+        T.dx[f][r][cc] = d;
+    }
+    for (int k = tid; k < F_COUNT * ADYH * ATX; k += ATX * ATY) {
+        const int f = k / (ADYH * ATX), rem = k - f * (ADYH * ATX), r = rem / ATX, cc = rem - r * ATX;
+        const int jj = j0 + r - 2;
+        float d = 0.f;
+        if (jj >= -1 && jj + 1 <= n && i0 + cc < m)
+            d = ff_diff(T.th[f][r + 1][cc + 2], T.tl[f][r + 1][cc + 2], T.th[f][r][cc + 2], T.tl[f][r][cc + 2]);
+        T.dy[f][r][cc] = d;
+    }
+    __syncthreads();
+    for (int k = tid; k < F_COUNT * ATY * ASXW; k += ATX * ATY) {
+        const int f = k / (ATY * ASXW), rem = k - f * (ATY * ASXW), r = rem / ASXW, cc = rem - r * ASXW;
+        T.sx[f][r][cc] = T.dx[f][r][cc + 1] - T.dx[f][r][cc];
+    }
+    for (int k = tid; k < F_COUNT * ASYH * ATX; k += ATX * ATY) {
+        const int f = k / (ASYH * ATX), rem = k - f * (ASYH * ATX), r = rem / ATX, cc = rem - r * ATX;
+        T.sy[f][r][cc] = T.dy[f][r + 1][cc] - T.dy[f][r][cc];
+    }
+    __syncthreads();
+    if (i >= m || j >= n) return;
+    const float hx = (float)a.hx, hy = (float)a.hy;
+    const size_t ci = (size_t)(j + 1) * m + i;
+    const int ir = T.col[tx + 3];
+    if (c.clock) bv = c.clock[CLK_BV_STATE];
+    velo V{F.vel, m, n, bv};
+    // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
+    if (j > 0) {
+        const double un = V.u(i, j), vn = V.v(i, j);
+        const bool ru = dpos(un), rv = dpos(vn);
+        const float uh = ff_hi(un) * (ru ? hx : -hx), vh = ff_hi(vn) * (rv ? hy : -hy);
+        const bool inner = rv ? j > 1 : j < n - 1;
+        const float ex_X = eno_x_sp(Sm, F_X, ty, tx, ru), ex_Y = eno_x_sp(Sm, F_Y, ty, tx, ru);
+        const float ey_X = eno_y_sp(Sm, F_X, ty, tx, rv, inner, j0, n),
+                    ey_Y = eno_y_sp(Sm, F_Y, ty, tx, rv, inner, j0, n);
+        B[F_X][ci] = add_inc(Sm.tile[F_X][ty + 2][tx + 2], fmaf(-vh, ey_X, -uh * ex_X));
+        B[F_Y][ci] = add_inc(Sm.tile[F_Y][ty + 2][tx + 2], fmaf(-vh, ey_Y, -uh * ex_Y));
+    }
+    // staggered velocity and spin (shear_sim.cc:330-333): the velocity
+    // differences in FP64, everything after them in FP32
+    const double u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
+    const double v00 = V.v(i, j), v10 = V.v(ir, j), v01 = V.v(i, j + 1), v11 = V.v(ir, j + 1);
+    const float uc = 0.25f * ((ff_hi(u00) + ff_hi(u10)) + (ff_hi(u01) + ff_hi(u11)));
+    const float vc = 0.25f * ((ff_hi(v00) + ff_hi(v10)) + (ff_hi(v01) + ff_hi(v11)));
+    const float two_omega = hx * (ff_hi(v10 - v00) + ff_hi(v11 - v01)) - hy * (ff_hi(u01 - u00) + ff_hi(u11 - u10));
+    const bool ru = uc > 0.f, rv = vc > 0.f;
+    const float uh = uc * (ru ? hx : -hx), vh = vc * (rv ? hy : -hy);
+    float f1[5], f2[5];
+    const bool inner = rv ? j > 0 : j < n - 1;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        f1[k] = eno_x_sp(Sm, k, ty, tx, ru);
+        f2[k] = eno_y_sp(Sm, k, ty, tx, rv, inner, j0, n);
+    }
+    const double p = Sm.tile[F_P][ty + 2][tx + 2], q = Sm.tile[F_Q][ty + 2][tx + 2];
+    const double s = Sm.tile[F_S][ty + 2][tx + 2], t = Sm.tile[F_TAU][ty + 2][tx + 2];
+    double cchi = add_inc(Sm.tile[F_CHI][ty + 2][tx + 2], fmaf(-vh, f2[4], -uh * f1[4])), ddev, dtmp;
+    const double devsq = fma(3 * q, q, fma(s, s, t * t));
+    const bool athermal = c.stz_model >= 2;
+    const long long dbits = __double_as_longlong(devsq);
+    if (dbits < __double_as_longlong(0.999e-24) || (athermal && dbits < __double_as_longlong(c.yield_cut2))) {
+        ddev = 0;
+        dtmp = 0;
+    } else {
+        int iters;
+        const stz_law_params<double> lp = law_params(c);
+        dtmp = adaptive_plastic(lp, sqrt(devsq), cchi, ddev, dt, iters);
+        if (iters >= c.substep_cap) atomicExch(&F.flags[FL_SUBSTEP_CAP], 1);
+        if (iters > 1) atomicMax(&F.flags[FL_SUBSTEP_MAX], iters);
+    }
+    B[F_CHI][ci] = cchi;
+    F.ddev[ci] = ddev;
+    if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
+    const float tf = ff_hi(t), sf = ff_hi(s);
+    const float inc_p = fmaf(-vh, f2[0], -uh * f1[0]), inc_q = fmaf(-vh, f2[1], -uh * f1[1]);
+    const float inc_s = fmaf(two_omega, tf, fmaf(-vh, f2[2], -uh * f1[2]));
+    const float inc_t = fmaf(-two_omega, sf, fmaf(-vh, f2[3], -uh * f1[3]));
+    const double pn = add_inc(p, inc_p);
+    double qn = add_inc(q, inc_q), sn = add_inc(s, inc_s), tn = add_inc(t, inc_t);
+    if (dtmp != 0) {
+        qn -= dtmp * q;
+        sn -= dtmp * s;
+        tn -= dtmp * t;
     }
     B[F_P][ci] = pn;
     B[F_Q][ci] = qn;
@@ -603,6 +874,9 @@ cudaError_t prepare_step_kernels() {
     if (dev < 64 && (done >> dev & 1)) return cudaSuccess;
     e = cudaFuncSetAttribute(k_advect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(adv_smem) + 128));
     if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_advect_sp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(adv_smem_sp) + 128));
+    if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_direct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(direct_tile));
     if (e == cudaSuccess && dev < 64) done |= 1ull << dev;
     return e;
@@ -647,8 +921,11 @@ void advection(const step_consts &c, const field_maps &maps, fields_dev &F, int 
     a.hy = 0.5 * c.ysp * dt;
     a.xf = 0.5 / dt * c.xsp;
     a.yf = 0.5 / dt * c.ysp;
-    k_advect<<<dim3(ceil_div(c.m, ATX), ceil_div(c.n, ATY)), dim3(ATX, ATY), sizeof(adv_smem) + 128, st>>>(
-        c, a, maps, F, cur, dt, bv, 1);
+    const dim3 grid(ceil_div(c.m, ATX), ceil_div(c.n, ATY));
+    if (c.sp_increments)
+        k_advect_sp<<<grid, dim3(ATX, ATY), sizeof(adv_smem_sp) + 128, st>>>(c, a, maps, F, cur, dt, bv, 1);
+    else
+        k_advect<<<grid, dim3(ATX, ATY), sizeof(adv_smem) + 128, st>>>(c, a, maps, F, cur, dt, bv, 1);
     note_launch();
     if (c.chi_diff != 0 || c.chi_len != 0) {
         k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);

@@ -12,6 +12,8 @@ namespace stzg {
 // (j+1)*m + i.  The state is double-buffered: the advection kernel reads
 // buffer `cur` and writes buffer `cur^1`.
 enum { F_P = 0, F_Q, F_S, F_TAU, F_CHI, F_X, F_Y, F_COUNT };
+// Slots of fields_dev::flags.
+enum { FL_SUBSTEP_CAP = 0, FL_SUBSTEP_MAX, FL_VEL_CHANGED, FL_TMA, FL_PASSES, FL_LOOP_ERR, FL_COUNT = 8 };
 
 struct fields_dev {
     double *f[2][F_COUNT];
@@ -19,8 +21,10 @@ struct fields_dev {
     double *eps_pl;  // accumulated plastic strain (cells, m*n)
     double2 *vel;    // node velocity, rows 0..n, index j*m+i (solver array)
     double2 *src;    // projection right-hand side, same layout
-    int *flags;      // [0]: plastic sub-step cap reached, [1]: max sub-steps, [2]: scratch of
-                     // the velocity upload, [3]: an advection tile copy wait ran out
+    int *flags;      // FL_COUNT ints: [0] plastic sub-step cap reached, [1] max sub-steps,
+                     // [2] scratch of the velocity upload, [3] an advection tile copy wait
+                     // ran out, [4] passes of the last device-loop solve, [5] its error
+                     // (1 pass cap reached, 2 NaN residual)
     // Per-cell combinations of the advected stress that the nodal net force
     // (shear_sim::net_force, shear_sim.cc:447-453) sums with +-1 weights:
     // U = xf A + yf tau, W = xf A - yf tau, Y1 = xf tau - yf B,
@@ -43,6 +47,9 @@ struct step_consts {
     // kernel arguments from the host).  Layout: CLK_* below.
     const double *clock;
     double xbc;  // bcs*cxx of the projection operator (wall source = -+xbc*bv)
+    // advection with FP32 differences and increments on the FP64 state
+    // (mixed-precision handles); 0: all FP64, bit-exact
+    int sp_increments;
 };
 
 // Device clock slots: time, wall speed of the stored state, wall speed and
@@ -86,7 +93,8 @@ struct field_maps {
     CUtensorMap f[2][F_COUNT];
 };
 int make_field_maps(const step_consts &c, const fields_dev &F, field_maps *out);
-// F.flags[3] is set when a tile's copy wait runs out (status, no fault).
+// F.flags[FL_TMA] is set when a tile's copy wait runs out (status, no fault); that
+// tile of the next state is then left unwritten.
 void advection(const step_consts &c, const field_maps &maps, fields_dev &F, int cur, double dt, double bv,
                cudaStream_t st);
 // Opts the advection kernel into the shared memory its tile needs (once per

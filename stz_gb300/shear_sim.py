@@ -36,14 +36,15 @@ class ShearSim:
 
     def __init__(self, params: StzParams, chi=None, *, precision=_lib.FP64, tol_mode=_lib.TOL_REFERENCE,
                  tol=1e4, track_plastic=True, device=0, inner_cycles=0, use_graphs=True,
-                 extrapolate=False, substep_cap=0):
+                 extrapolate=False, substep_cap=0, advection=_lib.ADV_AUTO):
         lib = _lib.load()
         self.params = params.copy()
         self.m, self.n = params.m, params.n
         self.options = _lib.default_options(precision=precision, tol_mode=tol_mode, tol=tol,
                                             track_plastic=int(track_plastic), device=device,
                                             inner_cycles=inner_cycles, use_graphs=int(use_graphs),
-                                            extrapolate=int(extrapolate), substep_cap=int(substep_cap))
+                                            extrapolate=int(extrapolate), substep_cap=int(substep_cap),
+                                            advection=int(advection))
         h = ctypes.c_void_p()
         _lib.check(lib.stzg_create(ctypes.byref(self.params), ctypes.byref(self.options), ctypes.byref(h)))
         self.h = h
@@ -94,6 +95,16 @@ class ShearSim:
         chi = random_chi(self.m, self.n, l, tem_avg, tem_stdev, self.params.TZ, seed)
         self.set_state(chi)
         return chi
+
+    def init_fields(self, chi_case, tem_base=600.0, tem_delta=200.0):
+        """shear_sim::init_fields (shear_sim.cc:60-114)."""
+        _lib.check(self.lib.stzg_init_fields(self.h, int(chi_case), float(tem_base), float(tem_delta)))
+
+    def initialize_chi_bicubic(self, arr, lo=0.0, sca=1.0):
+        """shear_sim::initialize_chi_bicubic (shear_sim.cc:832-909); arr is (nn, mm)."""
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        nn, mm = a.shape
+        _lib.check(self.lib.stzg_chi_bicubic(self.h, mm, nn, _ptr(a), float(lo), float(sca)))
 
     @property
     def time(self):

@@ -5,8 +5,9 @@ application allocator that owns the device memory, a fixed memory budget, a
 thread that must not stall the GPU): its reduction scratch is a static
 device array.  It is checked through the C ABI against the allocating path
 (stzg_mg_l2_error on a handle, which reduces through the handle's own scratch)
-on two calls in a row with different inputs, so the second call also shows
-that nothing left in the shared array leaks into the next result.  This file
+and against the CPU oracle's residual sum (mds, tgmg.in.cc:55-64) on two
+calls in a row with different inputs, so the second call also shows that
+nothing left in the shared array leaks into the next result.  This file
 is collected last so that a run stopping at its first failure has run every
 other test.
 """
@@ -15,6 +16,7 @@ import ctypes
 import numpy as np
 import pytest
 
+from oracle.bind import OracleSim
 from stz_gb300 import _lib
 from stz_gb300.params import simple_shear
 from stz_gb300.shear_sim import ShearSim
@@ -30,6 +32,7 @@ def test_noalloc_residual_norms_match_allocating_path():
     dt = 0.01
     chi = np.full((N, N), 600 / 21000.0)
     sim = ShearSim(P, chi)
+    oracle = OracleSim(P, chi)
     nodes = N * (N + 1)
     rng = np.random.default_rng(17)
     dev = torch.device("cuda", 0)
@@ -47,6 +50,9 @@ def test_noalloc_residual_norms_match_allocating_path():
         mean_sq = sim.mg_l2_error(dt, src, vel)  # allocating path: sum/nodes
         assert r2 == pytest.approx(mean_sq * nodes, rel=1e-12)
         assert b2 == pytest.approx(float(np.sum(src ** 2)), rel=1e-12)
+        o_r2, o_b2 = oracle.mg_residual_sqnorms(dt, src, vel)
+        assert r2 == pytest.approx(o_r2, rel=1e-12)
+        assert b2 == pytest.approx(o_b2, rel=1e-12)
 
 
 def test_noalloc_rejects_oversized_grid():
