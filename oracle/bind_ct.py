@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from oracle.bind import REFERENCE_ROOT, build_reference
+from oracle.bind import build_reference, reference_root
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CT_REF_SO = os.path.join(HERE, "_ref", "libctref.so")
@@ -23,7 +23,7 @@ _lib = None
 def available():
     if os.path.exists(CT_REF_SO):
         return True
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "esim")):
+    if reference_root() is None:
         return False
     build_reference(force=True)
     return os.path.exists(CT_REF_SO)
@@ -41,6 +41,7 @@ def _load():
         L.ctref_create.argtypes = [ctypes.POINTER(CtParams)]
         L.ctref_destroy.argtypes = [V]
         L.ctref_init_fields.argtypes = [V, I, D, D]
+        L.ctref_chi_bicubic.argtypes = [V, I, I, _P, D, D]
         L.ctref_get_field.argtypes = [V, I, _P]
         L.ctref_set_field.argtypes = [V, I, _P]
         L.ctref_steps.argtypes = [V, D, I]
@@ -77,6 +78,11 @@ class ReferenceCt:
 
     def init_fields(self, chi_case, base, delta):
         self.L.ctref_init_fields(self.h, chi_case, base, delta)
+
+    def chi_bicubic(self, arr, lo, sca):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        nn, mm = a.shape
+        self.L.ctref_chi_bicubic(self.h, mm, nn, a.ctypes.data_as(_P), lo, sca)
 
     def get(self, name):
         out = np.empty((self.P.n + 1, self.P.m))

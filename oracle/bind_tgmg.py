@@ -11,7 +11,7 @@ import os
 
 import numpy as np
 
-from oracle.bind import REFERENCE_ROOT, build_reference
+from oracle.bind import build_reference, reference_root
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TGMG_REF_SO = os.path.join(HERE, "_ref", "libtgmgref.so")
@@ -24,7 +24,7 @@ _lib = None
 def available():
     if os.path.exists(TGMG_REF_SO):
         return True
-    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "esim")):
+    if reference_root() is None:
         return False
     build_reference(force=True)
     return os.path.exists(TGMG_REF_SO)

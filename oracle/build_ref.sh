@@ -4,7 +4,11 @@
 # step from their sources, read in place under the reference tree, into
 # oracle/_ref/libstzref.so, libtgmgref.so and libctref.so (test-only).
 #
-#   oracle/build_ref.sh [REFERENCE_ROOT]     (default: /root/reference)
+#   oracle/build_ref.sh [REFERENCE_ROOT]
+#   oracle/build_ref.sh --root     prints the reference tree it would use and
+#                                  exits 0, or exits 2 when it is absent
+#
+# REFERENCE_ROOT defaults to $STZ_REFERENCE_ROOT, else /root/reference.
 #
 # Recipe (the reference's own make files are not used):
 #   1. esim/tgmg/tgmg_compile.pl expands tgmg.in.cc into tgmg.cc.  The script
@@ -24,7 +28,13 @@
 #      include path: its headers share names with esim/sb/main's).
 # Only x86/Arm-neutral flags are used; nothing here runs on the GPU.
 set -e
-REF=${1:-/root/reference}
+DEFAULT_REF=${STZ_REFERENCE_ROOT:-/root/reference}
+if [ "$1" = "--root" ]; then
+    [ -f "$DEFAULT_REF/esim/tgmg/tgmg.in.cc" ] || exit 2
+    echo "$DEFAULT_REF"
+    exit 0
+fi
+REF=${1:-$DEFAULT_REF}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 ESIM="$REF/esim"

@@ -98,6 +98,38 @@ void stzref_set_state(void *vh, const double *chi) {
     s.time = 0;
 }
 
+// shear_sim::init_fields (shear_sim.cc:60-114) with the solver's velocity
+// array cleared (the reference leaves it unset; set_state clears it too).
+void stzref_init_fields(void *vh, int chi_case, double tem_base, double tem_delta) {
+    shear_sim &s = *((ref_handle *)vh)->sim;
+    s.init_fields(chi_case, tem_base, tem_delta);
+    for (int k = 0; k < s.m * (s.n + 1); k++) s.vel[k].x = s.vel[k].y = 0;
+    s.time = 0;
+}
+
+// shear_sim::initialize_chi_bicubic (shear_sim.cc:832-909): chi of rows
+// 0..n-1 from the bicubic interpolant of arr (mm x nn); the other fields as
+// init_fields sets them.  Ghost rows of chi keep their previous values in the
+// reference; here they get the linear extrapolation of set_boundaries, so
+// that the state is defined.
+void stzref_chi_bicubic(void *vh, int mm, int nn, const double *arr, double lo, double sca) {
+    shear_sim &s = *((ref_handle *)vh)->sim;
+    std::vector<double> a(arr, arr + (size_t)mm * nn);
+    s.initialize_chi_bicubic(mm, nn, a.data(), lo, sca);
+    int m = s.m, n = s.n;
+    for (int i = 0; i < m; i++) {
+        s.fm[i - m].chi = 2 * s.fm[i].chi - s.fm[i + m].chi;
+        s.fm[i + m * n].chi = 2 * s.fm[i + m * (n - 1)].chi - s.fm[i + m * (n - 2)].chi;
+    }
+    for (int k = 0; k < m * (n + 1); k++) s.vel[k].x = s.vel[k].y = 0;
+    s.time = 0;
+}
+
+// shear_sim::l2_comparison (shear_sim.cc:460-502) of two reference runs.
+void stzref_l2_comparison(void *va, void *vb, double *l2) {
+    ((ref_handle *)va)->sim->l2_comparison(*((ref_handle *)vb)->sim, l2);
+}
+
 // Replaces the tolerance multiplier of qs_multi.cc:14 (default 1e4).
 void stzref_set_acc_mult(void *vh, double mult) {
     qs_multi &q = ((ref_handle *)vh)->sim->qsm;

@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures from the reference itself.
 
-Run in a checkout that has the SURGroup/STZ tree available (default
-/root/reference, override with STZ_REFERENCE_ROOT):
+Run in a checkout that has the SURGroup/STZ tree available (the tree
+oracle/build_ref.sh resolves: STZ_REFERENCE_ROOT, else the recipe's default):
 
     python tests/golden/make_golden.py
 
@@ -9,7 +9,8 @@ It builds oracle/_ref/libstzref.so from the reference sources
 (oracle/build_ref.sh), runs the reference's own
 shear_sim::step_forward_quasistatic (esim/sb/main/shear_sim.cc:280) and
 shear_sim::step_forward (shear_sim.cc:185) and the frame export and
-diagnostics (output, qs_measure, tractions, compute_strain) on seeded
+diagnostics (output, qs_measure, tractions, compute_strain), the initial
+states of init_fields and initialize_chi_bicubic and l2_comparison on seeded
 inputs, and stores
 inputs and outputs as compressed .npz files next to this script.  Names given
 on the command line restrict it to those fixtures.  The chi inputs come from the oracle's seeded random-field generator;
@@ -132,8 +133,120 @@ def make(name, spec):
     return cycles
 
 
+# Initial states of the reference drivers, then quasi-static steps from
+# them: shear_sim::init_fields (shear_sim.cc:60-114, chi cases 0-2) and
+# shear_sim::initialize_chi_bicubic (shear_sim.cc:832-909):
+# name -> (params, set-up, dt, steps, tolerance multiplier); set-up is
+# ("init", chi_case, tem_base, tem_delta) or ("bicubic", (mm, nn, seed), lo, sca)
+INIT_CASES = {
+    "init_case0_32x24": (plastic_shear(32, 24, u_bdry=2.0), ("init", 0, 600.0, 200.0), 0.01, 40, 10.0),
+    "init_case1_40x20": (plastic_shear(40, 20, u_bdry=2.0), ("init", 1, 630.0, 170.0), 0.01, 40, 10.0),
+    "init_case2_48x24": (plastic_shear(48, 24, u_bdry=2.0, x_half=2.0), ("init", 2, 600.0, 200.0), 0.01, 40,
+                         10.0),
+    "bicubic_36x28": (plastic_shear(36, 28, u_bdry=2.0), ("bicubic", (9, 7, 21), 550.0 / 21000, 100.0 / 21000),
+                      0.01, 40, 10.0),
+}
+
+
+def init_state(sim, setup):
+    if setup[0] == "init":
+        _, case, base, delta = setup
+        sim.init_fields(case, base, delta)
+        return {}
+    _, (mm, nn, seed), lo, sca = setup
+    arr = np.random.default_rng(seed).random((nn, mm))
+    sim.chi_bicubic(arr, lo, sca)
+    return {"bicubic_arr": arr}
+
+
+def make_init(name, spec):
+    P, setup, dt, steps, mult = spec
+    sim = ReferenceSim(P)
+    out = init_state(sim, setup)
+    out.update({k + "0": v for k, v in sim.fields().items() if k != "eps_pl"})
+    sim.set_acc_mult(mult)
+    cycles = sim.steps(dt, steps)
+    out.update(sim.fields())
+    meta = {"kind": "init", "params": P.as_dict(), "setup": list(setup[:1]) + [setup[1] if setup[0] == "init"
+                                                                              else list(setup[1])] +
+            list(setup[2:]), "dt": dt, "steps": steps, "acc_mult": mult, "cycles": int(cycles), "time": sim.time,
+            "source": "reference shear_sim::init_fields / initialize_chi_bicubic, then step_forward_quasistatic, "
+                      "built from source"}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **out)
+    return cycles
+
+
+# shear_sim::l2_comparison (shear_sim.cc:460-502) of an explicit run and a
+# quasi-static run from the same state, as the shear_compare driver does:
+# name -> (params, chi (l, std, seed), tmult, frame times, quasi-static steps per frame, multiplier)
+L2_CASES = {
+    "l2cmp_32x16": (plastic_shear(32, 16, u_bdry=2.0, viscosity=0.02, x_half=2.0), (3, 30, 31), 0.5,
+                           (0.05, 0.1, 0.15), 5, 10.0),
+}
+
+
+def make_l2(name, spec):
+    P, (l, std, seed), tmult, frames, nq, mult = spec
+    chi = random_chi(P.m, P.n, l, 600.0, std, P.TZ, seed)
+    d = ReferenceSim(P, chi)
+    q = ReferenceSim(P, chi)
+    q.set_acc_mult(mult)
+    dx = (P.bx - P.ax) / P.m
+    dt = dx * dx * tmult
+    out = {"chi0": chi}
+    l2s = [d.l2_comparison(q)]
+    t_prev = 0.0
+    for k, t in enumerate(frames):
+        d.advance_direct(dt, t)
+        q.steps((t - t_prev) / nq, nq)
+        t_prev = t
+        l2s.append(d.l2_comparison(q))
+    out["l2"] = np.array(l2s)
+    out.update({"direct_" + k: v for k, v in d.fields().items()})
+    out.update({"qs_" + k: v for k, v in q.fields().items()})
+    meta = {"kind": "l2", "params": P.as_dict(), "tmult": tmult, "dt": dt, "frames": list(frames), "qs_steps": nq,
+            "acc_mult": mult, "time": d.time,
+            "source": "reference shear_sim::l2_comparison of a step_forward run and a step_forward_quasistatic "
+                      "run, built from source"}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **out)
+    return out["l2"][-1]
+
+
+# Coarse Galerkin operators of the quasi-static system (tgmg::setup ->
+# calculate_rat, tgmg.in.cc:667-736, generated compute_rat): every level's
+# stored stencils (9 blocks and the inverse centre) for a grid shape.
+COARSE_CASES = {"coarseops_24x24": (24, 24), "coarseops_32x32": (32, 32), "coarseops_40x72": (40, 72),
+                "coarseops_80x80": (80, 80)}
+
+
+def make_coarse(name, shape):
+    m, n = shape
+    P = simple_shear(m, n)
+    sim = ReferenceSim(P, np.full((n, m), 600 / 21000.0))
+    levels = sim.mg_levels(0.01)
+    out = {f"level{k}": sim.mg_stencil(0.01, k) for k in range(len(levels))}
+    meta = {"kind": "coarse", "params": P.as_dict(), "dt": 0.01, "levels": [list(x) for x in levels],
+            "source": "reference tgmg_level::s after tgmg::setup of qs_multi, built from source"}
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **out)
+    return len(levels)
+
+
 def main():
     only = sys.argv[1:]
+    for name, shape in COARSE_CASES.items():
+        if only and name not in only:
+            continue
+        print(f"{name}: {make_coarse(name, shape)} coarse levels")
+    for name, spec in INIT_CASES.items():
+        if only and name not in only:
+            continue
+        c = make_init(name, spec)
+        print(f"{name}: {c} V-cycles")
+    for name, spec in L2_CASES.items():
+        if only and name not in only:
+            continue
+        l2 = make_l2(name, spec)
+        print(f"{name}: l2 {l2}")
     for name, spec in CASES.items():
         if only and name not in only:
             continue

@@ -1,7 +1,7 @@
 """Regenerates the general-multigrid golden fixtures from the reference itself.
 
-Run where the SURGroup/STZ tree is available (default /root/reference,
-override with STZ_REFERENCE_ROOT):
+Run where the SURGroup/STZ tree is available (the tree oracle/build_ref.sh
+resolves: STZ_REFERENCE_ROOT, else the recipe's default):
 
     python tests/golden/make_golden_tgmg.py
 
