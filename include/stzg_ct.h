@@ -40,6 +40,11 @@ int stzg_ct_create(const stzg_ct_params *p, int device, stzg_ct **out);
 int stzg_ct_destroy(stzg_ct *s);
 /* shear_sim::init_fields(chi_case, tem_base, tem_delta) (shear_sim.cc:59-131). */
 int stzg_ct_init_fields(stzg_ct *s, int chi_case, double tem_base, double tem_delta);
+/* shear_sim::initialize_chi_bicubic(mm, nn, arr, lo, sca) (shear_sim.cc:
+ * 1067-1134): chi of the cells = lo + sca * the bicubic interpolant of arr
+ * (mm x nn samples over the domain, row-major, periodic in x and, when y_prd,
+ * in y; nn >= 2), then set_boundaries; the other fields are unchanged. */
+int stzg_ct_chi_bicubic(stzg_ct *s, int mm, int nn, const double *arr, double lo, double sca);
 /* Copies one field in or out (rows 0..n).  set_field re-applies the
  * boundary conditions (set_boundaries, shear_sim.cc:778-811). */
 int stzg_ct_set_field(stzg_ct *s, int field, const double *host);

@@ -78,6 +78,12 @@ void ctref_init_fields(void *vh, int chi_case, double base, double delta) {
 }
 
 // Rows 0..n of one field (m per row).
+// shear_sim::initialize_chi_bicubic (shear_sim.cc:1067-1134), as it is.
+void ctref_chi_bicubic(void *vh, int mm, int nn, const double *arr, double lo, double sca) {
+    std::vector<double> a(arr, arr + (size_t)mm * nn);
+    ((ct_handle *)vh)->sim->initialize_chi_bicubic(mm, nn, a.data(), lo, sca);
+}
+
 void ctref_get_field(void *vh, int id, double *out) {
     shear_sim &s = *((ct_handle *)vh)->sim;
     for (int j = 0; j <= s.n; j++)

@@ -776,6 +776,78 @@ int stzg_ct_init_fields(stzg_ct *s, int chi_case, double tem_base, double tem_de
     return STZG_OK;
 }
 
+// shear_sim::initialize_chi_bicubic of the variant
+// (coord_transforms/simple_shear/shear_sim.cc:1067-1134): chi of the cells
+// (rows 0..n-1) = lo + sca times the bicubic Hermite interpolant of arr
+// (mm x nn, periodic in x, and in y when y is periodic), derivatives by
+// centred differences; with walls the first and last sample rows use the
+// row itself as the missing neighbour with the factor 1/2 of the centred
+// difference, as the reference's expression gives (its factor 1 applies only
+// where j == 0 and j == mm-1 together).  Then set_boundaries.  The other
+// fields are left as they are.
+int stzg_ct_chi_bicubic(stzg_ct *s, int mm, int nn, const double *arr, double lo, double sca) {
+    if (!s || !arr || mm < 1 || nn < 2) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CUDA(cudaSetDevice(s->device));
+    const ct_consts &c = s->c;
+    const bool yp = c.yp != 0;
+    const long mn = (long)mm * nn;
+    std::vector<double> ax(mn), ay(mn), axy(mn);
+    for (int j = 0; j < nn; j++)
+        for (int i = 0; i < mm; i++) {
+            const long r = (long)j * mm;
+            ax[r + i] = 0.5 * (arr[r + (i == mm - 1 ? 0 : i + 1)] - arr[r + (i == 0 ? mm - 1 : i - 1)]);
+        }
+    for (int j = 0; j < nn; j++) {
+        const long r = (long)j * mm;
+        const long rd = j == 0 ? (yp ? r + (mn - mm) : r) : r - mm;
+        const long ru = j == nn - 1 ? (yp ? r + (mm - mn) : r) : r + mm;
+        const double fac = (!yp && j == 0 && j == mm - 1) ? 1. : 0.5;
+        for (int i = 0; i < mm; i++) {
+            ay[r + i] = fac * (arr[ru + i] - arr[rd + i]);
+            axy[r + i] = fac * (ax[ru + i] - ax[rd + i]);
+        }
+    }
+    const double xs = c.dx * mm / c.lx, ys = c.dy * nn / c.ly;
+    std::vector<double> chi((size_t)c.m * c.n);
+    for (int j = 0; j < c.n; j++) {
+        double t = (j + 0.5) * ys - 0.5;
+        int hi;
+        if (yp) {
+            if (t < 0) t += nn;
+            hi = nn - 1;
+        } else {
+            hi = nn - 2;
+        }
+        int jj = (int)t;
+        jj = jj < 0 ? 0 : (jj > hi ? hi : jj);
+        const long up = jj == nn - 1 ? mm - mn : mm;  // offset of the next sample row
+        t -= jj;
+        const double u = 1. - t;
+        const double w0 = t * u * u, w1 = u * u * (1 + 2 * t), w2 = t * t * (3 - 2 * t), w3 = -t * t * u;
+        for (int i = 0; i < c.m; i++) {
+            double x = (i + 0.5) * xs - 0.5;
+            if (x < 0) x += mm;
+            int ii = (int)x;
+            if (ii >= mm) ii -= mm;
+            const long a = ii + (long)mm * jj, b = (ii == mm - 1 ? ii - mm : ii) + 1 + (long)mm * jj;
+            x -= ii;
+            const double v = 1 - x;
+            const double h0 = x * v * v, h1 = v * v * (1 + 2 * x), h2 = x * x * (3 - 2 * x), h3 = -x * x * v;
+            const double r0 = axy[a] * h0 + ay[a] * h1 + ay[b] * h2 + axy[b] * h3;
+            const double r1 = ax[a] * h0 + arr[a] * h1 + arr[b] * h2 + ax[b] * h3;
+            const double r2 = ax[a + up] * h0 + arr[a + up] * h1 + arr[b + up] * h2 + ax[b + up] * h3;
+            const double r3 = axy[a + up] * h0 + ay[a + up] * h1 + ay[b + up] * h2 + axy[b + up] * h3;
+            chi[(size_t)j * c.m + i] = lo + sca * (w0 * r0 + w1 * r1 + w2 * r2 + w3 * r3);
+        }
+    }
+    double *d = s->F.f[s->cur][CCHI];
+    STZG_CUDA(cudaMemcpy2DAsync(d + 2 * c.gm + 2, c.gm * sizeof(double), chi.data(), c.m * sizeof(double),
+                                c.m * sizeof(double), c.n, cudaMemcpyHostToDevice, s->st));
+    boundaries(s, s->cur);
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
 static double *ct_field_ptr(stzg_ct *s, int field) {
     return field == STZG_CT_DDEV ? s->F.ddev : s->F.f[s->cur][field];
 }

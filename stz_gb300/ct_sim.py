@@ -11,7 +11,7 @@ import numpy as np
 
 from . import _lib
 
-EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_set_field", "stzg_ct_get_field",
+EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_chi_bicubic", "stzg_ct_set_field", "stzg_ct_get_field",
            "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs", "stzg_ct_step_direct", "stzg_ct_tracers_init",
            "stzg_ct_tracers_update", "stzg_ct_tracers_get"]
 FIELDS = ("u", "v", "p", "q", "s", "tau", "chi", "X", "Y", "ddev")
@@ -70,6 +70,7 @@ def load():
         "stzg_ct_create": (I, [ctypes.POINTER(CtParams), I, ctypes.POINTER(V)]),
         "stzg_ct_destroy": (I, [V]),
         "stzg_ct_init_fields": (I, [V, I, D, D]),
+        "stzg_ct_chi_bicubic": (I, [V, I, I, ctypes.POINTER(ctypes.c_double), D, D]),
         "stzg_ct_set_field": (I, [V, I, _P]),
         "stzg_ct_get_field": (I, [V, I, _P]),
         "stzg_ct_set_time": (I, [V, D]),
@@ -113,6 +114,13 @@ class CtSim:
 
     def init_fields(self, chi_case=0, tem_base=600, tem_delta=200):
         _lib.check(self.lib.stzg_ct_init_fields(self.h, chi_case, tem_base, tem_delta))
+
+    def initialize_chi_bicubic(self, arr, lo=0.0, sca=1.0):
+        """shear_sim::initialize_chi_bicubic (shear_sim.cc:1067-1134); arr is (nn, mm)."""
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        nn, mm = a.shape
+        _lib.check(self.lib.stzg_ct_chi_bicubic(self.h, mm, nn, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                float(lo), float(sca)))
 
     def get(self, name):
         out = np.empty((self.P.n + 1, self.P.m))

@@ -1,8 +1,8 @@
 """Regenerates the golden fixtures of the coord_transforms step from the
 reference itself.
 
-Run where the SURGroup/STZ tree is available (default /root/reference,
-override with STZ_REFERENCE_ROOT):
+Run where the SURGroup/STZ tree is available (the tree oracle/build_ref.sh
+resolves: STZ_REFERENCE_ROOT, else the recipe's default):
 
     python tests/golden/make_golden_ct.py
 
@@ -12,8 +12,9 @@ up the driver's Vitreloy configuration (shear_coord_transform.cc:20-89) on a
 small grid with shear_sim::init_fields, runs step_forward_quasistatic, and
 stores the initial and final fields (rows 0..n), the time and the V-cycle
 count as tests/golden/ct_*.npz; the tracer cases (ct_tracers_*.npz) add
-shear_sim::initialize_tracers / update_tracers, and the ctdirect_*.npz cases
-run the explicit shear_sim::step_forward from an advanced quasi-static state.
+shear_sim::initialize_tracers / update_tracers, the ctdirect_*.npz cases
+run the explicit shear_sim::step_forward from an advanced quasi-static state,
+and the ct_bicubic_*.npz cases the driver's bicubic chi set-up.
 """
 import json
 import os
@@ -140,8 +141,54 @@ def make_direct(name, case):
     ref.close()
 
 
+# The driver program's set-up (shear_coord_transform.cc:93-101): init_fields,
+# then chi from the bicubic interpolant of a 64 x 32 sample array (a 2 x 2
+# block of ones in a field of zeros, scaled 550 K + 30 K), then quasi-static
+# steps: name -> (m, n, y_prd, chi_case, tem_base, tem_delta, dt, steps,
+# sample array shape, lo, sca).  The walled case uses a random sample array
+# (its one-sided first and last sample rows matter there).
+BICUBIC_CASES = {
+    "ct_bicubic_prd64x32": (64, 32, True, 0, 580.0, 220.0, 0.5 / 1e-3 / 600, 0, (32, 64), 550.0, 30.0),
+    "ct_bicubic_wall48x24": (48, 24, False, 0, 580.0, 220.0, 3e6 / 2e4 / 600, 20, (7, 9), 560.0, 40.0),
+}
+
+
+def bicubic_array(shape):
+    nn, mm = shape
+    if (nn, mm) == (32, 64):
+        a = np.zeros((nn, mm))
+        a[15:17, 31:33] = 1.0  # i > 30 && i < 33 && j > 14 && j < 17
+        return a
+    return np.random.default_rng(7).random((nn, mm))
+
+
+def make_bicubic(name, case):
+    m, n, yp, cc, base, delta, dt, steps, shape, lo, sca = case
+    P = transform_shear(m, n, y_prd=yp)
+    ref = ReferenceCt(P)
+    ref.init_fields(cc, base, delta)
+    arr = bicubic_array(shape)
+    ref.chi_bicubic(arr, lo / P.TZ, sca / P.TZ)
+    init = ref.fields()
+    ref.steps(dt, steps)
+    final = ref.fields()
+    out = {"init_" + k: v for k, v in init.items()}
+    out.update({"final_" + k: v for k, v in final.items()})
+    out["bicubic_arr"] = arr
+    params = {k: getattr(P, k) for k, _ in P._fields_}
+    meta = {"params": params, "chi_case": cc, "tem_base": base, "tem_delta": delta, "dt": dt, "steps": steps,
+            "lo": lo / P.TZ, "sca": sca / P.TZ, "time": ref.time, "vcount": ref.vcount}
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, "chi range (K)", init["chi"].min() * P.TZ, init["chi"].max() * P.TZ, "time", ref.time)
+    ref.close()
+
+
 def main(argv):
-    names = argv[1:] or list(CASES) + list(TRACER_CASES) + list(DIRECT_CASES)
+    names = argv[1:] or list(CASES) + list(TRACER_CASES) + list(DIRECT_CASES) + list(BICUBIC_CASES)
+    if len(names) == 1 and names[0] in BICUBIC_CASES:
+        make_bicubic(names[0], BICUBIC_CASES[names[0]])
+        return
     if len(names) == 1 and names[0] in TRACER_CASES:
         make_tracers(names[0], TRACER_CASES[names[0]])
         return

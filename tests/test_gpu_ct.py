@@ -144,3 +144,27 @@ def test_ct_explicit_step_matches_reference(name):
     # the update moved the state
     assert np.abs(ref["s"] - arr["init_s"]).max() > 1e-4
     sim.close()
+
+
+@pytest.mark.parametrize("name", golden_names("ct_bicubic"))
+def test_ct_chi_bicubic_matches_reference(name):
+    """shear_sim::initialize_chi_bicubic of the variant (the driver program's
+    set-up: init_fields, then chi from a sample array) reproduces the
+    reference's state, ghost layers through set_boundaries included; with
+    walls, quasi-static steps from it follow the reference."""
+    from stz_gb300.ct_sim import CtSim
+    meta, arr = _load(name)
+    P = _params(meta)
+    sim = CtSim(P)
+    sim.init_fields(meta["chi_case"], meta["tem_base"], meta["tem_delta"])
+    sim.initialize_chi_bicubic(arr["bicubic_arr"], meta["lo"], meta["sca"])
+    for k in FIELDS:
+        a, b = sim.get(k), arr["init_" + k]
+        assert np.abs(a - b).max() <= 1e-15 * max(np.abs(b).max(), 1.0), (name, k)
+    if meta["steps"]:
+        sim.step_forward_quasistatic(meta["dt"], meta["steps"])
+        err = ct_errors({k: arr["final_" + k] for k in FIELDS}, sim.fields(), P)
+        vel = err.pop("velocity")
+        assert vel < 1e-5, (vel, err)
+        assert max(err.values()) < 1e-7, err
+    sim.close()
