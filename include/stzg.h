@@ -64,10 +64,13 @@ typedef struct {
                           2 = quadratic, 3v(n) - 3v(n-1) + v(n-2) */
     int substep_cap;   /* iteration cap of the plastic sub-stepping per cell and step
                           (0: 4194304); reaching it returns STZG_ESUBSTEP */
-    int advection;     /* STZG_ADV_AUTO (0) and STZG_ADV_FP64: the advection runs in FP64,
-                          bit-exact with the per-point ENO2.  STZG_ADV_SPLIT (mixed-precision
-                          handles only): ENO differences and increments in FP32 from
-                          exactly split FP64 values, added to the FP64 state in FP64. */
+    int advection;     /* Mixed-precision handles: STZG_ADV_AUTO (0) or STZG_ADV_SPLIT run the
+                          advection, the projection source and the stress correction in
+                          float-float arithmetic (pairs of floats, ~2^-44 relative) on the
+                          FP64 state, each field updated by FP64 additions, with the ENO
+                          choices of the FP64 path; STZG_ADV_FP64 keeps them FP64.  FP64
+                          handles always run them in FP64, bit-exact with the per-point
+                          ENO2. */
     int reserved[5];
 } stzg_options;
 

@@ -535,7 +535,7 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     s->n = p->n;
     s->sc = make_step_consts(*p);
     s->sc.track_plastic = o.track_plastic;
-    s->sc.sp_increments = o.precision == STZG_MIXED && o.advection == STZG_ADV_SPLIT;
+    s->sc.sp_increments = o.precision == STZG_MIXED && o.advection != STZG_ADV_FP64;
     if (o.substep_cap > 0) s->sc.substep_cap = o.substep_cap;
     int st = STZG_OK;
     auto bail = [&](int code) {

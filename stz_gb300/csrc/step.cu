@@ -6,6 +6,13 @@
 
 namespace stzg {
 
+// x = hi + lo as floats on the host (hi the nearest float, lo the nearest
+// float of the remainder): the float-float form of a launch constant.
+void split_host(double x, float *hi, float *lo) {
+    *hi = (float)x;
+    *lo = (float)(x - (double)*hi);
+}
+
 step_consts make_step_consts(const stz_params &p) {
     step_consts c;
     c.m = p.m;
@@ -38,6 +45,7 @@ step_consts make_step_consts(const stz_params &p) {
     c.track_plastic = 0;
     c.substep_cap = 1 << 22;
     c.yield_cut2 = p.s_y * p.s_y * (1 - 1e-12);
+    c.yield_cut2f = (float)(c.yield_cut2 * (1 - 1e-6));
     c.clock = nullptr;
     c.xbc = 0;
     c.sp_increments = 0;
@@ -375,70 +383,81 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
     }
 }
 
-// ---- single-precision increments (mixed-precision handles) ------------------
-// The same step with the ENO differences and the advective increments in
-// FP32 while the state stays FP64: every staged value is split on the
-// integer pipe into a float pair hi + lo (ff_split_d), each first difference
-// f(c+1) - f(c) is formed from the pairs by TwoSum (ff_diff: the float
-// rounding of the exact difference, however close the two values are), and
-// the second differences, the ENO choice and value, the upwind products and
-// the rotation term run in FP32 (with an exact FP64 tie-break of the ENO
-// choice, below).  Each field then takes its increment with
-// one FP64 addition, so the state carries no FP32 rounding of its own, only
-// that of the increment (relative 2^-24 of a change that is itself a small
-// part of the field per step).  The velocity differences of the spin come
-// from FP64 subtractions; the plastic law, the stress norm of the yield test
-// and the net-force combinations stay FP64.  On GB300, where FP64 issues at
-// 1/57 of the FP32 rate, this takes the kernel off the FP64 pipe.
-struct eno_tile_sp {
+// ---- float-float advection (mixed-precision handles) ------------------------
+// The same step with the ENO differences, the upwind products and the
+// increments in float-float (double-word) arithmetic on the FP32 pipe while
+// the state stays FP64.  Every staged value is split on the integer pipe
+// into a float pair hi + lo (ff_split_d, 48 of its 53 significant bits); each
+// first difference f(c+1) - f(c) is formed from the pairs by TwoSum and kept
+// as a pair (relative error ~2^-44 of the difference, plus ~2^-47 of the
+// values); the ENO value is the chosen second difference plus twice the
+// centre difference, the increment u hs eno in both directions with the
+// product errors (FMA) and the sums by TwoSum, and the spin from pair
+// differences of the node velocities.  Each field takes its increment with
+// two FP64 additions (hi, then lo), so the state carries the rounding of the
+// FP64 path plus ~2^-44 of the increment per step.  The ENO choice
+// |S(i)| > |S(i-1)| is taken on the high parts where the two magnitudes
+// differ by more than that approximation's error bound; near ties it is
+// recomputed in FP64 from the staged tile with k_advect's operations, so the
+// choice is always the FP64 path's (a different choice changes the value by
+// the difference of two second differences, which near an inflection is not
+// small).  The yield test runs on a float-float stress norm; cells near or
+// above a cut-off take the FP64 norm and the FP64 plastic law as k_advect
+// does.  The net force is formed by k_source_ff from the stresses, so no
+// per-cell combinations are written.  GB300 issues FP64 at 1/57 of the FP32
+// rate; an elastic cell here needs two FP64 additions per field.
+struct eno_tile_ff {
     float th[F_COUNT][AROWS][ACOLS];  // hi / lo parts of the staged values (X unwrapped)
     float tl[F_COUNT][AROWS][ACOLS];
-    float dx[F_COUNT][ATY][ADXW];
-    float dy[F_COUNT][ADYH][ATX];
-    float sx[F_COUNT][ATY][ASXW];
-    float sy[F_COUNT][ASYH][ATX];
-    double xo[ACOLS];
-    int col[ACOLS];
+    float dxh[F_COUNT][ATY][ADXW];    // first differences in x: tile columns cc, cc+1
+    float dxl[F_COUNT][ATY][ADXW];
+    float dyh[F_COUNT][ADYH][ATX];    // first differences in y: tile rows r, r+1
+    float dyl[F_COUNT][ADYH][ATX];
+    int xs[ACOLS];   // period shift of the unwrapped column: -1, 0, +1
+    int col[ACOLS];  // storage column of tile column c-2
 };
 
-struct adv_smem_sp {
+struct adv_smem_ff {
     double tile[F_COUNT][AROWS][ACOLS];  // staged fields, first: 128-byte aligned
-    eno_tile_sp T;
+    eno_tile_ff T;
     uint64_t bar;
 };
 
-__device__ __forceinline__ bool mag_gtf(float a, float b) {
-    return (__float_as_uint(a) & 0x7fffffffu) > (__float_as_uint(b) & 0x7fffffffu);
+__device__ __forceinline__ ff split_ff(double d) {
+    ff r;
+    ff_split_d(d, r.hi, r.lo);
+    return r;
 }
-// The ENO choice |S(i)| > |S(i-1)| (or |S(i+1)|) is taken in FP32 where the
-// two magnitudes differ by more than the FP32 differences' error bound;
-// otherwise (rare: near ties) it is recomputed in FP64 from the staged tile
-// with k_advect's operations, so the choice always equals the FP64 path's.
-// A different choice would change the ENO value by the difference of the
-// two second differences, which near an inflection is not small.
-// Bound on |s_f - s| for the FP32 second differences of three first
-// differences a, b, c (each within ~2^-24 of its value plus ~2^-47 of the
-// values differenced): generous by a factor of ~16.
-__device__ __forceinline__ float tie_margin(float a, float b, float c, float vmag) {
-    return 1e-6f * (fabsf(a) + 2.f * fabsf(b) + fabsf(c)) + 1e-13f * vmag;
+
+// a - b for pairs a = (ah, al), b = (bh, bl): TwoSum of the high parts, the
+// low parts added to its error, renormalised.
+__device__ __forceinline__ ff ff_pair_diff(float ah, float al, float bh, float bl) {
+    const float s = ah - bh, bb = s - ah;
+    float e = (ah - (s - bb)) + (-bh - bb);
+    e += al - bl;
+    return ff_fast2sum(s, e);
 }
+__device__ __forceinline__ ff ff_x2(ff a) { return ff{2.f * a.hi, 2.f * a.lo}; }
+__device__ __forceinline__ float ffabs_hi(ff a) { return fabsf(a.hi); }
+
 // FP64 choice of k_advect in x (tile_differences with the X column
-// offsets, then eno_left / eno_right's magnitude test).
-__device__ __noinline__ bool pick_x64(const double (*tile)[AROWS][ACOLS], const double *xo, int f, int ty, int tx,
-                                      bool from_left) {
+// offsets, then eno_left / eno_right's magnitude test): true where it takes
+// the outer second difference.
+__device__ __noinline__ bool pick_x64(const double (*tile)[AROWS][ACOLS], const int *xs, double lx, int f, int ty,
+                                      int tx, bool from_left) {
     const int r = ty + 2, c0 = from_left ? tx : tx + 1;  // tile columns c0 .. c0+3
     double g[4];
     for (int q = 0; q < 4; q++) {
         g[q] = tile[f][r][c0 + q];
-        if (f == F_X && xo[c0 + q] != 0) g[q] += xo[c0 + q];
+        if (f == F_X && xs[c0 + q] != 0) g[q] += xs[c0 + q] < 0 ? -lx : lx;
     }
     const double da = g[1] - g[0], db = g[2] - g[1], dc = g[3] - g[2];
     // from the left: s0 = S(i) = dc - db, s1 = S(i-1) = db - da;
     // from the right: s0 = S(i) = db - da, s1 = S(i+1) = dc - db
     return from_left ? mag_gt(dc - db, db - da) : mag_gt(db - da, dc - db);
 }
-// FP64 choice in y (rows j0+r-2 .. j0+r-1 for difference r, zero where k_advect's
-// tile_differences leaves it zero).
+// FP64 choice in y (difference r between rows j0+r-2 and j0+r-1, zero where
+// k_advect's tile_differences leaves it zero).
 __device__ __noinline__ bool pick_y64(const double (*tile)[AROWS][ACOLS], int f, int ty, int tx, bool from_below,
                                       int j0, int n) {
     const int r0 = from_below ? ty : ty + 1;  // differences r0 .. r0+2
@@ -447,55 +466,89 @@ __device__ __noinline__ bool pick_y64(const double (*tile)[AROWS][ACOLS], int f,
         const int r = r0 + q, jj = j0 + r - 2;
         d[q] = (jj >= -1 && jj + 1 <= n) ? tile[f][r + 1][tx + 2] - tile[f][r][tx + 2] : 0.0;
     }
-    // from below: s0 = S(j) = d2 - d1, s1 = S(j-1) = d1 - d0;
-    // from above: s0 = S(j) = d1 - d0, s1 = S(j+1) = d2 - d1
     return from_below ? mag_gt(d[2] - d[1], d[1] - d[0]) : mag_gt(d[1] - d[0], d[2] - d[1]);
 }
-__device__ __forceinline__ float eno_x_sp(const adv_smem_sp &Sm, int f, int ty, int tx, bool from_left) {
-    const eno_tile_sp &T = Sm.T;
-    const float *d = T.dx[f][ty], *s = T.sx[f][ty];
-    const int k = tx + 1;
-    const int k1 = from_left ? k - 1 : k + 1;
-    const float s0 = s[k], s1 = s[k1];
-    const float gap = fabsf(fabsf(s0) - fabsf(s1));
-    const int ca = from_left ? k - 1 : k;  // first of the three differences
-    const float *h = T.th[f][ty + 2];
-    const float vmag = fabsf(h[ca]) + fabsf(h[ca + 1]) + fabsf(h[ca + 2]) + fabsf(h[ca + 3]);
-    bool outer;
-    if (gap > tie_margin(d[ca], d[ca + 1], d[ca + 2], vmag)) outer = mag_gtf(s0, s1);
-    else outer = pick_x64(Sm.tile, T.xo, f, ty, tx, from_left);
-    const float sv = outer ? s1 : s0;
-    return from_left ? fmaf(2.f, d[k], sv) : fmaf(-2.f, d[k + 1], sv);
+
+// ENO2 value from three consecutive first differences Da, Db, Dc around the
+// point (Db is the upwind centre difference): from the left (outer = Db - Da)
+// 2 Db + (|Dc - Db| > |Db - Da| ? Db - Da : Dc - Db); from the right
+// (outer = Dc - Db) -2 Db + (|Db - Da| > |Dc - Db| ? Dc - Db : Db - Da).
+// `exact` gives the FP64 path's choice where the high parts cannot decide.
+template <typename Exact>
+__device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float vmag, Exact exact) {
+    const float sl = Db.hi - Da.hi, sr = Dc.hi - Db.hi;
+    const float gap = from_left ? fabsf(sr) - fabsf(sl) : fabsf(sl) - fabsf(sr);
+    // error of the high-part second differences: the low parts (<= 2^-24 of
+    // each difference), the subtraction's rounding and the split (~2^-47 of
+    // the values), with a factor ~8 to spare
+    const float margin = 5e-7f * (ffabs_hi(Da) + 2.f * ffabs_hi(Db) + ffabs_hi(Dc)) + 1e-13f * vmag;
+    const bool outer = fabsf(gap) > margin ? gap > 0.f : exact();
+    // outer: from the left Db - Da, from the right Dc - Db
+    const bool use_ab = from_left == outer;
+    const ff s = use_ab ? ff_sub(Db, Da) : ff_sub(Dc, Db);
+    return ff_add(from_left ? ff_x2(Db) : ff_neg(ff_x2(Db)), s);
 }
-__device__ __forceinline__ float eno_y_sp(const adv_smem_sp &Sm, int f, int ty, int tx, bool from_below, bool inner,
-                                          int j0, int n) {
-    const eno_tile_sp &T = Sm.T;
-    const int ky = ty + 1;
-    const float s0 = T.sy[f][ky][tx];
-    const float dn = from_below ? T.dy[f][ky][tx] : T.dy[f][ky + 1][tx];
-    if (!inner) return from_below ? 2.f * dn : -2.f * dn;
-    const float s1 = from_below ? T.sy[f][ky - 1][tx] : T.sy[f][ky + 1][tx];
-    const int ra = from_below ? ty : ty + 1;  // first of the three differences
-    const float gap = fabsf(fabsf(s0) - fabsf(s1));
-    const float vmag = fabsf(T.th[f][ra][tx + 2]) + fabsf(T.th[f][ra + 1][tx + 2]) + fabsf(T.th[f][ra + 2][tx + 2]) +
-                       fabsf(T.th[f][ra + 3][tx + 2]);
-    bool outer;
-    if (gap > tie_margin(T.dy[f][ra][tx], T.dy[f][ra + 1][tx], T.dy[f][ra + 2][tx], vmag)) outer = mag_gtf(s0, s1);
-    else outer = pick_y64(Sm.tile, f, ty, tx, from_below, j0, n);
-    const float sv = outer ? s1 : s0;
-    return from_below ? fmaf(2.f, dn, sv) : fmaf(-2.f, dn, sv);
+
+__device__ __forceinline__ ff dx_pair(const eno_tile_ff &T, int f, int ty, int c) {
+    return ff{T.dxh[f][ty][c], T.dxl[f][ty][c]};
 }
-// a + b for the FP64 state value a and its FP32 increment b (one FP64 add).
-__device__ __forceinline__ double add_inc(double a, float b) { return a + ff_f2d(b); }
+__device__ __forceinline__ ff dy_pair(const eno_tile_ff &T, int f, int r, int tx) {
+    return ff{T.dyh[f][r][tx], T.dyl[f][r][tx]};
+}
+
+__device__ __forceinline__ ff eno_x_ff(const adv_smem_ff &Sm, int f, int ty, int tx, bool from_left, double lx) {
+    const eno_tile_ff &T = Sm.T;
+    const int c = from_left ? tx : tx + 1;  // differences c .. c+2 (tile columns c .. c+3)
+    const float vmag = fabsf(T.th[f][ty + 2][tx + 2]);
+    return eno_ff(dx_pair(T, f, ty, c), dx_pair(T, f, ty, c + 1), dx_pair(T, f, ty, c + 2), from_left, vmag,
+                  [&] { return pick_x64(Sm.tile, T.xs, lx, f, ty, tx, from_left); });
+}
+// y with the one-sided wall rows: `inner` is false on the last row before
+// the wall on the upwind side (value +-2 Db there).
+__device__ __forceinline__ ff eno_y_ff(const adv_smem_ff &Sm, int f, int ty, int tx, bool from_below, bool inner,
+                                       int j0, int n) {
+    const eno_tile_ff &T = Sm.T;
+    const int r = from_below ? ty : ty + 1;  // differences r .. r+2
+    const ff Db = dy_pair(T, f, r + 1, tx);
+    if (!inner) return from_below ? ff_x2(Db) : ff_neg(ff_x2(Db));
+    const float vmag = fabsf(T.th[f][ty + 2][tx + 2]);
+    return eno_ff(dy_pair(T, f, r, tx), Db, dy_pair(T, f, r + 2, tx), from_below, vmag,
+                  [&] { return pick_y64(Sm.tile, f, ty, tx, from_below, j0, n); });
+}
+
+// -(uh eno_x + vh eno_y)
+__device__ __forceinline__ ff upwind_inc(ff uh, ff ex, ff vh, ff ey) {
+    return ff_neg(ff_add(ff_mul(uh, ex), ff_mul(vh, ey)));
+}
+// a + inc for the FP64 state value a: the high part, then the low part
+__device__ __forceinline__ double add_ff(double a, ff inc) { return (a + ff_f2d(inc.hi)) + ff_f2d(inc.lo); }
 // u > 0 for a finite double, on the integer pipe
 __device__ __forceinline__ bool dpos(double u) { return __double_as_longlong(u) > 0; }
 
+// Float-float pairs of the per-launch constants hx, hy and of the period lx.
+struct advect_ff_consts {
+    float hxh, hxl, hyh, hyl, lxh, lxl;
+};
+
+// Node velocity as float pairs, the walls' +-bv substituted (no FP64 work).
+struct velo_ff {
+    const double2 *vel;
+    int m, n;
+    ff bv;
+    __device__ __forceinline__ ff u(int i, int j) const {
+        return j == 0 ? ff_neg(bv) : (j == n ? bv : split_ff(vel[(size_t)j * m + i].x));
+    }
+    __device__ __forceinline__ ff v(int i, int j) const {
+        return (j == 0 || j == n) ? ff{0.f, 0.f} : split_ff(vel[(size_t)j * m + i].y);
+    }
+};
+
 __global__ void __launch_bounds__(ATX * ATY)
-    k_advect_sp(step_consts c, advect_consts a, const __grid_constant__ field_maps maps, fields_dev F, int cur,
-                double dt, double bv, int emit_source) {
-    extern __shared__ __align__(128) unsigned char adv_raw_sp[];
-    adv_smem_sp &Sm = *reinterpret_cast<adv_smem_sp *>(adv_raw_sp + ((128 - (smem_addr(adv_raw_sp) & 127)) & 127));
-    eno_tile_sp &T = Sm.T;
+    k_advect_ff(step_consts c, advect_ff_consts h, const __grid_constant__ field_maps maps, fields_dev F, int cur,
+                double dt, double bv) {
+    extern __shared__ __align__(128) unsigned char adv_raw_ff[];
+    adv_smem_ff &Sm = *reinterpret_cast<adv_smem_ff *>(adv_raw_ff + ((128 - (smem_addr(adv_raw_ff) & 127)) & 127));
+    eno_tile_ff &T = Sm.T;
     const int m = c.m, n = c.n;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * ATX + tx;
     const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY;
@@ -509,7 +562,7 @@ __global__ void __launch_bounds__(ATX * ATY)
         int w = u % m;
         if (w < 0) w += m;
         T.col[tid] = w;
-        T.xo[tid] = u < 0 ? -c.lx : (u >= m ? c.lx : 0.0);
+        T.xs[tid] = u < 0 ? -1 : (u >= m ? 1 : 0);
     }
     __syncthreads();
     if (tid == 0) {
@@ -531,114 +584,108 @@ __global__ void __launch_bounds__(ATX * ATY)
         }
         __syncthreads();
     }
-    // split every staged value (X unwrapped across the seam first)
+    // split every staged value into a float pair
     for (int k = tid; k < kTileVals; k += ATX * ATY) {
         const int f = k / (AROWS * ACOLS), rem = k - f * (AROWS * ACOLS), r = rem / ACOLS, t = rem - r * ACOLS;
-        double v = Sm.tile[f][r][t];
-        if (f == F_X && T.xo[t] != 0) v += T.xo[t];
-        ff_split_d(v, T.th[f][r][t], T.tl[f][r][t]);
+        ff_split_d(Sm.tile[f][r][t], T.th[f][r][t], T.tl[f][r][t]);
     }
     __syncthreads();
-    // first differences: x on cell rows j0..j0+ATY-1, y on rows j0-2..j0+ATY+1
+    // first differences: x on cell rows j0..j0+ATY-1, y on rows j0-2..j0+ATY+1;
+    // X across the periodic seam gets the period (the unwrapped difference)
+    const ff lx{h.lxh, h.lxl};
     for (int k = tid; k < F_COUNT * ATY * ADXW; k += ATX * ATY) {
         const int f = k / (ATY * ADXW), rem = k - f * (ATY * ADXW), r = rem / ADXW, cc = rem - r * ADXW;
-        float d = 0.f;
-        if (j0 + r < n) d = ff_diff(T.th[f][r + 2][cc + 1], T.tl[f][r + 2][cc + 1], T.th[f][r + 2][cc], T.tl[f][r + 2][cc]);
-        T.dx[f][r][cc] = d;
+        ff d{0.f, 0.f};
+        if (j0 + r < n) {
+            d = ff_pair_diff(T.th[f][r + 2][cc + 1], T.tl[f][r + 2][cc + 1], T.th[f][r + 2][cc], T.tl[f][r + 2][cc]);
+            const int sh = T.xs[cc + 1] - T.xs[cc];
+            if (f == F_X && sh != 0) d = ff_add(d, sh > 0 ? lx : ff_neg(lx));
+        }
+        T.dxh[f][r][cc] = d.hi;
+        T.dxl[f][r][cc] = d.lo;
     }
     for (int k = tid; k < F_COUNT * ADYH * ATX; k += ATX * ATY) {
         const int f = k / (ADYH * ATX), rem = k - f * (ADYH * ATX), r = rem / ATX, cc = rem - r * ATX;
         const int jj = j0 + r - 2;
-        float d = 0.f;
+        ff d{0.f, 0.f};
         if (jj >= -1 && jj + 1 <= n && i0 + cc < m)
-            d = ff_diff(T.th[f][r + 1][cc + 2], T.tl[f][r + 1][cc + 2], T.th[f][r][cc + 2], T.tl[f][r][cc + 2]);
-        T.dy[f][r][cc] = d;
-    }
-    __syncthreads();
-    for (int k = tid; k < F_COUNT * ATY * ASXW; k += ATX * ATY) {
-        const int f = k / (ATY * ASXW), rem = k - f * (ATY * ASXW), r = rem / ASXW, cc = rem - r * ASXW;
-        T.sx[f][r][cc] = T.dx[f][r][cc + 1] - T.dx[f][r][cc];
-    }
-    for (int k = tid; k < F_COUNT * ASYH * ATX; k += ATX * ATY) {
-        const int f = k / (ASYH * ATX), rem = k - f * (ASYH * ATX), r = rem / ATX, cc = rem - r * ATX;
-        T.sy[f][r][cc] = T.dy[f][r + 1][cc] - T.dy[f][r][cc];
+            d = ff_pair_diff(T.th[f][r + 1][cc + 2], T.tl[f][r + 1][cc + 2], T.th[f][r][cc + 2], T.tl[f][r][cc + 2]);
+        T.dyh[f][r][cc] = d.hi;
+        T.dyl[f][r][cc] = d.lo;
     }
     __syncthreads();
     if (i >= m || j >= n) return;
-    const float hx = (float)a.hx, hy = (float)a.hy;
+    const ff hx{h.hxh, h.hxl}, hy{h.hyh, h.hyl};
     const size_t ci = (size_t)(j + 1) * m + i;
     const int ir = T.col[tx + 3];
     if (c.clock) bv = c.clock[CLK_BV_STATE];
-    velo V{F.vel, m, n, bv};
+    const velo_ff V{F.vel, m, n, split_ff(bv)};
     // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
     if (j > 0) {
-        const double un = V.u(i, j), vn = V.v(i, j);
-        const bool ru = dpos(un), rv = dpos(vn);
-        const float uh = ff_hi(un) * (ru ? hx : -hx), vh = ff_hi(vn) * (rv ? hy : -hy);
+        const ff un = V.u(i, j), vn = V.v(i, j);
+        const bool ru = un.hi > 0.f, rv = vn.hi > 0.f;
+        const ff uh = ff_mul(un, ru ? hx : ff_neg(hx)), vh = ff_mul(vn, rv ? hy : ff_neg(hy));
         const bool inner = rv ? j > 1 : j < n - 1;
-        const float ex_X = eno_x_sp(Sm, F_X, ty, tx, ru), ex_Y = eno_x_sp(Sm, F_Y, ty, tx, ru);
-        const float ey_X = eno_y_sp(Sm, F_X, ty, tx, rv, inner, j0, n),
-                    ey_Y = eno_y_sp(Sm, F_Y, ty, tx, rv, inner, j0, n);
-        B[F_X][ci] = add_inc(Sm.tile[F_X][ty + 2][tx + 2], fmaf(-vh, ey_X, -uh * ex_X));
-        B[F_Y][ci] = add_inc(Sm.tile[F_Y][ty + 2][tx + 2], fmaf(-vh, ey_Y, -uh * ex_Y));
-    }
-    // staggered velocity and spin (shear_sim.cc:330-333): the velocity
-    // differences in FP64, everything after them in FP32
-    const double u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
-    const double v00 = V.v(i, j), v10 = V.v(ir, j), v01 = V.v(i, j + 1), v11 = V.v(ir, j + 1);
-    const float uc = 0.25f * ((ff_hi(u00) + ff_hi(u10)) + (ff_hi(u01) + ff_hi(u11)));
-    const float vc = 0.25f * ((ff_hi(v00) + ff_hi(v10)) + (ff_hi(v01) + ff_hi(v11)));
-    const float two_omega = hx * (ff_hi(v10 - v00) + ff_hi(v11 - v01)) - hy * (ff_hi(u01 - u00) + ff_hi(u11 - u10));
-    const bool ru = uc > 0.f, rv = vc > 0.f;
-    const float uh = uc * (ru ? hx : -hx), vh = vc * (rv ? hy : -hy);
-    float f1[5], f2[5];
-    const bool inner = rv ? j > 0 : j < n - 1;
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
-        f1[k] = eno_x_sp(Sm, k, ty, tx, ru);
-        f2[k] = eno_y_sp(Sm, k, ty, tx, rv, inner, j0, n);
+        for (int f = F_X; f <= F_Y; f++) {
+            const ff ex = eno_x_ff(Sm, f, ty, tx, ru, c.lx), ey = eno_y_ff(Sm, f, ty, tx, rv, inner, j0, n);
+            B[f][ci] = add_ff(Sm.tile[f][ty + 2][tx + 2], upwind_inc(uh, ex, vh, ey));
+        }
     }
-    const double p = Sm.tile[F_P][ty + 2][tx + 2], q = Sm.tile[F_Q][ty + 2][tx + 2];
-    const double s = Sm.tile[F_S][ty + 2][tx + 2], t = Sm.tile[F_TAU][ty + 2][tx + 2];
-    double cchi = add_inc(Sm.tile[F_CHI][ty + 2][tx + 2], fmaf(-vh, f2[4], -uh * f1[4])), ddev, dtmp;
-    const double devsq = fma(3 * q, q, fma(s, s, t * t));
+    // staggered velocity and spin (shear_sim.cc:330-333) in pairs
+    const ff u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
+    const ff v00 = V.v(i, j), v10 = V.v(ir, j), v01 = V.v(i, j + 1), v11 = V.v(ir, j + 1);
+    ff uc = ff_add(ff_add(u00, u10), ff_add(u01, u11)), vc = ff_add(ff_add(v00, v10), ff_add(v01, v11));
+    uc = ff{0.25f * uc.hi, 0.25f * uc.lo};
+    vc = ff{0.25f * vc.hi, 0.25f * vc.lo};
+    const ff two_omega = ff_sub(ff_mul(hx, ff_add(ff_sub(v10, v00), ff_sub(v11, v01))),
+                                ff_mul(hy, ff_add(ff_sub(u01, u00), ff_sub(u11, u10))));
+    const bool ru = uc.hi > 0.f, rv = vc.hi > 0.f;
+    const ff uh = ff_mul(uc, ru ? hx : ff_neg(hx)), vh = ff_mul(vc, rv ? hy : ff_neg(hy));
+    const bool inner = rv ? j > 0 : j < n - 1;
+    auto inc_of = [&](int f) {
+        return upwind_inc(uh, eno_x_ff(Sm, f, ty, tx, ru, c.lx), vh, eno_y_ff(Sm, f, ty, tx, rv, inner, j0, n));
+    };
+    const ff qf{T.th[F_Q][ty + 2][tx + 2], T.tl[F_Q][ty + 2][tx + 2]};
+    const ff sf{T.th[F_S][ty + 2][tx + 2], T.tl[F_S][ty + 2][tx + 2]};
+    const ff tf{T.th[F_TAU][ty + 2][tx + 2], T.tl[F_TAU][ty + 2][tx + 2]};
+    double cchi = add_ff(Sm.tile[F_CHI][ty + 2][tx + 2], inc_of(F_CHI)), ddev = 0, dtmp = 0;
+    // Yield test: 3q^2 + s^2 + tau^2 in pairs (relative error ~2^-44); a cell
+    // clearly below the cut-offs of k_advect (1e-24, or an athermal law below
+    // yield) is elastic there too; any other cell takes k_advect's FP64 path.
+    const ff dsq = ff_add(ff_mul(ff{3.f, 0.f}, ff_mul(qf, qf)), ff_add(ff_mul(sf, sf), ff_mul(tf, tf)));
+    const float dv = dsq.hi + dsq.lo;
     const bool athermal = c.stz_model >= 2;
-    const long long dbits = __double_as_longlong(devsq);
-    if (dbits < __double_as_longlong(0.999e-24) || (athermal && dbits < __double_as_longlong(c.yield_cut2))) {
-        ddev = 0;
-        dtmp = 0;
-    } else {
-        int iters;
-        const stz_law_params<double> lp = law_params(c);
-        dtmp = adaptive_plastic(lp, sqrt(devsq), cchi, ddev, dt, iters);
-        if (iters >= c.substep_cap) atomicExch(&F.flags[FL_SUBSTEP_CAP], 1);
-        if (iters > 1) atomicMax(&F.flags[FL_SUBSTEP_MAX], iters);
+    const bool clearly_elastic = dv < 0.999e-24f * (1.f - 1e-6f) || (athermal && dv < c.yield_cut2f);
+    if (!clearly_elastic) {
+        const double q = Sm.tile[F_Q][ty + 2][tx + 2], s = Sm.tile[F_S][ty + 2][tx + 2],
+                     t = Sm.tile[F_TAU][ty + 2][tx + 2];
+        const double devsq = 3 * q * q + s * s + t * t;
+        const long long dbits = __double_as_longlong(devsq);
+        if (!(dbits < __double_as_longlong(0.999e-24) ||
+              (athermal && dbits < __double_as_longlong(c.yield_cut2)))) {
+            int iters;
+            const stz_law_params<double> lp = law_params(c);
+            dtmp = adaptive_plastic(lp, sqrt(devsq), cchi, ddev, dt, iters);
+            if (iters >= c.substep_cap) atomicExch(&F.flags[FL_SUBSTEP_CAP], 1);
+            if (iters > 1) atomicMax(&F.flags[FL_SUBSTEP_MAX], iters);
+        }
     }
     B[F_CHI][ci] = cchi;
     F.ddev[ci] = ddev;
-    if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
-    const float tf = ff_hi(t), sf = ff_hi(s);
-    const float inc_p = fmaf(-vh, f2[0], -uh * f1[0]), inc_q = fmaf(-vh, f2[1], -uh * f1[1]);
-    const float inc_s = fmaf(two_omega, tf, fmaf(-vh, f2[2], -uh * f1[2]));
-    const float inc_t = fmaf(-two_omega, sf, fmaf(-vh, f2[3], -uh * f1[3]));
-    const double pn = add_inc(p, inc_p);
-    double qn = add_inc(q, inc_q), sn = add_inc(s, inc_s), tn = add_inc(t, inc_t);
+    double qn = add_ff(Sm.tile[F_Q][ty + 2][tx + 2], inc_of(F_Q));
+    double sn = add_ff(Sm.tile[F_S][ty + 2][tx + 2], ff_add(inc_of(F_S), ff_mul(two_omega, tf)));
+    double tn = add_ff(Sm.tile[F_TAU][ty + 2][tx + 2], ff_sub(inc_of(F_TAU), ff_mul(two_omega, sf)));
     if (dtmp != 0) {
-        qn -= dtmp * q;
-        sn -= dtmp * s;
-        tn -= dtmp * t;
+        if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
+        qn -= dtmp * Sm.tile[F_Q][ty + 2][tx + 2];
+        sn -= dtmp * Sm.tile[F_S][ty + 2][tx + 2];
+        tn -= dtmp * Sm.tile[F_TAU][ty + 2][tx + 2];
     }
-    B[F_P][ci] = pn;
+    B[F_P][ci] = add_ff(Sm.tile[F_P][ty + 2][tx + 2], inc_of(F_P));
     B[F_Q][ci] = qn;
     B[F_S][ci] = sn;
     B[F_TAU][ci] = tn;
-    if (emit_source) {
-        const double pq = pn + qn, Aa = pq - sn, Bb = pq + sn;
-        F.pre[0][ci] = a.xf * Aa + a.yf * tn;
-        F.pre[1][ci] = a.xf * Aa - a.yf * tn;
-        F.pre[2][ci] = a.xf * tn - a.yf * Bb;
-        F.pre[3][ci] = a.xf * tn + a.yf * Bb;
-    }
 }
 
 // Explicit step (shear_sim::step_forward, shear_sim.cc:185-276) per cell
@@ -815,6 +862,55 @@ __global__ void k_source(step_consts c, fields_dev F, double xbc_bv) {
     F.src[(size_t)j * m + i] = f;
 }
 
+// The projection source of the float-float path (k_advect_ff writes no
+// per-cell combinations): net_force (shear_sim.cc:447-453) at the interior
+// nodes from the stresses of the four surrounding cells, every cell-to-cell
+// difference formed from float pairs by TwoSum (error ~2^-44 of the
+// difference plus ~2^-47 of the values), then scaled by xf, yf in pairs;
+// the wall rows as k_source.
+struct source_ff_consts {
+    float xfh, xfl, yfh, yfl;
+};
+
+__device__ __forceinline__ ff cell_diff(const double *f, size_t a, size_t b) {
+    float ah, al, bh, bl;
+    ff_split_d(f[a], ah, al);
+    ff_split_d(f[b], bh, bl);
+    return ff_pair_diff(ah, al, bh, bl);
+}
+
+__global__ void k_source_ff(step_consts c, fields_dev F, int cur, source_ff_consts h, double xbc_bv) {
+    const int m = c.m, n = c.n;
+    if (c.clock) {
+        xbc_bv = c.xbc * c.clock[CLK_BV];
+        cur = (int)c.clock[CLK_CUR] ^ 1;  // the state the advection wrote
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j > n) return;
+    double2 out;
+    if (j == 0 || j == n) {
+        out.x = j == 0 ? -xbc_bv : xbc_bv;
+        out.y = 0;
+    } else {
+        const int il = i == 0 ? m - 1 : i - 1;
+        const size_t k0 = IDX(il, j - 1), k1 = IDX(i, j - 1), k2 = IDX(il, j), k3 = IDX(i, j);
+        const double *P = F.f[cur][F_P], *Q = F.f[cur][F_Q], *S = F.f[cur][F_S], *T = F.f[cur][F_TAU];
+        // A = p + q - s, B = p + q + s: x differences of A, y differences of B
+        const ff dAx = ff_add(ff_sub(ff_add(cell_diff(P, k1, k0), cell_diff(Q, k1, k0)), cell_diff(S, k1, k0)),
+                              ff_sub(ff_add(cell_diff(P, k3, k2), cell_diff(Q, k3, k2)), cell_diff(S, k3, k2)));
+        const ff dBy = ff_add(ff_add(ff_add(cell_diff(P, k2, k0), cell_diff(Q, k2, k0)), cell_diff(S, k2, k0)),
+                              ff_add(ff_add(cell_diff(P, k3, k1), cell_diff(Q, k3, k1)), cell_diff(S, k3, k1)));
+        const ff dTy = ff_add(cell_diff(T, k0, k2), cell_diff(T, k1, k3));  // (t0 + t1) - (t2 + t3)
+        const ff dTx = ff_add(cell_diff(T, k0, k1), cell_diff(T, k2, k3));  // (t0 - t1) + (t2 - t3)
+        const ff xf{h.xfh, h.xfl}, yf{h.yfh, h.yfl};
+        const ff fx = ff_add(ff_mul(xf, dAx), ff_mul(yf, dTy)), fy = ff_add(ff_mul(xf, dTx), ff_mul(yf, dBy));
+        out.x = ff_f2d(fx.hi) + ff_f2d(fx.lo);
+        out.y = ff_f2d(fy.hi) + ff_f2d(fy.lo);
+    }
+    F.src[(size_t)j * m + i] = out;
+}
+
 // Stress correction from the solved velocity (shear_sim.cc:418-434).
 __global__ void k_project(step_consts c, fields_dev F, int cur, double hx, double hy) {
     const int m = c.m, n = c.n;
@@ -834,6 +930,37 @@ __global__ void k_project(step_consts c, fields_dev F, int cur, double hx, doubl
     S[F_Q][k] += -c.mu * third * (ux + vy);
     S[F_S][k] += c.mu * (ux - vy);
     S[F_TAU][k] += c.mu * (uy + vx);
+}
+
+// The stress correction of the float-float path: the velocity differences of
+// k_project from float pairs (TwoSum), the products with hx, hy, K, mu/3 and
+// mu in pairs, and each stress component takes its correction with two FP64
+// additions.
+struct project_ff_consts {
+    float hxh, hxl, hyh, hyl, Kh, Kl, m3h, m3l, muh, mul;
+};
+
+__global__ void k_project_ff(step_consts c, fields_dev F, int cur, project_ff_consts h) {
+    const int m = c.m, n = c.n;
+    if (c.clock) cur = (int)c.clock[CLK_CUR] ^ 1;  // the state the advection wrote
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const int ir = i == m - 1 ? 0 : i + 1;
+    const double2 a = F.vel[(size_t)j * m + i], b = F.vel[(size_t)j * m + ir], cu = F.vel[(size_t)(j + 1) * m + i],
+                  d = F.vel[(size_t)(j + 1) * m + ir];
+    const ff ax = split_ff(a.x), bx = split_ff(b.x), cx = split_ff(cu.x), dx = split_ff(d.x);
+    const ff ay = split_ff(a.y), by = split_ff(b.y), cy = split_ff(cu.y), dy = split_ff(d.y);
+    const ff hx{h.hxh, h.hxl}, hy{h.hyh, h.hyl};
+    const ff ux = ff_mul(hx, ff_add(ff_sub(bx, ax), ff_sub(dx, cx))), uy = ff_mul(hy, ff_add(ff_sub(cx, ax), ff_sub(dx, bx)));
+    const ff vx = ff_mul(hx, ff_add(ff_sub(by, ay), ff_sub(dy, cy))), vy = ff_mul(hy, ff_add(ff_sub(cy, ay), ff_sub(dy, by)));
+    const ff div = ff_add(ux, vy);
+    const size_t k = IDX(i, j);
+    double *const *S = F.f[cur];
+    S[F_P][k] = add_ff(S[F_P][k], ff_neg(ff_mul(ff{h.Kh, h.Kl}, div)));
+    S[F_Q][k] = add_ff(S[F_Q][k], ff_neg(ff_mul(ff{h.m3h, h.m3l}, div)));
+    S[F_S][k] = add_ff(S[F_S][k], ff_mul(ff{h.muh, h.mul}, ff_sub(ux, vy)));
+    S[F_TAU][k] = add_ff(S[F_TAU][k], ff_mul(ff{h.muh, h.mul}, ff_add(uy, vx)));
 }
 
 // set_boundaries (shear_sim.cc:552-581): ghost rows by linear extrapolation,
@@ -874,8 +1001,8 @@ cudaError_t prepare_step_kernels() {
     if (dev < 64 && (done >> dev & 1)) return cudaSuccess;
     e = cudaFuncSetAttribute(k_advect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(adv_smem) + 128));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_advect_sp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(adv_smem_sp) + 128));
+        e = cudaFuncSetAttribute(k_advect_ff, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(adv_smem_ff) + 128));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_direct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(direct_tile));
     if (e == cudaSuccess && dev < 64) done |= 1ull << dev;
@@ -922,10 +1049,15 @@ void advection(const step_consts &c, const field_maps &maps, fields_dev &F, int 
     a.xf = 0.5 / dt * c.xsp;
     a.yf = 0.5 / dt * c.ysp;
     const dim3 grid(ceil_div(c.m, ATX), ceil_div(c.n, ATY));
-    if (c.sp_increments)
-        k_advect_sp<<<grid, dim3(ATX, ATY), sizeof(adv_smem_sp) + 128, st>>>(c, a, maps, F, cur, dt, bv, 1);
-    else
+    if (c.sp_increments) {
+        advect_ff_consts h;
+        split_host(a.hx, &h.hxh, &h.hxl);
+        split_host(a.hy, &h.hyh, &h.hyl);
+        split_host(c.lx, &h.lxh, &h.lxl);
+        k_advect_ff<<<grid, dim3(ATX, ATY), sizeof(adv_smem_ff) + 128, st>>>(c, h, maps, F, cur, dt, bv);
+    } else {
         k_advect<<<grid, dim3(ATX, ATY), sizeof(adv_smem) + 128, st>>>(c, a, maps, F, cur, dt, bv, 1);
+    }
     note_launch();
     if (c.chi_diff != 0 || c.chi_len != 0) {
         k_chi_diffusion<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, dt);
@@ -957,13 +1089,19 @@ void direct_step(const step_consts &c, double viscosity, fields_dev &F, int cur,
 
 void projection_source(const step_consts &c, fields_dev &F, int cur, double dt, double xbc_bv, cudaStream_t st) {
     dim3 blk(32, 8);
-    k_source<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, xbc_bv);
+    if (c.sp_increments) {
+        source_ff_consts h;
+        split_host(0.5 / dt * c.xsp, &h.xfh, &h.xfl);
+        split_host(0.5 / dt * c.ysp, &h.yfh, &h.yfl);
+        k_source_ff<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, cur, h, xbc_bv);
+    } else {
+        k_source<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, xbc_bv);
+    }
     note_launch();
-    (void)cur;
-    (void)dt;
 }
 
 void precombine(const step_consts &c, fields_dev &F, int cur, double dt, cudaStream_t st) {
+    if (c.sp_increments) return;  // k_source_ff reads the stresses themselves
     dim3 blk(32, 8);
     k_precombine<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, 0.5 / dt * c.xsp, 0.5 / dt * c.ysp);
     note_launch();
@@ -973,7 +1111,18 @@ void projection_apply(const step_consts &c, fields_dev &F, int cur, double dt, d
                       cudaStream_t st) {
     dim3 blk(32, 8);
     const double hx = 0.5 * c.xsp * dt, hy = 0.5 * c.ysp * dt;
-    k_project<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, hx, hy); note_launch();
+    if (c.sp_increments) {
+        project_ff_consts h;
+        split_host(hx, &h.hxh, &h.hxl);
+        split_host(hy, &h.hyh, &h.hyl);
+        split_host(c.K, &h.Kh, &h.Kl);
+        split_host(c.mu * (1 / 3.0), &h.m3h, &h.m3l);
+        split_host(c.mu, &h.muh, &h.mul);
+        k_project_ff<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, h);
+    } else {
+        k_project<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, hx, hy);
+    }
+    note_launch();
     k_boundaries<<<ceil_div(c.m, 128), 128, 0, st>>>(c, F, cur, bp); note_launch();
     (void)bv;
 }

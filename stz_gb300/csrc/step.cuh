@@ -43,12 +43,13 @@ struct step_consts {
     int track_plastic;
     int substep_cap;
     double yield_cut2;  // s_y^2 (1 - 1e-12): athermal cells below it skip the plastic loop
+    float yield_cut2f;  // the same lowered by 1e-6, for the float-float path's test
     // Device clock of a graph-driven run (nullptr: wall quantities come as
     // kernel arguments from the host).  Layout: CLK_* below.
     const double *clock;
     double xbc;  // bcs*cxx of the projection operator (wall source = -+xbc*bv)
-    // advection with FP32 differences and increments on the FP64 state
-    // (mixed-precision handles); 0: all FP64, bit-exact
+    // advection, projection source and stress correction in float-float on
+    // the FP64 state (mixed-precision handles); 0: all FP64, bit-exact
     int sp_increments;
 };
 
@@ -58,6 +59,8 @@ struct step_consts {
 enum { CLK_TIME = 0, CLK_BV_STATE = 1, CLK_BV = 2, CLK_BP = 3, CLK_CUR = 4, CLK_COUNT = 5 };
 
 step_consts make_step_consts(const stz_params &p);
+// x as a float pair hi + lo (host).
+void split_host(double x, float *hi, float *lo);
 
 // |a| > |b| for finite doubles, compared as the magnitudes of their IEEE bit
 // patterns on the integer pipe (same result as fabs(a) > fabs(b)).

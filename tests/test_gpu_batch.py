@@ -58,3 +58,32 @@ def test_batch_runs_continue_and_autotune():
     assert abs(b.sim(2).time - ref.time) < 1e-12
     err = group_errors(ref.fields(), b.sim(2).fields(), ps[2].n)
     assert max(err.values()) < 1e-8, err
+
+
+@pytest.mark.parametrize("precision", [_lib.MIXED, _lib.FP64])
+def test_batch_config3_sizes_against_oracle(precision):
+    """Members of the batched configuration's grid sizes (192, 256, 384 and
+    512: odd periodic lines in the 192 and 384 hierarchies) with their own
+    chi and STZ parameters, run together in one graph, each against the CPU
+    oracle from the same state (both solved to a relative residual of 1e-12;
+    gate 1e-10 FP64, 1e-8 mixed)."""
+    from oracle.bind import OracleSim
+    sizes = [192, 256, 384, 512]
+    rng = np.random.default_rng(3)
+    ps, chis = [], []
+    for k, N in enumerate(sizes):
+        p = simple_shear(N, c0=float(rng.uniform(0.2, 0.6)), chi_inf_K=float(rng.uniform(800, 1000)))
+        ps.append(p)
+        chis.append(random_chi(N, N, 4, 600.0, float(rng.uniform(10, 50)), p.TZ, 60 + k))
+    steps, dt = 5, 0.01
+    b = Batch(ps, chis, precision=precision, tol=1e-12)
+    st = b.run(dt, steps)
+    assert st.failed == 0 and st.steps == steps * len(ps)
+    gate = 1e-10 if precision == _lib.FP64 else 1e-8
+    for k, (p, chi) in enumerate(zip(ps, chis)):
+        o = OracleSim(p, chi)
+        o.set_tolerance(1, 1e-13)
+        o.steps(dt, steps)
+        err = group_errors(o.fields(), b.sim(k).fields(), p.n)
+        assert max(err.values()) < gate, (sizes[k], err)
+    b.close()

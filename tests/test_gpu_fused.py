@@ -102,23 +102,26 @@ def test_streaming_runs_are_deterministic():
         assert np.array_equal(runs[0][k], runs[1][k]), k
 
 
-@pytest.mark.parametrize("case", ["elastic256"])
-def test_fp32_increment_advection(case):
-    """Mixed-precision handles can advect with FP32 ENO differences and
-    increments on the FP64 state (stzg_options.advection = STZG_ADV_SPLIT).
-    Against the same handle with FP64 advection and against the oracle, the
-    group-normalised error stays inside the mixed-precision gate (1e-8), on
-    an elastic run and on plastic-active runs (ENO choices, upwind switches
-    and the plastic law all exercised)."""
+@pytest.mark.parametrize("case", ["elastic256", "plastic128", "plastic_rect160x96", "plastic64_cfl06"])
+def test_float_float_advection(case):
+    """Mixed-precision handles advect, form the projection source and correct
+    the stresses in float-float arithmetic on the FP64 state (the default,
+    STZG_ADV_AUTO).  Against the same handle with FP64 advection
+    (STZG_ADV_FP64) and against the oracle, the group-normalised error stays
+    inside the mixed-precision gate (1e-8): an elastic run, plastic-active
+    runs (ENO choices, upwind switches, the plastic law) and a run at CFL 0.64
+    over 60 steps, where the reference-map increments are largest."""
     if case == "elastic256":
         P, steps = simple_shear(256), 60
     elif case == "plastic128":
         P, steps = plastic_shear(128, u_bdry=1.0), 40
+    elif case == "plastic64_cfl06":
+        P, steps = plastic_shear(64, u_bdry=2.0), 60
     else:
         P, steps = plastic_shear(160, 96, u_bdry=1.0), 40
     N, M = P.m, P.n
     chi = random_chi(N, M, 4, 600.0, 30.0, P.TZ, 21)
-    sp = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-12, advection=_lib.ADV_SPLIT)
+    sp = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-12)
     dp = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-12, advection=_lib.ADV_FP64)
     sp.steps(0.01, steps)
     dp.steps(0.01, steps)
