@@ -84,6 +84,43 @@ int stzg_ct_tracers_init(stzg_ct *s, int mm, int nn);
 int stzg_ct_tracers_update(stzg_ct *s, int *lost);
 int stzg_ct_tracers_get(stzg_ct *s, double *out, int cap, int *count);
 
+/* Frames and diagnostics.  stzg_ct_compute_strain: shear_sim::compute_strain
+ * (shear_sim.cc:1008-1059) with set_strain_boundaries (:814-850): per cell the
+ * Green-Lagrange strain of the physical deformation (the sheared grid's
+ * (1 lt; 0 1) applied to the inverse reference-map gradient): out holds six
+ * arrays of rows 0..n (m each): E_xx, E_xy, E_yy, the trace, the second
+ * invariant and the deviatoric norm.  stzg_ct_output_field: shear_sim::output
+ * (shear_sim.cc:937-1004) of one mode (0 u, 1 v, 2 p, 3 q, 4 s, 5 tau, 6 chi,
+ * 7 chi*TZ, 8 the untransformed deviatoric norm, 9 X, 10 Y, 11-16 the six
+ * strain values) as the Gnuplot binary matrix the reference writes (header
+ * row, then rows led by their y); *count receives the number of floats, out
+ * may be NULL to query it.  stzg_ct_write_frame: shear_sim::write_files
+ * (shear_sim.cc:892-931) into dir with the reference's flags (bit k: mode k
+ * for k <= 10, dev always; 2048 Exx, Exy, Eyy; 4096 E_I, E_II, Edev; 8192
+ * the tracers: update them when frame > 0, then tra.<frame> (text: position,
+ * reference point, p, chi, chi*TZ and the six strain values by bicubic
+ * interpolation) and teml.<frame> (chi*TZ on the tracer grid)); files are
+ * <dir>/<name>.<frame>, byte for byte the reference's for the same state.
+ * stzg_ct_solve_quasistatic / stzg_ct_solve: the frame loops of
+ * shear_sim::solve_quasistatic (shear_sim.cc:175-202) and shear_sim::solve
+ * (:133-172): frame 0 (quasi-static: only on the handle's first loop), then
+ * per frame the steps and the frame's files; verbose prints the reference's
+ * frame lines. */
+int stzg_ct_compute_strain(stzg_ct *s, double *out);
+int stzg_ct_output_field(stzg_ct *s, int mode, float *out, long *count);
+int stzg_ct_write_frame(stzg_ct *s, const char *dir, int frame, unsigned fflags);
+int stzg_ct_solve_quasistatic(stzg_ct *s, double duration, int frames, int steps, const char *dir,
+                              unsigned fflags, int verbose);
+int stzg_ct_solve(stzg_ct *s, double duration, int frames, const char *dir, unsigned fflags, int verbose);
+/* shear_sim::l2_comparison_transform (shear_sim.cc:619-711): s in the
+ * sheared frame against phys in the physical frame (lamb = 0, same grid):
+ * phys's u, v, p, q, s, tau, chi interpolated bilinearly (bilin_interp,
+ * :713-736) at the sheared node positions; l2[4] = velocity, stress, chi,
+ * reference map, with the reference's weights, times dx dy.  A shift past
+ * the ghost columns (where the reference reads outside its arrays) gives
+ * STZG_EINVAL. */
+int stzg_ct_l2_comparison_transform(stzg_ct *s, stzg_ct *phys, double *l2);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,6 +42,8 @@ def _load():
         L.ctref_destroy.argtypes = [V]
         L.ctref_init_fields.argtypes = [V, I, D, D]
         L.ctref_chi_bicubic.argtypes = [V, I, I, _P, D, D]
+        L.ctref_write_files.argtypes = [V, ctypes.c_char_p, I, ctypes.c_uint]
+        L.ctref_l2_comparison_transform.argtypes = [V, V, _P]
         L.ctref_get_field.argtypes = [V, I, _P]
         L.ctref_set_field.argtypes = [V, I, _P]
         L.ctref_steps.argtypes = [V, D, I]
@@ -78,6 +80,14 @@ class ReferenceCt:
 
     def init_fields(self, chi_case, base, delta):
         self.L.ctref_init_fields(self.h, chi_case, base, delta)
+
+    def l2_comparison_transform(self, phys):
+        out = np.zeros(4)
+        self.L.ctref_l2_comparison_transform(self.h, phys.h, out.ctypes.data_as(_P))
+        return out
+
+    def write_files(self, directory, k, fflags):
+        self.L.ctref_write_files(self.h, str(directory).encode(), k, fflags)
 
     def chi_bicubic(self, arr, lo, sca):
         a = np.ascontiguousarray(arr, dtype=np.float64)

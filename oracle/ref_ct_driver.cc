@@ -84,6 +84,20 @@ void ctref_chi_bicubic(void *vh, int mm, int nn, const double *arr, double lo, d
     ((ct_handle *)vh)->sim->initialize_chi_bicubic(mm, nn, a.data(), lo, sca);
 }
 
+// shear_sim::write_files(k) (shear_sim.cc:892-931) into dir with the given
+// output flags (both are constructor settings in the reference).
+void ctref_write_files(void *vh, const char *dir, int k, unsigned fflags) {
+    shear_sim &s = *((ct_handle *)vh)->sim;
+    const_cast<unsigned int &>(s.fflags) = fflags;
+    s.filename = dir;
+    s.write_files(k);
+}
+
+// shear_sim::l2_comparison_transform (shear_sim.cc:619-711) of two reference runs.
+void ctref_l2_comparison_transform(void *vt, void *vp, double *l2) {
+    ((ct_handle *)vt)->sim->l2_comparison_transform(*((ct_handle *)vp)->sim, l2);
+}
+
 void ctref_get_field(void *vh, int id, double *out) {
     shear_sim &s = *((ct_handle *)vh)->sim;
     for (int j = 0; j <= s.n; j++)

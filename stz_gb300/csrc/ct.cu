@@ -15,6 +15,8 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <cstdio>
+#include <string>
 #include <vector>
 
 #include "common.cuh"
@@ -512,6 +514,8 @@ struct stzg_ct {
     double *tr = nullptr;
     int *tr_ok = nullptr;
     int ntrace = 0, tr_cap = 0;
+    int tr_m = 0, tr_n = 0;  // the tracer grid of the last stzg_ct_tracers_init
+    int f_num = 0;           // frames written by the frame loops (shear_sim::f_num)
     double tr_time = 0;
 };
 
@@ -617,6 +621,276 @@ int projection_step(stzg_ct *s, double dt, long *vcycles) {
     k_ct_project<<<g2(s->c.m, s->c.n), kB2, 0, s->st>>>(s->c, s->F, s->cur, s->mg_z, dt, lt);
     note_launch();
     boundaries(s, s->cur);
+    return STZG_OK;
+}
+
+// ---- frames, strain and tracer files (shear_sim.cc:892-1059, 1360-1420) ----
+// Frames are written from a host copy of the ghosted arrays; the arithmetic
+// restates the reference's expressions in its order (host code is built
+// without floating-point contraction), so files written from the same state
+// hold the same bytes.
+
+// The ghosted host arrays of the current state: u, v, p, q, s, tau, chi, X,
+// Y, then the six strain values (cu, cv, cp, cq, cs, ctau of the reference's
+// c_field after compute_strain).
+struct ct_host {
+    int m, n, gm, gn;
+    std::vector<double> f[CF + 6];
+    size_t at(int i, int j) const { return (size_t)(j + 2) * gm + (i + 2); }  // i, j >= -2
+};
+
+int ct_fetch(stzg_ct *s, ct_host &h) {
+    const ct_consts &c = s->c;
+    h.m = c.m;
+    h.n = c.n;
+    h.gm = c.gm;
+    h.gn = c.n + 4;
+    const size_t pts = (size_t)h.gm * h.gn;
+    for (int f = 0; f < CF; f++) {
+        h.f[f].resize(pts);
+        STZG_CUDA(cudaMemcpyAsync(h.f[f].data(), s->F.f[s->cur][f], pts * sizeof(double), cudaMemcpyDeviceToHost,
+                                  s->st));
+    }
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    return STZG_OK;
+}
+
+// shear_sim::compute_strain (shear_sim.cc:1008-1059): the Green-Lagrange
+// strain of the physical deformation gradient T * (d(X,Y)/d(x,y))^-1, T = (1
+// lt; 0 1), with its components (E_xx, E_xy, E_yy), trace, second invariant
+// and deviatoric norm per cell, then set_strain_boundaries
+// (shear_sim.cc:814-850): ghost rows extrapolated (walls) or periodic, ghost
+// columns periodic.
+void ct_strain(const stzg_ct *s, ct_host &h, double lt) {
+    const ct_consts &c = s->c;
+    const int m = h.m, n = h.n;
+    double *E6[6];
+    for (int k = 0; k < 6; k++) {
+        h.f[CF + k].assign((size_t)h.gm * h.gn, 0.0);
+        E6[k] = h.f[CF + k].data();
+    }
+    const double *X = h.f[CX].data(), *Y = h.f[CY].data();
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            const size_t k = h.at(i, j);
+            const double Xy = 0.5 * c.ysp * (X[k + h.gm] - X[k - h.gm]), Yy = 0.5 * c.ysp * (Y[k + h.gm] - Y[k - h.gm]);
+            const double Xx = 0.5 * c.xsp * (X[k + 1] - X[k - 1]), Yx = 0.5 * c.xsp * (Y[k + 1] - Y[k - 1]);
+            const double J = 1 / (Xx * Yy - Xy * Yx);
+            const double ma = Yy * J, mb = -Xy * J, mc = -Yx * J, md = Xx * J;
+            // T * M with T = (1 lt; 0 1), in the order of mat::operator*
+            const double Fa = 1 * ma + lt * mc, Fb = 1 * mb + lt * md, Fc = 0 * ma + 1 * mc, Fd = 0 * mb + 1 * md;
+            // E = (F^T F - I) / 2 (mat::ATA)
+            double ea = Fa * Fa + Fc * Fc, eb = Fa * Fb + Fc * Fd, ed = Fb * Fb + Fd * Fd;
+            ea -= 1.;
+            ed -= 1.;
+            ea *= 0.5;
+            eb *= 0.5;
+            ed *= 0.5;
+            E6[0][k] = ea;
+            E6[1][k] = eb;
+            E6[2][k] = ed;
+            const double tr = ea + ed;
+            E6[3][k] = tr;
+            E6[4][k] = ea * ed - eb * eb;
+            const double tfac = 1 / 3. * tr;
+            ea -= tfac;
+            ed -= tfac;
+            E6[5][k] = std::sqrt(ea * ea + 2 * eb * eb + ed * ed + tfac * tfac);
+        }
+    auto copy6 = [&](size_t to, size_t from) {
+        for (int q = 0; q < 6; q++) E6[q][to] = E6[q][from];
+    };
+    for (int i = 0; i < m; i++) {
+        if (c.yp) {
+            copy6(h.at(i, -2), h.at(i, n - 2));
+            copy6(h.at(i, -1), h.at(i, n - 1));
+            copy6(h.at(i, n), h.at(i, 0));
+            copy6(h.at(i, n + 1), h.at(i, 1));
+        } else {
+            for (int q = 0; q < 6; q++) {
+                double *e = E6[q];
+                e[h.at(i, -1)] = 2 * e[h.at(i, 0)] - e[h.at(i, 1)];
+                e[h.at(i, -2)] = 2 * e[h.at(i, -1)] - e[h.at(i, 0)];
+                e[h.at(i, n)] = 2 * e[h.at(i, n - 1)] - e[h.at(i, n - 2)];
+                e[h.at(i, n + 1)] = 2 * e[h.at(i, n)] - e[h.at(i, n - 1)];
+            }
+        }
+    }
+    for (int j = -2; j < n + 2; j++) {
+        copy6(h.at(-2, j), h.at(m - 2, j));
+        copy6(h.at(-1, j), h.at(m - 1, j));
+        copy6(h.at(m, j), h.at(0, j));
+        copy6(h.at(m + 1, j), h.at(1, j));
+    }
+}
+
+// c_field::dev(lt) (fields.hh): the deviatoric norm of the untransformed stress
+double ct_dev(const ct_host &h, size_t k, double lt) {
+    const double p = h.f[CP][k], q = h.f[CQ][k], s = h.f[CS][k], tau = h.f[CTAU][k];
+    const double unt_tau = tau - lt * (p + q + s);
+    const double unt_q = q + lt * (1 / 3.) * (-tau + lt * .5 * (p + q + s));
+    const double unt_s = s + lt * (tau - lt * .5 * (p + q + s));
+    return std::sqrt(3 * unt_q * unt_q + unt_s * unt_s + unt_tau * unt_tau);
+}
+
+// shear_sim::output (shear_sim.cc:937-1004) of one mode into out: staggered
+// modes 2-8 on n rows of m cell centres; the others on n (y periodic) or n+1
+// rows of m nodes, plus (walls) the periodic copy of the first node, shifted
+// by the period for X.  Each row is led by its y coordinate, the header row
+// by the row length and the x coordinates.
+void ct_output(const stzg_ct *s, const ct_host &h, int mode, std::vector<float> &out) {
+    const ct_consts &c = s->c;
+    const int m = h.m, n = h.n;
+    const bool st = mode >= 2 && mode <= 8;
+    const int l = st ? m : (c.yp ? m : m + 1);
+    const int rows = st ? n : (c.yp ? n : n + 1);
+    const double lt = c.lamb * s->time;
+    out.assign((size_t)(rows + 1) * (l + 1), 0.f);
+    std::vector<float> buf(m + 2);
+    buf[0] = (float)l;
+    for (int i = 0; i < l; i++) buf[i + 1] = (float)(c.ax + (st ? (i + 0.5) * c.dx : i * c.dx));
+    std::copy(buf.begin(), buf.begin() + l + 1, out.begin());
+    for (int j = 0; j < rows; j++) {
+        buf[0] = (float)(c.ay + (st ? (j + 0.5) * c.dy : j * c.dy));
+        for (int i = 0; i < m; i++) {
+            const size_t k = h.at(i, j);
+            double v;
+            switch (mode) {
+                case 7: v = h.f[CCHI][k] * s->P.TZ; break;
+                case 8: v = ct_dev(h, k, lt); break;
+                default: v = mode <= 6 ? h.f[mode][k] : (mode <= 10 ? h.f[mode - 2][k] : h.f[CF + mode - 11][k]);
+            }
+            buf[i + 1] = (float)v;
+        }
+        if (!st) buf[m + 1] = mode == 9 ? (float)(buf[1] + c.bx - c.ax) : buf[1];
+        std::copy(buf.begin(), buf.begin() + l + 1, out.begin() + (size_t)(j + 1) * (l + 1));
+    }
+}
+
+int ct_write_floats(const char *dir, const char *prefix, int sn, const std::vector<float> &v) {
+    char path[4096];
+    std::snprintf(path, sizeof(path), "%s/%s.%d", dir, prefix, sn);
+    std::FILE *fp = std::fopen(path, "wb");
+    if (!fp) return fail(STZG_EINVAL, std::string("cannot open ") + path);
+    const size_t w = std::fwrite(v.data(), sizeof(float), v.size(), fp);
+    std::fclose(fp);
+    if (w != v.size()) return fail(STZG_EINVAL, std::string("short write to ") + path);
+    return STZG_OK;
+}
+
+// bicubic_interp (bi_interp.cc) of field `mode` (fval order: u, v, p, q, s,
+// tau, chi, X, Y, then the six strain values) at (x, y): the cubic
+// convolution through four samples in x on four rows, then across the rows,
+// on the ghosted grid (origin 2 cells before (ax, ay) for the node fields u,
+// v, X, Y, 1.5 cells for the others).  false where the grid square leaves
+// the ghosted grid (the reference stops the program there).  The reference
+// keeps the last grid square's coefficients between calls, stale when the
+// field has changed since; here they are formed anew each time.
+bool ct_bicubic(const stzg_ct *s, const ct_host &h, int mode, double x, double y, double *val) {
+    const ct_consts &c = s->c;
+    const bool cor = (1 << mode) & (3 | 384);
+    const double ox = c.ax - (cor ? 2 : 1.5) * c.dx, oy = c.ay - (cor ? 2 : 1.5) * c.dy;
+    x = (x - ox) * c.xsp;
+    y = (y - oy) * c.ysp;
+    const int i = (int)x, j = (int)y;
+    if (i < 1 || i > h.gm - 2 || j < 1 || j > h.gn - 2) return false;
+    const int fi = mode <= 8 ? mode : CF + mode - 9;
+    const double *F = h.f[fi].data();
+    auto cx = [&](int jj, double *q) {  // compute_x on ghosted row jj at column i
+        const size_t r = (size_t)jj * h.gm;
+        const double f0 = F[r + i - 1], f1 = F[r + i], f2 = F[r + i + 1], f3 = F[r + i + 2];
+        q[0] = f1;
+        q[1] = -0.5 * f0 + 0.5 * f2;
+        q[2] = f0 - 2.5 * f1 + 2 * f2 - 0.5 * f3;
+        q[3] = -0.5 * f0 + 1.5 * f1 - 1.5 * f2 + 0.5 * f3;
+    };
+    double r0[4], r1[4], r2[4], r3[4], a[16];
+    cx(j, r1);
+    cx(j + 1, r2);
+    cx(j - 1, r0);
+    cx(j + 2, r3);
+    for (int q = 0; q < 4; q++) {  // fill_a over the rows for the x power q
+        double *ap = a + 4 * q;
+        const double c0 = r0[q], c1 = r1[q], c2 = r2[q], c3 = r3[q];
+        ap[0] = c1;
+        ap[1] = -0.5 * c0 + 0.5 * c2;
+        ap[2] = c0 - 2.5 * c1 + 2 * c2 - 0.5 * c3;
+        ap[3] = -0.5 * c0 + 1.5 * c1 - 1.5 * c2 + 0.5 * c3;
+    }
+    x -= i;
+    y -= j;
+    auto yl = [&](const double *ap) { return *ap + y * (ap[1] + y * (ap[2] + y * ap[3])); };
+    *val = yl(a) + x * (yl(a + 4) + x * (yl(a + 8) + x * yl(a + 12)));
+    return true;
+}
+
+// shear_sim::write_files (shear_sim.cc:892-931) into directory dir.
+int ct_write_files(stzg_ct *s, const char *dir, int k, unsigned fflags) {
+    static const char *names[17] = {"u", "v", "p", "q", "s", "tau", "chi", "tem", "dev", "X", "Y",
+                                    "Exx", "Exy", "Eyy", "E_I", "E_II", "Edev"};
+    ct_host h;
+    STZG_CHECK(ct_fetch(s, h));
+    std::vector<float> buf;
+    for (int mode = 0; mode <= 10; mode++)
+        if ((fflags & (1u << mode)) || mode == 8) {  // the reference writes dev whatever the flags
+            ct_output(s, h, mode, buf);
+            STZG_CHECK(ct_write_floats(dir, names[mode], k, buf));
+        }
+    if (fflags & 14336) ct_strain(s, h, s->c.lamb * s->time);
+    for (int mode = 11; mode <= 16; mode++)
+        if (fflags & (mode <= 13 ? 2048u : 4096u)) {
+            ct_output(s, h, mode, buf);
+            STZG_CHECK(ct_write_floats(dir, names[mode], k, buf));
+        }
+    if ((fflags & 8192) && s->tr) {
+        if (k > 0) STZG_CHECK(stzg_ct_tracers_update(s, nullptr));  // the fields stay as fetched
+        std::vector<double> tr((size_t)6 * s->ntrace);
+        if (s->ntrace)
+            STZG_CUDA(cudaMemcpy(tr.data(), s->tr, sizeof(double) * tr.size(), cudaMemcpyDeviceToHost));
+        const ct_consts &c = s->c;
+        const double ilx = 1 / c.lx, ily = 1 / c.ly;
+        // output_tracers (shear_sim.cc:1360-1386)
+        char path[4096];
+        std::snprintf(path, sizeof(path), "%s/tra.%d", dir, k);
+        std::FILE *fp = std::fopen(path, "w");
+        if (!fp) return fail(STZG_EINVAL, std::string("cannot open ") + path);
+        for (int t = 0; t < s->ntrace; t++) {
+            const double *q = &tr[(size_t)6 * t];
+            const double xx = q[2], yy = q[3];
+            const double xw = xx - std::floor((xx - c.ax) * ilx) * c.lx, yw = yy - std::floor((yy - c.ay) * ily) * c.ly;
+            double v[8];
+            const int modes[8] = {2, 6, 9, 10, 11, 12, 13, 14};
+            for (int u = 0; u < 8; u++)
+                if (!ct_bicubic(s, h, modes[u], xw, yw, &v[u])) {
+                    std::fclose(fp);
+                    return fail(STZG_EINVAL, "a tracer left the interpolation grid");
+                }
+            std::fprintf(fp, "%.12g %.12g %.12g %.12g %.12g %.12g %.12g %.10g %.10g %.10g %.10g %.10g %.10g\n", xx, yy,
+                         q[0], q[1], v[0], v[1], v[1] * s->P.TZ, v[2], v[3], v[4], v[5], v[6], v[7]);
+        }
+        std::fclose(fp);
+        // output_tracers_matrix("teml", 4, k) (shear_sim.cc:1389-1420): chi*TZ at each
+        // tracer of the tracer grid
+        if (s->tr_m > c.m + 1) return fail(STZG_EINVAL, "tracer grid wider than the output buffer");
+        if (s->ntrace != s->tr_m * s->tr_n) return fail(STZG_EINVAL, "matrix output after tracers were lost");
+        const double delx = c.lx / s->tr_m, dely = (c.by - c.ay) / s->tr_n;
+        std::vector<float> mat((size_t)(s->tr_n + 1) * (s->tr_m + 1));
+        mat[0] = (float)s->tr_m;
+        for (int i = 0; i < s->tr_m; i++) mat[i + 1] = (float)(c.ax + (i + 0.5) * delx);
+        for (int j = 0; j < s->tr_n; j++) {
+            float *row = &mat[(size_t)(j + 1) * (s->tr_m + 1)];
+            row[0] = (float)(c.ay + (j + 0.5) * dely);
+            for (int i = 0; i < s->tr_m; i++) {
+                const double *q = &tr[(size_t)6 * (j * s->tr_m + i)];
+                const double xx = q[2], xw = xx - std::floor((xx - c.ax) * ilx) * c.lx, yy = q[3],
+                             yw = yy - std::floor((yy - c.ay) * ily) * c.ly;
+                double v;
+                if (!ct_bicubic(s, h, 6, xw, yw, &v)) return fail(STZG_EINVAL, "a tracer left the interpolation grid");
+                row[i + 1] = (float)(v * s->P.TZ);
+            }
+        }
+        STZG_CHECK(ct_write_floats(dir, "teml", k, mat));
+    }
     return STZG_OK;
 }
 
@@ -937,6 +1211,8 @@ int stzg_ct_tracers_init(stzg_ct *s, int mm, int nn) {
     STZG_CUDA(cudaMemcpyAsync(s->tr, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s->st));
     STZG_CUDA(cudaStreamSynchronize(s->st));
     s->ntrace = cnt;
+    s->tr_m = mm;
+    s->tr_n = nn;
     s->tr_time = s->time;
     return STZG_OK;
 }
@@ -1008,6 +1284,161 @@ int stzg_ct_step_qs(stzg_ct *s, double dt, int nsteps, long *vcycles, double *se
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     if (seconds) *seconds = 1e-3 * ms;
     STZG_CUDA(cudaGetLastError());
+    return STZG_OK;
+}
+
+
+int stzg_ct_compute_strain(stzg_ct *s, double *out) {
+    if (!s || !out) return fail(STZG_EINVAL, "null argument");
+    STZG_CUDA(cudaSetDevice(s->device));
+    ct_host h;
+    STZG_CHECK(ct_fetch(s, h));
+    ct_strain(s, h, s->c.lamb * s->time);
+    const int m = h.m, n = h.n;
+    for (int q = 0; q < 6; q++)
+        for (int j = 0; j <= n; j++)
+            for (int i = 0; i < m; i++) out[((size_t)q * (n + 1) + j) * m + i] = h.f[CF + q][h.at(i, j)];
+    return STZG_OK;
+}
+
+int stzg_ct_output_field(stzg_ct *s, int mode, float *out, long *count) {
+    if (!s || mode < 0 || mode > 16) return fail(STZG_EINVAL, "bad arguments");
+    STZG_CUDA(cudaSetDevice(s->device));
+    ct_host h;
+    STZG_CHECK(ct_fetch(s, h));
+    if (mode >= 11) ct_strain(s, h, s->c.lamb * s->time);
+    std::vector<float> buf;
+    ct_output(s, h, mode, buf);
+    if (count) *count = (long)buf.size();
+    if (out) std::memcpy(out, buf.data(), buf.size() * sizeof(float));
+    return STZG_OK;
+}
+
+int stzg_ct_write_frame(stzg_ct *s, const char *dir, int frame, unsigned fflags) {
+    if (!s || !dir) return fail(STZG_EINVAL, "null argument");
+    STZG_CUDA(cudaSetDevice(s->device));
+    return ct_write_files(s, dir, frame, fflags);
+}
+
+int stzg_ct_solve_quasistatic(stzg_ct *s, double duration, int frames, int steps, const char *dir,
+                              unsigned fflags, int verbose) {
+    if (!s || !dir || frames < 1 || steps < 1 || !(duration > 0)) return fail(STZG_EINVAL, "bad arguments");
+    const double time_interval = duration / frames, isteps = 1.0 / steps;
+    if (s->f_num == 0) {
+        STZG_CHECK(ct_write_files(s, dir, 0, fflags));
+        if (verbose) std::puts("# Output frame 0");
+    }
+    long vc = 0, solves = 0;
+    for (int k = 1; k <= frames; k++) {
+        long v = 0;
+        STZG_CHECK(stzg_ct_step_qs(s, time_interval * isteps, steps, &v, nullptr));
+        vc += v;
+        solves += steps;
+        STZG_CHECK(ct_write_files(s, dir, k, fflags));
+        if (verbose) std::printf("# Output frame %d [%d] {%.2f}\n", k, steps, solves ? (double)vc / solves : 0.0);
+    }
+    s->f_num += frames;
+    return STZG_OK;
+}
+
+int stzg_ct_solve(stzg_ct *s, double duration, int frames, const char *dir, unsigned fflags, int verbose) {
+    if (!s || !dir || frames < 1 || !(duration > 0)) return fail(STZG_EINVAL, "bad arguments");
+    const ct_consts &c = s->c;
+    // the explicit steps: below both the elastic-wave and the viscous limit
+    const double time_interval = duration / frames, cfl = 0.25 * c.dx,
+                 visc_cond = 0.25 * c.dx * c.dx / s->P.viscosity, dt = cfl < visc_cond ? cfl : visc_cond;
+    const int l = (int)(time_interval / dt) + 1;
+    const double adt = time_interval / l;
+    if (verbose) {
+        std::printf("CFL: %g\n", dt / c.dx);
+        std::printf("Viscosity Condition: %g\n", s->P.viscosity * dt * (1. / (c.xsp * c.xsp + c.ysp * c.ysp)));
+    }
+    STZG_CHECK(ct_write_files(s, dir, 0, fflags));
+    if (verbose) std::puts("# Output frame 0");
+    for (int k = 1; k <= frames; k++) {
+        STZG_CHECK(stzg_ct_step_direct(s, adt, l, nullptr));
+        STZG_CHECK(ct_write_files(s, dir, k, fflags));
+        if (verbose) std::printf("# Output frame %d [%d]\n", k, l);
+    }
+    return STZG_OK;
+}
+
+
+// shear_sim::l2_comparison_transform (shear_sim.cc:619-711): s runs in the
+// sheared frame, phys in the physical frame (lamb = 0) on the same grid; the
+// physical run's fields are interpolated bilinearly (bilin_interp,
+// shear_sim.cc:713-736) at the sheared position i + lt xsp y_j of each node,
+// and the squared differences are summed with the reference's weights
+// (stresses 2 tau^2 + 2 s^2 + 3 p^2 + 6 q^2 on the cell rows, velocity and
+// reference map over the node rows with the trapezoidal halves on rows 0 and
+// n), times dx dy.  The reference reads past its grid where the shift passes
+// the ghost columns; that is an error here.
+int stzg_ct_l2_comparison_transform(stzg_ct *s, stzg_ct *phys, double *l2) {
+    if (!s || !phys || !l2) return fail(STZG_EINVAL, "null argument");
+    if (s->c.m != phys->c.m || s->c.n != phys->c.n) return fail(STZG_EINVAL, "grids differ");
+    STZG_CUDA(cudaSetDevice(s->device));
+    ct_host a, b;
+    STZG_CHECK(ct_fetch(s, a));
+    STZG_CUDA(cudaSetDevice(phys->device));
+    STZG_CHECK(ct_fetch(phys, b));
+    const ct_consts &c = s->c;
+    const int m = c.m, n = c.n;
+    const double lt = c.lamb * s->time;
+    bool bad = false;
+    // bilinear values of u, v, p, q, s, tau, chi of b at (ii, jj)
+    auto interp = [&](double ii, double jj, double *r) {
+        const int left = (int)ii, down = (int)jj, right = left + 1, up = down + 1;
+        if (left < -2 || right > m + 1 || down < -2 || up > n + 1) {
+            bad = true;
+            for (int k = 0; k < 7; k++) r[k] = 0;
+            return;
+        }
+        const size_t dl = b.at(left, down), dr = dl + 1, ul = dl + b.gm, ur = dr + b.gm;
+        const double f = right - ii, g = ii - left;
+        for (int k = 0; k < 7; k++) {
+            const double *F = b.f[k].data();
+            r[k] = (up - jj) * (f * F[dl] + g * F[dr]) + (jj - down) * (f * F[ul] + g * F[ur]);
+        }
+    };
+    double t0 = 0, t1 = 0, t2 = 0, t3 = 0, iv[7];
+    for (int j = 0; j < n; j++) {
+        double c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+        for (int i = 0; i < m; i++) {
+            const double i_phys = i + lt * c.xsp * (c.ay + j * c.dy);
+            interp(i_phys, (double)j, iv);
+            const size_t k = a.at(i, j);
+            const double du = a.f[CU][k] - iv[0], dv = a.f[CV][k] - iv[1], dp = a.f[CP][k] - iv[2],
+                         dq = a.f[CQ][k] - iv[3], ds = a.f[CS][k] - iv[4], dtau = a.f[CTAU][k] - iv[5],
+                         dchi = a.f[CCHI][k] - iv[6], dX = a.f[CX][k] - b.f[CX][k], dY = a.f[CY][k] - b.f[CY][k];
+            c0 += du * du + dv * dv;
+            c1 += dtau * dtau + ds * ds + 3 * dp * dp + 6 * dq * dq;
+            c2 += dchi * dchi;
+            c3 += dX * dX + dY * dY;
+        }
+        if (j == 0) {
+            c0 *= 0.5;
+            c3 *= 0.5;
+        }
+        t0 += c0;
+        t1 += c1;
+        t2 += c2;
+        t3 += c3;
+    }
+    for (int i = 0; i < m; i++) {
+        const double i_phys = i + lt * c.xsp * (c.ay + n * c.dy);
+        interp(i_phys, (double)n, iv);
+        const size_t k = a.at(i, n);
+        const double du = a.f[CU][k] - iv[0], dv = a.f[CV][k] - iv[1], dX = a.f[CX][k] - b.f[CX][k],
+                     dY = a.f[CY][k] - b.f[CY][k];
+        t0 += 0.5 * (du * du + dv * dv);
+        t3 += 0.5 * (dX * dX + dY * dY);
+    }
+    if (bad) return fail(STZG_EINVAL, "the sheared position leaves the ghosted grid");
+    const double fac = c.dx * c.dy;
+    l2[0] = t0 * fac;
+    l2[1] = t1 * fac;
+    l2[2] = t2 * fac;
+    l2[3] = t3 * fac;
     return STZG_OK;
 }
 

@@ -963,10 +963,15 @@ __device__ __forceinline__ float2 march_residual(const top_op<float> &op, const 
     return r;
 }
 
+// Loads through the read-only path, or (CG) from L2: the persistent coarse
+// kernel reads data other blocks wrote earlier in the same launch.
+template <bool CG, typename V> __device__ __forceinline__ V ld_lvl(const V *p) { return CG ? __ldcg(p) : __ldg(p); }
+
 // Row j of a strip (pairs at xs + 2 lane, wrapped); zero outside the grid.
+template <bool CG = false>
 __device__ __forceinline__ float4 march_load(const float2 *__restrict__ a, int j, int m, int n, int gx) {
     if (j < 0 || j >= n) return make_float4(0.f, 0.f, 0.f, 0.f);
-    return __ldg(reinterpret_cast<const float4 *>(a + (size_t)j * m + gx));
+    return ld_lvl<CG>(reinterpret_cast<const float4 *>(a + (size_t)j * m + gx));
 }
 
 // halves_of(2J + q - 1, n, 0, J) for q = 0, 1, 2 on a bounded line of n
@@ -1011,13 +1016,13 @@ __device__ __forceinline__ float2 march_restrict(const float2 &r0, const float2 
 // Coarse z of a strip staged by one warp: columns cx0 + 0..32 (wrapped) of
 // rows Jlo .. Jlo + R - 1, zero outside the level.  Lane L's pair prolongs
 // from columns L (even node) and L, L + 1 (odd node).
-template <int R>
+template <int R, bool CG = false>
 __device__ __forceinline__ void stage_coarse(float2 (*cz)[33], const float2 *__restrict__ zc, int cm, int cn, int cx0,
                                              int Jlo, int lane) {
     for (int k = lane; k < R * 33; k += 32) {
         const int r = k / 33, c = k - r * 33, J = Jlo + r;
         float2 v = make_float2(0.f, 0.f);
-        if (J >= 0 && J < cn) v = __ldg(zc + (size_t)J * cm + wrapx(cx0 + c, cm));
+        if (J >= 0 && J < cn) v = ld_lvl<CG>(zc + (size_t)J * cm + wrapx(cx0 + c, cm));
         cz[r][c] = v;
     }
     __syncwarp();
@@ -1672,17 +1677,14 @@ __device__ __forceinline__ float2 lev_restrict(const float4 &r0, const float4 &r
     return make_float2(ax, ay);
 }
 
-template <int TCH>
-__global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<float> L, level_view<float> C) {
-    __shared__ stencil9<float> tab[kMarchStencils];
-    pdl_trigger();
-    stage_stencils(tab, L);
-    const int lane = threadIdx.x & 31, lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
-    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
-    if (J0 >= C.n) return;
-    pdl_wait();
+// One warp's march down a strip (coarse columns I0 .., coarse rows J0 ..
+// J0+TCH-1): the level's sweep, its residual and the restriction into the
+// child's b.  tab: the level's stencil table in shared memory.
+template <int TCH, bool CG>
+__device__ __forceinline__ void lev_down_march(const level_view<float> &L, const level_view<float> &C,
+                                               const stencil9<float> *tab, int I0, int J0, int lane) {
+    const int lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
     const int m = L.m, n = L.n;
-    const int I0 = blockIdx.x * kLevDownCols;
     const int xs = 2 * I0 - 6, y0 = 2 * J0;
     const int gx = wrapx(xs + 2 * lane, m);
     const int I = I0 + lane - 3;
@@ -1693,15 +1695,15 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<floa
     int S0 = 0, S1 = 0, S2 = 0, S3 = 0;                            // stencil classes of rows k-3 .. k
     float4 Rp = zero;                                              // residual row k-4
     const int kb = y0 - 4, ke = y0 + 2 * TCH + 1;
-    float4 nb0 = march_load(L.b, kb, m, n, gx), nb1 = march_load(L.b, kb + 1, m, n, gx);
+    float4 nb0 = march_load<CG>(L.b, kb, m, n, gx), nb1 = march_load<CG>(L.b, kb + 1, m, n, gx);
     int ns0 = row_class(L, kb), ns1 = row_class(L, kb + 1);
     for (int k = kb + 1; k <= ke; k += 2) {
         W0 = W2; W1 = W3; W2 = W4; W3 = zero; W4 = zero;
         B0 = B2; B1 = B3; B2 = nb0; B3 = nb1;
         S0 = S2; S1 = S3; S2 = ns0; S3 = ns1;
         if (k + 2 <= ke) {
-            nb0 = march_load(L.b, k + 1, m, n, gx);
-            nb1 = march_load(L.b, k + 2, m, n, gx);
+            nb0 = march_load<CG>(L.b, k + 1, m, n, gx);
+            nb1 = march_load<CG>(L.b, k + 2, m, n, gx);
             ns0 = row_class(L, k + 1);
             ns1 = row_class(L, k + 2);
         }
@@ -1726,17 +1728,24 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<floa
 }
 
 template <int TCH>
-__global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float> L, level_view<float> C) {
+__global__ void __launch_bounds__(32 * kMarchWarps) k_lev_down_m(level_view<float> L, level_view<float> C) {
     __shared__ stencil9<float> tab[kMarchStencils];
-    __shared__ float2 czs[kMarchWarps][TCH + 3][33];
     pdl_trigger();
     stage_stencils(tab, L);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
-    const int J0 = (blockIdx.y * kMarchWarps + w) * TCH;
+    const int J0 = (blockIdx.y * kMarchWarps + (threadIdx.x >> 5)) * TCH;
     if (J0 >= C.n) return;
     pdl_wait();
+    lev_down_march<TCH, false>(L, C, tab, blockIdx.x * kLevDownCols, J0, threadIdx.x & 31);
+}
+
+// One warp's march up a strip: the child's correction added to the swept z
+// the down march left in r (czs: the warp's shared staging of the child's
+// strip, TCH + 3 rows), the level's sweep, the result written to z.
+template <int TCH, bool CG>
+__device__ __forceinline__ void lev_up_march(const level_view<float> &L, const level_view<float> &C,
+                                             const stencil9<float> *tab, float2 (*czs)[33], int I0, int J0, int lane) {
+    const int lsrc = (lane + 31) & 31, rsrc = (lane + 1) & 31;
     const int m = L.m, n = L.n;
-    const int I0 = blockIdx.x * kLevUpCols;
     const int xs = 2 * I0 - 4, y0 = 2 * J0;
     const int gx = wrapx(xs + 2 * lane, m);
     const bool own = lane >= 2 && lane < 2 + kLevUpCols && xs + 2 * lane < m;
@@ -1745,24 +1754,24 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float>
     float4 B0 = zero, B1 = zero, B2 = zero;             // b rows k-2 .. k
     int S0 = 0, S1 = 0, S2 = 0;                         // stencil classes of rows k-2 .. k
     const int kb = y0 - 2, ke = y0 + 2 * TCH + 1;
-    float4 nz0 = march_load(L.r, kb, m, n, gx), nz1 = march_load(L.r, kb + 1, m, n, gx);
-    float4 nb0 = march_load(L.b, kb, m, n, gx), nb1 = march_load(L.b, kb + 1, m, n, gx);
+    float4 nz0 = march_load<CG>(L.r, kb, m, n, gx), nz1 = march_load<CG>(L.r, kb + 1, m, n, gx);
+    float4 nb0 = march_load<CG>(L.b, kb, m, n, gx), nb1 = march_load<CG>(L.b, kb + 1, m, n, gx);
     int ns0 = row_class(L, kb), ns1 = row_class(L, kb + 1);
-    stage_coarse<TCH + 3>(czs[w], C.z, C.m, C.n, xs / 2, J0 - 1, lane);
+    stage_coarse<TCH + 3, CG>(czs, C.z, C.m, C.n, xs / 2, J0 - 1, lane);
     for (int k = kb + 1; k <= ke; k += 2) {
         float4 z0 = nz0, z1 = nz1;
         B0 = B2; B1 = nb0; B2 = nb1;
         S0 = S2; S1 = ns0; S2 = ns1;
         if (k + 2 <= ke) {
-            nz0 = march_load(L.r, k + 1, m, n, gx);
-            nz1 = march_load(L.r, k + 2, m, n, gx);
-            nb0 = march_load(L.b, k + 1, m, n, gx);
-            nb1 = march_load(L.b, k + 2, m, n, gx);
+            nz0 = march_load<CG>(L.r, k + 1, m, n, gx);
+            nz1 = march_load<CG>(L.r, k + 2, m, n, gx);
+            nb0 = march_load<CG>(L.b, k + 1, m, n, gx);
+            nb1 = march_load<CG>(L.b, k + 2, m, n, gx);
             ns0 = row_class(L, k + 1);
             ns1 = row_class(L, k + 2);
         }
-        prolong_staged(z0, czs[w], J0 - 1, lane, k - 1, n);
-        prolong_staged(z1, czs[w], J0 - 1, lane, k, n);
+        prolong_staged(z0, czs, J0 - 1, lane, k - 1, n);
+        prolong_staged(z1, czs, J0 - 1, lane, k, n);
         W0 = W2; W1 = W3; W2 = z0; W3 = z1;
         const int je = k - 1, jo = k - 2;
         if (je >= 0 && je < n) lev_row_sweep(tab + S1, je, n, W1, W2, W3, B1, lsrc, rsrc);
@@ -1772,6 +1781,19 @@ __global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float>
             if (jo >= y0 && jo < y0 + 2 * TCH && jo < n) *reinterpret_cast<float4 *>(L.z + (size_t)jo * m + gx) = W1;
         }
     }
+}
+
+template <int TCH>
+__global__ void __launch_bounds__(32 * kMarchWarps) k_lev_up_m(level_view<float> L, level_view<float> C) {
+    __shared__ stencil9<float> tab[kMarchStencils];
+    __shared__ float2 czs[kMarchWarps][TCH + 3][33];
+    pdl_trigger();
+    stage_stencils(tab, L);
+    const int w = threadIdx.x >> 5;
+    const int J0 = (blockIdx.y * kMarchWarps + w) * TCH;
+    if (J0 >= C.n) return;
+    pdl_wait();
+    lev_up_march<TCH, false>(L, C, tab, czs[w], blockIdx.x * kLevUpCols, J0, threadIdx.x & 31);
 }
 
 // ---------------------------------------------------------------------------

@@ -396,12 +396,12 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
 // differences of the node velocities.  Each field takes its increment with
 // two FP64 additions (hi, then lo), so the state carries the rounding of the
 // FP64 path plus ~2^-44 of the increment per step.  The ENO choice
-// |S(i)| > |S(i-1)| is taken on the high parts where the two magnitudes
-// differ by more than that approximation's error bound; near ties it is
-// recomputed in FP64 from the staged tile with k_advect's operations, so the
-// choice is always the FP64 path's (a different choice changes the value by
-// the difference of two second differences, which near an inflection is not
-// small).  The yield test runs on a float-float stress norm; cells near or
+// |S(i)| > |S(i-1)| is taken on the pair second differences where the two
+// magnitudes differ by more than their error bound; near ties between
+// different values it is recomputed in FP64 from the staged tile with
+// k_advect's operations, so the choice is always the FP64 path's (a
+// different choice changes the value by the difference of two second
+// differences, which near an inflection is not small).  The yield test runs on a float-float stress norm; cells near or
 // above a cut-off take the FP64 norm and the FP64 plastic law as k_advect
 // does.  The net force is formed by k_source_ff from the stresses, so no
 // per-cell combinations are written.  GB300 issues FP64 at 1/57 of the FP32
@@ -473,20 +473,25 @@ __device__ __noinline__ bool pick_y64(const double (*tile)[AROWS][ACOLS], int f,
 // point (Db is the upwind centre difference): from the left (outer = Db - Da)
 // 2 Db + (|Dc - Db| > |Db - Da| ? Db - Da : Dc - Db); from the right
 // (outer = Dc - Db) -2 Db + (|Db - Da| > |Dc - Db| ? Dc - Db : Db - Da).
-// `exact` gives the FP64 path's choice where the high parts cannot decide.
+// The second differences are pairs; their magnitudes are compared in pairs
+// too, decided where they differ by more than the pairs' error bound (the
+// differences' ~2^-44 plus the split's ~2^-47 of the values, with room).
+// Where they are the same pair the choice does not change the value (a zero
+// or linear stretch of a field); any other near tie takes `exact`, the FP64
+// path's own choice.
+__device__ __forceinline__ ff ff_abs(ff a) { return a.hi < 0.f ? ff_neg(a) : a; }
 template <typename Exact>
 __device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float vmag, Exact exact) {
-    const float sl = Db.hi - Da.hi, sr = Dc.hi - Db.hi;
-    const float gap = from_left ? fabsf(sr) - fabsf(sl) : fabsf(sl) - fabsf(sr);
-    // error of the high-part second differences: the low parts (<= 2^-24 of
-    // each difference), the subtraction's rounding and the split (~2^-47 of
-    // the values), with a factor ~8 to spare
-    const float margin = 5e-7f * (ffabs_hi(Da) + 2.f * ffabs_hi(Db) + ffabs_hi(Dc)) + 1e-13f * vmag;
-    const bool outer = fabsf(gap) > margin ? gap > 0.f : exact();
-    // outer: from the left Db - Da, from the right Dc - Db
-    const bool use_ab = from_left == outer;
-    const ff s = use_ab ? ff_sub(Db, Da) : ff_sub(Dc, Db);
-    return ff_add(from_left ? ff_x2(Db) : ff_neg(ff_x2(Db)), s);
+    const ff sab = ff_sub(Db, Da), sbc = ff_sub(Dc, Db);
+    const ff inner = from_left ? sbc : sab, outer = from_left ? sab : sbc;
+    const ff g = ff_sub(ff_abs(inner), ff_abs(outer));
+    const float gap = g.hi + g.lo;
+    const float margin = 1e-12f * (fabsf(Da.hi) + 2.f * fabsf(Db.hi) + fabsf(Dc.hi)) + 4e-13f * vmag;
+    bool take_outer;
+    if (fabsf(gap) > margin) take_outer = gap > 0.f;
+    else if (inner.hi == outer.hi && inner.lo == outer.lo) take_outer = false;
+    else take_outer = exact();
+    return ff_add(from_left ? ff_x2(Db) : ff_neg(ff_x2(Db)), take_outer ? outer : inner);
 }
 
 __device__ __forceinline__ ff dx_pair(const eno_tile_ff &T, int f, int ty, int c) {

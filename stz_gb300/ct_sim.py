@@ -11,7 +11,9 @@ import numpy as np
 
 from . import _lib
 
-EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_chi_bicubic", "stzg_ct_set_field", "stzg_ct_get_field",
+EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_chi_bicubic",
+           "stzg_ct_compute_strain", "stzg_ct_output_field", "stzg_ct_write_frame", "stzg_ct_solve_quasistatic",
+           "stzg_ct_solve", "stzg_ct_l2_comparison_transform", "stzg_ct_set_field", "stzg_ct_get_field",
            "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs", "stzg_ct_step_direct", "stzg_ct_tracers_init",
            "stzg_ct_tracers_update", "stzg_ct_tracers_get"]
 FIELDS = ("u", "v", "p", "q", "s", "tau", "chi", "X", "Y", "ddev")
@@ -71,6 +73,12 @@ def load():
         "stzg_ct_destroy": (I, [V]),
         "stzg_ct_init_fields": (I, [V, I, D, D]),
         "stzg_ct_chi_bicubic": (I, [V, I, I, ctypes.POINTER(ctypes.c_double), D, D]),
+        "stzg_ct_compute_strain": (I, [V, ctypes.POINTER(ctypes.c_double)]),
+        "stzg_ct_output_field": (I, [V, I, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_long)]),
+        "stzg_ct_write_frame": (I, [V, ctypes.c_char_p, I, ctypes.c_uint]),
+        "stzg_ct_solve_quasistatic": (I, [V, D, I, I, ctypes.c_char_p, ctypes.c_uint, I]),
+        "stzg_ct_solve": (I, [V, D, I, ctypes.c_char_p, ctypes.c_uint, I]),
+        "stzg_ct_l2_comparison_transform": (I, [V, V, ctypes.POINTER(ctypes.c_double)]),
         "stzg_ct_set_field": (I, [V, I, _P]),
         "stzg_ct_get_field": (I, [V, I, _P]),
         "stzg_ct_set_time": (I, [V, D]),
@@ -121,6 +129,40 @@ class CtSim:
         nn, mm = a.shape
         _lib.check(self.lib.stzg_ct_chi_bicubic(self.h, mm, nn, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                                 float(lo), float(sca)))
+
+    def l2_comparison_transform(self, phys):
+        """shear_sim::l2_comparison_transform against a physical-frame run."""
+        out = np.zeros(4)
+        _lib.check(self.lib.stzg_ct_l2_comparison_transform(self.h, phys.h,
+                                                            out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def compute_strain(self):
+        """shear_sim::compute_strain: (6, n+1, m) = E_xx, E_xy, E_yy, trace, second invariant, deviatoric norm."""
+        out = np.empty(6 * (self.P.n + 1) * self.P.m)
+        _lib.check(self.lib.stzg_ct_compute_strain(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out.reshape(6, self.P.n + 1, self.P.m)
+
+    def output(self, mode):
+        """shear_sim::output of one mode as the float32 matrix the reference writes."""
+        n = ctypes.c_long()
+        _lib.check(self.lib.stzg_ct_output_field(self.h, int(mode), None, ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.float32)
+        _lib.check(self.lib.stzg_ct_output_field(self.h, int(mode), out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                 ctypes.byref(n)))
+        return out.reshape(-1, int(out[0]) + 1)
+
+    def write_files(self, directory, frame, fflags):
+        """shear_sim::write_files into `directory` with the reference's flags."""
+        _lib.check(self.lib.stzg_ct_write_frame(self.h, str(directory).encode(), int(frame), int(fflags)))
+
+    def solve_quasistatic(self, duration, frames, steps, directory, fflags, verbose=False):
+        _lib.check(self.lib.stzg_ct_solve_quasistatic(self.h, float(duration), int(frames), int(steps),
+                                                      str(directory).encode(), int(fflags), int(verbose)))
+
+    def solve(self, duration, frames, directory, fflags, verbose=False):
+        _lib.check(self.lib.stzg_ct_solve(self.h, float(duration), int(frames), str(directory).encode(),
+                                          int(fflags), int(verbose)))
 
     def get(self, name):
         out = np.empty((self.P.n + 1, self.P.m))

@@ -26,17 +26,19 @@ def golden_names(kind="quasistatic"):
     diagnostics of a quasi-static state), "tgmg" (the general multigrid on
     poisson_fd), "ct" (the step in sheared coordinates), "ct_tracers" (its
     Lagrangian tracers), "ct_direct" (its explicit step), "ct_bicubic" (its
-    bicubic chi set-up), "init" (the
+    bicubic chi set-up), "ct_frames" (its frame files), "ct_l2t" (its
+    l2_comparison_transform), "init" (the
     initial states of init_fields and initialize_chi_bicubic, then
     quasi-static steps), "l2" (l2_comparison of an explicit and a
     quasi-static run) or "coarse" (the coarse Galerkin operators of the
     quasi-static system)."""
     names = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
     prefix = {"direct": ("direct_",), "frames": ("frames_",), "tgmg": ("tgmg_",), "ct": ("ct_",),
-              "ct_tracers": ("ct_tracers_",), "ct_direct": ("ctdirect_",), "ct_bicubic": ("ct_bicubic_",), "init": ("init_", "bicubic_"),
+              "ct_tracers": ("ct_tracers_",), "ct_direct": ("ctdirect_",), "ct_bicubic": ("ct_bicubic_",), "ct_frames": ("ct_frames_",), "ct_l2t": ("ct_l2t_",), "init": ("init_", "bicubic_"),
               "l2": ("l2cmp_",), "coarse": ("coarseops_",)}
     if kind == "ct":
-        return [n for n in names if n.startswith("ct_") and not n.startswith(("ct_tracers_", "ct_bicubic_"))]
+        return [n for n in names
+                if n.startswith("ct_") and not n.startswith(("ct_tracers_", "ct_bicubic_", "ct_frames_", "ct_l2t_"))]
     if kind in prefix:
         return [n for n in names if n.startswith(prefix[kind])]
     return [n for n in names if not any(n.startswith(p) for ps in prefix.values() for p in ps)]

@@ -14,7 +14,8 @@ stores the initial and final fields (rows 0..n), the time and the V-cycle
 count as tests/golden/ct_*.npz; the tracer cases (ct_tracers_*.npz) add
 shear_sim::initialize_tracers / update_tracers, the ctdirect_*.npz cases
 run the explicit shear_sim::step_forward from an advanced quasi-static state,
-and the ct_bicubic_*.npz cases the driver's bicubic chi set-up.
+the ct_bicubic_*.npz cases the driver's bicubic chi set-up, and the
+ct_frames_*.npz cases the files of write_files (fields, strain, tracers).
 """
 import json
 import os
@@ -184,8 +185,90 @@ def make_bicubic(name, case):
     ref.close()
 
 
+# Frames (shear_sim::write_files with every output flag, strain and tracers
+# included) of a state after quasi-static steps, twice (the second after
+# more steps, so update_tracers runs inside it): name -> (m, n, y_prd,
+# chi_case, tem_base, tem_delta, dt, steps before each frame, tracer grid).
+# The fields before each frame are stored with the files' bytes.
+FRAME_CASES = {
+    "ct_frames_wall64x32": (64, 32, False, 0, 580.0, 220.0, 3e6 / 2e4 / 600, 10, (16, 8)),
+    "ct_frames_prd40x20": (40, 20, True, 1, 580.0, 220.0, 0.5 / 1e-3 / 600, 10, (10, 5)),
+}
+FRAME_FLAGS = 16383
+FRAME_FILES = ["u", "v", "p", "q", "s", "tau", "chi", "tem", "dev", "X", "Y", "Exx", "Exy", "Eyy", "E_I", "E_II",
+               "Edev", "tra", "teml"]
+
+
+def make_frames(name, case):
+    import tempfile
+    m, n, yp, cc, base, delta, dt, steps, (tm, tn) = case
+    P = transform_shear(m, n, y_prd=yp)
+    ref = ReferenceCt(P)
+    ref.init_fields(cc, base, delta)
+    ref.steps(dt, 1)  # the solver's work arrays first (see make_tracers)
+    ref.initialize_tracers(tm, tn)
+    out = {}
+    times = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for k in range(2):
+            ref.steps(dt, steps)
+            for f, v in ref.fields().items():
+                out[f"state{k}_{f}"] = v
+            out[f"tracers{k}"] = ref.tracers()
+            times.append(ref.time)
+            ref.write_files(tmp, k, FRAME_FLAGS)
+            for f in FRAME_FILES:
+                with open(os.path.join(tmp, f"{f}.{k}"), "rb") as fh:
+                    out[f"file{k}_{f}"] = np.frombuffer(fh.read(), dtype=np.uint8)
+    out["tracers_after"] = ref.tracers()
+    params = {k: getattr(P, k) for k, _ in P._fields_}
+    meta = {"params": params, "chi_case": cc, "dt": dt, "steps": steps, "times": times, "fflags": FRAME_FLAGS,
+            "tracer_grid": [tm, tn], "files": FRAME_FILES}
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, "times", times, "tracers", len(out["tracers_after"]))
+    ref.close()
+
+
+# l2_comparison_transform: a sheared-frame run (lamb, still walls) and a
+# physical-frame run (lamb = 0, walls at +-lamb) from init_fields(1), explicit
+# steps to the same time, as the reference's shear_compare driver does:
+# name -> (m, n, lamb, dt multiplier tmult, explicit steps)
+L2T_CASES = {"ct_l2t_32x16": (32, 16, 1e-2, 0.5, 40)}
+
+
+def make_l2t(name, case):
+    m, n, lamb, tmult, steps = case
+    Pt = transform_shear(m, n, y_prd=False, lamb=lamb, u_bdry=0.0)
+    Pp = transform_shear(m, n, y_prd=False, lamb=0.0, u_bdry=lamb)
+    t, p = ReferenceCt(Pt), ReferenceCt(Pp)
+    t.init_fields(1, 600.0, 200.0)
+    p.init_fields(1, 600.0, 200.0)
+    dx = (Pt.bx - Pt.ax) / m
+    dt = dx * dx * tmult
+    t.step_forward(dt, steps)
+    p.step_forward(dt, steps)
+    out = {"trans_" + k: v for k, v in t.fields().items()}
+    out.update({"phys_" + k: v for k, v in p.fields().items()})
+    out["l2"] = t.l2_comparison_transform(p)
+    meta = {"trans": {k: getattr(Pt, k) for k, _ in Pt._fields_}, "phys": {k: getattr(Pp, k) for k, _ in Pp._fields_},
+            "time": t.time, "dt": dt, "steps": steps}
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, "time", t.time, "l2", out["l2"])
+    t.close()
+    p.close()
+
+
 def main(argv):
-    names = argv[1:] or list(CASES) + list(TRACER_CASES) + list(DIRECT_CASES) + list(BICUBIC_CASES)
+    names = argv[1:] or list(CASES) + list(TRACER_CASES) + list(DIRECT_CASES) + list(BICUBIC_CASES) + \
+        list(FRAME_CASES) + list(L2T_CASES)
+    if len(names) == 1 and names[0] in L2T_CASES:
+        make_l2t(names[0], L2T_CASES[names[0]])
+        return
+    if len(names) == 1 and names[0] in FRAME_CASES:
+        make_frames(names[0], FRAME_CASES[names[0]])
+        return
     if len(names) == 1 and names[0] in BICUBIC_CASES:
         make_bicubic(names[0], BICUBIC_CASES[names[0]])
         return

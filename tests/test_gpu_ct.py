@@ -168,3 +168,79 @@ def test_ct_chi_bicubic_matches_reference(name):
         assert vel < 1e-5, (vel, err)
         assert max(err.values()) < 1e-7, err
     sim.close()
+
+
+@pytest.mark.parametrize("name", golden_names("ct_frames"))
+def test_ct_frames_match_reference(name, tmp_path):
+    """shear_sim::write_files of the variant with every output flag: from the
+    reference's own state, the field files equal the reference's byte for
+    byte, the strain files (compute_strain with set_strain_boundaries) and
+    the tracer files (bicubic interpolation at the tracers; at frame 1 after
+    the tracers' Newton update on the GPU) agree to float rounding."""
+    from stz_gb300.ct_sim import CtSim
+    meta, arr = _load(name)
+    P = _params(meta)
+    sim = CtSim(P)
+    sim.time = meta["times"][0]
+    tm, tn = meta["tracer_grid"]
+    sim.initialize_tracers(tm, tn)
+    field_files = ["u", "v", "p", "q", "s", "tau", "chi", "tem", "dev", "X", "Y"]
+    for k in range(2):
+        sim.time = meta["times"][k]  # set_field applies the wall positions of the current time
+        for f in FIELDS:
+            sim.set(f, arr[f"state{k}_{f}"])
+        sim.write_files(tmp_path, k, meta["fflags"])
+        for f in meta["files"]:
+            got = (tmp_path / f"{f}.{k}").read_bytes()
+            ref = arr[f"file{k}_{f}"].tobytes()
+            if f in field_files:
+                assert got == ref, (k, f)
+            elif f == "tra":
+                a = np.loadtxt(tmp_path / f"tra.{k}")
+                b = np.array([[float(x) for x in ln.split()] for ln in ref.decode().splitlines()])
+                assert a.shape == b.shape, (k, f)
+                np.testing.assert_allclose(a, b, rtol=1e-8, atol=1e-10 * np.abs(b).max(), err_msg=f"{k} {f}")
+            else:
+                a, b = np.frombuffer(got, np.float32), np.frombuffer(ref, np.float32)
+                assert a.shape == b.shape, (k, f)
+                np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-6 * np.abs(b).max(), err_msg=f"{k} {f}")
+    sim.close()
+
+
+def test_ct_frame_loop_writes_frames(tmp_path):
+    """stzg_ct_solve_quasistatic: frame 0, then the steps and files of every
+    frame (the frame loop of shear_sim::solve_quasistatic)."""
+    from stz_gb300.ct_sim import CtSim, transform_shear
+    P = transform_shear(32, 16, y_prd=False)
+    sim = CtSim(P)
+    sim.init_fields(0, 580.0, 220.0)
+    sim.solve_quasistatic(3 * 0.25, 3, 2, tmp_path, 4 | 256 | 2048)
+    for k in range(4):
+        for f in ("p", "dev", "Exx", "Exy", "Eyy"):
+            assert (tmp_path / f"{f}.{k}").stat().st_size > 0
+    assert sim.time == pytest.approx(0.75, rel=1e-14)
+    sim.close()
+
+
+@pytest.mark.parametrize("name", golden_names("ct_l2t"))
+def test_ct_l2_comparison_transform_matches_reference(name):
+    """shear_sim::l2_comparison_transform on handles holding the reference's
+    sheared-frame and physical-frame states: the reference's four numbers to
+    rounding."""
+    from stz_gb300.ct_sim import CtParams, CtSim
+    meta, arr = _load(name)
+
+    def handle(key, prefix):
+        P = CtParams()
+        for k, v in meta[key].items():
+            setattr(P, k, v)
+        h = CtSim(P)
+        h.time = meta["time"]
+        for f in FIELDS:
+            h.set(f, arr[prefix + f])
+        return h
+
+    t, p = handle("trans", "trans_"), handle("phys", "phys_")
+    np.testing.assert_allclose(t.l2_comparison_transform(p), arr["l2"], rtol=1e-12, atol=1e-300)
+    t.close()
+    p.close()
