@@ -197,7 +197,10 @@ int stzg_mg_stencil(stzg_sim *s, double dt, int level, double *out);
  * (scratch), 5 outer residual of the mixed solve (float-float) + FP32 copy +
  * norms, 6 / 7 the streaming FP32 top-level kernel down (sweep, residual,
  * restriction) / up (prolongation, sweep) alone (scratch; STZG_EINVAL where
- * the top level does not use them). */
+ * the top level does not use them), 8 projection source (net force from the
+ * stresses; writes the solve's right-hand side only), 9 stress correction
+ * from the current velocities and the wall rows (changes the stresses: the
+ * handle's state is no longer a step of the reference after it). */
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
 
 /* No counterpart in the reference.  Squared residual norms of the

@@ -978,7 +978,7 @@ int stzg_download(stzg_sim *s, double *const *down) {
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {
     if (!s || !ms || reps < 1 || !(dt > 0)) return fail(STZG_EINVAL, "bad arguments");
     STZG_CHECK(ensure_ops(s, dt));
-    if ((kernel == 2 || kernel >= 4) && s->O.precision != STZG_MIXED)
+    if ((kernel == 2 || (kernel >= 4 && kernel <= 7)) && s->O.precision != STZG_MIXED)
         return fail(STZG_EINVAL, "FP32 kernels need a mixed-precision handle");
     auto one = [&]() -> int {
         switch (kernel) {
@@ -992,6 +992,13 @@ int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {
             case 7:
                 if (!top_level_kernel(s->h32, kernel - 6, s->st))
                     return fail(STZG_EINVAL, "the top level does not use the streaming kernels");
+                break;
+            case 8:
+                precombine(s->sc, s->F, s->cur, dt, s->st);
+                projection_source(s->sc, s->F, s->cur, dt, s->q.bcs * s->q.cxx * s->bv_state, s->st);
+                break;
+            case 9:
+                projection_apply(s->sc, s->F, s->cur, dt, s->bv_state, bdry_pos(s, s->time), s->st);
                 break;
             default: return fail(STZG_EINVAL, "unknown kernel id");
         }

@@ -1372,7 +1372,8 @@ int stzg_ct_solve(stzg_ct *s, double duration, int frames, const char *dir, unsi
 // (stresses 2 tau^2 + 2 s^2 + 3 p^2 + 6 q^2 on the cell rows, velocity and
 // reference map over the node rows with the trapezoidal halves on rows 0 and
 // n), times dx dy.  The reference reads past its grid where the shift passes
-// the ghost columns; that is an error here.
+// the ghost columns; that is an error here.  Its extra line starts at
+// fm + gmn, past the whole allocation (gmn = gm*gn); row n is summed here.
 int stzg_ct_l2_comparison_transform(stzg_ct *s, stzg_ct *phys, double *l2) {
     if (!s || !phys || !l2) return fail(STZG_EINVAL, "null argument");
     if (s->c.m != phys->c.m || s->c.n != phys->c.n) return fail(STZG_EINVAL, "grids differ");

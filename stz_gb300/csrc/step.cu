@@ -406,22 +406,26 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
 // does.  The net force is formed by k_source_ff from the stresses, so no
 // per-cell combinations are written.  GB300 issues FP64 at 1/57 of the FP32
 // rate; an elastic cell here needs two FP64 additions per field.
-struct eno_tile_ff {
-    float th[F_COUNT][AROWS][ACOLS];  // hi / lo parts of the staged values (X unwrapped)
+// Shared memory of k_advect_ff: the split values, then the FP64 tile (the
+// TMA destination, needed only until it is split) overlaid by the first
+// differences, so that three blocks fit on an SM.
+struct adv_smem_ff {
+    float th[F_COUNT][AROWS][ACOLS];  // hi / lo parts of the staged values
     float tl[F_COUNT][AROWS][ACOLS];
-    float dxh[F_COUNT][ATY][ADXW];    // first differences in x: tile columns cc, cc+1
-    float dxl[F_COUNT][ATY][ADXW];
-    float dyh[F_COUNT][ADYH][ATX];    // first differences in y: tile rows r, r+1
-    float dyl[F_COUNT][ADYH][ATX];
+    union {
+        double tile[F_COUNT][AROWS][ACOLS];  // staged fields (128-byte aligned: 24192 B precede it)
+        struct {
+            float dxh[F_COUNT][ATY][ADXW];  // first differences in x: tile columns cc, cc+1
+            float dxl[F_COUNT][ATY][ADXW];
+            float dyh[F_COUNT][ADYH][ATX];  // first differences in y: tile rows r, r+1
+            float dyl[F_COUNT][ADYH][ATX];
+        } d;
+    } u;
     int xs[ACOLS];   // period shift of the unwrapped column: -1, 0, +1
     int col[ACOLS];  // storage column of tile column c-2
-};
-
-struct adv_smem_ff {
-    double tile[F_COUNT][AROWS][ACOLS];  // staged fields, first: 128-byte aligned
-    eno_tile_ff T;
     uint64_t bar;
 };
+static_assert(sizeof(float) * 2 * F_COUNT * AROWS * ACOLS % 128 == 0, "the TMA tile must stay 128-byte aligned");
 
 __device__ __forceinline__ ff split_ff(double d) {
     ff r;
@@ -441,30 +445,31 @@ __device__ __forceinline__ ff ff_x2(ff a) { return ff{2.f * a.hi, 2.f * a.lo}; }
 __device__ __forceinline__ float ffabs_hi(ff a) { return fabsf(a.hi); }
 
 // FP64 choice of k_advect in x (tile_differences with the X column
-// offsets, then eno_left / eno_right's magnitude test): true where it takes
-// the outer second difference.
-__device__ __noinline__ bool pick_x64(const double (*tile)[AROWS][ACOLS], const int *xs, double lx, int f, int ty,
-                                      int tx, bool from_left) {
-    const int r = ty + 2, c0 = from_left ? tx : tx + 1;  // tile columns c0 .. c0+3
+// offsets, then eno_left / eno_right's magnitude test) from the state in
+// global memory (row: storage row, cols: the tile's storage columns, xs: the
+// tile's period shifts): true where it takes the outer second difference.
+__device__ __noinline__ bool pick_x64(const double *__restrict__ f, size_t row, const int *cols, const int *xs,
+                                      bool is_x, double lx, int tx, bool from_left) {
+    const int c0 = from_left ? tx : tx + 1;  // tile columns c0 .. c0+3
     double g[4];
     for (int q = 0; q < 4; q++) {
-        g[q] = tile[f][r][c0 + q];
-        if (f == F_X && xs[c0 + q] != 0) g[q] += xs[c0 + q] < 0 ? -lx : lx;
+        g[q] = f[row + cols[c0 + q]];
+        if (is_x && xs[c0 + q] != 0) g[q] += xs[c0 + q] < 0 ? -lx : lx;
     }
     const double da = g[1] - g[0], db = g[2] - g[1], dc = g[3] - g[2];
     // from the left: s0 = S(i) = dc - db, s1 = S(i-1) = db - da;
     // from the right: s0 = S(i) = db - da, s1 = S(i+1) = dc - db
     return from_left ? mag_gt(dc - db, db - da) : mag_gt(db - da, dc - db);
 }
-// FP64 choice in y (difference r between rows j0+r-2 and j0+r-1, zero where
-// k_advect's tile_differences leaves it zero).
-__device__ __noinline__ bool pick_y64(const double (*tile)[AROWS][ACOLS], int f, int ty, int tx, bool from_below,
-                                      int j0, int n) {
+// FP64 choice in y (difference r between cell rows j0+r-2 and j0+r-1, zero
+// where k_advect's tile_differences leaves it zero) at storage column i.
+__device__ __noinline__ bool pick_y64(const double *__restrict__ f, int m, int i, int ty, bool from_below, int j0,
+                                      int n) {
     const int r0 = from_below ? ty : ty + 1;  // differences r0 .. r0+2
     double d[3];
     for (int q = 0; q < 3; q++) {
-        const int r = r0 + q, jj = j0 + r - 2;
-        d[q] = (jj >= -1 && jj + 1 <= n) ? tile[f][r + 1][tx + 2] - tile[f][r][tx + 2] : 0.0;
+        const int r = r0 + q, jj = j0 + r - 2;  // cell rows jj, jj+1 = storage rows jj+1, jj+2
+        d[q] = (jj >= -1 && jj + 1 <= n) ? f[(size_t)(jj + 2) * m + i] - f[(size_t)(jj + 1) * m + i] : 0.0;
     }
     return from_below ? mag_gt(d[2] - d[1], d[1] - d[0]) : mag_gt(d[1] - d[0], d[2] - d[1]);
 }
@@ -482,43 +487,66 @@ __device__ __noinline__ bool pick_y64(const double (*tile)[AROWS][ACOLS], int f,
 __device__ __forceinline__ ff ff_abs(ff a) { return a.hi < 0.f ? ff_neg(a) : a; }
 template <typename Exact>
 __device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float vmag, Exact exact) {
-    const ff sab = ff_sub(Db, Da), sbc = ff_sub(Dc, Db);
-    const ff inner = from_left ? sbc : sab, outer = from_left ? sab : sbc;
-    const ff g = ff_sub(ff_abs(inner), ff_abs(outer));
-    const float gap = g.hi + g.lo;
-    const float margin = 1e-12f * (fabsf(Da.hi) + 2.f * fabsf(Db.hi) + fabsf(Dc.hi)) + 4e-13f * vmag;
+    // second differences from the high parts: within |lo| parts and one
+    // float rounding of the pairs' values, themselves within ~2^-44 of the
+    // differences and ~2^-47 of the values of the exact ones
+    const float fab = Db.hi - Da.hi, fbc = Dc.hi - Db.hi;
+    const float fin = from_left ? fbc : fab, fout = from_left ? fab : fbc;
+    const float gap0 = fabsf(fin) - fabsf(fout);
+    const float big = fabsf(Da.hi) + 2.f * fabsf(Db.hi) + fabsf(Dc.hi);
+    const float lows = fabsf(Da.lo) + 2.f * fabsf(Db.lo) + fabsf(Dc.lo);
+    const float m0 = lows + 2.4e-7f * (fabsf(fin) + fabsf(fout)) + 1e-12f * big + 4e-13f * vmag;
     bool take_outer;
-    if (fabsf(gap) > margin) take_outer = gap > 0.f;
-    else if (inner.hi == outer.hi && inner.lo == outer.lo) take_outer = false;
-    else take_outer = exact();
-    return ff_add(from_left ? ff_x2(Db) : ff_neg(ff_x2(Db)), take_outer ? outer : inner);
+    if (fabsf(gap0) > m0) {
+        take_outer = gap0 > 0.f;
+    } else {
+        const ff sab = ff_sub(Db, Da), sbc = ff_sub(Dc, Db);
+        const ff inner = from_left ? sbc : sab, outer = from_left ? sab : sbc;
+        const ff g = ff_sub(ff_abs(inner), ff_abs(outer));
+        const float gap = g.hi + g.lo;
+        if (fabsf(gap) > 1e-12f * big + 4e-13f * vmag) take_outer = gap > 0.f;
+        else if (inner.hi == outer.hi && inner.lo == outer.lo) take_outer = false;
+        else take_outer = exact();
+    }
+    // outer: from the left Db - Da, from the right Dc - Db
+    const ff s = (from_left == take_outer) ? ff_sub(Db, Da) : ff_sub(Dc, Db);
+    return ff_add(from_left ? ff_x2(Db) : ff_neg(ff_x2(Db)), s);
 }
 
-__device__ __forceinline__ ff dx_pair(const eno_tile_ff &T, int f, int ty, int c) {
-    return ff{T.dxh[f][ty][c], T.dxl[f][ty][c]};
+__device__ __forceinline__ ff dx_pair(const adv_smem_ff &Sm, int f, int ty, int c) {
+    return ff{Sm.u.d.dxh[f][ty][c], Sm.u.d.dxl[f][ty][c]};
 }
-__device__ __forceinline__ ff dy_pair(const eno_tile_ff &T, int f, int r, int tx) {
-    return ff{T.dyh[f][r][tx], T.dyl[f][r][tx]};
+__device__ __forceinline__ ff dy_pair(const adv_smem_ff &Sm, int f, int r, int tx) {
+    return ff{Sm.u.d.dyh[f][r][tx], Sm.u.d.dyl[f][r][tx]};
 }
 
-__device__ __forceinline__ ff eno_x_ff(const adv_smem_ff &Sm, int f, int ty, int tx, bool from_left, double lx) {
-    const eno_tile_ff &T = Sm.T;
+// Where the FP64 choice is needed, the state buffer read (A), the point's
+// storage row and the tile geometry.
+struct eno_ctx {
+    const double *__restrict__ const *A;
+    int m, n, j0, j;
+    double lx;
+};
+
+__device__ __forceinline__ ff eno_x_ff(const adv_smem_ff &Sm, const eno_ctx &e, int f, int ty, int tx,
+                                       bool from_left) {
     const int c = from_left ? tx : tx + 1;  // differences c .. c+2 (tile columns c .. c+3)
-    const float vmag = fabsf(T.th[f][ty + 2][tx + 2]);
-    return eno_ff(dx_pair(T, f, ty, c), dx_pair(T, f, ty, c + 1), dx_pair(T, f, ty, c + 2), from_left, vmag,
-                  [&] { return pick_x64(Sm.tile, T.xs, lx, f, ty, tx, from_left); });
+    const float vmag = fabsf(Sm.th[f][ty + 2][tx + 2]);
+    return eno_ff(dx_pair(Sm, f, ty, c), dx_pair(Sm, f, ty, c + 1), dx_pair(Sm, f, ty, c + 2), from_left, vmag, [&] {
+        return pick_x64(e.A[f], (size_t)(e.j + 1) * e.m, Sm.col, Sm.xs, f == F_X, e.lx, tx, from_left);
+    });
 }
 // y with the one-sided wall rows: `inner` is false on the last row before
 // the wall on the upwind side (value +-2 Db there).
-__device__ __forceinline__ ff eno_y_ff(const adv_smem_ff &Sm, int f, int ty, int tx, bool from_below, bool inner,
-                                       int j0, int n) {
-    const eno_tile_ff &T = Sm.T;
+__device__ __forceinline__ ff eno_y_ff(const adv_smem_ff &Sm, const eno_ctx &e, int f, int ty, int tx,
+                                       bool from_below, bool inner) {
     const int r = from_below ? ty : ty + 1;  // differences r .. r+2
-    const ff Db = dy_pair(T, f, r + 1, tx);
+    const ff Db = dy_pair(Sm, f, r + 1, tx);
     if (!inner) return from_below ? ff_x2(Db) : ff_neg(ff_x2(Db));
-    const float vmag = fabsf(T.th[f][ty + 2][tx + 2]);
-    return eno_ff(dy_pair(T, f, r, tx), Db, dy_pair(T, f, r + 2, tx), from_below, vmag,
-                  [&] { return pick_y64(Sm.tile, f, ty, tx, from_below, j0, n); });
+    const float vmag = fabsf(Sm.th[f][ty + 2][tx + 2]);
+    return eno_ff(dy_pair(Sm, f, r, tx), Db, dy_pair(Sm, f, r + 2, tx), from_below, vmag, [&] {
+        return pick_y64(e.A[f], e.m, Sm.col[tx + 2], ty, from_below, e.j0, e.n);
+    });
 }
 
 // -(uh eno_x + vh eno_y)
@@ -548,12 +576,11 @@ struct velo_ff {
     }
 };
 
-__global__ void __launch_bounds__(ATX * ATY)
+__global__ void __launch_bounds__(ATX * ATY, 3)
     k_advect_ff(step_consts c, advect_ff_consts h, const __grid_constant__ field_maps maps, fields_dev F, int cur,
                 double dt, double bv) {
     extern __shared__ __align__(128) unsigned char adv_raw_ff[];
     adv_smem_ff &Sm = *reinterpret_cast<adv_smem_ff *>(adv_raw_ff + ((128 - (smem_addr(adv_raw_ff) & 127)) & 127));
-    eno_tile_ff &T = Sm.T;
     const int m = c.m, n = c.n;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * ATX + tx;
     const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY;
@@ -566,13 +593,13 @@ __global__ void __launch_bounds__(ATX * ATY)
         const int u = i0 + tid - 2;
         int w = u % m;
         if (w < 0) w += m;
-        T.col[tid] = w;
-        T.xs[tid] = u < 0 ? -1 : (u >= m ? 1 : 0);
+        Sm.col[tid] = w;
+        Sm.xs[tid] = u < 0 ? -1 : (u >= m ? 1 : 0);
     }
     __syncthreads();
     if (tid == 0) {
         mbar_expect_tx(&Sm.bar, kTileBytes);
-        for (int f = 0; f < F_COUNT; f++) tma_load_2d(&Sm.tile[f][0][0], &maps.f[cur][f], i0 - 2, j0 - 1, &Sm.bar);
+        for (int f = 0; f < F_COUNT; f++) tma_load_2d(&Sm.u.tile[f][0][0], &maps.f[cur][f], i0 - 2, j0 - 1, &Sm.bar);
     }
     if (__syncthreads_or(!mbar_wait_bounded(&Sm.bar))) {
         if (tid == 0) atomicExch(&F.flags[FL_TMA], 1);
@@ -585,14 +612,14 @@ __global__ void __launch_bounds__(ATX * ATY)
         for (int k = tid; k < kTileVals; k += ATX * ATY) {
             const int f = k / (AROWS * ACOLS), rem = k - f * (AROWS * ACOLS), r = rem / ACOLS, t = rem - r * ACOLS;
             const int u = i0 + t - 2, sr = j0 - 1 + r;
-            if ((u < 0 || u >= m) && sr >= 0 && sr <= n + 1) Sm.tile[f][r][t] = A[f][(size_t)sr * m + T.col[t]];
+            if ((u < 0 || u >= m) && sr >= 0 && sr <= n + 1) Sm.u.tile[f][r][t] = A[f][(size_t)sr * m + Sm.col[t]];
         }
         __syncthreads();
     }
     // split every staged value into a float pair
     for (int k = tid; k < kTileVals; k += ATX * ATY) {
         const int f = k / (AROWS * ACOLS), rem = k - f * (AROWS * ACOLS), r = rem / ACOLS, t = rem - r * ACOLS;
-        ff_split_d(Sm.tile[f][r][t], T.th[f][r][t], T.tl[f][r][t]);
+        ff_split_d(Sm.u.tile[f][r][t], Sm.th[f][r][t], Sm.tl[f][r][t]);
     }
     __syncthreads();
     // first differences: x on cell rows j0..j0+ATY-1, y on rows j0-2..j0+ATY+1;
@@ -602,27 +629,28 @@ __global__ void __launch_bounds__(ATX * ATY)
         const int f = k / (ATY * ADXW), rem = k - f * (ATY * ADXW), r = rem / ADXW, cc = rem - r * ADXW;
         ff d{0.f, 0.f};
         if (j0 + r < n) {
-            d = ff_pair_diff(T.th[f][r + 2][cc + 1], T.tl[f][r + 2][cc + 1], T.th[f][r + 2][cc], T.tl[f][r + 2][cc]);
-            const int sh = T.xs[cc + 1] - T.xs[cc];
+            d = ff_pair_diff(Sm.th[f][r + 2][cc + 1], Sm.tl[f][r + 2][cc + 1], Sm.th[f][r + 2][cc], Sm.tl[f][r + 2][cc]);
+            const int sh = Sm.xs[cc + 1] - Sm.xs[cc];
             if (f == F_X && sh != 0) d = ff_add(d, sh > 0 ? lx : ff_neg(lx));
         }
-        T.dxh[f][r][cc] = d.hi;
-        T.dxl[f][r][cc] = d.lo;
+        Sm.u.d.dxh[f][r][cc] = d.hi;
+        Sm.u.d.dxl[f][r][cc] = d.lo;
     }
     for (int k = tid; k < F_COUNT * ADYH * ATX; k += ATX * ATY) {
         const int f = k / (ADYH * ATX), rem = k - f * (ADYH * ATX), r = rem / ATX, cc = rem - r * ATX;
         const int jj = j0 + r - 2;
         ff d{0.f, 0.f};
         if (jj >= -1 && jj + 1 <= n && i0 + cc < m)
-            d = ff_pair_diff(T.th[f][r + 1][cc + 2], T.tl[f][r + 1][cc + 2], T.th[f][r][cc + 2], T.tl[f][r][cc + 2]);
-        T.dyh[f][r][cc] = d.hi;
-        T.dyl[f][r][cc] = d.lo;
+            d = ff_pair_diff(Sm.th[f][r + 1][cc + 2], Sm.tl[f][r + 1][cc + 2], Sm.th[f][r][cc + 2], Sm.tl[f][r][cc + 2]);
+        Sm.u.d.dyh[f][r][cc] = d.hi;
+        Sm.u.d.dyl[f][r][cc] = d.lo;
     }
     __syncthreads();
     if (i >= m || j >= n) return;
     const ff hx{h.hxh, h.hxl}, hy{h.hyh, h.hyl};
     const size_t ci = (size_t)(j + 1) * m + i;
-    const int ir = T.col[tx + 3];
+    const eno_ctx e{A, m, n, j0, j, c.lx};
+    const int ir = Sm.col[tx + 3];
     if (c.clock) bv = c.clock[CLK_BV_STATE];
     const velo_ff V{F.vel, m, n, split_ff(bv)};
     // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
@@ -633,8 +661,8 @@ __global__ void __launch_bounds__(ATX * ATY)
         const bool inner = rv ? j > 1 : j < n - 1;
 #pragma unroll
         for (int f = F_X; f <= F_Y; f++) {
-            const ff ex = eno_x_ff(Sm, f, ty, tx, ru, c.lx), ey = eno_y_ff(Sm, f, ty, tx, rv, inner, j0, n);
-            B[f][ci] = add_ff(Sm.tile[f][ty + 2][tx + 2], upwind_inc(uh, ex, vh, ey));
+            const ff ex = eno_x_ff(Sm, e, f, ty, tx, ru), ey = eno_y_ff(Sm, e, f, ty, tx, rv, inner);
+            B[f][ci] = add_ff(A[f][ci], upwind_inc(uh, ex, vh, ey));
         }
     }
     // staggered velocity and spin (shear_sim.cc:330-333) in pairs
@@ -649,12 +677,12 @@ __global__ void __launch_bounds__(ATX * ATY)
     const ff uh = ff_mul(uc, ru ? hx : ff_neg(hx)), vh = ff_mul(vc, rv ? hy : ff_neg(hy));
     const bool inner = rv ? j > 0 : j < n - 1;
     auto inc_of = [&](int f) {
-        return upwind_inc(uh, eno_x_ff(Sm, f, ty, tx, ru, c.lx), vh, eno_y_ff(Sm, f, ty, tx, rv, inner, j0, n));
+        return upwind_inc(uh, eno_x_ff(Sm, e, f, ty, tx, ru), vh, eno_y_ff(Sm, e, f, ty, tx, rv, inner));
     };
-    const ff qf{T.th[F_Q][ty + 2][tx + 2], T.tl[F_Q][ty + 2][tx + 2]};
-    const ff sf{T.th[F_S][ty + 2][tx + 2], T.tl[F_S][ty + 2][tx + 2]};
-    const ff tf{T.th[F_TAU][ty + 2][tx + 2], T.tl[F_TAU][ty + 2][tx + 2]};
-    double cchi = add_ff(Sm.tile[F_CHI][ty + 2][tx + 2], inc_of(F_CHI)), ddev = 0, dtmp = 0;
+    const ff qf{Sm.th[F_Q][ty + 2][tx + 2], Sm.tl[F_Q][ty + 2][tx + 2]};
+    const ff sf{Sm.th[F_S][ty + 2][tx + 2], Sm.tl[F_S][ty + 2][tx + 2]};
+    const ff tf{Sm.th[F_TAU][ty + 2][tx + 2], Sm.tl[F_TAU][ty + 2][tx + 2]};
+    double cchi = add_ff(A[F_CHI][ci], inc_of(F_CHI)), ddev = 0, dtmp = 0;
     // Yield test: 3q^2 + s^2 + tau^2 in pairs (relative error ~2^-44); a cell
     // clearly below the cut-offs of k_advect (1e-24, or an athermal law below
     // yield) is elastic there too; any other cell takes k_advect's FP64 path.
@@ -663,8 +691,8 @@ __global__ void __launch_bounds__(ATX * ATY)
     const bool athermal = c.stz_model >= 2;
     const bool clearly_elastic = dv < 0.999e-24f * (1.f - 1e-6f) || (athermal && dv < c.yield_cut2f);
     if (!clearly_elastic) {
-        const double q = Sm.tile[F_Q][ty + 2][tx + 2], s = Sm.tile[F_S][ty + 2][tx + 2],
-                     t = Sm.tile[F_TAU][ty + 2][tx + 2];
+        const double q = A[F_Q][ci], s = A[F_S][ci],
+                     t = A[F_TAU][ci];
         const double devsq = 3 * q * q + s * s + t * t;
         const long long dbits = __double_as_longlong(devsq);
         if (!(dbits < __double_as_longlong(0.999e-24) ||
@@ -678,16 +706,16 @@ __global__ void __launch_bounds__(ATX * ATY)
     }
     B[F_CHI][ci] = cchi;
     F.ddev[ci] = ddev;
-    double qn = add_ff(Sm.tile[F_Q][ty + 2][tx + 2], inc_of(F_Q));
-    double sn = add_ff(Sm.tile[F_S][ty + 2][tx + 2], ff_add(inc_of(F_S), ff_mul(two_omega, tf)));
-    double tn = add_ff(Sm.tile[F_TAU][ty + 2][tx + 2], ff_sub(inc_of(F_TAU), ff_mul(two_omega, sf)));
+    double qn = add_ff(A[F_Q][ci], inc_of(F_Q));
+    double sn = add_ff(A[F_S][ci], ff_add(inc_of(F_S), ff_mul(two_omega, tf)));
+    double tn = add_ff(A[F_TAU][ci], ff_sub(inc_of(F_TAU), ff_mul(two_omega, sf)));
     if (dtmp != 0) {
         if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
-        qn -= dtmp * Sm.tile[F_Q][ty + 2][tx + 2];
-        sn -= dtmp * Sm.tile[F_S][ty + 2][tx + 2];
-        tn -= dtmp * Sm.tile[F_TAU][ty + 2][tx + 2];
+        qn -= dtmp * A[F_Q][ci];
+        sn -= dtmp * A[F_S][ci];
+        tn -= dtmp * A[F_TAU][ci];
     }
-    B[F_P][ci] = add_ff(Sm.tile[F_P][ty + 2][tx + 2], inc_of(F_P));
+    B[F_P][ci] = add_ff(A[F_P][ci], inc_of(F_P));
     B[F_Q][ci] = qn;
     B[F_S][ci] = sn;
     B[F_TAU][ci] = tn;

@@ -226,7 +226,13 @@ def test_ct_frame_loop_writes_frames(tmp_path):
 def test_ct_l2_comparison_transform_matches_reference(name):
     """shear_sim::l2_comparison_transform on handles holding the reference's
     sheared-frame and physical-frame states: the reference's four numbers to
-    rounding."""
+    rounding, but for the top node row of the reference-map term.  The
+    reference's extra line (shear_sim.cc:675) starts at fm + gmn, and gmn is
+    gm*gn, the whole allocation (shear_sim.cc:30), so it reads past both grids;
+    in the fixture's process that memory held zeros, which leaves u, v equal to
+    row n's wall values here but drops row n's X, Y differences.  The handle
+    sums row n itself, so l2[3] is the reference's value plus that row's
+    0.5 (dX^2 + dY^2) dx dy, formed here from the fixture fields."""
     from stz_gb300.ct_sim import CtParams, CtSim
     meta, arr = _load(name)
 
@@ -241,6 +247,12 @@ def test_ct_l2_comparison_transform_matches_reference(name):
         return h
 
     t, p = handle("trans", "trans_"), handle("phys", "phys_")
-    np.testing.assert_allclose(t.l2_comparison_transform(p), arr["l2"], rtol=1e-12, atol=1e-300)
+    P = t.P
+    n = P.n
+    top = 0.5 * ((arr["trans_X"][n] - arr["phys_X"][n]) ** 2 + (arr["trans_Y"][n] - arr["phys_Y"][n]) ** 2).sum()
+    want = np.array(arr["l2"], dtype=float)
+    want[3] += top * (P.bx - P.ax) / P.m * (P.by - P.ay) / n
+    assert top > 0  # the case moves the physical walls: row n differs
+    np.testing.assert_allclose(t.l2_comparison_transform(p), want, rtol=1e-12, atol=1e-300)
     t.close()
     p.close()

@@ -291,11 +291,15 @@ def test_time_kernel_hook():
     g = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=1e-10)
     g.steps(0.01, 3)
     before = g.fields()
-    for k in (0, 2, 4, 5):
+    for k in (0, 2, 4, 5, 8):
         assert g.time_kernel(0.01, k, 3) > 0
     after = g.fields()
     for name in ("p", "q", "s", "tau", "chi", "X", "Y"):
         assert np.array_equal(before[name], after[name])
+    # id 9 applies the stress correction of the current velocities again
+    assert g.time_kernel(0.01, 9, 1) > 0
+    with pytest.raises(_lib.StzgError):
+        g.time_kernel(0.01, 10, 1)
 
 
 def test_time_kernel_top_level_streaming():
