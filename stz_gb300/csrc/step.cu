@@ -897,45 +897,58 @@ __global__ void k_source(step_consts c, fields_dev F, double xbc_bv) {
 
 // The projection source of the float-float path (k_advect_ff writes no
 // per-cell combinations): net_force (shear_sim.cc:447-453) at the interior
-// nodes from the stresses of the four surrounding cells, every cell-to-cell
-// difference formed from float pairs by TwoSum (error ~2^-44 of the
-// difference plus ~2^-47 of the values), then scaled by xf, yf in pairs;
-// the wall rows as k_source.
+// nodes from the stresses of the four surrounding cells.  A block of 32 x 8
+// nodes first forms, for each of the 33 x 9 cells around it, the pairs
+// A = p + q - s, B = p + q + s and tau from the split stresses (float-float
+// sums, error ~2^-47 of the values) in shared memory; each node then takes
+// the cell-to-cell differences of those pairs, whose high parts cancel
+// exactly where the cells agree, so the force keeps ~2^-44 of its own size
+// plus ~2^-47 of the stresses, and scales them by xf, yf in pairs.  The wall
+// rows as k_source.
 struct source_ff_consts {
     float xfh, xfl, yfh, yfl;
 };
 
-__device__ __forceinline__ ff cell_diff(const double *f, size_t a, size_t b) {
-    float ah, al, bh, bl;
-    ff_split_d(f[a], ah, al);
-    ff_split_d(f[b], bh, bl);
-    return ff_pair_diff(ah, al, bh, bl);
-}
+constexpr int SFX = 32, SFY = 8;
 
-__global__ void k_source_ff(step_consts c, fields_dev F, int cur, source_ff_consts h, double xbc_bv) {
+__global__ void __launch_bounds__(SFX * SFY) k_source_ff(step_consts c, fields_dev F, int cur, source_ff_consts h,
+                                                         double xbc_bv) {
+    __shared__ ff cA[SFY + 1][SFX + 1], cB[SFY + 1][SFX + 1], cT[SFY + 1][SFX + 1];
     const int m = c.m, n = c.n;
     if (c.clock) {
         xbc_bv = c.xbc * c.clock[CLK_BV];
         cur = (int)c.clock[CLK_CUR] ^ 1;  // the state the advection wrote
     }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i0 = blockIdx.x * SFX, j0 = blockIdx.y * SFY;
+    const int tid = threadIdx.y * SFX + threadIdx.x;
+    const double *P = F.f[cur][F_P], *Q = F.f[cur][F_Q], *S = F.f[cur][F_S], *T = F.f[cur][F_TAU];
+    // cells (i0 - 1 + cc, j0 - 1 + r); storage rows -1 .. n exist
+    for (int k = tid; k < (SFY + 1) * (SFX + 1); k += SFX * SFY) {
+        const int r = k / (SFX + 1), cc = k - r * (SFX + 1);
+        const int cj = j0 - 1 + r;
+        int ci = i0 - 1 + cc;
+        ci = ci < 0 ? ci + m : (ci >= m ? ci % m : ci);
+        if (cj > n) continue;
+        const size_t q = IDX(ci, cj);
+        const ff pp = split_ff(P[q]), qq = split_ff(Q[q]), ss = split_ff(S[q]);
+        const ff pq = ff_add(pp, qq);
+        cA[r][cc] = ff_sub(pq, ss);
+        cB[r][cc] = ff_add(pq, ss);
+        cT[r][cc] = split_ff(T[q]);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y, i = i0 + tx, j = j0 + ty;
     if (i >= m || j > n) return;
     double2 out;
     if (j == 0 || j == n) {
         out.x = j == 0 ? -xbc_bv : xbc_bv;
         out.y = 0;
     } else {
-        const int il = i == 0 ? m - 1 : i - 1;
-        const size_t k0 = IDX(il, j - 1), k1 = IDX(i, j - 1), k2 = IDX(il, j), k3 = IDX(i, j);
-        const double *P = F.f[cur][F_P], *Q = F.f[cur][F_Q], *S = F.f[cur][F_S], *T = F.f[cur][F_TAU];
-        // A = p + q - s, B = p + q + s: x differences of A, y differences of B
-        const ff dAx = ff_add(ff_sub(ff_add(cell_diff(P, k1, k0), cell_diff(Q, k1, k0)), cell_diff(S, k1, k0)),
-                              ff_sub(ff_add(cell_diff(P, k3, k2), cell_diff(Q, k3, k2)), cell_diff(S, k3, k2)));
-        const ff dBy = ff_add(ff_add(ff_add(cell_diff(P, k2, k0), cell_diff(Q, k2, k0)), cell_diff(S, k2, k0)),
-                              ff_add(ff_add(cell_diff(P, k3, k1), cell_diff(Q, k3, k1)), cell_diff(S, k3, k1)));
-        const ff dTy = ff_add(cell_diff(T, k0, k2), cell_diff(T, k1, k3));  // (t0 + t1) - (t2 + t3)
-        const ff dTx = ff_add(cell_diff(T, k0, k1), cell_diff(T, k2, k3));  // (t0 - t1) + (t2 - t3)
+        // cells k0 = (i-1, j-1), k1 = (i, j-1), k2 = (i-1, j), k3 = (i, j)
+        const ff dAx = ff_add(ff_sub(cA[ty][tx + 1], cA[ty][tx]), ff_sub(cA[ty + 1][tx + 1], cA[ty + 1][tx]));
+        const ff dBy = ff_add(ff_sub(cB[ty + 1][tx], cB[ty][tx]), ff_sub(cB[ty + 1][tx + 1], cB[ty][tx + 1]));
+        const ff dTy = ff_add(ff_sub(cT[ty][tx], cT[ty + 1][tx]), ff_sub(cT[ty][tx + 1], cT[ty + 1][tx + 1]));
+        const ff dTx = ff_add(ff_sub(cT[ty][tx], cT[ty][tx + 1]), ff_sub(cT[ty + 1][tx], cT[ty + 1][tx + 1]));
         const ff xf{h.xfh, h.xfl}, yf{h.yfh, h.yfl};
         const ff fx = ff_add(ff_mul(xf, dAx), ff_mul(yf, dTy)), fy = ff_add(ff_mul(xf, dTx), ff_mul(yf, dBy));
         out.x = ff_f2d(fx.hi) + ff_f2d(fx.lo);
@@ -965,25 +978,38 @@ __global__ void k_project(step_consts c, fields_dev F, int cur, double hx, doubl
     S[F_TAU][k] += c.mu * (uy + vx);
 }
 
-// The stress correction of the float-float path: the velocity differences of
-// k_project from float pairs (TwoSum), the products with hx, hy, K, mu/3 and
-// mu in pairs, and each stress component takes its correction with two FP64
-// additions.
+// The stress correction of the float-float path: each node's velocity is
+// split into float pairs once (a block of 32 x 8 cells stages its 33 x 9
+// nodes in shared memory), the velocity differences of k_project are taken
+// from the pairs, the products with hx, hy, K, mu/3 and mu in pairs, and each
+// stress component takes its correction with two FP64 additions.
 struct project_ff_consts {
     float hxh, hxl, hyh, hyl, Kh, Kl, m3h, m3l, muh, mul;
 };
 
-__global__ void k_project_ff(step_consts c, fields_dev F, int cur, project_ff_consts h) {
+__global__ void __launch_bounds__(SFX * SFY) k_project_ff(step_consts c, fields_dev F, int cur, project_ff_consts h) {
+    // velocities of the block's 33 x 9 nodes as pairs, split once each
+    __shared__ ff nU[SFY + 1][SFX + 1], nV[SFY + 1][SFX + 1];
     const int m = c.m, n = c.n;
     if (c.clock) cur = (int)c.clock[CLK_CUR] ^ 1;  // the state the advection wrote
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int i0 = blockIdx.x * SFX, j0 = blockIdx.y * SFY;
+    const int tid = threadIdx.y * SFX + threadIdx.x;
+    for (int k = tid; k < (SFY + 1) * (SFX + 1); k += SFX * SFY) {
+        const int r = k / (SFX + 1), cc = k - r * (SFX + 1);
+        const int nj = j0 + r;
+        int ni = i0 + cc;
+        ni = ni >= m ? ni % m : ni;
+        if (nj > n) continue;
+        const double2 v = F.vel[(size_t)nj * m + ni];
+        nU[r][cc] = split_ff(v.x);
+        nV[r][cc] = split_ff(v.y);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y, i = i0 + tx, j = j0 + ty;
     if (i >= m || j >= n) return;
-    const int ir = i == m - 1 ? 0 : i + 1;
-    const double2 a = F.vel[(size_t)j * m + i], b = F.vel[(size_t)j * m + ir], cu = F.vel[(size_t)(j + 1) * m + i],
-                  d = F.vel[(size_t)(j + 1) * m + ir];
-    const ff ax = split_ff(a.x), bx = split_ff(b.x), cx = split_ff(cu.x), dx = split_ff(d.x);
-    const ff ay = split_ff(a.y), by = split_ff(b.y), cy = split_ff(cu.y), dy = split_ff(d.y);
+    // nodes a = (i, j), b = (i+1, j), c = (i, j+1), d = (i+1, j+1)
+    const ff ax = nU[ty][tx], bx = nU[ty][tx + 1], cx = nU[ty + 1][tx], dx = nU[ty + 1][tx + 1];
+    const ff ay = nV[ty][tx], by = nV[ty][tx + 1], cy = nV[ty + 1][tx], dy = nV[ty + 1][tx + 1];
     const ff hx{h.hxh, h.hxl}, hy{h.hyh, h.hyl};
     const ff ux = ff_mul(hx, ff_add(ff_sub(bx, ax), ff_sub(dx, cx))), uy = ff_mul(hy, ff_add(ff_sub(cx, ax), ff_sub(dx, bx)));
     const ff vx = ff_mul(hx, ff_add(ff_sub(by, ay), ff_sub(dy, cy))), vy = ff_mul(hy, ff_add(ff_sub(cy, ay), ff_sub(dy, by)));
@@ -1126,7 +1152,8 @@ void projection_source(const step_consts &c, fields_dev &F, int cur, double dt, 
         source_ff_consts h;
         split_host(0.5 / dt * c.xsp, &h.xfh, &h.xfl);
         split_host(0.5 / dt * c.ysp, &h.yfh, &h.yfl);
-        k_source_ff<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, cur, h, xbc_bv);
+        const dim3 sb(SFX, SFY);
+        k_source_ff<<<g2(c.m, c.n + 1, sb), sb, 0, st>>>(c, F, cur, h, xbc_bv);
     } else {
         k_source<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, xbc_bv);
     }
@@ -1151,7 +1178,8 @@ void projection_apply(const step_consts &c, fields_dev &F, int cur, double dt, d
         split_host(c.K, &h.Kh, &h.Kl);
         split_host(c.mu * (1 / 3.0), &h.m3h, &h.m3l);
         split_host(c.mu, &h.muh, &h.mul);
-        k_project_ff<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, h);
+        const dim3 sb(SFX, SFY);
+        k_project_ff<<<g2(c.m, c.n, sb), sb, 0, st>>>(c, F, cur, h);
     } else {
         k_project<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, hx, hy);
     }
