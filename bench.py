@@ -41,8 +41,11 @@ TOP_BYTES_PER_NODE = 26.0        # one top-level streaming kernel: 6.5 words of 
 VCYCLE32_BYTES_PER_NODE = 69.3   # 17.3 words of 4 B: 13 W on the top level x (1 + 1/4 + 1/16 + ...)
 VCYCLE64_BYTES_PER_NODE = 138.7
 SWEEP32_BYTES_PER_NODE = 24      # one Gauss-Seidel sweep: read z, b; write z (float2)
-# DRAM bytes (read + write) of one launch at 2048x2048 from the committed ncu capture
-NCU_TRAFFIC_2048 = {"advect": 659.8e6, "residual_ff": 153.0e6}
+# DRAM bytes (read + write) of one launch at 2048x2048 from the committed ncu
+# captures (cold caches); the advection kernel per precision
+NCU_TRAFFIC_2048 = {"advect_mixed": 539.3e6, "advect_fp64": 659.8e6, "residual_ff": 153.0e6,
+                    "source_mixed": 174.9e6}
+SOURCE_BYTES_PER_NODE = 48       # read p,q,s,tau of the cells (8 B each, once per cell); write the source (16 B)
 DIRECT_BYTES_PER_CELL = 160      # explicit step: read u,v,p,q,s,tau,chi,X,Y; write them, ddev (8 B each)
 RESIDFF_BYTES_PER_NODE = 40      # read z, b as float-float (hi, lo float2 each); write r (float2)
 
@@ -372,7 +375,8 @@ def run_ours(args, dist):
     peak, peak_kind = measured_peaks()
     nn = N * (N + 1)
     t_adv = sim.time_kernel(DT, 0, 10)
-    rows = {"advect": (t_adv, ADVECT_BYTES_PER_CELL * N * N, 1.0)}
+    rows = {"advect": (t_adv, ADVECT_BYTES_PER_CELL * N * N, 1.0),
+            "source": (sim.time_kernel(DT, 8, 10), SOURCE_BYTES_PER_NODE * nn, 1.0)}
     if prec == _lib.MIXED:
         t_v32 = sim.time_kernel(DT, 4, 10)
         t_rff = sim.time_kernel(DT, 5, 10)
@@ -386,7 +390,8 @@ def run_ours(args, dist):
     dom = max(shares, key=shares.get)
     t, b, c = rows[dom]
     achieved = b / (t * 1e-3) / 1e9
-    traffic = NCU_TRAFFIC_2048.get(dom)
+    pkey = "mixed" if prec == _lib.MIXED else "fp64"
+    traffic = NCU_TRAFFIC_2048.get(dom, NCU_TRAFFIC_2048.get(f"{dom}_{pkey}"))
     line["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_kind": peak_kind,
                         "traffic": traffic * (N / 2048.0) ** 2 if traffic else None,
@@ -394,10 +399,26 @@ def run_ours(args, dist):
                                           "(cold caches), scaled by cells",
                         "ms_per_launch": t, "algorithmic_bytes": b,
                         "share_of_step": shares[dom] / (1e3 * dev_s / args.steps)}
-    if dom == "advect":
-        line["roofline"]["note"] = "FP64-ALU-bound (FP64 pipe 83% active under ncu); HBM is not the limit"
+    if dom == "advect" and prec == _lib.MIXED:
+        line["roofline"]["note"] = ("issue-bound float-float ENO arithmetic (issue slots 73% active, FP64 pipe "
+                                    "33%, DRAM 12% under ncu); its DRAM traffic equals the algorithmic bytes")
+    elif dom == "advect":
+        line["roofline"]["note"] = "FP64-pipe-bound (FP64 pipe 83% active under ncu); HBM is not the limit"
 
     line["kernels"] = {k: {"ms": t, "per_step": c, "GBs": b / (t * 1e-3) / 1e9} for k, (t, b, c) in rows.items()}
+    if prec == _lib.MIXED:
+        # the FP32 V-cycle with its coarse levels (<= 512 columns) and tail in
+        # one cooperative persistent kernel, against the per-level launches the
+        # run used (same arithmetic, bitwise equal results)
+        sched = {"used": "persistent" if sim.mg_persistent else "per_level", "per_level_ms": t_v32}
+        try:
+            sim.mg_persistent = True
+            sched["persistent_ms"] = sim.time_kernel(DT, 4, 20)
+            sim.mg_persistent = False
+        except _lib.StzgError as e:
+            sched["persistent_ms"] = None
+            sched["persistent_unavailable"] = str(e)
+        line["mg_coarse_schedule"] = sched
     line["mg_hbm_gbs"] = line["kernels"].get("vcycle_fp32", line["kernels"].get("vcycle_fp64"))["GBs"]
     if prec == _lib.MIXED:
         # the two top-level streaming kernels alone (the V-cycle's largest

@@ -203,6 +203,25 @@ int stzg_mg_stencil(stzg_sim *s, double dt, int level, double *out);
  * handle's state is no longer a step of the reference after it). */
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms);
 
+/* No counterpart in the reference (a schedule choice of the GPU multigrid,
+ * same arithmetic either way, results bitwise equal).  on = 1: a
+ * mixed-precision handle runs the FP32 V-cycle's levels of at most 512
+ * columns and its single-block tail in one persistent cooperative kernel
+ * with grid barriers between the level phases, where the device allows.
+ * Off by default: on GB300 at 2048^2 the FP32 V-cycle takes 0.178 ms with
+ * it against 0.145 ms with one launch per level chained by programmatic
+ * dependent launch (0.166 ms with the persistent kernel from 128 columns
+ * down); on = 0 restores the per-level launches.  on = 2 is a test of the kernel's
+ * bounded grid barrier: as 1, and the barrier's arrival count is set so that
+ * the next launch's first barrier never completes; each block gives up after
+ * about a second, the step reports STZG_ECUDA and the handle must be
+ * recreated.  STZG_EINVAL for an FP64 handle or on != 0 where the device does
+ * not take the kernel.  get reports whether a V-cycle of the handle uses it
+ * (0 also where no level qualifies); before the first step has built the
+ * coarse operators, whether it is enabled. */
+int stzg_set_mg_persistent(stzg_sim *s, int on);
+int stzg_get_mg_persistent(stzg_sim *s, int *on);
+
 /* No counterpart in the reference.  Squared residual norms of the
  * quasi-static system for time step dt on caller-owned device arrays,
  * without allocating any device memory: out_dev[0] = sum |b - A z|^2,

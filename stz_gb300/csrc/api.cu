@@ -418,6 +418,7 @@ static int solve_device_loop(stzg_sim *s, int *ncyc) {
     const double r2 = s->hnorm[0], b2 = s->hnorm[1];
     s->acc.checks += passes + 1;
     s->acc.last_error = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    if (s->hflags[FL_MG_BAR_ERR]) return check_flags(s);  // reports and clears the barrier error
     if (err == 2) return fail(STZG_ENAN, "NaN residual");
     if (err == 1) return fail(STZG_ENOTCONV, mixed ? "iterative refinement did not converge"
                                                    : "multigrid did not converge");
@@ -479,6 +480,13 @@ int check_flags(stzg_sim *s) {
         return fail(STZG_ECUDA, "an advection tile copy did not complete in time; tiles of the step were "
                                 "left unwritten, so the handle's state is undefined: recreate the handle");
     if (h[FL_SUBSTEP_CAP]) return fail(STZG_ESUBSTEP, "plastic sub-stepping reached its iteration cap");
+    if (h[FL_MG_BAR_ERR]) {
+        // the barrier's words are left mid-count: clear them for the next launch
+        STZG_CUDA(cudaMemsetAsync(s->F.flags + FL_MG_BAR_ERR, 0, (FL_MG_BAR + 2 - FL_MG_BAR_ERR) * sizeof(int), s->st));
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+        return fail(STZG_ECUDA, "a grid barrier of the persistent coarse multigrid kernel timed out; the "
+                                "velocity of the step is invalid: recreate the handle");
+    }
     return STZG_OK;
 }
 
@@ -572,6 +580,11 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if ((st = s->h64.allocate(s->m, s->n + 1, s->F.vel, s->F.src)) != STZG_OK) return bail(st);
     if (o.precision == STZG_MIXED) {
         if ((st = s->h32.allocate(s->m, s->n + 1, nullptr, nullptr)) != STZG_OK) return bail(st);
+        // the grid barrier of the persistent coarse kernel lives in the handle's
+        // flag words; the kernel is off by default (stzg_set_mg_persistent)
+        s->h32.bar = reinterpret_cast<unsigned *>(s->F.flags + FL_MG_BAR);
+        s->h32.bar_err = s->F.flags + FL_MG_BAR_ERR;
+        s->h32.persist = 0;
         float2 **ffa[4] = {&s->zhi, &s->zlo, &s->bhi, &s->blo};
         for (int k = 0; k < 4; k++)
             if ((st = dev_alloc(s, (void **)ffa[k], nn * sizeof(float2))) != STZG_OK) return bail(st);
@@ -973,6 +986,33 @@ int stzg_download(stzg_sim *s, double *const *down) {
     if (down[7]) jobs.push_back({down[7], s->F.vel, nn * sizeof(double2)});
     if (down[8]) jobs.push_back({down[8], s->F.eps_pl, (size_t)m * s->n * 8});
     return run_copies(s, jobs, cudaMemcpyDeviceToHost);
+}
+
+int stzg_set_mg_persistent(stzg_sim *s, int on) {
+    if (!s || s->O.precision != STZG_MIXED) return fail(STZG_EINVAL, "needs a mixed-precision handle");
+    STZG_CUDA(cudaSetDevice(s->O.device));
+    if (on && !coarse_persist_supported())
+        return fail(STZG_EINVAL, "the device does not take the persistent coarse kernel");
+    if ((on != 0) != (s->h32.persist != 0)) {
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+        drop_graphs(s);  // captured V-cycles used the other schedule
+        s->h32.persist = on ? 1 : 0;
+    }
+    if (on == 2) {
+        // test of the barrier's time limit: an arrival count that no block
+        // completes, so the next persistent launch's first barrier runs out
+        STZG_CUDA(cudaMemsetAsync(s->F.flags + FL_MG_BAR, 0x40, sizeof(int), s->st));
+        STZG_CUDA(cudaStreamSynchronize(s->st));
+    }
+    return STZG_OK;
+}
+
+int stzg_get_mg_persistent(stzg_sim *s, int *on) {
+    if (!s || !on) return fail(STZG_EINVAL, "null argument");
+    if (s->O.precision != STZG_MIXED) *on = 0;
+    else if (!s->h32.bottom_inv) *on = s->h32.persist;  // operators not built yet (first step)
+    else *on = coarse_persist_active(s->h32) ? 1 : 0;
+    return STZG_OK;
 }
 
 int stzg_time_kernel(stzg_sim *s, double dt, int kernel, int reps, double *ms) {

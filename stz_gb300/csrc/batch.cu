@@ -125,8 +125,10 @@ int add_instance(stzg_batch *b, cudaGraph_t root, int k, double dt, int nsteps, 
     const tuning tn = tuning_for(b, s);
     const bool mixed = s->O.precision == STZG_MIXED;
     if (s->h64.tail_limit != tn.tail_limit || s->h64.fuse != tn.fuse || s->h32.tail_limit != tn.tail_limit ||
-        s->h32.fuse != tn.fuse)
+        s->h32.fuse != tn.fuse || s->h32.persist)
         drop_graphs(s);  // the handle's own captured cycles used other knobs
+    // the instances' V-cycles run side by side: no cooperative whole-GPU kernel
+    s->h32.persist = 0;
     s->h64.tail_limit = tn.tail_limit;
     s->h64.fuse = tn.fuse;
     s->h32.tail_limit = tn.tail_limit;

@@ -68,15 +68,44 @@ __device__ __forceinline__ void ff_split_d(double d, float &hi, float &lo) {
     }
 }
 
-// float -> double on the integer pipe (exact for normal floats; zero and
-// subnormal floats give a signed zero, infinity and NaN convert normally).
-__device__ __forceinline__ double ff_f2d(float f) {
+// float -> double bits on the integer pipe (exact for normal floats; zero
+// and subnormal floats give a signed zero, infinity and NaN keep their class
+// and payload).
+__device__ __forceinline__ unsigned long long ff_f2d_bits(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xff;
-    if (e == 255) return (double)f;
+    const unsigned long long man = (unsigned long long)(u & 0x7fffffu) << 29;
     unsigned long long r = (unsigned long long)(u >> 31) << 63;
-    if (e != 0) r |= ((unsigned long long)(e - 127 + 1023) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)r);
+    if (e == 255) r |= 0x7ff0000000000000ull | man;
+    else if (e != 0) r |= ((unsigned long long)(e + 896) << 52) | man;
+    return r;
+}
+__device__ __forceinline__ double ff_f2d(float f) { return __longlong_as_double((long long)ff_f2d_bits(f)); }
+
+// hi + lo as one double without an FP64 instruction, for a pair whose lo is
+// at most one 24-bit ulp of hi with lo's sign or half of it with either sign
+// (ff_fast2sum and ff_split_d leave them so): lo is counted in units of hi's
+// 53-bit ulp (the bits below are dropped, an error below 2^-52 |hi|) and
+// added to hi's bit pattern, which stays in hi's binade except where hi is a
+// power of two and lo of the other sign (then the units are halved).  Pairs
+// with a larger lo take one FP64 addition.
+__device__ __forceinline__ double ff_to_d(float hi, float lo) {
+    const unsigned uh = __float_as_uint(hi), ul = __float_as_uint(lo);
+    const int eh = (uh >> 23) & 0xff, el = (ul >> 23) & 0xff;
+    unsigned long long H = ff_f2d_bits(hi);
+    if (eh == 0 || eh == 255 || el == 0) return __longlong_as_double((long long)H);
+    const int k = eh - el - 29;  // lo = ML * 2^-k units of hi's 53-bit ulp
+    if (k < -5) return __longlong_as_double((long long)H) + ff_f2d(lo);
+    if (k >= 24) return __longlong_as_double((long long)H);
+    const unsigned ml = (1u << 23) | (ul & 0x7fffffu);
+    unsigned long long x = k >= 0 ? (unsigned long long)(ml >> k) : (unsigned long long)ml << (-k);
+    if ((uh ^ ul) >> 31) {
+        if ((H & 0xfffffffffffffull) == 0) x <<= 1;
+        H -= x;
+    } else {
+        H += x;
+    }
+    return __longlong_as_double((long long)H);
 }
 
 // a - b for a = ah + al, b = bh + bl (pairs from ff_split_d), rounded to a

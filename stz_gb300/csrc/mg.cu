@@ -759,7 +759,7 @@ __global__ void k_ff_merge(const float2 *__restrict__ hi, const float2 *__restri
                            long count) {
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
         const float2 h = hi[k], l = lo[k];
-        a[k] = make_double2(ff_f2d(h.x) + ff_f2d(l.x), ff_f2d(h.y) + ff_f2d(l.y));
+        a[k] = make_double2(ff_to_d(h.x, l.x), ff_to_d(h.y, l.y));
     }
 }
 
@@ -1882,7 +1882,7 @@ __device__ void tail_prologue(const tail_levels &tl, const hierarchy_view<T> &H,
     }
     const int mn = S[tl.t].m * S[tl.t].n;
     for (int k = tid; k < mn; k += nth) {
-        S[tl.t].b[k] = H.lv[tl.t].b[k];
+        S[tl.t].b[k] = __ldcg(H.lv[tl.t].b + k);  // written by other blocks in the persistent kernel
         S[tl.t].z[k].x = 0;
         S[tl.t].z[k].y = 0;
     }
@@ -2039,26 +2039,27 @@ __device__ __forceinline__ void tail_pair_sweep(const pair_level &V, int n, int 
     }
 }
 
-__global__ void __launch_bounds__(1024) k_tail_pairs(tail_levels tl, hierarchy_view<float> H) {
-    extern __shared__ __align__(32) unsigned char tail_raw[];
-    __shared__ level_view<float> S[17];
-    __shared__ unsigned offs[17][5];
+// The coarsest inverse copied into the tail's shared memory (when it has a
+// place there), asynchronously: it arrives while the down sweeps run.
+__device__ __forceinline__ void tail_inv_prefetch(const tail_levels &tl, unsigned char *tail_raw, int tid, int nth) {
+    if (tl.inv_off < 0) return;
+    const int N = tl.inv_n;
+    double *dst = reinterpret_cast<double *>(tail_raw + tl.inv_off);
+    for (int k = tid; k < N * N; k += nth) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + k);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(tl.inv + k) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// The pair tail on one block of 32 x nw threads (lane, warp w): levels t ..
+// ml-1 down, the coarsest solve, back up to t; level t's b is read from and
+// its z written to global memory.  S, offs: the caller's shared views.
+__device__ void tail_pairs_body(const tail_levels &tl, const hierarchy_view<float> &H, unsigned char *tail_raw,
+                                level_view<float> *S, unsigned (*offs)[5], int lane, int w, int nw) {
     double *tsh = (double *)tail_raw;
-    const int lane = threadIdx.x, w = threadIdx.y, nw = blockDim.y;
     const int tid = w * 32 + lane, nth = 32 * nw;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int N = tl.inv_n;
-    if (tl.inv_off >= 0) {
-        // the coarsest inverse arrives while the down sweeps run
-        double *dst = reinterpret_cast<double *>(tail_raw + tl.inv_off);
-        for (int k = tid; k < N * N; k += nth) {
-            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + k);
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(tl.inv + k) : "memory");
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    }
-    pdl_trigger();
-    pdl_wait();
     tail_prologue(tl, H, S, tail_raw, tid, nth);
     if (tid == 0)
         for (int l = tl.t; l <= tl.ml; l++) {
@@ -2136,7 +2137,141 @@ __global__ void __launch_bounds__(1024) k_tail_pairs(tail_levels tl, hierarchy_v
     for (int k = tid; k < mn; k += nth) H.lv[tl.t].z[k] = V.z2[k];
 }
 
+__global__ void __launch_bounds__(1024) k_tail_pairs(tail_levels tl, hierarchy_view<float> H) {
+    extern __shared__ __align__(32) unsigned char tail_raw[];
+    __shared__ level_view<float> S[17];
+    __shared__ unsigned offs[17][5];
+    const int lane = threadIdx.x, w = threadIdx.y, nw = blockDim.y;
+    tail_inv_prefetch(tl, tail_raw, w * 32 + lane, 32 * nw);
+    pdl_trigger();
+    pdl_wait();
+    tail_pairs_body(tl, H, tail_raw, S, offs, lane, w, nw);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent coarse kernel: the streaming levels p .. t-1 (all at most
+// kPersistWidth wide), the pair tail on levels t .. ml and the way back up in
+// ONE cooperative launch of one block per SM.  Each level's march down is a
+// phase in which the grid's warps take the level's (strip, row block) units in
+// turn; a grid barrier separates the phases.  Block 0 runs the tail while the
+// others wait at the barrier after it.  Data that other blocks wrote in an
+// earlier phase are read through L2 (__ldcg): L1 is not coherent across SMs.
+// The barrier's waits are bounded: past kBarrierPolls polls the waiting block
+// sets the error word and the whole grid leaves at its next barrier (the
+// V-cycle's result is then invalid and the host reports the error).
+
+#ifndef STZG_PERSIST_WIDTH
+#define STZG_PERSIST_WIDTH 512
+#endif
+#ifndef STZG_BARRIER_SLEEP_NS
+#define STZG_BARRIER_SLEEP_NS 32
+#endif
+constexpr int kPersistWidth = STZG_PERSIST_WIDTH;  // widest level the persistent kernel marches
+constexpr int kPersistWarps = 16;    // warps per block (32 x 16 threads)
+constexpr int kPersistRows = 2;      // coarse rows per march unit
+constexpr long kBarrierPolls = 1L << 21;
+
+struct coarse_plan {
+    int p, t;        // streaming levels [p, t); the tail takes [t, ml]
+    tail_levels tl;
+    unsigned *bar;   // [0] arrivals, [1] generation
+    int *err;        // set to 1 when a barrier wait runs out
+};
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// All blocks of the grid meet here; false when a wait ran out (here or in
+// another block), after which the caller returns.
+__device__ bool grid_barrier(const coarse_plan &cp, unsigned &gen, int *s_ok) {
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        int ok = 1;
+        __threadfence();
+        if (atomicAdd(cp.bar, 1u) == gridDim.x - 1) {
+            atomicExch(cp.bar, 0u);
+            __threadfence();
+            atomicExch(cp.bar + 1, gen + 1);
+        } else {
+            long polls = 0;
+            while (ld_acquire(cp.bar + 1) == gen) {
+                if (++polls > kBarrierPolls) {
+                    atomicExch(cp.err, 1);
+                    ok = 0;
+                    break;
+                }
+                if ((polls & 1023) == 0 && *(volatile int *)cp.err) break;  // another block gave up
+                if (STZG_BARRIER_SLEEP_NS > 0) __nanosleep(STZG_BARRIER_SLEEP_NS);
+            }
+        }
+        gen++;
+        if (ok && *(volatile int *)cp.err) ok = 0;
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+// The level's stencil table into shared memory by the whole block.
+__device__ __forceinline__ void stage_table(stencil9<float> *tab, const level_view<float> &L, int tid, int nth) {
+    const float4 *src = reinterpret_cast<const float4 *>(L.st);
+    float4 *dst = reinterpret_cast<float4 *>(tab);
+    for (int k = tid; k < L.nst * 10; k += nth) dst[k] = __ldg(src + k);
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(32 * kPersistWarps, 1)
+    k_coarse_persist(coarse_plan cp, const __grid_constant__ hierarchy_view<float> H) {
+    extern __shared__ __align__(32) unsigned char tail_raw[];
+    __shared__ stencil9<float> tab[kMarchStencils];
+    __shared__ level_view<float> S[17];
+    __shared__ unsigned offs[17][5];
+    __shared__ int s_ok;
+    if (cp.p > cp.t) return;  // empty plan (set-up probe)
+    // a barrier of an earlier launch timed out: its words are stale until the
+    // host clears them, so this V-cycle is skipped (the host reports the error)
+    if (*(volatile int *)cp.err) return;
+    const int lane = threadIdx.x, w = threadIdx.y, tid = w * 32 + lane, nth = 32 * kPersistWarps;
+    const int gw = blockIdx.x * kPersistWarps + w, nwarps = gridDim.x * kPersistWarps;
+    // the generation cannot move before every block has arrived once
+    unsigned gen = tid == 0 ? ld_acquire(cp.bar + 1) : 0u;
+    if (blockIdx.x == 0) tail_inv_prefetch(cp.tl, tail_raw, tid, nth);
+    for (int l = cp.p; l < cp.t; l++) {
+        const level_view<float> &L = H.lv[l], &C = H.lv[l + 1];
+        stage_table(tab, L, tid, nth);
+        const int strips = (C.m + kLevDownCols - 1) / kLevDownCols;
+        const int units = strips * ((C.n + kPersistRows - 1) / kPersistRows);
+        for (int u = gw; u < units; u += nwarps) {
+            const int sx = u % strips, ry = u / strips;
+            lev_down_march<kPersistRows, true>(L, C, tab, sx * kLevDownCols, ry * kPersistRows, lane);
+        }
+        if (!grid_barrier(cp, gen, &s_ok)) return;
+    }
+    if (blockIdx.x == 0) tail_pairs_body(cp.tl, H, tail_raw, S, offs, lane, w, kPersistWarps);
+    if (!grid_barrier(cp, gen, &s_ok)) return;
+    // the up marches stage the child's strip per warp where the tail was
+    float2 (*czs)[33] = reinterpret_cast<float2 (*)[33]>(tail_raw) + w * (kPersistRows + 3);
+    for (int l = cp.t - 1; l >= cp.p; l--) {
+        const level_view<float> &L = H.lv[l], &C = H.lv[l + 1];
+        stage_table(tab, L, tid, nth);
+        const int strips = (C.m + kLevUpCols - 1) / kLevUpCols;
+        const int units = strips * ((C.n + kPersistRows - 1) / kPersistRows);
+        for (int u = gw; u < units; u += nwarps) {
+            const int sx = u % strips, ry = u / strips;
+            lev_up_march<kPersistRows, true>(L, C, tab, czs, sx * kLevUpCols, ry * kPersistRows, lane);
+            __syncwarp();  // the next unit restages czs
+        }
+        if (l > cp.p && !grid_barrier(cp, gen, &s_ok)) return;
+    }
+}
+
 constexpr size_t kTailSmem = 200 * 1024;
+#ifndef STZG_TAIL_WARPS
+#define STZG_TAIL_WARPS 32
+#endif
 
 // Shared memory of the tail from level t: the same partition as k_tail.
 template <typename T> size_t tail_smem_bytes(const hierarchy<T> &h, int t) {
@@ -2322,6 +2457,140 @@ template <typename T> void launch_top_up(hierarchy<T> &h, cudaStream_t st) {
     }
 }
 
+// Shared memory of the pair tail from level t, with the coarsest inverse
+// after the levels when it fits (its offset in *inv_off, else -1).
+template <typename T> static size_t pair_tail_smem(const hierarchy<T> &h, int t, int *inv_off) {
+    size_t smem = tail_smem_bytes(h, t);
+    *inv_off = -1;
+    const size_t off = (smem + 15) & ~(size_t)15;
+    const size_t need = sizeof(double) * (size_t)h.bottom_unknowns * h.bottom_unknowns;
+    if (off + need <= kTailSmem) {
+        *inv_off = (int)off;
+        smem = off + need;
+    }
+    return smem;
+}
+
+// First level of the persistent coarse kernel for a V-cycle whose tail
+// starts at t, or 0 where it does not apply: levels p .. t-1 stream and are at
+// most kPersistWidth wide, and the tail is a pair tail.
+static int persist_start(const hierarchy<float> &h, int t) {
+    if (!h.persist || !h.bar || !h.bar_err) return 0;
+    const int ml = h.nl - 1;
+    if (t > ml || t < 2 || !pair_tail(h, t)) return 0;
+    int p = t;
+    while (p > 1 && march_level(h, h.lv[p - 1]) && h.lv[p - 1].m <= kPersistWidth) p--;
+    return p < t ? p : 0;
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n < 1) n = 1;
+    }
+    return n;
+}
+
+constexpr size_t kPersistStage = sizeof(float2) * kPersistWarps * (kPersistRows + 3) * 33;
+
+static cudaError_t launch_persist(const coarse_plan &cp, const hierarchy_view<float> &hv, size_t smem,
+                                  cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(sm_count());
+    cfg.blockDim = dim3(32, kPersistWarps);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_coarse_persist, cp, hv);
+}
+
+static void coarse_persist(hierarchy<float> &h, int p, int t, cudaStream_t st) {
+    hierarchy_view<float> hv;
+    for (int l = 0; l < h.nl; l++) hv.lv[l] = h.lv[l];
+    coarse_plan cp;
+    cp.p = p;
+    cp.t = t;
+    cp.tl = tail_levels{t, h.nl - 1, h.bottom_inv, h.bottom_unknowns, -1};
+    size_t smem = pair_tail_smem(h, t, &cp.tl.inv_off);
+    if (smem < kPersistStage) smem = kPersistStage;
+    cp.bar = h.bar;
+    cp.err = h.bar_err;
+    launch_persist(cp, hv, smem, st);
+    note_launch();
+}
+
+__global__ void k_probe_stop(cudaGraphConditionalHandle h) { cudaGraphSetConditional(h, 0); }
+
+bool coarse_persist_supported() {
+    static signed char state[64];
+    static bool init = false;
+    if (!init) {
+        for (auto &x : state) x = -1;
+        init = true;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+    if (state[dev] >= 0) return state[dev] == 1;
+    state[dev] = 0;
+    int coop = 0, nb = 0;
+    const size_t smem = kTailSmem + 1024;
+    bool ok = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
+              cudaFuncSetAttribute(k_coarse_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+                  cudaSuccess &&
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_coarse_persist, 32 * kPersistWarps, smem) ==
+                  cudaSuccess &&
+              nb >= 1;
+    // one empty launch inside a WHILE body that runs once
+    cudaStream_t st = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    if (ok) ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+    cudaGraphConditionalHandle hc;
+    if (ok) ok = cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    cudaGraphNodeParams wp = {};
+    cudaGraphNode_t wnode;
+    if (ok) {
+        wp.type = cudaGraphNodeTypeConditional;
+        wp.conditional.handle = hc;
+        wp.conditional.type = cudaGraphCondTypeWhile;
+        wp.conditional.size = 1;
+        ok = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp) == cudaSuccess;
+    }
+    if (ok) {
+        ok = cudaStreamBeginCaptureToGraph(st, wp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            coarse_plan cp = {};
+            cp.p = 1;
+            cp.t = 0;  // empty
+            cp.tl.inv_off = -1;
+            hierarchy_view<float> hv = {};
+            bool launched = launch_persist(cp, hv, smem, st) == cudaSuccess;
+            k_probe_stop<<<1, 1, 0, st>>>(hc);
+            cudaGraph_t got = nullptr;
+            ok = cudaStreamEndCapture(st, &got) == cudaSuccess && launched;
+        }
+    }
+    if (ok) ok = cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+    if (ok) ok = cudaGraphLaunch(ex, st) == cudaSuccess && cudaStreamSynchronize(st) == cudaSuccess;
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    if (st) cudaStreamDestroy(st);
+    cudaGetLastError();  // a refused form leaves a non-sticky error behind
+    state[dev] = ok ? 1 : 0;
+    return ok;
+}
+
+bool coarse_persist_active(const hierarchy<float> &h) { return persist_start(h, tail_start(h)) > 0; }
+
 template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_sweeps, int bottom_fp64, bool zero_start) {
     typedef typename vec2_t<T>::type V;
     dim3 blk(32, 8);
@@ -2345,7 +2614,10 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
                                                                        h.lv[1].n);
         note_launch();
     }
-    const int down_end = t <= ml ? t : ml;  // levels [1, down_end) go down outside the tail
+    int p = 0;  // first level of the persistent coarse kernel (0: none)
+    if constexpr (sizeof(T) == 4) p = persist_start(h, t);
+    // levels [1, down_end) go down outside the tail (and the persistent kernel)
+    const int down_end = p ? p : (t <= ml ? t : ml);
     for (int i = 1; i < down_end; i++) {
         level_view<T> &L = h.lv[i];
         level_view<T> &C = h.lv[i + 1];
@@ -2365,23 +2637,19 @@ template <typename T> void vcycle(hierarchy<T> &h, cudaStream_t st, int bottom_s
         note_launch();
     }
     int up_from;
-    if (t <= ml) {
+    if (p) {
+        if constexpr (sizeof(T) == 4) coarse_persist(h, p, t, st);
+        up_from = p;
+    } else if (t <= ml) {
         hierarchy_view<T> hv;
         for (int l = 0; l < h.nl; l++) hv.lv[l] = h.lv[l];
         tail_levels tl{t, ml, h.bottom_inv, h.bottom_unknowns, -1};
         size_t smem = tail_smem_bytes(h, t);
-        if (sizeof(T) == 4 && pair_tail(h, t)) {
-            // room for a copy of the coarsest inverse after the levels
-            const size_t off = (smem + 15) & ~(size_t)15;
-            const size_t need = sizeof(double) * (size_t)h.bottom_unknowns * h.bottom_unknowns;
-            if (off + need <= kTailSmem) {
-                tl.inv_off = (int)off;
-                smem = off + need;
-            }
-        }
+        // room for a copy of the coarsest inverse after the levels
+        if (sizeof(T) == 4 && pair_tail(h, t)) smem = pair_tail_smem(h, t, &tl.inv_off);
         if constexpr (sizeof(T) == 4) {
             if (pair_tail(h, t))
-                launch_pdl(k_tail_pairs, dim3(1), dim3(32, 32), smem, st, tl, hv);
+                launch_pdl(k_tail_pairs, dim3(1), dim3(32, STZG_TAIL_WARPS), smem, st, tl, hv);
             else
                 k_tail<T><<<1, dim3(32, 32), smem, st>>>(tl, hv);
         } else {

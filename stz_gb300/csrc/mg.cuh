@@ -95,6 +95,15 @@ template <typename T> class hierarchy {
     // and whether wide single-precision levels use the fused tile kernels
     long tail_limit = -1;
     int fuse = 1;
+    // single precision: the coarse levels at most 512 wide and the tail in
+    // one cooperative persistent kernel (set by the owner once
+    // coarse_persist_supported() holds; bar: two zeroed device words for its
+    // grid barrier, bar_err: a device word it sets when a barrier wait runs
+    // out).  Off for hierarchies whose V-cycles may run concurrently with
+    // other kernels (batched graphs).
+    int persist = 0;
+    unsigned *bar = nullptr;
+    int *bar_err = nullptr;
     void release();
     ~hierarchy() { release(); }
     size_t device_bytes() const { return bytes_; }
@@ -115,6 +124,13 @@ template <typename T> void top_sweep(hierarchy<T> &h, cudaStream_t st);
 // One launch of the streaming top-level kernel down (0) or up (1) of the FP32
 // V-cycle, for timing; false where the top level does not use them.
 bool top_level_kernel(hierarchy<float> &h, int which, cudaStream_t st);
+// Whether this device takes the persistent coarse kernel: cooperative
+// launches, one block per SM with the tail's shared memory, and a launch
+// inside a conditional (WHILE) graph body, tried once per process on a
+// private stream with an empty plan.  Call outside any stream capture.
+bool coarse_persist_supported();
+// Whether a V-cycle of h would use the persistent coarse kernel.
+bool coarse_persist_active(const hierarchy<float> &h);
 
 // Sum of squared residuals of the top level into *out (device), optional
 // sum of squared b into *out_b.  Deterministic: fixed grid, ordered final sum.

@@ -421,6 +421,8 @@ struct adv_smem_ff {
             float dyl[F_COUNT][ADYH][ATX];
         } d;
     } u;
+    ff nu[ATY + 1][ATX + 1];  // node velocities (i0+c, j0+r) as pairs, walls substituted
+    ff nv[ATY + 1][ATX + 1];
     int xs[ACOLS];   // period shift of the unwrapped column: -1, 0, +1
     int col[ACOLS];  // storage column of tile column c-2
     uint64_t bar;
@@ -509,7 +511,8 @@ __device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float 
         else take_outer = exact();
     }
     // outer: from the left Db - Da, from the right Dc - Db
-    const ff s = (from_left == take_outer) ? ff_sub(Db, Da) : ff_sub(Dc, Db);
+    const bool lower = from_left == take_outer;
+    const ff s = ff_sub(lower ? Db : Dc, lower ? Da : Db);
     return ff_add(from_left ? ff_x2(Db) : ff_neg(ff_x2(Db)), s);
 }
 
@@ -553,8 +556,9 @@ __device__ __forceinline__ ff eno_y_ff(const adv_smem_ff &Sm, const eno_ctx &e, 
 __device__ __forceinline__ ff upwind_inc(ff uh, ff ex, ff vh, ff ey) {
     return ff_neg(ff_add(ff_mul(uh, ex), ff_mul(vh, ey)));
 }
-// a + inc for the FP64 state value a: the high part, then the low part
-__device__ __forceinline__ double add_ff(double a, ff inc) { return (a + ff_f2d(inc.hi)) + ff_f2d(inc.lo); }
+// a + inc for the FP64 state value a with one FP64 addition (the pair formed
+// as a double on the integer pipe)
+__device__ __forceinline__ double add_ff(double a, ff inc) { return a + ff_to_d(inc.hi, inc.lo); }
 // u > 0 for a finite double, on the integer pipe
 __device__ __forceinline__ bool dpos(double u) { return __double_as_longlong(u) > 0; }
 
@@ -601,6 +605,18 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
         mbar_expect_tx(&Sm.bar, kTileBytes);
         for (int f = 0; f < F_COUNT; f++) tma_load_2d(&Sm.u.tile[f][0][0], &maps.f[cur][f], i0 - 2, j0 - 1, &Sm.bar);
     }
+    // node velocities of the block as pairs while the tile arrives
+    if (c.clock) bv = c.clock[CLK_BV_STATE];
+    {
+        const velo_ff V{F.vel, m, n, split_ff(bv)};
+        for (int p = tid; p < (ATY + 1) * (ATX + 1); p += ATX * ATY) {
+            const int r = p / (ATX + 1), cc = p - r * (ATX + 1), nj = j0 + r;
+            if (nj > n) continue;
+            const int ni = Sm.col[cc + 2];
+            Sm.nu[r][cc] = V.u(ni, nj);
+            Sm.nv[r][cc] = V.v(ni, nj);
+        }
+    }
     if (__syncthreads_or(!mbar_wait_bounded(&Sm.bar))) {
         if (tid == 0) atomicExch(&F.flags[FL_TMA], 1);
         mbar_wait_bounded(&Sm.bar);
@@ -616,46 +632,55 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
         }
         __syncthreads();
     }
-    // split every staged value into a float pair
-    for (int k = tid; k < kTileVals; k += ATX * ATY) {
-        const int f = k / (AROWS * ACOLS), rem = k - f * (AROWS * ACOLS), r = rem / ACOLS, t = rem - r * ACOLS;
-        ff_split_d(Sm.u.tile[f][r][t], Sm.th[f][r][t], Sm.tl[f][r][t]);
+    // split every staged value into a float pair (one position per thread and
+    // pass, all fields: the position's index arithmetic is done once)
+    for (int p = tid; p < AROWS * ACOLS; p += ATX * ATY) {
+        const int r = p / ACOLS, t = p - r * ACOLS;
+#pragma unroll
+        for (int f = 0; f < F_COUNT; f++) ff_split_d(Sm.u.tile[f][r][t], Sm.th[f][r][t], Sm.tl[f][r][t]);
     }
     __syncthreads();
     // first differences: x on cell rows j0..j0+ATY-1, y on rows j0-2..j0+ATY+1;
     // X across the periodic seam gets the period (the unwrapped difference)
     const ff lx{h.lxh, h.lxl};
-    for (int k = tid; k < F_COUNT * ATY * ADXW; k += ATX * ATY) {
-        const int f = k / (ATY * ADXW), rem = k - f * (ATY * ADXW), r = rem / ADXW, cc = rem - r * ADXW;
-        ff d{0.f, 0.f};
-        if (j0 + r < n) {
-            d = ff_pair_diff(Sm.th[f][r + 2][cc + 1], Sm.tl[f][r + 2][cc + 1], Sm.th[f][r + 2][cc], Sm.tl[f][r + 2][cc]);
-            const int sh = Sm.xs[cc + 1] - Sm.xs[cc];
-            if (f == F_X && sh != 0) d = ff_add(d, sh > 0 ? lx : ff_neg(lx));
+    for (int p = tid; p < ATY * ADXW; p += ATX * ATY) {
+        const int r = p / ADXW, cc = p - r * ADXW;
+        const bool live = j0 + r < n;
+        const int sh = Sm.xs[cc + 1] - Sm.xs[cc];
+#pragma unroll
+        for (int f = 0; f < F_COUNT; f++) {
+            ff d{0.f, 0.f};
+            if (live) {
+                d = ff_pair_diff(Sm.th[f][r + 2][cc + 1], Sm.tl[f][r + 2][cc + 1], Sm.th[f][r + 2][cc],
+                                 Sm.tl[f][r + 2][cc]);
+                if (f == F_X && sh != 0) d = ff_add(d, sh > 0 ? lx : ff_neg(lx));
+            }
+            Sm.u.d.dxh[f][r][cc] = d.hi;
+            Sm.u.d.dxl[f][r][cc] = d.lo;
         }
-        Sm.u.d.dxh[f][r][cc] = d.hi;
-        Sm.u.d.dxl[f][r][cc] = d.lo;
     }
-    for (int k = tid; k < F_COUNT * ADYH * ATX; k += ATX * ATY) {
-        const int f = k / (ADYH * ATX), rem = k - f * (ADYH * ATX), r = rem / ATX, cc = rem - r * ATX;
+    for (int p = tid; p < ADYH * ATX; p += ATX * ATY) {
+        const int r = p / ATX, cc = p - r * ATX;
         const int jj = j0 + r - 2;
-        ff d{0.f, 0.f};
-        if (jj >= -1 && jj + 1 <= n && i0 + cc < m)
-            d = ff_pair_diff(Sm.th[f][r + 1][cc + 2], Sm.tl[f][r + 1][cc + 2], Sm.th[f][r][cc + 2], Sm.tl[f][r][cc + 2]);
-        Sm.u.d.dyh[f][r][cc] = d.hi;
-        Sm.u.d.dyl[f][r][cc] = d.lo;
+        const bool live = jj >= -1 && jj + 1 <= n && i0 + cc < m;
+#pragma unroll
+        for (int f = 0; f < F_COUNT; f++) {
+            ff d{0.f, 0.f};
+            if (live)
+                d = ff_pair_diff(Sm.th[f][r + 1][cc + 2], Sm.tl[f][r + 1][cc + 2], Sm.th[f][r][cc + 2],
+                                 Sm.tl[f][r][cc + 2]);
+            Sm.u.d.dyh[f][r][cc] = d.hi;
+            Sm.u.d.dyl[f][r][cc] = d.lo;
+        }
     }
     __syncthreads();
     if (i >= m || j >= n) return;
     const ff hx{h.hxh, h.hxl}, hy{h.hyh, h.hyl};
     const size_t ci = (size_t)(j + 1) * m + i;
     const eno_ctx e{A, m, n, j0, j, c.lx};
-    const int ir = Sm.col[tx + 3];
-    if (c.clock) bv = c.clock[CLK_BV_STATE];
-    const velo_ff V{F.vel, m, n, split_ff(bv)};
     // reference map at node (i,j), rows 1..n-1 (shear_sim.cc:310-327)
     if (j > 0) {
-        const ff un = V.u(i, j), vn = V.v(i, j);
+        const ff un = Sm.nu[ty][tx], vn = Sm.nv[ty][tx];
         const bool ru = un.hi > 0.f, rv = vn.hi > 0.f;
         const ff uh = ff_mul(un, ru ? hx : ff_neg(hx)), vh = ff_mul(vn, rv ? hy : ff_neg(hy));
         const bool inner = rv ? j > 1 : j < n - 1;
@@ -666,8 +691,8 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
         }
     }
     // staggered velocity and spin (shear_sim.cc:330-333) in pairs
-    const ff u00 = V.u(i, j), u10 = V.u(ir, j), u01 = V.u(i, j + 1), u11 = V.u(ir, j + 1);
-    const ff v00 = V.v(i, j), v10 = V.v(ir, j), v01 = V.v(i, j + 1), v11 = V.v(ir, j + 1);
+    const ff u00 = Sm.nu[ty][tx], u10 = Sm.nu[ty][tx + 1], u01 = Sm.nu[ty + 1][tx], u11 = Sm.nu[ty + 1][tx + 1];
+    const ff v00 = Sm.nv[ty][tx], v10 = Sm.nv[ty][tx + 1], v01 = Sm.nv[ty + 1][tx], v11 = Sm.nv[ty + 1][tx + 1];
     ff uc = ff_add(ff_add(u00, u10), ff_add(u01, u11)), vc = ff_add(ff_add(v00, v10), ff_add(v01, v11));
     uc = ff{0.25f * uc.hi, 0.25f * uc.lo};
     vc = ff{0.25f * vc.hi, 0.25f * vc.lo};
@@ -951,8 +976,8 @@ __global__ void __launch_bounds__(SFX * SFY) k_source_ff(step_consts c, fields_d
         const ff dTx = ff_add(ff_sub(cT[ty][tx], cT[ty][tx + 1]), ff_sub(cT[ty + 1][tx], cT[ty + 1][tx + 1]));
         const ff xf{h.xfh, h.xfl}, yf{h.yfh, h.yfl};
         const ff fx = ff_add(ff_mul(xf, dAx), ff_mul(yf, dTy)), fy = ff_add(ff_mul(xf, dTx), ff_mul(yf, dBy));
-        out.x = ff_f2d(fx.hi) + ff_f2d(fx.lo);
-        out.y = ff_f2d(fy.hi) + ff_f2d(fy.lo);
+        out.x = ff_to_d(fx.hi, fx.lo);
+        out.y = ff_to_d(fy.hi, fy.lo);
     }
     F.src[(size_t)j * m + i] = out;
 }

@@ -13,7 +13,17 @@ namespace stzg {
 // buffer `cur` and writes buffer `cur^1`.
 enum { F_P = 0, F_Q, F_S, F_TAU, F_CHI, F_X, F_Y, F_COUNT };
 // Slots of fields_dev::flags.
-enum { FL_SUBSTEP_CAP = 0, FL_SUBSTEP_MAX, FL_VEL_CHANGED, FL_TMA, FL_PASSES, FL_LOOP_ERR, FL_COUNT = 8 };
+enum {
+    FL_SUBSTEP_CAP = 0,
+    FL_SUBSTEP_MAX,
+    FL_VEL_CHANGED,
+    FL_TMA,
+    FL_PASSES,
+    FL_LOOP_ERR,
+    FL_MG_BAR_ERR,  // a grid-barrier wait of the persistent coarse multigrid kernel ran out
+    FL_MG_BAR = 8,  // two words: that barrier's arrivals and generation
+    FL_COUNT = 12
+};
 
 struct fields_dev {
     double *f[2][F_COUNT];
@@ -24,7 +34,8 @@ struct fields_dev {
     int *flags;      // FL_COUNT ints: [0] plastic sub-step cap reached, [1] max sub-steps,
                      // [2] scratch of the velocity upload, [3] an advection tile copy wait
                      // ran out, [4] passes of the last device-loop solve, [5] its error
-                     // (1 pass cap reached, 2 NaN residual)
+                     // (1 pass cap reached, 2 NaN residual), [6] a coarse-kernel barrier
+                     // wait ran out, [8..9] that barrier's words
     // Per-cell combinations of the advected stress that the nodal net force
     // (shear_sim::net_force, shear_sim.cc:447-453) sums with +-1 weights:
     // U = xf A + yf tau, W = xf A - yf tau, Y1 = xf tau - yf B,

@@ -154,6 +154,18 @@ class ShearSim:
         self.cycles += st.vcycles
         return st.vcycles
 
+    @property
+    def mg_persistent(self):
+        """Whether the FP32 V-cycle runs its coarse levels and tail in one
+        persistent kernel (stzg_get_mg_persistent)."""
+        on = ctypes.c_int()
+        _lib.check(self.lib.stzg_get_mg_persistent(self.h, ctypes.byref(on)))
+        return bool(on.value)
+
+    @mg_persistent.setter
+    def mg_persistent(self, on):
+        _lib.check(self.lib.stzg_set_mg_persistent(self.h, int(bool(on))))
+
     def time_kernel(self, dt, kernel, reps=10):
         """Average ms per launch of one kernel group (stzg_time_kernel)."""
         ms = ctypes.c_double()
