@@ -272,7 +272,11 @@ int solve_mixed(stzg_sim *s, int *ncyc) {
 // is tested first: a warm start that already meets the tolerance runs no
 // pass.  A pass cap (the tgmg_predict threshold, tgmg_config.hh:26-45, in
 // V-cycles) ends a solve that does not converge, with an error flag.
-__global__ void k_loop_start(const double *dnorm, int *flags, double tol2, cudaGraphConditionalHandle h) {
+// h_ran: the IF node after the loop (the float-float merge of the mixed
+// solve), taken only when a pass ran: otherwise the FP64 velocity is still
+// the solution and stays as it is.
+__global__ void k_loop_start(const double *dnorm, int *flags, double tol2, cudaGraphConditionalHandle h,
+                             cudaGraphConditionalHandle h_ran, int has_ran) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         const double r2 = dnorm[0], b2 = dnorm[1];
         const bool conv = b2 > 0 ? r2 <= tol2 * b2 : r2 == 0;
@@ -280,6 +284,7 @@ __global__ void k_loop_start(const double *dnorm, int *flags, double tol2, cudaG
         flags[FL_PASSES] = 0;
         flags[FL_LOOP_ERR] = nan ? 2 : 0;
         cudaGraphSetConditional(h, (!conv && !nan) ? 1u : 0u);
+        if (has_ran) cudaGraphSetConditional(h_ran, (!conv && !nan) ? 1u : 0u);
     }
 }
 
@@ -319,8 +324,9 @@ static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
     const int per_pass = mixed ? inner : 1;
     cudaGraph_t root = nullptr;
     STZG_CUDA(cudaGraphCreate(&root, 0));
-    cudaGraphConditionalHandle h;
+    cudaGraphConditionalHandle h, h_ran = 0;
     cudaError_t e = cudaGraphConditionalHandleCreate(&h, root, 0, 0);
+    if (e == cudaSuccess && mixed) e = cudaGraphConditionalHandleCreate(&h_ran, root, 0, 0);
     if (e != cudaSuccess) {
         cudaGraphDestroy(root);
         return cuda_fail(e, "cudaGraphConditionalHandleCreate");
@@ -336,7 +342,7 @@ static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
     // set-up: initial residual of the warm start, then the loop and the finish
     if (mixed) mixed_begin(s);
     launch_norms(s, mixed);
-    k_loop_start<<<1, 32, 0, s->st>>>(s->dnorm, s->F.flags, tol2, h);
+    k_loop_start<<<1, 32, 0, s->st>>>(s->dnorm, s->F.flags, tol2, h, h_ran, mixed ? 1 : 0);
     note_launch();
     {
         cudaStreamCaptureStatus cs;
@@ -360,14 +366,50 @@ static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
         cudaGraphDestroy(root);
         return abandon_capture(s, st);
     }
-    if (mixed) mixed_end(s);
-    else
+    cudaGraphNodeParams ip = {};  // mixed: IF a pass ran { merge }
+    if (mixed) {
+        cudaStreamCaptureStatus cs;
+        cudaGraph_t cg;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t ndeps = 0;
+        e = cudaStreamGetCaptureInfo(s->st, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+        cudaGraphNode_t inode;
+        if (e == cudaSuccess) {
+            ip.type = cudaGraphNodeTypeConditional;
+            ip.conditional.handle = h_ran;
+            ip.conditional.type = cudaGraphCondTypeIf;
+            ip.conditional.size = 1;
+            e = cudaGraphAddNode(&inode, cg, deps, nullptr, ndeps, &ip);
+        }
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(s->st, &inode, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(root);
+            return abandon_capture(s, cuda_fail(e, "conditional node"));
+        }
+    } else {
         for (int c = 0; c < s->extra_iters; c++) vcycle<double>(s->h64, s->st, 10, 1);
+    }
     cudaGraph_t got = nullptr;
     e = cudaStreamEndCapture(s->st, &got);
     if (e != cudaSuccess) {
         cudaGraphDestroy(root);
         return cuda_fail(e, "cudaStreamEndCapture");
+    }
+    const long cm0 = launch_count();
+    if (mixed) {
+        e = cudaStreamBeginCaptureToGraph(s->st, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(root);
+            return cuda_fail(e, "cudaStreamBeginCaptureToGraph(merge)");
+        }
+        mixed_end(s);
+        e = cudaStreamEndCapture(s->st, &got);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(root);
+            return cuda_fail(e, "cudaStreamEndCapture(merge)");
+        }
     }
     const long c1 = launch_count();
     // loop body: one pass and the convergence test
@@ -393,7 +435,8 @@ static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
     }
     const long c2 = launch_count();
     discount_launches(c2 - c0);  // graph nodes, counted when they execute
-    s->n_loop_outer = c1 - c0;
+    s->n_loop_merge = c1 - cm0;
+    s->n_loop_outer = cm0 - c0;
     s->n_loop_body = c2 - c1;
     e = cudaGraphInstantiate(&s->g_loop, root, 0);
     cudaGraphDestroy(root);
@@ -414,7 +457,7 @@ static int solve_device_loop(stzg_sim *s, int *ncyc) {
     STZG_CUDA(cudaMemcpyAsync(s->hnorm, s->dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
     STZG_CUDA(cudaStreamSynchronize(s->st));
     const int passes = s->hflags[FL_PASSES], err = s->hflags[FL_LOOP_ERR];
-    g_launches.fetch_add(s->n_loop_outer + passes * s->n_loop_body);
+    g_launches.fetch_add(s->n_loop_outer + (passes > 0 ? s->n_loop_merge : 0) + passes * s->n_loop_body);
     const double r2 = s->hnorm[0], b2 = s->hnorm[1];
     s->acc.checks += passes + 1;
     s->acc.last_error = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);

@@ -44,7 +44,7 @@ struct stzg_sim {
     // graph (set-up, WHILE node over passes, finish); kernel nodes outside
     // and inside the loop body
     cudaGraphExec_t g_loop = nullptr;
-    long n_loop_outer = 0, n_loop_body = 0;
+    long n_loop_outer = 0, n_loop_body = 0, n_loop_merge = 0;
     int g_loop_inner = 0;
     int *hflags = nullptr;  // pinned host copy of F.flags (FL_COUNT ints)
     double2 *vel_prev = nullptr;  // previous solution (extrapolated guesses)

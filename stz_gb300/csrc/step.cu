@@ -922,8 +922,9 @@ __global__ void k_source(step_consts c, fields_dev F, double xbc_bv) {
 
 // The projection source of the float-float path (k_advect_ff writes no
 // per-cell combinations): net_force (shear_sim.cc:447-453) at the interior
-// nodes from the stresses of the four surrounding cells.  A block of 32 x 8
-// nodes first forms, for each of the 33 x 9 cells around it, the pairs
+// nodes from the stresses of the four surrounding cells.  A block of 32 x 32
+// nodes (four rows per thread) first forms, for each of the 33 x 33 cells
+// around it, the pairs
 // A = p + q - s, B = p + q + s and tau from the split stresses (float-float
 // sums, error ~2^-47 of the values) in shared memory; each node then takes
 // the cell-to-cell differences of those pairs, whose high parts cancel
@@ -934,21 +935,25 @@ struct source_ff_consts {
     float xfh, xfl, yfh, yfl;
 };
 
-constexpr int SFX = 32, SFY = 8;
+constexpr int SFX = 32, SFY = 8;  // threads of a block
+constexpr int SFR = 4;            // node (cell) rows per thread: a block covers 32 x 32
 
 __global__ void __launch_bounds__(SFX * SFY) k_source_ff(step_consts c, fields_dev F, int cur, source_ff_consts h,
                                                          double xbc_bv) {
-    __shared__ ff cA[SFY + 1][SFX + 1], cB[SFY + 1][SFX + 1], cT[SFY + 1][SFX + 1];
+    constexpr int TY = SFY * SFR;  // node rows of the block
+    __shared__ ff cA[TY + 1][SFX + 1], cB[TY + 1][SFX + 1], cT[TY + 1][SFX + 1];
     const int m = c.m, n = c.n;
     if (c.clock) {
         xbc_bv = c.xbc * c.clock[CLK_BV];
         cur = (int)c.clock[CLK_CUR] ^ 1;  // the state the advection wrote
     }
-    const int i0 = blockIdx.x * SFX, j0 = blockIdx.y * SFY;
+    const int i0 = blockIdx.x * SFX, j0 = blockIdx.y * TY;
     const int tid = threadIdx.y * SFX + threadIdx.x;
     const double *P = F.f[cur][F_P], *Q = F.f[cur][F_Q], *S = F.f[cur][F_S], *T = F.f[cur][F_TAU];
-    // cells (i0 - 1 + cc, j0 - 1 + r); storage rows -1 .. n exist
-    for (int k = tid; k < (SFY + 1) * (SFX + 1); k += SFX * SFY) {
+    // cells (i0 - 1 + cc, j0 - 1 + r); storage rows -1 .. n exist (unrolled:
+    // the loads of all passes in flight together)
+#pragma unroll
+    for (int k = tid; k < (TY + 1) * (SFX + 1); k += SFX * SFY) {
         const int r = k / (SFX + 1), cc = k - r * (SFX + 1);
         const int cj = j0 - 1 + r;
         int ci = i0 - 1 + cc;
@@ -962,24 +967,29 @@ __global__ void __launch_bounds__(SFX * SFY) k_source_ff(step_consts c, fields_d
         cT[r][cc] = split_ff(T[q]);
     }
     __syncthreads();
-    const int tx = threadIdx.x, ty = threadIdx.y, i = i0 + tx, j = j0 + ty;
-    if (i >= m || j > n) return;
-    double2 out;
-    if (j == 0 || j == n) {
-        out.x = j == 0 ? -xbc_bv : xbc_bv;
-        out.y = 0;
-    } else {
-        // cells k0 = (i-1, j-1), k1 = (i, j-1), k2 = (i-1, j), k3 = (i, j)
-        const ff dAx = ff_add(ff_sub(cA[ty][tx + 1], cA[ty][tx]), ff_sub(cA[ty + 1][tx + 1], cA[ty + 1][tx]));
-        const ff dBy = ff_add(ff_sub(cB[ty + 1][tx], cB[ty][tx]), ff_sub(cB[ty + 1][tx + 1], cB[ty][tx + 1]));
-        const ff dTy = ff_add(ff_sub(cT[ty][tx], cT[ty + 1][tx]), ff_sub(cT[ty][tx + 1], cT[ty + 1][tx + 1]));
-        const ff dTx = ff_add(ff_sub(cT[ty][tx], cT[ty][tx + 1]), ff_sub(cT[ty + 1][tx], cT[ty + 1][tx + 1]));
-        const ff xf{h.xfh, h.xfl}, yf{h.yfh, h.yfl};
-        const ff fx = ff_add(ff_mul(xf, dAx), ff_mul(yf, dTy)), fy = ff_add(ff_mul(xf, dTx), ff_mul(yf, dBy));
-        out.x = ff_to_d(fx.hi, fx.lo);
-        out.y = ff_to_d(fy.hi, fy.lo);
+    const int tx = threadIdx.x, i = i0 + tx;
+    if (i >= m) return;
+    const ff xf{h.xfh, h.xfl}, yf{h.yfh, h.yfl};
+#pragma unroll
+    for (int q = 0; q < SFR; q++) {
+        const int ty = threadIdx.y + q * SFY, j = j0 + ty;
+        if (j > n) break;
+        double2 out;
+        if (j == 0 || j == n) {
+            out.x = j == 0 ? -xbc_bv : xbc_bv;
+            out.y = 0;
+        } else {
+            // cells k0 = (i-1, j-1), k1 = (i, j-1), k2 = (i-1, j), k3 = (i, j)
+            const ff dAx = ff_add(ff_sub(cA[ty][tx + 1], cA[ty][tx]), ff_sub(cA[ty + 1][tx + 1], cA[ty + 1][tx]));
+            const ff dBy = ff_add(ff_sub(cB[ty + 1][tx], cB[ty][tx]), ff_sub(cB[ty + 1][tx + 1], cB[ty][tx + 1]));
+            const ff dTy = ff_add(ff_sub(cT[ty][tx], cT[ty + 1][tx]), ff_sub(cT[ty][tx + 1], cT[ty + 1][tx + 1]));
+            const ff dTx = ff_add(ff_sub(cT[ty][tx], cT[ty][tx + 1]), ff_sub(cT[ty + 1][tx], cT[ty + 1][tx + 1]));
+            const ff fx = ff_add(ff_mul(xf, dAx), ff_mul(yf, dTy)), fy = ff_add(ff_mul(xf, dTx), ff_mul(yf, dBy));
+            out.x = ff_to_d(fx.hi, fx.lo);
+            out.y = ff_to_d(fy.hi, fy.lo);
+        }
+        F.src[(size_t)j * m + i] = out;
     }
-    F.src[(size_t)j * m + i] = out;
 }
 
 // Stress correction from the solved velocity (shear_sim.cc:418-434).
@@ -1004,8 +1014,8 @@ __global__ void k_project(step_consts c, fields_dev F, int cur, double hx, doubl
 }
 
 // The stress correction of the float-float path: each node's velocity is
-// split into float pairs once (a block of 32 x 8 cells stages its 33 x 9
-// nodes in shared memory), the velocity differences of k_project are taken
+// split into float pairs once (a block of 32 x 32 cells, four rows per
+// thread, stages its 33 x 33 nodes in shared memory), the velocity differences of k_project are taken
 // from the pairs, the products with hx, hy, K, mu/3 and mu in pairs, and each
 // stress component takes its correction with two FP64 additions.
 struct project_ff_consts {
@@ -1013,13 +1023,15 @@ struct project_ff_consts {
 };
 
 __global__ void __launch_bounds__(SFX * SFY) k_project_ff(step_consts c, fields_dev F, int cur, project_ff_consts h) {
-    // velocities of the block's 33 x 9 nodes as pairs, split once each
-    __shared__ ff nU[SFY + 1][SFX + 1], nV[SFY + 1][SFX + 1];
+    constexpr int TY = SFY * SFR;  // cell rows of the block
+    // velocities of the block's 33 x 33 nodes as pairs, split once each
+    __shared__ ff nU[TY + 1][SFX + 1], nV[TY + 1][SFX + 1];
     const int m = c.m, n = c.n;
     if (c.clock) cur = (int)c.clock[CLK_CUR] ^ 1;  // the state the advection wrote
-    const int i0 = blockIdx.x * SFX, j0 = blockIdx.y * SFY;
+    const int i0 = blockIdx.x * SFX, j0 = blockIdx.y * TY;
     const int tid = threadIdx.y * SFX + threadIdx.x;
-    for (int k = tid; k < (SFY + 1) * (SFX + 1); k += SFX * SFY) {
+#pragma unroll
+    for (int k = tid; k < (TY + 1) * (SFX + 1); k += SFX * SFY) {
         const int r = k / (SFX + 1), cc = k - r * (SFX + 1);
         const int nj = j0 + r;
         int ni = i0 + cc;
@@ -1030,21 +1042,28 @@ __global__ void __launch_bounds__(SFX * SFY) k_project_ff(step_consts c, fields_
         nV[r][cc] = split_ff(v.y);
     }
     __syncthreads();
-    const int tx = threadIdx.x, ty = threadIdx.y, i = i0 + tx, j = j0 + ty;
-    if (i >= m || j >= n) return;
-    // nodes a = (i, j), b = (i+1, j), c = (i, j+1), d = (i+1, j+1)
-    const ff ax = nU[ty][tx], bx = nU[ty][tx + 1], cx = nU[ty + 1][tx], dx = nU[ty + 1][tx + 1];
-    const ff ay = nV[ty][tx], by = nV[ty][tx + 1], cy = nV[ty + 1][tx], dy = nV[ty + 1][tx + 1];
+    const int tx = threadIdx.x, i = i0 + tx;
+    if (i >= m) return;
     const ff hx{h.hxh, h.hxl}, hy{h.hyh, h.hyl};
-    const ff ux = ff_mul(hx, ff_add(ff_sub(bx, ax), ff_sub(dx, cx))), uy = ff_mul(hy, ff_add(ff_sub(cx, ax), ff_sub(dx, bx)));
-    const ff vx = ff_mul(hx, ff_add(ff_sub(by, ay), ff_sub(dy, cy))), vy = ff_mul(hy, ff_add(ff_sub(cy, ay), ff_sub(dy, by)));
-    const ff div = ff_add(ux, vy);
-    const size_t k = IDX(i, j);
     double *const *S = F.f[cur];
-    S[F_P][k] = add_ff(S[F_P][k], ff_neg(ff_mul(ff{h.Kh, h.Kl}, div)));
-    S[F_Q][k] = add_ff(S[F_Q][k], ff_neg(ff_mul(ff{h.m3h, h.m3l}, div)));
-    S[F_S][k] = add_ff(S[F_S][k], ff_mul(ff{h.muh, h.mul}, ff_sub(ux, vy)));
-    S[F_TAU][k] = add_ff(S[F_TAU][k], ff_mul(ff{h.muh, h.mul}, ff_add(uy, vx)));
+#pragma unroll
+    for (int q = 0; q < SFR; q++) {
+        const int ty = threadIdx.y + q * SFY, j = j0 + ty;
+        if (j >= n) break;
+        // nodes a = (i, j), b = (i+1, j), c = (i, j+1), d = (i+1, j+1)
+        const ff ax = nU[ty][tx], bx = nU[ty][tx + 1], cx = nU[ty + 1][tx], dx = nU[ty + 1][tx + 1];
+        const ff ay = nV[ty][tx], by = nV[ty][tx + 1], cy = nV[ty + 1][tx], dy = nV[ty + 1][tx + 1];
+        const ff ux = ff_mul(hx, ff_add(ff_sub(bx, ax), ff_sub(dx, cx)));
+        const ff uy = ff_mul(hy, ff_add(ff_sub(cx, ax), ff_sub(dx, bx)));
+        const ff vx = ff_mul(hx, ff_add(ff_sub(by, ay), ff_sub(dy, cy)));
+        const ff vy = ff_mul(hy, ff_add(ff_sub(cy, ay), ff_sub(dy, by)));
+        const ff div = ff_add(ux, vy);
+        const size_t k = IDX(i, j);
+        S[F_P][k] = add_ff(S[F_P][k], ff_neg(ff_mul(ff{h.Kh, h.Kl}, div)));
+        S[F_Q][k] = add_ff(S[F_Q][k], ff_neg(ff_mul(ff{h.m3h, h.m3l}, div)));
+        S[F_S][k] = add_ff(S[F_S][k], ff_mul(ff{h.muh, h.mul}, ff_sub(ux, vy)));
+        S[F_TAU][k] = add_ff(S[F_TAU][k], ff_mul(ff{h.muh, h.mul}, ff_add(uy, vx)));
+    }
 }
 
 // set_boundaries (shear_sim.cc:552-581): ghost rows by linear extrapolation,
@@ -1178,7 +1197,7 @@ void projection_source(const step_consts &c, fields_dev &F, int cur, double dt, 
         split_host(0.5 / dt * c.xsp, &h.xfh, &h.xfl);
         split_host(0.5 / dt * c.ysp, &h.yfh, &h.yfl);
         const dim3 sb(SFX, SFY);
-        k_source_ff<<<g2(c.m, c.n + 1, sb), sb, 0, st>>>(c, F, cur, h, xbc_bv);
+        k_source_ff<<<g2(c.m, c.n + 1, dim3(SFX, SFY * SFR)), sb, 0, st>>>(c, F, cur, h, xbc_bv);
     } else {
         k_source<<<g2(c.m, c.n + 1, blk), blk, 0, st>>>(c, F, xbc_bv);
     }
@@ -1204,7 +1223,7 @@ void projection_apply(const step_consts &c, fields_dev &F, int cur, double dt, d
         split_host(c.mu * (1 / 3.0), &h.m3h, &h.m3l);
         split_host(c.mu, &h.muh, &h.mul);
         const dim3 sb(SFX, SFY);
-        k_project_ff<<<g2(c.m, c.n, sb), sb, 0, st>>>(c, F, cur, h);
+        k_project_ff<<<g2(c.m, c.n, dim3(SFX, SFY * SFR)), sb, 0, st>>>(c, F, cur, h);
     } else {
         k_project<<<g2(c.m, c.n, blk), blk, 0, st>>>(c, F, cur, hx, hy);
     }
