@@ -483,10 +483,13 @@ __device__ __noinline__ bool pick_y64(const double *__restrict__ f, int m, int i
 // The second differences are pairs; their magnitudes are compared in pairs
 // too, decided where they differ by more than the pairs' error bound (the
 // differences' ~2^-44 plus the split's ~2^-47 of the values, with room).
-// Where they are the same pair the choice does not change the value (a zero
-// or linear stretch of a field); any other near tie takes `exact`, the FP64
-// path's own choice.
+// Within the margin, candidates of the same sign (equal up to the margin)
+// give values within the float-float path's own error either way; a near tie
+// of opposite signs (the candidates differ by twice their size) takes the
+// inner candidate below kEnoTieRel of the field's scale and `exact`, the
+// FP64 path's own choice, above it.
 __device__ __forceinline__ ff ff_abs(ff a) { return a.hi < 0.f ? ff_neg(a) : a; }
+constexpr float kEnoTieRel = 1e-10f;
 template <typename Exact>
 __device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float vmag, Exact exact) {
     // second differences from the high parts: within |lo| parts and one
@@ -506,8 +509,18 @@ __device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float 
         const ff inner = from_left ? sbc : sab, outer = from_left ? sab : sbc;
         const ff g = ff_sub(ff_abs(inner), ff_abs(outer));
         const float gap = g.hi + g.lo;
-        if (fabsf(gap) > 1e-12f * big + 4e-13f * vmag) take_outer = gap > 0.f;
-        else if (inner.hi == outer.hi && inner.lo == outer.lo) take_outer = false;
+        const float margin = 1e-12f * big + 4e-13f * vmag, small = kEnoTieRel * (vmag + big);
+        if (fabsf(gap) > margin) take_outer = gap > 0.f;
+        // Within the margin the two candidates differ by at most |gap| plus
+        // its error where they have the same sign (or one is zero): either
+        // choice then moves the value by less than ~2e-12 (|value| +
+        // |differences|) times the upwind factor.  Of opposite signs they
+        // differ by twice their size: below kEnoTieRel (|value| +
+        // |differences|) that is grid-scale noise of the field at the level
+        // of the solver's tolerance, and the inner candidate is taken; above
+        // it the FP64 path's own choice.
+        else if (inner.hi * outer.hi >= 0.f || (fabsf(inner.hi) <= small && fabsf(outer.hi) <= small))
+            take_outer = false;
         else take_outer = exact();
     }
     // outer: from the left Db - Da, from the right Dc - Db
@@ -707,43 +720,45 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
     const ff qf{Sm.th[F_Q][ty + 2][tx + 2], Sm.tl[F_Q][ty + 2][tx + 2]};
     const ff sf{Sm.th[F_S][ty + 2][tx + 2], Sm.tl[F_S][ty + 2][tx + 2]};
     const ff tf{Sm.th[F_TAU][ty + 2][tx + 2], Sm.tl[F_TAU][ty + 2][tx + 2]};
-    double cchi = add_ff(A[F_CHI][ci], inc_of(F_CHI)), ddev = 0, dtmp = 0;
-    // Yield test: 3q^2 + s^2 + tau^2 in pairs (relative error ~2^-44); a cell
-    // clearly below the cut-offs of k_advect (1e-24, or an athermal law below
-    // yield) is elastic there too; any other cell takes k_advect's FP64 path.
-    const ff dsq = ff_add(ff_mul(ff{3.f, 0.f}, ff_mul(qf, qf)), ff_add(ff_mul(sf, sf), ff_mul(tf, tf)));
-    const float dv = dsq.hi + dsq.lo;
-    const bool athermal = c.stz_model >= 2;
-    const bool clearly_elastic = dv < 0.999e-24f * (1.f - 1e-6f) || (athermal && dv < c.yield_cut2f);
-    if (!clearly_elastic) {
-        const double q = A[F_Q][ci], s = A[F_S][ci],
-                     t = A[F_TAU][ci];
-        const double devsq = 3 * q * q + s * s + t * t;
-        const long long dbits = __double_as_longlong(devsq);
-        if (!(dbits < __double_as_longlong(0.999e-24) ||
-              (athermal && dbits < __double_as_longlong(c.yield_cut2)))) {
-            int iters;
-            const stz_law_params<double> lp = law_params(c);
-            dtmp = adaptive_plastic(lp, sqrt(devsq), cchi, ddev, dt, iters);
-            if (iters >= c.substep_cap) atomicExch(&F.flags[FL_SUBSTEP_CAP], 1);
-            if (iters > 1) atomicMax(&F.flags[FL_SUBSTEP_MAX], iters);
+    double ddev = 0, dtmp = 0;
+    // chi first (the plastic law takes the advected chi), then p, q, s, tau
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int f = k == 0 ? F_CHI : k - 1;
+        ff inc = inc_of(f);
+        if (f == F_S) inc = ff_add(inc, ff_mul(two_omega, tf));
+        else if (f == F_TAU) inc = ff_sub(inc, ff_mul(two_omega, sf));
+        const double a0 = A[f][ci];
+        double v = add_ff(a0, inc);
+        if (f == F_CHI) {
+            // Yield test: 3q^2 + s^2 + tau^2 in pairs (relative error ~2^-44);
+            // a cell clearly below the cut-offs of k_advect (1e-24, or an
+            // athermal law below yield) is elastic there too; any other cell
+            // takes k_advect's FP64 path.
+            const ff dsq = ff_add(ff_mul(ff{3.f, 0.f}, ff_mul(qf, qf)), ff_add(ff_mul(sf, sf), ff_mul(tf, tf)));
+            const float dv = dsq.hi + dsq.lo;
+            const bool athermal = c.stz_model >= 2;
+            const bool clearly_elastic = dv < 0.999e-24f * (1.f - 1e-6f) || (athermal && dv < c.yield_cut2f);
+            if (!clearly_elastic) {
+                const double q = A[F_Q][ci], s = A[F_S][ci], t = A[F_TAU][ci];
+                const double devsq = 3 * q * q + s * s + t * t;
+                const long long dbits = __double_as_longlong(devsq);
+                if (!(dbits < __double_as_longlong(0.999e-24) ||
+                      (athermal && dbits < __double_as_longlong(c.yield_cut2)))) {
+                    int iters;
+                    const stz_law_params<double> lp = law_params(c);
+                    dtmp = adaptive_plastic(lp, sqrt(devsq), v, ddev, dt, iters);
+                    if (iters >= c.substep_cap) atomicExch(&F.flags[FL_SUBSTEP_CAP], 1);
+                    if (iters > 1) atomicMax(&F.flags[FL_SUBSTEP_MAX], iters);
+                    if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
+                }
+            }
+            F.ddev[ci] = ddev;
+        } else if (f != F_P && dtmp != 0) {
+            v -= dtmp * a0;
         }
+        B[f][ci] = v;
     }
-    B[F_CHI][ci] = cchi;
-    F.ddev[ci] = ddev;
-    double qn = add_ff(A[F_Q][ci], inc_of(F_Q));
-    double sn = add_ff(A[F_S][ci], ff_add(inc_of(F_S), ff_mul(two_omega, tf)));
-    double tn = add_ff(A[F_TAU][ci], ff_sub(inc_of(F_TAU), ff_mul(two_omega, sf)));
-    if (dtmp != 0) {
-        if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
-        qn -= dtmp * A[F_Q][ci];
-        sn -= dtmp * A[F_S][ci];
-        tn -= dtmp * A[F_TAU][ci];
-    }
-    B[F_P][ci] = add_ff(A[F_P][ci], inc_of(F_P));
-    B[F_Q][ci] = qn;
-    B[F_S][ci] = sn;
-    B[F_TAU][ci] = tn;
 }
 
 // Explicit step (shear_sim::step_forward, shear_sim.cc:185-276) per cell

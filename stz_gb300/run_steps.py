@@ -24,13 +24,16 @@ def main(argv=None):
     ap.add_argument("--corr", type=float, default=16.0)
     ap.add_argument("--no-extrapolate", action="store_true")
     ap.add_argument("--direct", action="store_true", help="explicit steps (dt = dx^2/2) instead of quasi-static")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch every kernel from the host (a profiler then lists the solve's kernels too; "
+                         "the solve follows the host-side refinement policy)")
     a = ap.parse_args(argv)
     N = a.size
     P = simple_shear(N)
     chi = random_chi(N, N, a.corr, 600.0, a.std, P.TZ, 2)
     prec = _lib.MIXED if a.precision == "mixed" else _lib.FP64
     sim = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=a.tol,
-                   extrapolate=not a.no_extrapolate)
+                   extrapolate=not a.no_extrapolate, use_graphs=not a.no_graphs)
     if a.direct:
         ddt = 0.5 * (2.0 / N) ** 2
         sim.step_forward(ddt, a.warmup)
