@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--inner", type=int, default=0, help="FP32 V-cycles per refinement pass (0: library default)")
     ap.add_argument("--skip-extras", action="store_true", help="only the timed line (no FP64 leg, e2e, CPU)")
+    ap.add_argument("--skip-batch", action="store_true", help="no batched-configuration leg")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=100)
     return ap.parse_args()
 
 
@@ -244,6 +247,31 @@ def parity_vs_oracle(P, chi, nsteps, extrap, plastic=False):
         g.close()
     if plastic:
         out["eps_pl_max"] = float(ref["eps_pl"].max())
+    return out
+
+
+def batched_leg(args):
+    """The batched configuration: independent simple-shear simulations with
+    grids drawn from 64..512 squared (own chi fields and STZ constants),
+    advanced together in one CUDA graph after the per-size autotuner, in mixed
+    precision and in FP64.  value = the batch's cell-steps over the graph's
+    device time."""
+    from stz_gb300 import _lib
+    from stz_gb300.batch import Batch, batched_config
+    params, chis = batched_config(args.batch_count)
+    out = {"workload": f"{args.batch_count} simple-shear simulations, grids drawn from 64..512 squared, "
+                       f"{args.batch_steps} steps of dt {DT:g}, relative residual {RTOL:g}, one CUDA graph",
+           "cells": int(sum(p.m * p.n for p in params)), "unit": METRIC}
+    for name, prec in (("mixed", _lib.MIXED), ("fp64", _lib.FP64)):
+        b = Batch(params, chis, precision=prec, tol=RTOL)
+        t0 = time.time()
+        b.autotune(DT, 4)
+        tune_s = time.time() - t0
+        st = b.run(DT, args.batch_steps)
+        out[name] = {"value": st.cell_steps / st.seconds, "graph_seconds": st.seconds,
+                     "vcycles_per_instance_step": st.vcycles / (args.batch_count * args.batch_steps),
+                     "failed": int(st.failed), "autotune_s": tune_s}
+        b.close()
     return out
 
 
@@ -467,6 +495,8 @@ def run_ours(args, dist):
         h.close()
         return N * N * args.steps / dt_s * dist.ws
 
+    if prec == _lib.MIXED and not args.skip_batch:
+        line["batched"] = batched_leg(args)
     e2e_one = e2e_run(True)
     e2e_three = e2e_run(False)
     h2d = sum(t.numel() * 8 for t in up)

@@ -24,6 +24,9 @@ def main(argv=None):
     ap.add_argument("--corr", type=float, default=16.0)
     ap.add_argument("--no-extrapolate", action="store_true")
     ap.add_argument("--direct", action="store_true", help="explicit steps (dt = dx^2/2) instead of quasi-static")
+    ap.add_argument("--time-kernels", action="store_true",
+                    help="after the steps, time the kernel groups of stzg_time_kernel (advection, projection "
+                         "source, FP32 V-cycle, outer residual, stress correction) with CUDA events")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every kernel from the host (a profiler then lists the solve's kernels too; "
                          "the solve follows the host-side refinement policy)")
@@ -50,6 +53,15 @@ def main(argv=None):
     st = sim.stats
     print(f"N={N} {a.precision}: {1e3 * t / max(a.steps, 1):.2f} ms/step, {st.vcycles / max(a.steps, 1):.1f} "
           f"V-cycles/step, {st.refinements / max(a.steps, 1):.1f} passes/step, {st.kernel_launches} kernels")
+    if a.time_kernels:
+        ids = [(0, "advection"), (8, "projection source")]
+        if prec == _lib.MIXED:
+            ids += [(4, "FP32 V-cycle"), (5, "outer residual (float-float) + norms")]
+        else:
+            ids += [(3, "FP64 V-cycle")]
+        ids += [(9, "stress correction + wall rows (changes the stresses)")]
+        for k, name in ids:
+            print(f"  {name}: {sim.time_kernel(1e-2, k, 10):.4f} ms")
     sim.close()
 
 
