@@ -57,7 +57,7 @@ typedef struct {
     double tol;
     int track_plastic; /* accumulate eps_pl = sum ddev/(2 mu) per cell */
     int device;        /* CUDA device ordinal */
-    int inner_cycles;  /* mixed precision: FP32 V-cycles per refinement pass (0: auto) */
+    int inner_cycles;  /* mixed precision: FP32 V-cycles per refinement pass (0: auto, 3) */
     int use_graphs;    /* capture the V-cycle in a CUDA graph (1 default) */
     int extrapolate;   /* initial guess of each solve instead of the previous solution
                           v(n) (tgmg keeps z between solves): 1 = linear, 2v(n) - v(n-1);

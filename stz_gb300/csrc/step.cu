@@ -410,15 +410,12 @@ __global__ void __launch_bounds__(ATX * ATY) k_advect(step_consts c, advect_cons
 // TMA destination, needed only until it is split) overlaid by the first
 // differences, so that three blocks fit on an SM.
 struct adv_smem_ff {
-    float th[F_COUNT][AROWS][ACOLS];  // hi / lo parts of the staged values
-    float tl[F_COUNT][AROWS][ACOLS];
+    float2 t2[F_COUNT][AROWS][ACOLS];  // staged values as (hi, lo) pairs: one 64-bit access each
     union {
         double tile[F_COUNT][AROWS][ACOLS];  // staged fields (128-byte aligned: 24192 B precede it)
         struct {
-            float dxh[F_COUNT][ATY][ADXW];  // first differences in x: tile columns cc, cc+1
-            float dxl[F_COUNT][ATY][ADXW];
-            float dyh[F_COUNT][ADYH][ATX];  // first differences in y: tile rows r, r+1
-            float dyl[F_COUNT][ADYH][ATX];
+            float2 dx[F_COUNT][ATY][ADXW];  // first differences in x (pairs): tile columns cc, cc+1
+            float2 dy[F_COUNT][ADYH][ATX];  // first differences in y (pairs): tile rows r, r+1
         } d;
     } u;
     ff nu[ATY + 1][ATX + 1];  // node velocities (i0+c, j0+r) as pairs, walls substituted
@@ -499,8 +496,10 @@ __device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float 
     const float fin = from_left ? fbc : fab, fout = from_left ? fab : fbc;
     const float gap0 = fabsf(fin) - fabsf(fout);
     const float big = fabsf(Da.hi) + 2.f * fabsf(Db.hi) + fabsf(Dc.hi);
-    const float lows = fabsf(Da.lo) + 2.f * fabsf(Db.lo) + fabsf(Dc.lo);
-    const float m0 = lows + 2.4e-7f * (fabsf(fin) + fabsf(fout)) + 1e-12f * big + 4e-13f * vmag;
+    // bounds the low parts (<= 2^-24 big), one float rounding of each second
+    // difference (<= 2.4e-7 (|fin| + |fout|) <= 2.4e-7 big) and the pairs'
+    // own error (1e-12 big + 4e-13 vmag)
+    const float m0 = 3.1e-7f * big + 4e-13f * vmag;
     bool take_outer;
     if (fabsf(gap0) > m0) {
         take_outer = gap0 > 0.f;
@@ -530,10 +529,12 @@ __device__ __forceinline__ ff eno_ff(ff Da, ff Db, ff Dc, bool from_left, float 
 }
 
 __device__ __forceinline__ ff dx_pair(const adv_smem_ff &Sm, int f, int ty, int c) {
-    return ff{Sm.u.d.dxh[f][ty][c], Sm.u.d.dxl[f][ty][c]};
+    const float2 v = Sm.u.d.dx[f][ty][c];
+    return ff{v.x, v.y};
 }
 __device__ __forceinline__ ff dy_pair(const adv_smem_ff &Sm, int f, int r, int tx) {
-    return ff{Sm.u.d.dyh[f][r][tx], Sm.u.d.dyl[f][r][tx]};
+    const float2 v = Sm.u.d.dy[f][r][tx];
+    return ff{v.x, v.y};
 }
 
 // Where the FP64 choice is needed, the state buffer read (A), the point's
@@ -547,7 +548,7 @@ struct eno_ctx {
 __device__ __forceinline__ ff eno_x_ff(const adv_smem_ff &Sm, const eno_ctx &e, int f, int ty, int tx,
                                        bool from_left) {
     const int c = from_left ? tx : tx + 1;  // differences c .. c+2 (tile columns c .. c+3)
-    const float vmag = fabsf(Sm.th[f][ty + 2][tx + 2]);
+    const float vmag = fabsf(Sm.t2[f][ty + 2][tx + 2].x);
     return eno_ff(dx_pair(Sm, f, ty, c), dx_pair(Sm, f, ty, c + 1), dx_pair(Sm, f, ty, c + 2), from_left, vmag, [&] {
         return pick_x64(e.A[f], (size_t)(e.j + 1) * e.m, Sm.col, Sm.xs, f == F_X, e.lx, tx, from_left);
     });
@@ -559,7 +560,7 @@ __device__ __forceinline__ ff eno_y_ff(const adv_smem_ff &Sm, const eno_ctx &e, 
     const int r = from_below ? ty : ty + 1;  // differences r .. r+2
     const ff Db = dy_pair(Sm, f, r + 1, tx);
     if (!inner) return from_below ? ff_x2(Db) : ff_neg(ff_x2(Db));
-    const float vmag = fabsf(Sm.th[f][ty + 2][tx + 2]);
+    const float vmag = fabsf(Sm.t2[f][ty + 2][tx + 2].x);
     return eno_ff(dy_pair(Sm, f, r, tx), Db, dy_pair(Sm, f, r + 2, tx), from_below, vmag, [&] {
         return pick_y64(e.A[f], e.m, Sm.col[tx + 2], ty, from_below, e.j0, e.n);
     });
@@ -650,7 +651,11 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
     for (int p = tid; p < AROWS * ACOLS; p += ATX * ATY) {
         const int r = p / ACOLS, t = p - r * ACOLS;
 #pragma unroll
-        for (int f = 0; f < F_COUNT; f++) ff_split_d(Sm.u.tile[f][r][t], Sm.th[f][r][t], Sm.tl[f][r][t]);
+        for (int f = 0; f < F_COUNT; f++) {
+            float hh, ll;
+            ff_split_d(Sm.u.tile[f][r][t], hh, ll);
+            Sm.t2[f][r][t] = make_float2(hh, ll);
+        }
     }
     __syncthreads();
     // first differences: x on cell rows j0..j0+ATY-1, y on rows j0-2..j0+ATY+1;
@@ -664,12 +669,11 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
         for (int f = 0; f < F_COUNT; f++) {
             ff d{0.f, 0.f};
             if (live) {
-                d = ff_pair_diff(Sm.th[f][r + 2][cc + 1], Sm.tl[f][r + 2][cc + 1], Sm.th[f][r + 2][cc],
-                                 Sm.tl[f][r + 2][cc]);
+                const float2 a = Sm.t2[f][r + 2][cc + 1], b = Sm.t2[f][r + 2][cc];
+                d = ff_pair_diff(a.x, a.y, b.x, b.y);
                 if (f == F_X && sh != 0) d = ff_add(d, sh > 0 ? lx : ff_neg(lx));
             }
-            Sm.u.d.dxh[f][r][cc] = d.hi;
-            Sm.u.d.dxl[f][r][cc] = d.lo;
+            Sm.u.d.dx[f][r][cc] = make_float2(d.hi, d.lo);
         }
     }
     for (int p = tid; p < ADYH * ATX; p += ATX * ATY) {
@@ -679,11 +683,11 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
 #pragma unroll
         for (int f = 0; f < F_COUNT; f++) {
             ff d{0.f, 0.f};
-            if (live)
-                d = ff_pair_diff(Sm.th[f][r + 1][cc + 2], Sm.tl[f][r + 1][cc + 2], Sm.th[f][r][cc + 2],
-                                 Sm.tl[f][r][cc + 2]);
-            Sm.u.d.dyh[f][r][cc] = d.hi;
-            Sm.u.d.dyl[f][r][cc] = d.lo;
+            if (live) {
+                const float2 a = Sm.t2[f][r + 1][cc + 2], b = Sm.t2[f][r][cc + 2];
+                d = ff_pair_diff(a.x, a.y, b.x, b.y);
+            }
+            Sm.u.d.dy[f][r][cc] = make_float2(d.hi, d.lo);
         }
     }
     __syncthreads();
@@ -717,9 +721,8 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
     auto inc_of = [&](int f) {
         return upwind_inc(uh, eno_x_ff(Sm, e, f, ty, tx, ru), vh, eno_y_ff(Sm, e, f, ty, tx, rv, inner));
     };
-    const ff qf{Sm.th[F_Q][ty + 2][tx + 2], Sm.tl[F_Q][ty + 2][tx + 2]};
-    const ff sf{Sm.th[F_S][ty + 2][tx + 2], Sm.tl[F_S][ty + 2][tx + 2]};
-    const ff tf{Sm.th[F_TAU][ty + 2][tx + 2], Sm.tl[F_TAU][ty + 2][tx + 2]};
+    const float2 q2 = Sm.t2[F_Q][ty + 2][tx + 2], s2 = Sm.t2[F_S][ty + 2][tx + 2], t2 = Sm.t2[F_TAU][ty + 2][tx + 2];
+    const ff qf{q2.x, q2.y}, sf{s2.x, s2.y}, tf{t2.x, t2.y};
     double ddev = 0, dtmp = 0;
     // chi first (the plastic law takes the advected chi), then p, q, s, tau
 #pragma unroll
