@@ -59,6 +59,21 @@ int stzg_ct_get_time(stzg_ct *s, double *time);
  * seconds (optional) the device time. */
 int stzg_ct_step_qs(stzg_ct *s, double dt, int nsteps, long *vcycles, double *seconds);
 
+/* No counterpart in the reference, whose calibration harness (pfn.py through
+ * UQpy's RunModel) runs one simulation per parameter sample, one after the
+ * other.  Advances `count` independent handles (any sizes and parameters, all
+ * on one device) by nsteps quasi-static steps of dt each, driven from
+ * `threads` host threads (0: min(count, 16)); every handle keeps its own
+ * stream, so their kernels, host-side operator updates and solver checks
+ * overlap.  Each handle's result equals stzg_ct_step_qs on it alone.
+ * vcycles (optional, count entries) receives each handle's V-cycles;
+ * seconds (optional) the wall time of the whole batch.  On failure no further
+ * handle is started, the threads finish the handles they hold, and the
+ * status and message of the lowest-numbered failing handle are returned;
+ * its state is as stzg_ct_step_qs leaves it. */
+int stzg_ct_batch_step_qs(stzg_ct *const *handles, int count, double dt, int nsteps, int threads, long *vcycles,
+                          double *seconds);
+
 /* nsteps of shear_sim::step_forward(dt) (shear_sim.cc:218-349), the explicit
  * step: upwinded ENO2 advection of velocity, reference map, stresses and chi,
  * net force and viscous terms in sheared coordinates, the full elastic stress

@@ -15,11 +15,19 @@
 namespace stzg {
 
 static thread_local std::string g_msg;
-static std::atomic<long> g_launches(0);
+// Kernels launched by this thread (every count the library reports is a
+// difference taken within one call, so host threads driving separate handles
+// do not see each other's launches).
+struct launch_counter {
+    long n = 0;
+    void fetch_add(long k) { n += k; }
+    void fetch_sub(long k) { n -= k; }
+};
+static thread_local launch_counter g_launches;
 
-void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
-long launch_count() { return g_launches.load(std::memory_order_relaxed); }
-void discount_launches(long k) { g_launches.fetch_sub(k, std::memory_order_relaxed); }
+void note_launch() { g_launches.fetch_add(1); }
+long launch_count() { return g_launches.n; }
+void discount_launches(long k) { g_launches.fetch_sub(k); }
 
 int fail(int status, const std::string &msg) {
     g_msg = msg;

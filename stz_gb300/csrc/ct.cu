@@ -12,11 +12,15 @@
 // (lsn = n rows when y is periodic, n+1 with walls), its operator rebuilt
 // every step for the new shear lt = lamb*time as qs_multi::init does
 // (qs_multi.cc:31-46); source and velocities stay on the GPU.
+#include <algorithm>
+#include <atomic>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <cstdio>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -1287,6 +1291,41 @@ int stzg_ct_step_qs(stzg_ct *s, double dt, int nsteps, long *vcycles, double *se
     return STZG_OK;
 }
 
+int stzg_ct_batch_step_qs(stzg_ct *const *handles, int count, double dt, int nsteps, int threads, long *vcycles,
+                          double *seconds) {
+    if (!handles || count < 1 || !(dt > 0) || nsteps < 0 || threads < 0) return fail(STZG_EINVAL, "bad arguments");
+    for (int k = 0; k < count; k++)
+        if (!handles[k]) return fail(STZG_EINVAL, "null handle");
+    const int nt = threads > 0 ? std::min(threads, count) : std::min(count, 16);
+    std::atomic<int> next(0), first_bad(count);
+    std::vector<int> status(count, STZG_OK);
+    std::vector<std::string> msg(count);
+    const auto t0 = std::chrono::steady_clock::now();
+    auto work = [&]() {
+        for (;;) {
+            const int k = next.fetch_add(1);
+            if (k >= count || first_bad.load() < count) return;
+            long vc = 0;
+            const int st = stzg_ct_step_qs(handles[k], dt, nsteps, &vc, nullptr);
+            if (vcycles) vcycles[k] = vc;
+            if (st != STZG_OK) {
+                status[k] = st;
+                msg[k] = stzg_last_message();
+                int cur = first_bad.load();
+                while (k < cur && !first_bad.compare_exchange_weak(cur, k)) {
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; t++) pool.emplace_back(work);
+    work();
+    for (auto &th : pool) th.join();
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    const int bad = first_bad.load();
+    if (bad < count) return fail(status[bad], "handle " + std::to_string(bad) + ": " + msg[bad]);
+    return STZG_OK;
+}
 
 int stzg_ct_compute_strain(stzg_ct *s, double *out) {
     if (!s || !out) return fail(STZG_EINVAL, "null argument");

@@ -14,7 +14,7 @@ from . import _lib
 EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_chi_bicubic",
            "stzg_ct_compute_strain", "stzg_ct_output_field", "stzg_ct_write_frame", "stzg_ct_solve_quasistatic",
            "stzg_ct_solve", "stzg_ct_l2_comparison_transform", "stzg_ct_set_field", "stzg_ct_get_field",
-           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs", "stzg_ct_step_direct", "stzg_ct_tracers_init",
+           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_step_qs", "stzg_ct_batch_step_qs", "stzg_ct_step_direct", "stzg_ct_tracers_init",
            "stzg_ct_tracers_update", "stzg_ct_tracers_get"]
 FIELDS = ("u", "v", "p", "q", "s", "tau", "chi", "X", "Y", "ddev")
 BOLTZMANN = 1.3806503e-23
@@ -84,6 +84,7 @@ def load():
         "stzg_ct_set_time": (I, [V, D]),
         "stzg_ct_get_time": (I, [V, _P]),
         "stzg_ct_step_qs": (I, [V, D, I, ctypes.POINTER(ctypes.c_long), _P]),
+        "stzg_ct_batch_step_qs": (I, [ctypes.POINTER(V), I, D, I, I, ctypes.POINTER(ctypes.c_long), _P]),
         "stzg_ct_step_direct": (I, [V, D, I, _P]),
         "stzg_ct_tracers_init": (I, [V, I, I]),
         "stzg_ct_tracers_update": (I, [V, ctypes.POINTER(I)]),
@@ -216,3 +217,17 @@ class CtSim:
         if cnt.value:
             _lib.check(self.lib.stzg_ct_tracers_get(self.h, out.ctypes.data_as(_P), cnt.value, ctypes.byref(cnt)))
         return out
+
+
+def batch_step_qs(sims, dt, nsteps, threads=0):
+    """stzg_ct_batch_step_qs: advance independent CtSim handles together (one
+    host thread per handle up to `threads`, own streams).  Returns (vcycles per
+    handle, wall seconds)."""
+    lib = load()
+    hs = (ctypes.c_void_p * len(sims))(*[s.h.value for s in sims])
+    vc = (ctypes.c_long * len(sims))()
+    sec = ctypes.c_double()
+    _lib.check(lib.stzg_ct_batch_step_qs(hs, len(sims), float(dt), int(nsteps), int(threads), vc, ctypes.byref(sec)))
+    for s, v in zip(sims, vc):
+        s.vcycles = v
+    return list(vc), sec.value

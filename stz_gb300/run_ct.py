@@ -9,7 +9,10 @@ dt = tf/600.  Prints one JSON line.
 
 --direct DT times the explicit step (shear_sim::step_forward) of dt DT
 instead; --tracers MM NN adds an MM x NN tracer grid after the warm-up and
-times one update_tracers after the timed steps.
+times one update_tracers after the timed steps.  --batch K times K
+independent simulations of the given size (a UQ sweep: K parameter samples,
+here K chi levels) stepped one after the other and then together through
+stzg_ct_batch_step_qs, and prints both wall rates.
 """
 import argparse
 import json
@@ -27,10 +30,14 @@ def main(argv=None):
     ap.add_argument("--walls", action="store_true")
     ap.add_argument("--direct", type=float, default=None)
     ap.add_argument("--tracers", type=int, nargs=2, default=None)
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=0)
     args = ap.parse_args(argv)
     yp = not args.walls
     P = transform_shear(args.m, args.n, y_prd=yp)
     dt = (0.5 / 1e-3 if yp else 3e6 / 2e4) / 600
+    if args.batch:
+        return batch_main(args, P, dt, yp)
     sim = CtSim(P)
     sim.init_fields(0, 580.0, 220.0)
     kind = "quasi-static"
@@ -56,6 +63,40 @@ def main(argv=None):
                            "update_ms_wall": 1e3 * (time.perf_counter() - t0)}
     print(json.dumps(line))
     sim.close()
+    return line
+
+
+def batch_main(args, P, dt, yp):
+    from .ct_sim import batch_step_qs
+
+    def make():
+        sims = []
+        for k in range(args.batch):
+            sim = CtSim(P)
+            sim.init_fields(0, 560.0 + 40.0 * k / max(args.batch - 1, 1), 220.0)
+            sims.append(sim)
+        return sims
+
+    sims = make()
+    for s in sims:
+        s.step_forward_quasistatic(dt, args.warmup)
+    t0 = time.perf_counter()
+    for s in sims:
+        s.step_forward_quasistatic(dt, args.steps)
+    seq = time.perf_counter() - t0
+    for s in sims:
+        s.close()
+    sims = make()
+    batch_step_qs(sims, dt, args.warmup, args.threads)
+    _, wall = batch_step_qs(sims, dt, args.steps, args.threads)
+    cells = args.m * args.n * args.steps * args.batch
+    line = {"workload": "%d coord_transforms simple-shear simulations %dx%d, %s, quasi-static, %d steps of dt %.6g"
+                        % (args.batch, args.m, args.n, "y periodic, lamb 1e-3" if yp else "walls", args.steps, dt),
+            "metric": "cell-steps/s (wall)", "batched": cells / wall, "one_after_another": cells / seq,
+            "speedup": seq / wall, "threads": args.threads or min(args.batch, 16)}
+    for s in sims:
+        s.close()
+    print(json.dumps(line))
     return line
 
 

@@ -256,3 +256,37 @@ def test_ct_l2_comparison_transform_matches_reference(name):
     np.testing.assert_allclose(t.l2_comparison_transform(p), want, rtol=1e-12, atol=1e-300)
     t.close()
     p.close()
+
+
+def test_ct_batch_matches_single_handles():
+    """stzg_ct_batch_step_qs over handles of different sizes, boundary
+    conditions and strain rates, from several host threads: every handle ends
+    bit for bit where stzg_ct_step_qs alone takes it, with the same V-cycle
+    counts."""
+    from stz_gb300.ct_sim import CtSim, batch_step_qs, transform_shear
+    cases = [(32, 16, True, 1e-3), (48, 32, False, 0.0), (64, 32, True, 2e-3), (40, 24, False, 0.0),
+             (64, 64, True, 5e-4), (96, 48, False, 0.0)]
+
+    def make():
+        out = []
+        for k, (m, n, yp, lamb) in enumerate(cases):
+            sim = CtSim(transform_shear(m, n, y_prd=yp, lamb=lamb if yp else None))
+            sim.init_fields(k % 3, 600.0 + 10 * k, 200.0)
+            out.append(sim)
+        return out
+
+    dt, steps = 2e-3, 5
+    solo = make()
+    for s in solo:
+        s.step_forward_quasistatic(dt, steps)
+    batch = make()
+    vc, sec = batch_step_qs(batch, dt, steps, threads=4)
+    assert sec > 0
+    for a, b, v in zip(solo, batch, vc):
+        assert v == a.vcycles
+        fa, fb = a.fields(), b.fields()
+        for k in fa:
+            assert np.array_equal(fa[k], fb[k]), k
+        assert a.time == b.time
+    for s in solo + batch:
+        s.close()
