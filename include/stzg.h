@@ -67,8 +67,10 @@ typedef struct {
     int advection;     /* Mixed-precision handles: STZG_ADV_AUTO (0) or STZG_ADV_SPLIT run the
                           advection, the projection source and the stress correction in
                           float-float arithmetic (pairs of floats, ~2^-44 relative) on the
-                          FP64 state, each field updated by FP64 additions, with the ENO
-                          choices of the FP64 path; STZG_ADV_FP64 keeps them FP64.  FP64
+                          FP64 state, each field updated by one FP64 addition, with the ENO
+                          choices of the FP64 path wherever the two candidates differ by
+                          more than 1e-10 of the field's scale; STZG_ADV_FP64 keeps them
+                          FP64.  FP64
                           handles always run them in FP64, bit-exact with the per-point
                           ENO2. */
     int reserved[5];
