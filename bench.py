@@ -428,8 +428,8 @@ def run_ours(args, dist):
                         "ms_per_launch": t, "algorithmic_bytes": b,
                         "share_of_step": shares[dom] / (1e3 * dev_s / args.steps)}
     if dom == "advect" and prec == _lib.MIXED:
-        line["roofline"]["note"] = ("issue-bound float-float ENO arithmetic (issue slots 73% active, FP64 pipe "
-                                    "33%, DRAM 12% under ncu); its DRAM traffic equals the algorithmic bytes")
+        line["roofline"]["note"] = ("issue-bound float-float ENO arithmetic (issue slots 66% active, FP64 pipe "
+                                    "25%, DRAM 13% under ncu); its DRAM traffic equals the algorithmic bytes")
     elif dom == "advect":
         line["roofline"]["note"] = "FP64-pipe-bound (FP64 pipe 83% active under ncu); HBM is not the limit"
 
@@ -495,16 +495,50 @@ def run_ours(args, dist):
         h.close()
         return N * N * args.steps / dt_s * dist.ws
 
+    def e2e_c_field_run():
+        # the reference's own layout: one array of c_field records (19 doubles
+        # per point, rows -1..n) in ordinary host memory, converted to and from
+        # the pinned upload buffers on the host cores every step
+        from stz_gb300.shear_sim import C_FIELD_DOUBLES, c_field_pack, c_field_unpack
+        up_np = [t.numpy() for t in up]
+        down_np = [t.numpy() for t in down]
+        rec = np.zeros(((N + 2) * N, C_FIELD_DOUBLES))
+        h = ShearSim(P, chi, precision=prec, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, extrapolate=extrap,
+                     inner_cycles=args.inner)
+        h.steps(DT, args.warmup)
+        h.download(down_p)
+        c_field_unpack(down_np, N, N, rec)
+        t_pack = t_unpack = 0.0
+        t0 = time.time()
+        for _ in range(args.steps):
+            a = time.time()
+            c_field_pack(rec, N, N, up_np)
+            b = time.time()
+            h.step_host(DT, up_p, down_p)
+            c = time.time()
+            c_field_unpack(down_np, N, N, rec)
+            t_pack += b - a
+            t_unpack += time.time() - c
+        dt_s = time.time() - t0
+        h.close()
+        return {"value": N * N * args.steps / dt_s * dist.ws, "unit": METRIC,
+                "pack_ms_per_step": 1e3 * t_pack / args.steps, "unpack_ms_per_step": 1e3 * t_unpack / args.steps,
+                "host_threads": os.cpu_count(),
+                "api": "stzg_c_field_pack + stzg_step_qs_host + stzg_c_field_unpack on the reference's "
+                       "c_field array (152 B per point, pageable host memory)"}
+
     if prec == _lib.MIXED and not args.skip_batch:
         line["batched"] = batched_leg(args)
     e2e_one = e2e_run(True)
     e2e_three = e2e_run(False)
+    e2e_aos = e2e_c_field_run()
     h2d = sum(t.numel() * 8 for t in up)
     d2h = sum(t.numel() * 8 for t in down)
     line["e2e"] = {"value": e2e_one, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                    "steps": args.steps, "warmup": args.warmup,
                    "api": "stzg_step_qs_host (upload, step, download in one call; pinned host buffers)",
-                   "three_calls": {"value": e2e_three, "api": "stzg_upload + stzg_step_qs + stzg_download"}}
+                   "three_calls": {"value": e2e_three, "api": "stzg_upload + stzg_step_qs + stzg_download"},
+                   "c_field_layout": e2e_aos}
 
     if not args.skip_cpu:
         line["cpu_baseline"] = cpu_baseline(P, chi, args.cpu_steps)

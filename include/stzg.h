@@ -149,6 +149,17 @@ int stzg_download(stzg_sim *s, double *const *down);
  * projection leaves alone (chi rows, interior rows of X and Y, eps_pl) are
  * copied back while the multigrid solve runs. */
 int stzg_step_qs_host(stzg_sim *s, double dt, const double *const *up, double *const *down, stzg_stats *stats);
+/* No counterpart in the reference, which holds its state only as an array of
+ * c_field records (fields.hh:7-114: 19 doubles, u, v, p, q, s, tau, chi, X,
+ * Y, ddev first; shear_sim::fm - m, rows -1..n of m records, node values on
+ * rows 0..n).  Host-side conversions (multithreaded) between that array
+ * (fm_rows, m*(n+2) records) and the first 8 buffers of stzg_upload's `up` /
+ * stzg_download's `down` layout: p, q, s, tau, chi (all rows), X, Y, vel
+ * (x, y pairs from u, v).  NULL entries are skipped; the other record members
+ * are left as they are.  A caller that keeps the reference's layout calls
+ * pack, stzg_step_qs_host, unpack. */
+int stzg_c_field_pack(const void *fm_rows, int m, int n, double *const *soa);
+int stzg_c_field_unpack(const double *const *soa, int m, int n, void *fm_rows);
 
 /* Replaces: shear_sim::step_forward_quasistatic (shear_sim.cc:280-291),
  * called nsteps times; stats may be NULL. */

@@ -33,6 +33,7 @@ EXPORTS = [
     "stzg_mg_solve", "stzg_mg_vcycle", "stzg_mg_l2_error", "stzg_mg_levels", "stzg_mg_stencil",
     "stzg_l2_comparison", "stzg_random_chi", "stzg_upload", "stzg_download", "stzg_time_kernel",
     "stzg_set_mg_persistent", "stzg_get_mg_persistent", "stzg_residual_norms_noalloc",
+    "stzg_c_field_pack", "stzg_c_field_unpack",
     "stzg_batch_create", "stzg_batch_destroy", "stzg_batch_size", "stzg_batch_sim", "stzg_batch_set_tuning",
     "stzg_batch_autotune", "stzg_batch_get_tuning", "stzg_batch_run",
     "stzg_adjoint_forward", "stzg_adjoint_backward",
@@ -118,6 +119,8 @@ def load(path=None):
         "stzg_download": (I, [V, ctypes.POINTER(ctypes.c_void_p)]),
         "stzg_time_kernel": (I, [V, D, I, I, _P]),
         "stzg_set_mg_persistent": (I, [V, I]),
+        "stzg_c_field_pack": (I, [V, I, I, ctypes.POINTER(_P)]),
+        "stzg_c_field_unpack": (I, [ctypes.POINTER(_P), I, I, V]),
         "stzg_get_mg_persistent": (I, [V, ctypes.POINTER(I)]),
         "stzg_residual_norms_noalloc": (I, [ctypes.POINTER(StzParams), D, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_void_p]),

@@ -2351,6 +2351,10 @@ template <typename T> static bool march_level(const hierarchy<T> &h, const level
            L.nst <= kMarchStencils;
 }
 
+#ifndef STZG_TAIL_MARCH_MAX
+#define STZG_TAIL_MARCH_MAX 0  // widest streaming level the tail may take instead
+#endif
+
 // First level handled by the single-block tail (levels of at most
 // tail_points points, plus a direct coarsest solve); ml+1 when there is none.
 template <typename T> static int tail_start(const hierarchy<T> &h) {
@@ -2360,7 +2364,7 @@ template <typename T> static int tail_start(const hierarchy<T> &h) {
     int t = ml;
     // a level the streaming kernels take stays out of the tail (they are faster)
     while (t > 1 && (long)h.lv[t - 1].m * h.lv[t - 1].n <= limit && tail_smem_bytes(h, t - 1) <= kTailSmem &&
-           !march_level(h, h.lv[t - 1]))
+           (!march_level(h, h.lv[t - 1]) || h.lv[t - 1].m <= STZG_TAIL_MARCH_MAX))
         t--;
     if (tail_smem_bytes(h, t) > kTailSmem) return ml + 1;
     return t;

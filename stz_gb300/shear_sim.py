@@ -31,6 +31,25 @@ def random_chi(m, n, l, tem_avg, tem_std, TZ, seed):
     return out.reshape(n, m)
 
 
+C_FIELD_DOUBLES = 19  # fields.hh:7-114: u, v, p, q, s, tau, chi, X, Y, ddev, then the update scratch
+
+
+def c_field_pack(fm_rows, m, n, soa):
+    """stzg_c_field_pack: the reference's c_field array (m*(n+2) records of 19
+    doubles, rows -1..n) into the up/down buffers p, q, s, tau, chi, X, Y, vel
+    (None entries skipped)."""
+    rec = np.ascontiguousarray(fm_rows, dtype=np.float64)
+    arr = (ctypes.POINTER(ctypes.c_double) * 8)(*[None if a is None else _ptr(a) for a in soa[:8]])
+    _lib.check(_lib.load().stzg_c_field_pack(rec.ctypes.data_as(ctypes.c_void_p), m, n, arr))
+
+
+def c_field_unpack(soa, m, n, fm_rows):
+    """stzg_c_field_unpack: the buffers back into the c_field array in place."""
+    assert fm_rows.dtype == np.float64 and fm_rows.flags["C_CONTIGUOUS"]
+    arr = (ctypes.POINTER(ctypes.c_double) * 8)(*[None if a is None else _ptr(a) for a in soa[:8]])
+    _lib.check(_lib.load().stzg_c_field_unpack(arr, m, n, fm_rows.ctypes.data_as(ctypes.c_void_p)))
+
+
 class ShearSim:
     """One quasi-static STZ simulation on one GPU."""
 

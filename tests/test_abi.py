@@ -123,3 +123,31 @@ def _has_gpu():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+def test_c_field_pack_unpack_round_trip(lib):
+    """The reference's c_field array (19 doubles per point, rows -1..n) to the
+    upload buffers and back: cell fields from every row, node fields (X, Y and
+    u, v into vel pairs) from rows 0..n, other members untouched."""
+    from stz_gb300.shear_sim import C_FIELD_DOUBLES, c_field_pack, c_field_unpack
+    m, n = 7, 5
+    rng = np.random.default_rng(3)
+    rec = rng.standard_normal((n + 2) * m * C_FIELD_DOUBLES).reshape((n + 2) * m, C_FIELD_DOUBLES)
+    cells = [np.zeros((n + 2) * m) for _ in range(5)]
+    nodes = [np.zeros((n + 1) * m) for _ in range(2)]
+    vel = np.zeros(2 * (n + 1) * m)
+    soa = cells + nodes + [vel]
+    c_field_pack(rec, m, n, soa)
+    for q, col in enumerate((2, 3, 4, 5, 6)):
+        assert np.array_equal(cells[q], rec[:, col])
+    assert np.array_equal(nodes[0], rec[m:, 7]) and np.array_equal(nodes[1], rec[m:, 8])
+    assert np.array_equal(vel[0::2], rec[m:, 0]) and np.array_equal(vel[1::2], rec[m:, 1])
+    back = rng.standard_normal(rec.shape)
+    keep = back.copy()
+    c_field_unpack(soa, m, n, back)
+    for col in (2, 3, 4, 5, 6):
+        assert np.array_equal(back[:, col], rec[:, col])
+    for col in (0, 1, 7, 8):
+        assert np.array_equal(back[m:, col], rec[m:, col])
+        assert np.array_equal(back[:m, col], keep[:m, col])  # row -1 has no node values
+    assert np.array_equal(back[:, 9:], keep[:, 9:])
