@@ -365,7 +365,8 @@ def run_ours(args, dist):
     if prec == _lib.MIXED:
         nsteps = args.fp64_steps or min(args.warmup + args.steps, 60)
         a = ShearSim(P, chi, precision=_lib.FP64, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, extrapolate=extrap)
-        b = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, extrapolate=extrap)
+        b = ShearSim(P, chi, precision=_lib.MIXED, tol_mode=_lib.TOL_RELATIVE, tol=RTOL, extrapolate=extrap,
+                     inner_cycles=args.inner)
         a.steps(DT, nsteps)
         b.steps(DT, nsteps)
         from parity import group_errors
