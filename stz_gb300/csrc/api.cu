@@ -620,6 +620,9 @@ int stzg_create(const stz_params *p, const stzg_options *opt, stzg_sim **out) {
     if ((st = dev_alloc(s, (void **)&s->F.flags, FL_COUNT * sizeof(int))) != STZG_OK) return bail(st);
     for (int k = 0; k < 4; k++)
         if ((st = dev_alloc(s, (void **)&s->F.pre[k], nc * sizeof(double))) != STZG_OK) return bail(st);
+    // cells the float-float advection hands to the FP64 plastic pass (at most all of them)
+    if ((st = dev_alloc(s, (void **)&s->F.plist, (size_t)s->m * s->n * sizeof(unsigned))) != STZG_OK) return bail(st);
+    if ((st = dev_alloc(s, (void **)&s->F.pcount, sizeof(unsigned))) != STZG_OK) return bail(st);
     s->maps = new field_maps;
     if ((st = make_field_maps(s->sc, s->F, s->maps)) != STZG_OK) return bail(st);
     if (o.extrapolate)

@@ -723,8 +723,8 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
     };
     const float2 q2 = Sm.t2[F_Q][ty + 2][tx + 2], s2 = Sm.t2[F_S][ty + 2][tx + 2], t2 = Sm.t2[F_TAU][ty + 2][tx + 2];
     const ff qf{q2.x, q2.y}, sf{s2.x, s2.y}, tf{t2.x, t2.y};
-    double ddev = 0, dtmp = 0;
-    // chi first (the plastic law takes the advected chi), then p, q, s, tau
+    const double ddev = 0;
+    // chi first, then p, q, s, tau
 #pragma unroll
     for (int k = 0; k < 5; k++) {
         const int f = k == 0 ? F_CHI : k - 1;
@@ -742,25 +742,52 @@ __global__ void __launch_bounds__(ATX * ATY, 3)
             const float dv = dsq.hi + dsq.lo;
             const bool athermal = c.stz_model >= 2;
             const bool clearly_elastic = dv < 0.999e-24f * (1.f - 1e-6f) || (athermal && dv < c.yield_cut2f);
-            if (!clearly_elastic) {
-                const double q = A[F_Q][ci], s = A[F_S][ci], t = A[F_TAU][ci];
-                const double devsq = 3 * q * q + s * s + t * t;
-                const long long dbits = __double_as_longlong(devsq);
-                if (!(dbits < __double_as_longlong(0.999e-24) ||
-                      (athermal && dbits < __double_as_longlong(c.yield_cut2)))) {
-                    int iters;
-                    const stz_law_params<double> lp = law_params(c);
-                    dtmp = adaptive_plastic(lp, sqrt(devsq), v, ddev, dt, iters);
-                    if (iters >= c.substep_cap) atomicExch(&F.flags[FL_SUBSTEP_CAP], 1);
-                    if (iters > 1) atomicMax(&F.flags[FL_SUBSTEP_MAX], iters);
-                    if (c.track_plastic && ddev != 0) F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
-                }
-            }
+            // the FP64 test and the plastic law run in k_plastic_ff, on the
+            // listed cells after this kernel (kept out of this one, whose
+            // registers they would otherwise set)
+            if (!clearly_elastic) F.plist[atomicAdd(F.pcount, 1u)] = (unsigned)ci;
             F.ddev[ci] = ddev;
-        } else if (f != F_P && dtmp != 0) {
-            v -= dtmp * a0;
         }
         B[f][ci] = v;
+    }
+}
+
+// The plastic part of the float-float step for the cells k_advect_ff listed:
+// k_advect's FP64 yield test and, above the cut-offs, the FP64 plastic law
+// (adaptive_plastic_term, shear_sim.cc:513-548) on the advected chi, then
+// q, s, tau -= dtmp times their old values, ddev and the plastic strain.  The
+// same operations in the same order as k_advect, so the cell ends where the
+// one-pass form would take it.
+__global__ void k_plastic_ff(step_consts c, fields_dev F, int cur, double dt) {
+    if (c.clock) cur = (int)c.clock[CLK_CUR];
+    const unsigned cnt = *F.pcount;
+    const double *__restrict__ const *A = F.f[cur];
+    double *const *B = F.f[cur ^ 1];
+    const bool athermal = c.stz_model >= 2;
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+        const size_t ci = F.plist[k];
+        const double q = A[F_Q][ci], s = A[F_S][ci], t = A[F_TAU][ci];
+        const double devsq = 3 * q * q + s * s + t * t;
+        const long long dbits = __double_as_longlong(devsq);
+        if (dbits < __double_as_longlong(0.999e-24) || (athermal && dbits < __double_as_longlong(c.yield_cut2)))
+            continue;
+        int iters;
+        double chi = B[F_CHI][ci], ddev = 0;
+        const stz_law_params<double> lp = law_params(c);
+        const double dtmp = adaptive_plastic(lp, sqrt(devsq), chi, ddev, dt, iters);
+        if (iters >= c.substep_cap) atomicExch(&F.flags[FL_SUBSTEP_CAP], 1);
+        if (iters > 1) atomicMax(&F.flags[FL_SUBSTEP_MAX], iters);
+        B[F_CHI][ci] = chi;
+        F.ddev[ci] = ddev;
+        if (c.track_plastic && ddev != 0) {
+            const int m = c.m, j = (int)(ci / (size_t)m) - 1, i = (int)(ci - (size_t)(j + 1) * m);
+            F.eps_pl[(size_t)j * m + i] += ddev / (2 * c.mu);
+        }
+        if (dtmp != 0) {
+            B[F_Q][ci] -= dtmp * q;
+            B[F_S][ci] -= dtmp * s;
+            B[F_TAU][ci] -= dtmp * t;
+        }
     }
 }
 
@@ -1175,7 +1202,10 @@ void advection(const step_consts &c, const field_maps &maps, fields_dev &F, int 
         split_host(a.hx, &h.hxh, &h.hxl);
         split_host(a.hy, &h.hyh, &h.hyl);
         split_host(c.lx, &h.lxh, &h.lxl);
+        cudaMemsetAsync(F.pcount, 0, sizeof(unsigned), st);
         k_advect_ff<<<grid, dim3(ATX, ATY), sizeof(adv_smem_ff) + 128, st>>>(c, h, maps, F, cur, dt, bv);
+        note_launch();
+        k_plastic_ff<<<2 * 152, 256, 0, st>>>(c, F, cur, dt);
     } else {
         k_advect<<<grid, dim3(ATX, ATY), sizeof(adv_smem) + 128, st>>>(c, a, maps, F, cur, dt, bv, 1);
     }

@@ -41,6 +41,10 @@ struct fields_dev {
     // U = xf A + yf tau, W = xf A - yf tau, Y1 = xf tau - yf B,
     // Y2 = xf tau + yf B, A = p+q-s, B = p+q+s (xf, yf of projection_step).
     double *pre[4];
+    // Float-float advection: cells that the pair yield test cannot certify as
+    // elastic (their index, then their count), for the FP64 plastic pass.
+    unsigned *plist;
+    unsigned *pcount;
 };
 
 struct step_consts {
