@@ -43,7 +43,7 @@ VCYCLE64_BYTES_PER_NODE = 138.7
 SWEEP32_BYTES_PER_NODE = 24      # one Gauss-Seidel sweep: read z, b; write z (float2)
 # DRAM bytes (read + write) of one launch at 2048x2048 from the committed ncu
 # captures (cold caches); the advection kernel per precision
-NCU_TRAFFIC_2048 = {"advect_mixed": 539.3e6, "advect_fp64": 659.8e6, "residual_ff": 153.0e6,
+NCU_TRAFFIC_2048 = {"advect_mixed": 535.9e6, "advect_fp64": 659.8e6, "residual_ff": 153.0e6,
                     "source_mixed": 174.9e6}
 SOURCE_BYTES_PER_NODE = 48       # read p,q,s,tau of the cells (8 B each, once per cell); write the source (16 B)
 DIRECT_BYTES_PER_CELL = 160      # explicit step: read u,v,p,q,s,tau,chi,X,Y; write them, ddev (8 B each)
@@ -429,8 +429,8 @@ def run_ours(args, dist):
                         "ms_per_launch": t, "algorithmic_bytes": b,
                         "share_of_step": shares[dom] / (1e3 * dev_s / args.steps)}
     if dom == "advect" and prec == _lib.MIXED:
-        line["roofline"]["note"] = ("issue-bound float-float ENO arithmetic (issue slots 66% active, FP64 pipe "
-                                    "25%, DRAM 13% under ncu); its DRAM traffic equals the algorithmic bytes")
+        line["roofline"]["note"] = ("issue-bound float-float ENO arithmetic (issue slots 67% active, FP64 pipe "
+                                    "11%, DRAM 14% under ncu); its DRAM traffic equals the algorithmic bytes")
     elif dom == "advect":
         line["roofline"]["note"] = "FP64-pipe-bound (FP64 pipe 83% active under ncu); HBM is not the limit"
 
