@@ -354,6 +354,7 @@ def run_ours(args, dist):
             "config": bench_config(args, extrap, dist.ws),
             "clocks": clk, "gpu_launches": int(st.kernel_launches),
             "vcycles_per_step": st.vcycles / args.steps, "refinements_per_step": st.refinements / args.steps,
+            "extra_vcycles_per_step": st.extra_vcycles / args.steps,
             "wall_ms_per_step": 1e3 * wall / args.steps}
     if dist.rank != 0:
         return None
@@ -380,7 +381,8 @@ def run_ours(args, dist):
         a2.steps(DT, k64)
         fp64_value = N * N * k64 / a2.stats.seconds
         line["fp64"] = {"value": fp64_value, "ms_per_step": 1e3 * a2.stats.seconds / k64,
-                        "vcycles_per_step": a2.stats.vcycles / k64, "steps": k64}
+                        "vcycles_per_step": a2.stats.vcycles / k64,
+                        "extra_vcycles_per_step": a2.stats.extra_vcycles / k64, "steps": k64}
         line["speedup_mixed_vs_fp64"] = value / dist.ws / fp64_value
         line["rel_err_mixed_vs_fp64"] = {"steps": nsteps, **{k: float(v) for k, v in err.items()}}
         for h in (a, b, a2):
