@@ -382,12 +382,11 @@ static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
     }
     cudaGraphNodeParams ip = {};  // mixed: IF a pass ran { merge }
     if (mixed_extra > 0) {
-        // after convergence: the extra FP32 V-cycles on the last residual, the
-        // correction, then the merge
+        // after convergence: the extra FP32 V-cycles on the last residual, then
+        // the correction and the merge in one pass
         const long count = (long)s->m * (s->n + 1);
         for (int c = 0; c < mixed_extra; c++) vcycle<float>(s->h32, s->st, 10, 1, c == 0);
-        ff_correct(s->zhi, s->zlo, s->h32.lv[0].z, count, s->st);
-        mixed_end(s);
+        ff_correct_merge(s->zhi, s->zlo, s->h32.lv[0].z, s->F.vel, count, s->st);
     } else if (mixed) {
         cudaStreamCaptureStatus cs;
         cudaGraph_t cg;

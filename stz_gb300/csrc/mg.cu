@@ -773,6 +773,17 @@ __global__ void k_ff_correct(float2 *__restrict__ hi, float2 *__restrict__ lo, c
     }
 }
 
+// The last correction and the merge in one pass: a = (hi, lo) + e as a
+// double, without writing the pairs back (the solve ends here).
+__global__ void k_ff_correct_merge(const float2 *__restrict__ hi, const float2 *__restrict__ lo,
+                                   const float2 *__restrict__ e, double2 *__restrict__ a, long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        const float2 h = hi[k], l = lo[k], d = e[k];
+        const ff x = ff_add_f(ff{h.x, l.x}, d.x), y = ff_add_f(ff{h.y, l.y}, d.y);
+        a[k] = make_double2(ff_to_d(x.hi, x.lo), ff_to_d(y.hi, y.lo));
+    }
+}
+
 // Constants of the top-level operator as float-float pairs.
 struct ff_op {
     ff Kmx, Kmy, mx, my, qK, bcxx, bcyy;
@@ -2727,6 +2738,10 @@ void ff_merge(const float2 *hi, const float2 *lo, double2 *a, long count, cudaSt
 
 void ff_correct(float2 *hi, float2 *lo, const float2 *e32, long count, cudaStream_t st) {
     k_ff_correct<<<4 * 152, 256, 0, st>>>(hi, lo, e32, count); note_launch();
+}
+
+void ff_correct_merge(const float2 *hi, const float2 *lo, const float2 *e32, double2 *a, long count, cudaStream_t st) {
+    k_ff_correct_merge<<<4 * 152, 256, 0, st>>>(hi, lo, e32, a, count); note_launch();
 }
 
 void ff_residual(const top_op<double> &o, const float2 *zhi, const float2 *zlo, const float2 *bhi, const float2 *blo,
