@@ -80,8 +80,8 @@ int validate(const stz_params *p) {
 }
 
 void drop_graphs(stzg_sim *s) {
-    cudaGraphExec_t *g[4] = {&s->g_vc64, &s->g_res32, &s->g_pass32, &s->g_loop};
-    for (int k = 0; k < 4; k++)
+    cudaGraphExec_t *g[5] = {&s->g_vc64, &s->g_res32, &s->g_pass32, &s->g_loop, &s->g_loop_x};
+    for (int k = 0; k < 5; k++)
         if (*g[k]) {
             cudaGraphExecDestroy(*g[k]);
             *g[k] = nullptr;
@@ -321,11 +321,13 @@ static int abandon_capture(stzg_sim *s, int status) {
     return status;
 }
 
-static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
-    if (s->g_loop && s->g_loop_inner == inner) return STZG_OK;
-    if (s->g_loop) {
-        cudaGraphExecDestroy(s->g_loop);
-        s->g_loop = nullptr;
+static int build_loop_graph(stzg_sim *s, bool mixed, int inner, bool fused_extrap) {
+    cudaGraphExec_t &slot = fused_extrap ? s->g_loop_x : s->g_loop;
+    int &slot_inner = fused_extrap ? s->g_loop_x_inner : s->g_loop_inner;
+    if (slot && slot_inner == inner) return STZG_OK;
+    if (slot) {
+        cudaGraphExecDestroy(slot);
+        slot = nullptr;
     }
     const long count = (long)s->m * (s->n + 1);
     const double tol2 = s->O.tol * s->O.tol;
@@ -354,7 +356,10 @@ static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
         return cuda_fail(e, "cudaStreamBeginCaptureToGraph");
     }
     // set-up: initial residual of the warm start, then the loop and the finish
-    if (mixed) mixed_begin(s);
+    if (mixed && fused_extrap)
+        extrap_split(s->F.vel, s->vel_prev, s->F.src, s->zhi, s->zlo, s->bhi, s->blo, count, s->st);
+    else if (mixed)
+        mixed_begin(s);
     launch_norms(s, mixed);
     k_loop_start<<<1, 32, 0, s->st>>>(s->dnorm, s->F.flags, tol2, h, h_ran, mixed && mixed_extra == 0 ? 1 : 0);
     note_launch();
@@ -458,26 +463,24 @@ static int build_loop_graph(stzg_sim *s, bool mixed, int inner) {
     s->n_loop_merge = c1 - cm0;
     s->n_loop_outer = cm0 - c0;
     s->n_loop_body = c2 - c1;
-    e = cudaGraphInstantiate(&s->g_loop, root, 0);
+    e = cudaGraphInstantiate(&slot, root, 0);
     cudaGraphDestroy(root);
     if (e != cudaSuccess) {
-        s->g_loop = nullptr;
+        slot = nullptr;
         return cuda_fail(e, "cudaGraphInstantiate(solve loop)");
     }
-    s->g_loop_inner = inner;
+    slot_inner = inner;
     return STZG_OK;
 }
 
-static int solve_device_loop(stzg_sim *s, int *ncyc) {
+static int solve_device_loop(stzg_sim *s, int *ncyc, bool fused_extrap) {
     const bool mixed = s->O.precision == STZG_MIXED;
-    // three FP32 V-cycles per pass by default: a pass then ends well below the
-    // tolerance, as the FP64 solve does with its extra V-cycle.  One per pass
-    // stops at the first V-cycle that meets the tolerance (2048^2 over 300
-    // steps: 1.23 against 1.35 ms/step) but leaves the stresses 5e-8 from the
-    // FP64 path's after 25 steps (6.6e-9 with three)
+    // three FP32 V-cycles per pass by default: with the extra V-cycle after
+    // the loop, one, two and three per pass run equally fast at 2048^2, and
+    // three leave the smallest error against the FP64 path
     const int inner = mixed ? (s->O.inner_cycles > 0 ? s->O.inner_cycles : 3) : 1;
-    STZG_CHECK(build_loop_graph(s, mixed, inner));
-    STZG_CUDA(cudaGraphLaunch(s->g_loop, s->st));
+    STZG_CHECK(build_loop_graph(s, mixed, inner, fused_extrap));
+    STZG_CUDA(cudaGraphLaunch(fused_extrap ? s->g_loop_x : s->g_loop, s->st));
     STZG_CUDA(cudaMemcpyAsync(s->hflags, s->F.flags, FL_COUNT * sizeof(int), cudaMemcpyDeviceToHost, s->st));
     STZG_CUDA(cudaMemcpyAsync(s->hnorm, s->dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
     STZG_CUDA(cudaStreamSynchronize(s->st));
@@ -502,8 +505,16 @@ static int solve_device_loop(stzg_sim *s, int *ncyc) {
 }
 
 int solve(stzg_sim *s, int *ncyc) {
-    if (s->O.tol_mode == STZG_TOL_RELATIVE && s->O.use_graphs) return solve_device_loop(s, ncyc);
+    if (s->O.tol_mode == STZG_TOL_RELATIVE && s->O.use_graphs) return solve_device_loop(s, ncyc, false);
     return s->O.precision == STZG_MIXED ? solve_mixed(s, ncyc) : solve_fp64(s, ncyc);
+}
+
+// Whether the next solve takes its linear extrapolation inside the solve
+// graph (fused with the float-float split): mixed precision in the
+// device-side loop with the extra V-cycle, whose merge rewrites the velocity.
+static bool fused_extrapolation(const stzg_sim *s) {
+    return s->O.precision == STZG_MIXED && s->O.tol_mode == STZG_TOL_RELATIVE && s->O.use_graphs &&
+           s->O.extrapolate == 1 && s->have_prev && s->extra_iters > 0;
 }
 
 int do_projection(stzg_sim *s, double dt, bool fresh_combinations) {
@@ -511,6 +522,12 @@ int do_projection(stzg_sim *s, double dt, bool fresh_combinations) {
     if (!fresh_combinations) precombine(s->sc, s->F, s->cur, dt, s->st);
     const double bv = bdry_vel(s, s->time), bp = bdry_pos(s, s->time);
     projection_source(s->sc, s->F, s->cur, dt, s->q.bcs * s->q.cxx * bv, s->st);
+    if (fused_extrapolation(s)) {
+        STZG_CHECK(solve_device_loop(s, nullptr, true));
+        projection_apply(s->sc, s->F, s->cur, dt, bv, bp, s->st);
+        s->bv_state = bv;
+        return STZG_OK;
+    }
     if (s->O.extrapolate) {
         const long cnt = (long)s->m * (s->n + 1);
         if (s->have_prev && s->O.extrapolate >= 2 && s->have_prev2) {

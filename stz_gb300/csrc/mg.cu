@@ -735,6 +735,29 @@ __global__ void k_extrapolate(double2 *__restrict__ z, double2 *__restrict__ pre
 // orders below the 1e-10 stopping tolerance, while the FP32 value handed to
 // the V-cycles needs only single precision.
 
+// The linear extrapolation of the guess (k_extrapolate's arithmetic) fused
+// with the split: prev takes the last solution, the guess 2 v - prev goes
+// straight into pairs (hi, lo) without an FP64 store (the solve ends by
+// merging its result into v), and the source b into its pairs.
+__global__ void k_extrap_split(const double2 *__restrict__ v, double2 *__restrict__ prev,
+                               const double2 *__restrict__ b, float2 *__restrict__ hi, float2 *__restrict__ lo,
+                               float2 *__restrict__ bhi, float2 *__restrict__ blo, long count) {
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (long)gridDim.x * blockDim.x) {
+        const double2 a = v[k], p = prev[k], w = b[k];
+        prev[k] = a;
+        const double gx = 2 * a.x - p.x, gy = 2 * a.y - p.y;
+        float2 h, l;
+        ff_split_d(gx, h.x, l.x);
+        ff_split_d(gy, h.y, l.y);
+        hi[k] = h;
+        lo[k] = l;
+        ff_split_d(w.x, h.x, l.x);
+        ff_split_d(w.y, h.y, l.y);
+        bhi[k] = h;
+        blo[k] = l;
+    }
+}
+
 __global__ void k_ff_split(const double2 *__restrict__ a, float2 *__restrict__ hi, float2 *__restrict__ lo,
                            const double2 *__restrict__ a2, float2 *__restrict__ hi2, float2 *__restrict__ lo2,
                            long count) {
@@ -2730,6 +2753,11 @@ static ff ff_of(double d) {
 void ff_split(const double2 *a, float2 *hi, float2 *lo, const double2 *a2, float2 *hi2, float2 *lo2, long count,
               cudaStream_t st) {
     k_ff_split<<<4 * 152, 256, 0, st>>>(a, hi, lo, a2, hi2, lo2, count); note_launch();
+}
+
+void extrap_split(const double2 *v, double2 *prev, const double2 *b, float2 *hi, float2 *lo, float2 *bhi,
+                  float2 *blo, long count, cudaStream_t st) {
+    k_extrap_split<<<4 * 152, 256, 0, st>>>(v, prev, b, hi, lo, bhi, blo, count); note_launch();
 }
 
 void ff_merge(const float2 *hi, const float2 *lo, double2 *a, long count, cudaStream_t st) {

@@ -152,6 +152,9 @@ void ff_split(const double2 *a, float2 *hi, float2 *lo, const double2 *a2, float
               cudaStream_t st);
 void ff_merge(const float2 *hi, const float2 *lo, double2 *a, long count, cudaStream_t st);
 void ff_correct(float2 *hi, float2 *lo, const float2 *e32, long count, cudaStream_t st);
+// prev = v; (hi, lo) = split(2 v - prev_old); (bhi, blo) = split(b)
+void extrap_split(const double2 *v, double2 *prev, const double2 *b, float2 *hi, float2 *lo, float2 *bhi,
+                  float2 *blo, long count, cudaStream_t st);
 // a = (hi, lo) + e32 as doubles (the last correction and the merge in one pass)
 void ff_correct_merge(const float2 *hi, const float2 *lo, const float2 *e32, double2 *a, long count, cudaStream_t st);
 void ff_residual(const top_op<double> &op64, const float2 *zhi, const float2 *zlo, const float2 *bhi,

@@ -44,6 +44,8 @@ struct stzg_sim {
     // graph (set-up, WHILE node over passes, finish); kernel nodes outside
     // and inside the loop body
     cudaGraphExec_t g_loop = nullptr;
+    cudaGraphExec_t g_loop_x = nullptr;  // the same with the guess's extrapolation fused into its split
+    int g_loop_x_inner = 0;
     long n_loop_outer = 0, n_loop_body = 0, n_loop_merge = 0;
     int g_loop_inner = 0;
     int *hflags = nullptr;  // pinned host copy of F.flags (FL_COUNT ints)
