@@ -995,21 +995,40 @@ __global__ void __launch_bounds__(SFX * SFY) k_source_ff(step_consts c, fields_d
     const int i0 = blockIdx.x * SFX, j0 = blockIdx.y * TY;
     const int tid = threadIdx.y * SFX + threadIdx.x;
     const double *P = F.f[cur][F_P], *Q = F.f[cur][F_Q], *S = F.f[cur][F_S], *T = F.f[cur][F_TAU];
-    // cells (i0 - 1 + cc, j0 - 1 + r); storage rows -1 .. n exist (unrolled:
-    // the loads of all passes in flight together)
+    // cells (i0 - 1 + cc, j0 - 1 + r); storage rows -1 .. n exist.  The
+    // passes go in two halves, each issuing all its loads before it splits
+    // anything, so that more loads are in flight per thread.
+    constexpr int kCells = (TY + 1) * (SFX + 1), kPasses = (kCells + SFX * SFY - 1) / (SFX * SFY);
+    constexpr int kHalf = (kPasses + 1) / 2;
 #pragma unroll
-    for (int k = tid; k < (TY + 1) * (SFX + 1); k += SFX * SFY) {
-        const int r = k / (SFX + 1), cc = k - r * (SFX + 1);
-        const int cj = j0 - 1 + r;
-        int ci = i0 - 1 + cc;
-        ci = ci < 0 ? ci + m : (ci >= m ? ci % m : ci);
-        if (cj > n) continue;
-        const size_t q = IDX(ci, cj);
-        const ff pp = split_ff(P[q]), qq = split_ff(Q[q]), ss = split_ff(S[q]);
-        const ff pq = ff_add(pp, qq);
-        cA[r][cc] = ff_sub(pq, ss);
-        cB[r][cc] = ff_add(pq, ss);
-        cT[r][cc] = split_ff(T[q]);
+    for (int h0 = 0; h0 < kPasses; h0 += kHalf) {
+        double vp[kHalf], vq[kHalf], vs[kHalf], vt[kHalf];
+        int rr[kHalf], cw[kHalf];
+#pragma unroll
+        for (int it = 0; it < kHalf; it++) {
+            const int k = tid + (h0 + it) * SFX * SFY;
+            const int r = k / (SFX + 1), cc = k - r * (SFX + 1);
+            const int cj = j0 - 1 + r;
+            int ci = i0 - 1 + cc;
+            ci = ci < 0 ? ci + m : (ci >= m ? ci % m : ci);
+            const bool live = h0 + it < kPasses && k < kCells && cj <= n;
+            rr[it] = live ? r : -1;
+            cw[it] = cc;
+            const size_t q = live ? IDX(ci, cj) : 0;
+            vp[it] = live ? P[q] : 0.0;
+            vq[it] = live ? Q[q] : 0.0;
+            vs[it] = live ? S[q] : 0.0;
+            vt[it] = live ? T[q] : 0.0;
+        }
+#pragma unroll
+        for (int it = 0; it < kHalf; it++) {
+            if (rr[it] < 0) continue;
+            const ff pp = split_ff(vp[it]), qq = split_ff(vq[it]), ss = split_ff(vs[it]);
+            const ff pq = ff_add(pp, qq);
+            cA[rr[it]][cw[it]] = ff_sub(pq, ss);
+            cB[rr[it]][cw[it]] = ff_add(pq, ss);
+            cT[rr[it]][cw[it]] = split_ff(vt[it]);
+        }
     }
     __syncthreads();
     const int tx = threadIdx.x, i = i0 + tx;
