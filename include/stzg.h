@@ -162,7 +162,11 @@ int stzg_c_field_pack(const void *fm_rows, int m, int n, double *const *soa);
 int stzg_c_field_unpack(const double *const *soa, int m, int n, void *fm_rows);
 
 /* Replaces: shear_sim::step_forward_quasistatic (shear_sim.cc:280-291),
- * called nsteps times; stats may be NULL. */
+ * called nsteps times; stats may be NULL.  With the relative stopping rule
+ * and graphs (and, for mixed precision, the extra V-cycle), the steps of one
+ * call run without a host round trip between them: a failure (NaN residual,
+ * pass cap, plastic sub-step cap) is reported once the call's last step has
+ * run, and the state is then undefined, as after any failed step. */
 int stzg_step_qs(stzg_sim *s, double dt, int nsteps, stzg_stats *stats);
 /* Replaces: shear_sim::step_forward (shear_sim.cc:185-276), the explicit
  * (direct) step: velocity and reference map advected with ENO2 and driven by

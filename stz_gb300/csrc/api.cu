@@ -291,6 +291,7 @@ __global__ void k_loop_start(const double *dnorm, int *flags, double tol2, cudaG
         const bool nan = isnan(r2);
         flags[FL_PASSES] = 0;
         flags[FL_LOOP_ERR] = nan ? 2 : 0;
+        if (nan && !flags[FL_ERR_FIRST]) flags[FL_ERR_FIRST] = 2;
         cudaGraphSetConditional(h, (!conv && !nan) ? 1u : 0u);
         if (has_ran) cudaGraphSetConditional(h_ran, (!conv && !nan) ? 1u : 0u);
     }
@@ -302,8 +303,10 @@ __global__ void k_loop_check(const double *dnorm, int *flags, double tol2, int c
         const bool conv = b2 > 0 ? r2 <= tol2 * b2 : r2 == 0;
         const bool nan = isnan(r2);
         const int it = ++flags[FL_PASSES];
+        ++flags[FL_PASSES_SUM];
         if (nan) flags[FL_LOOP_ERR] = 2;
         else if (!conv && it >= cap) flags[FL_LOOP_ERR] = 1;
+        if (flags[FL_LOOP_ERR] && !flags[FL_ERR_FIRST]) flags[FL_ERR_FIRST] = flags[FL_LOOP_ERR];
         cudaGraphSetConditional(h, (!conv && !nan && it < cap) ? 1u : 0u);
     }
 }
@@ -481,6 +484,14 @@ static int solve_device_loop(stzg_sim *s, int *ncyc, bool fused_extrap) {
     const int inner = mixed ? (s->O.inner_cycles > 0 ? s->O.inner_cycles : 3) : 1;
     STZG_CHECK(build_loop_graph(s, mixed, inner, fused_extrap));
     STZG_CUDA(cudaGraphLaunch(fused_extrap ? s->g_loop_x : s->g_loop, s->st));
+    if (s->defer_checks) {
+        // a multi-step call reads the pass counts and errors once, at its end
+        g_launches.fetch_add(s->n_loop_outer);
+        s->defer_solves++;
+        s->defer_inner = inner;
+        if (ncyc) *ncyc = 0;
+        return STZG_OK;
+    }
     STZG_CUDA(cudaMemcpyAsync(s->hflags, s->F.flags, FL_COUNT * sizeof(int), cudaMemcpyDeviceToHost, s->st));
     STZG_CUDA(cudaMemcpyAsync(s->hnorm, s->dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
     STZG_CUDA(cudaStreamSynchronize(s->st));
@@ -857,23 +868,71 @@ int stzg_get_time(stzg_sim *s, double *t) {
     return STZG_OK;
 }
 
+// The end of a multi-step call with deferred checks: the accumulated pass
+// count and the first error of its solves.
+static int finish_deferred(stzg_sim *s) {
+    s->defer_checks = false;
+    STZG_CUDA(cudaMemcpyAsync(s->hflags, s->F.flags, FL_COUNT * sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaMemcpyAsync(s->hnorm, s->dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    STZG_CUDA(cudaStreamSynchronize(s->st));
+    const bool mixed = s->O.precision == STZG_MIXED;
+    const long passes = s->hflags[FL_PASSES_SUM], solves = s->defer_solves;
+    const int err = s->hflags[FL_ERR_FIRST];
+    g_launches.fetch_add(passes * s->n_loop_body);
+    const double r2 = s->hnorm[0], b2 = s->hnorm[1];
+    s->acc.checks += passes + solves;
+    s->acc.last_error = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    // the step kernels' own failures (sub-step cap, tile copies, coarse
+    // barrier) come first: a solver error after them is their consequence
+    STZG_CHECK(check_flags(s));
+    if (err == 2) return fail(STZG_ENAN, "NaN residual");
+    if (err == 1) return fail(STZG_ENOTCONV, mixed ? "iterative refinement did not converge"
+                                                   : "multigrid did not converge");
+    const long cycles = passes * s->defer_inner;
+    s->acc.vcycles += cycles;
+    if (mixed) s->acc.refinements += passes;
+    s->acc.extra_vcycles += solves * s->extra_iters;
+    s->acc.solves += solves;
+    s->avg_vcount += cycles;
+    s->avg_solves += solves;
+    return STZG_OK;
+}
+
 int stzg_step_qs(stzg_sim *s, double dt, int nsteps, stzg_stats *stats) {
     if (!s || nsteps < 0 || !(dt > 0)) return fail(STZG_EINVAL, "bad step arguments");
     stzg_stats before = s->acc;
     const long l0 = launch_count();
     STZG_CHECK(ensure_ops(s, dt));
+    // Several steps in one call run without a host round trip between them:
+    // the device-side solve loops accumulate their pass counts and their
+    // first error in the flag words, read once after the last step.  A
+    // failure is then reported after that step (the state is undefined after
+    // a failed step either way).  Needs the device loop and no pass-dependent
+    // merge (the extra V-cycle merges every solve).
+    const bool defer = nsteps > 1 && s->O.tol_mode == STZG_TOL_RELATIVE && s->O.use_graphs &&
+                       (s->O.precision != STZG_MIXED || s->extra_iters > 0);
+    if (defer) {
+        STZG_CUDA(cudaMemsetAsync(s->F.flags + FL_PASSES_SUM, 0, 2 * sizeof(int), s->st));
+        s->defer_checks = true;
+        s->defer_solves = 0;
+    }
     STZG_CUDA(cudaEventRecord(s->ev0, s->st));
     for (int k = 0; k < nsteps; k++) {
         s->time += dt;  // shear_sim.cc:283
-        STZG_CHECK(do_advection(s, dt));
-        STZG_CHECK(do_projection(s, dt, true));
-        STZG_CHECK(check_flags(s));
+        int st = do_advection(s, dt);
+        if (st == STZG_OK) st = do_projection(s, dt, true);
+        if (st == STZG_OK && !defer) st = check_flags(s);
+        if (st != STZG_OK) {
+            s->defer_checks = false;
+            return st;
+        }
     }
     STZG_CUDA(cudaEventRecord(s->ev1, s->st));
     STZG_CUDA(cudaEventSynchronize(s->ev1));
     float ms = 0;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     s->acc.seconds += ms * 1e-3;
+    if (defer) STZG_CHECK(finish_deferred(s));
     STZG_CHECK(check_flags(s));
     if (stats) {
         *stats = s->acc;

@@ -46,6 +46,10 @@ struct stzg_sim {
     cudaGraphExec_t g_loop = nullptr;
     cudaGraphExec_t g_loop_x = nullptr;  // the same with the guess's extrapolation fused into its split
     int g_loop_x_inner = 0;
+    // multi-step calls: solves launched without reading their pass counts
+    bool defer_checks = false;
+    long defer_solves = 0;
+    int defer_inner = 1;
     long n_loop_outer = 0, n_loop_body = 0, n_loop_merge = 0;
     int g_loop_inner = 0;
     int *hflags = nullptr;  // pinned host copy of F.flags (FL_COUNT ints)

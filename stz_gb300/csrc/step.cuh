@@ -21,7 +21,9 @@ enum {
     FL_PASSES,
     FL_LOOP_ERR,
     FL_MG_BAR_ERR,  // a grid-barrier wait of the persistent coarse multigrid kernel ran out
-    FL_MG_BAR = 8,  // two words: that barrier's arrivals and generation
+    FL_MG_BAR = 8,  // two words (8, 9): that barrier's arrivals and generation
+    FL_PASSES_SUM = 10,  // passes of the device-loop solves since the host last cleared it
+    FL_ERR_FIRST,   // the first device-loop error since then (1 pass cap, 2 NaN)
     FL_COUNT = 12
 };
 
