@@ -52,7 +52,7 @@ def main(argv=None):
     t = time.time() - t0
     st = sim.stats
     print(f"N={N} {a.precision}: {1e3 * t / max(a.steps, 1):.2f} ms/step, {st.vcycles / max(a.steps, 1):.1f} "
-          f"V-cycles/step, {st.refinements / max(a.steps, 1):.1f} passes/step, {st.kernel_launches} kernels")
+          f"V-cycles/step (+{st.extra_vcycles / max(a.steps, 1):.1f} after convergence), {st.refinements / max(a.steps, 1):.1f} passes/step, {st.kernel_launches} kernels")
     if a.time_kernels:
         ids = [(0, "advection"), (8, "projection source")]
         if prec == _lib.MIXED:
