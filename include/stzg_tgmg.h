@@ -54,7 +54,10 @@ int stzg_tgmg_create_block(int m, int n, int x_prd, int y_prd, int block, const 
                            const int *cls, double acc, int device, stzg_tgmg **out);
 /* New operator values on the same grid: the problem class's stencil
  * changed, e.g. qs_multi::init before each solve (coord_transforms
- * qs_multi.cc:31-46).  Rebuilds the Galerkin hierarchy (tgmg::setup). */
+ * qs_multi.cc:31-46).  Rebuilds the Galerkin hierarchy (tgmg::setup).
+ * cls NULL keeps the class map of the last operator (ntable must then be
+ * the same); with the same class map, given or kept, only the stencil
+ * values are recomputed and uploaded. */
 int stzg_tgmg_set_operator(stzg_tgmg *g, const double *table, int ntable, const int *cls);
 int stzg_tgmg_destroy(stzg_tgmg *g);
 

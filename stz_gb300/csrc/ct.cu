@@ -612,7 +612,8 @@ int projection_step(stzg_ct *s, double dt, long *vcycles) {
     m22 pre;
     operator_for(s, lt, pre);
     STZG_CUDA(cudaStreamSynchronize(s->st));
-    STZG_CHECK(stzg_tgmg_set_operator(s->mg, s->table.data(), 2, s->cls.data()));
+    // the class map (wall rows or not) is the one the solver was created with
+    STZG_CHECK(stzg_tgmg_set_operator(s->mg, s->table.data(), 2, nullptr));
     const double xfac = 0.5 / dt * s->c.xsp, yfac = 0.5 / dt * s->c.ysp;
     k_ct_source<<<g2(s->c.m, s->c.lsn), kB2, 0, s->st>>>(s->c, s->F, s->cur, xfac, yfac, pre.a, pre.b, pre.c,
                                                         pre.d, s->mg_b);

@@ -441,6 +441,8 @@ template <int B> struct host_level {
     int m, n;
     bool rows;  // the stencil depends on the row only
     std::vector<int> cls;
+    std::vector<int> row_ids;  // rows: the stencil index of each row
+    bool cls_kept = false;     // cls equals the device copy already uploaded
     std::vector<gst<B>> table;
 };
 
@@ -568,8 +570,11 @@ template <int B> struct gst_eq {
 
 // Child level.  A fine level whose stencil depends on the row only, on an
 // even periodic x line, coarsens uniformly: its child depends on the row
-// only too and one Galerkin product per row suffices.
-template <int B> host_level<B> coarsen(const host_level<B> &F, int xp, int yp, int cm, int cn) {
+// only too and one Galerkin product per row suffices.  With the previous
+// child `old` of the same shape whose rows map to the same stencil indices,
+// its class map is taken over (only the stencil values are new).
+template <int B>
+host_level<B> coarsen(const host_level<B> &F, int xp, int yp, int cm, int cn, host_level<B> *old = nullptr) {
     host_level<B> C;
     C.m = cm;
     C.n = cn;
@@ -596,11 +601,18 @@ template <int B> host_level<B> coarsen(const host_level<B> &F, int xp, int yp, i
         ids[k] = it->second;
     }
     if (C.rows) {
-        C.cls.resize((size_t)cm * cn);
-        for (int J = 0; J < cn; J++)
-            for (int I = 0; I < cm; I++) C.cls[(size_t)J * cm + I] = ids[J];
+        if (old && old->rows && old->m == cm && old->n == cn && old->row_ids == ids) {
+            C.cls.swap(old->cls);
+            C.cls_kept = true;
+        } else {
+            C.cls.resize((size_t)cm * cn);
+            for (int J = 0; J < cn; J++)
+                for (int I = 0; I < cm; I++) C.cls[(size_t)J * cm + I] = ids[J];
+        }
+        C.row_ids.swap(ids);
     } else {
         C.cls.swap(ids);
+        if (old && old->m == cm && old->n == cn && old->cls == C.cls) C.cls_kept = true;
     }
     return C;
 }
@@ -926,14 +938,9 @@ template <int B> struct timed {
     }
 };
 
-// Top level from the problem's table (9 blocks per stencil, B*B doubles each).
-template <int B> int top_level(int m, int n, const double *table, int ntable, const int *cls, host_level<B> &top) {
-    const size_t mn = (size_t)m * n;
-    for (size_t k = 0; k < mn; k++)
-        if (cls[k] < 0 || cls[k] >= ntable) return fail(STZG_EINVAL, "stencil index out of range");
-    top.m = m;
-    top.n = n;
-    top.cls.assign(cls, cls + mn);
+// The top level's stencils from the problem's table (9 blocks per stencil,
+// B*B doubles each).
+template <int B> int fill_top_table(const double *table, int ntable, host_level<B> &top) {
     top.table.resize(ntable);
     std::memset(top.table.data(), 0, sizeof(gst<B>) * ntable);
     for (int c = 0; c < ntable; c++) {
@@ -943,6 +950,18 @@ template <int B> int top_level(int m, int n, const double *table, int ntable, co
         top.table[c].e[9] = block_inverse<B>(top.table[c].e[4]);
         top.table[c].nz = nonzero_mask(top.table[c]);
     }
+    return STZG_OK;
+}
+
+// Top level from the problem's table and class map.
+template <int B> int top_level(int m, int n, const double *table, int ntable, const int *cls, host_level<B> &top) {
+    const size_t mn = (size_t)m * n;
+    for (size_t k = 0; k < mn; k++)
+        if (cls[k] < 0 || cls[k] >= ntable) return fail(STZG_EINVAL, "stencil index out of range");
+    top.m = m;
+    top.n = n;
+    top.cls.assign(cls, cls + mn);
+    STZG_CHECK(fill_top_table<B>(table, ntable, top));
     top.rows = true;
     for (int j = 0; j < n && top.rows; j++)
         for (int i = 1; i < m; i++)
@@ -955,26 +974,42 @@ template <int B> int top_level(int m, int n, const double *table, int ntable, co
 
 // Galerkin hierarchy below the top and its upload (tables grow as needed;
 // sizes and z/b/r stay).  Also the dense coarsest inverse.
-template <int B> int build_hierarchy(tg<B> *g) {
+// Galerkin hierarchy below the top and its upload.  A level's class map goes
+// up only when it changed (the top's when the caller says so), so a new
+// operator on the same stencil pattern (the sheared-coordinates step: the
+// strain rate changes the values every step, not which point uses which
+// stencil) moves only the tables, a few hundred stencils.  The captured
+// iteration graph holds the levels' table pointers and the coarsest inverse
+// by value; it is dropped only when one of them moved or the bottom changed
+// between the dense inverse and smoothing.
+template <int B> int build_hierarchy(tg<B> *g, bool top_cls_kept = false) {
     const std::vector<std::pair<int, int>> sizes = level_sizes(g->host[0].m, g->host[0].n, g->xp, g->yp);
+    std::vector<host_level<B>> prev;
+    for (size_t l = 1; l < g->host.size(); l++) prev.push_back(std::move(g->host[l]));
     g->host.resize(1);
+    g->host[0].cls_kept = top_cls_kept;
     for (size_t l = 1; l < sizes.size(); l++)
-        g->host.push_back(coarsen(g->host[l - 1], g->xp, g->yp, sizes[l].first, sizes[l].second));
+        g->host.push_back(coarsen(g->host[l - 1], g->xp, g->yp, sizes[l].first, sizes[l].second,
+                                  l - 1 < prev.size() ? &prev[l - 1] : nullptr));
+    bool moved = false;
     for (int l = 0; l < g->nl; l++) {
         const host_level<B> &H = g->host[l];
         glevel<B> &L = g->lv[l];
         const size_t pts = (size_t)H.m * H.n;
-        STZG_CUDA(cudaMemcpyAsync((void *)L.cls, H.cls.data(), pts * sizeof(int), cudaMemcpyHostToDevice, g->st));
+        if (!H.cls_kept)
+            STZG_CUDA(cudaMemcpyAsync((void *)L.cls, H.cls.data(), pts * sizeof(int), cudaMemcpyHostToDevice, g->st));
         if (H.table.size() > g->st_cap[l]) {
             void *p;
             STZG_CHECK(g_alloc(g, &p, H.table.size() * sizeof(gst<B>)));
             L.st = (const gst<B> *)p;
             g->st_cap[l] = H.table.size();
+            moved = true;
         }
         STZG_CUDA(cudaMemcpyAsync((void *)L.st, H.table.data(), H.table.size() * sizeof(gst<B>),
                                   cudaMemcpyHostToDevice, g->st));
     }
     const host_level<B> &Bt = g->host.back();
+    const double *inv_was = g->inv;
     g->inv = nullptr;
     g->inv_n = 0;
     if (g->nl > 1 && (long)B * Bt.m * Bt.n <= kBottomDirect) {
@@ -992,6 +1027,7 @@ template <int B> int build_hierarchy(tg<B> *g) {
                                       g->st));
         }
     }
+    if (moved || g->inv != inv_was) drop_graph(g);
     STZG_CUDA(cudaStreamSynchronize(g->st));  // the host vectors are uploaded before they go
     return STZG_OK;
 }
@@ -1097,13 +1133,32 @@ int tg_create(int m, int n, int xp, int yp, const double *table, int ntable, con
     return STZG_OK;
 }
 
+// cls null: the class map of the last operator stays (ntable must match).
 template <int B> int tg_set_operator(tg<B> *g, const double *table, int ntable, const int *cls) {
+    host_level<B> &T = g->host[0];
+    const size_t mn = (size_t)T.m * T.n;
+    const bool kept = !cls || std::memcmp(cls, T.cls.data(), mn * sizeof(int)) == 0;
+    if (!cls && ntable != (int)T.table.size()) return fail(STZG_EINVAL, "stencil count differs from the class map's");
     host_level<B> top;
-    STZG_CHECK(top_level<B>(g->host[0].m, g->host[0].n, table, ntable, cls, top));
+    if (kept) {
+        // the same class map: new stencil values only
+        for (size_t k = 0; k < mn && cls; k++)
+            if (cls[k] >= ntable) return fail(STZG_EINVAL, "stencil index out of range");
+        top.m = T.m;
+        top.n = T.n;
+        top.rows = T.rows;
+        top.cls.swap(T.cls);
+        const int st = fill_top_table<B>(table, ntable, top);
+        if (st != STZG_OK) {
+            T.cls.swap(top.cls);
+            return st;
+        }
+    } else {
+        STZG_CHECK(top_level<B>(T.m, T.n, table, ntable, cls, top));
+    }
     STZG_CUDA(cudaStreamSynchronize(g->st));
-    g->host[0] = top;
-    drop_graph(g);  // table pointers and the coarsest inverse may have moved
-    return build_hierarchy(g);
+    g->host[0] = std::move(top);
+    return build_hierarchy(g, kept);
 }
 
 template <int B> int tg_copy(tg<B> *g, bv<B> *dev, const double *src, double *dst) {
@@ -1285,7 +1340,7 @@ int stzg_tgmg_destroy(stzg_tgmg *g) {
 }
 
 int stzg_tgmg_set_operator(stzg_tgmg *g, const double *table, int ntable, const int *cls) {
-    if (!table || ntable < 1 || !cls) return fail(STZG_EINVAL, "bad operator");
+    if (!table || ntable < 1) return fail(STZG_EINVAL, "bad operator");
     return dispatch(g, [&](auto *s) { return tg_set_operator(s, table, ntable, cls); });
 }
 

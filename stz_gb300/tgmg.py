@@ -151,10 +151,17 @@ class Tgmg:
                                                    device, ctypes.byref(h)))
         self.h = h
 
-    def set_operator(self, table, cls=None):
-        """New stencil values on the same grid (qs_multi::init + setup)."""
+    def set_operator(self, table, cls=None, keep_classes=False):
+        """New stencil values on the same grid (qs_multi::init + setup).
+        keep_classes: the class map stays the solver's last one and is not
+        passed (the same number of stencils is then required)."""
         q = self.q
-        q.table = np.ascontiguousarray(np.asarray(table, dtype=np.float64).reshape(-1, q.table.shape[1]))
+        table = np.ascontiguousarray(np.asarray(table, dtype=np.float64).reshape(-1, q.table.shape[1]))
+        if keep_classes:
+            _lib.check(self.lib.stzg_tgmg_set_operator(self.h, _dp(table), table.shape[0], None))
+            q.table = table
+            return
+        q.table = table
         if cls is not None:
             q.cls = np.ascontiguousarray(np.asarray(cls, dtype=np.int32).reshape(q.n, q.m))
         _lib.check(self.lib.stzg_tgmg_set_operator(self.h, _dp(q.table), q.table.shape[0],

@@ -246,6 +246,44 @@ def _block_operator(m, n, xp, yp, lt=0.3, seed=0, walls=True):
     return table, cls
 
 
+def test_block_operator_update_class_map():
+    """set_operator with a changed class map, and with the map kept (cls
+    NULL, only new stencil values): after each update the solver iterates bit
+    for bit like one created with that operator (the iteration graph captured
+    before an update that moves no table stays valid), and a kept map with
+    another stencil count is an error."""
+    tg = _tg()
+    from stz_gb300 import _lib
+    m, n = 40, 24
+    t0, cls0 = _block_operator(m, n, 1, 0, lt=0.1)
+    t1, _ = _block_operator(m, n, 1, 0, lt=0.45)
+    cls1 = cls0.copy()
+    cls1[n // 2, :] = 1  # an interior wall row: another stencil pattern
+    b = np.random.default_rng(6).standard_normal((n, m, 2))
+
+    def run(g, q):
+        q.b[...] = b
+        q.z[...] = 0
+        for _ in range(3):
+            g.v_cycle()
+        nl = len(g.levels())
+        return [q.z.copy(), g.stencil(1), g.stencil(nl - 1)]
+
+    q = tg.Problem(m, n, t0, cls0, 1e-26, x_prd=True, y_prd=False, block=2)
+    g = tg.Tgmg(q)
+    run(g, q)
+    for t, c, keep in ((t1, cls1, False), (t0, None, True), (t1, None, True), (t1, cls1, False)):
+        g.set_operator(t, None if keep else c, keep_classes=keep)
+        qf = tg.Problem(m, n, t, cls1, 1e-26, x_prd=True, y_prd=False, block=2)
+        gf = tg.Tgmg(qf)
+        for x, y in zip(run(g, q), run(gf, qf)):
+            assert np.array_equal(x, y)
+        gf.close()
+    with pytest.raises(_lib.StzgError):
+        g.set_operator(np.concatenate([t0, t0[:1]]), keep_classes=True)
+    g.close()
+
+
 @pytest.mark.parametrize("m,n,xp,yp", [(32, 17, 1, 0), (40, 24, 1, 1), (33, 27, 1, 1), (24, 19, 0, 0)])
 def test_block_operators(m, n, xp, yp):
     """tgmg<S,vec,mat>: Galerkin blocks and the converged solution of
