@@ -50,6 +50,10 @@ int stzg_ct_chi_bicubic(stzg_ct *s, int mm, int nn, const double *arr, double lo
 int stzg_ct_set_field(stzg_ct *s, int field, const double *host);
 int stzg_ct_get_field(stzg_ct *s, int field, double *host);
 int stzg_ct_set_time(stzg_ct *s, double time);
+/* The projection's solve: STZG_FP64 (0, the default) or STZG_MIXED (1) of
+ * stzg.h, FP32 V-cycles inside FP64 refinement (stzg_tgmg_set_precision),
+ * converged to the same threshold on the FP64 residual. */
+int stzg_ct_set_precision(stzg_ct *s, int precision);
 int stzg_ct_get_time(stzg_ct *s, double *time);
 /* nsteps of shear_sim::step_forward_quasistatic(dt) (shear_sim.cc:352-360):
  * advection_step (ENO2 advection, STZ plasticity, chi diffusion, updates,

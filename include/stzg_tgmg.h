@@ -60,6 +60,14 @@ int stzg_tgmg_create_block(int m, int n, int x_prd, int y_prd, int block, const 
  * values are recomputed and uploaded. */
 int stzg_tgmg_set_operator(stzg_tgmg *g, const double *table, int ntable, const int *cls);
 int stzg_tgmg_destroy(stzg_tgmg *g);
+/* precision 1 (STZG_MIXED of stzg.h): V-cycle solves and iterations
+ * (STZG_TGMG_VCYCLE, STZG_TGMG_SYM_VCYCLE) run as refinement passes, each an
+ * FP32 V-cycle on the FP32 rounding of the FP64 residual b - A z, its
+ * correction added to z in FP64; the predictor, l2_error and acc count and
+ * test passes and FP64 residuals as they do V-cycles.  Residuals must stay
+ * inside FP32's range (1e-38..3e38).  The other solver types, and precision 0
+ * (STZG_FP64, the default), run in FP64. */
+int stzg_tgmg_set_precision(stzg_tgmg *g, int precision);
 
 /* The source b and solution z (block*m*n doubles, row-major), copied in and out. */
 int stzg_tgmg_set_b(stzg_tgmg *g, const double *b);

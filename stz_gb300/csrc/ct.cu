@@ -1160,6 +1160,12 @@ int stzg_ct_set_time(stzg_ct *s, double time) {
     return STZG_OK;
 }
 
+int stzg_ct_set_precision(stzg_ct *s, int precision) {
+    if (!s) return fail(STZG_EINVAL, "null handle");
+    STZG_CUDA(cudaSetDevice(s->device));
+    return stzg_tgmg_set_precision(s->mg, precision);
+}
+
 int stzg_ct_get_time(stzg_ct *s, double *time) {
     if (!s || !time) return fail(STZG_EINVAL, "null argument");
     *time = s->time;

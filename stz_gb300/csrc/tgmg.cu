@@ -36,56 +36,59 @@ namespace {
 
 // Value of a point (B components) and a block (B x B, row-major: the
 // reference's vec and mat, vec.hh / mat.hh).
-template <int B> struct bv {
-    double c[B];
+template <int B, typename T = double> struct bv {
+    T c[B];
 };
-template <int B> struct bm {
-    double c[B * B];
+template <int B, typename T = double> struct bm {
+    T c[B * B];
 };
 
-template <int B> __host__ __device__ __forceinline__ bv<B> vzero() {
-    bv<B> r;
+template <int B, typename T> __host__ __device__ __forceinline__ bv<B, T> vzero() {
+    bv<B, T> r;
 #pragma unroll
     for (int k = 0; k < B; k++) r.c[k] = 0;
     return r;
 }
+__device__ __forceinline__ double tfma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float tfma(float a, float b, float c) { return fmaf(a, b, c); }
+
 // a += M x
-template <int B> __device__ __forceinline__ void madd(bv<B> &a, const bm<B> &M, const bv<B> &x) {
+template <int B, typename T> __device__ __forceinline__ void madd(bv<B, T> &a, const bm<B, T> &M, const bv<B, T> &x) {
 #pragma unroll
     for (int r = 0; r < B; r++)
 #pragma unroll
-        for (int c = 0; c < B; c++) a.c[r] = fma(M.c[r * B + c], x.c[c], a.c[r]);
+        for (int c = 0; c < B; c++) a.c[r] = tfma(M.c[r * B + c], x.c[c], a.c[r]);
 }
-template <int B> __device__ __forceinline__ bv<B> mul(const bm<B> &M, const bv<B> &x) {
-    bv<B> r;
+template <int B, typename T> __device__ __forceinline__ bv<B, T> mul(const bm<B, T> &M, const bv<B, T> &x) {
+    bv<B, T> r;
 #pragma unroll
     for (int i = 0; i < B; i++) {
-        double a = M.c[i * B] * x.c[0];
+        T a = M.c[i * B] * x.c[0];
 #pragma unroll
-        for (int c = 1; c < B; c++) a = fma(M.c[i * B + c], x.c[c], a);
+        for (int c = 1; c < B; c++) a = tfma(M.c[i * B + c], x.c[c], a);
         r.c[i] = a;
     }
     return r;
 }
-template <int B> __device__ __forceinline__ bv<B> vsub(const bv<B> &a, const bv<B> &b) {
-    bv<B> r;
+template <int B, typename T> __device__ __forceinline__ bv<B, T> vsub(const bv<B, T> &a, const bv<B, T> &b) {
+    bv<B, T> r;
 #pragma unroll
     for (int k = 0; k < B; k++) r.c[k] = a.c[k] - b.c[k];
     return r;
 }
 
-template <int B> struct gst {
-    bm<B> e[10];  // dl dc dr cl cc cr ul uc ur, inverse of cc (tgmg_level::s, tgmg.hh:256-265)
+template <int B, typename T = double> struct gst {
+    bm<B, T> e[10];  // dl dc dr cl cc cr ul uc ur, inverse of cc (tgmg_level::s, tgmg.hh:256-265)
     int nz;       // bit k set where off-diagonal block k is nonzero
     int pad;
 };
 
-template <int B> struct glevel {
+template <int B, typename T = double> struct glevel {
     int m, n, xp, yp;
     int cx_n, cy_n;  // colours per direction: 2, or 3 on an odd periodic line
     const int *cls;
-    const gst<B> *st;
-    bv<B> *z, *b, *r;
+    const gst<B, T> *st;
+    bv<B, T> *z, *b, *r;
 };
 
 constexpr int kMaxLevels = 17;
@@ -110,25 +113,25 @@ __host__ __device__ inline int nbr(int i, int d, int m, int prd) {
 // tgmg.in.cc:536-547); neighbours outside a non-periodic grid are skipped, and
 // so are zero blocks (an integer test on the stencil's mask: the FP64 pipe,
 // GB300's scarce one, only sees the nonzero products).
-template <int B>
-__device__ __forceinline__ bv<B> offdiag(const glevel<B> &L, const gst<B> &s, int i, int j) {
+template <int B, typename T>
+__device__ __forceinline__ bv<B, T> offdiag(const glevel<B, T> &L, const gst<B, T> &s, int i, int j) {
     const int il = nbr(i, -1, L.m, L.xp), ir = nbr(i, 1, L.m, L.xp);
     const int jd = nbr(j, -1, L.n, L.yp), ju = nbr(j, 1, L.n, L.yp);
     const int nz = s.nz;
-    bv<B> a = vzero<B>();
+    bv<B, T> a = vzero<B, T>();
     if (jd >= 0) {
-        const bv<B> *zr = L.z + (size_t)jd * L.m;
+        const bv<B, T> *zr = L.z + (size_t)jd * L.m;
         if ((nz & 1) && il >= 0) madd(a, s.e[0], zr[il]);
         if (nz & 2) madd(a, s.e[1], zr[i]);
         if ((nz & 4) && ir >= 0) madd(a, s.e[2], zr[ir]);
     }
     {
-        const bv<B> *zr = L.z + (size_t)j * L.m;
+        const bv<B, T> *zr = L.z + (size_t)j * L.m;
         if ((nz & 8) && il >= 0) madd(a, s.e[3], zr[il]);
         if ((nz & 32) && ir >= 0) madd(a, s.e[5], zr[ir]);
     }
     if (ju >= 0) {
-        const bv<B> *zr = L.z + (size_t)ju * L.m;
+        const bv<B, T> *zr = L.z + (size_t)ju * L.m;
         if ((nz & 64) && il >= 0) madd(a, s.e[6], zr[il]);
         if (nz & 128) madd(a, s.e[7], zr[i]);
         if ((nz & 256) && ir >= 0) madd(a, s.e[8], zr[ir]);
@@ -137,9 +140,9 @@ __device__ __forceinline__ bv<B> offdiag(const glevel<B> &L, const gst<B> &s, in
 }
 
 // r = b - A z at (i, j)
-template <int B>
-__device__ __forceinline__ bv<B> residual_at(const glevel<B> &L, const gst<B> &s, size_t ij, int i, int j) {
-    bv<B> a = offdiag(L, s, i, j);
+template <int B, typename T>
+__device__ __forceinline__ bv<B, T> residual_at(const glevel<B, T> &L, const gst<B, T> &s, size_t ij, int i, int j) {
+    bv<B, T> a = offdiag(L, s, i, j);
     madd(a, s.e[4], L.z[ij]);
     return vsub(L.b[ij], a);
 }
@@ -156,18 +159,18 @@ __device__ __forceinline__ int color_line(int k, int c, int m, int cn) {
 
 // One colour of Gauss-Seidel or SOR: z += omega (D^-1 (b - A'z) - z)
 // (gauss_seidel, sor: tgmg.in.cc:128-230).
-template <int B, bool Relax>
-__global__ void k_tg_color(glevel<B> L, int cx, int cy, double omega) {
+template <int B, typename T, bool Relax>
+__global__ void k_tg_color(glevel<B, T> L, int cx, int cy, double omega) {
     const int i = color_line(blockIdx.x * blockDim.x + threadIdx.x, cx, L.m, L.cx_n);
     const int j = color_line(blockIdx.y * blockDim.y + threadIdx.y, cy, L.n, L.cy_n);
     if (i < 0 || j < 0) return;
     const size_t ij = (size_t)j * L.m + i;
-    const gst<B> &s = L.st[L.cls[ij]];
-    const bv<B> t = mul(s.e[9], vsub(L.b[ij], offdiag(L, s, i, j)));
+    const gst<B, T> &s = L.st[L.cls[ij]];
+    const bv<B, T> t = mul(s.e[9], vsub(L.b[ij], offdiag(L, s, i, j)));
     if (Relax) {
-        bv<B> z = L.z[ij];
+        bv<B, T> z = L.z[ij];
 #pragma unroll
-        for (int k = 0; k < B; k++) z.c[k] += omega * (t.c[k] - z.c[k]);
+        for (int k = 0; k < B; k++) z.c[k] += T(omega) * (t.c[k] - z.c[k]);
         L.z[ij] = z;
     } else {
         L.z[ij] = t;
@@ -184,7 +187,7 @@ template <int B> __global__ void k_tg_jacobi(glevel<B> L) {
 }
 
 // r = b - A z (tgmg_base::res, tgmg.hh:197-199).
-template <int B> __global__ void k_tg_residual(glevel<B> L) {
+template <int B, typename T> __global__ void k_tg_residual(glevel<B, T> L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= L.m || j >= L.n) return;
     const size_t ij = (size_t)j * L.m + i;
@@ -205,17 +208,17 @@ __device__ __forceinline__ int fine_at(int I, int d, int m, int prd) {
 // 1/4 from the interpolation's halves in each direction, summed as
 // (sum over rows of hy * (sum over columns of hx * r)) / 4 with the factors 2
 // applied as additions.
-template <int B>
-__device__ __forceinline__ bv<B> restrict_at(const glevel<B> &F, const bv<B> *r, int I, int J) {
-    bv<B> acc = vzero<B>();
+template <int B, typename T>
+__device__ __forceinline__ bv<B, T> restrict_at(const glevel<B, T> &F, const bv<B, T> *r, int I, int J) {
+    bv<B, T> acc = vzero<B, T>();
 #pragma unroll
     for (int dy = -1; dy <= 1; dy++) {
         const int fy = fine_at(J, dy, F.n, F.yp);
         if (fy < 0) continue;
         const int hy = halves_of(fy, F.n, F.yp, J);
         if (!hy) continue;
-        const bv<B> *rr = r + (size_t)fy * F.m;
-        bv<B> row = vzero<B>();
+        const bv<B, T> *rr = r + (size_t)fy * F.m;
+        bv<B, T> row = vzero<B, T>();
 #pragma unroll
         for (int dx = -1; dx <= 1; dx++) {
             const int fx = fine_at(I, dx, F.m, F.xp);
@@ -229,11 +232,11 @@ __device__ __forceinline__ bv<B> restrict_at(const glevel<B> &F, const bv<B> *r,
         for (int k = 0; k < B; k++) acc.c[k] += hy == 2 ? row.c[k] + row.c[k] : row.c[k];
     }
 #pragma unroll
-    for (int k = 0; k < B; k++) acc.c[k] *= 0.25;
+    for (int k = 0; k < B; k++) acc.c[k] *= T(0.25);
     return acc;
 }
 
-template <int B> __global__ void k_tg_restrict(glevel<B> F, glevel<B> C) {
+template <int B, typename T> __global__ void k_tg_restrict(glevel<B, T> F, glevel<B, T> C) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y;
     if (I >= C.m || J >= C.n) return;
     C.b[(size_t)J * C.m + I] = restrict_at(F, F.r, I, J);
@@ -242,41 +245,42 @@ template <int B> __global__ void k_tg_restrict(glevel<B> F, glevel<B> C) {
 // Interpolated child value at a parent point from the coarse indices of
 // p1d_halves: injection, the mean of two, or the mean of four (exact weights
 // 1, 1/2, 1/4 applied as one multiplication).
-template <int B>
-__device__ __forceinline__ bv<B> interp_at(const glevel<B> &C, int ny, const int *cy, int nx, const int *cx) {
-    const bv<B> *r0 = C.z + (size_t)cy[0] * C.m, *r1 = C.z + (size_t)cy[ny - 1] * C.m;
-    bv<B> o;
+template <int B, typename T>
+__device__ __forceinline__ bv<B, T> interp_at(const glevel<B, T> &C, int ny, const int *cy, int nx, const int *cx) {
+    const bv<B, T> *r0 = C.z + (size_t)cy[0] * C.m, *r1 = C.z + (size_t)cy[ny - 1] * C.m;
+    bv<B, T> o;
 #pragma unroll
     for (int k = 0; k < B; k++) {
-        if (ny == 1) o.c[k] = nx == 1 ? r0[cx[0]].c[k] : 0.5 * (r0[cx[0]].c[k] + r0[cx[1]].c[k]);
-        else if (nx == 1) o.c[k] = 0.5 * (r0[cx[0]].c[k] + r1[cx[0]].c[k]);
-        else o.c[k] = 0.25 * ((r0[cx[0]].c[k] + r0[cx[1]].c[k]) + (r1[cx[0]].c[k] + r1[cx[1]].c[k]));
+        if (ny == 1) o.c[k] = nx == 1 ? r0[cx[0]].c[k] : T(0.5) * (r0[cx[0]].c[k] + r0[cx[1]].c[k]);
+        else if (nx == 1) o.c[k] = T(0.5) * (r0[cx[0]].c[k] + r1[cx[0]].c[k]);
+        else o.c[k] = T(0.25) * ((r0[cx[0]].c[k] + r0[cx[1]].c[k]) + (r1[cx[0]].c[k] + r1[cx[1]].c[k]));
     }
     return o;
 }
 
 // Parent z += P z_child (apply_t, tgmg.in.cc:552-606).
-template <int B> __global__ void k_tg_prolong(glevel<B> C, glevel<B> F) {
+template <int B, typename T> __global__ void k_tg_prolong(glevel<B, T> C, glevel<B, T> F) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= F.m || j >= F.n) return;
     int cy[2], hy[2], cx[2], hx[2];
     const int ny = p1d_halves(j, F.n, F.yp, cy, hy), nx = p1d_halves(i, F.m, F.xp, cx, hx);
-    const bv<B> a = interp_at(C, ny, cy, nx, cx);
-    bv<B> &z = F.z[(size_t)j * F.m + i];
+    const bv<B, T> a = interp_at(C, ny, cy, nx, cx);
+    bv<B, T> &z = F.z[(size_t)j * F.m + i];
 #pragma unroll
     for (int k = 0; k < B; k++) z.c[k] += a.c[k];
 }
 
-// Coarsest level: z = A^-1 b with the dense FP64 inverse over its N unknowns.
-template <int B> __global__ void k_tg_bottom(glevel<B> L, const double *__restrict__ inv, int N) {
-    __shared__ double bb[kBottomDirect];
-    const double *b = (const double *)L.b;
-    double *z = (double *)L.z;
+// Coarsest level: z = A^-1 b with the dense inverse over its N unknowns (FP64;
+// its FP32 rounding in the correction cycles of a mixed-precision solver).
+template <int B, typename T> __global__ void k_tg_bottom(glevel<B, T> L, const T *__restrict__ inv, int N) {
+    __shared__ T bb[kBottomDirect];
+    const T *b = (const T *)L.b;
+    T *z = (T *)L.z;
     for (int k = threadIdx.x; k < N; k += blockDim.x) bb[k] = b[k];
     __syncthreads();
     for (int r = threadIdx.x; r < N; r += blockDim.x) {
-        const double *row = inv + (size_t)r * N;
-        double a = 0;
+        const T *row = inv + (size_t)r * N;
+        T a = 0;
         for (int k = 0; k < N; k++) a += row[k] * bb[k];
         z[r] = a;
     }
@@ -319,6 +323,43 @@ __global__ void k_tg_sum(const double *partials, int np, double *out) {
     if (threadIdx.x == 0) *out = t;
 }
 
+// Mixed precision, once per refinement pass on the top level: r = b - A z in
+// FP64, its FP32 rounding as the correction cycle's b, the correction's z
+// cleared, and per-block partial sums of |r|^2 in the order of k_tg_sqnorm
+// (the l2_error of a z is the same number either way).
+template <int B> __global__ void k_tg_resid_split(glevel<B> L, glevel<B, float> F, double *partials) {
+    __shared__ double sh[32];
+    const long mn = (long)L.m * L.n;
+    double acc = 0;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += (long)gridDim.x * blockDim.x) {
+        const int j = (int)(k / L.m), i = (int)(k - (long)j * L.m);
+        const bv<B> r = residual_at(L, L.st[L.cls[k]], (size_t)k, i, j);
+        bv<B, float> rf, zf;
+#pragma unroll
+        for (int c = 0; c < B; c++) {
+            acc += r.c[c] * r.c[c];
+            rf.c[c] = (float)r.c[c];
+            zf.c[c] = 0.f;
+        }
+        F.b[k] = rf;
+        F.z[k] = zf;
+    }
+    const double t = block_reduce(acc, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = t;
+}
+
+// z += e: a correction cycle's FP32 result added to the FP64 solution.
+template <int B> __global__ void k_tg_correct(glevel<B> L, const bv<B, float> *__restrict__ e) {
+    const long mn = (long)L.m * L.n;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += (long)gridDim.x * blockDim.x) {
+        const bv<B, float> d = e[k];
+        bv<B> z = L.z[k];
+#pragma unroll
+        for (int c = 0; c < B; c++) z.c[c] += (double)d.c[c];
+        L.z[k] = z;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Tail of the cycle on the small levels, one block of 32 x 32 threads: the
 // recursive V-cycle below level t (down sweeps from zero, residual and
@@ -327,14 +368,14 @@ __global__ void k_tg_sum(const double *partials, int np, double *out) {
 // and z of level t goes to global memory.  Phases are separated by
 // __syncthreads.
 
-template <int B> struct tail_args {
+template <int B, typename T> struct tail_args {
     int t, L, cd, cu, hb, sym;
-    const double *inv;
+    const T *inv;
     int inv_n;
-    glevel<B> lv[kMaxLevels];
+    glevel<B, T> lv[kMaxLevels];
 };
 
-template <int B> __device__ void tail_sweep(const glevel<B> &L, bool reverse) {
+template <int B, typename T> __device__ void tail_sweep(const glevel<B, T> &L, bool reverse) {
     const int nc = L.cx_n * L.cy_n;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
     const int kx = (L.m + 1) / 2, ky = (L.n + 1) / 2;
@@ -345,26 +386,26 @@ template <int B> __device__ void tail_sweep(const glevel<B> &L, bool reverse) {
             const int i = color_line(k % kx, cx, L.m, L.cx_n), j = color_line(k / kx, cy, L.n, L.cy_n);
             if (i < 0 || j < 0) continue;
             const size_t ij = (size_t)j * L.m + i;
-            const gst<B> &s = L.st[L.cls[ij]];
+            const gst<B, T> &s = L.st[L.cls[ij]];
             L.z[ij] = mul(s.e[9], vsub(L.b[ij], offdiag(L, s, i, j)));
         }
         __syncthreads();
     }
 }
 
-template <int B> __device__ void tail_clear(const glevel<B> &L) {
+template <int B, typename T> __device__ void tail_clear(const glevel<B, T> &L) {
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
-    for (int k = tid; k < L.m * L.n; k += nth) L.z[k] = vzero<B>();
+    for (int k = tid; k < L.m * L.n; k += nth) L.z[k] = vzero<B, T>();
     __syncthreads();
 }
 
-template <int B> __global__ void __launch_bounds__(1024) k_tg_tail(tail_args<B> a) {
+template <int B, typename T> __global__ void __launch_bounds__(1024) k_tg_tail(tail_args<B, T> a) {
     extern __shared__ __align__(16) double tsm[];
-    __shared__ glevel<B> S[kMaxLevels];
+    __shared__ glevel<B, T> S[kMaxLevels];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
     if (tid == 0) {
         size_t off = 0;
-        bv<B> *base = (bv<B> *)tsm;
+        bv<B, T> *base = (bv<B, T> *)tsm;
         for (int l = a.t; l <= a.L; l++) {
             S[l] = a.lv[l];
             const size_t mn = (size_t)S[l].m * S[l].n;
@@ -376,13 +417,13 @@ template <int B> __global__ void __launch_bounds__(1024) k_tg_tail(tail_args<B> 
     }
     __syncthreads();
     {
-        const glevel<B> &T = S[a.t];
-        for (int k = tid; k < T.m * T.n; k += nth) T.b[k] = a.lv[a.t].b[k];
+        const glevel<B, T> &Lt = S[a.t];
+        for (int k = tid; k < Lt.m * Lt.n; k += nth) Lt.b[k] = a.lv[a.t].b[k];
         __syncthreads();
     }
     // down: levels t..L-1 (down_gs_iterations, then residual and restriction)
     for (int i = a.t; i < a.L; i++) {
-        const glevel<B> &L = S[i], &C = S[i + 1];
+        const glevel<B, T> &L = S[i], &C = S[i + 1];
         tail_clear(L);
         for (int c = 0; c < a.cd; c++) tail_sweep(L, false);
         for (int k = tid; k < L.m * L.n; k += nth) {
@@ -398,13 +439,13 @@ template <int B> __global__ void __launch_bounds__(1024) k_tg_tail(tail_args<B> 
     }
     // coarsest level
     {
-        const glevel<B> &Bt = S[a.L];
+        const glevel<B, T> &Bt = S[a.L];
         if (a.inv) {
-            const double *b = (const double *)Bt.b;
-            double *z = (double *)Bt.z;
+            const T *b = (const T *)Bt.b;
+            T *z = (T *)Bt.z;
             for (int r = tid; r < a.inv_n; r += nth) {
-                const double *row = a.inv + (size_t)r * a.inv_n;
-                double acc = 0;
+                const T *row = a.inv + (size_t)r * a.inv_n;
+                T acc = 0;
                 for (int k = 0; k < a.inv_n; k++) acc += row[k] * b[k];
                 z[r] = acc;
             }
@@ -416,12 +457,12 @@ template <int B> __global__ void __launch_bounds__(1024) k_tg_tail(tail_args<B> 
     }
     // up: prolongation and up_gs_iterations on levels L-1..t
     for (int i = a.L; i > a.t; i--) {
-        const glevel<B> &C = S[i], &F = S[i - 1];
+        const glevel<B, T> &C = S[i], &F = S[i - 1];
         for (int k = tid; k < F.m * F.n; k += nth) {
             const int j = k / F.m, ii = k - j * F.m;
             int cy[2], hy[2], cx[2], hx[2];
             const int ny = p1d_halves(j, F.n, F.yp, cy, hy), nx = p1d_halves(ii, F.m, F.xp, cx, hx);
-            const bv<B> v = interp_at(C, ny, cy, nx, cx);
+            const bv<B, T> v = interp_at(C, ny, cy, nx, cx);
 #pragma unroll
             for (int q = 0; q < B; q++) F.z[k].c[q] += v.c[q];
         }
@@ -429,8 +470,8 @@ template <int B> __global__ void __launch_bounds__(1024) k_tg_tail(tail_args<B> 
         for (int c = 0; c < a.cu; c++) tail_sweep(F, a.sym != 0);
     }
     {
-        const glevel<B> &T = S[a.t];
-        for (int k = tid; k < T.m * T.n; k += nth) a.lv[a.t].z[k] = T.z[k];
+        const glevel<B, T> &Lt = S[a.t];
+        for (int k = tid; k < Lt.m * Lt.n; k += nth) a.lv[a.t].z[k] = Lt.z[k];
     }
 }
 
@@ -678,6 +719,15 @@ inline dim3 grid_of(int m, int n, dim3 b) { return dim3(ceil_div(m, b.x), ceil_d
 // ---------------------------------------------------------------------------
 // The solver state of one handle, for B components per point.
 
+// The levels one cycle runs on, with the coarsest level's dense inverse (null
+// where the bottom is smoothed): the solver's FP64 levels, or the FP32 levels
+// of a mixed-precision solver's correction cycles.
+template <int B, typename T> struct hview {
+    const glevel<B, T> *lv;
+    const T *inv;
+    int inv_n;
+};
+
 template <int B> struct tg {
     int device = 0;
     int xp = 0, yp = 0;
@@ -694,6 +744,19 @@ template <int B> struct tg {
     size_t inv_cap = 0;
     int tail_start = 1 << 30;  // first level handled by k_tg_tail (none if > nl-1)
     double *partials = nullptr, *dsum = nullptr, *hsum = nullptr;
+    std::vector<double> inv_host;  // the coarsest inverse, for its FP32 copy
+    std::vector<std::vector<gst<B, float>>> host32;  // FP32 tables as uploaded
+    std::vector<float> inv_host32;
+    // Mixed precision (V-cycle solves as refinement passes: FP32 V-cycles on
+    // the FP64 residual, corrections added in FP64): FP32 levels sharing the
+    // class maps of lv, their tables and the FP32 coarsest inverse.
+    bool mixed = false, have32 = false;
+    glevel<B, float> lf[kMaxLevels];
+    size_t stf_cap[kMaxLevels] = {0};
+    float *inv_f = nullptr;
+    size_t inv_f_cap = 0;
+    hview<B, double> v64() const { return hview<B, double>{lv, inv, inv_n}; }
+    hview<B, float> v32() const { return hview<B, float>{lf, inv ? inv_f : nullptr, inv_n}; }
     // graph of one iteration of the last (type, omega, cycles) used
     cudaGraphExec_t gexec = nullptr;
     int gkey[5] = {-1, 0, 0, 0, 0};
@@ -719,51 +782,52 @@ template <int B> void launch_note(tg<B> *g) {
 
 const dim3 kBlk(32, 8);
 
-template <int B> void sweep(tg<B> *g, const glevel<B> &L, bool reverse, double omega) {
+template <int B, typename T> void sweep(tg<B> *g, const glevel<B, T> &L, bool reverse, double omega) {
     const int nc = L.cx_n * L.cy_n;
     for (int q = 0; q < nc; q++) {
         const int c = reverse ? nc - 1 - q : q;
         const int cy = c / L.cx_n, cx = c % L.cx_n;
         const dim3 gr = grid_of((L.m + 1) / 2, (L.n + 1) / 2, kBlk);
-        if (omega == 1.0) k_tg_color<B, false><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
-        else k_tg_color<B, true><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
+        if (omega == 1.0) k_tg_color<B, T, false><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
+        else k_tg_color<B, T, true><<<gr, kBlk, 0, g->st>>>(L, cx, cy, omega);
         launch_note(g);
     }
 }
 
-template <int B> void clear_z(tg<B> *g, const glevel<B> &L) {
-    cudaMemsetAsync(L.z, 0, sizeof(bv<B>) * (size_t)L.m * L.n, g->st);
+template <int B, typename T> void clear_z(tg<B> *g, const glevel<B, T> &L) {
+    cudaMemsetAsync(L.z, 0, sizeof(bv<B, T>) * (size_t)L.m * L.n, g->st);
 }
 
 // down_gs_iterations (tgmg.hh:273-279): clear z, then cyc sweeps (the first
 // from zero).
-template <int B> void down_gs(tg<B> *g, const glevel<B> &L, int cyc) {
+template <int B, typename T> void down_gs(tg<B> *g, const glevel<B, T> &L, int cyc) {
     clear_z(g, L);
     for (int c = 0; c < cyc; c++) sweep(g, L, false, 1.0);
 }
 
 // up_gs_iterations (tgmg.hh:183-187): cyc sweeps, reversed when symmetric.
-template <int B> void up_gs(tg<B> *g, const glevel<B> &L, int cyc, bool sym) {
+template <int B, typename T> void up_gs(tg<B> *g, const glevel<B, T> &L, int cyc, bool sym) {
     for (int c = 0; c < cyc; c++) sweep(g, L, sym, 1.0);
 }
 
-template <int B> void restrict_to(tg<B> *g, const glevel<B> &F, const glevel<B> &C) {
-    k_tg_residual<B><<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(F);
+template <int B, typename T> void restrict_to(tg<B> *g, const glevel<B, T> &F, const glevel<B, T> &C) {
+    k_tg_residual<B, T><<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(F);
     launch_note(g);
-    k_tg_restrict<B><<<grid_of(C.m, C.n, kBlk), kBlk, 0, g->st>>>(F, C);
+    k_tg_restrict<B, T><<<grid_of(C.m, C.n, kBlk), kBlk, 0, g->st>>>(F, C);
     launch_note(g);
 }
 
-template <int B> void prolong(tg<B> *g, const glevel<B> &C, const glevel<B> &F) {
-    k_tg_prolong<B><<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(C, F);
+template <int B, typename T> void prolong(tg<B> *g, const glevel<B, T> &C, const glevel<B, T> &F) {
+    k_tg_prolong<B, T><<<grid_of(F.m, F.n, kBlk), kBlk, 0, g->st>>>(C, F);
     launch_note(g);
 }
 
 // Coarsest level: the reference's hcyc_bottom sweeps down and up
 // (tgmg.in.cc:350-352), replaced by the exact solve where it is available.
-template <int B> void bottom(tg<B> *g, const glevel<B> &Bt, int hcyc, bool sym) {
-    if (g->inv) {
-        k_tg_bottom<B><<<1, 256, 0, g->st>>>(Bt, g->inv, g->inv_n);
+template <int B, typename T> void bottom(tg<B> *g, const hview<B, T> &h, int hcyc, bool sym) {
+    const glevel<B, T> &Bt = h.lv[g->nl - 1];
+    if (h.inv) {
+        k_tg_bottom<B, T><<<1, 256, 0, g->st>>>(Bt, h.inv, h.inv_n);
         launch_note(g);
     } else {
         down_gs(g, Bt, hcyc);
@@ -771,24 +835,24 @@ template <int B> void bottom(tg<B> *g, const glevel<B> &Bt, int hcyc, bool sym) 
     }
 }
 
-template <int B> size_t tail_bytes(const tg<B> *g, int i) {
+template <int B, typename T> size_t tail_bytes(const tg<B> *g, const hview<B, T> &h, int i) {
     size_t smem = 0;
-    for (int l = i; l < g->nl; l++) smem += 3 * sizeof(bv<B>) * (size_t)g->lv[l].m * g->lv[l].n;
+    for (int l = i; l < g->nl; l++) smem += 3 * sizeof(bv<B, T>) * (size_t)h.lv[l].m * h.lv[l].n;
     return smem;
 }
 
-template <int B> void tail(tg<B> *g, int i, int cd, int cu, int hb, bool sym) {
-    tail_args<B> a;
+template <int B, typename T> void tail(tg<B> *g, const hview<B, T> &h, int i, int cd, int cu, int hb, bool sym) {
+    tail_args<B, T> a;
     a.t = i;
     a.L = g->nl - 1;
     a.cd = cd;
     a.cu = cu;
     a.hb = hb;
     a.sym = sym ? 1 : 0;
-    a.inv = g->inv;
-    a.inv_n = g->inv_n;
-    for (int l = 0; l < g->nl; l++) a.lv[l] = g->lv[l];
-    k_tg_tail<B><<<1, dim3(32, 32), tail_bytes(g, i), g->st>>>(a);
+    a.inv = h.inv;
+    a.inv_n = h.inv_n;
+    for (int l = 0; l < g->nl; l++) a.lv[l] = h.lv[l];
+    k_tg_tail<B, T><<<1, dim3(32, 32), tail_bytes(g, h, i), g->st>>>(a);
     launch_note(g);
 }
 
@@ -796,68 +860,98 @@ template <int B> void tail(tg<B> *g, int i, int cd, int cu, int hb, bool sym) {
 // below, prolongation, up_gs; the coarsest level is the bottom solve.  This
 // is v_cycle_internal (tgmg.in.cc:341-359) written recursively; levels from
 // tail_start down run in one k_tg_tail launch.
-template <int B> void vc(tg<B> *g, int i, int cd, int cu, int hb, bool sym) {
+template <int B, typename T> void vc(tg<B> *g, const hview<B, T> &h, int i, int cd, int cu, int hb, bool sym) {
     const int L = g->nl - 1;
     if (i == L) {
-        bottom(g, g->lv[L], hb, sym);
+        bottom(g, h, hb, sym);
         return;
     }
     if (i >= g->tail_start) {
-        tail(g, i, cd, cu, hb, sym);
+        tail(g, h, i, cd, cu, hb, sym);
         return;
     }
-    down_gs(g, g->lv[i], cd);
-    restrict_to(g, g->lv[i], g->lv[i + 1]);
-    vc(g, i + 1, cd, cu, hb, sym);
-    prolong(g, g->lv[i + 1], g->lv[i]);
-    up_gs(g, g->lv[i], cu, sym);
+    down_gs(g, h.lv[i], cd);
+    restrict_to(g, h.lv[i], h.lv[i + 1]);
+    vc(g, h, i + 1, cd, cu, hb, sym);
+    prolong(g, h.lv[i + 1], h.lv[i]);
+    up_gs(g, h.lv[i], cu, sym);
 }
 
 // v_cycle_internal from a level whose z has had its down sweeps: restrict,
 // cycle below, prolong, up sweeps.
-template <int B> void internal(tg<B> *g, int level, int cd, int cu, int hb, bool sym) {
-    restrict_to(g, g->lv[level], g->lv[level + 1]);
-    vc(g, level + 1, cd, cu, hb, sym);
-    prolong(g, g->lv[level + 1], g->lv[level]);
-    up_gs(g, g->lv[level], cu, sym);
+template <int B, typename T>
+void internal(tg<B> *g, const hview<B, T> &h, int level, int cd, int cu, int hb, bool sym) {
+    restrict_to(g, h.lv[level], h.lv[level + 1]);
+    vc(g, h, level + 1, cd, cu, hb, sym);
+    prolong(g, h.lv[level + 1], h.lv[level]);
+    up_gs(g, h.lv[level], cu, sym);
 }
 
 // tgmg::v_cycle (tgmg.in.cc:313-328).
-template <int B> void v_cycle(tg<B> *g, int cd, int cu, int hb, bool sym) {
-    for (int c = 0; c < cd; c++) sweep(g, g->lv[0], false, 1.0);
+template <int B, typename T> void v_cycle(tg<B> *g, const hview<B, T> &h, int cd, int cu, int hb, bool sym) {
+    for (int c = 0; c < cd; c++) sweep(g, h.lv[0], false, 1.0);
     if (g->nl > 1) {
-        restrict_to(g, g->lv[0], g->lv[1]);
-        vc(g, 1, cd, cu, hb, sym);
-        prolong(g, g->lv[1], g->lv[0]);
+        restrict_to(g, h.lv[0], h.lv[1]);
+        vc(g, h, 1, cd, cu, hb, sym);
+        prolong(g, h.lv[1], h.lv[0]);
     }
-    up_gs(g, g->lv[0], cu, sym);
+    up_gs(g, h.lv[0], cu, sym);
 }
 
 // tgmg::fmg_pre (tgmg.in.cc:369-402).
 template <int B> void fmg_pre(tg<B> *g, int cd, int cu, int hb, bool sym) {
+    const hview<B, double> h = g->v64();
     const int L = g->nl - 1;
-    for (int c = 0; c < cd; c++) sweep(g, g->lv[0], false, 1.0);
+    for (int c = 0; c < cd; c++) sweep(g, h.lv[0], false, 1.0);
     if (L > 0) {
-        restrict_to(g, g->lv[0], g->lv[1]);
+        restrict_to(g, h.lv[0], h.lv[1]);
         for (int i = 1; i < L; i++) {
-            down_gs(g, g->lv[i], cd);
-            restrict_to(g, g->lv[i], g->lv[i + 1]);
+            down_gs(g, h.lv[i], cd);
+            restrict_to(g, h.lv[i], h.lv[i + 1]);
         }
-        bottom(g, g->lv[L], hb, sym);
+        bottom(g, h, hb, sym);
         for (int i = L; i > 1; i--) {
-            prolong(g, g->lv[i], g->lv[i - 1]);
-            up_gs(g, g->lv[i - 1], cu, sym);
-            for (int c = 0; c < cd; c++) sweep(g, g->lv[i - 1], false, 1.0);
-            internal(g, i - 1, cd, cu, hb, sym);
+            prolong(g, h.lv[i], h.lv[i - 1]);
+            up_gs(g, h.lv[i - 1], cu, sym);
+            for (int c = 0; c < cd; c++) sweep(g, h.lv[i - 1], false, 1.0);
+            internal(g, h, i - 1, cd, cu, hb, sym);
         }
-        prolong(g, g->lv[1], g->lv[0]);
+        prolong(g, h.lv[1], h.lv[0]);
     }
-    up_gs(g, g->lv[0], cu, sym);
+    up_gs(g, h.lv[0], cu, sym);
 }
 
-// One iteration of a solver type (tgmg::iters, tgmg.hh:457-466).
+template <int B> bool uses_mixed(const tg<B> *g, int type) {
+    return g->mixed && (type == STZG_TGMG_VCYCLE || type == STZG_TGMG_SYM_VCYCLE);
+}
+
+// Mixed precision: the top level's FP64 residual of the current z into the
+// FP32 correction cycle's b, with its squared-norm partials.
+template <int B> void resid_split(tg<B> *g) {
+    k_tg_resid_split<B><<<kRedBlocks, kRedThreads, 0, g->st>>>(g->lv[0], g->lf[0], g->partials);
+    launch_note(g);
+}
+
+// One refinement pass of a mixed-precision V-cycle solve, after resid_split:
+// an FP32 V-cycle on the residual from a zero correction, the correction
+// added to the FP64 solution, and the new residual with its norm partials.
+// With a V-cycle's contraction per pass (the FP32 rounding of the correction
+// costs ~1e-7 of it), passes converge like FP64 V-cycles.
+template <int B> void mixed_pass(tg<B> *g, int cd, int cu, int hb, bool sym) {
+    v_cycle(g, g->v32(), cd, cu, hb, sym);
+    k_tg_correct<B><<<kRedBlocks, kRedThreads, 0, g->st>>>(g->lv[0], g->lf[0].z);
+    launch_note(g);
+    resid_split(g);
+}
+
+// One iteration of a solver type (tgmg::iters, tgmg.hh:457-466); a V-cycle of
+// a mixed-precision solver is one refinement pass.
 template <int B> void one_iteration(tg<B> *g, int type, double omega, int cd, int cu, int hb) {
     const glevel<B> &T = g->lv[0];
+    if (uses_mixed(g, type)) {
+        mixed_pass(g, cd, cu, hb, type == STZG_TGMG_SYM_VCYCLE);
+        return;
+    }
     switch (type) {
         case STZG_TGMG_JACOBI:
             k_tg_jacobi<B><<<grid_of(T.m, T.n, kBlk), kBlk, 0, g->st>>>(T);
@@ -868,10 +962,10 @@ template <int B> void one_iteration(tg<B> *g, int type, double omega, int cd, in
         case STZG_TGMG_SOR: sweep(g, T, false, omega); break;
         case STZG_TGMG_FMG:
             fmg_pre(g, cd, cu, hb, false);
-            v_cycle(g, cd, cu, hb, false);
+            v_cycle(g, g->v64(), cd, cu, hb, false);
             break;
-        case STZG_TGMG_VCYCLE: v_cycle(g, cd, cu, hb, false); break;
-        default: v_cycle(g, cd, cu, hb, true); break;
+        case STZG_TGMG_VCYCLE: v_cycle(g, g->v64(), cd, cu, hb, false); break;
+        default: v_cycle(g, g->v64(), cd, cu, hb, true); break;
     }
 }
 
@@ -883,7 +977,7 @@ template <int B> void drop_graph(tg<B> *g) {
 
 template <int B> int run_iterations(tg<B> *g, int type, int count, double omega, int cd, int cu, int hb) {
     if (count <= 0) return STZG_OK;
-    const int key[5] = {type, cd, cu, hb, 1};
+    const int key[5] = {type, cd, cu, hb, uses_mixed(g, type) ? 2 : 1};
     if (!g->gexec || std::memcmp(key, g->gkey, sizeof(key)) != 0 || g->gomega != omega) {
         drop_graph(g);
         const long k0 = g->kernels;
@@ -920,6 +1014,21 @@ template <int B> int l2_error(tg<B> *g, double *err) {
     STZG_CUDA(cudaStreamSynchronize(g->st));
     *err = g->hsum[0] / ((double)T.m * T.n);
     return STZG_OK;
+}
+
+// l2_error of the z the last resid_split saw, from its partials.
+template <int B> int l2_partials(tg<B> *g, double *err) {
+    const glevel<B> &T = g->lv[0];
+    k_tg_sum<<<1, 256, 0, g->st>>>(g->partials, kRedBlocks, g->dsum);
+    launch_note(g);
+    STZG_CUDA(cudaMemcpyAsync(g->hsum, g->dsum, sizeof(double), cudaMemcpyDeviceToHost, g->st));
+    STZG_CUDA(cudaStreamSynchronize(g->st));
+    *err = g->hsum[0] / ((double)T.m * T.n);
+    return STZG_OK;
+}
+
+template <int B> int check_l2(tg<B> *g, int type, double *err) {
+    return uses_mixed(g, type) ? l2_partials(g, err) : l2_error(g, err);
 }
 
 bool valid_type(int t) { return t >= STZG_TGMG_JACOBI && t <= STZG_TGMG_SYM_VCYCLE; }
@@ -974,6 +1083,47 @@ template <int B> int top_level(int m, int n, const double *table, int ntable, co
 
 // Galerkin hierarchy below the top and its upload (tables grow as needed;
 // sizes and z/b/r stay).  Also the dense coarsest inverse.
+// FP32 copies of every level's stencil table and of the coarsest inverse, for
+// the correction cycles of a mixed-precision solver (the FP32 levels share
+// the FP64 levels' class maps).  *moved is set where a buffer was
+// reallocated.  The host copies stay in the handle.
+template <int B> int upload_f32(tg<B> *g, bool *moved) {
+    g->host32.resize(g->nl);
+    for (int l = 0; l < g->nl; l++) {
+        const host_level<B> &H = g->host[l];
+        std::vector<gst<B, float>> &t = g->host32[l];
+        t.assign(H.table.size(), gst<B, float>{});
+        for (size_t c = 0; c < t.size(); c++) {
+            for (int k = 0; k < 10; k++)
+                for (int q = 0; q < B * B; q++) t[c].e[k].c[q] = (float)H.table[c].e[k].c[q];
+            t[c].nz = H.table[c].nz;
+        }
+        glevel<B, float> &F = g->lf[l];
+        if (t.size() > g->stf_cap[l]) {
+            void *p;
+            STZG_CHECK(g_alloc(g, &p, t.size() * sizeof(gst<B, float>)));
+            F.st = (const gst<B, float> *)p;
+            g->stf_cap[l] = t.size();
+            *moved = true;
+        }
+        STZG_CUDA(cudaMemcpyAsync((void *)F.st, t.data(), t.size() * sizeof(gst<B, float>), cudaMemcpyHostToDevice,
+                                  g->st));
+    }
+    if (!g->inv_host.empty()) {
+        std::vector<float> &f = g->inv_host32;
+        f.assign(g->inv_host.begin(), g->inv_host.end());
+        if (f.size() > g->inv_f_cap) {
+            void *p;
+            STZG_CHECK(g_alloc(g, &p, f.size() * sizeof(float)));
+            g->inv_f = (float *)p;
+            g->inv_f_cap = f.size();
+            *moved = true;
+        }
+        STZG_CUDA(cudaMemcpyAsync(g->inv_f, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, g->st));
+    }
+    return STZG_OK;
+}
+
 // Galerkin hierarchy below the top and its upload.  A level's class map goes
 // up only when it changed (the top's when the caller says so), so a new
 // operator on the same stencil pattern (the sheared-coordinates step: the
@@ -1012,8 +1162,10 @@ template <int B> int build_hierarchy(tg<B> *g, bool top_cls_kept = false) {
     const double *inv_was = g->inv;
     g->inv = nullptr;
     g->inv_n = 0;
+    g->inv_host.clear();
     if (g->nl > 1 && (long)B * Bt.m * Bt.n <= kBottomDirect) {
         std::vector<double> inv = dense_inverse(Bt, g->xp, g->yp);
+        g->inv_host = inv;
         if (!inv.empty()) {
             if (inv.size() > g->inv_cap) {
                 void *p;
@@ -1027,8 +1179,49 @@ template <int B> int build_hierarchy(tg<B> *g, bool top_cls_kept = false) {
                                       g->st));
         }
     }
+    if (g->have32) STZG_CHECK(upload_f32(g, &moved));
     if (moved || g->inv != inv_was) drop_graph(g);
     STZG_CUDA(cudaStreamSynchronize(g->st));  // the host vectors are uploaded before they go
+    return STZG_OK;
+}
+
+// Mixed precision on (V-cycle solves as refinement passes) or off.  The FP32
+// levels are made on first use: z, b, r per level and the tables.
+template <int B> int tg_set_precision(tg<B> *g, int precision) {
+    if (precision == 0) {
+        g->mixed = false;
+        return STZG_OK;
+    }
+    if (!g->have32) {
+        for (int l = 0; l < g->nl; l++) {
+            const glevel<B> &L = g->lv[l];
+            glevel<B, float> &F = g->lf[l];
+            F.m = L.m;
+            F.n = L.n;
+            F.xp = L.xp;
+            F.yp = L.yp;
+            F.cx_n = L.cx_n;
+            F.cy_n = L.cy_n;
+            F.cls = L.cls;
+            const size_t bytes = sizeof(bv<B, float>) * (size_t)L.m * L.n;
+            void *p;
+            STZG_CHECK(g_alloc(g, &p, bytes));
+            F.z = (bv<B, float> *)p;
+            STZG_CHECK(g_alloc(g, &p, bytes));
+            F.b = (bv<B, float> *)p;
+            STZG_CHECK(g_alloc(g, &p, bytes));
+            F.r = (bv<B, float> *)p;
+        }
+        if (g->tail_start < g->nl &&
+            cudaFuncSetAttribute(k_tg_tail<B, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
+                cudaSuccess)
+            return fail(STZG_ECUDA, "tail kernel attribute");
+        bool moved = false;
+        STZG_CHECK(upload_f32(g, &moved));
+        STZG_CUDA(cudaStreamSynchronize(g->st));
+        g->have32 = true;
+    }
+    g->mixed = true;
     return STZG_OK;
 }
 
@@ -1113,7 +1306,7 @@ int tg_create(int m, int n, int xp, int yp, const double *table, int ntable, con
             t = l;
         }
         if (t <= g->nl - 2) {
-            if (cudaFuncSetAttribute(k_tg_tail<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
+            if (cudaFuncSetAttribute(k_tg_tail<B, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
                 cudaSuccess)
                 return bail(fail(STZG_ECUDA, "tail kernel attribute"));
             g->tail_start = t;
@@ -1174,10 +1367,11 @@ int tg_solve(tg<B> *g, int type, stzg_tgmg_predict *tp, double omega, int cd, in
              double *l2) {
     timed<B> t(g);
     // tgmg::solve(type, tgmg_predict&, ...), tgmg.in.cc:266-301
+    if (uses_mixed(g, type)) resid_split(g);
     int nit = tp->lim / tp->mult;
     STZG_CHECK(run_iterations(g, type, nit, omega, cd, cu, hb));
     double acc;
-    STZG_CHECK(l2_error(g, &acc));
+    STZG_CHECK(check_l2(g, type, &acc));
     if (acc < g->acc) {
         if (tp->lim > 0) tp->lim -= 1 + tp->lim / tp->decay;
     } else {
@@ -1191,7 +1385,7 @@ int tg_solve(tg<B> *g, int type, stzg_tgmg_predict *tp, double omega, int cd, in
             }
             nit += k;
             STZG_CHECK(run_iterations(g, type, k, omega, cd, cu, hb));
-            STZG_CHECK(l2_error(g, &acc));
+            STZG_CHECK(check_l2(g, type, &acc));
         } while (acc >= g->acc && !std::isnan(acc));
     }
     tp->solves++;
@@ -1209,6 +1403,7 @@ int tg_solve_fixed(tg<B> *g, int type, int per_loop, int max_loops, double omega
                    int *iters, double *l2) {
     timed<B> t(g);
     // tgmg::solve(type, per_loop, max_loops, ...), tgmg.in.cc:182-197
+    if (uses_mixed(g, type)) resid_split(g);
     double acc = 0;
     int nloop = 0;
     do {
@@ -1219,7 +1414,7 @@ int tg_solve_fixed(tg<B> *g, int type, int per_loop, int max_loops, double omega
             return fail(STZG_ENOTCONV, "tgmg did not converge");
         }
         STZG_CHECK(run_iterations(g, type, per_loop, omega, cd, cu, hb));
-        STZG_CHECK(l2_error(g, &acc));
+        STZG_CHECK(check_l2(g, type, &acc));
     } while (acc > g->acc && !std::isnan(acc));
     t.done();
     if (iters) *iters = nloop * per_loop;
@@ -1230,6 +1425,7 @@ int tg_solve_fixed(tg<B> *g, int type, int per_loop, int max_loops, double omega
 
 template <int B> int tg_iterate(tg<B> *g, int type, int count, double omega, int cd, int cu, int hb) {
     timed<B> t(g);
+    if (uses_mixed(g, type) && count > 0) resid_split(g);
     STZG_CHECK(run_iterations(g, type, count, omega, cd, cu, hb));
     t.done();
     STZG_CUDA(cudaGetLastError());
@@ -1342,6 +1538,11 @@ int stzg_tgmg_destroy(stzg_tgmg *g) {
 int stzg_tgmg_set_operator(stzg_tgmg *g, const double *table, int ntable, const int *cls) {
     if (!table || ntable < 1) return fail(STZG_EINVAL, "bad operator");
     return dispatch(g, [&](auto *s) { return tg_set_operator(s, table, ntable, cls); });
+}
+
+int stzg_tgmg_set_precision(stzg_tgmg *g, int precision) {
+    if (precision != 0 && precision != 1) return fail(STZG_EINVAL, "precision must be 0 (FP64) or 1 (mixed)");
+    return dispatch(g, [&](auto *s) { return tg_set_precision(s, precision); });
 }
 
 int stzg_tgmg_set_b(stzg_tgmg *g, const double *b) {

@@ -18,6 +18,7 @@ from . import _lib
 # Every symbol include/stzg_tgmg.h declares.
 EXPORTS = [
     "stzg_tgmg_predict_init", "stzg_tgmg_create", "stzg_tgmg_create_block", "stzg_tgmg_set_operator",
+    "stzg_tgmg_set_precision",
     "stzg_tgmg_destroy", "stzg_tgmg_set_b", "stzg_tgmg_get_b",
     "stzg_tgmg_set_z", "stzg_tgmg_get_z", "stzg_tgmg_device_arrays", "stzg_tgmg_clear_z", "stzg_tgmg_solve", "stzg_tgmg_solve_fixed",
     "stzg_tgmg_iterate", "stzg_tgmg_l2_error", "stzg_tgmg_levels", "stzg_tgmg_stencil", "stzg_tgmg_last_timing",
@@ -61,6 +62,7 @@ def load():
         "stzg_tgmg_create": (I, [I, I, I, I, _P, I, _IP, D, I, ctypes.POINTER(V)]),
         "stzg_tgmg_create_block": (I, [I, I, I, I, I, _P, I, _IP, D, I, ctypes.POINTER(V)]),
         "stzg_tgmg_set_operator": (I, [V, _P, I, _IP]),
+        "stzg_tgmg_set_precision": (I, [V, I]),
         "stzg_tgmg_destroy": (I, [V]),
         "stzg_tgmg_set_b": (I, [V, _P]),
         "stzg_tgmg_get_b": (I, [V, _P]),
@@ -166,6 +168,11 @@ class Tgmg:
             q.cls = np.ascontiguousarray(np.asarray(cls, dtype=np.int32).reshape(q.n, q.m))
         _lib.check(self.lib.stzg_tgmg_set_operator(self.h, _dp(q.table), q.table.shape[0],
                                                    q.cls.ctypes.data_as(_IP)))
+
+    def set_precision(self, mixed):
+        """mixed: V-cycle solves and iterations run as refinement passes (an
+        FP32 V-cycle on the FP64 residual, the correction added in FP64)."""
+        _lib.check(self.lib.stzg_tgmg_set_precision(self.h, 1 if mixed else 0))
 
     def close(self):
         if getattr(self, "h", None):

@@ -52,12 +52,18 @@ def ct_errors(ref, got, P):
     return out
 
 
+@pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("name", golden_names("ct"))
-def test_ct_steps_match_reference(name):
+def test_ct_steps_match_reference(name, mixed):
+    """Also with the projection solved in mixed precision (FP32 V-cycles
+    inside FP64 refinement, the same threshold on the FP64 residual), under
+    the same gates."""
     from stz_gb300.ct_sim import CtSim
     meta, arr = _load(name)
     P = _params(meta)
     sim = CtSim(P)
+    if mixed:
+        sim.set_precision(True)
     sim.time = meta["time0"]
     for k in FIELDS:
         sim.set(k, arr["init_" + k])
@@ -289,4 +295,33 @@ def test_ct_batch_matches_single_handles():
             assert np.array_equal(fa[k], fb[k]), k
         assert a.time == b.time
     for s in solo + batch:
+        s.close()
+
+
+@pytest.mark.parametrize("m,n,yp", [(96, 48, False), (128, 64, True)])
+def test_ct_mixed_matches_fp64(m, n, yp):
+    """The projection in mixed precision against FP64 over 25 steps from the
+    driver program's set-up (walls; y periodic at the driver's strain rate):
+    both stop at the reference's threshold on the FP64 residual, so the
+    fields agree to the gates of the reference comparison, and a refinement
+    pass contracts like an FP64 V-cycle (as many passes as V-cycles, give or
+    take a few)."""
+    from stz_gb300.ct_sim import CtSim, transform_shear
+    P = transform_shear(m, n, y_prd=yp, lamb=1e-3 if yp else None)
+    sims = []
+    for mixed in (False, True):
+        sim = CtSim(P)
+        sim.init_fields(0, 580.0, 220.0)
+        if mixed:
+            sim.set_precision(True)
+        # the driver program's dt: tf/600 of its duration
+        sim.step_forward_quasistatic((0.5 / 1e-3 if yp else 3e6 / 2e4) / 600, 25)
+        sims.append(sim)
+    a, b = sims
+    err = ct_errors(a.fields(), b.fields(), P)
+    vel = err.pop("velocity")
+    assert vel < 1e-5, (vel, err)
+    assert max(err.values()) < 1e-7, err
+    assert abs(b.vcycles - a.vcycles) <= max(3, a.vcycles // 5), (a.vcycles, b.vcycles)
+    for s in sims:
         s.close()

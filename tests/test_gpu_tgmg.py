@@ -39,15 +39,19 @@ def test_hierarchy_and_stencils_match_reference(golden_tgmg):
     g.close()
 
 
-def test_vcycle_solve_matches_reference(golden_tgmg):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_vcycle_solve_matches_reference(golden_tgmg, mixed):
     """solve_v_cycle(tgmg_predict&) from z = 0 on the reference's source:
     converged under acc, and the solution agrees with the reference's and with
-    the exact discrete solution."""
+    the exact discrete solution; in mixed precision (FP32 V-cycles inside FP64
+    refinement) with as many passes as the reference's V-cycles."""
     name, meta, arr = golden_tgmg
     tg = _tg()
     q = _pfd(meta)
     q.b[...] = arr["b"]
     g = tg.Tgmg(q)
+    if mixed:
+        g.set_precision(True)
     tp = tg.Predict()
     assert g.solve_v_cycle(tp)
     assert g.l2_error() < q.acc
@@ -62,12 +66,15 @@ def test_vcycle_solve_matches_reference(golden_tgmg):
     g.close()
 
 
-def test_vcycle_contraction_from_zero(golden_tgmg):
+@pytest.mark.parametrize("mixed", [False, True])
+def test_vcycle_contraction_from_zero(golden_tgmg, mixed):
     name, meta, arr = golden_tgmg
     tg = _tg()
     q = _pfd(meta)
     q.b[...] = arr["b"]
     g = tg.Tgmg(q)
+    if mixed:
+        g.set_precision(True)
     hist = []
     for _ in range(6):
         g.v_cycle()
@@ -284,10 +291,13 @@ def test_block_operator_update_class_map():
     g.close()
 
 
+@pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("m,n,xp,yp", [(32, 17, 1, 0), (40, 24, 1, 1), (33, 27, 1, 1), (24, 19, 0, 0)])
-def test_block_operators(m, n, xp, yp):
+def test_block_operators(m, n, xp, yp, mixed):
     """tgmg<S,vec,mat>: Galerkin blocks and the converged solution of
-    qs_multi-type 2x2-block operators, periodic or walled in y."""
+    qs_multi-type 2x2-block operators, periodic or walled in y, in FP64 and
+    in mixed precision; a solver switched back to FP64 solves bit for bit
+    like one that never left it."""
     tg = _tg()
     table, cls = _block_operator(m, n, xp, yp, seed=m)
     ops, sizes = O.hierarchy(m, n, xp, yp, table, cls, 2)
@@ -306,6 +316,8 @@ def test_block_operators(m, n, xp, yp):
         mine = g.stencil(l)
         ref = O.stencils(ops[l], sizes[l][0], sizes[l][1], xp, yp, 2)
         assert np.abs(mine[:, :, :9] - ref[:, :, :9]).max() <= 1e-13 * np.abs(ref[:, :, :9]).max(), l
+    if mixed:
+        g.set_precision(True)
     tp = tg.Predict()
     assert g.solve_v_cycle(tp)
     assert g.l2_error() < q.acc
@@ -317,6 +329,16 @@ def test_block_operators(m, n, xp, yp):
         zx, got = O.solve(ops[0], b), q.z
     assert np.abs(got - zx).max() <= 1e-10 * np.abs(zx).max()
     assert g.l2_error() == pytest.approx(O.l2_error(ops[0], q.z, b, 2), rel=1e-3, abs=1e-28)
+    if mixed:
+        g.set_precision(False)
+        q.z[...] = 0
+        assert g.solve_v_cycle(tg.Predict())
+        q2 = tg.Problem(m, n, table, cls, 1e-26, x_prd=xp, y_prd=yp, block=2)
+        q2.b[...] = b
+        g2 = tg.Tgmg(q2)
+        assert g2.solve_v_cycle(tg.Predict())
+        assert np.array_equal(q.z, q2.z)
+        g2.close()
     g.close()
 
 
