@@ -79,6 +79,9 @@ template <class S> class tgmg {
 
     // tgmg::setup (tgmg.hh:331-335): the hierarchy is built by the constructor.
     void setup() {}
+    // Not in the reference: V-cycle solves as FP32 V-cycles inside FP64
+    // refinement (stzg_tgmg_set_precision), to the same acc.
+    void set_mixed_precision(bool on) { tgmg_check_or_exit(stzg_tgmg_set_precision(h_, on ? 1 : 0)); }
     void clear_z() {
         for (int k = 0; k < mn; k++) z_[k] = 0;
     }

@@ -98,8 +98,27 @@ constexpr int kRedBlocks = 4 * 152;
 constexpr int kRedThreads = 256;
 constexpr size_t kTailSmem = 200 * 1024; // shared memory of the single-block tail
 // Largest level the tail takes: one SM's FP64 pipe is slow (a 65 x 65
-// level alone kept the tail at ~120 us a cycle), so the tail starts at 33 x 33.
+// level alone kept the tail at ~120 us a cycle), so the tail starts at 33 x 33;
+// in FP32 one SM sweeps a 64 x 32 level of 2x2 blocks in well under the time
+// of the 11 launches the level otherwise costs.
 constexpr long kTailPoints = 1200;
+constexpr long kTailPointsF = 2048;
+
+// First level of the single-block tail for values of vbytes bytes per point:
+// the small levels that fit in its shared memory together (z, b, r), if
+// they are at least two (the coarsest alone is the bottom); 1 << 30 if none.
+inline int tail_start_for(const int *m, const int *n, int nl, size_t vbytes, long max_points) {
+    size_t bytes = 0;
+    int t = nl;
+    for (int l = nl - 1; l >= 1; l--) {
+        const long pts = (long)m[l] * n[l];
+        const size_t b = 3 * vbytes * (size_t)pts;
+        if (pts > max_points || bytes + b > kTailSmem) break;
+        bytes += b;
+        t = l;
+    }
+    return t <= nl - 2 ? t : 1 << 30;
+}
 
 // Neighbour index on a line of m points, or -1 outside a non-periodic line.
 __host__ __device__ inline int nbr(int i, int d, int m, int prd) {
@@ -303,10 +322,10 @@ __device__ __forceinline__ double block_reduce(double v, double *sh) {
 
 template <int B> __global__ void k_tg_sqnorm(glevel<B> L, double *partials) {
     __shared__ double sh[32];
-    const long mn = (long)L.m * L.n;
+    const int mn = L.m * L.n;  // at most 2^30 points (checked at creation): 32-bit indices
     double acc = 0;
-    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += (long)gridDim.x * blockDim.x) {
-        const int j = (int)(k / L.m), i = (int)(k - (long)j * L.m);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += gridDim.x * blockDim.x) {
+        const int j = k / L.m, i = k - j * L.m;
         const bv<B> r = residual_at(L, L.st[L.cls[k]], (size_t)k, i, j);
 #pragma unroll
         for (int c = 0; c < B; c++) acc += r.c[c] * r.c[c];
@@ -329,10 +348,10 @@ __global__ void k_tg_sum(const double *partials, int np, double *out) {
 // (the l2_error of a z is the same number either way).
 template <int B> __global__ void k_tg_resid_split(glevel<B> L, glevel<B, float> F, double *partials) {
     __shared__ double sh[32];
-    const long mn = (long)L.m * L.n;
+    const int mn = L.m * L.n;  // at most 2^30 points (checked at creation): 32-bit indices
     double acc = 0;
-    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += (long)gridDim.x * blockDim.x) {
-        const int j = (int)(k / L.m), i = (int)(k - (long)j * L.m);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += gridDim.x * blockDim.x) {
+        const int j = k / L.m, i = k - j * L.m;
         const bv<B> r = residual_at(L, L.st[L.cls[k]], (size_t)k, i, j);
         bv<B, float> rf, zf;
 #pragma unroll
@@ -350,8 +369,8 @@ template <int B> __global__ void k_tg_resid_split(glevel<B> L, glevel<B, float> 
 
 // z += e: a correction cycle's FP32 result added to the FP64 solution.
 template <int B> __global__ void k_tg_correct(glevel<B> L, const bv<B, float> *__restrict__ e) {
-    const long mn = (long)L.m * L.n;
-    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += (long)gridDim.x * blockDim.x) {
+    const int mn = L.m * L.n;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < mn; k += gridDim.x * blockDim.x) {
         const bv<B, float> d = e[k];
         bv<B> z = L.z[k];
 #pragma unroll
@@ -726,6 +745,7 @@ template <int B, typename T> struct hview {
     const glevel<B, T> *lv;
     const T *inv;
     int inv_n;
+    int tail_start;  // first level handled by k_tg_tail (none if > nl-1)
 };
 
 template <int B> struct tg {
@@ -755,8 +775,9 @@ template <int B> struct tg {
     size_t stf_cap[kMaxLevels] = {0};
     float *inv_f = nullptr;
     size_t inv_f_cap = 0;
-    hview<B, double> v64() const { return hview<B, double>{lv, inv, inv_n}; }
-    hview<B, float> v32() const { return hview<B, float>{lf, inv ? inv_f : nullptr, inv_n}; }
+    int tail_start_f = 1 << 30;  // the FP32 levels' tail start
+    hview<B, double> v64() const { return hview<B, double>{lv, inv, inv_n, tail_start}; }
+    hview<B, float> v32() const { return hview<B, float>{lf, inv ? inv_f : nullptr, inv_n, tail_start_f}; }
     // graph of one iteration of the last (type, omega, cycles) used
     cudaGraphExec_t gexec = nullptr;
     int gkey[5] = {-1, 0, 0, 0, 0};
@@ -866,7 +887,7 @@ template <int B, typename T> void vc(tg<B> *g, const hview<B, T> &h, int i, int 
         bottom(g, h, hb, sym);
         return;
     }
-    if (i >= g->tail_start) {
+    if (i >= h.tail_start) {
         tail(g, h, i, cd, cu, hb, sym);
         return;
     }
@@ -1212,7 +1233,7 @@ template <int B> int tg_set_precision(tg<B> *g, int precision) {
             STZG_CHECK(g_alloc(g, &p, bytes));
             F.r = (bv<B, float> *)p;
         }
-        if (g->tail_start < g->nl &&
+        if (g->tail_start_f < g->nl &&
             cudaFuncSetAttribute(k_tg_tail<B, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
                 cudaSuccess)
             return fail(STZG_ECUDA, "tail kernel attribute");
@@ -1296,21 +1317,17 @@ int tg_create(int m, int n, int xp, int yp, const double *table, int ntable, con
     // single-block tail: the small levels that fit in its shared memory
     // together, if they are at least two (the coarsest alone is the bottom)
     {
-        size_t bytes = 0;
-        int t = g->nl;
-        for (int l = g->nl - 1; l >= 1; l--) {
-            const long pts = (long)g->lv[l].m * g->lv[l].n;
-            const size_t b = 3 * sizeof(bv<B>) * (size_t)pts;
-            if (pts > kTailPoints || bytes + b > kTailSmem) break;
-            bytes += b;
-            t = l;
+        int ms[kMaxLevels], ns[kMaxLevels];
+        for (int l = 0; l < g->nl; l++) {
+            ms[l] = g->lv[l].m;
+            ns[l] = g->lv[l].n;
         }
-        if (t <= g->nl - 2) {
-            if (cudaFuncSetAttribute(k_tg_tail<B, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
+        g->tail_start = tail_start_for(ms, ns, g->nl, sizeof(bv<B>), kTailPoints);
+        g->tail_start_f = tail_start_for(ms, ns, g->nl, sizeof(bv<B, float>), kTailPointsF);
+        if (g->tail_start < g->nl &&
+            cudaFuncSetAttribute(k_tg_tail<B, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem) !=
                 cudaSuccess)
-                return bail(fail(STZG_ECUDA, "tail kernel attribute"));
-            g->tail_start = t;
-        }
+            return bail(fail(STZG_ECUDA, "tail kernel attribute"));
     }
     {
         void *p;
@@ -1501,6 +1518,7 @@ int stzg_tgmg_create_block(int m, int n, int x_prd, int y_prd, int block, const 
     *out = nullptr;
     if (block != 1 && block != 2) return fail(STZG_EINVAL, "block must be 1 or 2");
     if (m < 1 || n < 1 || !table || ntable < 1 || !cls) return fail(STZG_EINVAL, "bad grid or operator");
+    if ((long)m * n > (1L << 30)) return fail(STZG_EINVAL, "more than 2^30 grid points");
     if ((x_prd && m < 3) || (y_prd && n < 3)) return fail(STZG_EINVAL, "a periodic direction needs >= 3 points");
     if (!(acc >= 0)) return fail(STZG_EINVAL, "acc must be >= 0");
     const size_t mn = (size_t)m * n;

@@ -8,7 +8,11 @@ solve (the wall time includes the copies of b in and z out that the mirror of
 the reference's in-place arrays makes), V-cycles per solve, device time per
 V-cycle and its algorithmic HBM bandwidth.
 
-    python -m stz_gb300.run_pfd [--size 2049] [--trials 500]
+    python -m stz_gb300.run_pfd [--size 2049] [--trials 500] [--precision fp64|mixed]
+
+With --precision mixed each "V-cycle" is a refinement pass (an FP32 V-cycle
+on the FP64 residual, the correction added in FP64), and the bandwidth
+figure is left out (the pass moves different bytes).
 """
 import argparse
 import json
@@ -32,10 +36,13 @@ def main(argv=None):
     ap.add_argument("--size", type=int, default=2049)
     ap.add_argument("--trials", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     args = ap.parse_args(argv)
     m = n = args.size
     q = tgmg.PoissonFD(m, n, -8.0, 8.0, -8.0, 8.0)
     g = tgmg.Tgmg(q)
+    mixed = args.precision == "mixed"
+    g.set_precision(mixed)
     tp = tgmg.Predict()
     h = 2.0 * math.pi / args.trials
     for k in range(args.warmup):
@@ -60,9 +67,9 @@ def main(argv=None):
             "device_ms_per_solve": 1e3 * dev / args.trials,
             "vcycles_per_solve": tp.vcount / tp.solves, "extra_vcycles_per_solve": tp.extra_iters,
             "device_ms_per_vcycle": 1e3 * per_v,
-            "vcycle_algorithmic_GBs": VCYCLE_BYTES_PER_POINT * m * n / per_v / 1e9,
+            "vcycle_algorithmic_GBs": None if mixed else VCYCLE_BYTES_PER_POINT * m * n / per_v / 1e9,
             "kernels_per_solve": kernels / args.trials, "levels": g.levels(),
-            "final_l2_error": g.l2_error(), "acc": q.acc}
+            "final_l2_error": g.l2_error(), "acc": q.acc, "precision": args.precision}
     print(json.dumps(line))
     g.close()
     return line
