@@ -54,6 +54,12 @@ int stzg_ct_set_time(stzg_ct *s, double time);
  * stzg.h, FP32 V-cycles inside FP64 refinement (stzg_tgmg_set_precision),
  * converged to the same threshold on the FP64 residual. */
 int stzg_ct_set_precision(stzg_ct *s, int precision);
+/* How many V-cycles the projection's solve runs: 0 (the default) the
+ * reference's tgmg_predict counts (qs_multi::solve, tgmg.in.cc:266-301),
+ * which over-solve while the prediction settles; 1 V-cycles until the
+ * residual meets the same threshold, tested after each
+ * (stzg_tgmg_solve_checked), then the extra one. */
+int stzg_ct_set_solve_policy(stzg_ct *s, int policy);
 int stzg_ct_get_time(stzg_ct *s, double *time);
 /* nsteps of shear_sim::step_forward_quasistatic(dt) (shear_sim.cc:352-360):
  * advection_step (ENO2 advection, STZ plasticity, chi diffusion, updates,

@@ -95,6 +95,15 @@ int stzg_tgmg_solve(stzg_tgmg *g, int type, stzg_tgmg_predict *tp, double omega,
  * l2_error <= acc. */
 int stzg_tgmg_solve_fixed(stzg_tgmg *g, int type, int per_loop, int max_loops, double omega, int cyc_down,
                           int cyc_up, int hcyc_bottom, int *iters, double *l2);
+/* Not in the reference: iterations of one type until l2_error < acc, the
+ * residual tested before the first (a warm start may meet it already) and
+ * after each, at most max_iters, then extra_iters more; iters receives the
+ * count before the extra ones.  STZG_ENOTCONV past max_iters, STZG_ENAN on a
+ * NaN residual.  The predictor of stzg_tgmg_solve runs the counts it
+ * predicts whatever the need (tgmg.in.cc:266-301); this runs only what the
+ * residual asks for, at one residual check per iteration. */
+int stzg_tgmg_solve_checked(stzg_tgmg *g, int type, int max_iters, int extra_iters, double omega, int cyc_down,
+                            int cyc_up, int hcyc_bottom, int *iters, double *l2);
 /* count iterations of one type without convergence checks (tgmg::iters,
  * tgmg.hh:457-466): v_cycle / fmg_pre+v_cycle / jacobi / gauss_seidel / sor. */
 int stzg_tgmg_iterate(stzg_tgmg *g, int type, int count, double omega, int cyc_down, int cyc_up, int hcyc_bottom);

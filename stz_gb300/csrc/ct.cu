@@ -510,6 +510,7 @@ struct stzg_ct {
     std::vector<void *> owned;
     stzg_tgmg *mg = nullptr;
     stzg_tgmg_predict tp;
+    int checked = 0;  // solve policy: 0 the reference's predictor, 1 residual checks
     double2 *mg_b = nullptr, *mg_z = nullptr;
     std::vector<double> table;
     std::vector<int> cls;
@@ -620,7 +621,11 @@ int projection_step(stzg_ct *s, double dt, long *vcycles) {
     note_launch();
     STZG_CUDA(cudaStreamSynchronize(s->st));
     int it = 0;
-    const int st = stzg_tgmg_solve(s->mg, STZG_TGMG_VCYCLE, &s->tp, 1.0, 1, 1, 10, &it, nullptr);
+    // checked: V-cycles until the residual meets acc (at most the predictor's
+    // own limit, max_thresh / mult), then the extra one
+    const int st = s->checked ? stzg_tgmg_solve_checked(s->mg, STZG_TGMG_VCYCLE, s->tp.max_thresh / s->tp.mult,
+                                                        s->tp.extra_iters, 1.0, 1, 1, 10, &it, nullptr)
+                              : stzg_tgmg_solve(s->mg, STZG_TGMG_VCYCLE, &s->tp, 1.0, 1, 1, 10, &it, nullptr);
     if (st != STZG_OK) return st;
     if (vcycles) *vcycles += it;
     k_ct_project<<<g2(s->c.m, s->c.n), kB2, 0, s->st>>>(s->c, s->F, s->cur, s->mg_z, dt, lt);
@@ -1157,6 +1162,13 @@ int stzg_ct_get_field(stzg_ct *s, int field, double *host) {
 int stzg_ct_set_time(stzg_ct *s, double time) {
     if (!s) return fail(STZG_EINVAL, "null handle");
     s->time = time;
+    return STZG_OK;
+}
+
+int stzg_ct_set_solve_policy(stzg_ct *s, int policy) {
+    if (!s) return fail(STZG_EINVAL, "null handle");
+    if (policy != 0 && policy != 1) return fail(STZG_EINVAL, "policy must be 0 (predictor) or 1 (checked)");
+    s->checked = policy;
     return STZG_OK;
 }
 

@@ -14,7 +14,7 @@ from . import _lib
 EXPORTS = ["stzg_ct_create", "stzg_ct_destroy", "stzg_ct_init_fields", "stzg_ct_chi_bicubic",
            "stzg_ct_compute_strain", "stzg_ct_output_field", "stzg_ct_write_frame", "stzg_ct_solve_quasistatic",
            "stzg_ct_solve", "stzg_ct_l2_comparison_transform", "stzg_ct_set_field", "stzg_ct_get_field",
-           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_set_precision", "stzg_ct_step_qs", "stzg_ct_batch_step_qs", "stzg_ct_step_direct", "stzg_ct_tracers_init",
+           "stzg_ct_set_time", "stzg_ct_get_time", "stzg_ct_set_precision", "stzg_ct_set_solve_policy", "stzg_ct_step_qs", "stzg_ct_batch_step_qs", "stzg_ct_step_direct", "stzg_ct_tracers_init",
            "stzg_ct_tracers_update", "stzg_ct_tracers_get"]
 FIELDS = ("u", "v", "p", "q", "s", "tau", "chi", "X", "Y", "ddev")
 BOLTZMANN = 1.3806503e-23
@@ -83,6 +83,7 @@ def load():
         "stzg_ct_get_field": (I, [V, I, _P]),
         "stzg_ct_set_time": (I, [V, D]),
         "stzg_ct_set_precision": (I, [V, I]),
+        "stzg_ct_set_solve_policy": (I, [V, I]),
         "stzg_ct_get_time": (I, [V, _P]),
         "stzg_ct_step_qs": (I, [V, D, I, ctypes.POINTER(ctypes.c_long), _P]),
         "stzg_ct_batch_step_qs": (I, [ctypes.POINTER(V), I, D, I, I, ctypes.POINTER(ctypes.c_long), _P]),
@@ -192,6 +193,11 @@ class CtSim:
         """mixed: the projection solves with FP32 V-cycles inside FP64
         refinement, to the same threshold on the FP64 residual."""
         _lib.check(self.lib.stzg_ct_set_precision(self.h, 1 if mixed else 0))
+
+    def set_solve_policy(self, checked):
+        """checked: the projection runs V-cycles until its residual meets the
+        threshold (tested after each) instead of the predictor's counts."""
+        _lib.check(self.lib.stzg_ct_set_solve_policy(self.h, 1 if checked else 0))
 
     def step_forward_quasistatic(self, dt, nsteps=1):
         vc, sec = ctypes.c_long(), ctypes.c_double()

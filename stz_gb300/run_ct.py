@@ -5,7 +5,7 @@ scaled to a larger grid; warm-up steps, then timed steps of the driver's
 dt = tf/600.  Prints one JSON line.
 
     python -m stz_gb300.run_ct [--m 2048] [--n 1024] [--steps 20] [--warmup 3] [--walls]
-                               [--precision fp64|mixed] [--direct DT] [--tracers MM NN]
+                               [--precision fp64|mixed] [--checked] [--direct DT] [--tracers MM NN]
 
 --direct DT times the explicit step (shear_sim::step_forward) of dt DT
 instead; --tracers MM NN adds an MM x NN tracer grid after the warm-up and
@@ -30,6 +30,8 @@ def main(argv=None):
     ap.add_argument("--walls", action="store_true")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="the projection's solve: FP64 V-cycles, or FP32 V-cycles inside FP64 refinement")
+    ap.add_argument("--checked", action="store_true",
+                    help="V-cycles until the residual meets the threshold instead of the reference's predicted counts")
     ap.add_argument("--direct", type=float, default=None)
     ap.add_argument("--tracers", type=int, nargs=2, default=None)
     ap.add_argument("--batch", type=int, default=0)
@@ -43,6 +45,7 @@ def main(argv=None):
     sim = CtSim(P)
     sim.init_fields(0, 580.0, 220.0)
     sim.set_precision(args.precision == "mixed")
+    sim.set_solve_policy(args.checked)
     kind = "quasi-static"
     step = sim.step_forward_quasistatic
     if args.direct:
@@ -58,7 +61,8 @@ def main(argv=None):
             "metric": "cell-steps/s", "value": args.m * args.n * args.steps / sim.seconds,
             "ms_per_step": 1e3 * sim.seconds / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
             "vcycles_per_step": sim.vcycles / args.steps if not args.direct else 0, "steps": args.steps,
-            "warmup": args.warmup, "precision": args.precision}
+            "warmup": args.warmup, "precision": args.precision,
+            "solve": "checked" if args.checked else "predictor"}
     if args.tracers:
         t0 = time.perf_counter()
         lost = sim.update_tracers()
@@ -78,6 +82,7 @@ def batch_main(args, P, dt, yp):
             sim = CtSim(P)
             sim.init_fields(0, 560.0 + 40.0 * k / max(args.batch - 1, 1), 220.0)
             sim.set_precision(args.precision == "mixed")
+            sim.set_solve_policy(args.checked)
             sims.append(sim)
         return sims
 

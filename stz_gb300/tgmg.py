@@ -18,7 +18,7 @@ from . import _lib
 # Every symbol include/stzg_tgmg.h declares.
 EXPORTS = [
     "stzg_tgmg_predict_init", "stzg_tgmg_create", "stzg_tgmg_create_block", "stzg_tgmg_set_operator",
-    "stzg_tgmg_set_precision",
+    "stzg_tgmg_set_precision", "stzg_tgmg_solve_checked",
     "stzg_tgmg_destroy", "stzg_tgmg_set_b", "stzg_tgmg_get_b",
     "stzg_tgmg_set_z", "stzg_tgmg_get_z", "stzg_tgmg_device_arrays", "stzg_tgmg_clear_z", "stzg_tgmg_solve", "stzg_tgmg_solve_fixed",
     "stzg_tgmg_iterate", "stzg_tgmg_l2_error", "stzg_tgmg_levels", "stzg_tgmg_stencil", "stzg_tgmg_last_timing",
@@ -63,6 +63,7 @@ def load():
         "stzg_tgmg_create_block": (I, [I, I, I, I, I, _P, I, _IP, D, I, ctypes.POINTER(V)]),
         "stzg_tgmg_set_operator": (I, [V, _P, I, _IP]),
         "stzg_tgmg_set_precision": (I, [V, I]),
+        "stzg_tgmg_solve_checked": (I, [V, I, I, I, D, I, I, I, _IP, _P]),
         "stzg_tgmg_destroy": (I, [V]),
         "stzg_tgmg_set_b": (I, [V, _P]),
         "stzg_tgmg_get_b": (I, [V, _P]),
@@ -217,6 +218,20 @@ class Tgmg:
         self._pull()
         self.iterations, self.residual = it.value, l2.value
         if st == 4:  # not converged: the reference returns false
+            return False
+        _lib.check(st)
+        return True
+
+    def solve_v_cycle_checked(self, max_iters=2048, extra_iters=1, cyc_down=1, cyc_up=1, hcyc_bottom=10):
+        """V-cycles until l2_error < acc, tested before the first and after
+        each, then extra_iters more (not in the reference)."""
+        self._push()
+        it, l2 = ctypes.c_int(), ctypes.c_double()
+        st = self.lib.stzg_tgmg_solve_checked(self.h, VCYCLE, max_iters, extra_iters, 1.0, cyc_down, cyc_up,
+                                              hcyc_bottom, ctypes.byref(it), ctypes.byref(l2))
+        self._pull()
+        self.iterations, self.residual = it.value, l2.value
+        if st == 4:
             return False
         _lib.check(st)
         return True

@@ -67,6 +67,27 @@ def test_vcycle_solve_matches_reference(golden_tgmg, mixed):
 
 
 @pytest.mark.parametrize("mixed", [False, True])
+def test_checked_solve(golden_tgmg, mixed):
+    """stzg_tgmg_solve_checked: from z = 0 it converges with no more V-cycles
+    (passes) than the reference needed plus two and agrees with the
+    reference's solution; from a converged z it runs none but the extra one."""
+    name, meta, arr = golden_tgmg
+    tg = _tg()
+    q = _pfd(meta)
+    q.b[...] = arr["b"]
+    g = tg.Tgmg(q)
+    g.set_precision(mixed)
+    assert g.solve_v_cycle_checked()
+    assert g.iterations <= meta["vcycles"] + 2
+    assert g.residual < q.acc and g.l2_error() < q.acc
+    scale = np.abs(arr["z"]).max()
+    assert np.abs(q.z - arr["z"]).max() <= 1e-9 * scale
+    assert g.solve_v_cycle_checked()
+    assert g.iterations == 0
+    g.close()
+
+
+@pytest.mark.parametrize("mixed", [False, True])
 def test_vcycle_contraction_from_zero(golden_tgmg, mixed):
     name, meta, arr = golden_tgmg
     tg = _tg()
@@ -329,6 +350,14 @@ def test_block_operators(m, n, xp, yp, mixed):
         zx, got = O.solve(ops[0], b), q.z
     assert np.abs(got - zx).max() <= 1e-10 * np.abs(zx).max()
     assert g.l2_error() == pytest.approx(O.l2_error(ops[0], q.z, b, 2), rel=1e-3, abs=1e-28)
+    if mixed and xp and yp:
+        # periodic both ways: singular (constants), so the V-cycles stay FP64
+        q2 = tg.Problem(m, n, table, cls, 1e-26, x_prd=xp, y_prd=yp, block=2)
+        q2.b[...] = b
+        g2 = tg.Tgmg(q2)
+        assert g2.solve_v_cycle(tg.Predict())
+        assert np.array_equal(q.z, q2.z)
+        g2.close()
     if mixed:
         g.set_precision(False)
         q.z[...] = 0
