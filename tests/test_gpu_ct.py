@@ -358,3 +358,16 @@ def test_ct_checked_solve_policy(mixed):
     assert b.vcycles < a.vcycles, (a.vcycles, b.vcycles)
     for s in sims:
         s.close()
+
+
+def test_ct_bad_settings_are_statuses():
+    """Out-of-range precision and solve-policy values, and a null handle, are
+    STZG_EINVAL (1), and the handle still steps."""
+    from stz_gb300.ct_sim import CtSim, transform_shear
+    sim = CtSim(transform_shear(32, 16))
+    assert sim.lib.stzg_ct_set_precision(sim.h, 2) == 1
+    assert sim.lib.stzg_ct_set_solve_policy(sim.h, 2) == 1
+    assert sim.lib.stzg_ct_set_solve_policy(None, 1) == 1
+    sim.init_fields(0, 580.0, 220.0)
+    sim.step_forward_quasistatic(0.5 / 1e-3 / 600, 2)
+    sim.close()

@@ -210,6 +210,18 @@ def test_bad_arguments_are_statuses():
     assert lib.stzg_tgmg_create(2, 2, 0, 0, table.ctypes.data_as(P), 1, cls.ctypes.data_as(IP), 0.0, 0,
                                 ctypes.byref(h)) == 1
     assert not h.value
+    # a valid solver: bad precision, bad checked-solve limits, a kept class
+    # map with another stencil count
+    cls[1] = 0
+    assert lib.stzg_tgmg_create(2, 2, 0, 0, table.ctypes.data_as(P), 1, cls.ctypes.data_as(IP), 0.0, 0,
+                                ctypes.byref(h)) == 0
+    assert lib.stzg_tgmg_set_precision(h, 2) == 1
+    it, l2 = ctypes.c_int(), ctypes.c_double()
+    assert lib.stzg_tgmg_solve_checked(h, 4, -1, 1, ctypes.c_double(1.0), 1, 1, 10, ctypes.byref(it),
+                                       ctypes.byref(l2)) == 1
+    two = np.concatenate([table, table])
+    assert lib.stzg_tgmg_set_operator(h, two.ctypes.data_as(P), 2, None) == 1
+    assert lib.stzg_tgmg_destroy(h) == 0
 
 
 def test_reports_device_time_and_kernels():
