@@ -502,7 +502,6 @@ template <int B> struct host_level {
     bool rows;  // the stencil depends on the row only
     std::vector<int> cls;
     std::vector<int> row_ids;  // rows: the stencil index of each row
-    std::vector<char> used;    // top level: the stencils some point uses
     bool cls_kept = false;     // cls equals the device copy already uploaded
     std::vector<gst<B>> table;
 };
@@ -702,10 +701,14 @@ template <int B> std::vector<double> dense_inverse(const host_level<B> &L, int x
         }
     for (int r = 0; r < N; r++) X[(size_t)r * N + r] = 1;
     // a pivot at rounding level means a singular level (a periodic operator
-    // that annihilates constants): no inverse, the bottom is smoothed
+    // that annihilates constants): no inverse, the bottom is smoothed.  After
+    // six to eight Galerkin products the rounding pivots of such a level
+    // reach 4e-10 of its largest entry (the next pivot is ~0.3 of it), so the
+    // test sits well above them; an inverse built on them would carry
+    // entries ~1e10 times the operator's inverse scale.
     double amax = 0;
     for (double v : A) amax = std::max(amax, std::fabs(v));
-    const double tiny = 1e-12 * amax;
+    const double tiny = 1e-8 * amax;
     for (int c = 0; c < N; c++) {
         int p = c;
         for (int r = c + 1; r < N; r++)
@@ -765,13 +768,6 @@ template <int B> struct tg {
     size_t inv_cap = 0;
     int tail_start = 1 << 30;  // first level handled by k_tg_tail (none if > nl-1)
     double *partials = nullptr, *dsum = nullptr, *hsum = nullptr;
-    // Periodic in x and y with every used stencil's blocks summing to zero:
-    // the constants are the operator's null space.  The FP32 rounding of the
-    // tables leaves that mode nearly instead of exactly singular, and FP32
-    // correction cycles inside FP64 refinement were measured to stagnate or
-    // diverge on such operators at 512x256 and above, so their V-cycles stay
-    // FP64 in mixed mode.
-    bool null_const = false;
     std::vector<double> inv_host;  // the coarsest inverse, for its FP32 copy
     std::vector<std::vector<gst<B, float>>> host32;  // FP32 tables as uploaded
     std::vector<float> inv_host32;
@@ -951,7 +947,7 @@ template <int B> void fmg_pre(tg<B> *g, int cd, int cu, int hb, bool sym) {
 }
 
 template <int B> bool uses_mixed(const tg<B> *g, int type) {
-    return g->mixed && !g->null_const && (type == STZG_TGMG_VCYCLE || type == STZG_TGMG_SYM_VCYCLE);
+    return g->mixed && (type == STZG_TGMG_VCYCLE || type == STZG_TGMG_SYM_VCYCLE);
 }
 
 // Mixed precision: the top level's FP64 residual of the current z into the
@@ -1094,11 +1090,8 @@ template <int B> int fill_top_table(const double *table, int ntable, host_level<
 // Top level from the problem's table and class map.
 template <int B> int top_level(int m, int n, const double *table, int ntable, const int *cls, host_level<B> &top) {
     const size_t mn = (size_t)m * n;
-    top.used.assign(ntable, 0);
-    for (size_t k = 0; k < mn; k++) {
+    for (size_t k = 0; k < mn; k++)
         if (cls[k] < 0 || cls[k] >= ntable) return fail(STZG_EINVAL, "stencil index out of range");
-        top.used[cls[k]] = 1;
-    }
     top.m = m;
     top.n = n;
     top.cls.assign(cls, cls + mn);
@@ -1115,26 +1108,6 @@ template <int B> int top_level(int m, int n, const double *table, int ntable, co
 
 // Galerkin hierarchy below the top and its upload (tables grow as needed;
 // sizes and z/b/r stay).  Also the dense coarsest inverse.
-// Periodic in x and y with each top-level stencil's nine blocks summing to
-// zero (to 1e-12 of its largest entry): the constants are the null space.
-template <int B> bool constants_in_null(const tg<B> *g) {
-    if (!g->xp || !g->yp) return false;
-    const host_level<B> &T = g->host[0];
-    for (size_t c = 0; c < T.table.size(); c++) {
-        if (c < T.used.size() && !T.used[c]) continue;
-        const gst<B> &t = T.table[c];
-        double amax = 0, sum[B * B] = {0};
-        for (int k = 0; k < 9; k++)
-            for (int q = 0; q < B * B; q++) {
-                sum[q] += t.e[k].c[q];
-                amax = std::max(amax, std::fabs(t.e[k].c[q]));
-            }
-        for (int q = 0; q < B * B; q++)
-            if (std::fabs(sum[q]) > 1e-12 * amax) return false;
-    }
-    return true;
-}
-
 // FP32 copies of every level's stencil table and of the coarsest inverse, for
 // the correction cycles of a mixed-precision solver (the FP32 levels share
 // the FP64 levels' class maps).  *moved is set where a buffer was
@@ -1232,9 +1205,6 @@ template <int B> int build_hierarchy(tg<B> *g, bool top_cls_kept = false) {
         }
     }
     if (g->have32) STZG_CHECK(upload_f32(g, &moved));
-    const bool nc = constants_in_null(g);
-    if (nc != g->null_const) moved = true;  // a mixed solver's V-cycle changes precision
-    g->null_const = nc;
     if (moved || g->inv != inv_was) drop_graph(g);
     STZG_CUDA(cudaStreamSynchronize(g->st));  // the host vectors are uploaded before they go
     return STZG_OK;
@@ -1392,12 +1362,9 @@ template <int B> int tg_set_operator(tg<B> *g, const double *table, int ntable, 
         top.n = T.n;
         top.rows = T.rows;
         top.cls.swap(T.cls);
-        top.used.swap(T.used);
-        top.used.resize(ntable, 0);
         const int st = fill_top_table<B>(table, ntable, top);
         if (st != STZG_OK) {
             T.cls.swap(top.cls);
-            T.used.swap(top.used);
             return st;
         }
     } else {

@@ -362,14 +362,6 @@ def test_block_operators(m, n, xp, yp, mixed):
         zx, got = O.solve(ops[0], b), q.z
     assert np.abs(got - zx).max() <= 1e-10 * np.abs(zx).max()
     assert g.l2_error() == pytest.approx(O.l2_error(ops[0], q.z, b, 2), rel=1e-3, abs=1e-28)
-    if mixed and xp and yp:
-        # periodic both ways: singular (constants), so the V-cycles stay FP64
-        q2 = tg.Problem(m, n, table, cls, 1e-26, x_prd=xp, y_prd=yp, block=2)
-        q2.b[...] = b
-        g2 = tg.Tgmg(q2)
-        assert g2.solve_v_cycle(tg.Predict())
-        assert np.array_equal(q.z, q2.z)
-        g2.close()
     if mixed:
         g.set_precision(False)
         q.z[...] = 0
@@ -381,6 +373,30 @@ def test_block_operators(m, n, xp, yp, mixed):
         assert np.array_equal(q.z, q2.z)
         g2.close()
     g.close()
+
+
+@pytest.mark.parametrize("lt", [0.0, 0.02])
+def test_block_operator_periodic_large(lt):
+    """A singular periodic 2x2-block operator large enough that its coarsest
+    level's rounding pivots reach 1e-11..4e-10 of its largest entry (512x256,
+    eight levels): the coarsest level is recognised as singular and smoothed,
+    and FP64 V-cycles and mixed-precision passes both converge to acc."""
+    tg = _tg()
+    m, n = 512, 256
+    table, cls = _block_operator(m, n, 1, 1, lt=lt)
+    b = np.random.default_rng(1).standard_normal((n, m, 2)) * 1e-5
+    b -= b.mean(axis=(0, 1))
+    its = []
+    for mixed in (False, True):
+        q = tg.Problem(m, n, table, cls, (2.220446049250313e-16 * 1e4 * 2) ** 2, x_prd=1, y_prd=1, block=2)
+        q.b[...] = b
+        g = tg.Tgmg(q)
+        g.set_precision(mixed)
+        assert g.solve_v_cycle_checked(max_iters=40)
+        assert g.residual < q.acc
+        its.append(g.iterations)
+        g.close()
+    assert its[1] <= its[0] + 2, its
 
 
 def test_block_operator_update():
