@@ -18,7 +18,10 @@
 // (tgmg.in.cc:128-208), so iterates differ and converged solutions agree.
 // The coarsest level (more than 10 points, the next coarsening would have
 // at most 10, tgmg_config.hh:23) is solved exactly with a dense inverse
-// where it has at most 1024 unknowns, else smoothed like the reference.
+// where it has at most 1024 unknowns and is not singular, else smoothed like
+// the reference.  A mixed-precision solver (stzg_tgmg_set_precision) runs its
+// V-cycle solves as FP32 V-cycles on FP32 copies of the levels, inside FP64
+// refinement on the top level.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
