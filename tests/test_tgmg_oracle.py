@@ -72,3 +72,47 @@ def test_live_reference_matches_oracle():
             ref_s = ref.stencil(l)
             assert np.abs(mine[..., :9] - ref_s[..., :9]).max() <= 1e-15 * np.abs(ref_s[..., :9]).max()
         ref.close()
+
+
+def _gauss_jordan_pivots(A):
+    """Pivots of Gauss-Jordan elimination with partial pivoting (the order
+    the GPU solver's dense coarsest inverse uses), relative to max |A|."""
+    M = np.array(A, dtype=np.float64)
+    amax = np.abs(M).max()
+    piv = []
+    for c in range(M.shape[0]):
+        p = c + int(np.argmax(np.abs(M[c:, c])))
+        piv.append(abs(M[p, c]) / amax)
+        if p != c:
+            M[[p, c]] = M[[c, p]]
+        M[c] /= M[c, c]
+        col = M[:, c].copy()
+        col[c] = 0
+        M -= np.outer(col, M[c])
+    return np.sort(piv)
+
+
+def test_singular_coarsest_level_pivots():
+    """The coarsest level of a periodic 2x2-block operator that annihilates
+    rigid translations (the sheared-coordinates operator with y periodic,
+    512x256, seven levels) is singular, but its Galerkin rounding leaves
+    pivots between 1e-12 and 1e-8 of its largest entry, with the next pivot
+    far above: the solver takes a level as singular below 1e-8, not 1e-12."""
+    m, n = 512, 256
+    K, mu, lt = 2.5, 1.0, 0.02
+    L = K - 2. / 3. * mu
+    regh = np.array([[L + 2 * mu + lt * lt * mu, lt * mu + lt ** 3 * mu], [-lt * (L + mu), mu * (1 + lt * lt)]])
+    regv = np.array([[mu, lt * mu], [0, L + 2 * mu]])
+    regd = np.array([[-0.5 * lt * mu, 0.25 * (L + mu - 2 * lt * lt * mu)], [0.25 * (L + mu), -0.25 * lt * (L + 3 * mu)]])
+    ci = np.linalg.inv(-2 * (regh + regv))
+    regh, regv, regd = ci @ regh, ci @ regv, ci @ regd
+    table = np.stack([regd, regv, -regd, regh, np.eye(2), regh, -regd, regv, regd])[None]
+    cls = np.zeros((n, m), dtype=np.int32)
+    sizes = O.level_sizes(m, n, 1, 1)
+    A = O.operator(m, n, 1, 1, table, cls, 2)
+    for l in range(1, len(sizes)):
+        A, _ = O.galerkin(A, sizes[l - 1][0], sizes[l - 1][1], 1, 1, 2)
+    assert sizes[-1] == (8, 4)
+    piv = _gauss_jordan_pivots(A.toarray())
+    assert 1e-12 < piv[0] <= piv[1] < 1e-8, piv[:3]
+    assert piv[2] > 0.1, piv[:3]
