@@ -108,6 +108,15 @@ template <class S> class tgmg {
     bool solve_sor(double omega) { return solve_fixed(STZG_TGMG_SOR, 20, 1000, omega, 1, 1, 10); }
     bool solve_sor(tgmg_predict &tp, double omega) { return solve(STZG_TGMG_SOR, &tp, omega, 1, 1, 10); }
 
+    // Not in the reference: V-cycles until l2_error < acc, tested before the
+    // first and after each (stzg_tgmg_solve_checked), then extra_iters more.
+    bool solve_v_cycle_checked(int max_iters = 2048, int extra_iters = 1, int cyc_down = 1, int cyc_up = 1,
+                               int hcyc_bottom = 10) {
+        push();
+        return finish(stzg_tgmg_solve_checked(h_, STZG_TGMG_VCYCLE, max_iters, extra_iters, 1, cyc_down, cyc_up,
+                                              hcyc_bottom, nullptr, nullptr));
+    }
+
     void v_cycle(int cyc_down = 1, int cyc_up = 1, int hcyc_bottom = 10, bool symmetric = false) {
         iterate(symmetric ? STZG_TGMG_SYM_VCYCLE : STZG_TGMG_VCYCLE, 1, 1, cyc_down, cyc_up, hcyc_bottom);
     }
